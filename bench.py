@@ -1,0 +1,307 @@
+"""Benchmark: converged views/sec of the depth-to-view pipeline on one GB300.
+
+Workload (default "c2"): the super-resolution configuration -- a synthetic 5x5 light field of 512x512 RGB
+float32 views (rendered at 1024^2 and box-decimated, 5 planes + 20 Gaussian depth bumps, baseline 0.03,
+noise 0.005), 24 inputs warped to the 1024x1024 centre view and reconstructed with the gradient-constraint
+formulation (IBR_gradient) solved by conjugate gradient with FP32 iterates and FP64 dot products until the
+certified relative energy gap is <= 1e-4 (cap 500 iterations). One step = one full view: warp stage (target
+depth map, tau, dtau/dz), inverse footprint map, visibility, weights, weighted average, hole filling,
+gradient splatting and the CG solve.
+
+  value : views/sec with inputs resident in HBM (device pointers, lfrv_render_view_dev)
+  e2e   : views/sec through the host-buffer C ABI call (lfrv_render_view) from pinned host memory, with the
+          host->device copy of the views and depth maps and the device->host copy of the result inside
+  roofline : the dominant kernel of the step (by device time), algorithmic bytes per launch / its average
+          CUDA-event duration on the launch stream
+  cpu_baseline : the FP32 CPU restatement of the reference path (oracle port, OpenMP over the host cores) on
+          one full view of the same workload
+
+`--impl reference` times that CPU restatement alone as the reference arm (the reference's own path needs
+Qt, glm, OpenGL and its CUDA runtime and cannot run here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "light-field-remote-vision_gb300"))
+
+WORKLOADS = {
+    "c2": dict(preset=2, algorithm=1, name="5x5 LF 512^2 -> 1024^2 (dsf 2), 24 views, IBR_gradient + CG to gap 1e-4"),
+    "c1": dict(preset=1, algorithm=0, name="3x3 LF 256^2, 8 views, IBR_color primal-dual TV, 300 x 300 iterations"),
+}
+
+
+def make_config(lfrv, wl: str, sc):
+    p = sc.params
+    V = sc.views.shape[0]
+    if wl == "c2":
+        return lfrv.default_config(w=p.w, h=p.h, dsf=p.dsf, nviews=V, nchannels=3, sigma_sensor=0.005,
+                                   ugrad_threshold=1.0, lambda_=0.05, lambda_max_factor=100.0, faithful=0,
+                                   cg_gap_tol=1e-4, cg_max_iter=500, hole_fill_iter=500)
+    return lfrv.default_config(w=p.w, h=p.h, dsf=p.dsf, nviews=V, nchannels=3, sigma_sensor=0.01,
+                               ugrad_threshold=1.0, lambda_=0.05, lambda_max_factor=100.0, niter=300, nmeta_iter=1,
+                               early_exit=0, faithful=1)
+
+
+def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int) -> float | None:
+    """Compulsory DRAM bytes of one launch of `kernel` (FP32 = 4 B)."""
+    table = {
+        "zbuffer_splat": 12 * V * n + 8 * N,          # depth (z, dz/dx, dz/dy) read, 64-bit key per target pixel
+        "tau": 12 * V * n + 4 * N + 16 * V * n,       # depth + target depth map read, tau and dp written
+        "bucket_build": 8 * V * n * 2 + 4 * V * n + 8 * (N + 2 * N),
+        "weights": 16 * V * n + 8 * N + 4 * V * n,    # tau + dp, gradient planes, weights written
+        "vis_any": 4 * N + 8 * V * n + 4 * V * n + 1 * N,
+        "initial_image": 24 * V * n + 4 * V * n + 4 * N + 16 * N,
+        "hole_list": 1 * N,
+        "hole_fill_iter": None,
+        "sobel": 12 * V * n + 8 * V * n,
+        "u_gradient": (8 + 4 + 8) * V * n + 4 * V * n + 4 * N + 12 * N,
+        "cg_init": 12 * N + 8 * N + 24 * N,
+        "cg_apply": 12 * N + 12 * N,
+        "cg_update": 48 * N + 24 * N,
+        "cg_dir": 24 * N + 12 * N,
+        "cg_energy": 24 * N + 8 * N,
+        "rof_iter": 88 * N,
+        "residual": 12 * N + 24 * V * n + 12 * V * n,
+        "dataterm_F": 12 * V * n + 8 * V * n + 4 * V * n + 12 * N + 12 * N,
+    }
+    return table.get(kernel)
+
+
+def sample_clocks(path: str):
+    return subprocess.Popen(
+        ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+         "--format=csv,noheader,nounits", "-lms", "200", "-i", os.environ.get("LOCAL_RANK", "0")],
+        stdout=open(path, "w"), stderr=subprocess.DEVNULL)
+
+
+def summarize_clocks(path: str) -> dict:
+    sm, mx, reasons = [], [], set()
+    try:
+        for line in open(path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for name, val in zip(names, f[5:9]):
+                if val.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+    except OSError:
+        pass
+    return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+            "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    try:
+        d = json.load(open(ROOT / "MEASURED_PEAKS.json"))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def cpu_step(pyoracle, wl: str, cfg, sc, algorithm: int) -> float:
+    t0 = time.perf_counter()
+    tau, dpart, _ = pyoracle.warp(sc.depth, sc.cams, sc.target)
+    if algorithm == 1:
+        pyoracle.ibr_gradient(cfg, sc.views, tau, dpart, prec=1)
+    else:
+        pyoracle.ibr_color(cfg, sc.views, tau, dpart, prec=1)
+    return time.perf_counter() - t0
+
+
+def run_reference(args, rank: int) -> None:
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import lfrv
+    import pyoracle
+
+    wl = WORKLOADS[args.workload]
+    sc = lfrv.synth_scene(lfrv.scene_params(wl["preset"]))
+    cfg = make_config(lfrv, args.workload, sc)
+    if args.workload == "c1":
+        cfg.niter = 30  # bounded sample: 30 x 30 iterations; the value is scaled to the 300 x 300 step below
+    for _ in range(args.warmup):
+        cpu_step(pyoracle, args.workload, cfg, sc, wl["algorithm"])
+    times = [cpu_step(pyoracle, args.workload, cfg, sc, wl["algorithm"]) for _ in range(args.steps)]
+    sec = sum(times) / len(times)
+    if args.workload == "c1":
+        sec *= 100.0  # ROF work scales with niter^2
+    cores = os.cpu_count()
+    v = 1.0 / sec
+    line = {"impl": "reference", "metric": "views/sec to energy gap <=1e-4", "value": v, "unit": "views/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": {"workload": wl["name"]},
+            "cpu_baseline": {"value": v, "unit": "views/s", "cores": cores, "kind": "port",
+                             "sample": "one full view per step (warp + solve), FP32 CPU restatement, OpenMP"},
+            "e2e": {"value": v, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank: int, world: int) -> None:
+    import torch
+    import lfrv
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    wl = WORKLOADS[args.workload]
+    sc = lfrv.synth_scene(lfrv.scene_params(wl["preset"]))
+    cfg = make_config(lfrv, args.workload, sc)
+    V, _, h, w = sc.views.shape
+    H, W = h * sc.params.dsf, w * sc.params.dsf
+    n, N, ks = h * w, H * W, sc.params.dsf + 1
+    stream = torch.cuda.Stream()
+    views = torch.from_numpy(sc.views).cuda()
+    depth = torch.from_numpy(sc.depth).cuda()
+    out = torch.empty((3, H, W), device="cuda", dtype=torch.float32)
+    ctx = lfrv.Context(dev, stream.cuda_stream)
+    torch.cuda.synchronize()
+
+    def step():
+        return ctx.render_view_dev(cfg, wl["algorithm"], views.data_ptr(), depth.data_ptr(), sc.cams, sc.target,
+                                   out.data_ptr())
+
+    for _ in range(max(args.warmup, 3)):
+        st = step()
+    torch.cuda.synchronize()
+    # the working set (24 views x 6 planes x 1 MB + the 1024^2 target state) exceeds nothing in L2 between
+    # steps: each step rewrites > 300 MB of buffers, so consecutive steps start from a cold L2
+    if world > 1:
+        torch.distributed.barrier()
+    clk_path = tempfile.mktemp(prefix="lfrv_clocks_")
+    clk = sample_clocks(clk_path)
+    l0 = ctx.launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    stats = [step() for _ in range(args.steps)]
+    e1.record(stream)
+    torch.cuda.synchronize()
+    launches = ctx.launch_count() - l0
+    ms = e0.elapsed_time(e1)
+    clk.terminate()
+    clk.wait()
+    clocks = summarize_clocks(clk_path)
+    sec = ms / 1e3
+    if world > 1:
+        t = torch.tensor([sec], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        sec = float(t.item())
+    value = world * args.steps / sec
+
+    # per-kernel device time over a second pass of the same steps (events on the launch stream)
+    ctx.profile_enable(True)
+    for _ in range(args.steps):
+        step()
+    prof = ctx.profile()
+    ctx.profile_enable(False)
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    avg_s = dom_ms / 1e3 / dom_n
+    abytes = algorithmic_bytes(dom, V, n, N, ks)
+    peak, peak_kind = measured_peak_hbm()
+    roof = None
+    if abytes:
+        ach = abytes / avg_s / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "peak_source": peak_kind, "traffic": None, "avg_launch_us": avg_s * 1e6,
+                "algorithmic_bytes_per_launch": abytes}
+
+    # end to end through the host-buffer C ABI call, pinned host memory
+    hv = torch.from_numpy(sc.views).pin_memory()
+    hd = torch.from_numpy(sc.depth).pin_memory()
+    ho = torch.empty((3, H, W), dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        ctx.render_view(cfg, wl["algorithm"], hv.data_ptr(), hd.data_ptr(), sc.cams, sc.target, ho.data_ptr())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        ctx.render_view(cfg, wl["algorithm"], hv.data_ptr(), hd.data_ptr(), sc.cams, sc.target, ho.data_ptr())
+    f1.record(stream)
+    torch.cuda.synchronize()
+    e2e_sec = max(f0.elapsed_time(f1) / 1e3, 1e-9)
+    wall = time.perf_counter() - t0
+    e2e_value = world * args.steps / max(e2e_sec, wall)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pyoracle
+
+        ccfg = make_config(lfrv, args.workload, sc)
+        if args.workload == "c1":
+            ccfg.niter = 30
+        t = cpu_step(pyoracle, args.workload, ccfg, sc, wl["algorithm"])
+        if args.workload == "c1":
+            t *= 100.0
+        cpu = {"value": 1.0 / t, "unit": "views/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "one full view (warp + solve) of the same workload, FP32 CPU restatement, OpenMP"}
+
+    if rank == 0:
+        line = {"metric": "views/sec to energy gap <=1e-4", "value": value, "unit": "views/s", "n_gpus": world,
+                "steps": args.steps, "warmup": max(args.warmup, 3), "ms_per_step": sec * 1e3 / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                "data": "synthetic (seeded planes + bumps light field, no dataset)",
+                "config": {"workload": wl["name"], "views": V, "input": [h, w], "target": [H, W],
+                           "cg_iterations": stats[-1].outer_iterations,
+                           "hole_fill_iterations": stats[-1].hole_fill_iterations, "gap": stats[-1].gap,
+                           "l2": "inputs and per-step buffers exceed L2 between steps (no flush needed)",
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "clocks": clocks, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+                "e2e": {"value": e2e_value, "unit": "views/s",
+                        "h2d_bytes_per_step": int(sc.views.nbytes + sc.depth.nbytes),
+                        "d2h_bytes_per_step": int(3 * H * W * 4)},
+                "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+        print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    run_ours(args, rank, world)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

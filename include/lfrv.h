@@ -1,0 +1,286 @@
+/* lfrv.h -- C ABI of the GB300 light-field remote-vision solver library (liblfrv.so).
+ *
+ * The reference (Nighteye/light-field-remote-vision) has no plugin or FFI layer: its hot path is
+ * reached through the config-driven C++ entry points
+ *     void sr_synthesize_view( Config_data*, int frame )      sources/super-resolution.h:12
+ *     void IBR_gradient( Config_data* )                       sources/gradientIBR.h:7
+ * and the cocolib-style stage functions coco_vtv_sr_*_unstructured( coco_vtv_data* )
+ * (sources/optimization.cuh:111-175), which allocate and free all device memory themselves, run on
+ * the default stream and assert() on any error (cocolib/cocolib/cuda/cuda_helper.h:38-44).
+ *
+ * This header replaces that boundary with plain C:
+ *   - every entry point returns an int status: LFRV_OK (0) or a negative LFRV_E_* code;
+ *     lfrv_last_error() returns a message for the calling thread's last failure;
+ *   - images are planar float32, channel-major (C x H x W), row-major, top-left origin;
+ *     per-view stacks are V x C x h x w in the order of the reference's import loops
+ *     (s = s_min..s_max skipping s_rmv, sources/import.cpp:144-160);
+ *   - host entry points take caller-owned host buffers and copy them in/out; *_dev entry points take
+ *     caller-owned device pointers and a cudaStream_t (passed as void*), and never synchronise the
+ *     device beyond that stream;
+ *   - a context (lfrv_ctx) owns the device workspace of one solve; contexts are independent, so
+ *     distinct threads may drive distinct contexts concurrently.
+ */
+#ifndef LFRV_H
+#define LFRV_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status codes */
+#define LFRV_OK              0
+#define LFRV_E_ARG          -1   /* bad argument (null pointer, size mismatch, unsupported option) */
+#define LFRV_E_CUDA         -2   /* a CUDA runtime call or kernel launch failed */
+#define LFRV_E_NOMEM        -3   /* device or host allocation failed */
+#define LFRV_E_IO           -4   /* file could not be opened, read or written */
+#define LFRV_E_FORMAT       -5   /* malformed file (PFM header, config syntax) */
+#define LFRV_E_NONFINITE    -6   /* non-finite value in an input or in the solver state */
+#define LFRV_E_TIMEOUT      -7   /* a bounded device-side wait gave up */
+#define LFRV_E_NODEVICE     -8   /* no CUDA device, or the library was built without a usable kernel image */
+
+const char *lfrv_last_error(void);
+const char *lfrv_version(void);
+
+/* ---------------------------------------------------------------- configuration
+ * Mirrors the keys of Config_data (sources/config.h:11-122, parsed in sources/config.cpp:67-129) that
+ * the IBR_color / IBR_gradient path reads, with the reference's defaults (sources/config.cpp:11-64).
+ * sigma_sensor holds the value AFTER the reference's division by 255 (sources/config.cpp:119).
+ */
+typedef struct lfrv_config {
+    int   w, h;              /* input (low-res) view size                       ("width", "height") */
+    int   dsf;               /* super-resolution factor; target is (dsf*w) x (dsf*h)        ("dsf") */
+    int   nviews;            /* number of input views (all views but s_rmv)                         */
+    int   nchannels;         /* must be 3 (sources/config.cpp:116)                                  */
+    float sigma_sensor;      /* sensor noise sigma, already divided by 255                          */
+    float ugrad_threshold;   /* clamp of the warped target gradient in the angular weights         */
+    float lambda;            /* TV smoothness                                                       */
+    float lambda_max_factor; /* lambda_max = lambda_max_factor * lambda in the regulariser weight   */
+    int   dw_type;           /* deformation weights: only 0 (Wanner) is implemented upstream        */
+    int   gw_type;           /* gradient-term weights (energy of the gradient data term)            */
+    float dt_alpha;          /* intensity data term weight                                          */
+    float dt_beta;           /* gradient data term weight                                           */
+    float gradient_step;     /* step of the gradient data term                                      */
+    int   niter;             /* outer FISTA iterations AND inner ROF iterations (reference reuses it) */
+    int   nmeta_iter;        /* re-weighting meta iterations                                         */
+    /* --- options with no Config_data counterpart --- */
+    int   faithful;          /* 1: reproduce the reference's control flow including its defects      */
+    int   early_exit;        /* 1: the reference's convergence tests (energy / moving pixels) apply  */
+    int   cg_max_iter;       /* IBR_gradient, corrected CG: iteration cap                             */
+    double cg_gap_tol;       /* IBR_gradient, corrected CG: stop when the certified relative energy
+                                gap ||r||^2 / (2 lambda_cg) / |E(u)| falls to this value (0: run the cap) */
+    int   hole_fill_iter;    /* IBR_gradient hole filling: Jacobi iteration cap (reference: 500)     */
+} lfrv_config;
+
+/* Fills *cfg with Config_data's defaults (sources/config.cpp:11-64) and this library's option defaults
+ * (faithful=1, early_exit=1, cg_max_iter=500, cg_gap_tol=1e-4, hole_fill_iter=500). */
+int lfrv_config_default(lfrv_config *cfg);
+
+/* Parses a reference config file (coco::config syntax: "key value" lines, '#' comments,
+ * "config <file>" includes processed in order, later keys override; cocolib/cocolib/common/
+ * parse_config.cpp:44-200) into *cfg, applying sigma_sensor /= 255 as Config_data::parse_config does.
+ * String-valued keys the solver needs (lf_name, tau_name, dpart_name, init_name, outdir, outfile,
+ * algorithm) are returned through lfrv_config_get_string after the call. s_min/s_max/s_rmv set nviews. */
+int lfrv_config_parse_file(const char *path, lfrv_config *cfg);
+int lfrv_config_set(lfrv_config *cfg, const char *key, const char *value);
+int lfrv_config_get_string(const char *key, char *buf, size_t buflen);
+int lfrv_config_get_int(const char *key, int *value);
+
+/* ---------------------------------------------------------------- cameras
+ * Pinhole P = K [R | t], t = -R C (sources/pinholeCamera.h:14-57). Row-major 3x3 K and R. */
+typedef struct lfrv_camera {
+    float K[9];
+    float R[9];
+    float t[3];
+    int   width, height;
+} lfrv_camera;
+
+/* ---------------------------------------------------------------- solve statistics */
+typedef struct lfrv_stats {
+    int    outer_iterations;     /* FISTA iterations run (IBR_color) or CG iterations (IBR_gradient) */
+    int    meta_iterations;
+    int    hole_fill_iterations;
+    int    stop_reason;          /* 0 cap reached, 1 tiny energy, 2 relative energy change, 3 < 1% pixels moving,
+                                    4 certified gap reached */
+    double energy;               /* last energy evaluated (reference formula for IBR_color, quadratic for CG) */
+    double gap;                  /* last certified relative gap (CG), else 0 */
+    double seconds;              /* device time of the solve (CUDA events) */
+    int    kernel_launches;      /* kernels this library launched for the call */
+} lfrv_stats;
+
+/* ---------------------------------------------------------------- contexts */
+typedef struct lfrv_ctx lfrv_ctx;
+
+int lfrv_ctx_create(lfrv_ctx **out, int device);
+int lfrv_ctx_destroy(lfrv_ctx *ctx);
+/* All device work of the context is issued on this stream (a cudaStream_t; NULL = legacy default). */
+int lfrv_ctx_set_stream(lfrv_ctx *ctx, void *cuda_stream);
+/* Counts kernels launched by the context since creation (or the last reset). */
+int lfrv_ctx_launch_count(lfrv_ctx *ctx, long long *count, int reset);
+/* Per-kernel device timing (no counterpart upstream; the reference prints iter/s from clock(),
+ * sources/super-resolution.cpp:266-270). enable=1 clears the records and records a CUDA event pair on the
+ * context stream around every kernel launch; lfrv_ctx_profile_read synchronises the stream and returns,
+ * for the index-th kernel name seen, its summed device time and launch count (LFRV_E_ARG past the end). */
+int lfrv_ctx_profile(lfrv_ctx *ctx, int enable);
+int lfrv_ctx_profile_read(lfrv_ctx *ctx, int index, char *name, size_t name_len, double *total_ms,
+                          long long *launches);
+
+/* ---------------------------------------------------------------- warp stage
+ * Replaces the GL warp exporter (fromMVE2coco: Scene::computeTargetDepthMap sources/openGL/scene.cpp:1506,
+ * Scene::exportWarps :1546, shaders tauWarp.frag:25-74, tauPartial.frag:23-48,
+ * depthSplatting.{vert,geom,frag}) with CUDA kernels writing headless device buffers.
+ *   depth   : V x 3 x h x w   (z, dz/dx, dz/dy) per input view, orthographic depth along the optical axis
+ *   cams    : V input cameras; target: the target camera (target->width x target->height = W x H)
+ *   tau     : V x 3 x h x w   (tau_x, tau_y, deformation weight), codes -2 / -1 as tauWarp.frag writes
+ *   dpart   : V x 3 x h x w   (sigma_z = 10, dtau_x/dz, dtau_y/dz) as tauPartial.frag writes
+ *   zbuf    : H x W            target depth map (0 where no quad covers a pixel centre), may be NULL
+ */
+int lfrv_warp(lfrv_ctx *ctx, int nviews, int w, int h,
+              const float *depth, const lfrv_camera *cams, const lfrv_camera *target,
+              float *tau, float *dpart, float *zbuf);
+int lfrv_warp_dev(lfrv_ctx *ctx, int nviews, int w, int h,
+                  const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target,
+                  float *d_tau, float *d_dpart, float *d_zbuf);
+
+/* ---------------------------------------------------------------- solvers
+ * lfrv_ibr_color replaces sr_synthesize_view (sources/super-resolution.cpp:54-338);
+ * lfrv_ibr_gradient replaces IBR_gradient (sources/gradientIBR.cpp:12-150).
+ *   views : V x 3 x h x w input views (the reference's view_data::_image_f)
+ *   tau   : V x 2 x h x w or V x 3 x h x w warps; only channels 0,1 are read (coco_vtv_sr_read_tau,
+ *           sources/optimization.cu:1170-1205, ignores the deformation channel)
+ *   dpart : V x 3 x h x w (sigma_z, dtau_x/dz, dtau_y/dz); the solver uses sigma_z*dtau/dz
+ *           (coco_vtv_sr_read_partial_tau, sources/optimization.cu:1208-1256)
+ *   init  : optional 3 x H x W starting image (the reference's init_name PFM), NULL = computed
+ *   out   : 3 x H x W result
+ * tau_stride_ch selects the channel count of the tau stack (2 or 3).
+ */
+int lfrv_ibr_color(lfrv_ctx *ctx, const lfrv_config *cfg,
+                   const float *views, const float *tau, int tau_channels, const float *dpart,
+                   const float *init, float *out, lfrv_stats *stats);
+int lfrv_ibr_color_dev(lfrv_ctx *ctx, const lfrv_config *cfg,
+                       const float *d_views, const float *d_tau, int tau_channels, const float *d_dpart,
+                       const float *d_init, float *d_out, lfrv_stats *stats);
+int lfrv_ibr_gradient(lfrv_ctx *ctx, const lfrv_config *cfg,
+                      const float *views, const float *tau, int tau_channels, const float *dpart,
+                      const float *init, float *out, lfrv_stats *stats);
+int lfrv_ibr_gradient_dev(lfrv_ctx *ctx, const lfrv_config *cfg,
+                          const float *d_views, const float *d_tau, int tau_channels, const float *d_dpart,
+                          const float *d_init, float *d_out, lfrv_stats *stats);
+
+/* Full depth-to-image pipeline on one target: the warp stage (fromMVE2coco's GL export,
+ * sources/openGL/scene.cpp:1506-1586) followed by the solver (algorithm 0 = IBR_color as
+ * sr_synthesize_view, 1 = IBR_gradient as IBR_gradient), as the reference's IBR_video loop chains them
+ * per frame (sources/main.cpp:359-403). views and depth are V x 3 x h x w; out is 3 x H x W.
+ * lfrv_render_view takes host buffers (copied in and out inside the call); _dev takes device pointers. */
+int lfrv_render_view(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm,
+                     const float *views, const float *depth,
+                     const lfrv_camera *cams, const lfrv_camera *target,
+                     float *out, lfrv_stats *stats);
+int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm,
+                         const float *d_views, const float *d_depth,
+                         const lfrv_camera *cams, const lfrv_camera *target,
+                         float *d_out, lfrv_stats *stats);
+
+/* ---------------------------------------------------------------- stage calls
+ * Fine-grained entry points mirroring the cocolib stage functions, used by the parity tests.
+ * All take host buffers. "views/tau/dpart" as above; U, G etc. are 3 x H x W.
+ */
+/* coco_vtv_sr_compute_weights_unstructured (sources/optimization.cu:1066-1167) with the reference's
+ * buffer semantics: gx/gy (H x W) are the gradient buffers the Sobel kernel writes (X1[0], X2[0]) and
+ * keep their old value where the kernel does not write; vis (H x W bytes) the visibility mask.
+ * Writes weights (V x h x w). */
+int lfrv_stage_weights(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                       int tau_channels, const float *dpart, const float *U, const uint8_t *vis,
+                       float *gx, float *gy, float *weights);
+/* coco_vtv_setup_visibility_mask (sources/optimization.cu:33-135): coverage (H x W) and vis (H x W). */
+int lfrv_stage_visibility(lfrv_ctx *ctx, const lfrv_config *cfg, const float *tau, int tau_channels,
+                          float *coverage, uint8_t *vis);
+/* vtv_sr_dataterm_intensities + the F computation of vtv_sr_ista_step_unstructured
+ * (sources/optimization.cu:1751-1812, 1835-1966): G (3 x H x W, before the [-1,1] clamp) and
+ * F = clamp(U - clamp(G,-1,1)/(lambda L), 0, 1). */
+int lfrv_stage_dataterm(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                        int tau_channels, const float *weights, const float *U, float *G, float *F);
+/* niter inner ROF iterations (sources/optimization.cu:1815-1828; vtv_rof.cu:118-147, 280-320;
+ * cuda_kernels.cu:504-532) in place on U (3 x H x W) and the duals P (6 x H x W: px0,py0,px1,py1,px2,py2)
+ * for data F (3 x H x W) and regulariser weight g (H x W). */
+int lfrv_stage_rof(lfrv_ctx *ctx, int W, int H, int niter, float tau, float sigma, float lambda,
+                   const float *F, const float *g, float *U, float *P);
+/* Reference energy (coco_vtv_sr_primal_energy_unstructured, sources/optimization.cu:1477-1717). */
+int lfrv_stage_energy(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                      int tau_channels, const float *weights, const float *U, const uint8_t *vis,
+                      double *energy, double *e_tv, double *e_data);
+/* Regulariser weight g (H x W) (coco_vtv_sr_init_regularizer_weight_unstructured,
+ * sources/optimization.cu:2251-2338). norm_in is the coverage accumulator's prior content
+ * (the reference never clears it here); norm_out receives its final content. */
+int lfrv_stage_regularizer(lfrv_ctx *ctx, const lfrv_config *cfg, const float *tau, int tau_channels,
+                           const float *weights, const float *norm_in, float *norm_out, float *g);
+/* Weighted-average initial image before hole filling (coco_vtv_sr_compute_initial_image,
+ * sources/optimization.cu:1300-1350): U (3 x H x W) and the weight sum norm (H x W). */
+int lfrv_stage_initial_image(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                             int tau_channels, const float *weights, float *U, float *norm);
+/* Push-pull hole filling (coco_vtv_push_pull, sources/optimization.cu:544-651) in place on U
+ * (3 x H x W) with visibility vis; faithful=1 reproduces the reference's final "U = filled - U". */
+int lfrv_stage_push_pull(lfrv_ctx *ctx, int W, int H, int faithful, const uint8_t *vis, float *U);
+/* IBR_gradient pieces: splat visibility (setup_target_visibility, sources/gradientIBR.cu:40-83),
+ * Laplacian hole filling (hole_filling, :87-152), gradient splatting (init_u_gradient, :833-920)
+ * and the Poisson CG (possion_conj_grad, sources/solver.cu:526-699). */
+int lfrv_stage_gradient_visibility(lfrv_ctx *ctx, const lfrv_config *cfg, const float *tau,
+                                   int tau_channels, uint8_t *vis);
+int lfrv_stage_hole_fill(lfrv_ctx *ctx, int W, int H, int max_iter, const uint8_t *vis, float *U,
+                         int *iterations);
+int lfrv_stage_u_gradient(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                          int tau_channels, const float *weights, float *gx, float *gy, float *mask);
+/* faithful=1: the reference's 5-iteration loop with its defects; faithful=0: conjugate gradient with
+ * FP64 dot products until the certified gap reaches gap_tol or max_iter iterations. */
+int lfrv_stage_cg(lfrv_ctx *ctx, int W, int H, int faithful, int max_iter, double gap_tol,
+                  const float *gx, const float *gy, float *U, int *iterations, double *gap);
+
+/* ---------------------------------------------------------------- files
+ * PFM as the reference reads and writes it: gsl_image_load_pfm (cocolib/cocolib/common/gsl_image.cpp:
+ * 416-500) flips rows on load; write_pfm_image_signed (cocolib/cocolib/cuda/cuda_helper.cu:340-375)
+ * flips on write. Buffers here are top-left origin, planar. */
+int lfrv_pfm_read(const char *path, int *w, int *h, int *channels, float *data, size_t capacity);
+int lfrv_pfm_write(const char *path, int w, int h, int channels, const float *data);
+
+/* ---------------------------------------------------------------- synthetic light fields
+ * No reference counterpart: the reference's datasets are absent, so seeded synthetic scenes stand in
+ * for them. Pinhole cameras on an n x n grid (R = I, centres at baseline*(i-c, j-c, 0)), fronto-parallel
+ * textured planes (each texture channel = 0.5 + 0.5/64 * sum of 64 seeded 2-D sinusoids), optional
+ * Gaussian depth bumps, views rendered at ss x resolution and box-decimated, Gaussian sensor noise.
+ */
+typedef struct lfrv_scene_params {
+    int      grid;            /* n for an n x n light field; the centre view is the target */
+    int      w, h;            /* input view size */
+    int      ss;              /* render supersampling of the inputs (box-decimated) */
+    int      dsf;             /* target size = dsf * input size */
+    double   baseline;
+    int      nplanes;
+    double   depths[16];      /* ascending; the last plane is a full background */
+    int      nbumps;
+    double   bump_amp;        /* world depth units */
+    double   bump_sigma_px;   /* in target pixels */
+    double   noise_sigma;
+    double   focal_per_256;   /* target focal length per 256 target pixels of width (300) */
+    uint64_t seed;
+} lfrv_scene_params;
+
+/* which: 1 = 3x3 256^2 (planes 1.0/1.5/2.5, baseline 0.05, noise 0.01);
+ *        2 = 5x5 512^2 inputs rendered at 1024^2 and decimated, 5 planes + 20 bumps, baseline 0.03,
+ *            noise 0.005, dsf 2. */
+int lfrv_scene_params_preset(int which, lfrv_scene_params *p);
+/* Sizes: views/depth V*3*h*w floats with V = grid^2 - 1; cams V+1 entries (inputs, then target);
+ * gt 3*H*W floats. Any output pointer may be NULL. */
+int lfrv_synth_scene(const lfrv_scene_params *p, float *views, float *depth, lfrv_camera *cams,
+                     float *gt);
+
+/* PSNR with peak 1.0 over all channels, excluding a border of `border` pixels
+ * (gsl_image_psnr, cocolib/cocolib/common/gsl_image.cpp:991-1025 uses border 2). */
+double lfrv_psnr(int W, int H, const float *a, const float *b, int border);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LFRV_H */

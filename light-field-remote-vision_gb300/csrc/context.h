@@ -1,0 +1,72 @@
+// context.h -- the lfrv_ctx object: device, stream, launch counter and the device workspace.
+#pragma once
+
+#include "kernels.h"
+#include "lfrv.h"
+#include "lfrv_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+namespace lfrv {
+
+void check_cuda(cudaError_t e, const char *what);
+#define LFRV_CUDA(call) ::lfrv::check_cuda((call), #call)
+
+// Growable device allocation owned by a context.
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+    void ensure(size_t b);
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(p); }
+    ~DevBuf() { release(); }
+};
+
+// Device workspace of one solve. Buffers are grown on demand and kept between calls.
+struct Workspace {
+    // per view
+    DevBuf img, tau, dp, wgt, res, vgrad, depth, tau_in, dpart_in, cams;
+    // inverse footprint map
+    DevBuf b_count, b_start, b_entries, b_aux;
+    // target
+    DevBuf U, Ua, Ub, Uprev, P, Pa, F, G, g, g0, tmp, cov, norm, vis, Xq, gx, gy, mask, zkey, zbuf;
+    // CG
+    DevBuf r, d, q, U0, holes, hole_count;
+    // reductions
+    DevBuf partial, sums;
+    // push-pull pyramid
+    DevBuf pp_img, pp_vis, pp_tmp, pp_orig;
+    // host staging for the host-buffer entry points
+    DevBuf in_views, in_tau, in_dpart, in_init, out_img;
+};
+
+// Per-kernel CUDA-event timing: a fixed pool of event pairs recorded in-stream; read after a sync.
+struct KernelProfiler {
+    struct Rec {
+        const char *name;
+        int slot;
+    };
+    std::vector<cudaEvent_t> ev;  // 2 per slot
+    std::vector<Rec> recs;
+    int next = 0;
+    bool overflow = false;
+    void init(int slots);
+    void destroy();
+    int begin(const char *name, cudaStream_t st);
+    void end(int slot, cudaStream_t st);
+};
+
+}  // namespace lfrv
+
+struct lfrv_ctx {
+    lfrv::KernelProfiler prof;
+    bool profiling = false;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    lfrv::LaunchCounter launches;
+    lfrv::Workspace ws;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};

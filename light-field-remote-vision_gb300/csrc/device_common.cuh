@@ -1,0 +1,158 @@
+// device_common.cuh -- device helpers shared by the lfrv kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lfrv {
+
+constexpr int kMaxKs = 5;  // ks = dsf + 1, dsf <= 4
+
+// ------------------------------------------------------------------ footprint of a source pixel
+// Restates cuda_set_A_bilinear (cocolib/cocolib/vtv/vtv_sr_kernels_unstructured.cu:658-718): a dsf-wide
+// box centred at tau - 0.5 covers ks x ks target pixels anchored at floor(px - dsf/2 + 1/2) with
+// px = tau - 0.5; the weights are the box/pixel overlaps dx*dy, normalised by their sum over the
+// in-image taps. The reference evaluates the anchor and the border overlaps in double and rounds each
+// overlap once to float; the expressions below produce the same floats:
+//   - px = tau - 0.5f is exact for 0.25 <= tau < 2^22 and otherwise rounded once, like the double path;
+//   - for dsf = 1, 2 the anchor floor(px - (dsf-1)/2) is exact in float; other dsf use double;
+//   - each overlap is a single rounding of the same exact value ((x + 1/2 + dsf/2) - px or
+//     px - (x - 1/2 - dsf/2)).
+// The products and the normalisation use round-to-nearest intrinsics so no FMA contraction changes them.
+struct Footprint {
+    int x0, y0;
+    float A[kMaxKs * kMaxKs];  // entry ks*i + j: row offset i, column offset j
+};
+
+__device__ __forceinline__ int fp_anchor(float p, int dsf) {
+    if (dsf == 1) return (int)floorf(p);
+    if (dsf == 2) return (int)floorf(p - 0.5f);
+    return (int)floor((double)p - 0.5 * dsf + 0.5);
+}
+
+__device__ __forceinline__ float fp_overlap(int k, int ks, int coord, float p, int dsf) {
+    if (k == 0) return __fsub_rn((float)coord + 0.5f + 0.5f * (float)dsf, p);
+    if (k == ks - 1) return __fsub_rn(p, (float)coord - 0.5f - 0.5f * (float)dsf);
+    return 1.0f;
+}
+
+template <int KS>
+__device__ __forceinline__ void footprint(float tx, float ty, int dsf, int W, int H, Footprint &fp) {
+    const float px = tx - 0.5f, py = ty - 0.5f;
+    fp.x0 = fp_anchor(px, dsf);
+    fp.y0 = fp_anchor(py, dsf);
+    float dxs[KS], dys[KS];
+#pragma unroll
+    for (int k = 0; k < KS; ++k) {
+        dxs[k] = fp_overlap(k, KS, fp.x0 + k, px, dsf);
+        dys[k] = fp_overlap(k, KS, fp.y0 + k, py, dsf);
+    }
+    float norm = 0.0f;
+#pragma unroll
+    for (int j = 0; j < KS; ++j) {
+#pragma unroll
+        for (int i = 0; i < KS; ++i) {
+            const int x = fp.x0 + j, y = fp.y0 + i;
+            const bool in = (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1);
+            const float a = in ? __fmul_rn(dxs[j], dys[i]) : 0.0f;
+            fp.A[KS * i + j] = a;
+            norm = __fadd_rn(norm, a);
+        }
+    }
+    if (norm != 0.0f) {
+#pragma unroll
+        for (int e = 0; e < KS * KS; ++e) fp.A[e] = __fdiv_rn(fp.A[e], norm);
+    }
+}
+
+// Single normalised weight of tap (j, i) of a footprint (used by the inverse-map gathers).
+template <int KS>
+__device__ __forceinline__ float footprint_tap(float tx, float ty, int dsf, int W, int H, int j, int i) {
+    Footprint fp;
+    footprint<KS>(tx, ty, dsf, W, H, fp);
+    return fp.A[KS * i + j];
+}
+
+// Raw overlap product of tap (j, i) (setup_visibility_mask, sources/gradientIBR_kernels.cuh:26-49).
+template <int KS>
+__device__ __forceinline__ float footprint_raw(float tx, float ty, int dsf, int j, int i, int x0, int y0) {
+    const float px = tx - 0.5f, py = ty - 0.5f;
+    return __fmul_rn(fp_overlap(j, KS, x0 + j, px, dsf), fp_overlap(i, KS, y0 + i, py, dsf));
+}
+
+// Gather set (cuda_convolution_nonsep_device_param, vtv_sr_kernels_unstructured.cu:286): tau in [0,W]x[0,H].
+__device__ __forceinline__ bool in_gather(float tx, float ty, int W, int H) {
+    return !(tx < 0.0f || ty < 0.0f || tx > (float)W || ty > (float)H);
+}
+
+// Splat set (vtv_sr_init_forward_warp_structure_unstructured, sources/optimization.cu:906-927):
+// gather set and floor(tau - 0.5) inside the target.
+__device__ __forceinline__ bool in_splat(float tx, float ty, int W, int H) {
+    if (!in_gather(tx, ty, W, H)) return false;
+    const int px = (int)floorf(tx - 0.5f), py = (int)floorf(ty - 0.5f);
+    return !(px < 0 || py < 0 || px > W - 1 || py > H - 1);
+}
+
+// Luminance of the Sobel kernels (vtv_sr_kernels_unstructured.cu:121-130).
+__device__ __forceinline__ float lum(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
+
+// ------------------------------------------------------------------ block reductions (FP64)
+// Deterministic: fixed shuffle tree inside a warp, fixed order across warps.
+template <int NT>
+__device__ __forceinline__ double block_sum(double v, double *smem /* >= NT/32 */) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) smem[wid] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int i = 0; i < NT / 32; ++i) s += smem[i];
+    }
+    __syncthreads();
+    return s;  // valid in thread 0
+}
+
+// ------------------------------------------------------------------ bounded grid barrier
+// For kernels launched cooperatively (all blocks co-resident). Every wait is bounded: after
+// kSpinLimit polls the block records LFRV timeout in *err and returns false; callers then exit.
+struct GridBarrier {
+    unsigned int *count;  // monotonically increasing arrival counter (zeroed before the launch)
+    int *err;             // set to 1 on timeout
+};
+
+constexpr long long kSpinLimit = 1ll << 26;
+
+__device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &generation) {
+    __syncthreads();
+    generation += 1;
+    bool ok = true;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        __threadfence();
+        const unsigned int target = generation * (gridDim.x * gridDim.y);
+        atomicAdd(gb.count, 1u);
+        long long spins = 0;
+        while (true) {
+            const unsigned int seen = *((volatile unsigned int *)gb.count);
+            if ((int)(seen - target) >= 0) break;
+            if (*((volatile int *)gb.err)) {
+                ok = false;
+                break;
+            }
+            if (++spins > kSpinLimit) {
+                atomicExch(gb.err, 1);
+                ok = false;
+                break;
+            }
+            __nanosleep(32);
+        }
+        __threadfence();
+    }
+    __shared__ int s_ok;
+    if (threadIdx.x == 0 && threadIdx.y == 0) s_ok = ok ? 1 : 0;
+    __syncthreads();
+    return s_ok != 0;
+}
+
+}  // namespace lfrv

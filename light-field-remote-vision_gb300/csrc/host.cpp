@@ -1,0 +1,1266 @@
+// host.cpp -- C++ host orchestration of the lfrv solvers and the extern "C" boundary.
+//
+// The drivers follow the reference's control flow:
+//   color_solve    : sr_synthesize_view (sources/super-resolution.cpp:54-338) and the cocolib stage
+//                    functions it calls (sources/optimization.cu);
+//   gradient_solve : IBR_gradient (sources/gradientIBR.cpp:12-150) with sources/gradientIBR.cu and
+//                    possion_conj_grad (sources/solver.cu:526-699);
+//   warp           : the GL warp exporter (sources/openGL/scene.cpp:1506-1586) restated as kernels.
+// With cfg.faithful the reference's defects that change results are reproduced:
+//   D5 the Sobel of compute_weights writes into the channel-0 dual variables (optimization.cu:1090-1092);
+//   D6 the coverage accumulator is not cleared before the regulariser weight (optimization.cu:2262-2300);
+//   D7 push-pull returns "filled - U" (optimization.cu:640-644);
+//   D1 the CG loop of possion_conj_grad (beta == 1, alpha accumulator never cleared, 5 iterations).
+// D2 (the FISTA extrapolation is overwritten by the next step, optimization.cu:1765-1767) never changes
+// the result, so the extrapolation is not computed; the iterate simply advances.
+#include "context.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace lfrv {
+
+void check_cuda(cudaError_t e, const char *what) {
+    if (e != cudaSuccess) raise(e == cudaErrorMemoryAllocation ? LFRV_E_NOMEM : LFRV_E_CUDA, "%s: %s", what,
+                                cudaGetErrorString(e));
+}
+
+void DevBuf::ensure(size_t b) {
+    if (b <= bytes && p) return;
+    release();
+    if (b == 0) b = 16;
+    LFRV_CUDA(cudaMalloc(&p, b));
+    bytes = b;
+}
+
+void DevBuf::release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+}
+
+void KernelProfiler::init(int slots) {
+    if (!ev.empty()) return;
+    ev.resize(2 * (size_t)slots);
+    for (auto &e : ev) LFRV_CUDA(cudaEventCreate(&e));
+    recs.reserve(slots);
+}
+
+void KernelProfiler::destroy() {
+    for (auto &e : ev) cudaEventDestroy(e);
+    ev.clear();
+    recs.clear();
+    next = 0;
+}
+
+int KernelProfiler::begin(const char *name, cudaStream_t st) {
+    if (2 * (size_t)(next + 1) > ev.size()) {
+        overflow = true;
+        return -1;
+    }
+    const int slot = next++;
+    cudaEventRecord(ev[2 * slot], st);
+    recs.push_back({name, slot});
+    return slot;
+}
+
+void KernelProfiler::end(int slot, cudaStream_t st) {
+    if (slot >= 0) cudaEventRecord(ev[2 * slot + 1], st);
+}
+
+ProfScope::ProfScope(LaunchCounter &lc, const char *name, cudaStream_t s) : p(lc.prof), slot(-1), st(s) {
+    if (p) slot = p->begin(name, st);
+}
+
+ProfScope::~ProfScope() {
+    if (p) p->end(slot, st);
+}
+
+static void swap_buf(DevBuf &a, DevBuf &b) {
+    std::swap(a.p, b.p);
+    std::swap(a.bytes, b.bytes);
+}
+
+static void check_launch(const char *what) {
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) raise(LFRV_E_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+}
+
+static void sync(lfrv_ctx *c) { LFRV_CUDA(cudaStreamSynchronize(c->stream)); }
+
+// ------------------------------------------------------------------ geometry and validation
+static Geometry geometry(const lfrv_config &cfg) {
+    if (cfg.nchannels != 3) raise(LFRV_E_ARG, "nchannels must be 3 (sources/config.cpp:116), got %d", cfg.nchannels);
+    if (cfg.w <= 0 || cfg.h <= 0) raise(LFRV_E_ARG, "bad view size %d x %d", cfg.w, cfg.h);
+    if (cfg.dsf < 1 || cfg.dsf > 4) raise(LFRV_E_ARG, "dsf must be in 1..4, got %d", cfg.dsf);
+    if (cfg.nviews < 1 || cfg.nviews > 255) raise(LFRV_E_ARG, "nviews must be in 1..255, got %d", cfg.nviews);
+    if ((long long)cfg.w * cfg.h >= (1ll << 24)) raise(LFRV_E_ARG, "views larger than 2^24 pixels are not supported");
+    Geometry G;
+    G.V = cfg.nviews;
+    G.w = cfg.w;
+    G.h = cfg.h;
+    G.n = cfg.w * cfg.h;
+    G.dsf = cfg.dsf;
+    G.W = cfg.w * cfg.dsf;
+    G.H = cfg.h * cfg.dsf;
+    G.N = (size_t)G.W * G.H;
+    return G;
+}
+
+static void check_solver_options(const lfrv_config &cfg) {
+    if (cfg.dw_type != 0) raise(LFRV_E_ARG, "dw_type %d: only 0 exists upstream (optimization.cu:1141-1147)", cfg.dw_type);
+    if (cfg.dt_beta != 0.0f) raise(LFRV_E_ARG, "dt_beta > 0 (gradient data term) is not implemented");
+    if (cfg.niter < 0 || cfg.nmeta_iter < 0) raise(LFRV_E_ARG, "negative iteration count");
+    if (!(cfg.lambda > 0.0f)) raise(LFRV_E_ARG, "lambda must be > 0");
+}
+
+// ------------------------------------------------------------------ reductions
+static double *partial_buf(lfrv_ctx *c, size_t count) {
+    c->ws.partial.ensure(sizeof(double) * std::max<size_t>(count, 1));
+    return c->ws.partial.as<double>();
+}
+
+// Reduces `count` partials at `partial` into sums[slot] on the device.
+static void reduce_to(lfrv_ctx *c, int count, const double *partial, int slot) {
+    c->ws.sums.ensure(sizeof(double) * 64);
+    launch_reduce_final(count, partial, c->ws.sums.as<double>() + slot, c->stream, c->launches);
+    check_launch("reduce");
+}
+
+static void read_sums(lfrv_ctx *c, double *host, int count) {
+    LFRV_CUDA(cudaMemcpyAsync(host, c->ws.sums.p, sizeof(double) * count, cudaMemcpyDeviceToHost, c->stream));
+    sync(c);
+}
+
+// ------------------------------------------------------------------ inverse footprint map
+static Buckets build_buckets(lfrv_ctx *c, const Geometry &G, const float *tau2) {
+    Workspace &ws = c->ws;
+    const int ks = G.dsf + 1;
+    Buckets B;
+    B.BW = G.W + ks - 1;
+    B.BH = G.H + ks - 1;
+    B.nb = B.BW * B.BH;
+    ws.b_count.ensure(sizeof(unsigned int) * B.nb);
+    ws.b_start.ensure(sizeof(unsigned int) * (B.nb + 1));
+    ws.b_entries.ensure(sizeof(unsigned int) * (size_t)G.V * G.n);
+    const int nblk = (B.nb + 1023) / 1024;
+    ws.b_aux.ensure(sizeof(unsigned int) * (4 * (size_t)nblk + 4 * 1024 + 16));
+    unsigned int *aux = ws.b_aux.as<unsigned int>();
+    B.count = ws.b_count.as<unsigned int>();
+    B.start = ws.b_start.as<unsigned int>();
+    B.entries = ws.b_entries.as<unsigned int>();
+    B.block_sums = aux;
+    B.block_offsets = aux + nblk;
+    B.block_sums2 = aux + 2 * nblk;
+    B.block_offsets2 = aux + 2 * nblk + 1024;
+    B.total = aux + 2 * nblk + 2048;
+    B.total2 = aux + 2 * nblk + 2049;
+    launch_bucket_build(G, tau2, B, c->stream, c->launches);
+    check_launch("bucket build");
+    return B;
+}
+
+// ------------------------------------------------------------------ shared pieces
+static void gaussian_kernel_init() {
+    // gsl_kernel_gauss_1xn(11, 2.0) (cocolib/cocolib/common/gsl_matrix_convolutions.cpp:42-63), uploaded as float
+    double kd[11], s = 0;
+    for (int x = -5; x <= 5; ++x) {
+        kd[x + 5] = std::exp(-0.5 * x * x / 4.0);
+        s += kd[x + 5];
+    }
+    float k[11];
+    for (int i = 0; i < 11; ++i) k[i] = (float)(kd[i] / s);
+    set_gaussian(k);
+}
+
+struct ColorBuffers {
+    float *U, *Ua, *Ub, *P, *Pa, *F, *g, *g0, *tmp, *cov, *norm, *Xq, *gx, *gy, *res, *wgt, *Uprev, *Uprev_meta;
+    uint8_t *vis;
+};
+
+static ColorBuffers color_buffers(lfrv_ctx *c, const Geometry &G) {
+    Workspace &ws = c->ws;
+    const size_t N = G.N, f = sizeof(float);
+    ws.U.ensure(3 * N * f);
+    ws.Ua.ensure(3 * N * f);
+    ws.Ub.ensure(3 * N * f);
+    ws.Uprev.ensure(6 * N * f);
+    ws.P.ensure(6 * N * f);
+    ws.Pa.ensure(6 * N * f);
+    ws.F.ensure(3 * N * f);
+    ws.g.ensure(N * f);
+    ws.g0.ensure(N * f);
+    ws.tmp.ensure(N * f);
+    ws.cov.ensure(N * f);
+    ws.norm.ensure(N * f);
+    ws.Xq.ensure(2 * N * f);
+    ws.gx.ensure(N * f);
+    ws.gy.ensure(N * f);
+    ws.vis.ensure(N);
+    ws.wgt.ensure((size_t)G.V * G.n * f);
+    ws.res.ensure((size_t)G.V * 3 * G.n * f);
+    ColorBuffers b;
+    b.U = ws.U.as<float>();
+    b.Ua = ws.Ua.as<float>();
+    b.Ub = ws.Ub.as<float>();
+    b.P = ws.P.as<float>();
+    b.Pa = ws.Pa.as<float>();
+    b.F = ws.F.as<float>();
+    b.g = ws.g.as<float>();
+    b.g0 = ws.g0.as<float>();
+    b.tmp = ws.tmp.as<float>();
+    b.cov = ws.cov.as<float>();
+    b.norm = ws.norm.as<float>();
+    b.Xq = ws.Xq.as<float>();
+    b.gx = ws.gx.as<float>();
+    b.gy = ws.gy.as<float>();
+    b.vis = ws.vis.as<uint8_t>();
+    b.wgt = ws.wgt.as<float>();
+    b.res = ws.res.as<float>();
+    b.Uprev = ws.Uprev.as<float>();
+    b.Uprev_meta = ws.Uprev.as<float>() + 3 * N;
+    return b;
+}
+
+// Sobel of the luminance of U into (gx, gy) with visibility mask; optional sum of |gx| + |gy| into sums[slot].
+static void sobel_target(lfrv_ctx *c, const Geometry &G, const float *U, float *gx, float *gy, const uint8_t *vis,
+                         int abs_slot) {
+    double *part = nullptr;
+    const int np = sobel_partials(G.W, G.H);
+    if (abs_slot >= 0) part = partial_buf(c, np);
+    launch_sobel(G.W, G.H, 1, U, 0, G.N, gx, gy, 0, vis, part, c->stream, c->launches);
+    check_launch("sobel");
+    if (abs_slot >= 0) reduce_to(c, np, part, abs_slot);
+}
+
+// Weighted residuals of every view at U (and the intensity energy into sums[slot]).
+static void residual(lfrv_ctx *c, const Geometry &G, const float *U, const float *img, const float *tau2,
+                     const float *wgt, float s2, float *res, int slot) {
+    const int np = residual_partials(G);
+    double *part = partial_buf(c, np);
+    launch_residual(G, U, img, tau2, wgt, s2, res, part, c->stream, c->launches);
+    check_launch("residual");
+    reduce_to(c, np, part, slot);
+}
+
+// ------------------------------------------------------------------ IBR_color
+static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
+                        const float *init, float *out, lfrv_stats *st) {
+    check_solver_options(cfg);
+    const Geometry G = geometry(cfg);
+    const size_t N = G.N;
+    cudaStream_t s = c->stream;
+    Workspace &ws = c->ws;
+    const bool faithful = cfg.faithful != 0;
+    const float sigma = cfg.sigma_sensor, s2 = cfg.sigma_sensor * cfg.sigma_sensor;
+    const Buckets B = build_buckets(c, G, tau2);
+    ColorBuffers b = color_buffers(c, G);
+    LFRV_CUDA(cudaMemsetAsync(b.U, 0, 3 * N * sizeof(float), s));
+    LFRV_CUDA(cudaMemsetAsync(b.P, 0, 6 * N * sizeof(float), s));
+    LFRV_CUDA(cudaMemsetAsync(b.Xq, 0, 2 * N * sizeof(float), s));
+    LFRV_CUDA(cudaMemsetAsync(b.vis, 0, N, s));
+    LFRV_CUDA(cudaMemsetAsync(b.gx, 0, N * sizeof(float), s));
+    LFRV_CUDA(cudaMemsetAsync(b.gy, 0, N * sizeof(float), s));
+    // gradient buffers of compute_weights: the channel-0 duals when faithful (D5)
+    auto grad_x = [&]() { return faithful ? ws.P.as<float>() : b.gx; };
+    auto grad_y = [&]() { return faithful ? ws.P.as<float>() + N : b.gy; };
+    auto compute_weights = [&]() {
+        sobel_target(c, G, ws.U.as<float>(), grad_x(), grad_y(), b.vis, -1);
+        launch_weights(G, grad_x(), grad_y(), tau2, dp2, sigma, cfg.ugrad_threshold, b.wgt, s, c->launches);
+        check_launch("weights");
+    };
+    compute_weights();  // super-resolution.cpp:157, U = 0 and an empty visibility mask
+    launch_coverage(G, B, tau2, b.cov, b.vis, s, c->launches);  // :160
+    check_launch("coverage");
+    // content of the reference's coverage accumulator (norm_mask) before the regulariser weight
+    const float *norm_prior = b.cov;
+    if (init) {
+        LFRV_CUDA(cudaMemcpyAsync(ws.U.p, init, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    } else {
+        launch_initial_image(G, B, tau2, img, b.wgt, ws.U.as<float>(), b.norm, s, c->launches);  // :165
+        check_launch("initial image");
+        norm_prior = b.norm;
+        ws.pp_img.ensure(sizeof(float) * 3 * (N / 2 + 16));
+        ws.pp_vis.ensure(N / 2 + 16 + N);
+        ws.pp_tmp.ensure(sizeof(float) * 3 * (N / 2 + (size_t)G.W + 16));
+        ws.pp_orig.ensure(sizeof(float) * 3 * N);
+        PushPull pp;
+        float *pi = ws.pp_img.as<float>();
+        uint8_t *pv = ws.pp_vis.as<uint8_t>();
+        pp.vis[0] = pv;
+        pv += N;
+        for (int l = 1; l <= 10; ++l) {
+            const size_t sz = (size_t)(G.W >> l) * (G.H >> l);
+            pp.img[l] = pi;
+            pp.vis[l] = pv;
+            pi += 3 * sz;
+            pv += sz;
+        }
+        pp.tmp = ws.pp_tmp.as<float>();
+        pp.orig = ws.pp_orig.as<float>();
+        launch_push_pull(G.W, G.H, faithful, b.vis, ws.U.as<float>(), pp, s, c->launches);
+        check_launch("push-pull");
+    }
+    if (!faithful) norm_prior = nullptr;
+    if (cfg.early_exit) {
+        LFRV_CUDA(cudaMemcpyAsync(b.Uprev, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        LFRV_CUDA(cudaMemcpyAsync(b.Uprev_meta, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+    // primal-dual constants of coco_vtv_sr_iteration_fista_unstructured (optimization.cu:1739-1741)
+    const float tau_pd = (float)(0.3 / std::sqrt(8.0)), sigma_pd = (float)(0.3 / std::sqrt(8.0));
+    const float L = (float)(1.0 / cfg.lambda);
+    const float lam_prox = (float)(1.0 / L);
+    const float fscale = (float)(-1.0 / (double)(cfg.lambda * L));
+    const float EPS = 1e-4f, MAX_DIFF = 1e-3f, PERCENT_MOVING = 0.01f;
+    const int mp = moving_partials(N);
+
+    auto energy = [&](bool need_tv) -> float {
+        // residual pass (also the data term input of the next iteration) + TV term of the reference energy
+        residual(c, G, ws.U.as<float>(), img, tau2, b.wgt, s2, b.res, 1);
+        if (!need_tv) return 0.0f;
+        sobel_target(c, G, ws.U.as<float>(), b.Xq, b.Xq + N, b.vis, 0);
+        double sums[2];
+        read_sums(c, sums, 2);
+        const float e_tv = (float)sums[0], e_int = (float)sums[1];
+        return cfg.lambda * e_tv + cfg.dt_alpha * e_int;
+    };
+    auto moving = [&](const float *a, const float *bb) -> int {
+        double *part = partial_buf(c, mp);
+        launch_moving(N, a, bb, MAX_DIFF, part, s, c->launches);
+        check_launch("moving");
+        reduce_to(c, mp, part, 2);
+        double v[3];
+        read_sums(c, v, 3);
+        return (int)v[2];
+    };
+
+    float E = 0.0f, E_prev = 0.0f, E_prev_reweight = 0.0f;
+    int total_k = 0, reason = 0, r = 0;
+    const bool track = cfg.early_exit != 0;
+    for (r = 0; r < cfg.nmeta_iter; ++r) {
+        compute_weights();
+        launch_regweight(G, B, tau2, b.wgt, norm_prior, s2, cfg.lambda_max_factor * cfg.lambda, cfg.lambda,
+                         (float)G.V, b.g0, b.norm, s, c->launches);
+        check_launch("regularizer weight");
+        launch_blur(G.W, G.H, b.g0, b.tmp, b.g, s, c->launches);
+        check_launch("blur");
+        E = energy(true);
+        E_prev = E;
+        int k;
+        for (k = 0; k < cfg.niter; ++k) {
+            launch_dataterm_F(G, B, tau2, b.res, s2, cfg.dt_alpha, fscale, ws.U.as<float>(), b.F, nullptr, s,
+                              c->launches);
+            check_launch("data term");
+            // niter inner ROF iterations from Uq = U (ping-pong buffers)
+            const float *Ucur = ws.U.as<float>();
+            float *Udst = ws.Ua.as<float>();
+            for (int it = 0; it < cfg.niter; ++it) {
+                launch_rof_iter(G.W, G.H, tau_pd, sigma_pd, lam_prox, Ucur, ws.P.as<float>(), b.F, b.g, Udst,
+                                ws.Pa.as<float>(), s, c->launches);
+                swap_buf(ws.P, ws.Pa);
+                Ucur = Udst;
+                Udst = (Udst == ws.Ua.as<float>()) ? ws.Ub.as<float>() : ws.Ua.as<float>();
+            }
+            int nM = 0;
+            if (track) nM = moving(Ucur, ws.U.as<float>());
+            // U <- the ROF result
+            if (Ucur == ws.Ua.as<float>()) swap_buf(ws.U, ws.Ua);
+            else if (Ucur == ws.Ub.as<float>()) swap_buf(ws.U, ws.Ub);
+            ++total_k;
+            E = energy(track);
+            if (!track) continue;
+            if (E < EPS) {
+                reason = 1;
+                break;
+            }
+            const double rel = std::fabs((double)((E - E_prev) / E));
+            if (rel < (double)EPS) {
+                reason = 2;
+                break;
+            }
+            E_prev = E;
+            // sr_compare_images against R_prev (the iterate kept at the last non-breaking iteration)
+            nM = moving(ws.U.as<float>(), b.Uprev);
+            if ((float)nM / (float)N < PERCENT_MOVING) {
+                reason = 3;
+                break;
+            }
+            LFRV_CUDA(cudaMemcpyAsync(b.Uprev, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        }
+        if (faithful) norm_prior = (k > 0) ? b.cov : b.norm;  // data term clears and re-accumulates the coverage
+        if (!track) continue;
+        if (E < EPS) {
+            if (E_prev_reweight < EPS) break;
+            E_prev_reweight = E;
+            continue;
+        }
+        const int nM = moving(ws.U.as<float>(), b.Uprev_meta);
+        if ((float)nM / (float)N < PERCENT_MOVING) break;
+        LFRV_CUDA(cudaMemcpyAsync(b.Uprev_meta, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
+    LFRV_CUDA(cudaMemcpyAsync(out, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    if (st) {
+        st->outer_iterations = total_k;
+        st->meta_iterations = std::min(r + 1, cfg.nmeta_iter);
+        st->stop_reason = reason;
+        st->energy = (double)E;
+    }
+}
+
+// ------------------------------------------------------------------ IBR_gradient
+static int hole_fill(lfrv_ctx *c, int W, int H, const uint8_t *vis, float *U, int max_iter) {
+    Workspace &ws = c->ws;
+    const size_t N = (size_t)W * H;
+    cudaStream_t s = c->stream;
+    ws.holes.ensure(sizeof(int) * (N + H + 16));
+    ws.hole_count.ensure(sizeof(int) * 4);
+    launch_hole_list(W, H, vis, ws.holes.as<int>(), ws.hole_count.as<int>(), s, c->launches);
+    check_launch("hole list");
+    int nholes = 0;
+    LFRV_CUDA(cudaMemcpyAsync(&nholes, ws.hole_count.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    sync(c);
+    // hole_filling (sources/gradientIBR.cu:87-152): stop when the change of the last channel's
+    // sum(lap * U) drops below epsilon = 1e-3 (float energies).
+    ws.Ua.ensure(3 * N * sizeof(float));
+    float *A = U, *Bb = ws.Ua.as<float>();
+    LFRV_CUDA(cudaMemcpyAsync(Bb, A, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    const int np = hole_fill_partials(nholes);
+    float energy = 0.0f, previous = 0.0f;
+    int k;
+    for (k = 0; k < max_iter; ++k) {
+        previous = energy;
+        double e = 0.0;
+        if (nholes > 0) {
+            double *part = partial_buf(c, np);
+            launch_hole_fill_iter(W, H, ws.holes.as<int>(), nholes, A, Bb, part, s, c->launches);
+            check_launch("hole fill");
+            reduce_to(c, np, part, 0);
+            read_sums(c, &e, 1);
+            std::swap(A, Bb);
+        }
+        energy = (float)e;
+        if (std::fabs(previous - energy) < 1e-3f) {
+            ++k;
+            break;
+        }
+    }
+    if (A != U) LFRV_CUDA(cudaMemcpyAsync(U, A, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    return k;
+}
+
+static void u_gradient(lfrv_ctx *c, const Geometry &G, const Buckets &B, const float *img, const float *tau2,
+                       const float *wgt, float s2, float *gx, float *gy, float *mask) {
+    Workspace &ws = c->ws;
+    ws.vgrad.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    float *vg = ws.vgrad.as<float>();
+    // Sobel of every input view's luminance (compute_gradient, sources/gradientIBR_kernels.cuh:57-100)
+    launch_sobel(G.w, G.h, G.V, img, (size_t)3 * G.n, (size_t)G.n, vg, vg + G.n, (size_t)2 * G.n, nullptr, nullptr,
+                 c->stream, c->launches);
+    check_launch("view sobel");
+    launch_u_gradient(G, B, tau2, vg, wgt, s2, gx, gy, mask, c->stream, c->launches);
+    check_launch("gradient splat");
+}
+
+// Conjugate gradient of possion_conj_grad (faithful) or the corrected CG (see lfrv_stage_cg).
+static int cg_solve(lfrv_ctx *c, int W, int H, bool faithful, int max_iter, double gap_tol, const float *gx,
+                    const float *gy, float *U, double *gap_out) {
+    Workspace &ws = c->ws;
+    const size_t N = (size_t)W * H;
+    cudaStream_t s = c->stream;
+    ws.r.ensure(3 * N * sizeof(float));
+    ws.d.ensure(3 * N * sizeof(float));
+    ws.q.ensure(3 * N * sizeof(float));
+    ws.U0.ensure(3 * N * sizeof(float));
+    float *r = ws.r.as<float>(), *d = ws.d.as<float>(), *q = ws.q.as<float>(), *U0 = ws.U0.as<float>();
+    LFRV_CUDA(cudaMemcpyAsync(U0, U, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    const int np = cg_partials(W, H);
+    double *part = partial_buf(c, 3 * (size_t)np);
+    ws.sums.ensure(sizeof(double) * 64);
+    double *sums = ws.sums.as<double>();
+    auto reduce3 = [&](double out[3]) {
+        launch_reduce_segments(np, 3, part, sums, s, c->launches);
+        check_launch("reduce3");
+        LFRV_CUDA(cudaMemcpyAsync(out, sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+        sync(c);
+    };
+    const float lambda = 1.0f;  // possion_conj_grad: lambda = 1.0 (solver.cu:541)
+    double delta[3];
+    launch_cg_init(W, H, U, gx, gy, r, d, faithful, part, s, c->launches);
+    check_launch("cg init");
+    reduce3(delta);
+    int it = 0;
+    if (faithful) {
+        double dAlpha[3] = {0, 0, 0};
+        const float beta[3] = {1.0f, 1.0f, 1.0f};
+        for (it = 0; it < 5; ++it) {
+            double dq[3], rr[3];
+            launch_cg_apply(W, H, d, lambda, q, part, s, c->launches);
+            check_launch("cg apply");
+            reduce3(dq);
+            float alpha[3];
+            for (int ch = 0; ch < 3; ++ch) {
+                dAlpha[ch] += dq[ch];
+                alpha[ch] = (float)delta[ch] / (float)dAlpha[ch];
+            }
+            launch_cg_update(W, H, alpha, d, q, U, r, part, s, c->launches);
+            check_launch("cg update");
+            reduce3(rr);
+            for (int ch = 0; ch < 3; ++ch) dAlpha[ch] = (double)alpha[ch] + rr[ch];
+            launch_cg_dir(W, H, beta, r, d, s, c->launches);
+            check_launch("cg dir");
+        }
+        if (gap_out) *gap_out = 0.0;
+        return it;
+    }
+    // E(u) by one FP64 pass; then E_{k+1} = E_k - alpha_k delta_k / 2 and the certificate
+    // E(u) - E* <= ||r||^2 / (2 lambda).
+    double E;
+    {
+        launch_cg_energy(W, H, U, U0, gx, gy, part, s, c->launches);
+        check_launch("cg energy");
+        double e3[3];
+        reduce3(e3);
+        E = e3[0] + e3[1] + e3[2];
+    }
+    double gap = 1e300;
+    for (it = 0;; ++it) {
+        const double bound = (delta[0] + delta[1] + delta[2]) / (2.0 * (double)lambda);
+        gap = (E - bound) > 0 ? bound / (E - bound) : 1e300;
+        if (it >= max_iter || (gap_tol > 0 && gap <= gap_tol)) break;
+        double dq[3], rr[3];
+        launch_cg_apply(W, H, d, lambda, q, part, s, c->launches);
+        check_launch("cg apply");
+        reduce3(dq);
+        float alpha[3];
+        double alpha_d[3];
+        for (int ch = 0; ch < 3; ++ch) {
+            alpha_d[ch] = (dq[ch] > 0) ? delta[ch] / dq[ch] : 0.0;
+            alpha[ch] = (float)alpha_d[ch];
+        }
+        launch_cg_update(W, H, alpha, d, q, U, r, part, s, c->launches);
+        check_launch("cg update");
+        reduce3(rr);
+        float beta[3];
+        for (int ch = 0; ch < 3; ++ch) {
+            E -= 0.5 * alpha_d[ch] * delta[ch];
+            beta[ch] = (delta[ch] > 0) ? (float)(rr[ch] / delta[ch]) : 0.0f;
+            delta[ch] = rr[ch];
+        }
+        launch_cg_dir(W, H, beta, r, d, s, c->launches);
+        check_launch("cg dir");
+    }
+    if (gap_out) *gap_out = gap;
+    return it;
+}
+
+static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
+                           const float *init, float *out, lfrv_stats *st) {
+    check_solver_options(cfg);
+    const Geometry G = geometry(cfg);
+    if (G.W < 2 || G.H < 2) raise(LFRV_E_ARG, "IBR_gradient needs a target of at least 2 x 2 pixels");
+    const size_t N = G.N;
+    cudaStream_t s = c->stream;
+    Workspace &ws = c->ws;
+    const float s2 = cfg.sigma_sensor * cfg.sigma_sensor;
+    const Buckets B = build_buckets(c, G, tau2);
+    ColorBuffers b = color_buffers(c, G);
+    ws.mask.ensure(N * sizeof(float));
+    launch_vis_any(G, B, tau2, b.vis, s, c->launches);  // setup_target_visibility
+    check_launch("visibility");
+    // compute_weights with U = 0: the unmasked Sobel of 0 is 0 (sources/gradientIBR.cu:575-577)
+    LFRV_CUDA(cudaMemsetAsync(b.gx, 0, N * sizeof(float), s));
+    LFRV_CUDA(cudaMemsetAsync(b.gy, 0, N * sizeof(float), s));
+    launch_weights(G, b.gx, b.gy, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, s, c->launches);
+    check_launch("weights");
+    float *U = ws.U.as<float>();
+    int hf = 0;
+    if (init) {
+        LFRV_CUDA(cudaMemcpyAsync(U, init, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    } else {
+        launch_initial_image(G, B, tau2, img, b.wgt, U, b.norm, s, c->launches);
+        check_launch("initial image");
+        hf = hole_fill(c, G.W, G.H, b.vis, U, cfg.hole_fill_iter);
+    }
+    u_gradient(c, G, B, img, tau2, b.wgt, s2, b.gx, b.gy, ws.mask.as<float>());
+    double gap = 0;
+    const int it = cg_solve(c, G.W, G.H, cfg.faithful != 0, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U, &gap);
+    LFRV_CUDA(cudaMemcpyAsync(out, U, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    if (st) {
+        st->outer_iterations = it;
+        st->hole_fill_iterations = hf;
+        st->gap = gap;
+        st->stop_reason = (!cfg.faithful && cfg.cg_gap_tol > 0 && gap <= cfg.cg_gap_tol) ? 4 : 0;
+    }
+}
+
+// ------------------------------------------------------------------ warp stage
+static void mat3mul(const double *A, const double *B, double *C) {
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) {
+            double s = 0;
+            for (int k = 0; k < 3; ++k) s += A[3 * r + k] * B[3 * k + c];
+            C[3 * r + c] = s;
+        }
+}
+
+static void inv3(const double *m, double *o) {
+    const double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5], g = m[6], h = m[7], i = m[8];
+    const double A = e * i - f * h, B = -(d * i - f * g), C = d * h - e * g;
+    const double det = a * A + b * B + c * C;
+    if (det == 0) raise(LFRV_E_ARG, "singular camera intrinsics");
+    o[0] = A / det;
+    o[1] = -(b * i - c * h) / det;
+    o[2] = (b * f - c * e) / det;
+    o[3] = B / det;
+    o[4] = (a * i - c * g) / det;
+    o[5] = -(a * f - c * d) / det;
+    o[6] = C / det;
+    o[7] = -(a * h - b * g) / det;
+    o[8] = (a * e - b * d) / det;
+}
+
+// Folds view k and target u into M = K_u R_u R_k^T K_k^-1, b = K_u (t_u - R_u R_k^T t_k).
+static DevCamera fold_camera(const lfrv_camera &k, const lfrv_camera &u) {
+    double Kk[9], Rk[9], Ku[9], Ru[9], Kki[9], RkT[9];
+    for (int i = 0; i < 9; ++i) {
+        Kk[i] = k.K[i];
+        Rk[i] = k.R[i];
+        Ku[i] = u.K[i];
+        Ru[i] = u.R[i];
+    }
+    inv3(Kk, Kki);
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) RkT[3 * r + c] = Rk[3 * c + r];
+    double T1[9], T2[9], M[9];
+    mat3mul(RkT, Kki, T1);
+    mat3mul(Ru, T1, T2);
+    mat3mul(Ku, T2, M);
+    double RuRkT[9];
+    mat3mul(Ru, RkT, RuRkT);
+    double v[3];
+    for (int r = 0; r < 3; ++r) {
+        double sacc = 0;
+        for (int c = 0; c < 3; ++c) sacc += RuRkT[3 * r + c] * k.t[c];
+        v[r] = u.t[r] - sacc;
+    }
+    DevCamera d;
+    std::memset(&d, 0, sizeof(d));
+    for (int i = 0; i < 9; ++i) d.M[i] = (float)M[i];
+    for (int r = 0; r < 3; ++r) {
+        double sacc = 0;
+        for (int c = 0; c < 3; ++c) sacc += Ku[3 * r + c] * v[c];
+        d.t[r] = (float)sacc;
+    }
+    d.W = u.width;
+    d.H = u.height;
+    return d;
+}
+
+static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfrv_camera *cams,
+                 const lfrv_camera *target, float *tau3, float *dpart3, float *tau2, float *dp2, float *zbuf_out) {
+    if (V < 1 || V > 255 || w <= 0 || h <= 0 || !depth || !cams || !target) raise(LFRV_E_ARG, "bad warp arguments");
+    Workspace &ws = c->ws;
+    const int W = target->width, H = target->height;
+    if (W <= 0 || H <= 0) raise(LFRV_E_ARG, "bad target size");
+    const size_t N = (size_t)W * H;
+    std::vector<DevCamera> dc(V);
+    for (int v = 0; v < V; ++v) dc[v] = fold_camera(cams[v], *target);
+    DevCamera tgt;
+    std::memset(&tgt, 0, sizeof(tgt));
+    tgt.W = W;
+    tgt.H = H;
+    ws.cams.ensure(sizeof(DevCamera) * V);
+    LFRV_CUDA(cudaMemcpyAsync(ws.cams.p, dc.data(), sizeof(DevCamera) * V, cudaMemcpyHostToDevice, c->stream));
+    ws.zkey.ensure(sizeof(unsigned long long) * N);
+    ws.zbuf.ensure(sizeof(float) * N);
+    launch_zbuffer_clear(W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
+    launch_zbuffer_splat(V, w, h, depth, ws.cams.as<DevCamera>(), tgt, ws.zkey.as<unsigned long long>(), c->stream,
+                         c->launches);
+    launch_zbuffer_resolve(W, H, ws.zkey.as<unsigned long long>(), ws.zbuf.as<float>(), c->stream, c->launches);
+    check_launch("z-buffer");
+    launch_tau(V, w, h, depth, ws.cams.as<DevCamera>(), tgt, ws.zbuf.as<float>(), tau3, dpart3, tau2, dp2, c->stream,
+               c->launches);
+    check_launch("tau");
+    if (zbuf_out)
+        LFRV_CUDA(cudaMemcpyAsync(zbuf_out, ws.zbuf.p, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->stream));
+    // host copies of the cameras must stay alive until the copy completes
+    sync(c);
+}
+
+// ------------------------------------------------------------------ helpers for host-buffer entry points
+struct HostIO {
+    lfrv_ctx *c;
+    template <class T>
+    T *up(DevBuf &buf, const T *host, size_t count) {
+        if (!host) return nullptr;
+        buf.ensure(sizeof(T) * count);
+        LFRV_CUDA(cudaMemcpyAsync(buf.p, host, sizeof(T) * count, cudaMemcpyHostToDevice, c->stream));
+        return buf.as<T>();
+    }
+    template <class T>
+    void down(T *host, const T *dev, size_t count) {
+        if (!host) return;
+        LFRV_CUDA(cudaMemcpyAsync(host, dev, sizeof(T) * count, cudaMemcpyDeviceToHost, c->stream));
+    }
+};
+
+// Converts caller tau (tau_channels per view) and dpart (3 per view) into the solver layout.
+static void prepare_geometry_inputs(lfrv_ctx *c, const Geometry &G, const float *d_tau, int tau_channels,
+                                    const float *d_dpart) {
+    if (tau_channels != 2 && tau_channels != 3) raise(LFRV_E_ARG, "tau_channels must be 2 or 3");
+    Workspace &ws = c->ws;
+    ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    launch_copy_tau(G.V, G.n, d_tau, tau_channels, ws.tau.as<float>(), c->stream, c->launches);
+    if (d_dpart) launch_premultiply_dpart(G.V, G.n, d_dpart, 3, ws.dp.as<float>(), c->stream, c->launches);
+    else LFRV_CUDA(cudaMemsetAsync(ws.dp.p, 0, sizeof(float) * 2 * (size_t)G.V * G.n, c->stream));
+    check_launch("input layout");
+}
+
+static void begin_timing(lfrv_ctx *c) { LFRV_CUDA(cudaEventRecord(c->ev0, c->stream)); }
+static void end_timing(lfrv_ctx *c, lfrv_stats *st, long long launches0) {
+    LFRV_CUDA(cudaEventRecord(c->ev1, c->stream));
+    LFRV_CUDA(cudaEventSynchronize(c->ev1));
+    if (st) {
+        float ms = 0;
+        cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+        st->seconds = ms * 1e-3;
+        st->kernel_launches = (int)(c->launches.n - launches0);
+    }
+}
+
+}  // namespace lfrv
+
+using namespace lfrv;
+
+#define CTX_CHECK(ctx)                                                   \
+    if (!(ctx)) return lfrv::fail(LFRV_E_ARG, "null context");           \
+    LFRV_CUDA(cudaSetDevice((ctx)->device));
+
+// ====================================================================== contexts
+extern "C" int lfrv_ctx_create(lfrv_ctx **out, int device) {
+    LFRV_API_BEGIN
+    if (!out) return fail(LFRV_E_ARG, "null output pointer");
+    int count = 0;
+    if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        return fail(LFRV_E_NODEVICE, "no CUDA device available");
+    }
+    if (device < 0 || device >= count) return fail(LFRV_E_ARG, "device %d out of range", device);
+    LFRV_CUDA(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    LFRV_CUDA(cudaGetDeviceProperties(&prop, device));
+    if (prop.major * 10 + prop.minor < 100)
+        return fail(LFRV_E_NODEVICE, "device %d is sm_%d%d; this library carries sm_103a code only", device,
+                    prop.major, prop.minor);
+    lfrv_ctx *c = new lfrv_ctx;
+    c->device = device;
+    LFRV_CUDA(cudaEventCreate(&c->ev0));
+    LFRV_CUDA(cudaEventCreate(&c->ev1));
+    gaussian_kernel_init();
+    {
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            delete c;
+            return fail(LFRV_E_NODEVICE, "kernel image not loadable on device %d: %s", device, cudaGetErrorString(e));
+        }
+    }
+    *out = c;
+    LFRV_API_END
+}
+
+extern "C" int lfrv_ctx_destroy(lfrv_ctx *ctx) {
+    LFRV_API_BEGIN
+    if (!ctx) return LFRV_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    else cudaDeviceSynchronize();
+    if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+    if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    ctx->prof.destroy();
+    delete ctx;
+    LFRV_API_END
+}
+
+extern "C" int lfrv_ctx_set_stream(lfrv_ctx *ctx, void *cuda_stream) {
+    LFRV_API_BEGIN
+    if (!ctx) return fail(LFRV_E_ARG, "null context");
+    ctx->stream = (cudaStream_t)cuda_stream;
+    LFRV_API_END
+}
+
+extern "C" int lfrv_ctx_launch_count(lfrv_ctx *ctx, long long *count, int reset) {
+    LFRV_API_BEGIN
+    if (!ctx || !count) return fail(LFRV_E_ARG, "null argument");
+    *count = ctx->launches.n;
+    if (reset) ctx->launches.n = 0;
+    LFRV_API_END
+}
+
+extern "C" int lfrv_ctx_profile(lfrv_ctx *ctx, int enable) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (enable) {
+        ctx->prof.init(1 << 16);
+        ctx->prof.recs.clear();
+        ctx->prof.next = 0;
+        ctx->prof.overflow = false;
+        ctx->launches.prof = &ctx->prof;
+    } else {
+        ctx->launches.prof = nullptr;
+    }
+    LFRV_API_END
+}
+
+extern "C" int lfrv_ctx_profile_read(lfrv_ctx *ctx, int index, char *name, size_t name_len, double *total_ms,
+                                     long long *launches) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (ctx->stream) LFRV_CUDA(cudaStreamSynchronize(ctx->stream));
+    else LFRV_CUDA(cudaDeviceSynchronize());
+    // aggregate per kernel name in first-seen order
+    std::vector<std::string> names;
+    std::vector<double> ms;
+    std::vector<long long> cnt;
+    for (const auto &r : ctx->prof.recs) {
+        float t = 0.f;
+        LFRV_CUDA(cudaEventElapsedTime(&t, ctx->prof.ev[2 * r.slot], ctx->prof.ev[2 * r.slot + 1]));
+        size_t k = 0;
+        while (k < names.size() && names[k] != r.name) ++k;
+        if (k == names.size()) {
+            names.push_back(r.name);
+            ms.push_back(0.0);
+            cnt.push_back(0);
+        }
+        ms[k] += t;
+        cnt[k] += 1;
+    }
+    if (index < 0 || index >= (int)names.size()) return fail(LFRV_E_ARG, "profile index %d out of range", index);
+    if (name && name_len) std::snprintf(name, name_len, "%s", names[index].c_str());
+    if (total_ms) *total_ms = ms[index];
+    if (launches) *launches = cnt[index];
+    if (ctx->prof.overflow) return fail(LFRV_E_ARG, "profile event pool overflowed; totals are partial");
+    LFRV_API_END
+}
+
+// ====================================================================== warp
+extern "C" int lfrv_warp_dev(lfrv_ctx *ctx, int nviews, int w, int h, const float *d_depth, const lfrv_camera *cams,
+                             const lfrv_camera *target, float *d_tau, float *d_dpart, float *d_zbuf) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    warp(ctx, nviews, w, h, d_depth, cams, target, d_tau, d_dpart, nullptr, nullptr, d_zbuf);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_warp(lfrv_ctx *ctx, int nviews, int w, int h, const float *depth, const lfrv_camera *cams,
+                         const lfrv_camera *target, float *tau, float *dpart, float *zbuf) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!depth || !target) return fail(LFRV_E_ARG, "null argument");
+    HostIO io{ctx};
+    const size_t n = (size_t)w * h, V = (size_t)nviews, N = (size_t)target->width * target->height;
+    float *dd = io.up(ctx->ws.depth, depth, V * 3 * n);
+    ctx->ws.in_tau.ensure(sizeof(float) * V * 3 * n);
+    ctx->ws.in_dpart.ensure(sizeof(float) * V * 3 * n);
+    ctx->ws.out_img.ensure(sizeof(float) * N);
+    warp(ctx, nviews, w, h, dd, cams, target, ctx->ws.in_tau.as<float>(), ctx->ws.in_dpart.as<float>(), nullptr,
+         nullptr, ctx->ws.out_img.as<float>());
+    io.down(tau, ctx->ws.in_tau.as<float>(), V * 3 * n);
+    io.down(dpart, ctx->ws.in_dpart.as<float>(), V * 3 * n);
+    io.down(zbuf, ctx->ws.out_img.as<float>(), N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+// ====================================================================== solvers
+static int solve_dev(lfrv_ctx *ctx, const lfrv_config *cfg, bool color, const float *d_views, const float *d_tau,
+                     int tau_channels, const float *d_dpart, const float *d_init, float *d_out, lfrv_stats *stats) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!cfg || !d_views || !d_tau || !d_out) return fail(LFRV_E_ARG, "null argument");
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    const Geometry G = geometry(*cfg);
+    const long long l0 = ctx->launches.n;
+    begin_timing(ctx);
+    prepare_geometry_inputs(ctx, G, d_tau, tau_channels, d_dpart);
+    if (color)
+        color_solve(ctx, *cfg, d_views, ctx->ws.tau.as<float>(), ctx->ws.dp.as<float>(), d_init, d_out, stats);
+    else
+        gradient_solve(ctx, *cfg, d_views, ctx->ws.tau.as<float>(), ctx->ws.dp.as<float>(), d_init, d_out, stats);
+    end_timing(ctx, stats, l0);
+    LFRV_API_END
+}
+
+static int solve_host(lfrv_ctx *ctx, const lfrv_config *cfg, bool color, const float *views, const float *tau,
+                      int tau_channels, const float *dpart, const float *init, float *out, lfrv_stats *stats) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!cfg || !views || !tau || !out) return fail(LFRV_E_ARG, "null argument");
+    const Geometry G = geometry(*cfg);
+    HostIO io{ctx};
+    const size_t n = G.n, V = G.V;
+    const float *dv = io.up(ctx->ws.in_views, views, V * 3 * n);
+    const float *dt = io.up(ctx->ws.in_tau, tau, V * (size_t)tau_channels * n);
+    const float *dd = io.up(ctx->ws.in_dpart, dpart, V * 3 * n);
+    const float *di = io.up(ctx->ws.in_init, init, 3 * G.N);
+    ctx->ws.out_img.ensure(sizeof(float) * 3 * G.N);
+    const int rc = solve_dev(ctx, cfg, color, dv, dt, tau_channels, dd, di, ctx->ws.out_img.as<float>(), stats);
+    if (rc != LFRV_OK) return rc;
+    io.down(out, ctx->ws.out_img.as<float>(), 3 * G.N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_ibr_color_dev(lfrv_ctx *ctx, const lfrv_config *cfg, const float *d_views, const float *d_tau,
+                                  int tau_channels, const float *d_dpart, const float *d_init, float *d_out,
+                                  lfrv_stats *stats) {
+    return solve_dev(ctx, cfg, true, d_views, d_tau, tau_channels, d_dpart, d_init, d_out, stats);
+}
+extern "C" int lfrv_ibr_gradient_dev(lfrv_ctx *ctx, const lfrv_config *cfg, const float *d_views, const float *d_tau,
+                                     int tau_channels, const float *d_dpart, const float *d_init, float *d_out,
+                                     lfrv_stats *stats) {
+    return solve_dev(ctx, cfg, false, d_views, d_tau, tau_channels, d_dpart, d_init, d_out, stats);
+}
+extern "C" int lfrv_ibr_color(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                              int tau_channels, const float *dpart, const float *init, float *out, lfrv_stats *stats) {
+    return solve_host(ctx, cfg, true, views, tau, tau_channels, dpart, init, out, stats);
+}
+extern "C" int lfrv_ibr_gradient(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                                 int tau_channels, const float *dpart, const float *init, float *out,
+                                 lfrv_stats *stats) {
+    return solve_host(ctx, cfg, false, views, tau, tau_channels, dpart, init, out, stats);
+}
+
+extern "C" int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm, const float *d_views,
+                                    const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target,
+                                    float *d_out, lfrv_stats *stats) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!cfg || !d_views || !d_depth || !cams || !target || !d_out) return fail(LFRV_E_ARG, "null argument");
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    const Geometry G = geometry(*cfg);
+    if (target->width != G.W || target->height != G.H) return fail(LFRV_E_ARG, "target size mismatch");
+    const long long l0 = ctx->launches.n;
+    begin_timing(ctx);
+    Workspace &ws = ctx->ws;
+    ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr);
+    if (algorithm == 0) color_solve(ctx, *cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
+    else gradient_solve(ctx, *cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
+    end_timing(ctx, stats, l0);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_render_view(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm, const float *views,
+                                const float *depth, const lfrv_camera *cams, const lfrv_camera *target, float *out,
+                                lfrv_stats *stats) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!cfg || !views || !depth || !out) return fail(LFRV_E_ARG, "null argument");
+    const Geometry G = geometry(*cfg);
+    HostIO io{ctx};
+    const size_t n = G.n, V = G.V;
+    const float *dv = io.up(ctx->ws.in_views, views, V * 3 * n);
+    const float *dd = io.up(ctx->ws.depth, depth, V * 3 * n);
+    ctx->ws.out_img.ensure(sizeof(float) * 3 * G.N);
+    const int rc = lfrv_render_view_dev(ctx, cfg, algorithm, dv, dd, cams, target, ctx->ws.out_img.as<float>(), stats);
+    if (rc != LFRV_OK) return rc;
+    io.down(out, ctx->ws.out_img.as<float>(), 3 * G.N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+// ====================================================================== stage calls
+namespace {
+
+struct StageInputs {
+    Geometry G;
+    const float *img = nullptr, *tau2 = nullptr, *dp2 = nullptr;
+};
+
+StageInputs stage_inputs(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau, int tau_ch,
+                         const float *dpart) {
+    StageInputs si;
+    si.G = geometry(*cfg);
+    HostIO io{ctx};
+    const size_t n = si.G.n, V = si.G.V;
+    std::vector<float> zeros;
+    if (!views) {
+        zeros.assign(V * 3 * n, 0.0f);
+        views = zeros.data();
+    }
+    si.img = io.up(ctx->ws.in_views, views, V * 3 * n);
+    const float *dt = io.up(ctx->ws.in_tau, tau, V * (size_t)tau_ch * n);
+    const float *dd = io.up(ctx->ws.in_dpart, dpart, V * 3 * n);
+    prepare_geometry_inputs(ctx, si.G, dt, tau_ch, dd);
+    si.tau2 = ctx->ws.tau.as<float>();
+    si.dp2 = ctx->ws.dp.as<float>();
+    sync(ctx);
+    return si;
+}
+
+}  // namespace
+
+extern "C" int lfrv_stage_visibility(lfrv_ctx *ctx, const lfrv_config *cfg, const float *tau, int tau_channels,
+                                     float *coverage, uint8_t *vis) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    StageInputs si = stage_inputs(ctx, cfg, nullptr, tau, tau_channels, nullptr);
+    const Buckets B = build_buckets(ctx, si.G, si.tau2);
+    ColorBuffers b = color_buffers(ctx, si.G);
+    launch_coverage(si.G, B, si.tau2, b.cov, b.vis, ctx->stream, ctx->launches);
+    check_launch("coverage");
+    HostIO io{ctx};
+    io.down(coverage, b.cov, si.G.N);
+    io.down(vis, b.vis, si.G.N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_weights(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                                  int tau_channels, const float *dpart, const float *U, const uint8_t *vis, float *gx,
+                                  float *gy, float *weights) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    StageInputs si = stage_inputs(ctx, cfg, views, tau, tau_channels, dpart);
+    const Geometry &G = si.G;
+    ColorBuffers b = color_buffers(ctx, G);
+    HostIO io{ctx};
+    io.up(ctx->ws.U, U, 3 * G.N);
+    io.up(ctx->ws.vis, vis, G.N);
+    io.up(ctx->ws.gx, gx, G.N);
+    io.up(ctx->ws.gy, gy, G.N);
+    launch_sobel(G.W, G.H, 1, ctx->ws.U.as<float>(), 0, G.N, b.gx, b.gy, 0, b.vis, nullptr, ctx->stream,
+                 ctx->launches);
+    launch_weights(G, b.gx, b.gy, si.tau2, si.dp2, cfg->sigma_sensor, cfg->ugrad_threshold, b.wgt, ctx->stream,
+                   ctx->launches);
+    check_launch("weights");
+    io.down(gx, b.gx, G.N);
+    io.down(gy, b.gy, G.N);
+    io.down(weights, b.wgt, (size_t)G.V * G.n);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_dataterm(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                                   int tau_channels, const float *weights, const float *U, float *Gout, float *F) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    StageInputs si = stage_inputs(ctx, cfg, views, tau, tau_channels, nullptr);
+    const Geometry &G = si.G;
+    const Buckets B = build_buckets(ctx, G, si.tau2);
+    ColorBuffers b = color_buffers(ctx, G);
+    HostIO io{ctx};
+    io.up(ctx->ws.wgt, weights, (size_t)G.V * G.n);
+    io.up(ctx->ws.U, U, 3 * G.N);
+    ctx->ws.G.ensure(sizeof(float) * 3 * G.N);
+    const float s2 = cfg->sigma_sensor * cfg->sigma_sensor;
+    residual(ctx, G, ctx->ws.U.as<float>(), si.img, si.tau2, b.wgt, s2, b.res, 0);
+    const float L = (float)(1.0 / cfg->lambda);
+    const float fscale = (float)(-1.0 / (double)(cfg->lambda * L));
+    launch_dataterm_F(G, B, si.tau2, b.res, s2, cfg->dt_alpha, fscale, ctx->ws.U.as<float>(), b.F,
+                      ctx->ws.G.as<float>(), ctx->stream, ctx->launches);
+    check_launch("data term");
+    io.down(Gout, ctx->ws.G.as<float>(), 3 * G.N);
+    io.down(F, b.F, 3 * G.N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_rof(lfrv_ctx *ctx, int W, int H, int niter, float tau, float sigma, float lambda,
+                              const float *F, const float *g, float *U, float *P) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (W <= 0 || H <= 0 || niter < 0 || !F || !g || !U || !P) return fail(LFRV_E_ARG, "bad arguments");
+    const size_t N = (size_t)W * H;
+    Workspace &ws = ctx->ws;
+    HostIO io{ctx};
+    io.up(ws.F, F, 3 * N);
+    io.up(ws.g, g, N);
+    io.up(ws.U, U, 3 * N);
+    io.up(ws.P, P, 6 * N);
+    ws.Ua.ensure(3 * N * sizeof(float));
+    ws.Pa.ensure(6 * N * sizeof(float));
+    for (int it = 0; it < niter; ++it) {
+        launch_rof_iter(W, H, tau, sigma, lambda, ws.U.as<float>(), ws.P.as<float>(), ws.F.as<float>(),
+                        ws.g.as<float>(), ws.Ua.as<float>(), ws.Pa.as<float>(), ctx->stream, ctx->launches);
+        swap_buf(ws.U, ws.Ua);
+        swap_buf(ws.P, ws.Pa);
+    }
+    check_launch("rof");
+    io.down(U, ws.U.as<float>(), 3 * N);
+    io.down(P, ws.P.as<float>(), 6 * N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_energy(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                                 int tau_channels, const float *weights, const float *U, const uint8_t *vis,
+                                 double *energy, double *e_tv, double *e_data) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    StageInputs si = stage_inputs(ctx, cfg, views, tau, tau_channels, nullptr);
+    const Geometry &G = si.G;
+    ColorBuffers b = color_buffers(ctx, G);
+    HostIO io{ctx};
+    io.up(ctx->ws.wgt, weights, (size_t)G.V * G.n);
+    io.up(ctx->ws.U, U, 3 * G.N);
+    io.up(ctx->ws.vis, vis, G.N);
+    LFRV_CUDA(cudaMemsetAsync(b.Xq, 0, 2 * G.N * sizeof(float), ctx->stream));
+    const float s2 = cfg->sigma_sensor * cfg->sigma_sensor;
+    sobel_target(ctx, G, ctx->ws.U.as<float>(), b.Xq, b.Xq + G.N, b.vis, 0);
+    residual(ctx, G, ctx->ws.U.as<float>(), si.img, si.tau2, b.wgt, s2, b.res, 1);
+    double sums[2];
+    read_sums(ctx, sums, 2);
+    if (e_tv) *e_tv = sums[0];
+    if (e_data) *e_data = sums[1];
+    if (energy) *energy = (double)cfg->lambda * sums[0] + (double)cfg->dt_alpha * sums[1];
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_regularizer(lfrv_ctx *ctx, const lfrv_config *cfg, const float *tau, int tau_channels,
+                                      const float *weights, const float *norm_in, float *norm_out, float *g) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    StageInputs si = stage_inputs(ctx, cfg, nullptr, tau, tau_channels, nullptr);
+    const Geometry &G = si.G;
+    const Buckets B = build_buckets(ctx, G, si.tau2);
+    ColorBuffers b = color_buffers(ctx, G);
+    HostIO io{ctx};
+    io.up(ctx->ws.wgt, weights, (size_t)G.V * G.n);
+    const float *prior = norm_in ? io.up(ctx->ws.norm, norm_in, G.N) : nullptr;
+    const float s2 = cfg->sigma_sensor * cfg->sigma_sensor;
+    launch_regweight(G, B, si.tau2, b.wgt, prior, s2, cfg->lambda_max_factor * cfg->lambda, cfg->lambda, (float)G.V,
+                     b.g0, b.norm, ctx->stream, ctx->launches);
+    launch_blur(G.W, G.H, b.g0, b.tmp, b.g, ctx->stream, ctx->launches);
+    check_launch("regularizer");
+    io.down(norm_out, b.norm, G.N);
+    io.down(g, b.g, G.N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_initial_image(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                                        int tau_channels, const float *weights, float *U, float *norm) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    StageInputs si = stage_inputs(ctx, cfg, views, tau, tau_channels, nullptr);
+    const Geometry &G = si.G;
+    const Buckets B = build_buckets(ctx, G, si.tau2);
+    ColorBuffers b = color_buffers(ctx, G);
+    HostIO io{ctx};
+    io.up(ctx->ws.wgt, weights, (size_t)G.V * G.n);
+    launch_initial_image(G, B, si.tau2, si.img, b.wgt, ctx->ws.U.as<float>(), b.norm, ctx->stream, ctx->launches);
+    check_launch("initial image");
+    io.down(U, ctx->ws.U.as<float>(), 3 * G.N);
+    io.down(norm, b.norm, G.N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_push_pull(lfrv_ctx *ctx, int W, int H, int faithful, const uint8_t *vis, float *U) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (W <= 0 || H <= 0 || !vis || !U) return fail(LFRV_E_ARG, "bad arguments");
+    const size_t N = (size_t)W * H;
+    Workspace &ws = ctx->ws;
+    HostIO io{ctx};
+    io.up(ws.U, U, 3 * N);
+    io.up(ws.vis, vis, N);
+    ws.pp_img.ensure(sizeof(float) * 3 * (N / 2 + 16));
+    ws.pp_vis.ensure(N / 2 + 16 + N);
+    ws.pp_tmp.ensure(sizeof(float) * 3 * (N / 2 + (size_t)W + 16));
+    ws.pp_orig.ensure(sizeof(float) * 3 * N);
+    PushPull pp;
+    float *pi = ws.pp_img.as<float>();
+    uint8_t *pv = ws.pp_vis.as<uint8_t>();
+    pp.vis[0] = pv;
+    pv += N;
+    for (int l = 1; l <= 10; ++l) {
+        const size_t sz = (size_t)(W >> l) * (H >> l);
+        pp.img[l] = pi;
+        pp.vis[l] = pv;
+        pi += 3 * sz;
+        pv += sz;
+    }
+    pp.tmp = ws.pp_tmp.as<float>();
+    pp.orig = ws.pp_orig.as<float>();
+    launch_push_pull(W, H, faithful != 0, ws.vis.as<uint8_t>(), ws.U.as<float>(), pp, ctx->stream, ctx->launches);
+    check_launch("push-pull");
+    io.down(U, ws.U.as<float>(), 3 * N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_gradient_visibility(lfrv_ctx *ctx, const lfrv_config *cfg, const float *tau,
+                                              int tau_channels, uint8_t *vis) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    StageInputs si = stage_inputs(ctx, cfg, nullptr, tau, tau_channels, nullptr);
+    const Buckets B = build_buckets(ctx, si.G, si.tau2);
+    ColorBuffers b = color_buffers(ctx, si.G);
+    launch_vis_any(si.G, B, si.tau2, b.vis, ctx->stream, ctx->launches);
+    check_launch("visibility");
+    HostIO io{ctx};
+    io.down(vis, b.vis, si.G.N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_hole_fill(lfrv_ctx *ctx, int W, int H, int max_iter, const uint8_t *vis, float *U,
+                                    int *iterations) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (W <= 0 || H <= 0 || !vis || !U) return fail(LFRV_E_ARG, "bad arguments");
+    const size_t N = (size_t)W * H;
+    HostIO io{ctx};
+    io.up(ctx->ws.U, U, 3 * N);
+    io.up(ctx->ws.vis, vis, N);
+    const int it = hole_fill(ctx, W, H, ctx->ws.vis.as<uint8_t>(), ctx->ws.U.as<float>(), max_iter);
+    if (iterations) *iterations = it;
+    io.down(U, ctx->ws.U.as<float>(), 3 * N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_u_gradient(lfrv_ctx *ctx, const lfrv_config *cfg, const float *views, const float *tau,
+                                     int tau_channels, const float *weights, float *gx, float *gy, float *mask) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    StageInputs si = stage_inputs(ctx, cfg, views, tau, tau_channels, nullptr);
+    const Geometry &G = si.G;
+    const Buckets B = build_buckets(ctx, G, si.tau2);
+    ColorBuffers b = color_buffers(ctx, G);
+    HostIO io{ctx};
+    io.up(ctx->ws.wgt, weights, (size_t)G.V * G.n);
+    ctx->ws.mask.ensure(sizeof(float) * G.N);
+    u_gradient(ctx, G, B, si.img, si.tau2, b.wgt, cfg->sigma_sensor * cfg->sigma_sensor, b.gx, b.gy,
+               ctx->ws.mask.as<float>());
+    io.down(gx, b.gx, G.N);
+    io.down(gy, b.gy, G.N);
+    io.down(mask, ctx->ws.mask.as<float>(), G.N);
+    sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_cg(lfrv_ctx *ctx, int W, int H, int faithful, int max_iter, double gap_tol, const float *gx,
+                             const float *gy, float *U, int *iterations, double *gap) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (W < 2 || H < 2 || !gx || !gy || !U) return fail(LFRV_E_ARG, "bad arguments");
+    const size_t N = (size_t)W * H;
+    HostIO io{ctx};
+    io.up(ctx->ws.gx, gx, N);
+    io.up(ctx->ws.gy, gy, N);
+    io.up(ctx->ws.U, U, 3 * N);
+    const int it = cg_solve(ctx, W, H, faithful != 0, max_iter, gap_tol, ctx->ws.gx.as<float>(),
+                            ctx->ws.gy.as<float>(), ctx->ws.U.as<float>(), gap);
+    if (iterations) *iterations = it;
+    io.down(U, ctx->ws.U.as<float>(), 3 * N);
+    sync(ctx);
+    LFRV_API_END
+}

@@ -1,0 +1,122 @@
+// kernels.h -- host-side declarations of the lfrv kernel launchers (internal to liblfrv).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace lfrv {
+
+struct KernelProfiler;
+
+// Counts kernel launches issued by a context; optionally times them per kernel name.
+struct LaunchCounter {
+    long long n = 0;
+    KernelProfiler *prof = nullptr;
+    void add(int k) { n += k; }
+};
+
+// Records a CUDA event pair on `st` around its scope when the context profiles (no host synchronisation).
+struct ProfScope {
+    ProfScope(LaunchCounter &lc, const char *name, cudaStream_t st);
+    ~ProfScope();
+    KernelProfiler *p;
+    int slot;
+    cudaStream_t st;
+};
+
+// Sizes of one solve: V views of w x h source pixels, target W x H = (dsf w) x (dsf h).
+struct Geometry {
+    int V, w, h, n, W, H, dsf;
+    size_t N;
+};
+
+// Inverse footprint map: source pixels of all views bucketed by footprint anchor.
+struct Buckets {
+    int BW, BH, nb;                     // bucket grid (W + ks - 1) x (H + ks - 1)
+    unsigned int *count, *start;        // nb, nb + 1
+    unsigned int *entries;              // V * n capacity, (view << 24) | pixel
+    unsigned int *block_sums, *block_offsets, *block_sums2, *block_offsets2, *total, *total2;
+};
+
+// ---- warp stage (kernels_warp.cu)
+struct DevCamera {
+    float K[9], R[9], t[3], Kinv[9];
+    // M = K_u R_u R_k^T K_k^-1 for input cameras (filled per view by the host)
+    float M[9];
+    int W, H;
+};
+void launch_zbuffer_clear(int W, int H, unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc);
+void launch_zbuffer_splat(int V, int w, int h, const float *depth, const DevCamera *cams_dev, const DevCamera &target,
+                          unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc);
+void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float *zbuf, cudaStream_t st,
+                            LaunchCounter &lc);
+// tau3/dpart3: reference format (V x 3 x n); tau2/dp2: solver format (V x 2 x n), dp2 premultiplied by sigma_z.
+// Any output may be null.
+void launch_tau(int V, int w, int h, const float *depth, const DevCamera *cams_dev, const DevCamera &target,
+                const float *zbuf, float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st,
+                LaunchCounter &lc);
+
+// ---- solver stage (kernels_solver.cu)
+void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc);
+void launch_residual(const Geometry &G, const float *U, const float *img, const float *tau, const float *wgt, float s2,
+                     float *res, double *partial, cudaStream_t st, LaunchCounter &lc);
+int residual_partials(const Geometry &G);
+void launch_weights(const Geometry &G, const float *gx, const float *gy, const float *tau, const float *dp, float sigma,
+                    float thr, float *wgt, cudaStream_t st, LaunchCounter &lc);
+void launch_coverage(const Geometry &G, const Buckets &B, const float *tau, float *cov, uint8_t *vis, cudaStream_t st,
+                     LaunchCounter &lc);
+void launch_vis_any(const Geometry &G, const Buckets &B, const float *tau, uint8_t *vis, cudaStream_t st,
+                    LaunchCounter &lc);
+void launch_initial_image(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *wgt,
+                          float *U, float *norm, cudaStream_t st, LaunchCounter &lc);
+void launch_dataterm_F(const Geometry &G, const Buckets &B, const float *tau, const float *res, float s2, float alpha,
+                       float fscale, const float *U, float *F, float *G_out, cudaStream_t st, LaunchCounter &lc);
+void launch_regweight(const Geometry &G, const Buckets &B, const float *tau, const float *wgt, const float *norm_prior,
+                      float s2, float lmax, float lmin, float mmax, float *g0, float *norm_out, cudaStream_t st,
+                      LaunchCounter &lc);
+void launch_u_gradient(const Geometry &G, const Buckets &B, const float *tau, const float *vgrad, const float *wgt,
+                       float s2, float *gx, float *gy, float *mask, cudaStream_t st, LaunchCounter &lc);
+void launch_sobel(int W, int H, int count, const float *rgb, size_t in_stride, size_t ch_stride, float *gx, float *gy,
+                  size_t out_stride, const uint8_t *vis, double *abs_partial, cudaStream_t st, LaunchCounter &lc);
+int sobel_partials(int W, int H);
+void launch_rof_iter(int W, int H, float tau, float sigma, float lam, const float *U, const float *P, const float *F,
+                     const float *g, float *Uo, float *Po, cudaStream_t st, LaunchCounter &lc);
+void launch_moving(size_t N, const float *A, const float *B, float thr, double *partial, cudaStream_t st,
+                   LaunchCounter &lc);
+int moving_partials(size_t N);
+void set_gaussian(const float k[11]);
+void launch_blur(int W, int H, const float *in, float *tmp, float *out, cudaStream_t st, LaunchCounter &lc);
+void launch_reduce_final(int count, const double *partial, double *out, cudaStream_t st, LaunchCounter &lc);
+void launch_premultiply_dpart(int V, int n, const float *dpart3, int ch, float *dp, cudaStream_t st, LaunchCounter &lc);
+void launch_copy_tau(int V, int n, const float *tau_in, int ch, float *tau, cudaStream_t st, LaunchCounter &lc);
+
+// ---- push-pull (kernels_pushpull.cu)
+// Pyramid buffers: img levels (3 channels each) and visibility levels, level s of size (W>>s) x (H>>s).
+struct PushPull {
+    float *img[11];
+    uint8_t *vis[11];
+    float *tmp;      // W x (H/2) x 3 scratch for the separable reduce/expand
+    float *orig;     // 3 x N copy of the input (faithful "filled - U")
+};
+void launch_push_pull(int W, int H, bool faithful, const uint8_t *vis, float *U, PushPull &pp, cudaStream_t st,
+                      LaunchCounter &lc);
+
+// ---- IBR_gradient: hole filling and CG (kernels_cg.cu)
+void launch_hole_fill_iter(int W, int H, const int *holes, int nholes, const float *Uin, float *Uout,
+                           double *partial, cudaStream_t st, LaunchCounter &lc);
+int hole_fill_partials(int nholes);
+void launch_hole_list(int W, int H, const uint8_t *vis, int *holes, int *count, cudaStream_t st, LaunchCounter &lc);
+void launch_cg_init(int W, int H, const float *U, const float *gx, const float *gy, float *r, float *d, bool faithful,
+                    double *partial, cudaStream_t st, LaunchCounter &lc);
+void launch_cg_apply(int W, int H, const float *d, float lambda, float *q, double *partial, cudaStream_t st,
+                     LaunchCounter &lc);
+void launch_cg_update(int W, int H, const float alpha[3], const float *d, const float *q, float *U, float *r,
+                      double *partial, cudaStream_t st, LaunchCounter &lc);
+void launch_cg_dir(int W, int H, const float beta[3], const float *r, float *d, cudaStream_t st, LaunchCounter &lc);
+void launch_reduce_segments(int count, int nseg, const double *partial, double *out, cudaStream_t st, LaunchCounter &lc);
+int cg_partials(int W, int H);
+void launch_cg_energy(int W, int H, const float *U, const float *U0, const float *gx, const float *gy, double *partial,
+                      cudaStream_t st, LaunchCounter &lc);
+
+}  // namespace lfrv

@@ -1,0 +1,714 @@
+// kernels_solver.cu -- solver-stage kernels of the IBR_color / IBR_gradient path (sm_103a).
+//
+// Layout in HBM (all planar float32, row-major, top-left origin):
+//   per view v (V views, n = w*h source pixels): img[v][3][n], tau[v][2][n] (tau_x, tau_y),
+//     dp[v][2][n] (sigma_z * dtau/dz), wgt[v][n] (omega_i), res[v][3][n] (weighted residual scratch)
+//   target (N = W*H pixels): U[3][N], P[6][N] duals (px0,py0,px1,py1,px2,py2), F[3][N], g[N], masks.
+//
+// The reference splats A_i^T r with one launch per host-computed non-overlapping cell segment
+// (sources/optimization.cu:882-1025, 1921-1951). Here the scatter becomes a deterministic gather: source
+// pixels of all views are bucketed by the anchor of their footprint (counting sort, buckets sorted by
+// (view, pixel)), and every target pixel reads the ks x ks anchor buckets that can reach it, recomputing
+// the footprint weights from tau instead of storing A (the reference stores ks^2 floats per source pixel).
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace lfrv {
+
+// ====================================================================== inverse footprint map
+__global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
+                               unsigned int *__restrict__ cnt) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    if (m >= n) return;
+    const float tx = tau[(size_t)v * 2 * n + m], ty = tau[(size_t)v * 2 * n + n + m];
+    if (!in_splat(tx, ty, W, H)) return;
+    const int ks = dsf + 1;
+    const int x0 = fp_anchor(tx - 0.5f, dsf), y0 = fp_anchor(ty - 0.5f, dsf);
+    atomicAdd(&cnt[(size_t)(y0 + ks - 1) * BW + (x0 + ks - 1)], 1u);
+}
+
+__global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
+                              const unsigned int *__restrict__ start, unsigned int *__restrict__ cursor,
+                              unsigned int *__restrict__ entries) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    if (m >= n) return;
+    const float tx = tau[(size_t)v * 2 * n + m], ty = tau[(size_t)v * 2 * n + n + m];
+    if (!in_splat(tx, ty, W, H)) return;
+    const int ks = dsf + 1;
+    const int x0 = fp_anchor(tx - 0.5f, dsf), y0 = fp_anchor(ty - 0.5f, dsf);
+    const size_t b = (size_t)(y0 + ks - 1) * BW + (x0 + ks - 1);
+    const unsigned int slot = start[b] + atomicAdd(&cursor[b], 1u);
+    entries[slot] = ((unsigned int)v << 24) | (unsigned int)m;
+}
+
+// Orders each bucket by (view, pixel) so the gathers sum in a fixed order.
+__global__ void k_bucket_sort(int nb, const unsigned int *__restrict__ start, unsigned int *__restrict__ entries) {
+    const int b = blockIdx.x * blockDim.x + threadIdx.x;
+    if (b >= nb) return;
+    const unsigned int s = start[b], e = start[b + 1];
+    for (unsigned int i = s + 1; i < e; ++i) {
+        const unsigned int key = entries[i];
+        unsigned int j = i;
+        while (j > s && entries[j - 1] > key) {
+            entries[j] = entries[j - 1];
+            --j;
+        }
+        entries[j] = key;
+    }
+}
+
+// Exclusive scan of unsigned counts (three-phase: block scans, scan of block sums, add back).
+constexpr int kScanBlock = 1024;
+
+__global__ void k_scan_blocks(int nb, const unsigned int *__restrict__ in, unsigned int *__restrict__ out,
+                              unsigned int *__restrict__ block_sums) {
+    __shared__ unsigned int s[kScanBlock];
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    const unsigned int v = (i < nb) ? in[i] : 0u;
+    s[threadIdx.x] = v;
+    __syncthreads();
+    for (int off = 1; off < kScanBlock; off <<= 1) {
+        const unsigned int t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0u;
+        __syncthreads();
+        s[threadIdx.x] += t;
+        __syncthreads();
+    }
+    if (i < nb) out[i] = s[threadIdx.x] - v;  // exclusive
+    if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = s[threadIdx.x];
+}
+
+__global__ void k_scan_add(int nb, unsigned int *__restrict__ out, const unsigned int *__restrict__ block_offsets,
+                           const unsigned int *__restrict__ block_sums_total, unsigned int *__restrict__ out_last) {
+    const int i = blockIdx.x * kScanBlock + threadIdx.x;
+    if (i < nb) out[i] += block_offsets[blockIdx.x];
+    if (i == 0) *out_last = *block_sums_total;
+}
+
+// ====================================================================== per-source gathers (v = A u)
+// Weighted residual e = w * (A_i U - v_i) over the gather set, and the intensity energy
+// sum sigma^2 w (A_i U - v_i)^2 (vtv_sr_dataterm_intensities sources/optimization.cu:1871-1903 and
+// coco_vtv_sr_primal_energy_unstructured :1560-1608). Outside the gather set A_i U = 0.
+template <int KS>
+__global__ void __launch_bounds__(256) k_residual(int V, int n, int W, int H, int dsf, const float *__restrict__ U,
+                                                  const float *__restrict__ img, const float *__restrict__ tau,
+                                                  const float *__restrict__ wgt, float s2,
+                                                  float *__restrict__ res, double *__restrict__ partial) {
+    __shared__ double red[8];
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    const size_t N = (size_t)W * H;
+    double e = 0.0;
+    if (m < n) {
+        const float tx = tau[(size_t)v * 2 * n + m], ty = tau[(size_t)v * 2 * n + n + m];
+        float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+        if (in_gather(tx, ty, W, H)) {
+            Footprint fp;
+            footprint<KS>(tx, ty, dsf, W, H, fp);
+#pragma unroll
+            for (int j = 0; j < KS; ++j)
+#pragma unroll
+                for (int i = 0; i < KS; ++i) {
+                    const int x = fp.x0 + j, y = fp.y0 + i;
+                    if (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1) {
+                        const float A = fp.A[KS * i + j];
+                        const size_t o = (size_t)y * W + x;
+                        a0 += A * __ldg(U + o);
+                        a1 += A * __ldg(U + N + o);
+                        a2 += A * __ldg(U + 2 * N + o);
+                    }
+                }
+        }
+        const float *iv = img + (size_t)v * 3 * n;
+        const float w = wgt[(size_t)v * n + m];
+        const float d0 = a0 - iv[m], d1 = a1 - iv[n + m], d2 = a2 - iv[2 * n + m];
+        float *rv = res + (size_t)v * 3 * n;
+        rv[m] = d0 * w;
+        rv[n + m] = d1 * w;
+        rv[2 * n + m] = d2 * w;
+        e = (double)s2 * (double)w * ((double)d0 * d0 + (double)d1 * d1 + (double)d2 * d2);
+    }
+    const double s = block_sum<256>(e, red);
+    if (threadIdx.x == 0) partial[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = s;
+}
+
+// Angular and deformation weights of every source pixel (coco_vtv_sr_compute_weights_unstructured,
+// sources/optimization.cu:1094-1163; vtv_sr_angular_weights_device and vtv_sr_gold_deform_weights_device,
+// vtv_sr_kernels_unstructured.cu:174-266): w = 1/(sg^2 + sigma^2) * deform with sg = clamp(A_i grad) . dpart.
+template <int KS>
+__global__ void __launch_bounds__(256) k_weights(int V, int n, int w, int h, int W, int H, int dsf,
+                                                 const float *__restrict__ gx, const float *__restrict__ gy,
+                                                 const float *__restrict__ tau, const float *__restrict__ dp,
+                                                 float sigma, float thr, float *__restrict__ wgt) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    if (m >= n) return;
+    const float *tx = tau + (size_t)v * 2 * n, *ty = tx + n;
+    const float txm = tx[m], tym = ty[m];
+    float ax = 0.f, ay = 0.f;
+    if (in_gather(txm, tym, W, H)) {
+        Footprint fp;
+        footprint<KS>(txm, tym, dsf, W, H, fp);
+#pragma unroll
+        for (int j = 0; j < KS; ++j)
+#pragma unroll
+            for (int i = 0; i < KS; ++i) {
+                const int x = fp.x0 + j, y = fp.y0 + i;
+                if (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1) {
+                    const float A = fp.A[KS * i + j];
+                    const size_t o = (size_t)y * W + x;
+                    ax += A * __ldg(gx + o);
+                    ay += A * __ldg(gy + o);
+                }
+            }
+    }
+    // angular weight
+    const float norm = sqrtf(ax * ax + ay * ay);
+    if (norm > thr) {
+        ax = ax / norm * thr;
+        ay = ay / norm * thr;
+    }
+    float sg = ax * dp[(size_t)v * 2 * n + m] + ay * dp[(size_t)v * 2 * n + n + m];
+    if (sg > 0.5f) sg = 0.5f;
+    const float ang = 1.0f / (sg * sg + sigma * sigma);
+    // deformation weight
+    const int mx = m % w, my = m / w;
+    auto out = [&](int k) { return tx[k] < 0.f || tx[k] > (float)W || ty[k] < 0.f || ty[k] > (float)H; };
+    float def;
+    if (out(m)) def = 0.0f;
+    else if (mx == 0 || my == 0 || mx == w - 1 || my == h - 1) def = 1.0f;
+    else if (out(m - 1) || out(m + 1) || out(m - w) || out(m + w)) def = 1.0f;
+    else {
+        const float Dxx = 0.5f * (tx[m + 1] - tx[m - 1]);
+        const float Dyx = 0.5f * (ty[m + 1] - ty[m - 1]);
+        const float Dxy = 0.5f * (tx[m + w] - tx[m - w]);
+        const float Dyy = 0.5f * (ty[m + w] - ty[m - w]);
+        const float N = fabsf(Dxx * Dyy - Dxy * Dyx);
+        def = (N > 1.0f) ? 1.0f / N : 1.0f;
+    }
+    wgt[(size_t)v * n + m] = ang * def;
+}
+
+// ====================================================================== A^T gathers (per target pixel)
+struct SplatSrc {
+    const float *ch[3];   // payload channel c of view v at ch[c] + v * stride[c]
+    size_t stride[3];
+    const float *scale;   // optional per-source factor (weights), stride n per view
+};
+
+// Accumulates sum_entries A * payload and sum_entries A (times the optional scale) for target (x, y).
+template <int KS, int NCH>
+__device__ __forceinline__ void splat_accumulate(int x, int y, int W, int H, int n, int dsf, int BW,
+                                                 const unsigned int *__restrict__ start,
+                                                 const unsigned int *__restrict__ entries,
+                                                 const float *__restrict__ tau, const SplatSrc &src, float acc[3],
+                                                 float &norm) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[c] = 0.f;
+    norm = 0.f;
+#pragma unroll
+    for (int i = 0; i < KS; ++i) {
+#pragma unroll
+        for (int j = 0; j < KS; ++j) {
+            const int ax = x - j, ay = y - i;  // anchor whose tap (j, i) lands on (x, y)
+            const size_t b = (size_t)(ay + KS - 1) * BW + (ax + KS - 1);
+            const unsigned int s = __ldg(start + b), e = __ldg(start + b + 1);
+            for (unsigned int k = s; k < e; ++k) {
+                const unsigned int ent = __ldg(entries + k);
+                const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
+                const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
+                float A = footprint_tap<KS>(tx, ty, dsf, W, H, j, i);
+                if (src.scale) A = __ldg(src.scale + (size_t)v * n + m) * A;
+                norm += A;
+#pragma unroll
+                for (int c = 0; c < NCH; ++c) acc[c] += A * __ldg(src.ch[c] + (size_t)v * src.stride[c] + m);
+            }
+        }
+    }
+}
+
+// Coverage and visibility (coco_vtv_setup_visibility_mask sources/optimization.cu:33-135):
+// cov = sum A, vis = cov >= 1.
+template <int KS>
+__global__ void k_coverage(int W, int H, int n, int dsf, int BW, const unsigned int *__restrict__ start,
+                           const unsigned int *__restrict__ entries, const float *__restrict__ tau,
+                           float *__restrict__ cov, uint8_t *__restrict__ vis) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    SplatSrc src{{nullptr, nullptr, nullptr}, {0, 0, 0}, nullptr};
+    float acc[3], norm;
+    splat_accumulate<KS, 0>(x, y, W, H, n, dsf, BW, start, entries, tau, src, acc, norm);
+    const size_t o = (size_t)y * W + x;
+    cov[o] = norm;
+    vis[o] = (norm < 1.0f) ? 0 : 1;
+}
+
+// Visibility of IBR_gradient (setup_target_visibility, sources/gradientIBR.cu:40-83): some splatted tap
+// with a non-zero raw overlap.
+template <int KS>
+__global__ void k_vis_any(int W, int H, int n, int dsf, int BW, const unsigned int *__restrict__ start,
+                          const unsigned int *__restrict__ entries, const float *__restrict__ tau,
+                          uint8_t *__restrict__ vis) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    bool any = false;
+#pragma unroll
+    for (int i = 0; i < KS; ++i)
+#pragma unroll
+        for (int j = 0; j < KS; ++j) {
+            const int ax = x - j, ay = y - i;
+            const size_t b = (size_t)(ay + KS - 1) * BW + (ax + KS - 1);
+            const unsigned int s = start[b], e = start[b + 1];
+            for (unsigned int k = s; k < e && !any; ++k) {
+                const unsigned int ent = entries[k];
+                const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
+                const float tx = tau[(size_t)v * 2 * n + m], ty = tau[(size_t)v * 2 * n + n + m];
+                if (footprint_raw<KS>(tx, ty, dsf, j, i, ax, ay) != 0.0f) any = true;
+            }
+        }
+    vis[(size_t)y * W + x] = any ? 1 : 0;
+}
+
+// Weighted average (coco_vtv_sr_compute_initial_image sources/optimization.cu:1300-1344):
+// U = sum w A v / sum w A where the weight sum is non-zero.
+template <int KS>
+__global__ void k_initial_image(int W, int H, int n, int dsf, int BW, const unsigned int *__restrict__ start,
+                                const unsigned int *__restrict__ entries, const float *__restrict__ tau,
+                                SplatSrc src, float *__restrict__ U, float *__restrict__ norm_out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    float acc[3], norm;
+    splat_accumulate<KS, 3>(x, y, W, H, n, dsf, BW, start, entries, tau, src, acc, norm);
+    const size_t o = (size_t)y * W + x, N = (size_t)W * H;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) U[c * N + o] = (norm != 0.f) ? acc[c] / norm : acc[c];
+    if (norm_out) norm_out[o] = norm;
+}
+
+// Data-term gradient and the proximal data F (vtv_sr_dataterm_intensities :1953-1963 and
+// vtv_sr_ista_step_unstructured :1785-1812): G = alpha sigma^2 sum A e / sum A, F = clamp(U + fs clamp(G)).
+template <int KS>
+__global__ void k_dataterm_F(int W, int H, int n, int dsf, int BW, const unsigned int *__restrict__ start,
+                             const unsigned int *__restrict__ entries, const float *__restrict__ tau, SplatSrc src,
+                             float s2, float alpha, float fscale, const float *__restrict__ U,
+                             float *__restrict__ F, float *__restrict__ G_out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    float acc[3], norm;
+    splat_accumulate<KS, 3>(x, y, W, H, n, dsf, BW, start, entries, tau, src, acc, norm);
+    const size_t o = (size_t)y * W + x, N = (size_t)W * H;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float gi = (norm != 0.f) ? acc[c] / norm : acc[c];
+        gi *= s2;
+        float G = 0.f + alpha * gi;
+        if (G_out) G_out[c * N + o] = G;
+        G = fminf(1.0f, fmaxf(-1.0f, G));
+        G *= fscale;
+        G += U[c * N + o];
+        F[c * N + o] = fminf(1.0f, fmaxf(0.0f, G));
+    }
+}
+
+// Regulariser weight before the blur (coco_vtv_sr_init_regularizer_weight_unstructured
+// sources/optimization.cu:2262-2319, vtv_sr_init_regularizer_weight_device vtv_sr_kernels.cu:1172-1195).
+// norm_prior is the coverage accumulator's content before the call (never cleared upstream).
+template <int KS>
+__global__ void k_regweight(int W, int H, int n, int dsf, int BW, const unsigned int *__restrict__ start,
+                            const unsigned int *__restrict__ entries, const float *__restrict__ tau, SplatSrc src,
+                            const float *__restrict__ norm_prior, float s2, float lmax, float lmin, float mmax,
+                            float *__restrict__ g0, float *__restrict__ norm_out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    float acc[3], norm;
+    splat_accumulate<KS, 1>(x, y, W, H, n, dsf, BW, start, entries, tau, src, acc, norm);
+    const size_t o = (size_t)y * W + x;
+    const float nm = (norm_prior ? norm_prior[o] : 0.f) + norm;
+    float m = (nm != 0.f) ? acc[0] / nm : acc[0];
+    m *= s2;
+    g0[o] = (m == 0.0f) ? lmax : fmaxf(lmin, lmax - m / mmax);
+    if (norm_out) norm_out[o] = nm;
+}
+
+// Gradient splatting of IBR_gradient (init_u_gradient sources/gradientIBR.cu:856-916): payload
+// (Sobel_x, Sobel_y, weight) of every source pixel, normalised by the coverage; mask scaled by sigma^2.
+template <int KS>
+__global__ void k_u_gradient(int W, int H, int n, int dsf, int BW, const unsigned int *__restrict__ start,
+                             const unsigned int *__restrict__ entries, const float *__restrict__ tau, SplatSrc src,
+                             float s2, float *__restrict__ gx, float *__restrict__ gy, float *__restrict__ mask) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    float acc[3], norm;
+    splat_accumulate<KS, 3>(x, y, W, H, n, dsf, BW, start, entries, tau, src, acc, norm);
+    const size_t o = (size_t)y * W + x;
+    if (norm != 0.f) {
+        acc[0] /= norm;
+        acc[1] /= norm;
+        acc[2] /= norm;
+    }
+    gx[o] = acc[0];
+    gy[o] = acc[1];
+    mask[o] = acc[2] * s2;
+}
+
+// ====================================================================== stencils on the target
+// Sobel of the luminance (vtv_sr_compute_gradient_device, vtv_sr_kernels_unstructured.cu:96-148); with a
+// mask, interior pixels without a fully visible 3x3 neighbourhood keep the old content of gx/gy.
+// Also used on source views (sources/gradientIBR_kernels.cuh:57-100, no mask); views are addressed with a
+// per-blockIdx.z plane stride.
+__global__ void k_sobel(int W, int H, const float *__restrict__ rgb, size_t in_stride, size_t ch_stride,
+                        float *__restrict__ gx, float *__restrict__ gy, size_t out_stride,
+                        const uint8_t *__restrict__ vis, double *__restrict__ abs_partial) {
+    __shared__ double red[8];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    const float *r = rgb + (size_t)z * in_stride, *g = r + ch_stride, *b = g + ch_stride;
+    float *ox = gx + (size_t)z * out_stride, *oy = gy + (size_t)z * out_stride;
+    double a = 0.0;
+    if (x < W && y < H) {
+        const size_t o = (size_t)y * W + x;
+        float gX = 0.f, gY = 0.f;
+        bool write = true;
+        if (0 < x && x < W - 1 && 0 < y && y < H - 1) {
+            if (vis) {
+                for (int dy = -1; dy <= 1 && write; ++dy)
+                    for (int dx = -1; dx <= 1; ++dx)
+                        if (!vis[o + (ptrdiff_t)dy * W + dx]) {
+                            write = false;
+                            break;
+                        }
+            }
+            if (write) {
+                auto L = [&](int dx, int dy) {
+                    const size_t q = o + (ptrdiff_t)dy * W + dx;
+                    return lum(r[q], g[q], b[q]);
+                };
+                const float Ypp = L(-1, -1), Ypc = L(0, -1), Ypn = L(1, -1);
+                const float Ycp = L(-1, 0), Ycn = L(1, 0);
+                const float Ynp = L(-1, 1), Ync = L(0, 1), Ynn = L(1, 1);
+                gX = (Ypn + 2.f * Ycn + Ynn - Ypp - 2.f * Ycp - Ynp) / 8.f;
+                gY = (Ynp + 2.f * Ync + Ynn - Ypp - 2.f * Ypc - Ypn) / 8.f;
+            }
+        }
+        if (write) {
+            ox[o] = gX;
+            oy[o] = gY;
+        }
+        if (abs_partial) a = fabs((double)ox[o]) + fabs((double)oy[o]);
+    }
+    if (abs_partial) {
+        // block of 32x8 threads
+        const int tid = threadIdx.y * blockDim.x + threadIdx.x;
+        double v = a;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+        if ((tid & 31) == 0) red[tid >> 5] = v;
+        __syncthreads();
+        if (tid == 0) {
+            double s = 0;
+            for (int i = 0; i < (int)(blockDim.x * blockDim.y) / 32; ++i) s += red[i];
+            abs_partial[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = s;
+        }
+    }
+}
+
+// One inner ROF iteration (dual step vtv_rof.cu:118-147, TV_F reprojection onto the ball of radius g
+// vtv_rof.cu:280-320, primal prox cuda_kernels.cu:504-532) fused: the duals of the pixel and of its left
+// and upper neighbours are recomputed from the previous iterate so one launch reads (U, P, F, g) and
+// writes (U', P'). Ping-pong buffers keep the Jacobi semantics of the reference's separate launches.
+__device__ __forceinline__ void rof_dual(int x, int y, int W, int H, size_t N, float sigma,
+                                         const float *__restrict__ U, const float *__restrict__ P,
+                                         const float *__restrict__ g, float p[6]) {
+    const size_t o = (size_t)y * W + x;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float u = __ldg(U + c * N + o);
+        const float gxv = (x < W - 1) ? __ldg(U + c * N + o + 1) - u : 0.f;
+        const float gyv = (y < H - 1) ? __ldg(U + c * N + o + W) - u : 0.f;
+        p[2 * c] = __ldg(P + (2 * c) * N + o) + sigma * gxv;
+        p[2 * c + 1] = __ldg(P + (2 * c + 1) * N + o) + sigma * gyv;
+    }
+    float nn = 0.f;
+    nn += p[0] * p[0] + p[2] * p[2] + p[4] * p[4];
+    nn += p[1] * p[1] + p[3] * p[3] + p[5] * p[5];
+    nn = sqrtf(nn);
+    const float r = __ldg(g + o);
+    if (nn > r) {
+        const float s = r / nn;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) p[k] *= s;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_rof_iter(int W, int H, float tau, float sigma, float lam,
+                                                  const float *__restrict__ U, const float *__restrict__ P,
+                                                  const float *__restrict__ F, const float *__restrict__ g,
+                                                  float *__restrict__ Uo, float *__restrict__ Po) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t N = (size_t)W * H, o = (size_t)y * W + x;
+    float p[6], pl[6], pt[6];
+    rof_dual(x, y, W, H, N, sigma, U, P, g, p);
+    if (x > 0) rof_dual(x - 1, y, W, H, N, sigma, U, P, g, pl);
+    if (y > 0) rof_dual(x, y - 1, W, H, N, sigma, U, P, g, pt);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) Po[k * N + o] = p[k];
+    const float denom = tau + lam;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float step = p[2 * c] + p[2 * c + 1];
+        if (x > 0) step -= pl[2 * c];
+        if (y > 0) step -= pt[2 * c + 1];
+        const float unew = __ldg(U + c * N + o) + tau * step;
+        Uo[c * N + o] = (tau * __ldg(F + c * N + o) + lam * unew) / denom;
+    }
+}
+
+// Count of pixels whose largest channel change reaches thr (sr_compare_images,
+// sources/super-resolution.cpp:16-51).
+__global__ void k_moving(size_t N, const float *__restrict__ A, const float *__restrict__ B, float thr,
+                         double *__restrict__ partial) {
+    __shared__ double red[8];
+    const size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    double c = 0.0;
+    if (o < N) {
+        float mx = 0.f;
+#pragma unroll
+        for (int ch = 0; ch < 3; ++ch) mx = fmaxf(mx, fabsf(A[ch * N + o] - B[ch * N + o]));
+        c = (mx < thr) ? 0.0 : 1.0;
+    }
+    const double s = block_sum<256>(c, red);
+    if (threadIdx.x == 0) partial[blockIdx.x] = s;
+}
+
+// Separable 11-tap Gaussian with clamp-to-edge (convolutionRowGPU / convolutionColumnGPU,
+// cocolib/cocolib/cuda/cuda_convolutions.cu:110-238; kernel from gsl_kernel_gauss_1xn(11, 2.0)).
+__constant__ float c_gauss[11];
+
+__global__ void k_blur_rows(int W, int H, const float *__restrict__ in, float *__restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    float s = 0.f;
+#pragma unroll
+    for (int k = -5; k <= 5; ++k) {
+        const int xx = min(max(x + k, 0), W - 1);
+        s += in[(size_t)y * W + xx] * c_gauss[5 - k];
+    }
+    out[(size_t)y * W + x] = s;
+}
+
+__global__ void k_blur_cols(int W, int H, const float *__restrict__ in, float *__restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    float s = 0.f;
+#pragma unroll
+    for (int k = -5; k <= 5; ++k) {
+        const int yy = min(max(y + k, 0), H - 1);
+        s += in[(size_t)yy * W + x] * c_gauss[5 - k];
+    }
+    out[(size_t)y * W + x] = s;
+}
+
+// Deterministic final reduction of FP64 partials (single block).
+__global__ void k_reduce_final(int count, const double *__restrict__ partial, double *__restrict__ out) {
+    __shared__ double red[32];
+    double s = 0.0;
+    for (int i = threadIdx.x; i < count; i += blockDim.x) s += partial[i];
+    const double t = block_sum<1024>(s, red);
+    if (threadIdx.x == 0) *out = t;
+}
+
+// Elementwise helpers.
+__global__ void k_fill_u8(size_t n, uint8_t *p, uint8_t v) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) p[i] = v;
+}
+
+__global__ void k_premultiply_dpart(int V, int n, const float *__restrict__ dpart3, int dpart_channels,
+                                    float *__restrict__ dp) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    if (m >= n) return;
+    const float *src = dpart3 + (size_t)v * dpart_channels * n;
+    const float sz = src[m];
+    dp[(size_t)v * 2 * n + m] = src[n + m] * sz;
+    dp[(size_t)v * 2 * n + n + m] = src[2 * n + m] * sz;
+}
+
+__global__ void k_copy_tau(int V, int n, const float *__restrict__ tau_in, int tau_channels,
+                           float *__restrict__ tau) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    if (m >= n) return;
+    const float *src = tau_in + (size_t)v * tau_channels * n;
+    tau[(size_t)v * 2 * n + m] = src[m];
+    tau[(size_t)v * 2 * n + n + m] = src[n + m];
+}
+
+// ====================================================================== host launchers
+static inline dim3 grid2(int W, int H, dim3 b) { return dim3((W + b.x - 1) / b.x, (H + b.y - 1) / b.y); }
+
+#define LFRV_KS_DISPATCH(ks, KERNEL, GRID, BLOCK, STREAM, ...)                          \
+    switch (ks) {                                                                       \
+        case 2: KERNEL<2><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
+        case 3: KERNEL<3><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
+        case 4: KERNEL<4><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
+        case 5: KERNEL<5><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
+        default: break;                                                                 \
+    }
+
+void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "bucket_build", st);
+    const int ks = G.dsf + 1;
+    const dim3 b1(256), gs((G.n + 255) / 256, G.V);
+    cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
+    k_bucket_count<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.count);
+    lc.add(1);
+    const int nblk = (B.nb + kScanBlock - 1) / kScanBlock;
+    k_scan_blocks<<<nblk, kScanBlock, 0, st>>>(B.nb, B.count, B.start, B.block_sums);
+    lc.add(1);
+    // scan of block sums (nblk <= kScanBlock^2 covers 2^20 * 1024 buckets)
+    const int nblk2 = (nblk + kScanBlock - 1) / kScanBlock;
+    k_scan_blocks<<<nblk2, kScanBlock, 0, st>>>(nblk, B.block_sums, B.block_offsets, B.block_sums2);
+    lc.add(1);
+    if (nblk2 > 1) {
+        // third level: at most kScanBlock entries
+        k_scan_blocks<<<1, kScanBlock, 0, st>>>(nblk2, B.block_sums2, B.block_offsets2, B.total2);
+        k_scan_add<<<nblk2, kScanBlock, 0, st>>>(nblk, B.block_offsets, B.block_offsets2, B.total2, B.total);
+        lc.add(2);
+    } else {
+        cudaMemcpyAsync(B.total, B.block_sums2, sizeof(unsigned int), cudaMemcpyDeviceToDevice, st);
+    }
+    k_scan_add<<<nblk, kScanBlock, 0, st>>>(B.nb, B.start, B.block_offsets, B.total, B.start + B.nb);
+    lc.add(1);
+    cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
+    k_bucket_fill<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.start, B.count, B.entries);
+    k_bucket_sort<<<(B.nb + 255) / 256, 256, 0, st>>>(B.nb, B.start, B.entries);
+    lc.add(2);
+    (void)ks;
+}
+
+void launch_residual(const Geometry &G, const float *U, const float *img, const float *tau, const float *wgt, float s2,
+                     float *res, double *partial, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "residual", st);
+    const dim3 b(256), g((G.n + 255) / 256, G.V);
+    LFRV_KS_DISPATCH(G.dsf + 1, k_residual, g, b, st, G.V, G.n, G.W, G.H, G.dsf, U, img, tau, wgt, s2, res, partial);
+    lc.add(1);
+}
+int residual_partials(const Geometry &G) { return ((G.n + 255) / 256) * G.V; }
+
+void launch_weights(const Geometry &G, const float *gx, const float *gy, const float *tau, const float *dp, float sigma,
+                    float thr, float *wgt, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "weights", st);
+    const dim3 b(256), g((G.n + 255) / 256, G.V);
+    LFRV_KS_DISPATCH(G.dsf + 1, k_weights, g, b, st, G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr,
+                     wgt);
+    lc.add(1);
+}
+
+static const dim3 kTile(32, 8);
+
+void launch_coverage(const Geometry &G, const Buckets &B, const float *tau, float *cov, uint8_t *vis, cudaStream_t st,
+                     LaunchCounter &lc) {
+    LFRV_KS_DISPATCH(G.dsf + 1, k_coverage, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW, B.start,
+                     B.entries, tau, cov, vis);
+    lc.add(1);
+}
+
+void launch_vis_any(const Geometry &G, const Buckets &B, const float *tau, uint8_t *vis, cudaStream_t st,
+                    LaunchCounter &lc) {
+    LFRV_KS_DISPATCH(G.dsf + 1, k_vis_any, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW, B.start,
+                     B.entries, tau, vis);
+    lc.add(1);
+}
+
+void launch_initial_image(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *wgt,
+                          float *U, float *norm, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "initial_image", st);
+    const size_t s3 = (size_t)3 * G.n;
+    SplatSrc src{{img, img + G.n, img + 2 * (size_t)G.n}, {s3, s3, s3}, wgt};
+    LFRV_KS_DISPATCH(G.dsf + 1, k_initial_image, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW,
+                     B.start, B.entries, tau, src, U, norm);
+    lc.add(1);
+}
+
+void launch_dataterm_F(const Geometry &G, const Buckets &B, const float *tau, const float *res, float s2, float alpha,
+                       float fscale, const float *U, float *F, float *G_out, cudaStream_t st, LaunchCounter &lc) {
+    const size_t s3 = (size_t)3 * G.n;
+    SplatSrc src{{res, res + G.n, res + 2 * (size_t)G.n}, {s3, s3, s3}, nullptr};
+    LFRV_KS_DISPATCH(G.dsf + 1, k_dataterm_F, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW, B.start,
+                     B.entries, tau, src, s2, alpha, fscale, U, F, G_out);
+    lc.add(1);
+}
+
+void launch_regweight(const Geometry &G, const Buckets &B, const float *tau, const float *wgt, const float *norm_prior,
+                      float s2, float lmax, float lmin, float mmax, float *g0, float *norm_out, cudaStream_t st,
+                      LaunchCounter &lc) {
+    SplatSrc src{{wgt, nullptr, nullptr}, {(size_t)G.n, 0, 0}, nullptr};
+    LFRV_KS_DISPATCH(G.dsf + 1, k_regweight, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW, B.start,
+                     B.entries, tau, src, norm_prior, s2, lmax, lmin, mmax, g0, norm_out);
+    lc.add(1);
+}
+
+void launch_u_gradient(const Geometry &G, const Buckets &B, const float *tau, const float *vgrad, const float *wgt,
+                       float s2, float *gx, float *gy, float *mask, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "u_gradient", st);
+    // vgrad: per view [2][n] (Sobel x, Sobel y); weights [V][n]
+    SplatSrc src{{vgrad, vgrad + G.n, wgt}, {(size_t)2 * G.n, (size_t)2 * G.n, (size_t)G.n}, nullptr};
+    LFRV_KS_DISPATCH(G.dsf + 1, k_u_gradient, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW, B.start,
+                     B.entries, tau, src, s2, gx, gy, mask);
+    lc.add(1);
+}
+
+void launch_sobel(int W, int H, int count, const float *rgb, size_t in_stride, size_t ch_stride, float *gx, float *gy,
+                  size_t out_stride, const uint8_t *vis, double *abs_partial, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "sobel", st);
+    const dim3 b(32, 8), g((W + 31) / 32, (H + 7) / 8, count);
+    k_sobel<<<g, b, 0, st>>>(W, H, rgb, in_stride, ch_stride, gx, gy, out_stride, vis, abs_partial);
+    lc.add(1);
+}
+int sobel_partials(int W, int H) { return ((W + 31) / 32) * ((H + 7) / 8); }
+
+void launch_rof_iter(int W, int H, float tau, float sigma, float lam, const float *U, const float *P, const float *F,
+                     const float *g, float *Uo, float *Po, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "rof_iter", st);
+    k_rof_iter<<<grid2(W, H, kTile), kTile, 0, st>>>(W, H, tau, sigma, lam, U, P, F, g, Uo, Po);
+    lc.add(1);
+}
+
+void launch_moving(size_t N, const float *A, const float *B, float thr, double *partial, cudaStream_t st,
+                   LaunchCounter &lc) {
+    k_moving<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, A, B, thr, partial);
+    lc.add(1);
+}
+int moving_partials(size_t N) { return (int)((N + 255) / 256); }
+
+void set_gaussian(const float k[11]) { cudaMemcpyToSymbol(c_gauss, k, sizeof(float) * 11); }
+
+void launch_blur(int W, int H, const float *in, float *tmp, float *out, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "blur", st);
+    k_blur_rows<<<grid2(W, H, kTile), kTile, 0, st>>>(W, H, in, tmp);
+    k_blur_cols<<<grid2(W, H, kTile), kTile, 0, st>>>(W, H, tmp, out);
+    lc.add(2);
+}
+
+void launch_reduce_final(int count, const double *partial, double *out, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "reduce_final", st);
+    k_reduce_final<<<1, 1024, 0, st>>>(count, partial, out);
+    lc.add(1);
+}
+
+void launch_premultiply_dpart(int V, int n, const float *dpart3, int ch, float *dp, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "premultiply_dpart", st);
+    k_premultiply_dpart<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, n, dpart3, ch, dp);
+    lc.add(1);
+}
+
+void launch_copy_tau(int V, int n, const float *tau_in, int ch, float *tau, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "copy_tau", st);
+    k_copy_tau<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, n, tau_in, ch, tau);
+    lc.add(1);
+}
+
+}  // namespace lfrv

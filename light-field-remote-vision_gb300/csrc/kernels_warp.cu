@@ -1,0 +1,234 @@
+// kernels_warp.cu -- warp stage: target depth map, tau warps, dtau/dz (sm_103a).
+//
+// Restates the GL pipeline of the reference's warp exporter as CUDA kernels writing device buffers:
+//   target depth map: Scene::computeTargetDepthMap (sources/openGL/scene.cpp:1506-1544) drawing
+//     depthSplatting.{vert,geom,frag}: each input pixel becomes a tilted quad, rasterised into the target
+//     with a depth test; the colour written is the quad centre's target depth;
+//   tau: tauWarp.frag:25-74 (projection, deformation weight capped at 30, visibility codes -2 / -1 with a
+//     0.10 depth tolerance against the bilinearly sampled target depth map);
+//   dtau/dz: tauPartial.frag:23-48 (sigma_z = 10 in channel 0).
+// Per input view the host folds the cameras into M = K_u R_u R_k^T K_k^-1 and b = K_u (t_u - R_u R_k^T t_k),
+// so the target homogeneous point of input pixel (x, y) at depth z is x_h = M (z (x, y, 1)) + b.
+#include "device_common.cuh"
+#include "kernels.h"
+
+namespace lfrv {
+
+__device__ __forceinline__ void mv3(const float *M, float x, float y, float z, float *o) {
+    o[0] = M[0] * x + M[1] * y + M[2] * z;
+    o[1] = M[3] * x + M[4] * y + M[5] * z;
+    o[2] = M[6] * x + M[7] * y + M[8] * z;
+}
+
+// x_h of the point at pixel-space (px, py) with depth z seen from view cam.
+__device__ __forceinline__ void warp_point(const DevCamera &c, float px, float py, float z, float *xh) {
+    mv3(c.M, z * px, z * py, z, xh);
+    xh[0] += c.t[0];
+    xh[1] += c.t[1];
+    xh[2] += c.t[2];
+}
+
+// ------------------------------------------------------------------ target depth map
+__global__ void k_zclear(size_t N, unsigned long long *zkey) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) zkey[i] = 0ull;
+}
+
+__device__ __forceinline__ float edgef(float ax, float ay, float bx, float by, float px, float py) {
+    return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
+}
+__device__ __forceinline__ bool top_left(float ax, float ay, float bx, float by, bool ccw) {
+    const float ex = bx - ax, ey = by - ay;
+    if (!ccw) return (ey == 0.f && ex < 0.f) || ey > 0.f;
+    return (ey == 0.f && ex > 0.f) || ey < 0.f;
+}
+
+// Covered pixel centres of a triangle keep the largest interpolated 1/z (nearest surface); ties keep the
+// smaller centre depth. Key = (bits(1/z) << 32) | (~bits(z_centre)), both positive floats.
+__device__ void raster_tri(const float *v0, const float *v1, const float *v2, float zc, int W, int H,
+                           unsigned long long *zkey) {
+    const float area = edgef(v0[0], v0[1], v1[0], v1[1], v2[0], v2[1]);
+    if (area == 0.f) return;
+    const bool ccw = area > 0.f;
+    const int xmin = max(0, (int)floorf(fminf(v0[0], fminf(v1[0], v2[0])) - 0.5f));
+    const int xmax = min(W - 1, (int)ceilf(fmaxf(v0[0], fmaxf(v1[0], v2[0])) - 0.5f));
+    const int ymin = max(0, (int)floorf(fminf(v0[1], fminf(v1[1], v2[1])) - 0.5f));
+    const int ymax = min(H - 1, (int)ceilf(fmaxf(v0[1], fmaxf(v1[1], v2[1])) - 0.5f));
+    if (xmax < xmin || ymax < ymin) return;
+    if ((xmax - xmin) > 64 || (ymax - ymin) > 64) return;  // degenerate (grazing) quads are skipped
+    const bool tl0 = top_left(v1[0], v1[1], v2[0], v2[1], ccw);
+    const bool tl1 = top_left(v2[0], v2[1], v0[0], v0[1], ccw);
+    const bool tl2 = top_left(v0[0], v0[1], v1[0], v1[1], ccw);
+    const unsigned int zlow = ~__float_as_uint(zc);
+    for (int y = ymin; y <= ymax; ++y)
+        for (int x = xmin; x <= xmax; ++x) {
+            const float px = x + 0.5f, py = y + 0.5f;
+            float w0 = edgef(v1[0], v1[1], v2[0], v2[1], px, py);
+            float w1 = edgef(v2[0], v2[1], v0[0], v0[1], px, py);
+            float w2 = edgef(v0[0], v0[1], v1[0], v1[1], px, py);
+            if (!ccw) {
+                w0 = -w0;
+                w1 = -w1;
+                w2 = -w2;
+            }
+            if (w0 < 0.f || w1 < 0.f || w2 < 0.f) continue;
+            if ((w0 == 0.f && !tl0) || (w1 == 0.f && !tl1) || (w2 == 0.f && !tl2)) continue;
+            const float s = w0 + w1 + w2;
+            const float iz = (w0 * v0[2] + w1 * v1[2] + w2 * v2[2]) / s;
+            if (!(iz > 0.f)) continue;
+            const unsigned long long key = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
+            atomicMax(zkey + (size_t)y * W + x, key);
+        }
+}
+
+__global__ void __launch_bounds__(256) k_zsplat(int V, int w, int h, const float *__restrict__ depth,
+                                                const DevCamera *__restrict__ cams, int W, int H,
+                                                unsigned long long *__restrict__ zkey) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    const int n = w * h;
+    if (m >= n) return;
+    const float *dz = depth + (size_t)v * 3 * n;
+    const float z = dz[m], zx = dz[n + m], zy = dz[2 * n + m];
+    if (z >= 1000.0f * 0.5f) return;  // INVALID_DEPTH / 2 (depthSplatting.geom:21)
+    const DevCamera c = cams[v];
+    const float cx = (m % w) + 0.5f, cy = (m / w) + 0.5f;
+    float xh[3];
+    warp_point(c, cx, cy, z, xh);
+    const float zc = xh[2];
+    const float off[4][2] = {{-0.5f, -0.5f}, {-0.5f, 0.5f}, {0.5f, -0.5f}, {0.5f, 0.5f}};  // BL TL BR TR
+    float vert[4][3];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const float dx = off[k][0], dy = off[k][1];
+        warp_point(c, cx + dx, cy + dy, z + dx * zx + dy * zy, xh);
+        if (!(xh[2] > 1e-2f)) return;  // behind the near plane (zNear = 1e-2, sources/pinholeCamera.cpp:133)
+        vert[k][0] = xh[0] / xh[2];
+        vert[k][1] = xh[1] / xh[2];
+        vert[k][2] = 1.0f / xh[2];
+    }
+    raster_tri(vert[0], vert[1], vert[2], zc, W, H, zkey);
+    raster_tri(vert[1], vert[2], vert[3], zc, W, H, zkey);
+}
+
+__global__ void k_zresolve(size_t N, const unsigned long long *__restrict__ zkey, float *__restrict__ zbuf) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N) return;
+    const unsigned long long k = zkey[i];
+    zbuf[i] = k ? __uint_as_float(~(unsigned int)(k & 0xFFFFFFFFull)) : 0.0f;
+}
+
+// ------------------------------------------------------------------ tau and dtau/dz
+// GL_LINEAR on a sampler2DRect with CLAMP_TO_EDGE (sources/openGL/texture.cpp:153-156).
+__device__ __forceinline__ float bilinear_clamp(const float *img, int W, int H, float u, float v) {
+    const float fx = u - 0.5f, fy = v - 0.5f;
+    const float flx = floorf(fx), fly = floorf(fy);
+    const float ax = fx - flx, ay = fy - fly;
+    const int x0 = (int)flx, y0 = (int)fly;
+    auto at = [&](int x, int y) {
+        x = min(max(x, 0), W - 1);
+        y = min(max(y, 0), H - 1);
+        return __ldg(img + (size_t)y * W + x);
+    };
+    return (1.f - ay) * ((1.f - ax) * at(x0, y0) + ax * at(x0 + 1, y0)) +
+           ay * ((1.f - ax) * at(x0, y0 + 1) + ax * at(x0 + 1, y0 + 1));
+}
+
+__global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *__restrict__ depth,
+                                             const DevCamera *__restrict__ cams, int W, int H,
+                                             const float *__restrict__ zbuf, float *__restrict__ tau3,
+                                             float *__restrict__ dpart3, float *__restrict__ tau2,
+                                             float *__restrict__ dp2) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    const int n = w * h;
+    if (m >= n) return;
+    const float *dz = depth + (size_t)v * 3 * n;
+    const float z = dz[m], zx = dz[n + m], zy = dz[2 * n + m];
+    const DevCamera &c = cams[v];
+    const float x = (m % w) + 0.5f, y = (m / w) + 0.5f;
+    float xuh[3];
+    warp_point(c, x, y, z, xuh);
+    float xu = 0.f, yu = 0.f;
+    if (xuh[2] != 0.f) {
+        xu = xuh[0] / xuh[2];
+        yu = xuh[1] / xuh[2];
+    }
+    // Jacobian of the euclidean normalisation applied to M columns (tauWarp.frag:41-50)
+    float m0[3], m1[3], mk[3];
+    mv3(c.M, x * zx + z, y * zx, zx, m0);
+    mv3(c.M, x * zy, y * zy + z, zy, m1);
+    mv3(c.M, x, y, 1.0f, mk);
+    const float iz = 1.0f / xuh[2];
+    const float d00 = (m0[0] - xu * m0[2]) * iz, d01 = (m0[1] - yu * m0[2]) * iz;
+    const float d10 = (m1[0] - xu * m1[2]) * iz, d11 = (m1[1] - yu * m1[2]) * iz;
+    float deform = 1.0f / fabsf(d00 * d11 - d01 * d10);
+    if (deform >= 30.0f) deform = 30.0f;
+    const float rx = (mk[0] - xu * mk[2]) * iz, ry = (mk[1] - yu * mk[2]) * iz;
+    float t0, t1, t2;
+    if (xu <= 0.f || (float)W <= xu || yu <= 0.f || (float)H <= yu || z >= 500.0f) {
+        t0 = -2.0f;
+        t1 = -2.0f;
+        t2 = 0.0f;
+    } else if (xuh[2] > bilinear_clamp(zbuf, W, H, xu, yu) + 0.10f) {
+        t0 = -1.0f;
+        t1 = -1.0f;
+        t2 = 0.0f;
+    } else {
+        t0 = xu;
+        t1 = yu;
+        t2 = deform;
+    }
+    const size_t b3 = (size_t)v * 3 * n, b2 = (size_t)v * 2 * n;
+    if (tau3) {
+        tau3[b3 + m] = t0;
+        tau3[b3 + n + m] = t1;
+        tau3[b3 + 2 * n + m] = t2;
+    }
+    if (dpart3) {
+        dpart3[b3 + m] = 10.0f;
+        dpart3[b3 + n + m] = rx;
+        dpart3[b3 + 2 * n + m] = ry;
+    }
+    if (tau2) {
+        tau2[b2 + m] = t0;
+        tau2[b2 + n + m] = t1;
+    }
+    if (dp2) {
+        dp2[b2 + m] = 10.0f * rx;
+        dp2[b2 + n + m] = 10.0f * ry;
+    }
+}
+
+void launch_zbuffer_clear(int W, int H, unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "zbuffer_clear", st);
+    const size_t N = (size_t)W * H;
+    k_zclear<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, zkey);
+    lc.add(1);
+}
+
+void launch_zbuffer_splat(int V, int w, int h, const float *depth, const DevCamera *cams_dev, const DevCamera &target,
+                          unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "zbuffer_splat", st);
+    const int n = w * h;
+    k_zsplat<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, depth, cams_dev, target.W, target.H, zkey);
+    lc.add(1);
+}
+
+void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float *zbuf, cudaStream_t st,
+                            LaunchCounter &lc) {
+    const size_t N = (size_t)W * H;
+    k_zresolve<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, zkey, zbuf);
+    lc.add(1);
+}
+
+void launch_tau(int V, int w, int h, const float *depth, const DevCamera *cams_dev, const DevCamera &target,
+                const float *zbuf, float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st,
+                LaunchCounter &lc) {
+    const int n = w * h;
+    k_tau<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, depth, cams_dev, target.W, target.H, zbuf, tau3, dpart3,
+                                                   tau2, dp2);
+    lc.add(1);
+}
+
+}  // namespace lfrv

@@ -1,0 +1,445 @@
+"""Python binding of liblfrv.so (ctypes over the C ABI declared in include/lfrv.h).
+
+The reference's entry points are C++ functions driven by a Config_data object:
+    sr_synthesize_view(Config_data*)   -> Context.ibr_color(cfg, views, tau, dpart)
+    IBR_gradient(Config_data*)         -> Context.ibr_gradient(cfg, views, tau, dpart)
+    fromMVE2coco (GL warp export)      -> Context.warp(depth, cams, target)
+Arrays are numpy float32, planar channel-major (V x C x h x w for view stacks, C x H x W for images).
+Every call raises LfrvError with the library's message on a non-zero status. There is no CPU fallback:
+loading fails if liblfrv.so is missing and every compute call needs a CUDA device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = Path(os.environ.get("LFRV_LIB", _HERE / "liblfrv.so"))
+
+OK, E_ARG, E_CUDA, E_NOMEM, E_IO, E_FORMAT, E_NONFINITE, E_TIMEOUT, E_NODEVICE = 0, -1, -2, -3, -4, -5, -6, -7, -8
+
+
+class LfrvError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"lfrv status {status}: {message}")
+        self.status = status
+
+
+class Config(C.Structure):
+    _fields_ = [("w", C.c_int), ("h", C.c_int), ("dsf", C.c_int), ("nviews", C.c_int), ("nchannels", C.c_int),
+                ("sigma_sensor", C.c_float), ("ugrad_threshold", C.c_float), ("lambda_", C.c_float),
+                ("lambda_max_factor", C.c_float), ("dw_type", C.c_int), ("gw_type", C.c_int),
+                ("dt_alpha", C.c_float), ("dt_beta", C.c_float), ("gradient_step", C.c_float),
+                ("niter", C.c_int), ("nmeta_iter", C.c_int), ("faithful", C.c_int), ("early_exit", C.c_int),
+                ("cg_max_iter", C.c_int), ("cg_gap_tol", C.c_double), ("hole_fill_iter", C.c_int)]
+
+    def copy(self) -> "Config":
+        c = Config()
+        C.pointer(c)[0] = self
+        return c
+
+
+class Camera(C.Structure):
+    _fields_ = [("K", C.c_float * 9), ("R", C.c_float * 9), ("t", C.c_float * 3), ("width", C.c_int),
+                ("height", C.c_int)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("outer_iterations", C.c_int), ("meta_iterations", C.c_int), ("hole_fill_iterations", C.c_int),
+                ("stop_reason", C.c_int), ("energy", C.c_double), ("gap", C.c_double), ("seconds", C.c_double),
+                ("kernel_launches", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class SceneParams(C.Structure):
+    _fields_ = [("grid", C.c_int), ("w", C.c_int), ("h", C.c_int), ("ss", C.c_int), ("dsf", C.c_int),
+                ("baseline", C.c_double), ("nplanes", C.c_int), ("depths", C.c_double * 16), ("nbumps", C.c_int),
+                ("bump_amp", C.c_double), ("bump_sigma_px", C.c_double), ("noise_sigma", C.c_double),
+                ("focal_per_256", C.c_double), ("seed", C.c_uint64)]
+
+
+_F = C.POINTER(C.c_float)
+_U8 = C.POINTER(C.c_uint8)
+_D = C.POINTER(C.c_double)
+_I = C.POINTER(C.c_int)
+
+
+def _load() -> C.CDLL:
+    if not LIB_PATH.exists():
+        raise LfrvError(E_NODEVICE, f"{LIB_PATH} not built; run __graft_entry__.build() first")
+    lib = C.CDLL(str(LIB_PATH))
+    lib.lfrv_last_error.restype = C.c_char_p
+    lib.lfrv_version.restype = C.c_char_p
+    lib.lfrv_psnr.restype = C.c_double
+    lib.lfrv_psnr.argtypes = [C.c_int, C.c_int, _F, _F, C.c_int]
+    return lib
+
+
+LIB = _load()
+
+# Every function declared in include/lfrv.h.
+EXPORTED = [
+    "lfrv_last_error", "lfrv_version", "lfrv_config_default", "lfrv_config_parse_file", "lfrv_config_set",
+    "lfrv_config_get_string", "lfrv_config_get_int", "lfrv_ctx_create", "lfrv_ctx_destroy", "lfrv_ctx_set_stream",
+    "lfrv_ctx_launch_count", "lfrv_ctx_profile", "lfrv_ctx_profile_read", "lfrv_warp", "lfrv_warp_dev", "lfrv_ibr_color", "lfrv_ibr_color_dev",
+    "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_stage_weights",
+    "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
+    "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
+    "lfrv_stage_u_gradient", "lfrv_stage_cg", "lfrv_pfm_read", "lfrv_pfm_write", "lfrv_scene_params_preset",
+    "lfrv_synth_scene", "lfrv_psnr",
+]
+
+
+def _check(status: int) -> None:
+    if status != OK:
+        raise LfrvError(status, LIB.lfrv_last_error().decode(errors="replace"))
+
+
+def fptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.float32 and a.flags.c_contiguous, "float32 C-contiguous array expected"
+    return a.ctypes.data_as(_F)
+
+
+def u8ptr(a: np.ndarray | None):
+    if a is None:
+        return None
+    assert a.dtype == np.uint8 and a.flags.c_contiguous
+    return a.ctypes.data_as(_U8)
+
+
+def f32(a) -> np.ndarray:
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+# ------------------------------------------------------------------ configuration
+def default_config(**overrides) -> Config:
+    cfg = Config()
+    _check(LIB.lfrv_config_default(C.byref(cfg)))
+    for k, v in overrides.items():
+        setattr(cfg, "lambda_" if k == "lambda" else k, v)
+    return cfg
+
+
+def parse_config(path: str, cfg: Config | None = None) -> Config:
+    cfg = cfg or default_config()
+    _check(LIB.lfrv_config_parse_file(str(path).encode(), C.byref(cfg)))
+    return cfg
+
+
+def config_string(key: str) -> str:
+    buf = C.create_string_buffer(1024)
+    _check(LIB.lfrv_config_get_string(key.encode(), buf, C.c_size_t(len(buf))))
+    return buf.value.decode()
+
+
+# ------------------------------------------------------------------ synthetic scenes
+@dataclass
+class Scene:
+    params: SceneParams
+    views: np.ndarray   # V x 3 x h x w
+    depth: np.ndarray   # V x 3 x h x w (z, dz/dx, dz/dy)
+    cams: list          # V input cameras
+    target: Camera
+    gt: np.ndarray      # 3 x H x W
+
+
+def scene_params(preset: int, **overrides) -> SceneParams:
+    p = SceneParams()
+    _check(LIB.lfrv_scene_params_preset(preset, C.byref(p)))
+    for k, v in overrides.items():
+        if k == "depths":
+            for i, d in enumerate(v):
+                p.depths[i] = d
+            p.nplanes = len(v)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def synth_scene(p: SceneParams) -> Scene:
+    V = p.grid * p.grid - 1
+    h, w, H, W = p.h, p.w, p.h * p.dsf, p.w * p.dsf
+    views = np.zeros((V, 3, h, w), np.float32)
+    depth = np.zeros((V, 3, h, w), np.float32)
+    cams = (Camera * (V + 1))()
+    gt = np.zeros((3, H, W), np.float32)
+    _check(LIB.lfrv_synth_scene(C.byref(p), fptr(views), fptr(depth), cams, fptr(gt)))
+    return Scene(p, views, depth, [cams[i] for i in range(V)], cams[V], gt)
+
+
+def cameras_array(cams) -> C.Array:
+    arr = (Camera * len(cams))()
+    for i, c in enumerate(cams):
+        arr[i] = c
+    return arr
+
+
+def psnr(a: np.ndarray, b: np.ndarray, border: int = 2) -> float:
+    a, b = f32(a), f32(b)
+    return LIB.lfrv_psnr(a.shape[-1], a.shape[-2], fptr(a), fptr(b), border)
+
+
+def pfm_read(path: str) -> np.ndarray:
+    w, h, c = C.c_int(), C.c_int(), C.c_int()
+    _check(LIB.lfrv_pfm_read(str(path).encode(), C.byref(w), C.byref(h), C.byref(c), None, C.c_size_t(0)))
+    out = np.zeros((c.value, h.value, w.value), np.float32)
+    _check(LIB.lfrv_pfm_read(str(path).encode(), C.byref(w), C.byref(h), C.byref(c), fptr(out),
+                             C.c_size_t(out.size)))
+    return out
+
+
+def pfm_write(path: str, img: np.ndarray) -> None:
+    img = f32(img)
+    if img.ndim == 2:
+        img = img[None]
+    _check(LIB.lfrv_pfm_write(str(path).encode(), img.shape[2], img.shape[1], img.shape[0], fptr(img)))
+
+
+# ------------------------------------------------------------------ contexts
+class Context:
+    """One device workspace (lfrv_ctx). Work is issued on `stream` (a cudaStream_t as int, 0 = default)."""
+
+    def __init__(self, device: int = 0, stream: int | None = None):
+        self._h = C.c_void_p()
+        _check(LIB.lfrv_ctx_create(C.byref(self._h), device))
+        if stream:
+            self.set_stream(stream)
+
+    def close(self) -> None:
+        if self._h:
+            LIB.lfrv_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream: int) -> None:
+        _check(LIB.lfrv_ctx_set_stream(self._h, C.c_void_p(stream)))
+
+    def launch_count(self, reset: bool = False) -> int:
+        n = C.c_longlong()
+        _check(LIB.lfrv_ctx_launch_count(self._h, C.byref(n), int(reset)))
+        return n.value
+
+    def profile_enable(self, on: bool = True) -> None:
+        _check(LIB.lfrv_ctx_profile(self._h, int(on)))
+
+    def profile(self) -> dict:
+        """{kernel launcher name: (total device ms, launches)} since profile_enable(True)."""
+        out = {}
+        name = C.create_string_buffer(128)
+        ms, cnt = C.c_double(), C.c_longlong()
+        i = 0
+        while True:
+            st = LIB.lfrv_ctx_profile_read(self._h, i, name, C.c_size_t(len(name)), C.byref(ms), C.byref(cnt))
+            if st != OK:
+                break
+            out[name.value.decode()] = (ms.value, cnt.value)
+            i += 1
+        return out
+
+    # ---- warp stage
+    def warp(self, depth: np.ndarray, cams, target: Camera):
+        depth = f32(depth)
+        V, _, h, w = depth.shape
+        tau = np.zeros((V, 3, h, w), np.float32)
+        dpart = np.zeros((V, 3, h, w), np.float32)
+        zbuf = np.zeros((target.height, target.width), np.float32)
+        _check(LIB.lfrv_warp(self._h, V, w, h, fptr(depth), cameras_array(cams), C.byref(target), fptr(tau),
+                             fptr(dpart), fptr(zbuf)))
+        return tau, dpart, zbuf
+
+    def warp_dev(self, nviews: int, w: int, h: int, d_depth: int, cams, target: Camera, d_tau: int, d_dpart: int,
+                 d_zbuf: int = 0) -> None:
+        _check(LIB.lfrv_warp_dev(self._h, nviews, w, h, C.c_void_p(d_depth), cameras_array(cams), C.byref(target),
+                                 C.c_void_p(d_tau), C.c_void_p(d_dpart), C.c_void_p(d_zbuf or None)))
+
+    # ---- solvers
+    def _solve(self, fn, cfg: Config, views, tau, dpart, init=None):
+        views, tau = f32(views), f32(tau)
+        dpart = None if dpart is None else f32(dpart)
+        init = None if init is None else f32(init)
+        H, W = cfg.h * cfg.dsf, cfg.w * cfg.dsf
+        out = np.zeros((3, H, W), np.float32)
+        st = Stats()
+        _check(fn(self._h, C.byref(cfg), fptr(views), fptr(tau), tau.shape[1], fptr(dpart), fptr(init), fptr(out),
+                  C.byref(st)))
+        return out, st
+
+    def ibr_color(self, cfg: Config, views, tau, dpart, init=None):
+        return self._solve(LIB.lfrv_ibr_color, cfg, views, tau, dpart, init)
+
+    def ibr_gradient(self, cfg: Config, views, tau, dpart, init=None):
+        return self._solve(LIB.lfrv_ibr_gradient, cfg, views, tau, dpart, init)
+
+    def solve_dev(self, algorithm: int, cfg: Config, d_views: int, d_tau: int, tau_channels: int, d_dpart: int,
+                  d_out: int, d_init: int = 0) -> Stats:
+        st = Stats()
+        fn = LIB.lfrv_ibr_color_dev if algorithm == 0 else LIB.lfrv_ibr_gradient_dev
+        _check(fn(self._h, C.byref(cfg), C.c_void_p(d_views), C.c_void_p(d_tau), tau_channels,
+                  C.c_void_p(d_dpart or None), C.c_void_p(d_init or None), C.c_void_p(d_out), C.byref(st)))
+        return st
+
+    def render_view_dev(self, cfg: Config, algorithm: int, d_views: int, d_depth: int, cams, target: Camera,
+                        d_out: int) -> Stats:
+        st = Stats()
+        _check(LIB.lfrv_render_view_dev(self._h, C.byref(cfg), algorithm, C.c_void_p(d_views), C.c_void_p(d_depth),
+                                        cameras_array(cams), C.byref(target), C.c_void_p(d_out), C.byref(st)))
+        return st
+
+    def render_view(self, cfg: Config, algorithm: int, views, depth, cams, target: Camera, out=None):
+        """Host-buffer pipeline (copies inside the call). views/depth/out may be numpy arrays or host pointers."""
+        st = Stats()
+        views_p = views if isinstance(views, int) else f32(views).ctypes.data
+        depth_p = depth if isinstance(depth, int) else f32(depth).ctypes.data
+        if out is None:
+            out = np.zeros((3, cfg.h * cfg.dsf, cfg.w * cfg.dsf), np.float32)
+        out_p = out if isinstance(out, int) else out.ctypes.data
+        _check(LIB.lfrv_render_view(self._h, C.byref(cfg), algorithm, C.c_void_p(views_p), C.c_void_p(depth_p),
+                                    cameras_array(cams), C.byref(target), C.c_void_p(out_p), C.byref(st)))
+        return out, st
+
+    # ---- stage calls (parity tests)
+    def stage_visibility(self, cfg: Config, tau):
+        tau = f32(tau)
+        H, W = cfg.h * cfg.dsf, cfg.w * cfg.dsf
+        cov = np.zeros((H, W), np.float32)
+        vis = np.zeros((H, W), np.uint8)
+        _check(LIB.lfrv_stage_visibility(self._h, C.byref(cfg), fptr(tau), tau.shape[1], fptr(cov), u8ptr(vis)))
+        return cov, vis
+
+    def stage_weights(self, cfg: Config, views, tau, dpart, U, vis, gx, gy):
+        views, tau, dpart, U = f32(views), f32(tau), f32(dpart), f32(U)
+        vis = np.ascontiguousarray(vis, np.uint8)
+        gx, gy = f32(gx).copy(), f32(gy).copy()
+        wgt = np.zeros((cfg.nviews, cfg.h, cfg.w), np.float32)
+        _check(LIB.lfrv_stage_weights(self._h, C.byref(cfg), fptr(views), fptr(tau), tau.shape[1], fptr(dpart),
+                                      fptr(U), u8ptr(vis), fptr(gx), fptr(gy), fptr(wgt)))
+        return gx, gy, wgt
+
+    def stage_dataterm(self, cfg: Config, views, tau, weights, U):
+        views, tau, weights, U = f32(views), f32(tau), f32(weights), f32(U)
+        G = np.zeros_like(U)
+        F = np.zeros_like(U)
+        _check(LIB.lfrv_stage_dataterm(self._h, C.byref(cfg), fptr(views), fptr(tau), tau.shape[1], fptr(weights),
+                                       fptr(U), fptr(G), fptr(F)))
+        return G, F
+
+    def stage_rof(self, niter: int, tau: float, sigma: float, lam: float, F, g, U, P):
+        F, g = f32(F), f32(g)
+        U, P = f32(U).copy(), f32(P).copy()
+        H, W = U.shape[1], U.shape[2]
+        _check(LIB.lfrv_stage_rof(self._h, W, H, niter, C.c_float(tau), C.c_float(sigma), C.c_float(lam), fptr(F),
+                                  fptr(g), fptr(U), fptr(P)))
+        return U, P
+
+    def stage_energy(self, cfg: Config, views, tau, weights, U, vis):
+        views, tau, weights, U = f32(views), f32(tau), f32(weights), f32(U)
+        vis = np.ascontiguousarray(vis, np.uint8)
+        e, et, ed = C.c_double(), C.c_double(), C.c_double()
+        _check(LIB.lfrv_stage_energy(self._h, C.byref(cfg), fptr(views), fptr(tau), tau.shape[1], fptr(weights),
+                                     fptr(U), u8ptr(vis), C.byref(e), C.byref(et), C.byref(ed)))
+        return e.value, et.value, ed.value
+
+    def stage_regularizer(self, cfg: Config, tau, weights, norm_in=None):
+        tau, weights = f32(tau), f32(weights)
+        H, W = cfg.h * cfg.dsf, cfg.w * cfg.dsf
+        norm_out = np.zeros((H, W), np.float32)
+        g = np.zeros((H, W), np.float32)
+        _check(LIB.lfrv_stage_regularizer(self._h, C.byref(cfg), fptr(tau), tau.shape[1], fptr(weights),
+                                          fptr(None if norm_in is None else f32(norm_in)), fptr(norm_out), fptr(g)))
+        return norm_out, g
+
+    def stage_initial_image(self, cfg: Config, views, tau, weights):
+        views, tau, weights = f32(views), f32(tau), f32(weights)
+        H, W = cfg.h * cfg.dsf, cfg.w * cfg.dsf
+        U = np.zeros((3, H, W), np.float32)
+        norm = np.zeros((H, W), np.float32)
+        _check(LIB.lfrv_stage_initial_image(self._h, C.byref(cfg), fptr(views), fptr(tau), tau.shape[1],
+                                            fptr(weights), fptr(U), fptr(norm)))
+        return U, norm
+
+    def stage_push_pull(self, U, vis, faithful: bool = True):
+        U = f32(U).copy()
+        vis = np.ascontiguousarray(vis, np.uint8)
+        _check(LIB.lfrv_stage_push_pull(self._h, U.shape[2], U.shape[1], int(faithful), u8ptr(vis), fptr(U)))
+        return U
+
+    def stage_gradient_visibility(self, cfg: Config, tau):
+        tau = f32(tau)
+        vis = np.zeros((cfg.h * cfg.dsf, cfg.w * cfg.dsf), np.uint8)
+        _check(LIB.lfrv_stage_gradient_visibility(self._h, C.byref(cfg), fptr(tau), tau.shape[1], u8ptr(vis)))
+        return vis
+
+    def stage_hole_fill(self, U, vis, max_iter: int = 500):
+        U = f32(U).copy()
+        vis = np.ascontiguousarray(vis, np.uint8)
+        it = C.c_int()
+        _check(LIB.lfrv_stage_hole_fill(self._h, U.shape[2], U.shape[1], max_iter, u8ptr(vis), fptr(U),
+                                        C.byref(it)))
+        return U, it.value
+
+    def stage_u_gradient(self, cfg: Config, views, tau, weights):
+        views, tau, weights = f32(views), f32(tau), f32(weights)
+        H, W = cfg.h * cfg.dsf, cfg.w * cfg.dsf
+        gx, gy, mask = (np.zeros((H, W), np.float32) for _ in range(3))
+        _check(LIB.lfrv_stage_u_gradient(self._h, C.byref(cfg), fptr(views), fptr(tau), tau.shape[1], fptr(weights),
+                                         fptr(gx), fptr(gy), fptr(mask)))
+        return gx, gy, mask
+
+    def stage_cg(self, gx, gy, U, faithful: bool, max_iter: int = 500, gap_tol: float = 1e-4):
+        gx, gy = f32(gx), f32(gy)
+        U = f32(U).copy()
+        it, gap = C.c_int(), C.c_double()
+        _check(LIB.lfrv_stage_cg(self._h, U.shape[2], U.shape[1], int(faithful), max_iter, C.c_double(gap_tol),
+                                 fptr(gx), fptr(gy), fptr(U), C.byref(it), C.byref(gap)))
+        return U, it.value, gap.value
+
+
+def _declare() -> None:
+    vp = C.c_void_p
+    LIB.lfrv_ctx_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+    LIB.lfrv_ctx_destroy.argtypes = [vp]
+    LIB.lfrv_ctx_set_stream.argtypes = [vp, vp]
+    LIB.lfrv_ctx_launch_count.argtypes = [vp, C.POINTER(C.c_longlong), C.c_int]
+    LIB.lfrv_ctx_profile.argtypes = [vp, C.c_int]
+    LIB.lfrv_ctx_profile_read.argtypes = [vp, C.c_int, C.c_char_p, C.c_size_t, _D, C.POINTER(C.c_longlong)]
+    LIB.lfrv_warp.argtypes = [vp, C.c_int, C.c_int, C.c_int, _F, C.POINTER(Camera), C.POINTER(Camera), _F, _F, _F]
+    LIB.lfrv_warp_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, C.POINTER(Camera), C.POINTER(Camera), vp, vp, vp]
+    for name in ("lfrv_ibr_color", "lfrv_ibr_gradient"):
+        getattr(LIB, name).argtypes = [vp, C.POINTER(Config), _F, _F, C.c_int, _F, _F, _F, C.POINTER(Stats)]
+    for name in ("lfrv_ibr_color_dev", "lfrv_ibr_gradient_dev"):
+        getattr(LIB, name).argtypes = [vp, C.POINTER(Config), vp, vp, C.c_int, vp, vp, vp, C.POINTER(Stats)]
+    LIB.lfrv_render_view_dev.argtypes = [vp, C.POINTER(Config), C.c_int, vp, vp, C.POINTER(Camera),
+                                         C.POINTER(Camera), vp, C.POINTER(Stats)]
+    LIB.lfrv_render_view.argtypes = [vp, C.POINTER(Config), C.c_int, vp, vp, C.POINTER(Camera), C.POINTER(Camera),
+                                     vp, C.POINTER(Stats)]
+    LIB.lfrv_stage_rof.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, _F, _F, _F, _F]
+    LIB.lfrv_stage_cg.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _F, _F, _F, _I, _D]
+    LIB.lfrv_stage_push_pull.argtypes = [vp, C.c_int, C.c_int, C.c_int, _U8, _F]
+    LIB.lfrv_stage_hole_fill.argtypes = [vp, C.c_int, C.c_int, C.c_int, _U8, _F, _I]
+    LIB.lfrv_synth_scene.argtypes = [C.POINTER(SceneParams), _F, _F, C.POINTER(Camera), _F]
+    LIB.lfrv_scene_params_preset.argtypes = [C.c_int, C.POINTER(SceneParams)]
+    LIB.lfrv_config_get_string.argtypes = [C.c_char_p, C.c_char_p, C.c_size_t]
+    LIB.lfrv_pfm_read.argtypes = [C.c_char_p, _I, _I, _I, _F, C.c_size_t]
+    LIB.lfrv_pfm_write.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, _F]
+
+
+_declare()
