@@ -391,7 +391,10 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
             LFRV_CUDA(cudaMemcpyAsync(b.Uprev, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
         }
         if (faithful) norm_prior = (k > 0) ? b.cov : b.norm;  // data term clears and re-accumulates the coverage
-        if (!track) continue;
+        if (!track) {
+            if (r == cfg.nmeta_iter - 1) E = energy(true);  // reported energy of the final iterate
+            continue;
+        }
         if (E < EPS) {
             if (E_prev_reweight < EPS) break;
             E_prev_reweight = E;

@@ -380,9 +380,13 @@ __global__ void k_sobel(int W, int H, const float *__restrict__ rgb, size_t in_s
                         }
             }
             if (write) {
+                // The reference evaluates the luminance as a double expression rounded to float; the
+                // masked (target) Sobel does the same because the angular weights amplify its rounding.
                 auto L = [&](int dx, int dy) {
                     const size_t q = o + (ptrdiff_t)dy * W + dx;
-                    return lum(r[q], g[q], b[q]);
+                    if (!vis) return lum(r[q], g[q], b[q]);
+                    return (float)__dadd_rn(__dadd_rn(__dmul_rn(0.2126, (double)r[q]), __dmul_rn(0.7152, (double)g[q])),
+                                            __dmul_rn(0.0722, (double)b[q]));
                 };
                 const float Ypp = L(-1, -1), Ypc = L(0, -1), Ypn = L(1, -1);
                 const float Ycp = L(-1, 0), Ycn = L(1, 0);

@@ -535,6 +535,7 @@ struct ColorState {
     lfrv_config cfg;
     size_t N;
     Vec<T> U[3], Uq[3], G[3], X1[3], X2[3], X1q, X2q, g, norm_mask, cov;
+    Vec<T> gxs, gys;  // gradient buffers of the corrected mode (the reference writes into X1[0], X2[0])
     std::vector<uint8_t> vis;
     T alpha = 1;
 
@@ -551,6 +552,8 @@ struct ColorState {
         }
         X1q.assign(N, 0);
         X2q.assign(N, 0);
+        gxs.assign(N, 0);
+        gys.assign(N, 0);
         g.assign(N, 0);
         norm_mask.assign(N, 0);
         cov.assign(N, 0);
@@ -560,12 +563,14 @@ struct ColorState {
 };
 
 // coco_vtv_sr_compute_weights_unstructured, sources/optimization.cu:1066-1167. The Sobel kernel writes
-// into X1[0], X2[0] (the channel-0 dual variables) with the visibility mask.
+// into X1[0], X2[0] (the channel-0 dual variables) with the visibility mask (defect D5, faithful mode);
+// the corrected mode writes into buffers of its own.
 template <class T>
 void color_compute_weights(ColorState<T> &S) {
-    sobel(S.P.W, S.P.H, S.U[0].data(), S.U[1].data(), S.U[2].data(), S.X1[0].data(), S.X2[0].data(), S.vis.data());
-    for (auto &vw : S.P.views)
-        view_weights(S.P, vw, S.X1[0].data(), S.X2[0].data(), (T)S.cfg.sigma_sensor, (T)S.cfg.ugrad_threshold);
+    T *gx = S.cfg.faithful ? S.X1[0].data() : S.gxs.data();
+    T *gy = S.cfg.faithful ? S.X2[0].data() : S.gys.data();
+    sobel(S.P.W, S.P.H, S.U[0].data(), S.U[1].data(), S.U[2].data(), gx, gy, S.vis.data());
+    for (auto &vw : S.P.views) view_weights(S.P, vw, gx, gy, (T)S.cfg.sigma_sensor, (T)S.cfg.ugrad_threshold);
 }
 
 // coco_vtv_setup_visibility_mask, sources/optimization.cu:33-135: coverage by splatting ones with A,
@@ -608,6 +613,8 @@ void color_initial_image(ColorState<T> &S, bool fill) {
 // vtv_sr_init_regularizer_weight_device (cocolib/cocolib/vtv/vtv_sr_kernels.cu:1172-1195).
 template <class T>
 void color_regularizer(ColorState<T> &S) {
+    // The reference never clears the coverage accumulator here (defect D6, faithful mode).
+    if (!S.cfg.faithful) std::fill(S.norm_mask.begin(), S.norm_mask.end(), T(0));
     Vec<T> m(S.N, T(0));
     for (auto &vw : S.P.views) {
         const T *in[1] = {vw.w.data()};

@@ -24,10 +24,13 @@ def test_warp_vs_oracle(ctx, preset, w):
     sc = scene(preset, w)
     tau, dpart, zb = ctx.warp(sc.depth, sc.cams, sc.target)
     rtau, rdpart, rzb = pyoracle.warp(sc.depth, sc.cams, sc.target)
-    # z-buffer: identical coverage almost everywhere, same depth where both cover
+    # z-buffer: identical coverage almost everywhere, same depth where both cover. Overlapping quads of one
+    # surface tie in depth; float and double rasterisation may keep different ones, whose centre depths differ
+    # by the surface's depth change across a pixel (the value only feeds the 0.10 occlusion tolerance).
     both = (zb > 0) & (rzb > 0)
     assert np.mean((zb > 0) != (rzb > 0)) < 0.01
-    assert np.mean(np.abs(zb[both] - rzb[both]) > 1e-4) < 0.01
+    assert np.mean(np.abs(zb[both] - rzb[both]) > 1e-4) < 0.03
+    assert np.mean(np.abs(zb[both] - rzb[both]) > 2e-2) < 0.005
     # tau codes
     code = np.where(tau[:, 0] < 0, tau[:, 0], 0)
     rcode = np.where(rtau[:, 0] < 0, rtau[:, 0], 0)
@@ -64,7 +67,9 @@ def test_weights(ctx, preset, w):
     gx, gy, wg = ctx.stage_weights(cfg, sc.views, tau, dpart, U, vis, gx0, gy0)
     rgx, rgy, rwg = pyoracle.stage_weights(cfg, sc.views, tau, dpart, U, vis, gx0, gy0, prec=1)
     assert np.max(np.abs(gx - rgx)) < 1e-5 and np.max(np.abs(gy - rgy)) < 1e-5
-    assert rel_err(wg, rwg, floor=1.0) < 1e-4
+    # w = 1/(sg^2 + sigma^2) with sg = (A grad) . dpart: on random-noise U the two products of sg cancel by up
+    # to ~1e3, so a one-ulp difference in the gathered gradient (FMA contraction) reaches ~2e-4 in w.
+    assert rel_err(wg, rwg, floor=1.0) < 5e-4
     assert N > 0
 
 
