@@ -35,8 +35,8 @@ struct Workspace {
     DevBuf U, Ua, Ub, Uprev, P, Pa, F, G, g, g0, tmp, cov, norm, vis, Xq, gx, gy, mask, zkey, zbuf;
     // CG
     DevBuf r, d, q, U0, holes, hole_count;
-    // reductions
-    DevBuf partial, sums;
+    // reductions and persistent-solver state
+    DevBuf partial, sums, state, barrier;
     // push-pull pyramid
     DevBuf pp_img, pp_vis, pp_tmp, pp_orig;
     // host staging for the host-buffer entry points
@@ -59,9 +59,17 @@ struct KernelProfiler {
     void end(int slot, cudaStream_t st);
 };
 
+// Statistics left on the device by persistent solvers of the current call, read after the stream completes.
+struct Pending {
+    bool cg = false, hole_fill = false;
+    lfrv_stats *stats = nullptr;
+    double gap_tol = 0.0;
+};
+
 }  // namespace lfrv
 
 struct lfrv_ctx {
+    lfrv::Pending pending;
     lfrv::KernelProfiler prof;
     bool profiling = false;
     int device = 0;

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "kernels.h"
+
 namespace lfrv {
 
 constexpr int kMaxKs = 5;  // ks = dsf + 1, dsf <= 4
@@ -65,12 +67,34 @@ __device__ __forceinline__ void footprint(float tx, float ty, int dsf, int W, in
     }
 }
 
-// Single normalised weight of tap (j, i) of a footprint (used by the inverse-map gathers).
+// Normalised weight of the single tap (j, i) of the footprint anchored at (x0, y0), with the float operations
+// of footprint() (same products, same summation order of the norm, one division): the inverse-map gathers
+// need one tap per visit. raw receives the un-normalised overlap dx*dy of that tap (0 when off-image).
+// (J, I) are compile-time constants at every call site (fully unrolled loops), so the selection folds away.
 template <int KS>
-__device__ __forceinline__ float footprint_tap(float tx, float ty, int dsf, int W, int H, int j, int i) {
-    Footprint fp;
-    footprint<KS>(tx, ty, dsf, W, H, fp);
-    return fp.A[KS * i + j];
+__device__ __forceinline__ float footprint_tap(float tx, float ty, int dsf, int W, int H, int x0, int y0, int J, int I,
+                                               float &raw) {
+    const float px = tx - 0.5f, py = ty - 0.5f;
+    float dxs[KS], dys[KS];
+#pragma unroll
+    for (int k = 0; k < KS; ++k) {
+        dxs[k] = fp_overlap(k, KS, x0 + k, px, dsf);
+        dys[k] = fp_overlap(k, KS, y0 + k, py, dsf);
+    }
+    float norm = 0.0f, tap = 0.0f;
+#pragma unroll
+    for (int j = 0; j < KS; ++j) {
+#pragma unroll
+        for (int i = 0; i < KS; ++i) {
+            const int x = x0 + j, y = y0 + i;
+            const bool in = (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1);
+            const float a = in ? __fmul_rn(dxs[j], dys[i]) : 0.0f;
+            norm = __fadd_rn(norm, a);
+            if (j == J && i == I) tap = a;
+        }
+    }
+    raw = tap;
+    return (norm != 0.0f) ? __fdiv_rn(tap, norm) : tap;
 }
 
 // Raw overlap product of tap (j, i) (setup_visibility_mask, sources/gradientIBR_kernels.cuh:26-49).
@@ -115,14 +139,11 @@ __device__ __forceinline__ double block_sum(double v, double *smem /* >= NT/32 *
 }
 
 // ------------------------------------------------------------------ bounded grid barrier
-// For kernels launched cooperatively (all blocks co-resident). Every wait is bounded: after
-// kSpinLimit polls the block records LFRV timeout in *err and returns false; callers then exit.
-struct GridBarrier {
-    unsigned int *count;  // monotonically increasing arrival counter (zeroed before the launch)
-    int *err;             // set to 1 on timeout
-};
-
-constexpr long long kSpinLimit = 1ll << 26;
+// For kernels launched cooperatively (all blocks co-resident). GridBarrier (kernels.h) holds a monotonically
+// increasing arrival counter and an error flag, both zeroed before the launch. Every wait is bounded: after
+// kSpinLimit polls (about 2^22 * 64 ns, a fraction of a second) the block sets *err and returns false;
+// callers then exit, and the host reports LFRV_E_TIMEOUT.
+constexpr long long kSpinLimit = 1ll << 22;
 
 __device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &generation) {
     __syncthreads();

@@ -414,7 +414,25 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
 }
 
 // ------------------------------------------------------------------ IBR_gradient
-static int hole_fill(lfrv_ctx *c, int W, int H, const uint8_t *vis, float *U, int max_iter) {
+// Device state of the persistent solvers, read back after the stream completes (lfrv::finish_stats):
+// [0..2] CG delta, [3] CG energy, [4] CG certified gap, [5] CG iterations, [8] hole-fill iterations.
+static double *solver_state(lfrv_ctx *c) {
+    c->ws.state.ensure(sizeof(double) * 16);
+    return c->ws.state.as<double>();
+}
+
+static GridBarrier fresh_barrier(lfrv_ctx *c) {
+    c->ws.barrier.ensure(64);
+    LFRV_CUDA(cudaMemsetAsync(c->ws.barrier.p, 0, 64, c->stream));
+    GridBarrier gb;
+    gb.count = c->ws.barrier.as<unsigned int>();
+    gb.err = reinterpret_cast<int *>(c->ws.barrier.as<unsigned int>() + 4);
+    return gb;
+}
+
+// hole_filling (sources/gradientIBR.cu:87-152) on the device: hole list, then one persistent launch that runs
+// the Jacobi iterations and their energy test (|change of the last channel's sum(lap * U)| < 1e-3).
+static void hole_fill_async(lfrv_ctx *c, int W, int H, const uint8_t *vis, float *U, int max_iter) {
     Workspace &ws = c->ws;
     const size_t N = (size_t)W * H;
     cudaStream_t s = c->stream;
@@ -422,63 +440,43 @@ static int hole_fill(lfrv_ctx *c, int W, int H, const uint8_t *vis, float *U, in
     ws.hole_count.ensure(sizeof(int) * 4);
     launch_hole_list(W, H, vis, ws.holes.as<int>(), ws.hole_count.as<int>(), s, c->launches);
     check_launch("hole list");
-    int nholes = 0;
-    LFRV_CUDA(cudaMemcpyAsync(&nholes, ws.hole_count.p, sizeof(int), cudaMemcpyDeviceToHost, s));
-    sync(c);
-    // hole_filling (sources/gradientIBR.cu:87-152): stop when the change of the last channel's
-    // sum(lap * U) drops below epsilon = 1e-3 (float energies).
     ws.Ua.ensure(3 * N * sizeof(float));
-    float *A = U, *Bb = ws.Ua.as<float>();
-    LFRV_CUDA(cudaMemcpyAsync(Bb, A, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    const int np = hole_fill_partials(nholes);
-    float energy = 0.0f, previous = 0.0f;
-    int k;
-    for (k = 0; k < max_iter; ++k) {
-        previous = energy;
-        double e = 0.0;
-        if (nholes > 0) {
-            double *part = partial_buf(c, np);
-            launch_hole_fill_iter(W, H, ws.holes.as<int>(), nholes, A, Bb, part, s, c->launches);
-            check_launch("hole fill");
-            reduce_to(c, np, part, 0);
-            read_sums(c, &e, 1);
-            std::swap(A, Bb);
-        }
-        energy = (float)e;
-        if (std::fabs(previous - energy) < 1e-3f) {
-            ++k;
-            break;
-        }
-    }
-    if (A != U) LFRV_CUDA(cudaMemcpyAsync(U, A, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    return k;
+    LFRV_CUDA(cudaMemcpyAsync(ws.Ua.p, U, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    double *part = partial_buf(c, 2 * (size_t)persistent_partials());
+    const GridBarrier gb = fresh_barrier(c);
+    LFRV_CUDA(launch_hole_fill_persistent(W, H, ws.holes.as<int>(), ws.hole_count.as<int>(), U, ws.Ua.as<float>(),
+                                          part, gb, max_iter, solver_state(c) + 8, s, c->launches));
+    c->pending.hole_fill = true;
+}
+
+// Sobel of every input view's luminance (compute_gradient, sources/gradientIBR_kernels.cuh:57-100).
+static float *view_gradients(lfrv_ctx *c, const Geometry &G, const float *img) {
+    Workspace &ws = c->ws;
+    ws.vgrad.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    float *vg = ws.vgrad.as<float>();
+    launch_sobel(G.w, G.h, G.V, img, (size_t)3 * G.n, (size_t)G.n, vg, vg + G.n, (size_t)2 * G.n, nullptr, nullptr,
+                 c->stream, c->launches);
+    check_launch("view sobel");
+    return vg;
 }
 
 static void u_gradient(lfrv_ctx *c, const Geometry &G, const Buckets &B, const float *img, const float *tau2,
                        const float *wgt, float s2, float *gx, float *gy, float *mask) {
-    Workspace &ws = c->ws;
-    ws.vgrad.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
-    float *vg = ws.vgrad.as<float>();
-    // Sobel of every input view's luminance (compute_gradient, sources/gradientIBR_kernels.cuh:57-100)
-    launch_sobel(G.w, G.h, G.V, img, (size_t)3 * G.n, (size_t)G.n, vg, vg + G.n, (size_t)2 * G.n, nullptr, nullptr,
-                 c->stream, c->launches);
-    check_launch("view sobel");
+    float *vg = view_gradients(c, G, img);
     launch_u_gradient(G, B, tau2, vg, wgt, s2, gx, gy, mask, c->stream, c->launches);
     check_launch("gradient splat");
 }
 
-// Conjugate gradient of possion_conj_grad (faithful) or the corrected CG (see lfrv_stage_cg).
-static int cg_solve(lfrv_ctx *c, int W, int H, bool faithful, int max_iter, double gap_tol, const float *gx,
-                    const float *gy, float *U, double *gap_out) {
+// possion_conj_grad with the reference's loop (faithful, defect D1): 5 iterations, host-side scalars as the
+// reference computes them (sources/solver.cu:612-676).
+static int cg_faithful(lfrv_ctx *c, int W, int H, const float *gx, const float *gy, float *U) {
     Workspace &ws = c->ws;
     const size_t N = (size_t)W * H;
     cudaStream_t s = c->stream;
     ws.r.ensure(3 * N * sizeof(float));
     ws.d.ensure(3 * N * sizeof(float));
     ws.q.ensure(3 * N * sizeof(float));
-    ws.U0.ensure(3 * N * sizeof(float));
-    float *r = ws.r.as<float>(), *d = ws.d.as<float>(), *q = ws.q.as<float>(), *U0 = ws.U0.as<float>();
-    LFRV_CUDA(cudaMemcpyAsync(U0, U, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    float *r = ws.r.as<float>(), *d = ws.d.as<float>(), *q = ws.q.as<float>();
     const int np = cg_partials(W, H);
     double *part = partial_buf(c, 3 * (size_t)np);
     ws.sums.ensure(sizeof(double) * 64);
@@ -491,72 +489,46 @@ static int cg_solve(lfrv_ctx *c, int W, int H, bool faithful, int max_iter, doub
     };
     const float lambda = 1.0f;  // possion_conj_grad: lambda = 1.0 (solver.cu:541)
     double delta[3];
-    launch_cg_init(W, H, U, gx, gy, r, d, faithful, part, s, c->launches);
+    launch_cg_init(W, H, U, gx, gy, r, d, true, part, s, c->launches);
     check_launch("cg init");
     reduce3(delta);
-    int it = 0;
-    if (faithful) {
-        double dAlpha[3] = {0, 0, 0};
-        const float beta[3] = {1.0f, 1.0f, 1.0f};
-        for (it = 0; it < 5; ++it) {
-            double dq[3], rr[3];
-            launch_cg_apply(W, H, d, lambda, q, part, s, c->launches);
-            check_launch("cg apply");
-            reduce3(dq);
-            float alpha[3];
-            for (int ch = 0; ch < 3; ++ch) {
-                dAlpha[ch] += dq[ch];
-                alpha[ch] = (float)delta[ch] / (float)dAlpha[ch];
-            }
-            launch_cg_update(W, H, alpha, d, q, U, r, part, s, c->launches);
-            check_launch("cg update");
-            reduce3(rr);
-            for (int ch = 0; ch < 3; ++ch) dAlpha[ch] = (double)alpha[ch] + rr[ch];
-            launch_cg_dir(W, H, beta, r, d, s, c->launches);
-            check_launch("cg dir");
-        }
-        if (gap_out) *gap_out = 0.0;
-        return it;
-    }
-    // E(u) by one FP64 pass; then E_{k+1} = E_k - alpha_k delta_k / 2 and the certificate
-    // E(u) - E* <= ||r||^2 / (2 lambda).
-    double E;
-    {
-        launch_cg_energy(W, H, U, U0, gx, gy, part, s, c->launches);
-        check_launch("cg energy");
-        double e3[3];
-        reduce3(e3);
-        E = e3[0] + e3[1] + e3[2];
-    }
-    double gap = 1e300;
-    for (it = 0;; ++it) {
-        const double bound = (delta[0] + delta[1] + delta[2]) / (2.0 * (double)lambda);
-        gap = (E - bound) > 0 ? bound / (E - bound) : 1e300;
-        if (it >= max_iter || (gap_tol > 0 && gap <= gap_tol)) break;
+    double dAlpha[3] = {0, 0, 0};
+    const float beta[3] = {1.0f, 1.0f, 1.0f};
+    int it;
+    for (it = 0; it < 5; ++it) {
         double dq[3], rr[3];
         launch_cg_apply(W, H, d, lambda, q, part, s, c->launches);
         check_launch("cg apply");
         reduce3(dq);
         float alpha[3];
-        double alpha_d[3];
         for (int ch = 0; ch < 3; ++ch) {
-            alpha_d[ch] = (dq[ch] > 0) ? delta[ch] / dq[ch] : 0.0;
-            alpha[ch] = (float)alpha_d[ch];
+            dAlpha[ch] += dq[ch];
+            alpha[ch] = (float)delta[ch] / (float)dAlpha[ch];
         }
         launch_cg_update(W, H, alpha, d, q, U, r, part, s, c->launches);
         check_launch("cg update");
         reduce3(rr);
-        float beta[3];
-        for (int ch = 0; ch < 3; ++ch) {
-            E -= 0.5 * alpha_d[ch] * delta[ch];
-            beta[ch] = (delta[ch] > 0) ? (float)(rr[ch] / delta[ch]) : 0.0f;
-            delta[ch] = rr[ch];
-        }
+        for (int ch = 0; ch < 3; ++ch) dAlpha[ch] = (double)alpha[ch] + rr[ch];
         launch_cg_dir(W, H, beta, r, d, s, c->launches);
         check_launch("cg dir");
     }
-    if (gap_out) *gap_out = gap;
     return it;
+}
+
+// Corrected CG: one persistent launch (FP32 iterates, FP64 dot products, certified-gap stop on the device).
+static void cg_persistent_async(lfrv_ctx *c, int W, int H, int max_iter, double gap_tol, const float *gx,
+                                const float *gy, float *U) {
+    Workspace &ws = c->ws;
+    const size_t N = (size_t)W * H;
+    ws.r.ensure(3 * N * sizeof(float));
+    ws.d.ensure(3 * N * sizeof(float));
+    ws.q.ensure(3 * N * sizeof(float));
+    const size_t np = (size_t)persistent_partials();
+    double *part = partial_buf(c, 8 * np);
+    const GridBarrier gb = fresh_barrier(c);
+    LFRV_CUDA(launch_cg_persistent(W, H, gx, gy, U, ws.r.as<float>(), ws.d.as<float>(), ws.q.as<float>(), part,
+                                   part + 4 * np, gb, max_iter, gap_tol, solver_state(c), c->stream, c->launches));
+    c->pending.cg = true;
 }
 
 static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
@@ -571,32 +543,52 @@ static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img
     const Buckets B = build_buckets(c, G, tau2);
     ColorBuffers b = color_buffers(c, G);
     ws.mask.ensure(N * sizeof(float));
-    launch_vis_any(G, B, tau2, b.vis, s, c->launches);  // setup_target_visibility
-    check_launch("visibility");
-    // compute_weights with U = 0: the unmasked Sobel of 0 is 0 (sources/gradientIBR.cu:575-577)
-    LFRV_CUDA(cudaMemsetAsync(b.gx, 0, N * sizeof(float), s));
-    LFRV_CUDA(cudaMemsetAsync(b.gy, 0, N * sizeof(float), s));
-    launch_weights(G, b.gx, b.gy, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, s, c->launches);
+    // compute_weights with U = 0 (sources/gradientIBR.cu:575-577): the unmasked Sobel of 0 is 0, so the
+    // gathered gradient is 0 and the weights reduce to the deformation weights over sigma^2
+    launch_weights(G, nullptr, nullptr, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, s, c->launches);
     check_launch("weights");
+    // visibility, weighted average and gradient splat in one pass of the inverse map
+    float *vg = view_gradients(c, G, img);
     float *U = ws.U.as<float>();
-    int hf = 0;
-    if (init) {
-        LFRV_CUDA(cudaMemcpyAsync(U, init, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    } else {
-        launch_initial_image(G, B, tau2, img, b.wgt, U, b.norm, s, c->launches);
-        check_launch("initial image");
-        hf = hole_fill(c, G.W, G.H, b.vis, U, cfg.hole_fill_iter);
-    }
-    u_gradient(c, G, B, img, tau2, b.wgt, s2, b.gx, b.gy, ws.mask.as<float>());
-    double gap = 0;
-    const int it = cg_solve(c, G.W, G.H, cfg.faithful != 0, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U, &gap);
+    launch_gradient_setup(G, B, tau2, img, vg, b.wgt, s2, b.vis, U, b.gx, b.gy, ws.mask.as<float>(), s, c->launches);
+    check_launch("gradient set-up");
+    c->pending = Pending{};
+    if (init) LFRV_CUDA(cudaMemcpyAsync(U, init, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    else hole_fill_async(c, G.W, G.H, b.vis, U, cfg.hole_fill_iter);
+    int it_faithful = 0;
+    if (cfg.faithful) it_faithful = cg_faithful(c, G.W, G.H, b.gx, b.gy, U);
+    else cg_persistent_async(c, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U);
     LFRV_CUDA(cudaMemcpyAsync(out, U, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    c->pending.stats = st;
+    c->pending.gap_tol = cfg.cg_gap_tol;
     if (st) {
-        st->outer_iterations = it;
-        st->hole_fill_iterations = hf;
-        st->gap = gap;
-        st->stop_reason = (!cfg.faithful && cfg.cg_gap_tol > 0 && gap <= cfg.cg_gap_tol) ? 4 : 0;
+        st->outer_iterations = it_faithful;
+        st->hole_fill_iterations = 0;
+        st->gap = 0;
+        st->stop_reason = 0;
     }
+}
+
+// After the stream has completed: solver statistics kept on the device, and the barrier status.
+void finish_stats(lfrv_ctx *c) {
+    Pending &p = c->pending;
+    if (!p.cg && !p.hole_fill) return;
+    double state[16];
+    int bar[8];
+    LFRV_CUDA(cudaMemcpy(state, c->ws.state.p, sizeof(state), cudaMemcpyDeviceToHost));
+    LFRV_CUDA(cudaMemcpy(bar, c->ws.barrier.p, sizeof(bar), cudaMemcpyDeviceToHost));
+    const bool timeout = bar[4] != 0;
+    if (p.stats) {
+        if (p.hole_fill) p.stats->hole_fill_iterations = (int)state[8];
+        if (p.cg) {
+            p.stats->outer_iterations = (int)state[5];
+            p.stats->gap = state[4];
+            p.stats->energy = state[3];
+            p.stats->stop_reason = (p.gap_tol > 0 && state[4] <= p.gap_tol) ? 4 : 0;
+        }
+    }
+    p = Pending{};
+    if (timeout) raise(LFRV_E_TIMEOUT, "a device-side grid barrier gave up waiting (persistent solver)");
 }
 
 // ------------------------------------------------------------------ warp stage
@@ -626,7 +618,7 @@ static void inv3(const double *m, double *o) {
 }
 
 // Folds view k and target u into M = K_u R_u R_k^T K_k^-1, b = K_u (t_u - R_u R_k^T t_k).
-static DevCamera fold_camera(const lfrv_camera &k, const lfrv_camera &u) {
+static void fold_camera(const lfrv_camera &k, const lfrv_camera &u, float *Mout, float *bout) {
     double Kk[9], Rk[9], Ku[9], Ru[9], Kki[9], RkT[9];
     for (int i = 0; i < 9; ++i) {
         Kk[i] = k.K[i];
@@ -649,48 +641,36 @@ static DevCamera fold_camera(const lfrv_camera &k, const lfrv_camera &u) {
         for (int c = 0; c < 3; ++c) sacc += RuRkT[3 * r + c] * k.t[c];
         v[r] = u.t[r] - sacc;
     }
-    DevCamera d;
-    std::memset(&d, 0, sizeof(d));
-    for (int i = 0; i < 9; ++i) d.M[i] = (float)M[i];
+    for (int i = 0; i < 9; ++i) Mout[i] = (float)M[i];
     for (int r = 0; r < 3; ++r) {
         double sacc = 0;
         for (int c = 0; c < 3; ++c) sacc += Ku[3 * r + c] * v[c];
-        d.t[r] = (float)sacc;
+        bout[r] = (float)sacc;
     }
-    d.W = u.width;
-    d.H = u.height;
-    return d;
 }
 
 static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfrv_camera *cams,
                  const lfrv_camera *target, float *tau3, float *dpart3, float *tau2, float *dp2, float *zbuf_out) {
-    if (V < 1 || V > 255 || w <= 0 || h <= 0 || !depth || !cams || !target) raise(LFRV_E_ARG, "bad warp arguments");
+    if (V < 1 || V > kMaxViews || w <= 0 || h <= 0 || !depth || !cams || !target)
+        raise(LFRV_E_ARG, "bad warp arguments");
     Workspace &ws = c->ws;
     const int W = target->width, H = target->height;
     if (W <= 0 || H <= 0) raise(LFRV_E_ARG, "bad target size");
     const size_t N = (size_t)W * H;
-    std::vector<DevCamera> dc(V);
-    for (int v = 0; v < V; ++v) dc[v] = fold_camera(cams[v], *target);
-    DevCamera tgt;
-    std::memset(&tgt, 0, sizeof(tgt));
-    tgt.W = W;
-    tgt.H = H;
-    ws.cams.ensure(sizeof(DevCamera) * V);
-    LFRV_CUDA(cudaMemcpyAsync(ws.cams.p, dc.data(), sizeof(DevCamera) * V, cudaMemcpyHostToDevice, c->stream));
+    // the folded cameras travel as a kernel parameter: no upload, no host synchronisation
+    WarpCams wc;
+    std::memset(&wc, 0, sizeof(wc));
+    for (int v = 0; v < V; ++v) fold_camera(cams[v], *target, wc.M[v], wc.b[v]);
     ws.zkey.ensure(sizeof(unsigned long long) * N);
     ws.zbuf.ensure(sizeof(float) * N);
     launch_zbuffer_clear(W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
-    launch_zbuffer_splat(V, w, h, depth, ws.cams.as<DevCamera>(), tgt, ws.zkey.as<unsigned long long>(), c->stream,
-                         c->launches);
+    launch_zbuffer_splat(V, w, h, depth, wc, W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
     launch_zbuffer_resolve(W, H, ws.zkey.as<unsigned long long>(), ws.zbuf.as<float>(), c->stream, c->launches);
     check_launch("z-buffer");
-    launch_tau(V, w, h, depth, ws.cams.as<DevCamera>(), tgt, ws.zbuf.as<float>(), tau3, dpart3, tau2, dp2, c->stream,
-               c->launches);
+    launch_tau(V, w, h, depth, wc, W, H, ws.zbuf.as<float>(), tau3, dpart3, tau2, dp2, c->stream, c->launches);
     check_launch("tau");
     if (zbuf_out)
         LFRV_CUDA(cudaMemcpyAsync(zbuf_out, ws.zbuf.p, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->stream));
-    // host copies of the cameras must stay alive until the copy completes
-    sync(c);
 }
 
 // ------------------------------------------------------------------ helpers for host-buffer entry points
@@ -733,6 +713,7 @@ static void end_timing(lfrv_ctx *c, lfrv_stats *st, long long launches0) {
         st->seconds = ms * 1e-3;
         st->kernel_launches = (int)(c->launches.n - launches0);
     }
+    finish_stats(c);
 }
 
 }  // namespace lfrv
@@ -1223,10 +1204,15 @@ extern "C" int lfrv_stage_hole_fill(lfrv_ctx *ctx, int W, int H, int max_iter, c
     HostIO io{ctx};
     io.up(ctx->ws.U, U, 3 * N);
     io.up(ctx->ws.vis, vis, N);
-    const int it = hole_fill(ctx, W, H, ctx->ws.vis.as<uint8_t>(), ctx->ws.U.as<float>(), max_iter);
-    if (iterations) *iterations = it;
+    lfrv_stats st;
+    std::memset(&st, 0, sizeof(st));
+    ctx->pending = Pending{};
+    hole_fill_async(ctx, W, H, ctx->ws.vis.as<uint8_t>(), ctx->ws.U.as<float>(), max_iter);
+    ctx->pending.stats = &st;
     io.down(U, ctx->ws.U.as<float>(), 3 * N);
     sync(ctx);
+    finish_stats(ctx);
+    if (iterations) *iterations = st.hole_fill_iterations;
     LFRV_API_END
 }
 
@@ -1260,10 +1246,22 @@ extern "C" int lfrv_stage_cg(lfrv_ctx *ctx, int W, int H, int faithful, int max_
     io.up(ctx->ws.gx, gx, N);
     io.up(ctx->ws.gy, gy, N);
     io.up(ctx->ws.U, U, 3 * N);
-    const int it = cg_solve(ctx, W, H, faithful != 0, max_iter, gap_tol, ctx->ws.gx.as<float>(),
-                            ctx->ws.gy.as<float>(), ctx->ws.U.as<float>(), gap);
-    if (iterations) *iterations = it;
+    lfrv_stats st;
+    std::memset(&st, 0, sizeof(st));
+    ctx->pending = Pending{};
+    if (faithful) {
+        st.outer_iterations = cg_faithful(ctx, W, H, ctx->ws.gx.as<float>(), ctx->ws.gy.as<float>(),
+                                          ctx->ws.U.as<float>());
+    } else {
+        cg_persistent_async(ctx, W, H, max_iter, gap_tol, ctx->ws.gx.as<float>(), ctx->ws.gy.as<float>(),
+                            ctx->ws.U.as<float>());
+        ctx->pending.stats = &st;
+        ctx->pending.gap_tol = gap_tol;
+    }
     io.down(U, ctx->ws.U.as<float>(), 3 * N);
     sync(ctx);
+    finish_stats(ctx);
+    if (iterations) *iterations = st.outer_iterations;
+    if (gap) *gap = st.gap;
     LFRV_API_END
 }

@@ -40,22 +40,22 @@ struct Buckets {
 };
 
 // ---- warp stage (kernels_warp.cu)
-struct DevCamera {
-    float K[9], R[9], t[3], Kinv[9];
-    // M = K_u R_u R_k^T K_k^-1 for input cameras (filled per view by the host)
-    float M[9];
-    int W, H;
+// Per input view, the cameras folded by the host: x_h = M (z (x, y, 1)) + b with M = K_u R_u R_k^T K_k^-1 and
+// b = K_u (t_u - R_u R_k^T t_k). Passed by value as a kernel parameter (at most kMaxViews views).
+constexpr int kMaxViews = 255;
+struct WarpCams {
+    float M[kMaxViews][9];
+    float b[kMaxViews][3];
 };
 void launch_zbuffer_clear(int W, int H, unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc);
-void launch_zbuffer_splat(int V, int w, int h, const float *depth, const DevCamera *cams_dev, const DevCamera &target,
+void launch_zbuffer_splat(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H,
                           unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc);
 void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float *zbuf, cudaStream_t st,
                             LaunchCounter &lc);
 // tau3/dpart3: reference format (V x 3 x n); tau2/dp2: solver format (V x 2 x n), dp2 premultiplied by sigma_z.
 // Any output may be null.
-void launch_tau(int V, int w, int h, const float *depth, const DevCamera *cams_dev, const DevCamera &target,
-                const float *zbuf, float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st,
-                LaunchCounter &lc);
+void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H, const float *zbuf,
+                float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc);
 
 // ---- solver stage (kernels_solver.cu)
 void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc);
@@ -77,6 +77,9 @@ void launch_regweight(const Geometry &G, const Buckets &B, const float *tau, con
                       LaunchCounter &lc);
 void launch_u_gradient(const Geometry &G, const Buckets &B, const float *tau, const float *vgrad, const float *wgt,
                        float s2, float *gx, float *gy, float *mask, cudaStream_t st, LaunchCounter &lc);
+void launch_gradient_setup(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *vgrad,
+                           const float *wgt, float s2, uint8_t *vis, float *U, float *gx, float *gy, float *mask,
+                           cudaStream_t st, LaunchCounter &lc);
 void launch_sobel(int W, int H, int count, const float *rgb, size_t in_stride, size_t ch_stride, float *gx, float *gy,
                   size_t out_stride, const uint8_t *vis, double *abs_partial, cudaStream_t st, LaunchCounter &lc);
 int sobel_partials(int W, int H);
@@ -116,6 +119,20 @@ void launch_cg_update(int W, int H, const float alpha[3], const float *d, const 
 void launch_cg_dir(int W, int H, const float beta[3], const float *r, float *d, cudaStream_t st, LaunchCounter &lc);
 void launch_reduce_segments(int count, int nseg, const double *partial, double *out, cudaStream_t st, LaunchCounter &lc);
 int cg_partials(int W, int H);
+
+// Persistent (cooperative) solvers. The grid barrier's counter and error flag are zeroed before each launch;
+// a barrier wait that exceeds its spin limit sets *err = 1 and the kernel returns.
+struct GridBarrier {
+    unsigned int *count;
+    int *err;
+};
+int persistent_partials();  // upper bound of blocks (partials per slot)
+cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
+                                 float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
+                                 double *state, cudaStream_t st, LaunchCounter &lc);
+cudaError_t launch_hole_fill_persistent(int W, int H, const int *holes, const int *count, float *A, float *B,
+                                        double *part, GridBarrier gb, int max_iter, double *state, cudaStream_t st,
+                                        LaunchCounter &lc);
 void launch_cg_energy(int W, int H, const float *U, const float *U0, const float *gx, const float *gy, double *partial,
                       cudaStream_t st, LaunchCounter &lc);
 

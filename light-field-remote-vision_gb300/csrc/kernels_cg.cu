@@ -13,34 +13,69 @@
 
 namespace lfrv {
 
-// Hole list in raster order: per-row counts, an exclusive scan over rows, per-row writes.
+// Hole list in raster order: one warp per row counts its holes (ballot), one block scans the row counts,
+// one warp per row writes its holes in order.
 __global__ void k_hole_rows(int W, int H, const uint8_t *__restrict__ vis, int *__restrict__ row_count) {
-    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (y >= H) return;
     int c = 0;
-    for (int x = 0; x < W; ++x) c += vis[(size_t)y * W + x] ? 0 : 1;
-    row_count[y] = c;
+    for (int x0 = 0; x0 < W; x0 += 32) {
+        const int x = x0 + lane;
+        const bool hole = (x < W) && !vis[(size_t)y * W + x];
+        c += __popc(__ballot_sync(0xffffffffu, hole));
+    }
+    if (lane == 0) row_count[y] = c;
 }
 
+// Exclusive scan of H row counts in one block of 1024 threads (chunks of 1024 rows).
 __global__ void k_hole_scan(int H, int *__restrict__ row_count, int *__restrict__ total) {
-    // single thread: H <= 16384 rows
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    int s = 0;
-    for (int y = 0; y < H; ++y) {
-        const int c = row_count[y];
-        row_count[y] = s;
-        s += c;
+    __shared__ int warp_tot[32];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int base = 0; base < H; base += 1024) {
+        const int y = base + threadIdx.x;
+        const int v = (y < H) ? row_count[y] : 0;
+        int incl = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
+        }
+        if (lane == 31) warp_tot[wid] = incl;
+        __syncthreads();
+        if (wid == 0) {
+            int wt = warp_tot[lane];
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, wt, o);
+                if (lane >= o) wt += t;
+            }
+            warp_tot[lane] = wt;  // inclusive over warps
+        }
+        __syncthreads();
+        const int before = (wid > 0) ? warp_tot[wid - 1] : 0;
+        if (y < H) row_count[y] = carry + before + incl - v;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_tot[31];
+        __syncthreads();
     }
-    *total = s;
+    if (threadIdx.x == 0) *total = carry;
 }
 
 __global__ void k_hole_write(int W, int H, const uint8_t *__restrict__ vis, const int *__restrict__ row_start,
                              int *__restrict__ holes) {
-    const int y = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (y >= H) return;
     int k = row_start[y];
-    for (int x = 0; x < W; ++x)
-        if (!vis[(size_t)y * W + x]) holes[k++] = y * W + x;
+    for (int x0 = 0; x0 < W; x0 += 32) {
+        const int x = x0 + lane;
+        const bool hole = (x < W) && !vis[(size_t)y * W + x];
+        const unsigned int m = __ballot_sync(0xffffffffu, hole);
+        if (hole) holes[k + __popc(m & ((1u << lane) - 1u))] = y * W + x;
+        k += __popc(m);
+    }
 }
 
 // One Jacobi step on the holes; partial = sum over holes of lap * U_new for channel 2 (the reference keeps
@@ -233,6 +268,260 @@ __global__ void __launch_bounds__(256) k_cg_energy(int W, int H, const float *__
     cg_block3(acc[0], acc[1], acc[2], partial);
 }
 
+// ====================================================================== persistent solvers
+// One cooperative launch runs a whole iteration loop; phases are separated by the bounded grid barrier of
+// device_common.cuh. Values written by other blocks inside the launch are read through L2 (__ldcg).
+constexpr int kPersistThreads = 512;
+
+// Sums `count` FP64 partials per slot in a fixed order (identical in every block).
+__device__ void block_reduce_partials(const double *partial, int count, int nslots, double *out_smem) {
+    __shared__ double red[kPersistThreads / 32][4];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int sl = 0; sl < nslots; ++sl) {
+        double s = 0.0;
+        for (int i = threadIdx.x; i < count; i += blockDim.x) s += __ldcg(partial + (size_t)sl * count + i);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) red[wid][sl] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < nslots) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += red[w][threadIdx.x];
+        out_smem[threadIdx.x] = t;
+    }
+    __syncthreads();
+}
+
+// Block sum of up to 4 per-thread values into partial[slot * gridDim.x + blockIdx.x].
+__device__ void block_partials(const double v[4], int nslots, double *partial) {
+    __shared__ double red[kPersistThreads / 32][4];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int sl = 0; sl < nslots; ++sl) {
+        double s = v[sl];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) red[wid][sl] = s;
+    }
+    __syncthreads();
+    if (threadIdx.x < nslots) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += red[w][threadIdx.x];
+        partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+    }
+    __syncthreads();
+}
+
+__device__ __forceinline__ float ldcg_op(const float *d, int W, int H, int x, int y, size_t o, float lambda) {
+    const float c = __ldcg(d + o);
+    float lx, ly;
+    if (x == 0) lx = c - __ldcg(d + o + 1);
+    else if (x < W - 1) lx = 2.f * c - __ldcg(d + o - 1) - __ldcg(d + o + 1);
+    else lx = c - __ldcg(d + o - 1);
+    if (y == 0) ly = c - __ldcg(d + o + W);
+    else if (y < H - 1) ly = 2.f * c - __ldcg(d + o - W) - __ldcg(d + o + W);
+    else ly = c - __ldcg(d + o - W);
+    return lambda * c + lx + ly;
+}
+
+// d_new = r + beta d_old evaluated at any pixel (the direction update folded into the operator pass).
+__device__ __forceinline__ float dnew_at(const float *r, const float *d, float beta, size_t o) {
+    return __ldcg(r + o) + beta * __ldcg(d + o);
+}
+
+// Corrected CG of the IBR_gradient normal equations, all iterations in one launch. State layout (doubles):
+// [0..2] delta, [3] E, [4] gap, [5] iterations, [6] status (0 ok, 1 barrier timeout).
+__global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H, const float *__restrict__ gX,
+                                                                   const float *__restrict__ gY, float *U, float *r,
+                                                                   float *dA, float *dB, double *partA,
+                                                                   double *partB, GridBarrier gb, int max_iter,
+                                                                   double gap_tol, double *state) {
+    __shared__ double sh[8];
+    const size_t N = (size_t)W * H;
+    const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nthr = (size_t)gridDim.x * blockDim.x;
+    const float lambda = 1.0f;
+    unsigned int gen = 0;
+    // ---- phase 0: r = b - A x (initConjGrad, solver.cu:383-467) and E(x0) = 1/2 ||grad x0 - g||^2 (x0 = u0)
+    {
+        double acc[4] = {0, 0, 0, 0};
+        for (size_t o = tid; o < N; o += nthr) {
+            const int x = (int)(o % W), y = (int)(o / W);
+            const float gxo = __ldg(gX + o), gyo = __ldg(gY + o);
+            const float gxl = (x > 0) ? __ldg(gX + o - 1) : 0.f, gyu = (y > 0) ? __ldg(gY + o - W) : 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float *u = U + c * N;
+                const float uc = __ldcg(u + o);
+                float lx, ly;
+                if (x == 0) lx = uc - __ldcg(u + o + 1) + gxo;
+                else if (x < W - 1) lx = 2.f * uc - __ldcg(u + o - 1) - __ldcg(u + o + 1) + gxo - gxl;
+                else lx = uc - __ldcg(u + o - 1) - gxl;
+                if (y == 0) ly = uc - __ldcg(u + o + W) + gyo;
+                else if (y < H - 1) ly = 2.f * uc - __ldcg(u + o - W) - __ldcg(u + o + W) + gyo - gyu;
+                else ly = uc - __ldcg(u + o - W) - gyu;
+                const float rv = -(lx + ly);
+                r[c * N + o] = rv;
+                acc[c] += (double)(rv * rv);
+                float e = 0.f;
+                if (x < W - 1) {
+                    const float a = __ldcg(u + o + 1) - uc - gxo;
+                    e += a * a;
+                }
+                if (y < H - 1) {
+                    const float a = __ldcg(u + o + W) - uc - gyo;
+                    e += a * a;
+                }
+                acc[3] += 0.5 * (double)e;
+            }
+        }
+        block_partials(acc, 4, partB);
+    }
+    if (!grid_sync(gb, gen)) return;
+    block_reduce_partials(partB, gridDim.x, 4, sh);
+    double delta[3] = {sh[0], sh[1], sh[2]};
+    double E = sh[3];
+    float beta[3] = {0.f, 0.f, 0.f};
+    const float *dold = r;  // d_0 = r_0 (beta = 0)
+    float *dnew = dA;
+    double gap = 1e300;
+    int it = 0;
+    for (;; ++it) {
+        const double bound = (delta[0] + delta[1] + delta[2]) / (2.0 * (double)lambda);
+        gap = (E - bound) > 0 ? bound / (E - bound) : 1e300;
+        if (it >= max_iter || (gap_tol > 0 && gap <= gap_tol)) break;
+        // ---- phase A: d = r + beta d_old, q = A d, d . q
+        {
+            double acc[4] = {0, 0, 0, 0};
+            for (size_t o = tid; o < N; o += nthr) {
+                const int x = (int)(o % W), y = (int)(o / W);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float *rc = r + c * N, *dc = dold + c * N;
+                    const float b = beta[c];
+                    const float dcv = dnew_at(rc, dc, b, o);
+                    float lx, ly;
+                    if (x == 0) lx = dcv - dnew_at(rc, dc, b, o + 1);
+                    else if (x < W - 1) lx = 2.f * dcv - dnew_at(rc, dc, b, o - 1) - dnew_at(rc, dc, b, o + 1);
+                    else lx = dcv - dnew_at(rc, dc, b, o - 1);
+                    if (y == 0) ly = dcv - dnew_at(rc, dc, b, o + W);
+                    else if (y < H - 1) ly = 2.f * dcv - dnew_at(rc, dc, b, o - W) - dnew_at(rc, dc, b, o + W);
+                    else ly = dcv - dnew_at(rc, dc, b, o - W);
+                    const float qv = lambda * dcv + lx + ly;
+                    dnew[c * N + o] = dcv;
+                    acc[c] += (double)(dcv * qv);
+                }
+            }
+            block_partials(acc, 3, partA);
+        }
+        if (!grid_sync(gb, gen)) return;
+        block_reduce_partials(partA, gridDim.x, 3, sh);
+        float alpha[3];
+        double alpha_d[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            alpha_d[c] = (sh[c] > 0) ? delta[c] / sh[c] : 0.0;
+            alpha[c] = (float)alpha_d[c];
+            E -= 0.5 * alpha_d[c] * delta[c];
+        }
+        // ---- phase B: x += alpha d, r -= alpha A d, r . r
+        {
+            double acc[4] = {0, 0, 0, 0};
+            for (size_t o = tid; o < N; o += nthr) {
+                const int x = (int)(o % W), y = (int)(o / W);
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float *dc = dnew + c * N;
+                    const float qv = ldcg_op(dc, W, H, x, y, o, lambda);
+                    const float dv = __ldcg(dc + o);
+                    U[c * N + o] = __ldcg(U + c * N + o) + alpha[c] * dv;
+                    const float rv = __ldcg(r + c * N + o) - alpha[c] * qv;
+                    r[c * N + o] = rv;
+                    acc[c] += (double)(rv * rv);
+                }
+            }
+            block_partials(acc, 3, partB);
+        }
+        if (!grid_sync(gb, gen)) return;
+        block_reduce_partials(partB, gridDim.x, 3, sh);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            beta[c] = (delta[c] > 0) ? (float)(sh[c] / delta[c]) : 0.f;
+            delta[c] = sh[c];
+        }
+        dold = dnew;
+        dnew = (dnew == dA) ? dB : dA;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        state[0] = delta[0];
+        state[1] = delta[1];
+        state[2] = delta[2];
+        state[3] = E;
+        state[4] = gap;
+        state[5] = (double)it;
+    }
+}
+
+// Hole filling with the whole iteration loop in one launch (hole_filling, sources/gradientIBR.cu:87-152).
+// count: device pointer to the number of holes. A holds the initial image (and the result); B is a copy.
+// state: [0] iterations.
+__global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W, int H, const int *__restrict__ holes,
+                                                                          const int *__restrict__ count, float *A,
+                                                                          float *B, double *part, GridBarrier gb,
+                                                                          int max_iter, double *state) {
+    __shared__ double sh[8];
+    const size_t N = (size_t)W * H;
+    const int nh = *count;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+    unsigned int gen = 0;
+    float *src = A, *dst = B;
+    float energy = 0.0f, previous = 0.0f;
+    int k;
+    for (k = 0; k < max_iter; ++k) {
+        previous = energy;
+        double acc[4] = {0, 0, 0, 0};
+        for (int h = tid; h < nh; h += nthr) {
+            const int o = __ldg(holes + h);
+            const int ox = o % W, oy = o / W;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float *u = src + c * N;
+                float v = 0.f, wt = 0.f;
+                if (ox > 0) { v += __ldcg(u + o - 1); wt += 1.f; }
+                if (oy > 0) { v += __ldcg(u + o - W); wt += 1.f; }
+                if (ox < W - 1) { v += __ldcg(u + o + 1); wt += 1.f; }
+                if (oy < H - 1) { v += __ldcg(u + o + W); wt += 1.f; }
+                v /= wt;
+                const float uc = __ldcg(u + o);
+                const float lap = v - uc;
+                const float un = uc + lap;
+                dst[c * N + o] = un;
+                if (c == 2) acc[0] += (double)(lap * un);
+            }
+        }
+        block_partials(acc, 1, part);
+        if (!grid_sync(gb, gen)) return;
+        block_reduce_partials(part, gridDim.x, 1, sh);
+        energy = (float)sh[0];
+        float *t = src;
+        src = dst;
+        dst = t;
+        if (fabsf(previous - energy) < 1e-3f) {
+            ++k;
+            break;
+        }
+        // partials are rewritten next iteration only after every block has read them
+        if (!grid_sync(gb, gen)) return;
+    }
+    if (src != A) {  // copy the holes of the result back into A
+        for (int h = tid; h < nh; h += nthr) {
+            const int o = __ldg(holes + h);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) A[c * N + o] = __ldcg(src + c * N + o);
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) state[0] = (double)k;
+}
+
 // ------------------------------------------------------------------ launchers
 static inline dim3 cg_grid(int W, int H) { return dim3((W + kCgBX - 1) / kCgBX, (H + kCgBY - 1) / kCgBY); }
 int cg_partials(int W, int H) {
@@ -244,13 +533,57 @@ void launch_hole_list(int W, int H, const uint8_t *vis, int *holes, int *count, 
     ProfScope _ps(lc, "hole_list", st);
     // row starts are kept in holes[N .. N + H) scratch supplied by the caller (holes has N + H entries)
     int *row = holes + (size_t)W * H;
-    k_hole_rows<<<(H + 127) / 128, 128, 0, st>>>(W, H, vis, row);
-    k_hole_scan<<<1, 32, 0, st>>>(H, row, count);
-    k_hole_write<<<(H + 127) / 128, 128, 0, st>>>(W, H, vis, row, holes);
+    const int rows_per_block = 256 / 32;
+    k_hole_rows<<<(H + rows_per_block - 1) / rows_per_block, 256, 0, st>>>(W, H, vis, row);
+    k_hole_scan<<<1, 1024, 0, st>>>(H, row, count);
+    k_hole_write<<<(H + rows_per_block - 1) / rows_per_block, 256, 0, st>>>(W, H, vis, row, holes);
     lc.add(3);
 }
 
 int hole_fill_partials(int nholes) { return (nholes + 255) / 256; }
+
+// Blocks of a cooperative launch: every block must be resident at once (the grid barrier waits for all).
+static int coop_blocks(const void *kernel, int want) {
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistThreads, 0);
+    per_sm = per_sm < 2 ? per_sm : 2;
+    const int resident = sms * per_sm;
+    return want < resident ? (want > 0 ? want : 1) : resident;
+}
+
+int persistent_partials() {
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    return 2 * sms;
+}
+
+cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
+                                 float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
+                                 double *state, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "cg_persistent", st);
+    const size_t N = (size_t)W * H;
+    const int blocks = coop_blocks((const void *)k_cg_persistent, (int)((N + kPersistThreads - 1) / kPersistThreads));
+    void *args[] = {&W, &H, (void *)&gx, (void *)&gy, &U, &r, &dA, &dB, &partA, &partB, &gb, &max_iter, &gap_tol,
+                    &state};
+    lc.add(1);
+    return cudaLaunchCooperativeKernel((const void *)k_cg_persistent, dim3(blocks), dim3(kPersistThreads), args, 0, st);
+}
+
+cudaError_t launch_hole_fill_persistent(int W, int H, const int *holes, const int *count, float *A, float *B,
+                                        double *part, GridBarrier gb, int max_iter, double *state, cudaStream_t st,
+                                        LaunchCounter &lc) {
+    ProfScope _ps(lc, "hole_fill", st);
+    const size_t N = (size_t)W * H;
+    const int blocks =
+        coop_blocks((const void *)k_hole_fill_persistent, (int)((N + kPersistThreads - 1) / kPersistThreads));
+    void *args[] = {&W, &H, (void *)&holes, (void *)&count, &A, &B, &part, &gb, &max_iter, &state};
+    lc.add(1);
+    return cudaLaunchCooperativeKernel((const void *)k_hole_fill_persistent, dim3(blocks), dim3(kPersistThreads), args,
+                                       0, st);
+}
 
 void launch_hole_fill_iter(int W, int H, const int *holes, int nholes, const float *Uin, float *Uout, double *partial,
                            cudaStream_t st, LaunchCounter &lc) {

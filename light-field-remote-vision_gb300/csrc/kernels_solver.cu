@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(256) k_weights(int V, int n, int w, int h, int
     const float *tx = tau + (size_t)v * 2 * n, *ty = tx + n;
     const float txm = tx[m], tym = ty[m];
     float ax = 0.f, ay = 0.f;
-    if (in_gather(txm, tym, W, H)) {
+    if (gx && in_gather(txm, tym, W, H)) {  // gx == nullptr: the target gradient is identically zero
         Footprint fp;
         footprint<KS>(txm, tym, dsf, W, H, fp);
 #pragma unroll
@@ -218,7 +218,8 @@ __device__ __forceinline__ void splat_accumulate(int x, int y, int W, int H, int
                 const unsigned int ent = __ldg(entries + k);
                 const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
                 const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
-                float A = footprint_tap<KS>(tx, ty, dsf, W, H, j, i);
+                float raw;
+                float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw);
                 if (src.scale) A = __ldg(src.scale + (size_t)v * n + m) * A;
                 norm += A;
 #pragma unroll
@@ -268,6 +269,75 @@ __global__ void k_vis_any(int W, int H, int n, int dsf, int BW, const unsigned i
             }
         }
     vis[(size_t)y * W + x] = any ? 1 : 0;
+}
+
+// IBR_gradient set-up in one traversal of the inverse map (per target pixel):
+//   visibility   setup_target_visibility (sources/gradientIBR.cu:40-83): some splatted raw overlap != 0;
+//   weighted average of compute_initial_image (:724-808): U = sum w A v / sum w A;
+//   gradient splat of init_u_gradient (:833-920): (gx, gy, mask) = sum A (Sobel_x, Sobel_y, w) / sum A,
+//   mask scaled by sigma^2.
+// img: per view [3][n]; vgrad: per view [2][n] (Sobel of the view luminance); wgt: per view [n].
+template <int KS>
+__global__ void __launch_bounds__(256) k_gradient_setup(int W, int H, int n, int dsf, int BW,
+                                                        const unsigned int *__restrict__ start,
+                                                        const unsigned int *__restrict__ entries,
+                                                        const float *__restrict__ tau, const float *__restrict__ img,
+                                                        const float *__restrict__ vgrad, const float *__restrict__ wgt,
+                                                        float s2, uint8_t *__restrict__ vis, float *__restrict__ U,
+                                                        float *__restrict__ gx, float *__restrict__ gy,
+                                                        float *__restrict__ mask) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    float u0 = 0.f, u1 = 0.f, u2 = 0.f, wn = 0.f;   // weighted average
+    float g0 = 0.f, g1 = 0.f, g2 = 0.f, nrm = 0.f;  // gradient splat
+    bool any = false;
+#pragma unroll
+    for (int i = 0; i < KS; ++i) {
+#pragma unroll
+        for (int j = 0; j < KS; ++j) {
+            const int ax = x - j, ay = y - i;
+            const size_t b = (size_t)(ay + KS - 1) * BW + (ax + KS - 1);
+            const unsigned int s = __ldg(start + b), e = __ldg(start + b + 1);
+            for (unsigned int k = s; k < e; ++k) {
+                const unsigned int ent = __ldg(entries + k);
+                const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
+                const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
+                float raw;
+                const float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw);
+                any |= (raw != 0.0f);
+                const float w = __ldg(wgt + (size_t)v * n + m);
+                const float wA = w * A;
+                const float *iv = img + (size_t)v * 3 * n;
+                wn += wA;
+                u0 += wA * __ldg(iv + m);
+                u1 += wA * __ldg(iv + n + m);
+                u2 += wA * __ldg(iv + 2 * n + m);
+                const float *gv = vgrad + (size_t)v * 2 * n;
+                nrm += A;
+                g0 += A * __ldg(gv + m);
+                g1 += A * __ldg(gv + n + m);
+                g2 += A * w;
+            }
+        }
+    }
+    const size_t o = (size_t)y * W + x, N = (size_t)W * H;
+    vis[o] = any ? 1 : 0;
+    if (wn != 0.f) {
+        u0 /= wn;
+        u1 /= wn;
+        u2 /= wn;
+    }
+    U[o] = u0;
+    U[N + o] = u1;
+    U[2 * N + o] = u2;
+    if (nrm != 0.f) {
+        g0 /= nrm;
+        g1 /= nrm;
+        g2 /= nrm;
+    }
+    gx[o] = g0;
+    gy[o] = g1;
+    mask[o] = g2 * s2;
 }
 
 // Weighted average (coco_vtv_sr_compute_initial_image sources/optimization.cu:1300-1344):
@@ -662,6 +732,15 @@ void launch_u_gradient(const Geometry &G, const Buckets &B, const float *tau, co
     SplatSrc src{{vgrad, vgrad + G.n, wgt}, {(size_t)2 * G.n, (size_t)2 * G.n, (size_t)G.n}, nullptr};
     LFRV_KS_DISPATCH(G.dsf + 1, k_u_gradient, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW, B.start,
                      B.entries, tau, src, s2, gx, gy, mask);
+    lc.add(1);
+}
+
+void launch_gradient_setup(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *vgrad,
+                           const float *wgt, float s2, uint8_t *vis, float *U, float *gx, float *gy, float *mask,
+                           cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "gradient_setup", st);
+    LFRV_KS_DISPATCH(G.dsf + 1, k_gradient_setup, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW,
+                     B.start, B.entries, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask);
     lc.add(1);
 }
 

@@ -21,11 +21,24 @@ __device__ __forceinline__ void mv3(const float *M, float x, float y, float z, f
 }
 
 // x_h of the point at pixel-space (px, py) with depth z seen from view cam.
-__device__ __forceinline__ void warp_point(const DevCamera &c, float px, float py, float z, float *xh) {
+struct ViewCam {
+    float M[9], b[3];
+};
+
+__device__ __forceinline__ ViewCam view_cam(const WarpCams &cams, int v) {
+    ViewCam c;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) c.M[i] = cams.M[v][i];
+#pragma unroll
+    for (int i = 0; i < 3; ++i) c.b[i] = cams.b[v][i];
+    return c;
+}
+
+__device__ __forceinline__ void warp_point(const ViewCam &c, float px, float py, float z, float *xh) {
     mv3(c.M, z * px, z * py, z, xh);
-    xh[0] += c.t[0];
-    xh[1] += c.t[1];
-    xh[2] += c.t[2];
+    xh[0] += c.b[0];
+    xh[1] += c.b[1];
+    xh[2] += c.b[2];
 }
 
 // ------------------------------------------------------------------ target depth map
@@ -77,12 +90,14 @@ __device__ void raster_tri(const float *v0, const float *v1, const float *v2, fl
             const float iz = (w0 * v0[2] + w1 * v1[2] + w2 * v2[2]) / s;
             if (!(iz > 0.f)) continue;
             const unsigned long long key = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
-            atomicMax(zkey + (size_t)y * W + x, key);
+            unsigned long long *slot = zkey + (size_t)y * W + x;
+            // keys only grow: a candidate already beaten needs no atomic
+            if (__ldcg(slot) < key) atomicMax(slot, key);
         }
 }
 
 __global__ void __launch_bounds__(256) k_zsplat(int V, int w, int h, const float *__restrict__ depth,
-                                                const DevCamera *__restrict__ cams, int W, int H,
+                                                const WarpCams cams, int W, int H,
                                                 unsigned long long *__restrict__ zkey) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     const int v = blockIdx.y;
@@ -91,7 +106,7 @@ __global__ void __launch_bounds__(256) k_zsplat(int V, int w, int h, const float
     const float *dz = depth + (size_t)v * 3 * n;
     const float z = dz[m], zx = dz[n + m], zy = dz[2 * n + m];
     if (z >= 1000.0f * 0.5f) return;  // INVALID_DEPTH / 2 (depthSplatting.geom:21)
-    const DevCamera c = cams[v];
+    const ViewCam c = view_cam(cams, v);
     const float cx = (m % w) + 0.5f, cy = (m / w) + 0.5f;
     float xh[3];
     warp_point(c, cx, cy, z, xh);
@@ -135,7 +150,7 @@ __device__ __forceinline__ float bilinear_clamp(const float *img, int W, int H, 
 }
 
 __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *__restrict__ depth,
-                                             const DevCamera *__restrict__ cams, int W, int H,
+                                             const WarpCams cams, int W, int H,
                                              const float *__restrict__ zbuf, float *__restrict__ tau3,
                                              float *__restrict__ dpart3, float *__restrict__ tau2,
                                              float *__restrict__ dp2) {
@@ -145,7 +160,7 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
     if (m >= n) return;
     const float *dz = depth + (size_t)v * 3 * n;
     const float z = dz[m], zx = dz[n + m], zy = dz[2 * n + m];
-    const DevCamera &c = cams[v];
+    const ViewCam c = view_cam(cams, v);
     const float x = (m % w) + 0.5f, y = (m / w) + 0.5f;
     float xuh[3];
     warp_point(c, x, y, z, xuh);
@@ -207,11 +222,11 @@ void launch_zbuffer_clear(int W, int H, unsigned long long *zkey, cudaStream_t s
     lc.add(1);
 }
 
-void launch_zbuffer_splat(int V, int w, int h, const float *depth, const DevCamera *cams_dev, const DevCamera &target,
+void launch_zbuffer_splat(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H,
                           unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "zbuffer_splat", st);
     const int n = w * h;
-    k_zsplat<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, depth, cams_dev, target.W, target.H, zkey);
+    k_zsplat<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zkey);
     lc.add(1);
 }
 
@@ -222,12 +237,10 @@ void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float 
     lc.add(1);
 }
 
-void launch_tau(int V, int w, int h, const float *depth, const DevCamera *cams_dev, const DevCamera &target,
-                const float *zbuf, float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st,
-                LaunchCounter &lc) {
+void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H, const float *zbuf,
+                float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc) {
     const int n = w * h;
-    k_tau<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, depth, cams_dev, target.W, target.H, zbuf, tau3, dpart3,
-                                                   tau2, dp2);
+    k_tau<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zbuf, tau3, dpart3, tau2, dp2);
     lc.add(1);
 }
 
