@@ -54,9 +54,15 @@ def make_config(lfrv, wl: str, sc):
                                early_exit=0, faithful=1)
 
 
-def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int) -> float | None:
-    """Compulsory DRAM bytes of one launch of `kernel` (FP32 = 4 B)."""
+def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: int = 0) -> float | None:
+    """Compulsory DRAM bytes of one launch of `kernel` (FP32 = 4 B; V views of n pixels, N target pixels)."""
     table = {
+        # r = b - A u0 (g_x, g_y, u read, r written), then per iteration: r, d_old read, d written (phase A);
+        # d, u, r read, u, r written (phase B)
+        "cg_persistent": 32 * N + cg_iters * 96 * N,
+        # inverse map (bucket starts + 4 B entries), per source pixel tau 8 B + colour 12 B + Sobel 8 B +
+        # weight 4 B; vis 1 B, U 12 B, g_x, g_y, mask 12 B written per target pixel
+        "gradient_setup": 4 * N + 4 * V * n + 32 * V * n + 25 * N,
         "zbuffer_splat": 12 * V * n + 8 * N,          # depth (z, dz/dx, dz/dy) read, 64-bit key per target pixel
         "tau": 12 * V * n + 4 * N + 16 * V * n,       # depth + target depth map read, tau and dp written
         "bucket_build": 8 * V * n * 2 + 4 * V * n + 8 * (N + 2 * N),
@@ -223,7 +229,7 @@ def run_ours(args, rank: int, world: int) -> None:
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_n = prof[dom]
     avg_s = dom_ms / 1e3 / dom_n
-    abytes = algorithmic_bytes(dom, V, n, N, ks)
+    abytes = algorithmic_bytes(dom, V, n, N, ks, cg_iters=int(st.outer_iterations))
     peak, peak_kind = measured_peak_hbm()
     roof = None
     if abytes:

@@ -243,6 +243,11 @@ int lfrv_stage_cg(lfrv_ctx *ctx, int W, int H, int faithful, int max_iter, doubl
  * flips on write. Buffers here are top-left origin, planar. */
 int lfrv_pfm_read(const char *path, int *w, int *h, int *channels, float *data, size_t capacity);
 int lfrv_pfm_write(const char *path, int w, int h, int channels, const float *data);
+/* 8-bit PNG as gsl_image_load / gsl_image_save read and write it through Qt (cocolib/cocolib/common/
+ * gsl_image.cpp:539-640): channels scaled by 1/255 on read (grey replicated to RGB, alpha dropped), written
+ * as clamp(int(v * 255), 0, 255). rgb is 3 x h x w. Needs zlib at build time, else LFRV_E_IO. */
+int lfrv_png_read(const char *path, int *w, int *h, float *rgb, size_t capacity);
+int lfrv_png_write(const char *path, int w, int h, const float *rgb);
 
 /* ---------------------------------------------------------------- synthetic light fields
  * No reference counterpart: the reference's datasets are absent, so seeded synthetic scenes stand in

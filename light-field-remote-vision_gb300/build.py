@@ -32,8 +32,16 @@ ORACLE_LIB = ROOT / "oracle" / "liblfrv_oracle.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-std=c++17", "-O3", "-lineinfo", f"-I{INCLUDE}", f"-I{CSRC}",
                "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp"]
-LIB_SOURCES = ["errors.cpp", "io.cpp", "synth.cpp", "host.cpp",
+LIB_SOURCES = ["errors.cpp", "io.cpp", "png.cpp", "synth.cpp", "host.cpp",
                "kernels_solver.cu", "kernels_warp.cu", "kernels_pushpull.cu", "kernels_cg.cu"]
+
+
+def _have_zlib() -> bool:
+    """True when zlib's header and library are present (PNG light fields need it)."""
+    probe = BUILD / "zprobe.c"
+    probe.write_text("#include <zlib.h>\nint main(void){return (int)zlibVersion()[0] == 0;}\n")
+    res = subprocess.run(["gcc", str(probe), "-o", str(BUILD / "zprobe"), "-lz"], capture_output=True)
+    return res.returncode == 0
 
 
 def _nvcc() -> str:
@@ -63,6 +71,7 @@ def _stale(target: Path, deps: list[Path]) -> bool:
 def build_library(force: bool = False, verbose: bool = False) -> Path:
     nvcc = _nvcc()
     BUILD.mkdir(exist_ok=True)
+    zlib = _have_zlib()
     headers = list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [INCLUDE / "lfrv.h"]
     jobs = []
     objs = []
@@ -72,12 +81,15 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
         objs.append(o)
         if force or _stale(o, [s] + headers):
             extra = ["-Xptxas", "-v"] if (verbose and s.suffix == ".cu") else []
+            if zlib and s.name == "png.cpp":
+                extra.append("-DLFRV_HAVE_ZLIB")
             jobs.append([nvcc, *ARCH, *NVCC_COMMON, *extra, "-c", str(s), "-o", str(o)])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:
             list(ex.map(lambda c: _run(c, verbose), jobs))
     if force or jobs or _stale(LIB, objs):
-        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-Xcompiler", "-fopenmp", "-lgomp"], verbose)
+        _run([nvcc, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-Xcompiler", "-fopenmp", "-lgomp",
+              *(["-lz"] if zlib else [])], verbose)
     main_src = CSRC / "ulf_main.cpp"
     if main_src.exists() and (force or _stale(ULF, [main_src, LIB])):
         ULF.parent.mkdir(exist_ok=True)

@@ -8,6 +8,8 @@
 // channel. Its per-pixel operator (updateAlpha :201-310), initial residual (initConjGrad :361-505) and the
 // updates (updateSolution :130-198, updateDir :508-523) are restated here; the dot products are FP64
 // block partials reduced in a fixed order (the reference accumulates float atomics in arbitrary order).
+#include <algorithm>
+
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -324,9 +326,22 @@ __device__ __forceinline__ float ldcg_op(const float *d, int W, int H, int x, in
     return lambda * c + lx + ly;
 }
 
-// d_new = r + beta d_old evaluated at any pixel (the direction update folded into the operator pass).
-__device__ __forceinline__ float dnew_at(const float *r, const float *d, float beta, size_t o) {
-    return __ldcg(r + o) + beta * __ldcg(d + o);
+// Tiles of the persistent CG: kTileX x kTileY pixels staged with a one-pixel halo.
+constexpr int kTileX = 64, kTileY = 16, kHaloX = kTileX + 2, kHaloY = kTileY + 2;
+
+// Operator of updateAlpha (sources/solver.cu:222-271) on a shared-memory tile: (tx, ty) is the pixel's tile
+// position (halo included), (x, y) its image position for the one-sided border differences.
+__device__ __forceinline__ float tile_op(const float (*t)[kHaloX], int tx, int ty, int x, int y, int W, int H,
+                                         float lambda) {
+    const float c = t[ty][tx];
+    float lx, ly;
+    if (x == 0) lx = c - t[ty][tx + 1];
+    else if (x < W - 1) lx = 2.f * c - t[ty][tx - 1] - t[ty][tx + 1];
+    else lx = c - t[ty][tx - 1];
+    if (y == 0) ly = c - t[ty + 1][tx];
+    else if (y < H - 1) ly = 2.f * c - t[ty - 1][tx] - t[ty + 1][tx];
+    else ly = c - t[ty - 1][tx];
+    return lambda * c + lx + ly;
 }
 
 // Corrected CG of the IBR_gradient normal equations, all iterations in one launch. State layout (doubles):
@@ -339,6 +354,8 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
     __shared__ double sh[8];
     const size_t N = (size_t)W * H;
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nthr = (size_t)gridDim.x * blockDim.x;
+    __shared__ float tile[3][kHaloY][kHaloX];
+    const int tiles_x = (W + kTileX - 1) / kTileX, ntiles = tiles_x * ((H + kTileY - 1) / kTileY);
     const float lambda = 1.0f;
     unsigned int gen = 0;
     // ---- phase 0: r = b - A x (initConjGrad, solver.cu:383-467) and E(x0) = 1/2 ||grad x0 - g||^2 (x0 = u0)
@@ -389,27 +406,35 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
         const double bound = (delta[0] + delta[1] + delta[2]) / (2.0 * (double)lambda);
         gap = (E - bound) > 0 ? bound / (E - bound) : 1e300;
         if (it >= max_iter || (gap_tol > 0 && gap <= gap_tol)) break;
-        // ---- phase A: d = r + beta d_old, q = A d, d . q
+        // ---- phase A: d = r + beta d_old on each tile + halo in shared memory, q = A d, d . q
         {
             double acc[4] = {0, 0, 0, 0};
-            for (size_t o = tid; o < N; o += nthr) {
-                const int x = (int)(o % W), y = (int)(o / W);
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float *rc = r + c * N, *dc = dold + c * N;
-                    const float b = beta[c];
-                    const float dcv = dnew_at(rc, dc, b, o);
-                    float lx, ly;
-                    if (x == 0) lx = dcv - dnew_at(rc, dc, b, o + 1);
-                    else if (x < W - 1) lx = 2.f * dcv - dnew_at(rc, dc, b, o - 1) - dnew_at(rc, dc, b, o + 1);
-                    else lx = dcv - dnew_at(rc, dc, b, o - 1);
-                    if (y == 0) ly = dcv - dnew_at(rc, dc, b, o + W);
-                    else if (y < H - 1) ly = 2.f * dcv - dnew_at(rc, dc, b, o - W) - dnew_at(rc, dc, b, o + W);
-                    else ly = dcv - dnew_at(rc, dc, b, o - W);
-                    const float qv = lambda * dcv + lx + ly;
-                    dnew[c * N + o] = dcv;
-                    acc[c] += (double)(dcv * qv);
+            for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+                const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
+                for (int k = threadIdx.x; k < 3 * kHaloY * kHaloX; k += blockDim.x) {
+                    const int c = k / (kHaloY * kHaloX), rem = k % (kHaloY * kHaloX);
+                    const int gx = x0 - 1 + rem % kHaloX, gy = y0 - 1 + rem / kHaloX;
+                    float v = 0.f;
+                    if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+                        const size_t o = c * N + (size_t)gy * W + gx;
+                        v = __ldcg(r + o) + beta[c] * __ldcg(dold + o);
+                    }
+                    tile[c][rem / kHaloX][rem % kHaloX] = v;
                 }
+                __syncthreads();
+                for (int p = threadIdx.x; p < kTileX * kTileY; p += blockDim.x) {
+                    const int lx = p % kTileX, ly = p / kTileX, x = x0 + lx, y = y0 + ly;
+                    if (x >= W || y >= H) continue;
+                    const size_t o = (size_t)y * W + x;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float qv = tile_op(tile[c], lx + 1, ly + 1, x, y, W, H, lambda);
+                        const float dcv = tile[c][ly + 1][lx + 1];
+                        dnew[c * N + o] = dcv;
+                        acc[c] += (double)(dcv * qv);
+                    }
+                }
+                __syncthreads();
             }
             block_partials(acc, 3, partA);
         }
@@ -423,21 +448,33 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
             alpha[c] = (float)alpha_d[c];
             E -= 0.5 * alpha_d[c] * delta[c];
         }
-        // ---- phase B: x += alpha d, r -= alpha A d, r . r
+        // ---- phase B: x += alpha d, r -= alpha A d, r . r (d tile + halo in shared memory)
         {
             double acc[4] = {0, 0, 0, 0};
-            for (size_t o = tid; o < N; o += nthr) {
-                const int x = (int)(o % W), y = (int)(o / W);
-#pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float *dc = dnew + c * N;
-                    const float qv = ldcg_op(dc, W, H, x, y, o, lambda);
-                    const float dv = __ldcg(dc + o);
-                    U[c * N + o] = __ldcg(U + c * N + o) + alpha[c] * dv;
-                    const float rv = __ldcg(r + c * N + o) - alpha[c] * qv;
-                    r[c * N + o] = rv;
-                    acc[c] += (double)(rv * rv);
+            for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+                const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
+                for (int k = threadIdx.x; k < 3 * kHaloY * kHaloX; k += blockDim.x) {
+                    const int c = k / (kHaloY * kHaloX), rem = k % (kHaloY * kHaloX);
+                    const int gx = x0 - 1 + rem % kHaloX, gy = y0 - 1 + rem / kHaloX;
+                    tile[c][rem / kHaloX][rem % kHaloX] =
+                        (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __ldcg(dnew + c * N + (size_t)gy * W + gx) : 0.f;
                 }
+                __syncthreads();
+                for (int p = threadIdx.x; p < kTileX * kTileY; p += blockDim.x) {
+                    const int lx = p % kTileX, ly = p / kTileX, x = x0 + lx, y = y0 + ly;
+                    if (x >= W || y >= H) continue;
+                    const size_t o = (size_t)y * W + x;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float qv = tile_op(tile[c], lx + 1, ly + 1, x, y, W, H, lambda);
+                        const float dv = tile[c][ly + 1][lx + 1];
+                        U[c * N + o] = __ldcg(U + c * N + o) + alpha[c] * dv;
+                        const float rv = __ldcg(r + c * N + o) - alpha[c] * qv;
+                        r[c * N + o] = rv;
+                        acc[c] += (double)(rv * rv);
+                    }
+                }
+                __syncthreads();
             }
             block_partials(acc, 3, partB);
         }
@@ -565,7 +602,9 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
                                  double *state, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "cg_persistent", st);
     const size_t N = (size_t)W * H;
-    const int blocks = coop_blocks((const void *)k_cg_persistent, (int)((N + kPersistThreads - 1) / kPersistThreads));
+    const int ntiles = ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
+    const int blocks = coop_blocks((const void *)k_cg_persistent,
+                                   std::max(ntiles, (int)((N + kPersistThreads - 1) / kPersistThreads)));
     void *args[] = {&W, &H, (void *)&gx, (void *)&gy, &U, &r, &dA, &dB, &partA, &partB, &gb, &max_iter, &gap_tol,
                     &state};
     lc.add(1);

@@ -91,7 +91,8 @@ EXPORTED = [
     "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_stage_weights",
     "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
-    "lfrv_stage_u_gradient", "lfrv_stage_cg", "lfrv_pfm_read", "lfrv_pfm_write", "lfrv_scene_params_preset",
+    "lfrv_stage_u_gradient", "lfrv_stage_cg", "lfrv_pfm_read", "lfrv_pfm_write", "lfrv_png_read", "lfrv_png_write",
+    "lfrv_scene_params_preset",
     "lfrv_synth_scene", "lfrv_psnr",
 ]
 
@@ -201,6 +202,22 @@ def pfm_write(path: str, img: np.ndarray) -> None:
     if img.ndim == 2:
         img = img[None]
     _check(LIB.lfrv_pfm_write(str(path).encode(), img.shape[2], img.shape[1], img.shape[0], fptr(img)))
+
+
+def png_read(path: str) -> np.ndarray:
+    """8-bit PNG as planar RGB floats in [0, 1] (value / 255, grey replicated), shape (3, h, w)."""
+    w, h = C.c_int(), C.c_int()
+    _check(LIB.lfrv_png_read(str(path).encode(), C.byref(w), C.byref(h), None, C.c_size_t(0)))
+    out = np.zeros((3, h.value, w.value), np.float32)
+    _check(LIB.lfrv_png_read(str(path).encode(), C.byref(w), C.byref(h), fptr(out), C.c_size_t(out.size)))
+    return out
+
+
+def png_write(path: str, img: np.ndarray) -> None:
+    """Planar RGB floats (3, h, w) written as 8-bit RGB, clamp(int(v * 255), 0, 255) per channel."""
+    img = f32(img)
+    assert img.ndim == 3 and img.shape[0] == 3, "planar RGB (3, h, w) expected"
+    _check(LIB.lfrv_png_write(str(path).encode(), img.shape[2], img.shape[1], fptr(img)))
 
 
 # ------------------------------------------------------------------ contexts
@@ -440,6 +457,8 @@ def _declare() -> None:
     LIB.lfrv_config_get_string.argtypes = [C.c_char_p, C.c_char_p, C.c_size_t]
     LIB.lfrv_pfm_read.argtypes = [C.c_char_p, _I, _I, _I, _F, C.c_size_t]
     LIB.lfrv_pfm_write.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, _F]
+    LIB.lfrv_png_read.argtypes = [C.c_char_p, _I, _I, _F, C.c_size_t]
+    LIB.lfrv_png_write.argtypes = [C.c_char_p, C.c_int, C.c_int, _F]
 
 
 _declare()
