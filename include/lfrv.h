@@ -121,8 +121,10 @@ int lfrv_ctx_set_stream(lfrv_ctx *ctx, void *cuda_stream);
 int lfrv_ctx_launch_count(lfrv_ctx *ctx, long long *count, int reset);
 /* Per-kernel device timing (no counterpart upstream; the reference prints iter/s from clock(),
  * sources/super-resolution.cpp:266-270). enable=1 clears the records and records a CUDA event pair on the
- * context stream around every kernel launch; lfrv_ctx_profile_read synchronises the stream and returns,
- * for the index-th kernel name seen, its summed device time and launch count (LFRV_E_ARG past the end). */
+ * context stream around every kernel launch (when its pool of 16384 pairs fills, the stream is synchronised
+ * and the pairs are folded into per-kernel totals, so profiling mode adds host waits between launches);
+ * lfrv_ctx_profile_read synchronises the stream and returns, for the index-th kernel name seen, its summed
+ * device time and launch count (LFRV_E_ARG past the end). */
 int lfrv_ctx_profile(lfrv_ctx *ctx, int enable);
 int lfrv_ctx_profile_read(lfrv_ctx *ctx, int index, char *name, size_t name_len, double *total_ms,
                           long long *launches);

@@ -43,7 +43,8 @@ struct Workspace {
     DevBuf in_views, in_tau, in_dpart, in_init, out_img;
 };
 
-// Per-kernel CUDA-event timing: a fixed pool of event pairs recorded in-stream; read after a sync.
+// Per-kernel CUDA-event timing: a fixed pool of event pairs recorded in-stream. When the pool is full the
+// stream is synchronised and the recorded pairs are folded into per-name totals (profiling mode only).
 struct KernelProfiler {
     struct Rec {
         const char *name;
@@ -52,9 +53,13 @@ struct KernelProfiler {
     std::vector<cudaEvent_t> ev;  // 2 per slot
     std::vector<Rec> recs;
     int next = 0;
-    bool overflow = false;
+    std::vector<std::string> names;  // totals in first-seen order
+    std::vector<double> ms;
+    std::vector<long long> count;
     void init(int slots);
     void destroy();
+    void reset();
+    void fold(cudaStream_t st);  // synchronises st, adds the recorded pairs to the totals, frees the pool
     int begin(const char *name, cudaStream_t st);
     void end(int slot, cudaStream_t st);
 };

@@ -52,15 +52,38 @@ void KernelProfiler::init(int slots) {
 void KernelProfiler::destroy() {
     for (auto &e : ev) cudaEventDestroy(e);
     ev.clear();
+    reset();
+}
+
+void KernelProfiler::reset() {
+    recs.clear();
+    next = 0;
+    names.clear();
+    ms.clear();
+    count.clear();
+}
+
+void KernelProfiler::fold(cudaStream_t st) {
+    LFRV_CUDA(cudaStreamSynchronize(st));
+    for (const auto &r : recs) {
+        float t = 0.f;
+        LFRV_CUDA(cudaEventElapsedTime(&t, ev[2 * r.slot], ev[2 * r.slot + 1]));
+        size_t k = 0;
+        while (k < names.size() && names[k] != r.name) ++k;
+        if (k == names.size()) {
+            names.push_back(r.name);
+            ms.push_back(0.0);
+            count.push_back(0);
+        }
+        ms[k] += t;
+        count[k] += 1;
+    }
     recs.clear();
     next = 0;
 }
 
 int KernelProfiler::begin(const char *name, cudaStream_t st) {
-    if (2 * (size_t)(next + 1) > ev.size()) {
-        overflow = true;
-        return -1;
-    }
+    if (2 * (size_t)(next + 1) > ev.size()) fold(st);
     const int slot = next++;
     cudaEventRecord(ev[2 * slot], st);
     recs.push_back({name, slot});
@@ -788,10 +811,8 @@ extern "C" int lfrv_ctx_profile(lfrv_ctx *ctx, int enable) {
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
     if (enable) {
-        ctx->prof.init(1 << 16);
-        ctx->prof.recs.clear();
-        ctx->prof.next = 0;
-        ctx->prof.overflow = false;
+        ctx->prof.init(1 << 14);
+        ctx->prof.reset();
         ctx->launches.prof = &ctx->prof;
     } else {
         ctx->launches.prof = nullptr;
@@ -803,30 +824,12 @@ extern "C" int lfrv_ctx_profile_read(lfrv_ctx *ctx, int index, char *name, size_
                                      long long *launches) {
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
-    if (ctx->stream) LFRV_CUDA(cudaStreamSynchronize(ctx->stream));
-    else LFRV_CUDA(cudaDeviceSynchronize());
-    // aggregate per kernel name in first-seen order
-    std::vector<std::string> names;
-    std::vector<double> ms;
-    std::vector<long long> cnt;
-    for (const auto &r : ctx->prof.recs) {
-        float t = 0.f;
-        LFRV_CUDA(cudaEventElapsedTime(&t, ctx->prof.ev[2 * r.slot], ctx->prof.ev[2 * r.slot + 1]));
-        size_t k = 0;
-        while (k < names.size() && names[k] != r.name) ++k;
-        if (k == names.size()) {
-            names.push_back(r.name);
-            ms.push_back(0.0);
-            cnt.push_back(0);
-        }
-        ms[k] += t;
-        cnt[k] += 1;
-    }
-    if (index < 0 || index >= (int)names.size()) return fail(LFRV_E_ARG, "profile index %d out of range", index);
-    if (name && name_len) std::snprintf(name, name_len, "%s", names[index].c_str());
-    if (total_ms) *total_ms = ms[index];
-    if (launches) *launches = cnt[index];
-    if (ctx->prof.overflow) return fail(LFRV_E_ARG, "profile event pool overflowed; totals are partial");
+    ctx->prof.fold(ctx->stream);
+    const KernelProfiler &p = ctx->prof;
+    if (index < 0 || index >= (int)p.names.size()) return fail(LFRV_E_ARG, "profile index %d out of range", index);
+    if (name && name_len) std::snprintf(name, name_len, "%s", p.names[index].c_str());
+    if (total_ms) *total_ms = p.ms[index];
+    if (launches) *launches = p.count[index];
     LFRV_API_END
 }
 

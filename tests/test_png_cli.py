@@ -148,8 +148,13 @@ def test_ulf_matches_library_call(tmp_path):
                         "-cg_max_iter", "200"], capture_output=True, text=True, timeout=300)
     assert r.returncode == 0, r.stderr
     got = lfrv.pfm_read(tmp_path / "output.pfm")
+    # the file's keys go through the reference's conventions (sigma_sensor is divided by 255 on parse)
+    fcfg = lfrv.parse_config(tmp_path / "run.cfg")
+    fcfg.w, fcfg.h, fcfg.nviews, fcfg.nchannels = cfg.w, cfg.h, V, 3
+    fcfg.faithful, fcfg.cg_gap_tol, fcfg.cg_max_iter = 0, 1e-5, 200
+    assert abs(fcfg.sigma_sensor - cfg.sigma_sensor / 255.0) < 1e-9
     with lfrv.Context(0) as ctx:
-        want, _ = ctx.ibr_gradient(cfg, sc.views, tau, dpart)
+        want, _ = ctx.ibr_gradient(fcfg, sc.views, tau, dpart)
     np.testing.assert_array_equal(got, want)
     png = lfrv.png_read(tmp_path / "result.png")
     q = np.clip((want.astype(np.float64) * 255.0).astype(np.int64), 0, 255)
