@@ -239,6 +239,26 @@ int lfrv_stage_u_gradient(lfrv_ctx *ctx, const lfrv_config *cfg, const float *vi
 int lfrv_stage_cg(lfrv_ctx *ctx, int W, int H, int faithful, int max_iter, double gap_tol,
                   const float *gx, const float *gy, float *U, int *iterations, double *gap);
 
+/* Allocation-free corrected CG. No reference counterpart.
+ * The same solver as lfrv_stage_cg with faithful = 0, on caller-owned DEVICE buffers on `stream`
+ * (a cudaStream_t of the current device, or NULL for the legacy default stream): gx, gy are H x W,
+ * U is 3 x H x W (in: u0, out: the solution).
+ * All of its scratch sits in one fixed device array built into the library. That array holds r and two
+ * direction buffers, the FP64 block partials, the solver state and the grid-barrier words. It is about
+ * 9.5 MB per device, for W * H <= LFRV_CG_STATIC_MAX_PIXELS. No call allocates or frees device memory,
+ * and none creates a context or a stream: this is the entry point for callers that cannot allocate.
+ * - Larger images are rejected with LFRV_E_ARG, before any device work.
+ * - First call on a device: it looks up the array's address with that device current. Later calls
+ *   reuse the cached address. This setup must happen before any stream capture that includes the call.
+ * - The barrier words are cleared on `stream` before each launch. Nothing else needs to start at zero.
+ * - There is one array per device. Calls that overlap on the same device race on it, even from different
+ *   streams or threads. Order such calls, for example on one stream.
+ * - With iterations or gap non-NULL the call synchronises `stream` and reads the iteration count, the
+ *   certified gap and the barrier status (LFRV_E_TIMEOUT). With both NULL it only enqueues work. */
+#define LFRV_CG_STATIC_MAX_PIXELS (512 * 512)
+int lfrv_cg_solve_static(void *stream, int W, int H, int max_iter, double gap_tol, const float *gx,
+                         const float *gy, float *U, int *iterations, double *gap);
+
 /* ---------------------------------------------------------------- files
  * PFM as the reference reads and writes it: gsl_image_load_pfm (cocolib/cocolib/common/gsl_image.cpp:
  * 416-500) flips rows on load; write_pfm_image_signed (cocolib/cocolib/cuda/cuda_helper.cu:340-375)

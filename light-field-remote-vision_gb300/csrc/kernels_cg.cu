@@ -9,9 +9,11 @@
 // updates (updateSolution :130-198, updateDir :508-523) are restated here; the dot products are FP64
 // block partials reduced in a fixed order (the reference accumulates float atomics in arbitrary order).
 #include <algorithm>
+#include <mutex>
 
 #include "device_common.cuh"
 #include "kernels.h"
+#include "lfrv_internal.h"
 
 namespace lfrv {
 
@@ -673,3 +675,81 @@ void launch_cg_energy(int W, int H, const float *U, const float *U0, const float
 }
 
 }  // namespace lfrv
+
+// ====================================================================== allocation-free CG entry point
+// lfrv_cg_solve_static runs k_cg_persistent with all of its scratch in one file-scope device array instead of
+// context buffers: r and the two direction buffers (3 planes of kStaticPixels floats each), the FP64 block
+// partials of phases A and B (4 doubles per block each), 16 doubles of solver state, 64 bytes of barrier words.
+namespace {
+
+constexpr size_t kStaticPixels = LFRV_CG_STATIC_MAX_PIXELS;
+constexpr int kStaticBlocks = 1024;  // cooperative blocks the partial slots hold (2 per SM for <= 512 SMs)
+constexpr size_t kStaticVecBytes = 9 * kStaticPixels * sizeof(float);
+constexpr size_t kStaticPartBytes = 2 * 4 * (size_t)kStaticBlocks * sizeof(double);
+constexpr size_t kStaticStateBytes = 16 * sizeof(double);
+constexpr size_t kStaticBarrierBytes = 64;
+constexpr size_t kStaticBytes = kStaticVecBytes + kStaticPartBytes + kStaticStateBytes + kStaticBarrierBytes;
+static_assert(kStaticVecBytes % 256 == 0 && kStaticPartBytes % 64 == 0, "scratch sections stay aligned");
+constexpr int kMaxDevices = 64;
+
+__device__ __align__(256) unsigned char g_cg_scratch[kStaticBytes];
+
+std::mutex g_scratch_mu;
+unsigned char *g_scratch_addr[kMaxDevices] = {};
+
+// Address of this device's copy of g_cg_scratch, looked up once per device with that device current.
+unsigned char *static_scratch(int dev) {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (!g_scratch_addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_cg_scratch);
+        if (e != cudaSuccess || !p)
+            lfrv::raise(LFRV_E_CUDA, "cudaGetSymbolAddress(g_cg_scratch): %s", cudaGetErrorString(e));
+        g_scratch_addr[dev] = static_cast<unsigned char *>(p);
+    }
+    return g_scratch_addr[dev];
+}
+
+}  // namespace
+
+extern "C" int lfrv_cg_solve_static(void *stream, int W, int H, int max_iter, double gap_tol, const float *gx,
+                                    const float *gy, float *U, int *iterations, double *gap) {
+    using namespace lfrv;
+    LFRV_API_BEGIN
+    if (W < 2 || H < 2 || !gx || !gy || !U || max_iter < 0) return fail(LFRV_E_ARG, "bad arguments");
+    if ((size_t)W * H > kStaticPixels)
+        return fail(LFRV_E_ARG, "%d x %d pixels exceed LFRV_CG_STATIC_MAX_PIXELS (%zu)", W, H, kStaticPixels);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(LFRV_E_NODEVICE, "cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return fail(LFRV_E_ARG, "device %d out of range", dev);
+    if (persistent_partials() > kStaticBlocks)
+        return fail(LFRV_E_ARG, "this device needs more than %d cooperative blocks", kStaticBlocks);
+    unsigned char *base = static_scratch(dev);
+    float *r = reinterpret_cast<float *>(base);
+    float *dA = r + 3 * kStaticPixels, *dB = dA + 3 * kStaticPixels;
+    double *partA = reinterpret_cast<double *>(base + kStaticVecBytes), *partB = partA + 4 * kStaticBlocks;
+    double *state = partB + 4 * kStaticBlocks;
+    unsigned int *bar = reinterpret_cast<unsigned int *>(state + 16);
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    e = cudaMemsetAsync(bar, 0, kStaticBarrierBytes, st);  // arrival count and error flag start at zero
+    if (e != cudaSuccess) return fail(LFRV_E_CUDA, "clearing the barrier words: %s", cudaGetErrorString(e));
+    GridBarrier gb;
+    gb.count = bar;
+    gb.err = reinterpret_cast<int *>(bar + 4);
+    LaunchCounter lc;
+    e = launch_cg_persistent(W, H, gx, gy, U, r, dA, dB, partA, partB, gb, max_iter, gap_tol, state, st, lc);
+    if (e != cudaSuccess) return fail(LFRV_E_CUDA, "k_cg_persistent launch: %s", cudaGetErrorString(e));
+    if (iterations || gap) {
+        double hs[16];
+        int hb[8];
+        e = cudaStreamSynchronize(st);
+        if (e == cudaSuccess) e = cudaMemcpy(hs, state, sizeof(hs), cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess) e = cudaMemcpy(hb, bar, sizeof(hb), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return fail(LFRV_E_CUDA, "reading the solver state: %s", cudaGetErrorString(e));
+        if (hb[4] != 0) return fail(LFRV_E_TIMEOUT, "a device-side grid barrier gave up waiting");
+        if (iterations) *iterations = (int)hs[5];
+        if (gap) *gap = hs[4];
+    }
+    LFRV_API_END
+}

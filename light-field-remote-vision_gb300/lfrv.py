@@ -91,7 +91,7 @@ EXPORTED = [
     "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_stage_weights",
     "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
-    "lfrv_stage_u_gradient", "lfrv_stage_cg", "lfrv_pfm_read", "lfrv_pfm_write", "lfrv_png_read", "lfrv_png_write",
+    "lfrv_stage_u_gradient", "lfrv_stage_cg", "lfrv_cg_solve_static", "lfrv_pfm_read", "lfrv_pfm_write", "lfrv_png_read", "lfrv_png_write",
     "lfrv_scene_params_preset",
     "lfrv_synth_scene", "lfrv_psnr",
 ]
@@ -202,6 +202,19 @@ def pfm_write(path: str, img: np.ndarray) -> None:
     if img.ndim == 2:
         img = img[None]
     _check(LIB.lfrv_pfm_write(str(path).encode(), img.shape[2], img.shape[1], img.shape[0], fptr(img)))
+
+
+CG_STATIC_MAX_PIXELS = 512 * 512
+
+
+def cg_solve_static(stream: int, W: int, H: int, max_iter: int, gap_tol: float, d_gx: int, d_gy: int, d_U: int,
+                    want_stats: bool = True):
+    """Allocation-free corrected CG on device pointers (lfrv_cg_solve_static); returns (iterations, gap)."""
+    it, gap = C.c_int(-1), C.c_double(float("nan"))
+    _check(LIB.lfrv_cg_solve_static(C.c_void_p(stream or None), W, H, max_iter, C.c_double(gap_tol),
+                                    C.c_void_p(d_gx), C.c_void_p(d_gy), C.c_void_p(d_U),
+                                    C.byref(it) if want_stats else None, C.byref(gap) if want_stats else None))
+    return it.value, gap.value
 
 
 def png_read(path: str) -> np.ndarray:
@@ -457,6 +470,7 @@ def _declare() -> None:
     LIB.lfrv_config_get_string.argtypes = [C.c_char_p, C.c_char_p, C.c_size_t]
     LIB.lfrv_pfm_read.argtypes = [C.c_char_p, _I, _I, _I, _F, C.c_size_t]
     LIB.lfrv_pfm_write.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, _F]
+    LIB.lfrv_cg_solve_static.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp, _I, _D]
     LIB.lfrv_png_read.argtypes = [C.c_char_p, _I, _I, _F, C.c_size_t]
     LIB.lfrv_png_write.argtypes = [C.c_char_p, C.c_int, C.c_int, _F]
 
