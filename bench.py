@@ -54,7 +54,8 @@ def make_config(lfrv, wl: str, sc):
                                early_exit=0, faithful=1)
 
 
-def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: int = 0) -> float | None:
+def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: int = 0,
+                      rof_iters: int = 0) -> float | None:
     """Compulsory DRAM bytes of one launch of `kernel` (FP32 = 4 B; V views of n pixels, N target pixels)."""
     table = {
         # r = b - A u0 (g_x, g_y, u read, r written), then per iteration: r, d_old read, d written (phase A);
@@ -79,6 +80,8 @@ def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: in
         "cg_dir": 24 * N + 12 * N,
         "cg_energy": 24 * N + 8 * N,
         "rof_iter": 88 * N,
+        # all inner iterations of one ISTA step in one launch: 88 B per target pixel per iteration
+        "rof_persistent": 88 * N * rof_iters,
         "residual": 12 * N + 24 * V * n + 12 * V * n,
         "dataterm_F": 12 * V * n + 8 * V * n + 4 * V * n + 12 * N + 12 * N,
     }
@@ -229,7 +232,7 @@ def run_ours(args, rank: int, world: int) -> None:
     dom = max(prof, key=lambda k: prof[k][0])
     dom_ms, dom_n = prof[dom]
     avg_s = dom_ms / 1e3 / dom_n
-    abytes = algorithmic_bytes(dom, V, n, N, ks, cg_iters=int(st.outer_iterations))
+    abytes = algorithmic_bytes(dom, V, n, N, ks, cg_iters=int(st.outer_iterations), rof_iters=int(cfg.niter))
     peak, peak_kind = measured_peak_hbm()
     roof = None
     if abytes:

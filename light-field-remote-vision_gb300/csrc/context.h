@@ -67,6 +67,7 @@ struct KernelProfiler {
 // Statistics left on the device by persistent solvers of the current call, read after the stream completes.
 struct Pending {
     bool cg = false, hole_fill = false;
+    bool barrier = false;  // a persistent kernel used the grid barrier since the last check (error word armed)
     lfrv_stats *stats = nullptr;
     double gap_tol = 0.0;
 };
@@ -74,6 +75,9 @@ struct Pending {
 }  // namespace lfrv
 
 struct lfrv_ctx {
+    // host-buffer calls upload on a second stream so the copies overlap the warp stage (created on first use)
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t up_start = nullptr, up_depth[4] = {}, up_views = nullptr;
     lfrv::Pending pending;
     lfrv::KernelProfiler prof;
     bool profiling = false;

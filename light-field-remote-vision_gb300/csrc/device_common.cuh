@@ -97,6 +97,42 @@ __device__ __forceinline__ float footprint_tap(float tx, float ty, int dsf, int 
     return (norm != 0.0f) ? __fdiv_rn(tap, norm) : tap;
 }
 
+// The norm footprint_tap divides by, for the footprint anchored at (x0, y0): the same products summed in
+// the same order (j outer, i inner), so footprint_tap_n(..., footprint_norm(...), raw) == footprint_tap(...).
+template <int KS>
+__device__ __forceinline__ float footprint_norm(float tx, float ty, int dsf, int W, int H, int x0, int y0) {
+    const float px = tx - 0.5f, py = ty - 0.5f;
+    float dxs[KS], dys[KS];
+#pragma unroll
+    for (int k = 0; k < KS; ++k) {
+        dxs[k] = fp_overlap(k, KS, x0 + k, px, dsf);
+        dys[k] = fp_overlap(k, KS, y0 + k, py, dsf);
+    }
+    float norm = 0.0f;
+#pragma unroll
+    for (int j = 0; j < KS; ++j) {
+#pragma unroll
+        for (int i = 0; i < KS; ++i) {
+            const int x = x0 + j, y = y0 + i;
+            const bool in = (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1);
+            norm = __fadd_rn(norm, in ? __fmul_rn(dxs[j], dys[i]) : 0.0f);
+        }
+    }
+    return norm;
+}
+
+// Tap (J, I) of the footprint anchored at (x0, y0) given its norm (from footprint_norm).
+template <int KS>
+__device__ __forceinline__ float footprint_tap_n(float tx, float ty, int dsf, int W, int H, int x0, int y0, int J,
+                                                 int I, float norm, float &raw) {
+    const float px = tx - 0.5f, py = ty - 0.5f;
+    const int x = x0 + J, y = y0 + I;
+    const bool in = (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1);
+    const float a = in ? __fmul_rn(fp_overlap(J, KS, x, px, dsf), fp_overlap(I, KS, y, py, dsf)) : 0.0f;
+    raw = a;
+    return (norm != 0.0f) ? __fdiv_rn(a, norm) : a;
+}
+
 // Raw overlap product of tap (j, i) (setup_visibility_mask, sources/gradientIBR_kernels.cuh:26-49).
 template <int KS>
 __device__ __forceinline__ float footprint_raw(float tx, float ty, int dsf, int j, int i, int x0, int y0) {
@@ -145,13 +181,14 @@ __device__ __forceinline__ double block_sum(double v, double *smem /* >= NT/32 *
 // callers then exit, and the host reports LFRV_E_TIMEOUT.
 constexpr long long kSpinLimit = 1ll << 22;
 
-__device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &generation) {
+// nblocks: the blocks taking part (blocks 0 .. nblocks-1; the others must have returned before any barrier).
+__device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &generation, unsigned int nblocks) {
     __syncthreads();
     generation += 1;
     bool ok = true;
     if (threadIdx.x == 0 && threadIdx.y == 0) {
         __threadfence();
-        const unsigned int target = generation * (gridDim.x * gridDim.y);
+        const unsigned int target = generation * nblocks;
         atomicAdd(gb.count, 1u);
         long long spins = 0;
         while (true) {
@@ -174,6 +211,10 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &g
     if (threadIdx.x == 0 && threadIdx.y == 0) s_ok = ok ? 1 : 0;
     __syncthreads();
     return s_ok != 0;
+}
+
+__device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &generation) {
+    return grid_sync(gb, generation, gridDim.x * gridDim.y);
 }
 
 }  // namespace lfrv

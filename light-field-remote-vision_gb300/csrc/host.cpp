@@ -107,6 +107,8 @@ static void swap_buf(DevBuf &a, DevBuf &b) {
     std::swap(a.bytes, b.bytes);
 }
 
+static GridBarrier fresh_barrier(lfrv_ctx *c);
+
 static void check_launch(const char *what) {
     const cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) raise(LFRV_E_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
@@ -377,16 +379,16 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
             launch_dataterm_F(G, B, tau2, b.res, s2, cfg.dt_alpha, fscale, ws.U.as<float>(), b.F, nullptr, s,
                               c->launches);
             check_launch("data term");
-            // niter inner ROF iterations from Uq = U (ping-pong buffers)
-            const float *Ucur = ws.U.as<float>();
-            float *Udst = ws.Ua.as<float>();
-            for (int it = 0; it < cfg.niter; ++it) {
-                launch_rof_iter(G.W, G.H, tau_pd, sigma_pd, lam_prox, Ucur, ws.P.as<float>(), b.F, b.g, Udst,
-                                ws.Pa.as<float>(), s, c->launches);
-                swap_buf(ws.P, ws.Pa);
-                Ucur = Udst;
-                Udst = (Udst == ws.Ua.as<float>()) ? ws.Ub.as<float>() : ws.Ua.as<float>();
-            }
+            // niter inner ROF iterations from Uq = U in one persistent launch over (Ua, P) <-> (Ub, Pa);
+            // U itself stays the previous iterate (the moving-pixel test compares against it)
+            LFRV_CUDA(cudaMemcpyAsync(ws.Ua.p, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+            const GridBarrier gb = fresh_barrier(c);
+            LFRV_CUDA(launch_rof_persistent(G.W, G.H, cfg.niter, tau_pd, sigma_pd, lam_prox, ws.Ua.as<float>(),
+                                            ws.P.as<float>(), ws.Ub.as<float>(), ws.Pa.as<float>(), b.F, b.g, gb, s,
+                                            c->launches));
+            const bool odd = (rof_persistent_steps(cfg.niter) & 1) != 0;
+            const float *Ucur = odd ? ws.Ub.as<float>() : ws.Ua.as<float>();
+            if (odd) swap_buf(ws.P, ws.Pa);
             int nM = 0;
             if (track) nM = moving(Ucur, ws.U.as<float>());
             // U <- the ROF result
@@ -445,8 +447,11 @@ static double *solver_state(lfrv_ctx *c) {
 }
 
 static GridBarrier fresh_barrier(lfrv_ctx *c) {
+    // the arrival counter restarts for every launch; the error word is cleared only by the first launch
+    // since the last check, so a timeout of an earlier launch of the same call is still reported
     c->ws.barrier.ensure(64);
-    LFRV_CUDA(cudaMemsetAsync(c->ws.barrier.p, 0, 64, c->stream));
+    LFRV_CUDA(cudaMemsetAsync(c->ws.barrier.p, 0, c->pending.barrier ? 16 : 64, c->stream));
+    c->pending.barrier = true;
     GridBarrier gb;
     gb.count = c->ws.barrier.as<unsigned int>();
     gb.err = reinterpret_cast<int *>(c->ws.barrier.as<unsigned int>() + 4);
@@ -595,11 +600,11 @@ static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img
 // After the stream has completed: solver statistics kept on the device, and the barrier status.
 void finish_stats(lfrv_ctx *c) {
     Pending &p = c->pending;
-    if (!p.cg && !p.hole_fill) return;
+    if (!p.cg && !p.hole_fill && !p.barrier) return;
     double state[16];
-    int bar[8];
-    LFRV_CUDA(cudaMemcpy(state, c->ws.state.p, sizeof(state), cudaMemcpyDeviceToHost));
-    LFRV_CUDA(cudaMemcpy(bar, c->ws.barrier.p, sizeof(bar), cudaMemcpyDeviceToHost));
+    int bar[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (p.cg || p.hole_fill) LFRV_CUDA(cudaMemcpy(state, c->ws.state.p, sizeof(state), cudaMemcpyDeviceToHost));
+    if (p.barrier) LFRV_CUDA(cudaMemcpy(bar, c->ws.barrier.p, sizeof(bar), cudaMemcpyDeviceToHost));
     const bool timeout = bar[4] != 0;
     if (p.stats) {
         if (p.hole_fill) p.stats->hole_fill_iterations = (int)state[8];
@@ -672,8 +677,18 @@ static void fold_camera(const lfrv_camera &k, const lfrv_camera &u, float *Mout,
     }
 }
 
+// Depth maps arriving in view chunks on the copy stream: chunk k (views up to v_end[k]) is complete when
+// depth_ready[k] fires; the colour views when views_ready fires.
+struct UploadPlan {
+    int chunks = 0;
+    int v_end[4] = {0, 0, 0, 0};
+    cudaEvent_t depth_ready[4] = {};
+    cudaEvent_t views_ready = nullptr;
+};
+
 static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfrv_camera *cams,
-                 const lfrv_camera *target, float *tau3, float *dpart3, float *tau2, float *dp2, float *zbuf_out) {
+                 const lfrv_camera *target, float *tau3, float *dpart3, float *tau2, float *dp2, float *zbuf_out,
+                 const UploadPlan *plan = nullptr) {
     if (V < 1 || V > kMaxViews || w <= 0 || h <= 0 || !depth || !cams || !target)
         raise(LFRV_E_ARG, "bad warp arguments");
     Workspace &ws = c->ws;
@@ -687,7 +702,25 @@ static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfr
     ws.zkey.ensure(sizeof(unsigned long long) * N);
     ws.zbuf.ensure(sizeof(float) * N);
     launch_zbuffer_clear(W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
-    launch_zbuffer_splat(V, w, h, depth, wc, W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
+    if (plan) {
+        // splat each chunk of views as soon as its depth maps have arrived
+        int v0 = 0;
+        for (int k = 0; k < plan->chunks; ++k) {
+            LFRV_CUDA(cudaStreamWaitEvent(c->stream, plan->depth_ready[k], 0));
+            const int v1 = plan->v_end[k];
+            WarpCams part;
+            std::memset(&part, 0, sizeof(part));
+            for (int v = v0; v < v1; ++v) {
+                std::memcpy(part.M[v - v0], wc.M[v], sizeof(wc.M[v]));
+                std::memcpy(part.b[v - v0], wc.b[v], sizeof(wc.b[v]));
+            }
+            launch_zbuffer_splat(v1 - v0, w, h, depth + (size_t)v0 * 3 * w * h, part, W, H,
+                                 ws.zkey.as<unsigned long long>(), c->stream, c->launches);
+            v0 = v1;
+        }
+    } else {
+        launch_zbuffer_splat(V, w, h, depth, wc, W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
+    }
     launch_zbuffer_resolve(W, H, ws.zkey.as<unsigned long long>(), ws.zbuf.as<float>(), c->stream, c->launches);
     check_launch("z-buffer");
     launch_tau(V, w, h, depth, wc, W, H, ws.zbuf.as<float>(), tau3, dpart3, tau2, dp2, c->stream, c->launches);
@@ -726,7 +759,10 @@ static void prepare_geometry_inputs(lfrv_ctx *c, const Geometry &G, const float 
     check_launch("input layout");
 }
 
-static void begin_timing(lfrv_ctx *c) { LFRV_CUDA(cudaEventRecord(c->ev0, c->stream)); }
+static void begin_timing(lfrv_ctx *c) {
+    c->pending = Pending{};
+    LFRV_CUDA(cudaEventRecord(c->ev0, c->stream));
+}
 static void end_timing(lfrv_ctx *c, lfrv_stats *st, long long launches0) {
     LFRV_CUDA(cudaEventRecord(c->ev1, c->stream));
     LFRV_CUDA(cudaEventSynchronize(c->ev1));
@@ -787,6 +823,13 @@ extern "C" int lfrv_ctx_destroy(lfrv_ctx *ctx) {
     else cudaDeviceSynchronize();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->copy_stream) {
+        cudaStreamSynchronize(ctx->copy_stream);
+        cudaStreamDestroy(ctx->copy_stream);
+        cudaEventDestroy(ctx->up_start);
+        cudaEventDestroy(ctx->up_views);
+        for (auto e : ctx->up_depth) cudaEventDestroy(e);
+    }
     ctx->prof.destroy();
     delete ctx;
     LFRV_API_END
@@ -921,25 +964,47 @@ extern "C" int lfrv_ibr_gradient(lfrv_ctx *ctx, const lfrv_config *cfg, const fl
     return solve_host(ctx, cfg, false, views, tau, tau_channels, dpart, init, out, stats);
 }
 
+// Warp stage + solve of one target view on device buffers; with a plan the inputs are still arriving on the
+// copy stream, and with host_out the result is copied back before the call synchronises.
+static void render_view_impl(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const float *d_views,
+                             const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target, float *d_out,
+                             lfrv_stats *stats, const UploadPlan *plan, float *host_out) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    const Geometry G = geometry(cfg);
+    if (target->width != G.W || target->height != G.H) raise(LFRV_E_ARG, "target size mismatch");
+    const long long l0 = ctx->launches.n;
+    begin_timing(ctx);
+    Workspace &ws = ctx->ws;
+    ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr,
+         plan);
+    if (plan) LFRV_CUDA(cudaStreamWaitEvent(ctx->stream, plan->views_ready, 0));
+    if (algorithm == 0) color_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
+    else gradient_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
+    if (host_out)
+        LFRV_CUDA(cudaMemcpyAsync(host_out, d_out, sizeof(float) * 3 * G.N, cudaMemcpyDeviceToHost, ctx->stream));
+    end_timing(ctx, stats, l0);
+}
+
 extern "C" int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm, const float *d_views,
                                     const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target,
                                     float *d_out, lfrv_stats *stats) {
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
     if (!cfg || !d_views || !d_depth || !cams || !target || !d_out) return fail(LFRV_E_ARG, "null argument");
-    if (stats) std::memset(stats, 0, sizeof(*stats));
-    const Geometry G = geometry(*cfg);
-    if (target->width != G.W || target->height != G.H) return fail(LFRV_E_ARG, "target size mismatch");
-    const long long l0 = ctx->launches.n;
-    begin_timing(ctx);
-    Workspace &ws = ctx->ws;
-    ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
-    ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
-    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr);
-    if (algorithm == 0) color_solve(ctx, *cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
-    else gradient_solve(ctx, *cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
-    end_timing(ctx, stats, l0);
+    render_view_impl(ctx, *cfg, algorithm, d_views, d_depth, cams, target, d_out, stats, nullptr, nullptr);
     LFRV_API_END
+}
+
+static cudaStream_t copy_stream(lfrv_ctx *c) {
+    if (!c->copy_stream) {
+        LFRV_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        LFRV_CUDA(cudaEventCreateWithFlags(&c->up_start, cudaEventDisableTiming));
+        LFRV_CUDA(cudaEventCreateWithFlags(&c->up_views, cudaEventDisableTiming));
+        for (auto &e : c->up_depth) LFRV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    return c->copy_stream;
 }
 
 extern "C" int lfrv_render_view(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm, const float *views,
@@ -947,17 +1012,36 @@ extern "C" int lfrv_render_view(lfrv_ctx *ctx, const lfrv_config *cfg, int algor
                                 lfrv_stats *stats) {
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
-    if (!cfg || !views || !depth || !out) return fail(LFRV_E_ARG, "null argument");
+    if (!cfg || !views || !depth || !out || !cams || !target) return fail(LFRV_E_ARG, "null argument");
     const Geometry G = geometry(*cfg);
-    HostIO io{ctx};
-    const size_t n = G.n, V = G.V;
-    const float *dv = io.up(ctx->ws.in_views, views, V * 3 * n);
-    const float *dd = io.up(ctx->ws.depth, depth, V * 3 * n);
-    ctx->ws.out_img.ensure(sizeof(float) * 3 * G.N);
-    const int rc = lfrv_render_view_dev(ctx, cfg, algorithm, dv, dd, cams, target, ctx->ws.out_img.as<float>(), stats);
-    if (rc != LFRV_OK) return rc;
-    io.down(out, ctx->ws.out_img.as<float>(), 3 * G.N);
-    sync(ctx);
+    if (G.V < 1 || G.V > kMaxViews) return fail(LFRV_E_ARG, "bad view count");
+    const size_t n = G.n, V = G.V, per_view = 3 * n * sizeof(float);
+    Workspace &ws = ctx->ws;
+    ws.in_views.ensure(V * per_view);
+    ws.depth.ensure(V * per_view);
+    ws.out_img.ensure(sizeof(float) * 3 * G.N);
+    // uploads on the copy stream, after whatever the context stream has queued on these buffers; the depth
+    // maps first, in up to 4 chunks of views, then the colour views
+    cudaStream_t cs = copy_stream(ctx);
+    LFRV_CUDA(cudaEventRecord(ctx->up_start, ctx->stream));
+    LFRV_CUDA(cudaStreamWaitEvent(cs, ctx->up_start, 0));
+    UploadPlan plan;
+    plan.chunks = G.V < 4 ? G.V : 4;
+    int v0 = 0;
+    for (int k = 0; k < plan.chunks; ++k) {
+        const int v1 = (int)((V * (size_t)(k + 1)) / plan.chunks);
+        LFRV_CUDA(cudaMemcpyAsync(ws.depth.as<char>() + v0 * per_view, reinterpret_cast<const char *>(depth) + v0 * per_view,
+                                  (size_t)(v1 - v0) * per_view, cudaMemcpyHostToDevice, cs));
+        LFRV_CUDA(cudaEventRecord(ctx->up_depth[k], cs));
+        plan.v_end[k] = v1;
+        plan.depth_ready[k] = ctx->up_depth[k];
+        v0 = v1;
+    }
+    LFRV_CUDA(cudaMemcpyAsync(ws.in_views.p, views, V * per_view, cudaMemcpyHostToDevice, cs));
+    LFRV_CUDA(cudaEventRecord(ctx->up_views, cs));
+    plan.views_ready = ctx->up_views;
+    render_view_impl(ctx, *cfg, algorithm, ws.in_views.as<float>(), ws.depth.as<float>(), cams, target,
+                     ws.out_img.as<float>(), stats, &plan, out);
     LFRV_API_END
 }
 
@@ -1072,16 +1156,16 @@ extern "C" int lfrv_stage_rof(lfrv_ctx *ctx, int W, int H, int niter, float tau,
     io.up(ws.P, P, 6 * N);
     ws.Ua.ensure(3 * N * sizeof(float));
     ws.Pa.ensure(6 * N * sizeof(float));
-    for (int it = 0; it < niter; ++it) {
-        launch_rof_iter(W, H, tau, sigma, lambda, ws.U.as<float>(), ws.P.as<float>(), ws.F.as<float>(),
-                        ws.g.as<float>(), ws.Ua.as<float>(), ws.Pa.as<float>(), ctx->stream, ctx->launches);
-        swap_buf(ws.U, ws.Ua);
-        swap_buf(ws.P, ws.Pa);
-    }
-    check_launch("rof");
-    io.down(U, ws.U.as<float>(), 3 * N);
-    io.down(P, ws.P.as<float>(), 6 * N);
+    ctx->pending = Pending{};
+    const GridBarrier gb = fresh_barrier(ctx);
+    LFRV_CUDA(launch_rof_persistent(W, H, niter, tau, sigma, lambda, ws.U.as<float>(), ws.P.as<float>(),
+                                    ws.Ua.as<float>(), ws.Pa.as<float>(), ws.F.as<float>(), ws.g.as<float>(), gb,
+                                    ctx->stream, ctx->launches));
+    const bool odd = (rof_persistent_steps(niter) & 1) != 0;
+    io.down(U, odd ? ws.Ua.as<float>() : ws.U.as<float>(), 3 * N);
+    io.down(P, odd ? ws.Pa.as<float>() : ws.P.as<float>(), 6 * N);
     sync(ctx);
+    finish_stats(ctx);
     LFRV_API_END
 }
 

@@ -126,7 +126,11 @@ struct GridBarrier {
     unsigned int *count;
     int *err;
 };
-int persistent_partials();  // upper bound of blocks (partials per slot)
+int persistent_partials();
+int rof_persistent_steps(int niter);
+cudaError_t launch_rof_persistent(int W, int H, int niter, float tau, float sigma, float lam, float *U0, float *P0,
+                                  float *U1, float *P1, const float *F, const float *g, GridBarrier gb, cudaStream_t st,
+                                  LaunchCounter &lc);  // upper bound of blocks (partials per slot)
 cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
                                  float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
                                  double *state, cudaStream_t st, LaunchCounter &lc);

@@ -279,11 +279,27 @@ constexpr int kPersistThreads = 512;
 
 // Sums `count` FP64 partials per slot in a fixed order (identical in every block).
 __device__ void block_reduce_partials(const double *partial, int count, int nslots, double *out_smem) {
-    __shared__ double red[kPersistThreads / 32][4];
+    // one warp: lane-strided sums then a shuffle tree, in FP64 and a fixed order (the FP64 pipe is narrow on
+    // this part, so the other warps stay out of it)
+    if (threadIdx.x < 32) {
+        for (int sl = 0; sl < nslots; ++sl) {
+            double s = 0.0;
+            for (int i = threadIdx.x; i < count; i += 32) s += __ldcg(partial + (size_t)sl * count + i);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (threadIdx.x == 0) out_smem[sl] = s;
+        }
+    }
+    __syncthreads();
+}
+
+// Block sum of up to 4 per-thread FP32 values: warp trees in FP32 (each lane holds a handful of terms),
+// the warp sums added in FP64 in a fixed order into partial[slot * stride + blockIdx.x].
+__device__ void block_partials_f(const float v[4], int nslots, double *partial, int stride) {
+    __shared__ float red[kPersistThreads / 32][4];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int sl = 0; sl < nslots; ++sl) {
-        double s = 0.0;
-        for (int i = threadIdx.x; i < count; i += blockDim.x) s += __ldcg(partial + (size_t)sl * count + i);
+        float s = v[sl];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
         if (lane == 0) red[wid][sl] = s;
@@ -291,14 +307,15 @@ __device__ void block_reduce_partials(const double *partial, int count, int nslo
     __syncthreads();
     if (threadIdx.x < nslots) {
         double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += red[w][threadIdx.x];
-        out_smem[threadIdx.x] = t;
+        for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += (double)red[w][threadIdx.x];
+        partial[(size_t)threadIdx.x * stride + blockIdx.x] = t;
     }
     __syncthreads();
 }
 
-// Block sum of up to 4 per-thread values into partial[slot * gridDim.x + blockIdx.x].
-__device__ void block_partials(const double v[4], int nslots, double *partial) {
+// Block sum of up to 4 per-thread values into partial[slot * stride + blockIdx.x] (stride: gridDim.x, or
+// the number of participating blocks).
+__device__ void block_partials(const double v[4], int nslots, double *partial, int stride) {
     __shared__ double red[kPersistThreads / 32][4];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int sl = 0; sl < nslots; ++sl) {
@@ -311,7 +328,7 @@ __device__ void block_partials(const double v[4], int nslots, double *partial) {
     if (threadIdx.x < nslots) {
         double t = 0.0;
         for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += red[w][threadIdx.x];
-        partial[(size_t)threadIdx.x * gridDim.x + blockIdx.x] = t;
+        partial[(size_t)threadIdx.x * stride + blockIdx.x] = t;
     }
     __syncthreads();
 }
@@ -362,7 +379,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
     unsigned int gen = 0;
     // ---- phase 0: r = b - A x (initConjGrad, solver.cu:383-467) and E(x0) = 1/2 ||grad x0 - g||^2 (x0 = u0)
     {
-        double acc[4] = {0, 0, 0, 0};
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
         for (size_t o = tid; o < N; o += nthr) {
             const int x = (int)(o % W), y = (int)(o / W);
             const float gxo = __ldg(gX + o), gyo = __ldg(gY + o);
@@ -380,7 +397,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                 else ly = uc - __ldcg(u + o - W) - gyu;
                 const float rv = -(lx + ly);
                 r[c * N + o] = rv;
-                acc[c] += (double)(rv * rv);
+                acc[c] += rv * rv;
                 float e = 0.f;
                 if (x < W - 1) {
                     const float a = __ldcg(u + o + 1) - uc - gxo;
@@ -390,13 +407,18 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                     const float a = __ldcg(u + o + W) - uc - gyo;
                     e += a * a;
                 }
-                acc[3] += 0.5 * (double)e;
+                acc[3] += 0.5f * e;
             }
         }
-        block_partials(acc, 4, partB);
+        block_partials_f(acc, 4, partB, gridDim.x);
     }
     if (!grid_sync(gb, gen)) return;
     block_reduce_partials(partB, gridDim.x, 4, sh);
+    // The FP64 scalars (delta, E, gap) live in thread 0 of each block, which derives the float coefficients
+    // and the stop decision and hands them to the block through shared memory (every block computes the same
+    // values from the same partials, so the grid agrees).
+    __shared__ float s_coef[3];
+    __shared__ int s_stop;
     double delta[3] = {sh[0], sh[1], sh[2]};
     double E = sh[3];
     float beta[3] = {0.f, 0.f, 0.f};
@@ -405,12 +427,16 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
     double gap = 1e300;
     int it = 0;
     for (;; ++it) {
-        const double bound = (delta[0] + delta[1] + delta[2]) / (2.0 * (double)lambda);
-        gap = (E - bound) > 0 ? bound / (E - bound) : 1e300;
-        if (it >= max_iter || (gap_tol > 0 && gap <= gap_tol)) break;
+        if (threadIdx.x == 0) {
+            const double bound = (delta[0] + delta[1] + delta[2]) / (2.0 * (double)lambda);
+            gap = (E - bound) > 0 ? bound / (E - bound) : 1e300;
+            s_stop = (it >= max_iter || (gap_tol > 0 && gap <= gap_tol)) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_stop) break;
         // ---- phase A: d = r + beta d_old on each tile + halo in shared memory, q = A d, d . q
         {
-            double acc[4] = {0, 0, 0, 0};
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
             for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
                 const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
                 for (int k = threadIdx.x; k < 3 * kHaloY * kHaloX; k += blockDim.x) {
@@ -433,26 +459,28 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                         const float qv = tile_op(tile[c], lx + 1, ly + 1, x, y, W, H, lambda);
                         const float dcv = tile[c][ly + 1][lx + 1];
                         dnew[c * N + o] = dcv;
-                        acc[c] += (double)(dcv * qv);
+                        acc[c] += dcv * qv;
                     }
                 }
                 __syncthreads();
             }
-            block_partials(acc, 3, partA);
+            block_partials_f(acc, 3, partA, gridDim.x);
         }
         if (!grid_sync(gb, gen)) return;
         block_reduce_partials(partA, gridDim.x, 3, sh);
-        float alpha[3];
-        double alpha_d[3];
+        if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            alpha_d[c] = (sh[c] > 0) ? delta[c] / sh[c] : 0.0;
-            alpha[c] = (float)alpha_d[c];
-            E -= 0.5 * alpha_d[c] * delta[c];
+            for (int c = 0; c < 3; ++c) {
+                const double alpha_d = (sh[c] > 0) ? delta[c] / sh[c] : 0.0;
+                s_coef[c] = (float)alpha_d;
+                E -= 0.5 * alpha_d * delta[c];
+            }
         }
+        __syncthreads();
+        const float alpha[3] = {s_coef[0], s_coef[1], s_coef[2]};
         // ---- phase B: x += alpha d, r -= alpha A d, r . r (d tile + halo in shared memory)
         {
-            double acc[4] = {0, 0, 0, 0};
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
             for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
                 const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
                 for (int k = threadIdx.x; k < 3 * kHaloY * kHaloX; k += blockDim.x) {
@@ -473,20 +501,25 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                         U[c * N + o] = __ldcg(U + c * N + o) + alpha[c] * dv;
                         const float rv = __ldcg(r + c * N + o) - alpha[c] * qv;
                         r[c * N + o] = rv;
-                        acc[c] += (double)(rv * rv);
+                        acc[c] += rv * rv;
                     }
                 }
                 __syncthreads();
             }
-            block_partials(acc, 3, partB);
+            block_partials_f(acc, 3, partB, gridDim.x);
         }
         if (!grid_sync(gb, gen)) return;
         block_reduce_partials(partB, gridDim.x, 3, sh);
+        if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            beta[c] = (delta[c] > 0) ? (float)(sh[c] / delta[c]) : 0.f;
-            delta[c] = sh[c];
+            for (int c = 0; c < 3; ++c) {
+                s_coef[c] = (delta[c] > 0) ? (float)(sh[c] / delta[c]) : 0.f;
+                delta[c] = sh[c];
+            }
         }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 3; ++c) beta[c] = s_coef[c];
         dold = dnew;
         dnew = (dnew == dA) ? dB : dA;
     }
@@ -503,6 +536,12 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
 // Hole filling with the whole iteration loop in one launch (hole_filling, sources/gradientIBR.cu:87-152).
 // count: device pointer to the number of holes. A holds the initial image (and the result); B is a copy.
 // state: [0] iterations.
+// Only as many blocks as the hole count needs take part (kHoleFillPerBlock holes each; the others return at
+// once), so the grid barrier of each iteration spans few blocks. The energy partials alternate between two
+// slots by iteration parity: a block overwrites slot k & 1 in iteration k + 2 only after every block passed
+// the barrier of iteration k + 1, i.e. after all of them read it, so one barrier per iteration suffices.
+constexpr int kHoleFillPerBlock = 4 * kPersistThreads;
+
 __global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W, int H, const int *__restrict__ holes,
                                                                           const int *__restrict__ count, float *A,
                                                                           float *B, double *part, GridBarrier gb,
@@ -510,7 +549,9 @@ __global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W,
     __shared__ double sh[8];
     const size_t N = (size_t)W * H;
     const int nh = *count;
-    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = gridDim.x * blockDim.x;
+    const int active = min((int)gridDim.x, max(1, (nh + kHoleFillPerBlock - 1) / kHoleFillPerBlock));
+    if ((int)blockIdx.x >= active) return;
+    const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = active * blockDim.x;
     unsigned int gen = 0;
     float *src = A, *dst = B;
     float energy = 0.0f, previous = 0.0f;
@@ -537,9 +578,10 @@ __global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W,
                 if (c == 2) acc[0] += (double)(lap * un);
             }
         }
-        block_partials(acc, 1, part);
-        if (!grid_sync(gb, gen)) return;
-        block_reduce_partials(part, gridDim.x, 1, sh);
+        double *slot = part + (size_t)(k & 1) * active;
+        block_partials(acc, 1, slot, active);
+        if (!grid_sync(gb, gen, active)) return;
+        block_reduce_partials(slot, active, 1, sh);
         energy = (float)sh[0];
         float *t = src;
         src = dst;
@@ -548,8 +590,6 @@ __global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W,
             ++k;
             break;
         }
-        // partials are rewritten next iteration only after every block has read them
-        if (!grid_sync(gb, gen)) return;
     }
     if (src != A) {  // copy the holes of the result back into A
         for (int h = tid; h < nh; h += nthr) {

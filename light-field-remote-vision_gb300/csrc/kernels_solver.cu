@@ -10,6 +10,8 @@
 // pixels of all views are bucketed by the anchor of their footprint (counting sort, buckets sorted by
 // (view, pixel)), and every target pixel reads the ks x ks anchor buckets that can reach it, recomputing
 // the footprint weights from tau instead of storing A (the reference stores ks^2 floats per source pixel).
+#include <algorithm>
+
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -277,20 +279,52 @@ __global__ void k_vis_any(int W, int H, int n, int dsf, int BW, const unsigned i
 //   gradient splat of init_u_gradient (:833-920): (gx, gy, mask) = sum A (Sobel_x, Sobel_y, w) / sum A,
 //   mask scaled by sigma^2.
 // img: per view [3][n]; vgrad: per view [2][n] (Sobel of the view luminance); wgt: per view [n].
-template <int KS>
-__global__ void __launch_bounds__(256) k_gradient_setup(int W, int H, int n, int dsf, int BW,
-                                                        const unsigned int *__restrict__ start,
-                                                        const unsigned int *__restrict__ entries,
-                                                        const float *__restrict__ tau, const float *__restrict__ img,
-                                                        const float *__restrict__ vgrad, const float *__restrict__ wgt,
-                                                        float s2, uint8_t *__restrict__ vis, float *__restrict__ U,
-                                                        float *__restrict__ gx, float *__restrict__ gy,
-                                                        float *__restrict__ mask) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W || y >= H) return;
-    float u0 = 0.f, u1 = 0.f, u2 = 0.f, wn = 0.f;   // weighted average
+struct SetupAcc {
+    float u0 = 0.f, u1 = 0.f, u2 = 0.f, wn = 0.f;  // weighted average
     float g0 = 0.f, g1 = 0.f, g2 = 0.f, nrm = 0.f;  // gradient splat
     bool any = false;
+    __device__ __forceinline__ void add(float A, float raw, float w, float c0, float c1, float c2, float s0, float s1) {
+        any |= (raw != 0.0f);
+        const float wA = w * A;
+        wn += wA;
+        u0 += wA * c0;
+        u1 += wA * c1;
+        u2 += wA * c2;
+        nrm += A;
+        g0 += A * s0;
+        g1 += A * s1;
+        g2 += A * w;
+    }
+    __device__ __forceinline__ void store(size_t o, size_t N, float s2, uint8_t *vis, float *U, float *gx, float *gy,
+                                          float *mask) {
+        vis[o] = any ? 1 : 0;
+        if (wn != 0.f) {
+            u0 /= wn;
+            u1 /= wn;
+            u2 /= wn;
+        }
+        U[o] = u0;
+        U[N + o] = u1;
+        U[2 * N + o] = u2;
+        if (nrm != 0.f) {
+            g0 /= nrm;
+            g1 /= nrm;
+            g2 /= nrm;
+        }
+        gx[o] = g0;
+        gy[o] = g1;
+        mask[o] = g2 * s2;
+    }
+};
+
+// The set-up of one target pixel reading every entry straight from global memory.
+template <int KS>
+__device__ __forceinline__ void gradient_setup_global(int x, int y, int W, int H, int n, int dsf, int BW,
+                                                      const unsigned int *__restrict__ start,
+                                                      const unsigned int *__restrict__ entries,
+                                                      const float *__restrict__ tau, const float *__restrict__ img,
+                                                      const float *__restrict__ vgrad, const float *__restrict__ wgt,
+                                                      SetupAcc &acc) {
 #pragma unroll
     for (int i = 0; i < KS; ++i) {
 #pragma unroll
@@ -304,40 +338,194 @@ __global__ void __launch_bounds__(256) k_gradient_setup(int W, int H, int n, int
                 const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
                 float raw;
                 const float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw);
-                any |= (raw != 0.0f);
-                const float w = __ldg(wgt + (size_t)v * n + m);
-                const float wA = w * A;
                 const float *iv = img + (size_t)v * 3 * n;
-                wn += wA;
-                u0 += wA * __ldg(iv + m);
-                u1 += wA * __ldg(iv + n + m);
-                u2 += wA * __ldg(iv + 2 * n + m);
                 const float *gv = vgrad + (size_t)v * 2 * n;
-                nrm += A;
-                g0 += A * __ldg(gv + m);
-                g1 += A * __ldg(gv + n + m);
-                g2 += A * w;
+                acc.add(A, raw, __ldg(wgt + (size_t)v * n + m), __ldg(iv + m), __ldg(iv + n + m), __ldg(iv + 2 * n + m),
+                        __ldg(gv + m), __ldg(gv + n + m));
             }
         }
     }
-    const size_t o = (size_t)y * W + x, N = (size_t)W * H;
-    vis[o] = any ? 1 : 0;
-    if (wn != 0.f) {
-        u0 /= wn;
-        u1 /= wn;
-        u2 /= wn;
+}
+
+// Anchor-row form (KS <= 3). The entries of one anchor bucket reach a KS x KS block of target pixels, so
+// instead of every target pixel re-reading the entries of its KS^2 buckets, a lane owns one bucket, reads
+// each of its entries once and accumulates all KS^2 taps in registers (partials P[i][j][field]). A warp owns
+// 32 consecutive anchors of one anchor row; pixel x of tap row i sums P[i][0] of anchor x, P[i][1] of anchor
+// x-1, ... (warp shuffles, fixed order), and the block adds the KS tap rows of each pixel from shared memory
+// in fixed order. Lanes 0 .. KS-2 only feed their right neighbours, so a warp outputs 33 - KS pixels.
+// The summation order differs from the per-pixel form (per-bucket partials first) but is fixed, so results
+// are deterministic. Fields: 0 w A, 1-3 w A v, 4 A, 5-6 A Sobel, 7 A w, 8 visibility (raw overlap != 0).
+constexpr int kGrWarps = 8;
+
+template <int KS>
+__global__ void __launch_bounds__(kGrWarps * 32, 2) k_gradient_setup_rows(int W, int H, int n, int dsf, int BW,
+                                                                       const unsigned int *__restrict__ start,
+                                                                       const unsigned int *__restrict__ entries,
+                                                                       const float *__restrict__ tau,
+                                                                       const float *__restrict__ img,
+                                                                       const float *__restrict__ vgrad,
+                                                                       const float *__restrict__ wgt, float s2,
+                                                                       uint8_t *__restrict__ vis,
+                                                                       float *__restrict__ U, float *__restrict__ gx,
+                                                                       float *__restrict__ gy,
+                                                                       float *__restrict__ mask) {
+    constexpr int TXO = 33 - KS;                 // output pixels per warp row
+    constexpr int ROWS = kGrWarps * 2;           // anchor rows per block (2 per warp: 2w, 2w + 1)
+    constexpr int TY = ROWS - (KS - 1);          // output pixel rows per block
+    constexpr int NF = 9;
+    __shared__ float part[TY][KS][TXO][NF];      // (pixel row, tap row, pixel, field)
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x0 = blockIdx.x * TXO, y0 = blockIdx.y * TY;
+    const int BH = H + KS - 1;
+    const int bx = x0 + lane;                    // bucket column = anchor x + KS - 1
+    const int ax = bx - (KS - 1);
+    // warp w takes anchor rows 2w and 2w + 1: one of each parity (with dsf = 2 the populated anchors often
+    // sit on every other row, so rows w and w + 8 would leave half the warps idle)
+    for (int q = 0; q < 2; ++q) {
+        const int rr = 2 * warp + q;
+        const int ay = y0 - (KS - 1) + rr, by = ay + KS - 1;
+        float P[KS][KS][8];
+#pragma unroll
+        for (int i = 0; i < KS; ++i)
+#pragma unroll
+            for (int j = 0; j < KS; ++j)
+#pragma unroll
+                for (int f = 0; f < 8; ++f) P[i][j][f] = 0.f;
+        unsigned int anyb = 0;
+        if (bx < BW && by < BH) {
+            const size_t b = (size_t)by * BW + bx;
+            const unsigned int s = __ldg(start + b), e = __ldg(start + b + 1);
+            // software pipeline: the entry index two ahead and the source data one ahead are in flight while
+            // the current entry is accumulated
+            struct Src {
+                float tx, ty, w, c0, c1, c2, s0, s1;
+            };
+            auto fetch = [&](unsigned int ent) {
+                const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
+                const float *iv = img + (size_t)v * 3 * n;
+                const float *gv = vgrad + (size_t)v * 2 * n;
+                Src d;
+                d.tx = __ldg(tau + (size_t)v * 2 * n + m);
+                d.ty = __ldg(tau + (size_t)v * 2 * n + n + m);
+                d.w = __ldg(wgt + (size_t)v * n + m);
+                d.c0 = __ldg(iv + m);
+                d.c1 = __ldg(iv + n + m);
+                d.c2 = __ldg(iv + 2 * n + m);
+                d.s0 = __ldg(gv + m);
+                d.s1 = __ldg(gv + n + m);
+                return d;
+            };
+            Src cur = {};
+            unsigned int ent_next = 0;
+            if (s < e) cur = fetch(__ldg(entries + s));
+            if (s + 1 < e) ent_next = __ldg(entries + s + 1);
+            for (unsigned int k = s; k < e; ++k) {
+                Src nxt = {};
+                if (k + 1 < e) nxt = fetch(ent_next);
+                if (k + 2 < e) ent_next = __ldg(entries + k + 2);
+                const float tx = cur.tx, ty = cur.ty, w = cur.w, c0 = cur.c0, c1 = cur.c1, c2 = cur.c2;
+                const float s0 = cur.s0, s1 = cur.s1;
+                cur = nxt;
+                const float px = tx - 0.5f, py = ty - 0.5f;
+                float dxs[KS], dys[KS];
+#pragma unroll
+                for (int q = 0; q < KS; ++q) {
+                    dxs[q] = fp_overlap(q, KS, ax + q, px, dsf);
+                    dys[q] = fp_overlap(q, KS, ay + q, py, dsf);
+                }
+                float a[KS][KS], norm = 0.f;
+#pragma unroll
+                for (int j = 0; j < KS; ++j)
+#pragma unroll
+                    for (int i = 0; i < KS; ++i) {
+                        const int x = ax + j, y = ay + i;
+                        const bool in = (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1);
+                        a[i][j] = in ? __fmul_rn(dxs[j], dys[i]) : 0.0f;
+                        norm = __fadd_rn(norm, a[i][j]);
+                    }
+#pragma unroll
+                for (int i = 0; i < KS; ++i)
+#pragma unroll
+                    for (int j = 0; j < KS; ++j) {
+                        const float A = (norm != 0.0f) ? __fdiv_rn(a[i][j], norm) : a[i][j];
+                        if (a[i][j] != 0.0f) anyb |= 1u << (i * KS + j);
+                        const float wA = w * A;
+                        P[i][j][0] += wA;
+                        P[i][j][1] += wA * c0;
+                        P[i][j][2] += wA * c1;
+                        P[i][j][3] += wA * c2;
+                        P[i][j][4] += A;
+                        P[i][j][5] += A * s0;
+                        P[i][j][6] += A * s1;
+                        P[i][j][7] += A * w;
+                    }
+            }
+        }
+        // merge along x: pixel ax (this lane) takes tap j of anchor ax - j (lane - j)
+#pragma unroll
+        for (int i = 0; i < KS; ++i) {
+            const int py = ay + i - y0;  // output pixel row inside the tile
+            float sum[8];
+            unsigned int anyp = 0;
+#pragma unroll
+            for (int f = 0; f < 8; ++f) sum[f] = P[i][0][f];
+            anyp |= (anyb >> (i * KS)) & 1u;
+#pragma unroll
+            for (int j = 1; j < KS; ++j) {
+#pragma unroll
+                for (int f = 0; f < 8; ++f) sum[f] += __shfl_up_sync(0xffffffffu, P[i][j][f], j);
+                anyp |= (__shfl_up_sync(0xffffffffu, anyb, j) >> (i * KS + j)) & 1u;
+            }
+            if (lane >= KS - 1 && py >= 0 && py < TY) {
+                float *dst = part[py][i][lane - (KS - 1)];
+#pragma unroll
+                for (int f = 0; f < 8; ++f) dst[f] = sum[f];
+                dst[8] = anyp ? 1.f : 0.f;
+            }
+        }
     }
-    U[o] = u0;
-    U[N + o] = u1;
-    U[2 * N + o] = u2;
-    if (nrm != 0.f) {
-        g0 /= nrm;
-        g1 /= nrm;
-        g2 /= nrm;
+    __syncthreads();
+    // add the tap rows of every pixel in order and normalise (as SetupAcc::store)
+    const size_t N = (size_t)W * H;
+    for (int p = threadIdx.x; p < TY * TXO; p += kGrWarps * 32) {
+        const int lx = p % TXO, ly = p / TXO, x = x0 + lx, y = y0 + ly;
+        if (x >= W || y >= H) continue;
+        SetupAcc acc;
+        float any = 0.f;
+#pragma unroll
+        for (int i = 0; i < KS; ++i) {
+            const float *c = part[ly][i][lx];
+            acc.wn += c[0];
+            acc.u0 += c[1];
+            acc.u1 += c[2];
+            acc.u2 += c[3];
+            acc.nrm += c[4];
+            acc.g0 += c[5];
+            acc.g1 += c[6];
+            acc.g2 += c[7];
+            any += c[8];
+        }
+        acc.any = any != 0.f;
+        acc.store((size_t)y * W + x, N, s2, vis, U, gx, gy, mask);
     }
-    gx[o] = g0;
-    gy[o] = g1;
-    mask[o] = g2 * s2;
+}
+
+// Per-pixel form for KS > 3 (too many register partials for the anchor-row form).
+template <int KS>
+__global__ void __launch_bounds__(256) k_gradient_setup_px(int W, int H, int n, int dsf, int BW,
+                                                           const unsigned int *__restrict__ start,
+                                                           const unsigned int *__restrict__ entries,
+                                                           const float *__restrict__ tau, const float *__restrict__ img,
+                                                           const float *__restrict__ vgrad,
+                                                           const float *__restrict__ wgt, float s2,
+                                                           uint8_t *__restrict__ vis, float *__restrict__ U,
+                                                           float *__restrict__ gx, float *__restrict__ gy,
+                                                           float *__restrict__ mask) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    SetupAcc acc;
+    gradient_setup_global<KS>(x, y, W, H, n, dsf, BW, start, entries, tau, img, vgrad, wgt, acc);
+    acc.store((size_t)y * W + x, (size_t)W * H, s2, vis, U, gx, gy, mask);
 }
 
 // Weighted average (coco_vtv_sr_compute_initial_image sources/optimization.cu:1300-1344):
@@ -491,6 +679,19 @@ __global__ void k_sobel(int W, int H, const float *__restrict__ rgb, size_t in_s
 // vtv_rof.cu:280-320, primal prox cuda_kernels.cu:504-532) fused: the duals of the pixel and of its left
 // and upper neighbours are recomputed from the previous iterate so one launch reads (U, P, F, g) and
 // writes (U', P'). Ping-pong buffers keep the Jacobi semantics of the reference's separate launches.
+// Reprojection of the 6 dual components onto the Frobenius ball of radius r (vtv_rof.cu:280-320).
+__device__ __forceinline__ void rof_project(float p[6], float r) {
+    float nn = 0.f;
+    nn += p[0] * p[0] + p[2] * p[2] + p[4] * p[4];
+    nn += p[1] * p[1] + p[3] * p[3] + p[5] * p[5];
+    nn = sqrtf(nn);
+    if (nn > r) {
+        const float s = r / nn;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) p[k] *= s;
+    }
+}
+
 __device__ __forceinline__ void rof_dual(int x, int y, int W, int H, size_t N, float sigma,
                                          const float *__restrict__ U, const float *__restrict__ P,
                                          const float *__restrict__ g, float p[6]) {
@@ -503,16 +704,7 @@ __device__ __forceinline__ void rof_dual(int x, int y, int W, int H, size_t N, f
         p[2 * c] = __ldg(P + (2 * c) * N + o) + sigma * gxv;
         p[2 * c + 1] = __ldg(P + (2 * c + 1) * N + o) + sigma * gyv;
     }
-    float nn = 0.f;
-    nn += p[0] * p[0] + p[2] * p[2] + p[4] * p[4];
-    nn += p[1] * p[1] + p[3] * p[3] + p[5] * p[5];
-    nn = sqrtf(nn);
-    const float r = __ldg(g + o);
-    if (nn > r) {
-        const float s = r / nn;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) p[k] *= s;
-    }
+    rof_project(p, __ldg(g + o));
 }
 
 __global__ void __launch_bounds__(256) k_rof_iter(int W, int H, float tau, float sigma, float lam,
@@ -536,6 +728,99 @@ __global__ void __launch_bounds__(256) k_rof_iter(int W, int H, float tau, float
         if (y > 0) step -= pt[2 * c + 1];
         const float unew = __ldg(U + c * N + o) + tau * step;
         Uo[c * N + o] = (tau * __ldg(F + c * N + o) + lam * unew) / denom;
+    }
+}
+
+// All niter inner ROF iterations in one cooperative launch, temporally blocked. Each super-step runs up to
+// kRofK iterations: a block stages a (kRofTX + 2 kRofK) x (kRofTY + 2 kRofK) region of U, P, F, g in shared
+// memory, iterates there (dual step + reprojection in place, then the primal prox in place; each pixel's
+// arithmetic is k_rof_iter's), and writes back its kRofTX x kRofTY tile, whose values depend only on the
+// region (the halo absorbs one pixel of staleness per iteration from each side). Super-steps read one
+// global (U, P) pair and write the other, with a bounded grid barrier between them.
+constexpr int kRofTX = 32, kRofTY = 16, kRofK = 4, kRofThreads = 256;
+constexpr int kRofRX = kRofTX + 2 * kRofK, kRofRY = kRofTY + 2 * kRofK, kRofRN = kRofRX * kRofRY;
+constexpr size_t kRofSmem = (size_t)13 * kRofRN * sizeof(float);  // U 3, P 6, F 3, g 1 planes
+
+__global__ void __launch_bounds__(kRofThreads) k_rof_persistent(int W, int H, int niter, float tau, float sigma,
+                                                                float lam, float *U0, float *P0, float *U1,
+                                                                float *P1, const float *__restrict__ F,
+                                                                const float *__restrict__ g, GridBarrier gb) {
+    extern __shared__ float sm[];
+    float *sU = sm, *sP = sm + 3 * kRofRN, *sF = sm + 9 * kRofRN, *sG = sm + 12 * kRofRN;
+    const int tiles_x = (W + kRofTX - 1) / kRofTX, ntiles = tiles_x * ((H + kRofTY - 1) / kRofTY);
+    const size_t N = (size_t)W * H;
+    const float denom = tau + lam;
+    unsigned int gen = 0;
+    int step = 0;
+    for (int done = 0; done < niter; done += kRofK, ++step) {
+        const int iters = min(kRofK, niter - done);
+        const float *Ui = (step & 1) ? U1 : U0, *Pi = (step & 1) ? P1 : P0;
+        float *Uo = (step & 1) ? U0 : U1, *Po = (step & 1) ? P0 : P1;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            const int rx0 = (t % tiles_x) * kRofTX - kRofK, ry0 = (t / tiles_x) * kRofTY - kRofK;
+            for (int i = threadIdx.x; i < kRofRN; i += kRofThreads) {
+                const int gx = rx0 + i % kRofRX, gy = ry0 + i / kRofRX;
+                const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+                const size_t o = in ? (size_t)gy * W + gx : 0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    sU[c * kRofRN + i] = in ? __ldcg(Ui + c * N + o) : 0.f;
+                    sF[c * kRofRN + i] = in ? __ldg(F + c * N + o) : 0.f;
+                }
+#pragma unroll
+                for (int c = 0; c < 6; ++c) sP[c * kRofRN + i] = in ? __ldcg(Pi + c * N + o) : 0.f;
+                sG[i] = in ? __ldg(g + o) : 0.f;
+            }
+            __syncthreads();
+            for (int it = 0; it < iters; ++it) {
+                // dual step + reprojection (rof_dual), in place: reads U (unchanged here) and the pixel's own P
+                for (int i = threadIdx.x; i < kRofRN; i += kRofThreads) {
+                    const int lx = i % kRofRX, ly = i / kRofRX, gx = rx0 + lx, gy = ry0 + ly;
+                    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+                    float p[6];
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float *u = sU + c * kRofRN;
+                        const float uc = u[i];
+                        const float ur = (lx + 1 < kRofRX) ? u[i + 1] : 0.f, ud = (ly + 1 < kRofRY) ? u[i + kRofRX] : 0.f;
+                        const float gxv = (gx < W - 1) ? ur - uc : 0.f;
+                        const float gyv = (gy < H - 1) ? ud - uc : 0.f;
+                        p[2 * c] = sP[(2 * c) * kRofRN + i] + sigma * gxv;
+                        p[2 * c + 1] = sP[(2 * c + 1) * kRofRN + i] + sigma * gyv;
+                    }
+                    rof_project(p, sG[i]);
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) sP[k * kRofRN + i] = p[k];
+                }
+                __syncthreads();
+                // primal prox (k_rof_iter), in place: reads the new duals of the pixel and its left / upper neighbour
+                for (int i = threadIdx.x; i < kRofRN; i += kRofThreads) {
+                    const int lx = i % kRofRX, ly = i / kRofRX, gx = rx0 + lx, gy = ry0 + ly;
+                    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        float st = sP[(2 * c) * kRofRN + i] + sP[(2 * c + 1) * kRofRN + i];
+                        if (gx > 0) st -= (lx > 0) ? sP[(2 * c) * kRofRN + i - 1] : 0.f;
+                        if (gy > 0) st -= (ly > 0) ? sP[(2 * c + 1) * kRofRN + i - kRofRX] : 0.f;
+                        const float unew = sU[c * kRofRN + i] + tau * st;
+                        sU[c * kRofRN + i] = (tau * sF[c * kRofRN + i] + lam * unew) / denom;
+                    }
+                }
+                __syncthreads();
+            }
+            for (int i = threadIdx.x; i < kRofTX * kRofTY; i += kRofThreads) {
+                const int lx = kRofK + i % kRofTX, ly = kRofK + i / kRofTX, gx = rx0 + lx, gy = ry0 + ly;
+                if (gx >= W || gy >= H) continue;
+                const size_t o = (size_t)gy * W + gx;
+                const int r = ly * kRofRX + lx;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) Uo[c * N + o] = sU[c * kRofRN + r];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) Po[c * N + o] = sP[c * kRofRN + r];
+            }
+            __syncthreads();  // the next tile overwrites the staged region
+        }
+        if (!grid_sync(gb, gen)) return;
     }
 }
 
@@ -735,12 +1020,33 @@ void launch_u_gradient(const Geometry &G, const Buckets &B, const float *tau, co
     lc.add(1);
 }
 
+template <int KS>
+static void gradient_setup_ks(const Geometry &G, const Buckets &B, const float *tau, const float *img,
+                              const float *vgrad, const float *wgt, float s2, uint8_t *vis, float *U, float *gx,
+                              float *gy, float *mask, cudaStream_t st) {
+    if constexpr (KS <= 3) {
+        constexpr int TXO = 33 - KS, TY = kGrWarps * 2 - (KS - 1);
+        const dim3 g((G.W + TXO - 1) / TXO, (G.H + TY - 1) / TY);
+        k_gradient_setup_rows<KS><<<g, kGrWarps * 32, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau,
+                                                             img, vgrad, wgt, s2, vis, U, gx, gy, mask);
+    } else {
+        k_gradient_setup_px<KS><<<grid2(G.W, G.H, kTile), kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start,
+                                                                        B.entries, tau, img, vgrad, wgt, s2, vis, U,
+                                                                        gx, gy, mask);
+    }
+}
+
 void launch_gradient_setup(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *vgrad,
                            const float *wgt, float s2, uint8_t *vis, float *U, float *gx, float *gy, float *mask,
                            cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "gradient_setup", st);
-    LFRV_KS_DISPATCH(G.dsf + 1, k_gradient_setup, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW,
-                     B.start, B.entries, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask);
+    switch (G.dsf + 1) {
+        case 2: gradient_setup_ks<2>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
+        case 3: gradient_setup_ks<3>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
+        case 4: gradient_setup_ks<4>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
+        case 5: gradient_setup_ks<5>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
+        default: break;
+    }
     lc.add(1);
 }
 
@@ -752,6 +1058,29 @@ void launch_sobel(int W, int H, int count, const float *rgb, size_t in_stride, s
     lc.add(1);
 }
 int sobel_partials(int W, int H) { return ((W + 31) / 32) * ((H + 7) / 8); }
+
+// Number of super-steps of k_rof_persistent for niter iterations: the result is in (U1, P1) when it is odd.
+int rof_persistent_steps(int niter) { return (niter + kRofK - 1) / kRofK; }
+
+cudaError_t launch_rof_persistent(int W, int H, int niter, float tau, float sigma, float lam, float *U0, float *P0,
+                                  float *U1, float *P1, const float *F, const float *g, GridBarrier gb, cudaStream_t st,
+                                  LaunchCounter &lc) {
+    ProfScope _ps(lc, "rof_persistent", st);
+    cudaError_t e = cudaFuncSetAttribute(k_rof_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRofSmem);
+    if (e != cudaSuccess) return e;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rof_persistent, kRofThreads, kRofSmem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int ntiles = ((W + kRofTX - 1) / kRofTX) * ((H + kRofTY - 1) / kRofTY);
+    const int blocks = std::min(ntiles, sms * per_sm);
+    void *args[] = {&W, &H, &niter, &tau, &sigma, &lam, &U0, &P0, &U1, &P1, (void *)&F, (void *)&g, &gb};
+    lc.add(1);
+    return cudaLaunchCooperativeKernel((const void *)k_rof_persistent, dim3(blocks), dim3(kRofThreads), args, kRofSmem,
+                                       st);
+}
 
 void launch_rof_iter(int W, int H, float tau, float sigma, float lam, const float *U, const float *P, const float *F,
                      const float *g, float *Uo, float *Po, cudaStream_t st, LaunchCounter &lc) {
