@@ -9,9 +9,13 @@
 // updates (updateSolution :130-198, updateDir :508-523) are restated here; the dot products are FP64
 // block partials reduced in a fixed order (the reference accumulates float atomics in arbitrary order).
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
+#include <cudaTypedefs.h>
+
 #include "device_common.cuh"
+#include "tma.cuh"
 #include "kernels.h"
 #include "lfrv_internal.h"
 
@@ -363,20 +367,87 @@ __device__ __forceinline__ float tile_op(const float (*t)[kHaloX], int tx, int t
     return lambda * c + lx + ly;
 }
 
+// TMA form of the operator phases: each tile's halo arrives as one 3-D box per array (all 3 planes), x origin
+// rounded down to a 16-byte boundary (x0 - 4), double-buffered so the next tile's box is in flight while the
+// current one is used. Box rows are padded to a 128-byte multiple in shared memory.
+constexpr int kBoxX = kTileX + 8, kBoxY = kTileY + 2, kBoxPlane = kBoxX * kBoxY;
+constexpr unsigned kBoxBytes = 3u * kBoxPlane * sizeof(float);
+constexpr int kBoxStride = ((kBoxBytes + 127) / 128) * 128 / sizeof(float);  // floats between box buffers
+constexpr size_t kCgTmaSmem = 4 * (size_t)kBoxStride * sizeof(float) + 128;   // 2 stages x 2 arrays + alignment
+
+// Operator of updateAlpha on a box in shared memory: f(i) is the value at box index i.
+template <class F>
+__device__ __forceinline__ float box_op(F f, int i, int x, int y, int W, int H, float lambda) {
+    const float c = f(i);
+    float lx, ly;
+    if (x == 0) lx = c - f(i + 1);
+    else if (x < W - 1) lx = 2.f * c - f(i - 1) - f(i + 1);
+    else lx = c - f(i - 1);
+    if (y == 0) ly = c - f(i + kBoxX);
+    else if (y < H - 1) ly = 2.f * c - f(i - kBoxX) - f(i + kBoxX);
+    else ly = c - f(i - kBoxX);
+    return lambda * c + lx + ly;
+}
+
+// Thread 0 waits (bounded) for the stage's box; the block learns the outcome through shared memory, then every
+// other thread observes the completed phase itself (it returns at once) so the box contents are visible to it.
+__device__ __forceinline__ bool block_wait_box(uint64_t *bar, unsigned parity, int *s_flag) {
+    if (threadIdx.x == 0) *s_flag = mbar_wait(bar, parity, kSpinLimit) ? 1 : 0;
+    __syncthreads();
+    const bool ok = *s_flag != 0;
+    if (ok && threadIdx.x != 0) mbar_wait(bar, parity, kSpinLimit);
+    return ok;
+}
+
 // Corrected CG of the IBR_gradient normal equations, all iterations in one launch. State layout (doubles):
 // [0..2] delta, [3] E, [4] gap, [5] iterations, [6] status (0 ok, 1 barrier timeout).
+// TMA = true reads the operator phases' tiles through the tensor maps of r, dA and dB (W a multiple of 4).
+template <bool TMA>
 __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H, const float *__restrict__ gX,
                                                                    const float *__restrict__ gY, float *U, float *r,
                                                                    float *dA, float *dB, double *partA,
                                                                    double *partB, GridBarrier gb, int max_iter,
-                                                                   double gap_tol, double *state) {
+                                                                   double gap_tol, double *state,
+                                                                   const __grid_constant__ CUtensorMap mapR,
+                                                                   const __grid_constant__ CUtensorMap mapA,
+                                                                   const __grid_constant__ CUtensorMap mapB) {
     __shared__ double sh[8];
     const size_t N = (size_t)W * H;
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nthr = (size_t)gridDim.x * blockDim.x;
-    __shared__ float tile[3][kHaloY][kHaloX];
+    __shared__ float tile[TMA ? 1 : 3][TMA ? 1 : kHaloY][TMA ? 1 : kHaloX];
+    extern __shared__ __align__(128) float dyn_smem[];
+    // TMA destinations: [stage][array][kBoxStride], 128-byte aligned explicitly
+    float *boxes = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(dyn_smem) + 127) & ~uintptr_t(127));
+    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ int s_flag;
+    unsigned par[2] = {0u, 0u};
     const int tiles_x = (W + kTileX - 1) / kTileX, ntiles = tiles_x * ((H + kTileY - 1) / kTileY);
+    const int nk = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
     const float lambda = 1.0f;
     unsigned int gen = 0;
+    if (TMA && threadIdx.x == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_proxy_async_smem();
+    }
+    __syncthreads();
+    // thread 0 starts the loads of this block's k-th tile: arrays a0 (and a1 when two) into stage k & 1
+    auto issue = [&](int k, const CUtensorMap *a0, const CUtensorMap *a1) {
+        if (threadIdx.x != 0) return;
+        const int t = (int)blockIdx.x + k * (int)gridDim.x, st = k & 1;
+        const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&bars[st], a1 ? 2 * kBoxBytes : kBoxBytes);
+        tma_load_3d(boxes + (size_t)(2 * st) * kBoxStride, a0, x0 - 4, y0 - 1, 0, &bars[st]);
+        if (a1) tma_load_3d(boxes + (size_t)(2 * st + 1) * kBoxStride, a1, x0 - 4, y0 - 1, 0, &bars[st]);
+    };
+    // on a box that never arrived: flag the error, give the other stage's load a bounded wait, leave
+    auto abandon = [&](int k) {
+        if (threadIdx.x == 0) {
+            atomicExch(gb.err, 1);
+            if (k + 1 < nk) mbar_wait(&bars[(k + 1) & 1], par[(k + 1) & 1], kSpinLimit);
+        }
+    };
     // ---- phase 0: r = b - A x (initConjGrad, solver.cu:383-467) and E(x0) = 1/2 ||grad x0 - g||^2 (x0 = u0)
     {
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
@@ -412,6 +483,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
         }
         block_partials_f(acc, 4, partB, gridDim.x);
     }
+    if (TMA) fence_proxy_async_global();
     if (!grid_sync(gb, gen)) return;
     block_reduce_partials(partB, gridDim.x, 4, sh);
     // The FP64 scalars (delta, E, gap) live in thread 0 of each block, which derives the float coefficients
@@ -435,8 +507,41 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
         __syncthreads();
         if (s_stop) break;
         // ---- phase A: d = r + beta d_old on each tile + halo in shared memory, q = A d, d . q
-        {
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        float accA[4] = {0.f, 0.f, 0.f, 0.f};
+        if constexpr (TMA) {
+            const CUtensorMap *mdold = (dold == r) ? &mapR : (dold == dA ? &mapA : &mapB);
+            if (nk > 0) issue(0, &mapR, mdold);
+            for (int k = 0; k < nk; ++k) {
+                if (k + 1 < nk) issue(k + 1, &mapR, mdold);
+                const int st = k & 1;
+                if (!block_wait_box(&bars[st], par[st], &s_flag)) {
+                    abandon(k);
+                    return;
+                }
+                par[st] ^= 1u;
+                const int t = (int)blockIdx.x + k * (int)gridDim.x;
+                const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
+                const float *R = boxes + (size_t)(2 * st) * kBoxStride, *D = R + kBoxStride;
+                for (int p = threadIdx.x; p < kTileX * kTileY; p += blockDim.x) {
+                    const int lx = p % kTileX, ly = p / kTileX, x = x0 + lx, y = y0 + ly;
+                    if (x >= W || y >= H) continue;
+                    const size_t o = (size_t)y * W + x;
+                    const int bi = (ly + 1) * kBoxX + (lx + 4);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float *Rc = R + c * kBoxPlane, *Dc = D + c * kBoxPlane;
+                        const float b = beta[c];
+                        auto v = [&](int i) { return Rc[i] + b * Dc[i]; };
+                        const float qv = box_op(v, bi, x, y, W, H, lambda);
+                        const float dcv = v(bi);
+                        dnew[c * N + o] = dcv;
+                        accA[c] += dcv * qv;
+                    }
+                }
+                __syncthreads();
+            }
+        } else {
+            float *acc = accA;
             for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
                 const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
                 for (int k = threadIdx.x; k < 3 * kHaloY * kHaloX; k += blockDim.x) {
@@ -464,8 +569,9 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                 }
                 __syncthreads();
             }
-            block_partials_f(acc, 3, partA, gridDim.x);
         }
+        block_partials_f(accA, 3, partA, gridDim.x);
+        if (TMA) fence_proxy_async_global();
         if (!grid_sync(gb, gen)) return;
         block_reduce_partials(partA, gridDim.x, 3, sh);
         if (threadIdx.x == 0) {
@@ -479,8 +585,42 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
         __syncthreads();
         const float alpha[3] = {s_coef[0], s_coef[1], s_coef[2]};
         // ---- phase B: x += alpha d, r -= alpha A d, r . r (d tile + halo in shared memory)
-        {
-            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        float accB[4] = {0.f, 0.f, 0.f, 0.f};
+        if constexpr (TMA) {
+            const CUtensorMap *mdnew = (dnew == dA) ? &mapA : &mapB;
+            if (nk > 0) issue(0, mdnew, nullptr);
+            for (int k = 0; k < nk; ++k) {
+                if (k + 1 < nk) issue(k + 1, mdnew, nullptr);
+                const int st = k & 1;
+                if (!block_wait_box(&bars[st], par[st], &s_flag)) {
+                    abandon(k);
+                    return;
+                }
+                par[st] ^= 1u;
+                const int t = (int)blockIdx.x + k * (int)gridDim.x;
+                const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
+                const float *Dn = boxes + (size_t)(2 * st) * kBoxStride;
+                for (int p = threadIdx.x; p < kTileX * kTileY; p += blockDim.x) {
+                    const int lx = p % kTileX, ly = p / kTileX, x = x0 + lx, y = y0 + ly;
+                    if (x >= W || y >= H) continue;
+                    const size_t o = (size_t)y * W + x;
+                    const int bi = (ly + 1) * kBoxX + (lx + 4);
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float *Dc = Dn + c * kBoxPlane;
+                        auto v = [&](int i) { return Dc[i]; };
+                        const float qv = box_op(v, bi, x, y, W, H, lambda);
+                        const float dv = Dc[bi];
+                        U[c * N + o] = __ldcg(U + c * N + o) + alpha[c] * dv;
+                        const float rv = __ldcg(r + c * N + o) - alpha[c] * qv;
+                        r[c * N + o] = rv;
+                        accB[c] += rv * rv;
+                    }
+                }
+                __syncthreads();
+            }
+        } else {
+            float *acc = accB;
             for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
                 const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
                 for (int k = threadIdx.x; k < 3 * kHaloY * kHaloX; k += blockDim.x) {
@@ -506,8 +646,9 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                 }
                 __syncthreads();
             }
-            block_partials_f(acc, 3, partB, gridDim.x);
         }
+        block_partials_f(accB, 3, partB, gridDim.x);
+        if (TMA) fence_proxy_async_global();
         if (!grid_sync(gb, gen)) return;
         block_reduce_partials(partB, gridDim.x, 3, sh);
         if (threadIdx.x == 0) {
@@ -622,11 +763,11 @@ void launch_hole_list(int W, int H, const uint8_t *vis, int *holes, int *count, 
 int hole_fill_partials(int nholes) { return (nholes + 255) / 256; }
 
 // Blocks of a cooperative launch: every block must be resident at once (the grid barrier waits for all).
-static int coop_blocks(const void *kernel, int want) {
+static int coop_blocks(const void *kernel, int want, size_t smem = 0) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistThreads, smem);
     per_sm = per_sm < 2 ? per_sm : 2;
     const int resident = sms * per_sm;
     return want < resident ? (want > 0 ? want : 1) : resident;
@@ -645,12 +786,47 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
     ProfScope _ps(lc, "cg_persistent", st);
     const size_t N = (size_t)W * H;
     const int ntiles = ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
-    const int blocks = coop_blocks((const void *)k_cg_persistent,
-                                   std::max(ntiles, (int)((N + kPersistThreads - 1) / kPersistThreads)));
-    void *args[] = {&W, &H, (void *)&gx, (void *)&gy, &U, &r, &dA, &dB, &partA, &partB, &gb, &max_iter, &gap_tol,
-                    &state};
+    // the TMA form needs row pitches of a multiple of 16 bytes (W % 4 == 0) and the driver's encoder
+    CUtensorMap maps[3];
+    const bool tma = encode_tensor_map_3d(&maps[0], r, W, H, 3, kBoxX, kBoxY, 3) &&
+                     encode_tensor_map_3d(&maps[1], dA, W, H, 3, kBoxX, kBoxY, 3) &&
+                     encode_tensor_map_3d(&maps[2], dB, W, H, 3, kBoxX, kBoxY, 3);
+    if (!tma) std::memset(maps, 0, sizeof(maps));
+    const void *kern = tma ? (const void *)k_cg_persistent<true> : (const void *)k_cg_persistent<false>;
+    const size_t smem = tma ? kCgTmaSmem : 0;
+    if (tma) {
+        const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    const int blocks = coop_blocks(kern, std::max(ntiles, (int)((N + kPersistThreads - 1) / kPersistThreads)), smem);
+    void *args[] = {&W,     &H,        (void *)&gx, (void *)&gy, &U,       &r,       &dA,      &dB, &partA,
+                    &partB, &gb,       &max_iter,   &gap_tol,    &state,   &maps[0], &maps[1], &maps[2]};
     lc.add(1);
-    return cudaLaunchCooperativeKernel((const void *)k_cg_persistent, dim3(blocks), dim3(kPersistThreads), args, 0, st);
+    return cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(kPersistThreads), args, smem, st);
+}
+
+bool encode_tensor_map_3d(CUtensorMap *map, const float *base, int cols, int rows, int planes, int box_x, int box_y,
+                          int box_z) {
+    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+        cudaGetLastError();
+    });
+    if (!encode || !base || cols <= 0 || rows <= 0 || planes <= 0) return false;
+    if (((size_t)cols * sizeof(float)) % 16 != 0 || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)planes};
+    const cuuint64_t strides[2] = {(cuuint64_t)cols * sizeof(float), (cuuint64_t)cols * rows * sizeof(float)};
+    const cuuint32_t box[3] = {(cuuint32_t)box_x, (cuuint32_t)box_y, (cuuint32_t)box_z};
+    const cuuint32_t estride[3] = {1, 1, 1};
+    return encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<float *>(base), dims, strides, box, estride,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 cudaError_t launch_hole_fill_persistent(int W, int H, const int *holes, const int *count, float *A, float *B,

@@ -433,21 +433,27 @@ __global__ void __launch_bounds__(kGrWarps * 32, 2) k_gradient_setup_rows(int W,
                     dxs[q] = fp_overlap(q, KS, ax + q, px, dsf);
                     dys[q] = fp_overlap(q, KS, ay + q, py, dsf);
                 }
+                bool inx[KS], iny[KS];
+#pragma unroll
+                for (int q = 0; q < KS; ++q) {
+                    inx[q] = (0 <= ax + q && ax + q <= W - 1);
+                    iny[q] = (0 <= ay + q && ay + q <= H - 1);
+                }
                 float a[KS][KS], norm = 0.f;
 #pragma unroll
                 for (int j = 0; j < KS; ++j)
 #pragma unroll
                     for (int i = 0; i < KS; ++i) {
-                        const int x = ax + j, y = ay + i;
-                        const bool in = (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1);
-                        a[i][j] = in ? __fmul_rn(dxs[j], dys[i]) : 0.0f;
+                        a[i][j] = (inx[j] && iny[i]) ? __fmul_rn(dxs[j], dys[i]) : 0.0f;
                         norm = __fadd_rn(norm, a[i][j]);
                     }
+                // one reciprocal per entry: A = a * (1 / norm) is within an ulp of the reference's a / norm
+                const float inv = (norm != 0.0f) ? __frcp_rn(norm) : 1.0f;
 #pragma unroll
                 for (int i = 0; i < KS; ++i)
 #pragma unroll
                     for (int j = 0; j < KS; ++j) {
-                        const float A = (norm != 0.0f) ? __fdiv_rn(a[i][j], norm) : a[i][j];
+                        const float A = __fmul_rn(a[i][j], inv);
                         if (a[i][j] != 0.0f) anyb |= 1u << (i * KS + j);
                         const float wA = w * A;
                         P[i][j][0] += wA;

@@ -58,41 +58,80 @@ __device__ __forceinline__ bool top_left(float ax, float ay, float bx, float by,
 
 // Covered pixel centres of a triangle keep the largest interpolated 1/z (nearest surface); ties keep the
 // smaller centre depth. Key = (bits(1/z) << 32) | (~bits(z_centre)), both positive floats.
-__device__ void raster_tri(const float *v0, const float *v1, const float *v2, float zc, int W, int H,
-                           unsigned long long *zkey) {
+__device__ __forceinline__ void depth_test(int x, int y, int W, float iz, unsigned int zlow,
+                                           unsigned long long *zkey) {
+    if (!(iz > 0.f)) return;
+    const unsigned long long key = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
+    unsigned long long *slot = zkey + (size_t)y * W + x;
+    // keys only grow: a candidate already beaten needs no atomic
+    if (__ldcg(slot) < key) atomicMax(slot, key);
+}
+
+// Set-up of one triangle of the strip: orientation, top-left flags of its edges (v1v2, v2v0, v0v1) and its
+// clipped bounding box; live is false for zero area, an empty box, or a box wider than 64 pixels
+// (degenerate, grazing quads are skipped).
+struct TriSetup {
+    bool live, tl0, tl1, tl2;
+    float sgn;  // +1 counter-clockwise, -1 clockwise: edge values are multiplied by it
+    int xmin, xmax, ymin, ymax;
+};
+
+__device__ __forceinline__ TriSetup tri_setup(const float *v0, const float *v1, const float *v2, int W, int H) {
+    TriSetup t;
+    t.live = false;
     const float area = edgef(v0[0], v0[1], v1[0], v1[1], v2[0], v2[1]);
-    if (area == 0.f) return;
+    if (area == 0.f) return t;
     const bool ccw = area > 0.f;
-    const int xmin = max(0, (int)floorf(fminf(v0[0], fminf(v1[0], v2[0])) - 0.5f));
-    const int xmax = min(W - 1, (int)ceilf(fmaxf(v0[0], fmaxf(v1[0], v2[0])) - 0.5f));
-    const int ymin = max(0, (int)floorf(fminf(v0[1], fminf(v1[1], v2[1])) - 0.5f));
-    const int ymax = min(H - 1, (int)ceilf(fmaxf(v0[1], fmaxf(v1[1], v2[1])) - 0.5f));
-    if (xmax < xmin || ymax < ymin) return;
-    if ((xmax - xmin) > 64 || (ymax - ymin) > 64) return;  // degenerate (grazing) quads are skipped
-    const bool tl0 = top_left(v1[0], v1[1], v2[0], v2[1], ccw);
-    const bool tl1 = top_left(v2[0], v2[1], v0[0], v0[1], ccw);
-    const bool tl2 = top_left(v0[0], v0[1], v1[0], v1[1], ccw);
+    t.sgn = ccw ? 1.f : -1.f;
+    t.xmin = max(0, (int)floorf(fminf(v0[0], fminf(v1[0], v2[0])) - 0.5f));
+    t.xmax = min(W - 1, (int)ceilf(fmaxf(v0[0], fmaxf(v1[0], v2[0])) - 0.5f));
+    t.ymin = max(0, (int)floorf(fminf(v0[1], fminf(v1[1], v2[1])) - 0.5f));
+    t.ymax = min(H - 1, (int)ceilf(fmaxf(v0[1], fmaxf(v1[1], v2[1])) - 0.5f));
+    if (t.xmax < t.xmin || t.ymax < t.ymin) return t;
+    if ((t.xmax - t.xmin) > 64 || (t.ymax - t.ymin) > 64) return t;
+    t.tl0 = top_left(v1[0], v1[1], v2[0], v2[1], ccw);
+    t.tl1 = top_left(v2[0], v2[1], v0[0], v0[1], ccw);
+    t.tl2 = top_left(v0[0], v0[1], v1[0], v1[1], ccw);
+    t.live = true;
+    return t;
+}
+
+// Coverage test of a pixel centre given the three (unsigned) edge values; on success iz is the interpolated
+// 1/z of the triangle (w0 v0 + w1 v1 + w2 v2) / (w0 + w1 + w2).
+__device__ __forceinline__ bool tri_cover(const TriSetup &t, float e0, float e1, float e2, float z0, float z1,
+                                          float z2, float &iz) {
+    const float w0 = t.sgn * e0, w1 = t.sgn * e1, w2 = t.sgn * e2;
+    if (w0 < 0.f || w1 < 0.f || w2 < 0.f) return false;
+    if ((w0 == 0.f && !t.tl0) || (w1 == 0.f && !t.tl1) || (w2 == 0.f && !t.tl2)) return false;
+    const float s = w0 + w1 + w2;
+    iz = (w0 * z0 + w1 * z1 + w2 * z2) / s;
+    return true;
+}
+
+// The quad (strip BL v0, TL v1, BR v2, TR v3) as triangles A = (v0, v1, v2) and B = (v1, v2, v3), which share
+// the edge v1v2 (A's edge 0, B's edge 2). One pass over the union of their boxes evaluates that edge once per
+// pixel; each triangle's coverage and depth are those of rasterising it alone.
+__device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigned long long *zkey) {
+    const TriSetup A = tri_setup(v[0], v[1], v[2], W, H), B = tri_setup(v[1], v[2], v[3], W, H);
+    if (!A.live && !B.live) return;
+    const int xmin = A.live ? (B.live ? min(A.xmin, B.xmin) : A.xmin) : B.xmin;
+    const int xmax = A.live ? (B.live ? max(A.xmax, B.xmax) : A.xmax) : B.xmax;
+    const int ymin = A.live ? (B.live ? min(A.ymin, B.ymin) : A.ymin) : B.ymin;
+    const int ymax = A.live ? (B.live ? max(A.ymax, B.ymax) : A.ymax) : B.ymax;
     const unsigned int zlow = ~__float_as_uint(zc);
     for (int y = ymin; y <= ymax; ++y)
         for (int x = xmin; x <= xmax; ++x) {
             const float px = x + 0.5f, py = y + 0.5f;
-            float w0 = edgef(v1[0], v1[1], v2[0], v2[1], px, py);
-            float w1 = edgef(v2[0], v2[1], v0[0], v0[1], px, py);
-            float w2 = edgef(v0[0], v0[1], v1[0], v1[1], px, py);
-            if (!ccw) {
-                w0 = -w0;
-                w1 = -w1;
-                w2 = -w2;
-            }
-            if (w0 < 0.f || w1 < 0.f || w2 < 0.f) continue;
-            if ((w0 == 0.f && !tl0) || (w1 == 0.f && !tl1) || (w2 == 0.f && !tl2)) continue;
-            const float s = w0 + w1 + w2;
-            const float iz = (w0 * v0[2] + w1 * v1[2] + w2 * v2[2]) / s;
-            if (!(iz > 0.f)) continue;
-            const unsigned long long key = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
-            unsigned long long *slot = zkey + (size_t)y * W + x;
-            // keys only grow: a candidate already beaten needs no atomic
-            if (__ldcg(slot) < key) atomicMax(slot, key);
+            const float e12 = edgef(v[1][0], v[1][1], v[2][0], v[2][1], px, py);
+            float iz;
+            if (A.live && A.sgn * e12 >= 0.f &&
+                tri_cover(A, e12, edgef(v[2][0], v[2][1], v[0][0], v[0][1], px, py),
+                          edgef(v[0][0], v[0][1], v[1][0], v[1][1], px, py), v[0][2], v[1][2], v[2][2], iz))
+                depth_test(x, y, W, iz, zlow, zkey);
+            if (B.live && B.sgn * e12 >= 0.f &&
+                tri_cover(B, edgef(v[2][0], v[2][1], v[3][0], v[3][1], px, py),
+                          edgef(v[3][0], v[3][1], v[1][0], v[1][1], px, py), e12, v[1][2], v[2][2], v[3][2], iz))
+                depth_test(x, y, W, iz, zlow, zkey);
         }
 }
 
@@ -118,12 +157,12 @@ __global__ void __launch_bounds__(256) k_zsplat(int V, int w, int h, const float
         const float dx = off[k][0], dy = off[k][1];
         warp_point(c, cx + dx, cy + dy, z + dx * zx + dy * zy, xh);
         if (!(xh[2] > 1e-2f)) return;  // behind the near plane (zNear = 1e-2, sources/pinholeCamera.cpp:133)
-        vert[k][0] = xh[0] / xh[2];
-        vert[k][1] = xh[1] / xh[2];
-        vert[k][2] = 1.0f / xh[2];
+        const float iw = 1.0f / xh[2];
+        vert[k][0] = xh[0] * iw;
+        vert[k][1] = xh[1] * iw;
+        vert[k][2] = iw;
     }
-    raster_tri(vert[0], vert[1], vert[2], zc, W, H, zkey);
-    raster_tri(vert[1], vert[2], vert[3], zc, W, H, zkey);
+    raster_quad(vert, zc, W, H, zkey);
 }
 
 __global__ void k_zresolve(size_t N, const unsigned long long *__restrict__ zkey, float *__restrict__ zbuf) {

@@ -1,0 +1,66 @@
+// tma.cuh -- Tensor Memory Accelerator loads and mbarriers for sm_103a (inline PTX).
+//
+// A tiled cp.async.bulk.tensor load moves a box of a tensor described by a CUtensorMap (encoded on the host)
+// into shared memory and signals an mbarrier with the bytes it wrote; out-of-range elements are zero-filled.
+// The innermost coordinate times the element size must be a multiple of 16 bytes (x a multiple of 4 for
+// float); other coordinates, including negative ones, are free.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace lfrv {
+
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+// Makes mbarrier initialisation and earlier generic shared-memory accesses visible to the async proxy.
+__device__ __forceinline__ void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+
+// Orders this thread's generic global writes before later async-proxy (TMA) reads of the same data.
+__device__ __forceinline__ void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n"
+        " .reg .pred p;\n"
+        " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n"
+        "}\n"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return done != 0;
+}
+
+// Bounded wait for the phase with the given parity; false after `limit` polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity, long long limit) {
+    for (long long i = 0; i < limit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Host: a 3-D float tensor map over planes x rows x cols (cols contiguous) with the given box, zero fill out of
+// range. Returns false when the driver entry point is missing or the layout is not encodable (row pitch not a
+// multiple of 16 bytes, misaligned base).
+bool encode_tensor_map_3d(CUtensorMap *map, const float *base, int cols, int rows, int planes, int box_x, int box_y,
+                          int box_z);
+
+}  // namespace lfrv

@@ -192,9 +192,9 @@ def test_u_gradient(ctx, preset, w):
 
 
 @pytest.mark.parametrize("faithful", [True, False])
-def test_cg(ctx, faithful):
+@pytest.mark.parametrize("H,W", [(48, 64), (37, 53)])  # W % 4 == 0 takes the TMA tile path, 53 the plain one
+def test_cg(ctx, faithful, H, W):
     rng = np.random.default_rng(9)
-    H, W = 48, 64
     U = rng.uniform(0, 1, (3, H, W)).astype(np.float32)
     gx = rng.normal(0, 0.05, (H, W)).astype(np.float32)
     gy = rng.normal(0, 0.05, (H, W)).astype(np.float32)
