@@ -88,6 +88,15 @@ def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: in
     return table.get(kernel)
 
 
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu --set full capture of the
+# C2 step; the captures and their commands are summarised in profiles/*_c2.md.
+NCU_TRAFFIC_BYTES = {
+    "zbuffer_splat": 83.906816e6 + 2.437376e6,
+    "gradient_setup": 223.385600e6 + 20.086528e6,
+    "cg_persistent": 21.064704e6 + 18.125056e6,
+}
+
+
 def sample_clocks(path: str):
     return subprocess.Popen(
         ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -238,7 +247,9 @@ def run_ours(args, rank: int, world: int) -> None:
     if abytes:
         ach = abytes / avg_s / 1e9
         roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "peak_source": peak_kind, "traffic": None, "avg_launch_us": avg_s * 1e6,
+                "peak_source": peak_kind,
+                "traffic": NCU_TRAFFIC_BYTES.get(dom) if args.workload == "c2" else None,
+                "avg_launch_us": avg_s * 1e6,
                 "algorithmic_bytes_per_launch": abytes}
 
     # end to end through the host-buffer C ABI call, pinned host memory
