@@ -372,8 +372,9 @@ __device__ __forceinline__ float tile_op(const float (*t)[kHaloX], int tx, int t
 // current one is used. Box rows are padded to a 128-byte multiple in shared memory.
 constexpr int kBoxX = kTileX + 8, kBoxY = kTileY + 2, kBoxPlane = kBoxX * kBoxY;
 constexpr unsigned kBoxBytes = 3u * kBoxPlane * sizeof(float);
+constexpr unsigned kIntBytes = 3u * kTileX * kTileY * sizeof(float);  // interior box (no halo) of u or r
 constexpr int kBoxStride = ((kBoxBytes + 127) / 128) * 128 / sizeof(float);  // floats between box buffers
-constexpr size_t kCgTmaSmem = 4 * (size_t)kBoxStride * sizeof(float) + 128;   // 2 stages x 2 arrays + alignment
+constexpr size_t kCgTmaSmem = 6 * (size_t)kBoxStride * sizeof(float) + 128;   // 2 stages x 3 slots + alignment
 
 // Operator of updateAlpha on a box in shared memory: f(i) is the value at box index i.
 template <class F>
@@ -410,13 +411,15 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                                                                    double gap_tol, double *state,
                                                                    const __grid_constant__ CUtensorMap mapR,
                                                                    const __grid_constant__ CUtensorMap mapA,
-                                                                   const __grid_constant__ CUtensorMap mapB) {
+                                                                   const __grid_constant__ CUtensorMap mapB,
+                                                                   const __grid_constant__ CUtensorMap mapUi,
+                                                                   const __grid_constant__ CUtensorMap mapRi) {
     __shared__ double sh[8];
     const size_t N = (size_t)W * H;
     const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x, nthr = (size_t)gridDim.x * blockDim.x;
     __shared__ float tile[TMA ? 1 : 3][TMA ? 1 : kHaloY][TMA ? 1 : kHaloX];
     extern __shared__ __align__(128) float dyn_smem[];
-    // TMA destinations: [stage][array][kBoxStride], 128-byte aligned explicitly
+    // TMA destinations: [stage][slot][kBoxStride], 128-byte aligned explicitly
     float *boxes = reinterpret_cast<float *>((reinterpret_cast<uintptr_t>(dyn_smem) + 127) & ~uintptr_t(127));
     __shared__ __align__(8) uint64_t bars[2];
     __shared__ int s_flag;
@@ -431,15 +434,24 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
         fence_proxy_async_smem();
     }
     __syncthreads();
-    // thread 0 starts the loads of this block's k-th tile: arrays a0 (and a1 when two) into stage k & 1
-    auto issue = [&](int k, const CUtensorMap *a0, const CUtensorMap *a1) {
+    // thread 0 starts the loads of this block's k-th tile into stage k & 1. Phase A: halo boxes of r and d_old
+    // (slots 0, 1). Phase B: halo box of d_new (slot 0) and the interior boxes of u and r (slots 1, 2).
+    auto slot = [&](int st, int j) { return boxes + (size_t)(3 * st + j) * kBoxStride; };
+    auto issue = [&](int k, bool phase_b, const CUtensorMap *halo1) {
         if (threadIdx.x != 0) return;
         const int t = (int)blockIdx.x + k * (int)gridDim.x, st = k & 1;
         const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
         fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&bars[st], a1 ? 2 * kBoxBytes : kBoxBytes);
-        tma_load_3d(boxes + (size_t)(2 * st) * kBoxStride, a0, x0 - 4, y0 - 1, 0, &bars[st]);
-        if (a1) tma_load_3d(boxes + (size_t)(2 * st + 1) * kBoxStride, a1, x0 - 4, y0 - 1, 0, &bars[st]);
+        if (!phase_b) {
+            mbar_arrive_expect_tx(&bars[st], 2 * kBoxBytes);
+            tma_load_3d(slot(st, 0), &mapR, x0 - 4, y0 - 1, 0, &bars[st]);
+            tma_load_3d(slot(st, 1), halo1, x0 - 4, y0 - 1, 0, &bars[st]);
+        } else {
+            mbar_arrive_expect_tx(&bars[st], kBoxBytes + 2 * kIntBytes);
+            tma_load_3d(slot(st, 0), halo1, x0 - 4, y0 - 1, 0, &bars[st]);
+            tma_load_3d(slot(st, 1), &mapUi, x0, y0, 0, &bars[st]);
+            tma_load_3d(slot(st, 2), &mapRi, x0, y0, 0, &bars[st]);
+        }
     };
     // on a box that never arrived: flag the error, give the other stage's load a bounded wait, leave
     auto abandon = [&](int k) {
@@ -510,9 +522,9 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
         float accA[4] = {0.f, 0.f, 0.f, 0.f};
         if constexpr (TMA) {
             const CUtensorMap *mdold = (dold == r) ? &mapR : (dold == dA ? &mapA : &mapB);
-            if (nk > 0) issue(0, &mapR, mdold);
+            if (nk > 0) issue(0, false, mdold);
             for (int k = 0; k < nk; ++k) {
-                if (k + 1 < nk) issue(k + 1, &mapR, mdold);
+                if (k + 1 < nk) issue(k + 1, false, mdold);
                 const int st = k & 1;
                 if (!block_wait_box(&bars[st], par[st], &s_flag)) {
                     abandon(k);
@@ -521,7 +533,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                 par[st] ^= 1u;
                 const int t = (int)blockIdx.x + k * (int)gridDim.x;
                 const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
-                const float *R = boxes + (size_t)(2 * st) * kBoxStride, *D = R + kBoxStride;
+                const float *R = slot(st, 0), *D = slot(st, 1);
                 for (int p = threadIdx.x; p < kTileX * kTileY; p += blockDim.x) {
                     const int lx = p % kTileX, ly = p / kTileX, x = x0 + lx, y = y0 + ly;
                     if (x >= W || y >= H) continue;
@@ -588,9 +600,9 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
         float accB[4] = {0.f, 0.f, 0.f, 0.f};
         if constexpr (TMA) {
             const CUtensorMap *mdnew = (dnew == dA) ? &mapA : &mapB;
-            if (nk > 0) issue(0, mdnew, nullptr);
+            if (nk > 0) issue(0, true, mdnew);
             for (int k = 0; k < nk; ++k) {
-                if (k + 1 < nk) issue(k + 1, mdnew, nullptr);
+                if (k + 1 < nk) issue(k + 1, true, mdnew);
                 const int st = k & 1;
                 if (!block_wait_box(&bars[st], par[st], &s_flag)) {
                     abandon(k);
@@ -599,7 +611,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                 par[st] ^= 1u;
                 const int t = (int)blockIdx.x + k * (int)gridDim.x;
                 const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
-                const float *Dn = boxes + (size_t)(2 * st) * kBoxStride;
+                const float *Dn = slot(st, 0), *Ui = slot(st, 1), *Ri = slot(st, 2);
                 for (int p = threadIdx.x; p < kTileX * kTileY; p += blockDim.x) {
                     const int lx = p % kTileX, ly = p / kTileX, x = x0 + lx, y = y0 + ly;
                     if (x >= W || y >= H) continue;
@@ -611,8 +623,8 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                         auto v = [&](int i) { return Dc[i]; };
                         const float qv = box_op(v, bi, x, y, W, H, lambda);
                         const float dv = Dc[bi];
-                        U[c * N + o] = __ldcg(U + c * N + o) + alpha[c] * dv;
-                        const float rv = __ldcg(r + c * N + o) - alpha[c] * qv;
+                        U[c * N + o] = Ui[c * kTileX * kTileY + p] + alpha[c] * dv;
+                        const float rv = Ri[c * kTileX * kTileY + p] - alpha[c] * qv;
                         r[c * N + o] = rv;
                         accB[c] += rv * rv;
                     }
@@ -678,7 +690,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
 // count: device pointer to the number of holes. A holds the initial image (and the result); B is a copy.
 // state: [0] iterations.
 // Only as many blocks as the hole count needs take part (kHoleFillPerBlock holes each; the others return at
-// once), so the grid barrier of each iteration spans few blocks. The energy partials alternate between two
+// once), so the grid barrier of each iteration spans few blocks, and none is needed when one block suffices. The energy partials alternate between two
 // slots by iteration parity: a block overwrites slot k & 1 in iteration k + 2 only after every block passed
 // the barrier of iteration k + 1, i.e. after all of them read it, so one barrier per iteration suffices.
 constexpr int kHoleFillPerBlock = 4 * kPersistThreads;
@@ -721,7 +733,11 @@ __global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W,
         }
         double *slot = part + (size_t)(k & 1) * active;
         block_partials(acc, 1, slot, active);
-        if (!grid_sync(gb, gen, active)) return;
+        if (active > 1) {
+            if (!grid_sync(gb, gen, active)) return;
+        } else {
+            __syncthreads();  // one block: its own global writes are visible to it after the block barrier
+        }
         block_reduce_partials(slot, active, 1, sh);
         energy = (float)sh[0];
         float *t = src;
@@ -787,10 +803,12 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
     const size_t N = (size_t)W * H;
     const int ntiles = ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
     // the TMA form needs row pitches of a multiple of 16 bytes (W % 4 == 0) and the driver's encoder
-    CUtensorMap maps[3];
+    CUtensorMap maps[5];
     const bool tma = encode_tensor_map_3d(&maps[0], r, W, H, 3, kBoxX, kBoxY, 3) &&
                      encode_tensor_map_3d(&maps[1], dA, W, H, 3, kBoxX, kBoxY, 3) &&
-                     encode_tensor_map_3d(&maps[2], dB, W, H, 3, kBoxX, kBoxY, 3);
+                     encode_tensor_map_3d(&maps[2], dB, W, H, 3, kBoxX, kBoxY, 3) &&
+                     encode_tensor_map_3d(&maps[3], U, W, H, 3, kTileX, kTileY, 3) &&
+                     encode_tensor_map_3d(&maps[4], r, W, H, 3, kTileX, kTileY, 3);
     if (!tma) std::memset(maps, 0, sizeof(maps));
     const void *kern = tma ? (const void *)k_cg_persistent<true> : (const void *)k_cg_persistent<false>;
     const size_t smem = tma ? kCgTmaSmem : 0;
@@ -798,9 +816,14 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
         const cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    const int blocks = coop_blocks(kern, std::max(ntiles, (int)((N + kPersistThreads - 1) / kPersistThreads)), smem);
-    void *args[] = {&W,     &H,        (void *)&gx, (void *)&gy, &U,       &r,       &dA,      &dB, &partA,
-                    &partB, &gb,       &max_iter,   &gap_tol,    &state,   &maps[0], &maps[1], &maps[2]};
+    // as many blocks as can be resident, then as few as keep the per-block tile count at its minimum (equal
+    // tile counts: no block waits at the grid barrier for a straggler with one tile more)
+    const int resident = coop_blocks(kern, 1 << 30, smem);
+    const int per_block = (ntiles + resident - 1) / resident;
+    const int blocks = std::max(1, (ntiles + per_block - 1) / per_block);
+    void *args[] = {&W,       &H,       (void *)&gx, (void *)&gy, &U,       &r,       &dA,      &dB,
+                    &partA,   &partB,   &gb,         &max_iter,   &gap_tol, &state,   &maps[0], &maps[1],
+                    &maps[2], &maps[3], &maps[4]};
     lc.add(1);
     return cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(kPersistThreads), args, smem, st);
 }

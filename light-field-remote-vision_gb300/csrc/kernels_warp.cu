@@ -83,12 +83,20 @@ __device__ __forceinline__ TriSetup tri_setup(const float *v0, const float *v1, 
     if (area == 0.f) return t;
     const bool ccw = area > 0.f;
     t.sgn = ccw ? 1.f : -1.f;
-    t.xmin = max(0, (int)floorf(fminf(v0[0], fminf(v1[0], v2[0])) - 0.5f));
-    t.xmax = min(W - 1, (int)ceilf(fmaxf(v0[0], fmaxf(v1[0], v2[0])) - 0.5f));
-    t.ymin = max(0, (int)floorf(fminf(v0[1], fminf(v1[1], v2[1])) - 0.5f));
-    t.ymax = min(H - 1, (int)ceilf(fmaxf(v0[1], fmaxf(v1[1], v2[1])) - 0.5f));
+    // a pixel centre x + 1/2 can lie in the triangle only when min <= x + 1/2 <= max
+    const float x_lo = fminf(v0[0], fminf(v1[0], v2[0])), x_hi = fmaxf(v0[0], fmaxf(v1[0], v2[0]));
+    const float y_lo = fminf(v0[1], fminf(v1[1], v2[1])), y_hi = fmaxf(v0[1], fmaxf(v1[1], v2[1]));
+    // grazing triangles wider than 64 pixels are skipped, measured on the conservative clipped box
+    {
+        const int cx0 = max(0, (int)floorf(x_lo - 0.5f)), cx1 = min(W - 1, (int)ceilf(x_hi - 0.5f));
+        const int cy0 = max(0, (int)floorf(y_lo - 0.5f)), cy1 = min(H - 1, (int)ceilf(y_hi - 0.5f));
+        if (cx1 < cx0 || cy1 < cy0 || cx1 - cx0 > 64 || cy1 - cy0 > 64) return t;
+    }
+    t.xmin = max(0, (int)ceilf(x_lo - 0.5f));
+    t.xmax = min(W - 1, (int)floorf(x_hi - 0.5f));
+    t.ymin = max(0, (int)ceilf(y_lo - 0.5f));
+    t.ymax = min(H - 1, (int)floorf(y_hi - 0.5f));
     if (t.xmax < t.xmin || t.ymax < t.ymin) return t;
-    if ((t.xmax - t.xmin) > 64 || (t.ymax - t.ymin) > 64) return t;
     t.tl0 = top_left(v1[0], v1[1], v2[0], v2[1], ccw);
     t.tl1 = top_left(v2[0], v2[1], v0[0], v0[1], ccw);
     t.tl2 = top_left(v0[0], v0[1], v1[0], v1[1], ccw);
