@@ -83,8 +83,6 @@ void launch_gradient_setup(const Geometry &G, const Buckets &B, const float *tau
 void launch_sobel(int W, int H, int count, const float *rgb, size_t in_stride, size_t ch_stride, float *gx, float *gy,
                   size_t out_stride, const uint8_t *vis, double *abs_partial, cudaStream_t st, LaunchCounter &lc);
 int sobel_partials(int W, int H);
-void launch_rof_iter(int W, int H, float tau, float sigma, float lam, const float *U, const float *P, const float *F,
-                     const float *g, float *Uo, float *Po, cudaStream_t st, LaunchCounter &lc);
 void launch_moving(size_t N, const float *A, const float *B, float thr, double *partial, cudaStream_t st,
                    LaunchCounter &lc);
 int moving_partials(size_t N);

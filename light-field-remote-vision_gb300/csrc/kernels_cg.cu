@@ -686,6 +686,108 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
     }
 }
 
+// Hole filling for at most kSmallHoles holes, in one block and in shared memory. The visible pixels never change,
+// so every hole keeps, per direction (left, up, right, down: the summation order of compute_laplacian), either
+// the index of the neighbouring hole or the neighbour's fixed value; the iterations then touch shared memory
+// only. Each update is the same float expression as k_hole_fill_persistent's. holes must be in ascending pixel
+// order (k_hole_write): neighbours are found by binary search.
+constexpr int kSmallHoles = 2048, kSmallThreads = 256;
+constexpr size_t kSmallHoleSmem = (size_t)kSmallHoles * (6 * 4 + 12 * 4 + 4 * 2 + 4);
+
+__global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H, const int *__restrict__ holes,
+                                                                   const int *__restrict__ count, float *A,
+                                                                   int max_iter, double *state) {
+    const int nh = *count;
+    if (nh > kSmallHoles) return;  // the grid-wide kernel takes it
+    extern __shared__ __align__(16) float hsm[];
+    float *cur = hsm, *nxt = hsm + 3 * kSmallHoles;            // [3][kSmallHoles] each
+    float *fixedv = hsm + 6 * kSmallHoles;                      // [4 dirs][3][kSmallHoles]
+    float *wts = hsm + 18 * kSmallHoles;                        // [kSmallHoles]
+    short *nb = reinterpret_cast<short *>(hsm + 19 * kSmallHoles);  // [4][kSmallHoles]: hole index, -1 fixed, -2 none
+    __shared__ double red[kSmallThreads / 32];
+    __shared__ float s_energy;
+    const size_t N = (size_t)W * H;
+    for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
+        const int o = __ldg(holes + h);
+        const int ox = o % W, oy = o / W;
+        const bool has[4] = {ox > 0, oy > 0, ox < W - 1, oy < H - 1};
+        const int q[4] = {o - 1, o - W, o + 1, o + W};
+        float wt = 0.f;
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            short idx = -2;
+            if (has[d]) {
+                wt += 1.f;
+                int lo = 0, hi = nh - 1;  // binary search of q[d] among the holes
+                idx = -1;
+                while (lo <= hi) {
+                    const int mid = (lo + hi) >> 1, v = __ldg(holes + mid);
+                    if (v == q[d]) {
+                        idx = (short)mid;
+                        break;
+                    }
+                    if (v < q[d]) lo = mid + 1;
+                    else hi = mid - 1;
+                }
+                if (idx == -1)
+                    for (int c = 0; c < 3; ++c) fixedv[(d * 3 + c) * kSmallHoles + h] = A[c * N + q[d]];
+            }
+            nb[d * kSmallHoles + h] = idx;
+        }
+        wts[h] = wt;
+        for (int c = 0; c < 3; ++c) cur[c * kSmallHoles + h] = A[c * N + o];
+    }
+    __syncthreads();
+    float energy = 0.0f, previous = 0.0f;
+    int k;
+    for (k = 0; k < max_iter; ++k) {
+        previous = energy;
+        double acc = 0.0;
+        for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float v = 0.f;
+#pragma unroll
+                for (int d = 0; d < 4; ++d) {
+                    const short idx = nb[d * kSmallHoles + h];
+                    if (idx == -2) continue;
+                    v += (idx >= 0) ? cur[c * kSmallHoles + idx] : fixedv[(d * 3 + c) * kSmallHoles + h];
+                }
+                v /= wts[h];
+                const float uc = cur[c * kSmallHoles + h];
+                const float lap = v - uc;
+                const float un = uc + lap;
+                nxt[c * kSmallHoles + h] = un;
+                if (c == 2) acc += (double)(lap * un);
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double t = 0.0;
+            for (int w = 0; w < kSmallThreads / 32; ++w) t += red[w];
+            s_energy = (float)t;
+        }
+        __syncthreads();
+        energy = s_energy;
+        float *t = cur;
+        cur = nxt;
+        nxt = t;
+        if (fabsf(previous - energy) < 1e-3f) {
+            ++k;
+            break;
+        }
+    }
+    for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
+        const int o = __ldg(holes + h);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) A[c * N + o] = cur[c * kSmallHoles + h];
+    }
+    if (threadIdx.x == 0) state[0] = (double)k;
+}
+
 // Hole filling with the whole iteration loop in one launch (hole_filling, sources/gradientIBR.cu:87-152).
 // count: device pointer to the number of holes. A holds the initial image (and the result); B is a copy.
 // state: [0] iterations.
@@ -702,6 +804,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W,
     __shared__ double sh[8];
     const size_t N = (size_t)W * H;
     const int nh = *count;
+    if (nh <= kSmallHoles) return;  // k_hole_fill_small has done it
     const int active = min((int)gridDim.x, max(1, (nh + kHoleFillPerBlock - 1) / kHoleFillPerBlock));
     if ((int)blockIdx.x >= active) return;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = active * blockDim.x;
@@ -855,6 +958,17 @@ bool encode_tensor_map_3d(CUtensorMap *map, const float *base, int cols, int row
 cudaError_t launch_hole_fill_persistent(int W, int H, const int *holes, const int *count, float *A, float *B,
                                         double *part, GridBarrier gb, int max_iter, double *state, cudaStream_t st,
                                         LaunchCounter &lc) {
+    {
+        // few holes: one block in shared memory; the grid-wide kernel below then returns at once (and vice versa)
+        ProfScope _ps(lc, "hole_fill_small", st);
+        cudaError_t e = cudaFuncSetAttribute(k_hole_fill_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kSmallHoleSmem);
+        if (e != cudaSuccess) return e;
+        k_hole_fill_small<<<1, kSmallThreads, kSmallHoleSmem, st>>>(W, H, holes, count, A, max_iter, state);
+        lc.add(1);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
     ProfScope _ps(lc, "hole_fill", st);
     const size_t N = (size_t)W * H;
     const int blocks =

@@ -681,10 +681,6 @@ __global__ void k_sobel(int W, int H, const float *__restrict__ rgb, size_t in_s
     }
 }
 
-// One inner ROF iteration (dual step vtv_rof.cu:118-147, TV_F reprojection onto the ball of radius g
-// vtv_rof.cu:280-320, primal prox cuda_kernels.cu:504-532) fused: the duals of the pixel and of its left
-// and upper neighbours are recomputed from the previous iterate so one launch reads (U, P, F, g) and
-// writes (U', P'). Ping-pong buffers keep the Jacobi semantics of the reference's separate launches.
 // Reprojection of the 6 dual components onto the Frobenius ball of radius r (vtv_rof.cu:280-320).
 __device__ __forceinline__ void rof_project(float p[6], float r) {
     float nn = 0.f;
@@ -698,50 +694,13 @@ __device__ __forceinline__ void rof_project(float p[6], float r) {
     }
 }
 
-__device__ __forceinline__ void rof_dual(int x, int y, int W, int H, size_t N, float sigma,
-                                         const float *__restrict__ U, const float *__restrict__ P,
-                                         const float *__restrict__ g, float p[6]) {
-    const size_t o = (size_t)y * W + x;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float u = __ldg(U + c * N + o);
-        const float gxv = (x < W - 1) ? __ldg(U + c * N + o + 1) - u : 0.f;
-        const float gyv = (y < H - 1) ? __ldg(U + c * N + o + W) - u : 0.f;
-        p[2 * c] = __ldg(P + (2 * c) * N + o) + sigma * gxv;
-        p[2 * c + 1] = __ldg(P + (2 * c + 1) * N + o) + sigma * gyv;
-    }
-    rof_project(p, __ldg(g + o));
-}
-
-__global__ void __launch_bounds__(256) k_rof_iter(int W, int H, float tau, float sigma, float lam,
-                                                  const float *__restrict__ U, const float *__restrict__ P,
-                                                  const float *__restrict__ F, const float *__restrict__ g,
-                                                  float *__restrict__ Uo, float *__restrict__ Po) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W || y >= H) return;
-    const size_t N = (size_t)W * H, o = (size_t)y * W + x;
-    float p[6], pl[6], pt[6];
-    rof_dual(x, y, W, H, N, sigma, U, P, g, p);
-    if (x > 0) rof_dual(x - 1, y, W, H, N, sigma, U, P, g, pl);
-    if (y > 0) rof_dual(x, y - 1, W, H, N, sigma, U, P, g, pt);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) Po[k * N + o] = p[k];
-    const float denom = tau + lam;
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        float step = p[2 * c] + p[2 * c + 1];
-        if (x > 0) step -= pl[2 * c];
-        if (y > 0) step -= pt[2 * c + 1];
-        const float unew = __ldg(U + c * N + o) + tau * step;
-        Uo[c * N + o] = (tau * __ldg(F + c * N + o) + lam * unew) / denom;
-    }
-}
-
-// All niter inner ROF iterations in one cooperative launch, temporally blocked. Each super-step runs up to
-// kRofK iterations: a block stages a (kRofTX + 2 kRofK) x (kRofTY + 2 kRofK) region of U, P, F, g in shared
-// memory, iterates there (dual step + reprojection in place, then the primal prox in place; each pixel's
-// arithmetic is k_rof_iter's), and writes back its kRofTX x kRofTY tile, whose values depend only on the
-// region (the halo absorbs one pixel of staleness per iteration from each side). Super-steps read one
+// All niter inner ROF iterations in one cooperative launch, temporally blocked. One iteration is the dual step
+// p += sigma grad_fwd(U) (vtv_rof.cu:118-147), the reprojection of the 6 duals onto the ball of radius g
+// (vtv_rof.cu:280-320) and the primal prox U = (tau F + lambda (U + tau div_bwd p)) / (tau + lambda)
+// (cuda_kernels.cu:504-532). Each super-step runs up to kRofK iterations: a block stages a
+// (kRofTX + 2 kRofK) x (kRofTY + 2 kRofK) region of U, P, F, g in shared memory, iterates there (duals in
+// place, then the primal in place), and writes back its kRofTX x kRofTY tile, whose values depend only on
+// the region (the halo absorbs one pixel of staleness per iteration from each side). Super-steps read one
 // global (U, P) pair and write the other, with a bounded grid barrier between them.
 constexpr int kRofTX = 32, kRofTY = 16, kRofK = 4, kRofThreads = 256;
 constexpr int kRofRX = kRofTX + 2 * kRofK, kRofRY = kRofTY + 2 * kRofK, kRofRN = kRofRX * kRofRY;
@@ -779,7 +738,7 @@ __global__ void __launch_bounds__(kRofThreads) k_rof_persistent(int W, int H, in
             }
             __syncthreads();
             for (int it = 0; it < iters; ++it) {
-                // dual step + reprojection (rof_dual), in place: reads U (unchanged here) and the pixel's own P
+                // dual step + reprojection, in place: reads U (unchanged here) and the pixel's own P
                 for (int i = threadIdx.x; i < kRofRN; i += kRofThreads) {
                     const int lx = i % kRofRX, ly = i / kRofRX, gx = rx0 + lx, gy = ry0 + ly;
                     if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
@@ -799,7 +758,7 @@ __global__ void __launch_bounds__(kRofThreads) k_rof_persistent(int W, int H, in
                     for (int k = 0; k < 6; ++k) sP[k * kRofRN + i] = p[k];
                 }
                 __syncthreads();
-                // primal prox (k_rof_iter), in place: reads the new duals of the pixel and its left / upper neighbour
+                // primal prox, in place: reads the new duals of the pixel and its left / upper neighbour
                 for (int i = threadIdx.x; i < kRofRN; i += kRofThreads) {
                     const int lx = i % kRofRX, ly = i / kRofRX, gx = rx0 + lx, gy = ry0 + ly;
                     if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
@@ -1086,13 +1045,6 @@ cudaError_t launch_rof_persistent(int W, int H, int niter, float tau, float sigm
     lc.add(1);
     return cudaLaunchCooperativeKernel((const void *)k_rof_persistent, dim3(blocks), dim3(kRofThreads), args, kRofSmem,
                                        st);
-}
-
-void launch_rof_iter(int W, int H, float tau, float sigma, float lam, const float *U, const float *P, const float *F,
-                     const float *g, float *Uo, float *Po, cudaStream_t st, LaunchCounter &lc) {
-    ProfScope _ps(lc, "rof_iter", st);
-    k_rof_iter<<<grid2(W, H, kTile), kTile, 0, st>>>(W, H, tau, sigma, lam, U, P, F, g, Uo, Po);
-    lc.add(1);
 }
 
 void launch_moving(size_t N, const float *A, const float *B, float thr, double *partial, cudaStream_t st,

@@ -165,13 +165,18 @@ def test_gradient_visibility(ctx, preset, w):
     assert np.array_equal(ctx.stage_gradient_visibility(cfg, tau), pyoracle.stage_gradient_visibility(cfg, tau, prec=1))
 
 
-def test_hole_fill(ctx):
+# 868 holes take the single-block shared-memory kernel, 6000 the grid-wide persistent one
+@pytest.mark.parametrize("big", [False, True])
+def test_hole_fill(ctx, big):
     rng = np.random.default_rng(7)
-    H, W = 64, 72
+    H, W = (96, 128) if big else (64, 72)
     U = rng.uniform(0.1, 0.9, (3, H, W)).astype(np.float32)
     vis = np.ones((H, W), np.uint8)
-    vis[10:30, 5:40] = 0
-    vis[50:64, 60:72] = 0
+    if big:
+        vis[20:80, 10:110] = 0
+    else:
+        vis[10:30, 5:40] = 0
+        vis[50:64, 60:72] = 0
     U[:, vis == 0] = 0.0
     out, it = ctx.stage_hole_fill(U, vis, 500)
     ref, rit = pyoracle.stage_hole_fill(U, vis, 500, prec=1)
