@@ -129,6 +129,15 @@ int lfrv_ctx_profile(lfrv_ctx *ctx, int enable);
 int lfrv_ctx_profile_read(lfrv_ctx *ctx, int index, char *name, size_t name_len, double *total_ms,
                           long long *launches);
 
+/* ---------------------------------------------------------------- depth maps
+ * Radial to orthographic depth, in place (fromRadial2Ortho.frag:10-23, applied by InputView::filterDepthmap,
+ * sources/openGL/view.cpp:723-733, to MVE depth maps): depth is nviews x 3 x h x w (z, dz/dx, dz/dy); with
+ * X = K^-1 (x + 1/2, y + 1/2, 1) and d = |X| the result is z / d and its derivatives
+ * dz/dx / d - z (X . K^-1 column 0) / d^3 (column 1 for y). Only K of each camera is used. */
+int lfrv_depth_radial_to_ortho(lfrv_ctx *ctx, int nviews, int w, int h, const lfrv_camera *cams, float *depth);
+int lfrv_depth_radial_to_ortho_dev(lfrv_ctx *ctx, int nviews, int w, int h, const lfrv_camera *cams,
+                                   float *d_depth);
+
 /* ---------------------------------------------------------------- warp stage
  * Replaces the GL warp exporter (fromMVE2coco: Scene::computeTargetDepthMap sources/openGL/scene.cpp:1506,
  * Scene::exportWarps :1546, shaders tauWarp.frag:25-74, tauPartial.frag:23-48,

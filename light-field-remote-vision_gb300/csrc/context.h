@@ -33,6 +33,8 @@ struct Workspace {
     DevBuf b_count, b_start, b_entries, b_aux;
     // target
     DevBuf U, Ua, Ub, Uprev, P, Pa, F, G, g, g0, tmp, cov, norm, vis, Xq, gx, gy, mask, zkey, zbuf;
+    // gradient data term (dt_beta)
+    DevBuf lapU, resg, ugrad;
     // CG
     DevBuf r, d, q, U0, holes, hole_count;
     // reductions and persistent-solver state

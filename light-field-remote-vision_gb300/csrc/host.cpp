@@ -108,6 +108,7 @@ static void swap_buf(DevBuf &a, DevBuf &b) {
 }
 
 static GridBarrier fresh_barrier(lfrv_ctx *c);
+static float *view_gradients(lfrv_ctx *c, const Geometry &G, const float *img);
 
 static void check_launch(const char *what) {
     const cudaError_t e = cudaGetLastError();
@@ -137,7 +138,6 @@ static Geometry geometry(const lfrv_config &cfg) {
 
 static void check_solver_options(const lfrv_config &cfg) {
     if (cfg.dw_type != 0) raise(LFRV_E_ARG, "dw_type %d: only 0 exists upstream (optimization.cu:1141-1147)", cfg.dw_type);
-    if (cfg.dt_beta != 0.0f) raise(LFRV_E_ARG, "dt_beta > 0 (gradient data term) is not implemented");
     if (cfg.niter < 0 || cfg.nmeta_iter < 0) raise(LFRV_E_ARG, "negative iteration count");
     if (!(cfg.lambda > 0.0f)) raise(LFRV_E_ARG, "lambda must be > 0");
 }
@@ -271,6 +271,60 @@ static void residual(lfrv_ctx *c, const Geometry &G, const float *U, const float
     reduce_to(c, np, part, slot);
 }
 
+// ------------------------------------------------------------------ gradient data term (dt_beta)
+// Buffers of the gradient data term (vtv_sr_dataterm_gradients, sources/optimization.cu:1969-2116) and of the
+// gradient term of the energy (:1610-1700); empty when dt_beta == 0.
+struct GradientTermBuffers {
+    bool on = false;
+    const float *vgrad = nullptr;  // Sobel of each view's luminance, 2 x n per view
+    float *lapU = nullptr, *resg = nullptr, *ugrad = nullptr;
+};
+
+static GradientTermBuffers gradient_term_buffers(lfrv_ctx *c, const lfrv_config &cfg, const Geometry &G,
+                                                 const float *img) {
+    GradientTermBuffers t;
+    if (cfg.dt_beta == 0.0f) return t;
+    Workspace &ws = c->ws;
+    ws.lapU.ensure(sizeof(float) * 3 * G.N);
+    ws.resg.ensure(sizeof(float) * 3 * (size_t)G.V * G.n);
+    ws.ugrad.ensure(sizeof(float) * 2 * G.N);
+    t.on = true;
+    t.vgrad = view_gradients(c, G, img);
+    t.lapU = ws.lapU.as<float>();
+    t.resg = ws.resg.as<float>();
+    t.ugrad = ws.ugrad.as<float>();
+    return t;
+}
+
+// Residuals of the gradient data term for the current U; the term is applied by the data-term kernel.
+static GradTerm gradient_residuals(lfrv_ctx *c, const lfrv_config &cfg, const Geometry &G,
+                                   const GradientTermBuffers &t, const float *U, const float *img, const float *tau2,
+                                   const float *wgt) {
+    GradTerm gt{nullptr, 0.f, 0.f, 0};
+    if (!(cfg.dt_beta > 0.0f)) return gt;  // the ISTA step runs the term for dt_beta > 0 (optimization.cu:1781)
+    launch_laplacian(G.W, G.H, 3, U, t.lapU, c->stream, c->launches);
+    launch_residual_grad(G, t.lapU, img, tau2, wgt, cfg.gw_type != 0, t.resg, c->stream, c->launches);
+    check_launch("gradient residual");
+    gt.resg = t.resg;
+    gt.beta = cfg.dt_beta;
+    gt.step = cfg.gradient_step;
+    gt.gw = cfg.gw_type != 0;
+    return gt;
+}
+
+// Gradient term of the reference energy into sums[slot]: Sobel of the luminance of U (no mask) gathered per view
+// and compared with the views' Sobel.
+static void energy_gradients(lfrv_ctx *c, const lfrv_config &cfg, const Geometry &G, const GradientTermBuffers &t,
+                             const float *U, const float *tau2, const float *wgt, int slot) {
+    launch_sobel(G.W, G.H, 1, U, 0, G.N, t.ugrad, t.ugrad + G.N, 0, nullptr, nullptr, c->stream, c->launches);
+    const int np = energy_grad_partials(G);
+    double *part = partial_buf(c, np);
+    launch_energy_grad(G, t.ugrad, t.vgrad, tau2, wgt, cfg.sigma_sensor * cfg.sigma_sensor, cfg.gw_type != 0, part,
+                       c->stream, c->launches);
+    check_launch("energy gradient term");
+    reduce_to(c, np, part, slot);
+}
+
 // ------------------------------------------------------------------ IBR_color
 static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
                         const float *init, float *out, lfrv_stats *st) {
@@ -283,6 +337,7 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
     const float sigma = cfg.sigma_sensor, s2 = cfg.sigma_sensor * cfg.sigma_sensor;
     const Buckets B = build_buckets(c, G, tau2);
     ColorBuffers b = color_buffers(c, G);
+    const GradientTermBuffers gtb = gradient_term_buffers(c, cfg, G, img);
     LFRV_CUDA(cudaMemsetAsync(b.U, 0, 3 * N * sizeof(float), s));
     LFRV_CUDA(cudaMemsetAsync(b.P, 0, 6 * N * sizeof(float), s));
     LFRV_CUDA(cudaMemsetAsync(b.Xq, 0, 2 * N * sizeof(float), s));
@@ -347,10 +402,11 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         residual(c, G, ws.U.as<float>(), img, tau2, b.wgt, s2, b.res, 1);
         if (!need_tv) return 0.0f;
         sobel_target(c, G, ws.U.as<float>(), b.Xq, b.Xq + N, b.vis, 0);
-        double sums[2];
-        read_sums(c, sums, 2);
-        const float e_tv = (float)sums[0], e_int = (float)sums[1];
-        return cfg.lambda * e_tv + cfg.dt_alpha * e_int;
+        if (gtb.on) energy_gradients(c, cfg, G, gtb, ws.U.as<float>(), tau2, b.wgt, 3);
+        double sums[4] = {0, 0, 0, 0};
+        read_sums(c, sums, gtb.on ? 4 : 2);
+        const float e_tv = (float)sums[0], e_int = (float)sums[1], e_grad = (float)sums[3];
+        return cfg.lambda * e_tv + cfg.dt_alpha * e_int + (gtb.on ? cfg.dt_beta * e_grad : 0.0f);
     };
     auto moving = [&](const float *a, const float *bb) -> int {
         double *part = partial_buf(c, mp);
@@ -376,7 +432,8 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         E_prev = E;
         int k;
         for (k = 0; k < cfg.niter; ++k) {
-            launch_dataterm_F(G, B, tau2, b.res, s2, cfg.dt_alpha, fscale, ws.U.as<float>(), b.F, nullptr, s,
+            const GradTerm gt = gradient_residuals(c, cfg, G, gtb, ws.U.as<float>(), img, tau2, b.wgt);
+            launch_dataterm_F(G, B, tau2, b.res, s2, cfg.dt_alpha, fscale, ws.U.as<float>(), b.F, nullptr, gt, s,
                               c->launches);
             check_launch("data term");
             // niter inner ROF iterations from Uq = U in one persistent launch over (Ua, P) <-> (Ub, Pa);
@@ -885,6 +942,57 @@ extern "C" int lfrv_warp_dev(lfrv_ctx *ctx, int nviews, int w, int h, const floa
     LFRV_API_END
 }
 
+// fromRadial2Ortho.frag (sources/openGL/frameBuffer.cpp:263-300, run by InputView::filterDepthmap,
+// sources/openGL/view.cpp:723-733) on device depth maps, in place.
+static void radial_to_ortho(lfrv_ctx *c, int nviews, int w, int h, const lfrv_camera *cams, float *d_depth) {
+    if (nviews < 1 || nviews > kMaxViews || w <= 0 || h <= 0 || !cams || !d_depth)
+        raise(LFRV_E_ARG, "bad radial-to-ortho arguments");
+    WarpCams kinv;
+    std::memset(&kinv, 0, sizeof(kinv));
+    for (int v = 0; v < nviews; ++v) {
+        const float *K = cams[v].K;
+        double m[9], inv[9];
+        for (int i = 0; i < 9; ++i) m[i] = K[i];
+        const double det = m[0] * (m[4] * m[8] - m[5] * m[7]) - m[1] * (m[3] * m[8] - m[5] * m[6]) +
+                           m[2] * (m[3] * m[7] - m[4] * m[6]);
+        if (det == 0.0) raise(LFRV_E_ARG, "camera %d: singular K", v);
+        inv[0] = (m[4] * m[8] - m[5] * m[7]) / det;
+        inv[1] = (m[2] * m[7] - m[1] * m[8]) / det;
+        inv[2] = (m[1] * m[5] - m[2] * m[4]) / det;
+        inv[3] = (m[5] * m[6] - m[3] * m[8]) / det;
+        inv[4] = (m[0] * m[8] - m[2] * m[6]) / det;
+        inv[5] = (m[2] * m[3] - m[0] * m[5]) / det;
+        inv[6] = (m[3] * m[7] - m[4] * m[6]) / det;
+        inv[7] = (m[1] * m[6] - m[0] * m[7]) / det;
+        inv[8] = (m[0] * m[4] - m[1] * m[3]) / det;
+        for (int i = 0; i < 9; ++i) kinv.M[v][i] = (float)inv[i];
+    }
+    launch_radial_to_ortho(nviews, w, h, kinv, d_depth, c->stream, c->launches);
+    check_launch("radial to ortho");
+}
+
+extern "C" int lfrv_depth_radial_to_ortho_dev(lfrv_ctx *ctx, int nviews, int w, int h, const lfrv_camera *cams,
+                                              float *d_depth) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    radial_to_ortho(ctx, nviews, w, h, cams, d_depth);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_depth_radial_to_ortho(lfrv_ctx *ctx, int nviews, int w, int h, const lfrv_camera *cams,
+                                          float *depth) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!depth) return fail(LFRV_E_ARG, "null depth");
+    const size_t count = (size_t)nviews * 3 * (size_t)w * h;
+    HostIO io{ctx};
+    float *d = io.up(ctx->ws.depth, depth, count);
+    radial_to_ortho(ctx, nviews, w, h, cams, d);
+    io.down(depth, d, count);
+    sync(ctx);
+    LFRV_API_END
+}
+
 extern "C" int lfrv_warp(lfrv_ctx *ctx, int nviews, int w, int h, const float *depth, const lfrv_camera *cams,
                          const lfrv_camera *target, float *tau, float *dpart, float *zbuf) {
     LFRV_API_BEGIN
@@ -1133,8 +1241,10 @@ extern "C" int lfrv_stage_dataterm(lfrv_ctx *ctx, const lfrv_config *cfg, const 
     residual(ctx, G, ctx->ws.U.as<float>(), si.img, si.tau2, b.wgt, s2, b.res, 0);
     const float L = (float)(1.0 / cfg->lambda);
     const float fscale = (float)(-1.0 / (double)(cfg->lambda * L));
+    const GradientTermBuffers gtb = gradient_term_buffers(ctx, *cfg, G, si.img);
+    const GradTerm gt = gradient_residuals(ctx, *cfg, G, gtb, ctx->ws.U.as<float>(), si.img, si.tau2, b.wgt);
     launch_dataterm_F(G, B, si.tau2, b.res, s2, cfg->dt_alpha, fscale, ctx->ws.U.as<float>(), b.F,
-                      ctx->ws.G.as<float>(), ctx->stream, ctx->launches);
+                      ctx->ws.G.as<float>(), gt, ctx->stream, ctx->launches);
     check_launch("data term");
     io.down(Gout, ctx->ws.G.as<float>(), 3 * G.N);
     io.down(F, b.F, 3 * G.N);
@@ -1185,11 +1295,14 @@ extern "C" int lfrv_stage_energy(lfrv_ctx *ctx, const lfrv_config *cfg, const fl
     const float s2 = cfg->sigma_sensor * cfg->sigma_sensor;
     sobel_target(ctx, G, ctx->ws.U.as<float>(), b.Xq, b.Xq + G.N, b.vis, 0);
     residual(ctx, G, ctx->ws.U.as<float>(), si.img, si.tau2, b.wgt, s2, b.res, 1);
-    double sums[2];
-    read_sums(ctx, sums, 2);
+    const GradientTermBuffers gtb = gradient_term_buffers(ctx, *cfg, G, si.img);
+    if (gtb.on) energy_gradients(ctx, *cfg, G, gtb, ctx->ws.U.as<float>(), si.tau2, b.wgt, 3);
+    double sums[4] = {0, 0, 0, 0};
+    read_sums(ctx, sums, gtb.on ? 4 : 2);
     if (e_tv) *e_tv = sums[0];
     if (e_data) *e_data = sums[1];
-    if (energy) *energy = (double)cfg->lambda * sums[0] + (double)cfg->dt_alpha * sums[1];
+    if (energy)
+        *energy = (double)cfg->lambda * sums[0] + (double)cfg->dt_alpha * sums[1] + (double)cfg->dt_beta * sums[3];
     LFRV_API_END
 }
 

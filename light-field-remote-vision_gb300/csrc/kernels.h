@@ -47,6 +47,9 @@ struct WarpCams {
     float M[kMaxViews][9];
     float b[kMaxViews][3];
 };
+// Radial to orthographic depth in place; kinv.M[v] holds K^-1 of view v.
+void launch_radial_to_ortho(int V, int w, int h, const WarpCams &kinv, float *depth, cudaStream_t st,
+                            LaunchCounter &lc);
 void launch_zbuffer_clear(int W, int H, unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc);
 void launch_zbuffer_splat(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H,
                           unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc);
@@ -70,8 +73,21 @@ void launch_vis_any(const Geometry &G, const Buckets &B, const float *tau, uint8
                     LaunchCounter &lc);
 void launch_initial_image(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *wgt,
                           float *U, float *norm, cudaStream_t st, LaunchCounter &lc);
+// Gradient data term of the ISTA step (dt_beta > 0): per-view residuals resg (3 x n each) and their weights.
+struct GradTerm {
+    const float *resg;  // nullptr: no gradient term
+    float beta, step;
+    int gw;
+};
 void launch_dataterm_F(const Geometry &G, const Buckets &B, const float *tau, const float *res, float s2, float alpha,
-                       float fscale, const float *U, float *F, float *G_out, cudaStream_t st, LaunchCounter &lc);
+                       float fscale, const float *U, float *F, float *G_out, const GradTerm &gt, cudaStream_t st,
+                       LaunchCounter &lc);
+void launch_laplacian(int W, int H, int planes, const float *in, float *out, cudaStream_t st, LaunchCounter &lc);
+void launch_residual_grad(const Geometry &G, const float *lapU, const float *img, const float *tau, const float *wgt,
+                          int gw, float *resg, cudaStream_t st, LaunchCounter &lc);
+int energy_grad_partials(const Geometry &G);
+void launch_energy_grad(const Geometry &G, const float *ugrad, const float *vgrad, const float *tau, const float *wgt,
+                        float s2, int gw, double *partial, cudaStream_t st, LaunchCounter &lc);
 void launch_regweight(const Geometry &G, const Buckets &B, const float *tau, const float *wgt, const float *norm_prior,
                       float s2, float lmax, float lmin, float mmax, float *g0, float *norm_out, cudaStream_t st,
                       LaunchCounter &lc);

@@ -706,9 +706,12 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
     short *nb = reinterpret_cast<short *>(hsm + 19 * kSmallHoles);  // [4][kSmallHoles]: hole index, -1 fixed, -2 none
     __shared__ double red[kSmallThreads / 32];
     __shared__ float s_energy;
+    __shared__ int s_holes[kSmallHoles];
     const size_t N = (size_t)W * H;
+    for (int h = threadIdx.x; h < nh; h += kSmallThreads) s_holes[h] = __ldg(holes + h);
+    __syncthreads();
     for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
-        const int o = __ldg(holes + h);
+        const int o = s_holes[h];
         const int ox = o % W, oy = o / W;
         const bool has[4] = {ox > 0, oy > 0, ox < W - 1, oy < H - 1};
         const int q[4] = {o - 1, o - W, o + 1, o + W};
@@ -721,7 +724,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
                 int lo = 0, hi = nh - 1;  // binary search of q[d] among the holes
                 idx = -1;
                 while (lo <= hi) {
-                    const int mid = (lo + hi) >> 1, v = __ldg(holes + mid);
+                    const int mid = (lo + hi) >> 1, v = s_holes[mid];
                     if (v == q[d]) {
                         idx = (short)mid;
                         break;
@@ -781,7 +784,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
         }
     }
     for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
-        const int o = __ldg(holes + h);
+        const int o = s_holes[h];
 #pragma unroll
         for (int c = 0; c < 3; ++c) A[c * N + o] = cur[c * kSmallHoles + h];
     }

@@ -552,21 +552,36 @@ __global__ void k_initial_image(int W, int H, int n, int dsf, int BW, const unsi
 
 // Data-term gradient and the proximal data F (vtv_sr_dataterm_intensities :1953-1963 and
 // vtv_sr_ista_step_unstructured :1785-1812): G = alpha sigma^2 sum A e / sum A, F = clamp(U + fs clamp(G)).
+// With a gradient term (gt.resg set, vtv_sr_dataterm_gradients sources/optimization.cu:1969-2116) the
+// residuals of the gradients are splatted too (same entries, same coverage) and
+// G += beta * (-step) * [sigma^2 if gw_type] * sum A resg / sum A.
 template <int KS>
 __global__ void k_dataterm_F(int W, int H, int n, int dsf, int BW, const unsigned int *__restrict__ start,
                              const unsigned int *__restrict__ entries, const float *__restrict__ tau, SplatSrc src,
                              float s2, float alpha, float fscale, const float *__restrict__ U,
-                             float *__restrict__ F, float *__restrict__ G_out) {
+                             float *__restrict__ F, float *__restrict__ G_out, GradTerm gt) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= W || y >= H) return;
     float acc[3], norm;
     splat_accumulate<KS, 3>(x, y, W, H, n, dsf, BW, start, entries, tau, src, acc, norm);
+    float accg[3] = {0.f, 0.f, 0.f}, normg = 0.f;
+    if (gt.resg) {
+        const size_t s3 = (size_t)3 * n;
+        const SplatSrc sg{{gt.resg, gt.resg + n, gt.resg + 2 * (size_t)n}, {s3, s3, s3}, nullptr};
+        splat_accumulate<KS, 3>(x, y, W, H, n, dsf, BW, start, entries, tau, sg, accg, normg);
+    }
     const size_t o = (size_t)y * W + x, N = (size_t)W * H;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
         float gi = (norm != 0.f) ? acc[c] / norm : acc[c];
         gi *= s2;
         float G = 0.f + alpha * gi;
+        if (gt.resg) {
+            float gg = (normg != 0.f) ? accg[c] / normg : accg[c];
+            if (gt.gw) gg *= s2;
+            gg *= -gt.step;
+            G += gt.beta * gg;
+        }
         if (G_out) G_out[c * N + o] = G;
         G = fminf(1.0f, fmaxf(-1.0f, G));
         G *= fscale;
@@ -958,11 +973,152 @@ void launch_initial_image(const Geometry &G, const Buckets &B, const float *tau,
 }
 
 void launch_dataterm_F(const Geometry &G, const Buckets &B, const float *tau, const float *res, float s2, float alpha,
-                       float fscale, const float *U, float *F, float *G_out, cudaStream_t st, LaunchCounter &lc) {
+                       float fscale, const float *U, float *F, float *G_out, const GradTerm &gt, cudaStream_t st,
+                       LaunchCounter &lc) {
+    ProfScope _ps(lc, "dataterm", st);
     const size_t s3 = (size_t)3 * G.n;
     SplatSrc src{{res, res + G.n, res + 2 * (size_t)G.n}, {s3, s3, s3}, nullptr};
     LFRV_KS_DISPATCH(G.dsf + 1, k_dataterm_F, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW, B.start,
-                     B.entries, tau, src, s2, alpha, fscale, U, F, G_out);
+                     B.entries, tau, src, s2, alpha, fscale, U, F, G_out, gt);
+    lc.add(1);
+}
+
+// cuda_laplacian_device (cocolib/cocolib/vtv/vtv_sr_kernels_unstructured.cu:720-760) without a visibility mask,
+// on `planes` planes of W x H: mean of the in-image 4-neighbours (left, up, right, down) minus the centre.
+__device__ __forceinline__ float laplacian_at(const float *u, int W, int H, int x, int y) {
+    const size_t o = (size_t)y * W + x;
+    float v = 0.f, wt = 0.f;
+    if (x > 0) { v += u[o - 1]; wt += 1.f; }
+    if (y > 0) { v += u[o - W]; wt += 1.f; }
+    if (x < W - 1) { v += u[o + 1]; wt += 1.f; }
+    if (y < H - 1) { v += u[o + W]; wt += 1.f; }
+    v /= wt;
+    v -= u[o];
+    return v;
+}
+
+__global__ void k_laplacian(int W, int H, int planes, const float *__restrict__ in, float *__restrict__ out) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t N = (size_t)W * H, o = (size_t)y * W + x;
+    for (int c = 0; c < planes; ++c) out[c * N + o] = laplacian_at(in + c * N, W, H, x, y);
+}
+
+// Residual of the gradient data term for every source pixel (vtv_sr_dataterm_gradients, optimization.cu:
+// 2010-2069): dsf^2 A_i lap(U) - lap(v_i), times omega_i when gw_type != 0. lapU is 3 x N (k_laplacian).
+template <int KS>
+__global__ void __launch_bounds__(256) k_residual_grad(int V, int w, int h, int W, int H, int dsf,
+                                                       const float *__restrict__ lapU, const float *__restrict__ img,
+                                                       const float *__restrict__ tau, const float *__restrict__ wgt,
+                                                       int gw, float *__restrict__ resg) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    const int n = w * h;
+    if (m >= n) return;
+    const size_t N = (size_t)W * H;
+    const float tx = tau[(size_t)v * 2 * n + m], ty = tau[(size_t)v * 2 * n + n + m];
+    float a[3] = {0.f, 0.f, 0.f};
+    if (in_gather(tx, ty, W, H)) {
+        Footprint fp;
+        footprint<KS>(tx, ty, dsf, W, H, fp);
+#pragma unroll
+        for (int j = 0; j < KS; ++j)
+#pragma unroll
+            for (int i = 0; i < KS; ++i) {
+                const int x = fp.x0 + j, y = fp.y0 + i;
+                if (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1) {
+                    const float A = fp.A[KS * i + j];
+                    const size_t o = (size_t)y * W + x;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) a[c] += A * __ldg(lapU + c * N + o);
+                }
+            }
+    }
+    const float dsf2 = (float)(dsf * dsf);
+    const int mx = m % w, my = m / w;
+    const float *iv = img + (size_t)v * 3 * n;
+    float *rv = resg + (size_t)v * 3 * n;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        float d = a[c] * dsf2;
+        d -= laplacian_at(iv + (size_t)c * n, w, h, mx, my);
+        if (gw) d *= wgt[(size_t)v * n + m];
+        rv[(size_t)c * n + m] = d;
+    }
+}
+
+// Gradient term of the reference energy (coco_vtv_sr_primal_energy_unstructured, optimization.cu:1610-1700):
+// per source pixel (A_i Sobel_x lum U - Sobel_x lum v_i)^2 + (same for y), times omega_i sigma^2 when
+// gw_type != 0. ugrad: 2 x N (Sobel of the luminance of U, no mask); vgrad: per view 2 x n.
+template <int KS>
+__global__ void __launch_bounds__(256) k_energy_grad(int V, int n, int W, int H, int dsf,
+                                                     const float *__restrict__ ugrad, const float *__restrict__ vgrad,
+                                                     const float *__restrict__ tau, const float *__restrict__ wgt,
+                                                     float s2, int gw, double *__restrict__ partial) {
+    __shared__ double red[8];
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    const size_t N = (size_t)W * H;
+    double e = 0.0;
+    if (m < n) {
+        const float tx = tau[(size_t)v * 2 * n + m], ty = tau[(size_t)v * 2 * n + n + m];
+        float ax = 0.f, ay = 0.f;
+        if (in_gather(tx, ty, W, H)) {
+            Footprint fp;
+            footprint<KS>(tx, ty, dsf, W, H, fp);
+#pragma unroll
+            for (int j = 0; j < KS; ++j)
+#pragma unroll
+                for (int i = 0; i < KS; ++i) {
+                    const int x = fp.x0 + j, y = fp.y0 + i;
+                    if (0 <= x && x <= W - 1 && 0 <= y && y <= H - 1) {
+                        const float A = fp.A[KS * i + j];
+                        const size_t o = (size_t)y * W + x;
+                        ax += A * __ldg(ugrad + o);
+                        ay += A * __ldg(ugrad + N + o);
+                    }
+                }
+        }
+        const float *vg = vgrad + (size_t)v * 2 * n;
+        float a = ax - vg[m], b = ay - vg[n + m];
+        a = a * a;
+        b = b * b;
+        if (gw) {
+            const float w = wgt[(size_t)v * n + m];
+            a *= w;
+            b *= w;
+            a *= s2;
+            b *= s2;
+        }
+        e = (double)a + (double)b;
+    }
+    const double s = block_sum<256>(e, red);
+    if (threadIdx.x == 0) partial[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = s;
+}
+
+int energy_grad_partials(const Geometry &G) { return ((G.n + 255) / 256) * G.V; }
+
+void launch_laplacian(int W, int H, int planes, const float *in, float *out, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "laplacian", st);
+    k_laplacian<<<grid2(W, H, kTile), kTile, 0, st>>>(W, H, planes, in, out);
+    lc.add(1);
+}
+
+void launch_residual_grad(const Geometry &G, const float *lapU, const float *img, const float *tau, const float *wgt,
+                          int gw, float *resg, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "residual_grad", st);
+    const dim3 b(256), g((G.n + 255) / 256, G.V);
+    LFRV_KS_DISPATCH(G.dsf + 1, k_residual_grad, g, b, st, G.V, G.w, G.h, G.W, G.H, G.dsf, lapU, img, tau, wgt, gw,
+                     resg);
+    lc.add(1);
+}
+
+void launch_energy_grad(const Geometry &G, const float *ugrad, const float *vgrad, const float *tau, const float *wgt,
+                        float s2, int gw, double *partial, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "energy_grad", st);
+    const dim3 b(256), g((G.n + 255) / 256, G.V);
+    LFRV_KS_DISPATCH(G.dsf + 1, k_energy_grad, g, b, st, G.V, G.n, G.W, G.H, G.dsf, ugrad, vgrad, tau, wgt, s2, gw,
+                     partial);
     lc.add(1);
 }
 

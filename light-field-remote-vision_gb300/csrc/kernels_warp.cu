@@ -277,8 +277,36 @@ void launch_zbuffer_splat(int V, int w, int h, const float *depth, const WarpCam
     lc.add(1);
 }
 
+// fromRadial2Ortho.frag:10-23: radial depth (and derivatives) to orthographic depth, in place. kinv holds K^-1
+// (row-major) of each view; X = K^-1 (x + 1/2, y + 1/2, 1), d = |X|, z / d and the derivatives' chain rule.
+__global__ void k_radial_to_ortho(int V, int w, int h, const WarpCams kinv, float *__restrict__ depth) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    const int n = w * h;
+    if (m >= n) return;
+    const float *K = kinv.M[v];
+    const float px = (m % w) + 0.5f, py = (m / w) + 0.5f;
+    const float X0 = K[0] * px + K[1] * py + K[2], X1 = K[3] * px + K[4] * py + K[5], X2 = K[6] * px + K[7] * py + K[8];
+    const float d = sqrtf(X0 * X0 + X1 * X1 + X2 * X2), d3 = d * d * d;
+    const float c0 = X0 * K[0] + X1 * K[3] + X2 * K[6], c1 = X0 * K[1] + X1 * K[4] + X2 * K[7];
+    float *dz = depth + (size_t)v * 3 * n;
+    const float z = dz[m], zx = dz[n + m], zy = dz[2 * n + m];
+    dz[m] = z / d;
+    dz[n + m] = zx / d - z * c0 / d3;
+    dz[2 * n + m] = zy / d - z * c1 / d3;
+}
+
+void launch_radial_to_ortho(int V, int w, int h, const WarpCams &kinv, float *depth, cudaStream_t st,
+                            LaunchCounter &lc) {
+    ProfScope _ps(lc, "radial_to_ortho", st);
+    const int n = w * h;
+    k_radial_to_ortho<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, kinv, depth);
+    lc.add(1);
+}
+
 void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float *zbuf, cudaStream_t st,
                             LaunchCounter &lc) {
+    ProfScope _ps(lc, "zbuffer_resolve", st);
     const size_t N = (size_t)W * H;
     k_zresolve<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, zkey, zbuf);
     lc.add(1);
@@ -286,6 +314,7 @@ void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float 
 
 void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H, const float *zbuf,
                 float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "tau", st);
     const int n = w * h;
     k_tau<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zbuf, tau3, dpart3, tau2, dp2);
     lc.add(1);

@@ -87,7 +87,8 @@ LIB = _load()
 EXPORTED = [
     "lfrv_last_error", "lfrv_version", "lfrv_config_default", "lfrv_config_parse_file", "lfrv_config_set",
     "lfrv_config_get_string", "lfrv_config_get_int", "lfrv_ctx_create", "lfrv_ctx_destroy", "lfrv_ctx_set_stream",
-    "lfrv_ctx_launch_count", "lfrv_ctx_profile", "lfrv_ctx_profile_read", "lfrv_warp", "lfrv_warp_dev", "lfrv_ibr_color", "lfrv_ibr_color_dev",
+    "lfrv_ctx_launch_count", "lfrv_ctx_profile", "lfrv_ctx_profile_read", "lfrv_depth_radial_to_ortho",
+    "lfrv_depth_radial_to_ortho_dev", "lfrv_warp", "lfrv_warp_dev", "lfrv_ibr_color", "lfrv_ibr_color_dev",
     "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_stage_weights",
     "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
@@ -286,6 +287,13 @@ class Context:
         return out
 
     # ---- warp stage
+    def depth_radial_to_ortho(self, depth: np.ndarray, cams) -> np.ndarray:
+        """Radial to orthographic depth maps (V x 3 x h x w); returns a converted copy."""
+        d = f32(depth).copy()
+        V, _, h, w = d.shape
+        _check(LIB.lfrv_depth_radial_to_ortho(self._h, V, w, h, cameras_array(cams), fptr(d)))
+        return d
+
     def warp(self, depth: np.ndarray, cams, target: Camera):
         depth = f32(depth)
         V, _, h, w = depth.shape
@@ -470,6 +478,8 @@ def _declare() -> None:
     LIB.lfrv_config_get_string.argtypes = [C.c_char_p, C.c_char_p, C.c_size_t]
     LIB.lfrv_pfm_read.argtypes = [C.c_char_p, _I, _I, _I, _F, C.c_size_t]
     LIB.lfrv_pfm_write.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, _F]
+    LIB.lfrv_depth_radial_to_ortho.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(Camera), _F]
+    LIB.lfrv_depth_radial_to_ortho_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(Camera), vp]
     LIB.lfrv_cg_solve_static.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp, _I, _D]
     LIB.lfrv_png_read.argtypes = [C.c_char_p, _I, _I, _F, C.c_size_t]
     LIB.lfrv_png_write.argtypes = [C.c_char_p, C.c_int, C.c_int, _F]

@@ -723,6 +723,66 @@ void color_dataterm(ColorState<T> &S, T *Gint[3]) {
         }
 }
 
+// cuda_laplacian_device (cocolib/cocolib/vtv/vtv_sr_kernels_unstructured.cu:720-760) without a visibility
+// mask: the mean of the in-image 4-neighbours (summed left, up, right, down) minus the centre.
+template <class T>
+void laplacian(int W, int H, const T *in, T *out) {
+    for (int oy = 0; oy < H; ++oy)
+        for (int ox = 0; ox < W; ++ox) {
+            const size_t o = (size_t)oy * W + ox;
+            T v = 0, wt = 0;
+            if (ox > 0) { v += in[o - 1]; wt += 1; }
+            if (oy > 0) { v += in[o - W]; wt += 1; }
+            if (ox < W - 1) { v += in[o + 1]; wt += 1; }
+            if (oy < H - 1) { v += in[o + W]; wt += 1; }
+            v /= wt;
+            v -= in[o];
+            out[o] = v;
+        }
+}
+
+// vtv_sr_dataterm_gradients, sources/optimization.cu:1969-2116 (dt_beta > 0): per view the residual
+// dsf^2 A_i lap(U) - lap(v_i) (times omega_i when gw_type != 0) is splatted with A_i^T; the sum is normalised
+// by the splatted coverage, scaled by sigma^2 (gw_type != 0) and by -gradient_step, and added as
+// G += dt_beta * G_gradients. norm_mask is cleared and re-accumulated (the same coverage as the intensities).
+template <class T>
+void color_dataterm_gradients(ColorState<T> &S) {
+    const size_t n = (size_t)S.P.w * S.P.h, N = S.N;
+    Vec<T> gg[3] = {Vec<T>(N, T(0)), Vec<T>(N, T(0)), Vec<T>(N, T(0))};
+    std::fill(S.norm_mask.begin(), S.norm_mask.end(), T(0));
+    Vec<T> lu[3] = {Vec<T>(N), Vec<T>(N), Vec<T>(N)};
+    for (int c = 0; c < 3; ++c) laplacian(S.P.W, S.P.H, S.U[c].data(), lu[c].data());
+    Vec<T> t0(n), t1(n), t2(n), lv(n);
+    const T dsf2 = (T)(float)(S.P.dsf * S.P.dsf);
+    for (auto &vw : S.P.views) {
+        const T *in[3] = {lu[0].data(), lu[1].data(), lu[2].data()};
+        T *out[3] = {t0.data(), t1.data(), t2.data()};
+        gather(S.P, vw, 3, in, out);
+        for (int c = 0; c < 3; ++c) {
+            for (size_t m = 0; m < n; ++m) out[c][m] *= dsf2;
+            laplacian(S.P.w, S.P.h, vw.img + c * n, lv.data());
+            for (size_t m = 0; m < n; ++m) out[c][m] -= lv[m];
+        }
+        if (S.cfg.gw_type != 0)
+            for (int c = 0; c < 3; ++c)
+                for (size_t m = 0; m < n; ++m) out[c][m] *= vw.w[m];
+        const T *sin_[3] = {t0.data(), t1.data(), t2.data()};
+        T *gp[3] = {gg[0].data(), gg[1].data(), gg[2].data()};
+        splat(S.P, vw, 3, sin_, gp, S.norm_mask.data(), (const T *)nullptr);
+    }
+    const T s2 = (T)S.cfg.sigma_sensor * (T)S.cfg.sigma_sensor;
+    const T step = -(T)S.cfg.gradient_step;
+    for (int c = 0; c < 3; ++c) {
+        normalize(N, gg[c].data(), S.norm_mask.data());
+        for (size_t o = 0; o < N; ++o) {
+            T v = gg[c][o];
+            if (S.cfg.gw_type != 0) v *= s2;
+            v *= step;
+            S.G[c][o] += (T)S.cfg.dt_beta * v;
+        }
+    }
+}
+
 // The primal-dual constants set by coco_vtv_sr_iteration_fista_unstructured (sources/optimization.cu:
 // 1736-1748): tau = sigma = 0.3/sqrt(8), L = 1/lambda; the F scale is -1/(lambda*L) computed in float.
 template <class T>
@@ -759,6 +819,7 @@ void color_fista_iteration(ColorState<T> &S) {
         T *gp[3] = {gi[0].data(), gi[1].data(), gi[2].data()};
         color_dataterm(S, gp);
     }
+    if (S.cfg.dt_beta > 0) color_dataterm_gradients(S);
     const RofConsts<T> k = rof_consts<T>(S.cfg);
     for (int c = 0; c < 3; ++c)
         for (size_t o = 0; o < N; ++o) {
@@ -1495,7 +1556,8 @@ int orc_stage_dataterm(int prec, const lfrv_config *cfg, const float *views, con
             }
         std::vector<T> gi(3 * S.N);
         T *gp[3] = {gi.data(), gi.data() + S.N, gi.data() + 2 * S.N};
-        orc::color_dataterm(S, gp);
+        if (cfg->dt_alpha > 0) orc::color_dataterm(S, gp);
+        if (cfg->dt_beta > 0) orc::color_dataterm_gradients(S);
         const orc::RofConsts<T> k = orc::rof_consts<T>(*cfg);
         for (int c = 0; c < 3; ++c)
             for (size_t o = 0; o < S.N; ++o) {
@@ -1689,6 +1751,34 @@ int orc_warp(int V, int w, int h, const float *depth, const lfrv_camera *cams, c
                     for (int c = 0; c < 3; ++c) tv[c * n + m] = t3[c];
                 if (dv)
                     for (int c = 0; c < 3; ++c) dv[c * n + m] = d3[c];
+            }
+    }
+    return 0;
+}
+
+// fromRadial2Ortho.frag:10-23 (FrameBuffer::fromRadial2Ortho, sources/openGL/frameBuffer.cpp:263-300), in
+// place on V x 3 x n depth maps (radial depth and its x / y derivatives): with X = K^-1 (x + 1/2, y + 1/2, 1)
+// and d = |X|, z_o = z / d, dz_o/dx = dz/dx / d - z (X . K^-1 column 0) / d^3, and likewise for y with column 1.
+// The shader's pow(d, 3.0) is written d * d * d here.
+int orc_depth_radial_to_ortho(int V, int w, int h, const lfrv_camera *cams, float *depth) {
+    const size_t n = (size_t)w * h;
+    for (int v = 0; v < V; ++v) {
+        const orc::Cam c = orc::to_cam(cams[v]);
+        float *dz = depth + (size_t)v * 3 * n;
+        for (int y = 0; y < h; ++y)
+            for (int x = 0; x < w; ++x) {
+                const size_t m = (size_t)y * w + x;
+                const double px = x + 0.5, py = y + 0.5;
+                const double X[3] = {c.Kinv[0] * px + c.Kinv[1] * py + c.Kinv[2],
+                                     c.Kinv[3] * px + c.Kinv[4] * py + c.Kinv[5],
+                                     c.Kinv[6] * px + c.Kinv[7] * py + c.Kinv[8]};
+                const double d = std::sqrt(X[0] * X[0] + X[1] * X[1] + X[2] * X[2]), d3 = d * d * d;
+                const double c0 = X[0] * c.Kinv[0] + X[1] * c.Kinv[3] + X[2] * c.Kinv[6];  // X . column 0
+                const double c1 = X[0] * c.Kinv[1] + X[1] * c.Kinv[4] + X[2] * c.Kinv[7];  // X . column 1
+                const double z = dz[m], zx = dz[n + m], zy = dz[2 * n + m];
+                dz[m] = (float)(z / d);
+                dz[n + m] = (float)(zx / d - z * c0 / d3);
+                dz[2 * n + m] = (float)(zy / d - z * c1 / d3);
             }
     }
     return 0;

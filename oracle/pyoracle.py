@@ -167,6 +167,14 @@ def warp(depth, cams, target):
     return tau, dpart, zbuf
 
 
+def depth_radial_to_ortho(depth, cams):
+    """fromRadial2Ortho.frag on V x 3 x h x w depth maps (returns a converted copy)."""
+    d = f32(depth).copy()
+    V, _, h, w = d.shape
+    LIB.orc_depth_radial_to_ortho(V, w, h, lfrv.cameras_array(cams), fptr(d))
+    return d
+
+
 def footprint(tx, ty, dsf, W, H, prec=1):
     x0, y0 = C.c_int(), C.c_int()
     A = np.zeros(25, np.float32)

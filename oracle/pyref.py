@@ -122,28 +122,60 @@ def weights(views, tau, dpart, U, vis, gx0, gy0, w, h, dsf, sigma, thr):
     return gx, gy, out.reshape(views.shape[0], h, w)
 
 
-def dataterm(views, tau, wg, U, w, h, dsf, sigma, alpha, lam):
-    """vtv_sr_dataterm_intensities (optimization.cu:1835-1966) and F of vtv_sr_ista_step_unstructured
-    (:1785-1812). Returns G (before the [-1,1] clamp) and F."""
+def laplacian(X, W, H):
+    """cuda_laplacian_device (vtv_sr_kernels_unstructured.cu:720-760) without a visibility mask."""
+    X = np.ascontiguousarray(X, np.float32).ravel()
+    out = np.zeros(W * H, np.float32)
+    LIB.ref_laplacian(W, H, _f(X), _f(out))
+    return out
+
+
+def dataterm(views, tau, wg, U, w, h, dsf, sigma, alpha, lam, beta=0.0, gw_type=0, gradient_step=0.1):
+    """vtv_sr_dataterm_intensities (optimization.cu:1835-1966), vtv_sr_dataterm_gradients (:1969-2116) when
+    beta > 0, and F of vtv_sr_ista_step_unstructured (:1775-1812). Returns G (before the [-1,1] clamp) and F."""
     W, H = w * dsf, h * dsf
     N, n = W * H, w * h
     wg = np.ascontiguousarray(wg, np.float32).reshape(-1, n)
-    Gi = np.zeros((3, N), np.float32)
-    norm = np.zeros(N, np.float32)
-    for k, v in enumerate(views_of(views, tau, w, h, dsf)):
-        t = v.gather3(U)
-        img = v.img.reshape(3, n)
-        for c in range(3):
-            LIB.ref_subtract_from(w, h, _f(img[c]), _f(t[c]))
-        for c in range(3):
-            LIB.ref_multiply_with(w, h, _f(t[c]), _f(wg[k]))
-        v.splat3(t, Gi, norm)
+    vlist = views_of(views, tau, w, h, dsf)
     G = np.zeros((3, N), np.float32)
     s2 = np.float32(sigma) * np.float32(sigma)
-    for c in range(3):
-        LIB.ref_normalize(W, H, _f(Gi[c]), _f(norm))
-        LIB.ref_scale(W, H, _f(Gi[c]), s2)
-        LIB.ref_add_scaled_to(W, H, _f(Gi[c]), alpha, _f(G[c]))
+    if alpha > 0:
+        Gi = np.zeros((3, N), np.float32)
+        norm = np.zeros(N, np.float32)
+        for k, v in enumerate(vlist):
+            t = v.gather3(U)
+            img = v.img.reshape(3, n)
+            for c in range(3):
+                LIB.ref_subtract_from(w, h, _f(img[c]), _f(t[c]))
+            for c in range(3):
+                LIB.ref_multiply_with(w, h, _f(t[c]), _f(wg[k]))
+            v.splat3(t, Gi, norm)
+        for c in range(3):
+            LIB.ref_normalize(W, H, _f(Gi[c]), _f(norm))
+            LIB.ref_scale(W, H, _f(Gi[c]), s2)
+            LIB.ref_add_scaled_to(W, H, _f(Gi[c]), alpha, _f(G[c]))
+    if beta > 0:
+        Gg = np.zeros((3, N), np.float32)
+        norm = np.zeros(N, np.float32)
+        Uf = np.ascontiguousarray(U, np.float32).reshape(3, N)
+        for k, v in enumerate(vlist):
+            lu = np.stack([laplacian(Uf[c], W, H) for c in range(3)])
+            t = v.gather3(lu)
+            img = v.img.reshape(3, n)
+            for c in range(3):
+                LIB.ref_scale(w, h, _f(t[c]), float(dsf * dsf))
+                lv = laplacian(img[c], w, h)
+                LIB.ref_subtract_from(w, h, _f(lv), _f(t[c]))
+            if gw_type != 0:
+                for c in range(3):
+                    LIB.ref_multiply_with(w, h, _f(t[c]), _f(wg[k]))
+            v.splat3(t, Gg, norm)
+        for c in range(3):
+            LIB.ref_normalize(W, H, _f(Gg[c]), _f(norm))
+            if gw_type != 0:
+                LIB.ref_scale(W, H, _f(Gg[c]), s2)
+            LIB.ref_scale(W, H, _f(Gg[c]), -np.float32(gradient_step))
+            LIB.ref_add_scaled_to(W, H, _f(Gg[c]), beta, _f(G[c]))
     Gout = G.copy()
     L = np.float32(1.0 / np.float64(np.float32(lam)))
     fscale = np.float32(-1.0 / np.float64(np.float32(lam) * L))

@@ -73,10 +73,16 @@ def test_weights(ctx, preset, w):
     assert N > 0
 
 
+# (dt_alpha, dt_beta, gw_type): intensities only; with the gradient term (vtv_sr_dataterm_gradients)
+# unweighted and weighted; the gradient term alone
+TERMS = [(1.0, 0.0, 0), (1.0, 0.5, 0), (1.0, 0.5, 1), (0.0, 1.0, 1)]
+
+
 @pytest.mark.parametrize("preset,w", [(1, 64), (2, 32)])
-def test_dataterm(ctx, preset, w):
+@pytest.mark.parametrize("alpha,beta,gw", TERMS)
+def test_dataterm(ctx, preset, w, alpha, beta, gw):
     sc, tau, dpart, _ = warped(preset, w)
-    cfg = color_config(sc)
+    cfg = color_config(sc, dt_alpha=alpha, dt_beta=beta, gw_type=gw, gradient_step=0.25)
     H = W = w * sc.params.dsf
     rng = np.random.default_rng(1)
     U = rng.uniform(0.2, 0.8, (3, H, W)).astype(np.float32)
@@ -102,9 +108,10 @@ def test_rof_vs_fp64(ctx):
 
 
 @pytest.mark.parametrize("preset,w", [(1, 64), (2, 32)])
-def test_energy(ctx, preset, w):
+@pytest.mark.parametrize("beta,gw", [(0.0, 0), (0.5, 0), (0.5, 1)])
+def test_energy(ctx, preset, w, beta, gw):
     sc, tau, dpart, _ = warped(preset, w)
-    cfg = color_config(sc)
+    cfg = color_config(sc, dt_beta=beta, gw_type=gw)
     H = W = w * sc.params.dsf
     rng = np.random.default_rng(3)
     U = rng.uniform(0.2, 0.8, (3, H, W)).astype(np.float32)
@@ -222,6 +229,16 @@ def test_ibr_color_vs_fp64(ctx, preset, w, niter):
     out, st = ctx.ibr_color(cfg, sc.views, tau, dpart)
     ref, rst = pyoracle.ibr_color(cfg, sc.views, tau, dpart, prec=0)
     assert st.outer_iterations == rst.outer_iterations == niter
+    assert rel_err(out, ref) <= 1e-4
+    assert abs(st.energy - rst.energy) <= 1e-4 * abs(rst.energy)
+
+
+@pytest.mark.parametrize("gw", [0, 1])
+def test_ibr_color_gradient_term_vs_fp64(ctx, gw):
+    sc, tau, dpart, _ = warped(1, 48)
+    cfg = color_config(sc, niter=8, early_exit=0, dt_beta=0.5, gw_type=gw, gradient_step=0.25)
+    out, st = ctx.ibr_color(cfg, sc.views, tau, dpart)
+    ref, rst = pyoracle.ibr_color(cfg, sc.views, tau, dpart, prec=0)
     assert rel_err(out, ref) <= 1e-4
     assert abs(st.energy - rst.energy) <= 1e-4 * abs(rst.energy)
 

@@ -48,16 +48,23 @@ def test_weights_bitexact(preset, w):
     assert np.array_equal(gx, ogx) and np.array_equal(gy, ogy) and np.array_equal(wr, ow)
 
 
+# (dt_alpha, dt_beta, gw_type): the intensity term alone, plus the gradient term (vtv_sr_dataterm_gradients)
+# unweighted and weighted, and the gradient term alone
+TERMS = [(1.0, 0.0, 0), (1.0, 0.5, 0), (1.0, 0.5, 1), (0.0, 1.0, 1)]
+
+
 @pytest.mark.parametrize("preset,w", CASES)
-def test_dataterm_bitexact(preset, w):
+@pytest.mark.parametrize("alpha,beta,gw", TERMS)
+def test_dataterm_bitexact(preset, w, alpha, beta, gw):
     sc, tau, _, _ = warped(preset, w)
-    cfg = color_config(sc)
+    cfg = color_config(sc, dt_alpha=alpha, dt_beta=beta, gw_type=gw, gradient_step=0.25)
     p = sc.params
     H = W = w * p.dsf
     rng = np.random.default_rng(1)
     U = rng.uniform(0.2, 0.8, (3, H, W)).astype(np.float32)
     wg = rng.uniform(0.5e4, 1e4, (len(sc.views), p.h, p.w)).astype(np.float32)
-    G, F = pyref.dataterm(sc.views, tau, wg, U, *geo(sc), cfg.sigma_sensor, cfg.dt_alpha, cfg.lambda_)
+    G, F = pyref.dataterm(sc.views, tau, wg, U, *geo(sc), cfg.sigma_sensor, cfg.dt_alpha, cfg.lambda_,
+                          beta=cfg.dt_beta, gw_type=gw, gradient_step=cfg.gradient_step)
     oG, oF = pyoracle.stage_dataterm(cfg, sc.views, tau, wg, U, prec=1)
     assert np.array_equal(G, oG) and np.array_equal(F, oF)
 
