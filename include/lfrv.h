@@ -138,6 +138,21 @@ int lfrv_depth_radial_to_ortho(lfrv_ctx *ctx, int nviews, int w, int h, const lf
 int lfrv_depth_radial_to_ortho_dev(lfrv_ctx *ctx, int nviews, int w, int h, const lfrv_camera *cams,
                                    float *d_depth);
 
+/* Warps from orthographic depth maps and cameras without the GL pipeline: import_warps_from_depth
+ * (sources/import.cpp:243-450), the path sr_synthesize_view and IBR_gradient take when a config names depth
+ * maps and cameras (sources/super-resolution.cpp:121-127, sources/gradientIBR.cpp:62-68).
+ * - depth is nviews x depth_channels x h x w; plane 0 holds z.
+ * - tau (nviews x 3 x h x w) receives tau_x, tau_y, tau_y, as the reference writes it.
+ * - Pixels whose depth is outside [1/1000, 1000], or that have no target coverage, get (-w, -h).
+ * - Pixels whose back-projection lands more than 10 pixels from the source pixel get (-2w, -2h).
+ * - faithful = 1 back-projects with the source view's R and C as the reference does (import.cpp:412-415).
+ *   faithful = 0 uses the target's. */
+int lfrv_warp_from_depth(lfrv_ctx *ctx, int nviews, int w, int h, int dsf, const float *depth, int depth_channels,
+                         const lfrv_camera *cams, const lfrv_camera *target, int faithful, float *tau);
+int lfrv_warp_from_depth_dev(lfrv_ctx *ctx, int nviews, int w, int h, int dsf, const float *d_depth,
+                             int depth_channels, const lfrv_camera *cams, const lfrv_camera *target, int faithful,
+                             float *d_tau);
+
 /* ---------------------------------------------------------------- warp stage
  * Replaces the GL warp exporter (fromMVE2coco: Scene::computeTargetDepthMap sources/openGL/scene.cpp:1506,
  * Scene::exportWarps :1546, shaders tauWarp.frag:25-74, tauPartial.frag:23-48,

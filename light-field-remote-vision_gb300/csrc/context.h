@@ -35,6 +35,8 @@ struct Workspace {
     DevBuf U, Ua, Ub, Uprev, P, Pa, F, G, g, g0, tmp, cov, norm, vis, Xq, gx, gy, mask, zkey, zbuf;
     // gradient data term (dt_beta)
     DevBuf lapU, resg, ugrad;
+    // target depth keys of the warps-from-depth path
+    DevBuf ukey;
     // CG
     DevBuf r, d, q, U0, holes, hole_count;
     // reductions and persistent-solver state

@@ -942,6 +942,69 @@ extern "C" int lfrv_warp_dev(lfrv_ctx *ctx, int nviews, int w, int h, const floa
     LFRV_API_END
 }
 
+// Float camera record of the warps-from-depth kernels, computed as the reference's glm float arithmetic.
+static void wfd_camera(const lfrv_camera &c, float *o) {
+    o[0] = c.K[0];
+    o[1] = c.K[4];
+    o[2] = c.K[2];
+    o[3] = c.K[5];
+    for (int i = 0; i < 9; ++i) o[4 + i] = c.R[i];
+    for (int r = 0; r < 3; ++r) o[13 + r] = -(c.R[0 * 3 + r] * c.t[0] + c.R[1 * 3 + r] * c.t[1] + c.R[2 * 3 + r] * c.t[2]);
+    for (int r = 0; r < 3; ++r) {
+        for (int col = 0; col < 3; ++col)
+            o[16 + r * 4 + col] =
+                c.K[r * 3 + 0] * c.R[0 * 3 + col] + c.K[r * 3 + 1] * c.R[1 * 3 + col] + c.K[r * 3 + 2] * c.R[2 * 3 + col];
+        o[16 + r * 4 + 3] = c.K[r * 3 + 0] * c.t[0] + c.K[r * 3 + 1] * c.t[1] + c.K[r * 3 + 2] * c.t[2];
+    }
+}
+
+// import_warps_from_depth (sources/import.cpp:243-450) on device buffers.
+static void warp_from_depth(lfrv_ctx *c, int nviews, int w, int h, int dsf, const float *d_depth, int depth_channels,
+                            const lfrv_camera *cams, const lfrv_camera *target, int faithful, float *d_tau) {
+    if (nviews < 1 || nviews > kMaxViews || w <= 0 || h <= 0 || dsf < 1 || !d_depth || !cams || !target || !d_tau ||
+        depth_channels < 1)
+        raise(LFRV_E_ARG, "bad warp-from-depth arguments");
+    const int W = target->width, H = target->height;
+    if (W <= 0 || H <= 0) raise(LFRV_E_ARG, "bad target size");
+    for (int v = 0; v <= nviews; ++v) {
+        const lfrv_camera &k = v < nviews ? cams[v] : *target;
+        if (k.K[0] == 0.0f || k.K[4] == 0.0f) raise(LFRV_E_ARG, "camera %d: zero focal length", v);
+    }
+    WfdCams wc;
+    std::memset(&wc, 0, sizeof(wc));
+    for (int v = 0; v < nviews; ++v) wfd_camera(cams[v], wc.c[v]);
+    wfd_camera(*target, wc.c[nviews]);
+    c->ws.ukey.ensure(sizeof(unsigned int) * (size_t)W * H);
+    launch_warp_from_depth(nviews, w, h, dsf, d_depth, depth_channels, wc, W, H, faithful, c->ws.ukey.as<unsigned int>(),
+                           d_tau, c->stream, c->launches);
+    check_launch("warp from depth");
+}
+
+extern "C" int lfrv_warp_from_depth_dev(lfrv_ctx *ctx, int nviews, int w, int h, int dsf, const float *d_depth,
+                                        int depth_channels, const lfrv_camera *cams, const lfrv_camera *target,
+                                        int faithful, float *d_tau) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    warp_from_depth(ctx, nviews, w, h, dsf, d_depth, depth_channels, cams, target, faithful, d_tau);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_warp_from_depth(lfrv_ctx *ctx, int nviews, int w, int h, int dsf, const float *depth,
+                                    int depth_channels, const lfrv_camera *cams, const lfrv_camera *target,
+                                    int faithful, float *tau) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!depth || !tau || nviews < 1 || depth_channels < 1) return fail(LFRV_E_ARG, "bad arguments");
+    const size_t n = (size_t)w * h;
+    HostIO io{ctx};
+    const float *dd = io.up(ctx->ws.depth, depth, (size_t)nviews * depth_channels * n);
+    ctx->ws.in_tau.ensure(sizeof(float) * 3 * nviews * n);
+    warp_from_depth(ctx, nviews, w, h, dsf, dd, depth_channels, cams, target, faithful, ctx->ws.in_tau.as<float>());
+    io.down(tau, ctx->ws.in_tau.as<float>(), 3 * (size_t)nviews * n);
+    sync(ctx);
+    LFRV_API_END
+}
+
 // fromRadial2Ortho.frag (sources/openGL/frameBuffer.cpp:263-300, run by InputView::filterDepthmap,
 // sources/openGL/view.cpp:723-733) on device depth maps, in place.
 static void radial_to_ortho(lfrv_ctx *c, int nviews, int w, int h, const lfrv_camera *cams, float *d_depth) {

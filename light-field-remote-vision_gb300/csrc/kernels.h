@@ -47,6 +47,14 @@ struct WarpCams {
     float M[kMaxViews][9];
     float b[kMaxViews][3];
 };
+// Cameras of the warps-from-depth path (views 0..V-1, then the target at V): fx, fy, cx, cy, R (9, row-major),
+// C (3), P = K [R | t] (12, row-major).
+struct WfdCams {
+    float c[kMaxViews + 1][28];
+};
+void launch_warp_from_depth(int V, int w, int h, int dsf, const float *depth, int depth_channels, const WfdCams &cams,
+                            int W, int H, int faithful, unsigned int *ukey, float *tau, cudaStream_t st,
+                            LaunchCounter &lc);
 // Radial to orthographic depth in place; kinv.M[v] holds K^-1 of view v.
 void launch_radial_to_ortho(int V, int w, int h, const WarpCams &kinv, float *depth, cudaStream_t st,
                             LaunchCounter &lc);

@@ -277,6 +277,120 @@ void launch_zbuffer_splat(int V, int w, int h, const float *depth, const WarpCam
     lc.add(1);
 }
 
+// ------------------------------------------------------------------ warps from depth maps without GL
+// import_warps_from_depth (sources/import.cpp:243-450), float arithmetic as the reference's glm. WfdCams holds per
+// camera (views, then the target at index V): fx, fy, cx, cy, row-major R, centre C, and P = K [R | t].
+// Order-preserving uint key of a float (atomicMin on keys is min on floats, negative values included).
+__device__ __forceinline__ unsigned int fkey(float f) {
+    const unsigned int u = __float_as_uint(f);
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+}
+__device__ __forceinline__ float fkey_inv(unsigned int k) {
+    return __uint_as_float((k & 0x80000000u) ? (k & 0x7fffffffu) : ~k);
+}
+
+// X = d K^-1 (px, py, 1) with kc's K; world = R^T X + C with rc's R, C; out = P (world, 1) with pc's P.
+__device__ __forceinline__ void wfd_transfer(const float *kc, const float *rc, const float *pc, float d, float px,
+                                             float py, float out[3]) {
+    const float i00 = (float)(1.0 / (double)kc[0]), i11 = (float)(1.0 / (double)kc[1]);
+    const float i20 = -kc[2] / kc[0], i21 = -kc[3] / kc[1];
+    const float X0 = d * i00 * px + d * i20, X1 = d * i11 * py + d * i21, X2 = d;
+    const float *R = rc + 4, *C = rc + 13;
+    float Xw[3];
+#pragma unroll
+    for (int r = 0; r < 3; ++r) Xw[r] = R[0 * 3 + r] * X0 + R[1 * 3 + r] * X1 + R[2 * 3 + r] * X2 + C[r];
+    const float *P = pc + 16;
+#pragma unroll
+    for (int r = 0; r < 3; ++r) out[r] = P[r * 4 + 0] * Xw[0] + P[r * 4 + 1] * Xw[1] + P[r * 4 + 2] * Xw[2] + P[r * 4 + 3];
+}
+
+__global__ void k_wfd_clear(size_t N, unsigned int *ukey) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < N) ukey[i] = fkey(1000.0f);
+}
+
+// Pass 1: warps and the target depth map (min over dsf x dsf pixels from int(tau) - dsf/2).
+__global__ void k_wfd_project(int V, int w, int h, int dsf, const float *__restrict__ depth, int depth_channels,
+                              const WfdCams cams, int W, int H, float *__restrict__ tau, unsigned int *ukey) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    const int n = w * h;
+    if (m >= n) return;
+    const float d = depth[(size_t)v * depth_channels * n + m];
+    float *tv = tau + (size_t)v * 3 * n;
+    if ((double)d < 1.0 / 1000.0 || 1000.0 < (double)d) {
+        tv[m] = (float)-(double)w;
+        tv[n + m] = tv[2 * n + m] = (float)-(double)h;
+        return;
+    }
+    const float *c = cams.c[v], *u = cams.c[V];
+    float X[3];
+    wfd_transfer(c, c, u, d, (float)(m % w) + 0.5f, (float)(m / w) + 0.5f, X);
+    const float txf = X[0] / X[2], tyf = X[1] / X[2];
+    tv[m] = txf;
+    tv[n + m] = tv[2 * n + m] = tyf;
+    const unsigned int k = fkey(X[2]);
+    for (int i = 0; i < dsf; ++i)
+        for (int j = 0; j < dsf; ++j) {
+            const int px = (int)txf - dsf / 2 + j, py = (int)tyf - dsf / 2 + i;
+            if (0 <= px && px <= W - 1 && 0 <= py && py <= H - 1) atomicMin(ukey + (size_t)py * W + px, k);
+        }
+}
+
+// Pass 2: coverage-weighted target depth over the footprint, back-projection, 10-pixel test.
+__global__ void k_wfd_visibility(int V, int w, int h, int dsf, const WfdCams cams, int W, int H, int faithful,
+                                 const unsigned int *__restrict__ ukey, float *__restrict__ tau) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = blockIdx.y;
+    const int n = w * h;
+    if (m >= n) return;
+    float *tv = tau + (size_t)v * 3 * n;
+    const double tx = tv[m], ty = tv[n + m];
+    const double hd = (double)(float)dsf * 0.5;
+    float u_d = 0.f, u_norm = 0.f;
+    for (int i = 0; i < dsf + 1; ++i)
+        for (int j = 0; j < dsf + 1; ++j) {
+            const int px = (int)floor(tx - hd + 0.5) + j, py = (int)floor(ty - hd + 0.5) + i;
+            if (!(0 <= px && px <= W - 1 && 0 <= py && py <= H - 1)) continue;
+            const float zu = fkey_inv(ukey[(size_t)py * W + px]);
+            if (zu == 1000.0f) continue;
+            float dx = 1.0f, dy = 1.0f;
+            if (j == 0) dx = (float)(((double)(float)px + 0.5) - (tx - hd));
+            else if (j == dsf) dx = (float)((tx + hd) - ((double)(float)px - 0.5));
+            if (i == 0) dy = (float)(((double)(float)py + 0.5) - (ty - hd));
+            else if (i == dsf) dy = (float)((ty + hd) - ((double)(float)py - 0.5));
+            u_d += dx * dy * zu;
+            u_norm += dx * dy;
+        }
+    if (u_norm == 0.0f) {
+        tv[m] = (float)-(double)w;
+        tv[n + m] = tv[2 * n + m] = (float)-(double)h;
+        return;
+    }
+    u_d /= u_norm;
+    const float *c = cams.c[v], *u = cams.c[V];
+    float X[3];
+    wfd_transfer(u, faithful ? c : u, c, u_d, (float)((int)tx) + 0.5f, (float)((int)ty) + 0.5f, X);
+    const int ox = (int)(X[0] / X[2]), oy = (int)(X[1] / X[2]);
+    const int x = m % w, y = m / w;
+    if (ox - x < -10 || 10 < ox - x || oy - y < -10 || 10 < oy - y) {
+        tv[m] = (float)(-(double)w * 2.0);
+        tv[n + m] = tv[2 * n + m] = (float)(-(double)h * 2.0);
+    }
+}
+
+void launch_warp_from_depth(int V, int w, int h, int dsf, const float *depth, int depth_channels, const WfdCams &cams,
+                            int W, int H, int faithful, unsigned int *ukey, float *tau, cudaStream_t st,
+                            LaunchCounter &lc) {
+    ProfScope _ps(lc, "warp_from_depth", st);
+    const size_t N = (size_t)W * H;
+    const int n = w * h;
+    k_wfd_clear<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, ukey);
+    k_wfd_project<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, dsf, depth, depth_channels, cams, W, H, tau, ukey);
+    k_wfd_visibility<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, dsf, cams, W, H, faithful, ukey, tau);
+    lc.add(3);
+}
+
 // fromRadial2Ortho.frag:10-23: radial depth (and derivatives) to orthographic depth, in place. kinv holds K^-1
 // (row-major) of each view; X = K^-1 (x + 1/2, y + 1/2, 1), d = |X|, z / d and the derivatives' chain rule.
 __global__ void k_radial_to_ortho(int V, int w, int h, const WarpCams kinv, float *__restrict__ depth) {

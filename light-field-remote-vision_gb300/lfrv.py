@@ -88,7 +88,7 @@ EXPORTED = [
     "lfrv_last_error", "lfrv_version", "lfrv_config_default", "lfrv_config_parse_file", "lfrv_config_set",
     "lfrv_config_get_string", "lfrv_config_get_int", "lfrv_ctx_create", "lfrv_ctx_destroy", "lfrv_ctx_set_stream",
     "lfrv_ctx_launch_count", "lfrv_ctx_profile", "lfrv_ctx_profile_read", "lfrv_depth_radial_to_ortho",
-    "lfrv_depth_radial_to_ortho_dev", "lfrv_warp", "lfrv_warp_dev", "lfrv_ibr_color", "lfrv_ibr_color_dev",
+    "lfrv_depth_radial_to_ortho_dev", "lfrv_warp_from_depth", "lfrv_warp_from_depth_dev", "lfrv_warp", "lfrv_warp_dev", "lfrv_ibr_color", "lfrv_ibr_color_dev",
     "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_stage_weights",
     "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
@@ -287,6 +287,15 @@ class Context:
         return out
 
     # ---- warp stage
+    def warp_from_depth(self, depth: np.ndarray, cams, target: Camera, dsf: int, faithful: bool = True):
+        """Warps (V x 3 x h x w) from depth maps (V x C x h x w, plane 0 = z) without the GL pipeline."""
+        depth = f32(depth)
+        V, ch, h, w = depth.shape
+        tau = np.zeros((V, 3, h, w), np.float32)
+        _check(LIB.lfrv_warp_from_depth(self._h, V, w, h, dsf, fptr(depth), ch, cameras_array(cams), C.byref(target),
+                                        int(faithful), fptr(tau)))
+        return tau
+
     def depth_radial_to_ortho(self, depth: np.ndarray, cams) -> np.ndarray:
         """Radial to orthographic depth maps (V x 3 x h x w); returns a converted copy."""
         d = f32(depth).copy()
@@ -478,6 +487,10 @@ def _declare() -> None:
     LIB.lfrv_config_get_string.argtypes = [C.c_char_p, C.c_char_p, C.c_size_t]
     LIB.lfrv_pfm_read.argtypes = [C.c_char_p, _I, _I, _I, _F, C.c_size_t]
     LIB.lfrv_pfm_write.argtypes = [C.c_char_p, C.c_int, C.c_int, C.c_int, _F]
+    LIB.lfrv_warp_from_depth.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, _F, C.c_int, C.POINTER(Camera),
+                                         C.POINTER(Camera), C.c_int, _F]
+    LIB.lfrv_warp_from_depth_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, vp, C.c_int, C.POINTER(Camera),
+                                             C.POINTER(Camera), C.c_int, vp]
     LIB.lfrv_depth_radial_to_ortho.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(Camera), _F]
     LIB.lfrv_depth_radial_to_ortho_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(Camera), vp]
     LIB.lfrv_cg_solve_static.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp, _I, _D]

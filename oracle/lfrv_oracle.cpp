@@ -1756,6 +1756,123 @@ int orc_warp(int V, int w, int h, const float *depth, const lfrv_camera *cams, c
     return 0;
 }
 
+// import_warps_from_depth, sources/import.cpp:243-450: warps from orthographic depth maps and cameras without
+// the GL pipeline, in float like the reference's glm arithmetic. Pass 1 projects every source pixel into the
+// target (tau = x_h / z_h) and keeps, over the dsf x dsf pixels from int(tau) - dsf/2, the smallest target depth
+// z_h. Pass 2 averages that depth map over the pixel's footprint (overlaps dx dy, INVALID_DEPTH texels skipped),
+// back-projects the nearest target pixel with it and marks the warp (-2w, -2h) when the result lands more than
+// 10 pixels from the source pixel; no coverage gives (-w, -h). Faithful mode back-projects with the source
+// camera's R and C (the reference passes v_i_cam's, import.cpp:412-415); otherwise with the target's.
+// tau: V x 3 x n (tau_x, tau_y, tau_y as the reference writes it).
+namespace orc {
+struct GlmCam {
+    float fx, fy, cx, cy;  // K entries the reference uses for K^-1
+    float R[9], C[3], P[12];  // row-major R, centre, P = K [R | t] in float
+};
+inline GlmCam glm_cam(const lfrv_camera &c) {
+    GlmCam g;
+    g.fx = c.K[0];
+    g.fy = c.K[4];
+    g.cx = c.K[2];
+    g.cy = c.K[5];
+    for (int i = 0; i < 9; ++i) g.R[i] = c.R[i];
+    for (int r = 0; r < 3; ++r) g.C[r] = -(c.R[0 * 3 + r] * c.t[0] + c.R[1 * 3 + r] * c.t[1] + c.R[2 * 3 + r] * c.t[2]);
+    for (int r = 0; r < 3; ++r) {
+        for (int col = 0; col < 3; ++col)
+            g.P[r * 4 + col] = c.K[r * 3 + 0] * c.R[0 * 3 + col] + c.K[r * 3 + 1] * c.R[1 * 3 + col] +
+                               c.K[r * 3 + 2] * c.R[2 * 3 + col];
+        g.P[r * 4 + 3] = c.K[r * 3 + 0] * c.t[0] + c.K[r * 3 + 1] * c.t[1] + c.K[r * 3 + 2] * c.t[2];
+    }
+    return g;
+}
+// X = d K^-1 (px, py, 1) with K^-1 = [[1/fx, 0, -cx/fx], [0, 1/fy, -cy/fy], [0, 0, 1]]; world = R^T X + C of `rc`;
+// then projected with `pc`: out = P (world, 1).
+inline void wfd_transfer(const GlmCam &kc, const GlmCam &rc, const GlmCam &pc, float d, float px, float py,
+                         float out[3]) {
+    const float i00 = (float)(1.0 / kc.fx), i11 = (float)(1.0 / kc.fy), i20 = -kc.cx / kc.fx, i21 = -kc.cy / kc.fy;
+    const float X[3] = {d * i00 * px + d * i20, d * i11 * py + d * i21, d};
+    float Xw[3];
+    for (int r = 0; r < 3; ++r) Xw[r] = rc.R[0 * 3 + r] * X[0] + rc.R[1 * 3 + r] * X[1] + rc.R[2 * 3 + r] * X[2] + rc.C[r];
+    for (int r = 0; r < 3; ++r)
+        out[r] = pc.P[r * 4 + 0] * Xw[0] + pc.P[r * 4 + 1] * Xw[1] + pc.P[r * 4 + 2] * Xw[2] + pc.P[r * 4 + 3];
+}
+}  // namespace orc
+
+int orc_warp_from_depth(int V, int w, int h, int dsf, const float *depth, int depth_channels, const lfrv_camera *cams,
+                        const lfrv_camera *target, int faithful, float *tau) {
+    const size_t n = (size_t)w * h;
+    const int W = target->width, H = target->height;
+    const double kInvalid = 1000.0;
+    std::vector<float> ud((size_t)W * H, (float)kInvalid);
+    const orc::GlmCam u = orc::glm_cam(*target);
+    for (int v = 0; v < V; ++v) {
+        const orc::GlmCam c = orc::glm_cam(cams[v]);
+        const float *dz = depth + (size_t)v * depth_channels * n;
+        float *tv = tau + (size_t)v * 3 * n;
+        for (size_t m = 0; m < n; ++m) {
+            const float d = dz[m];
+            if (d < 1.0 / kInvalid || kInvalid < d) {
+                tv[m] = (float)-(double)w;
+                tv[n + m] = tv[2 * n + m] = (float)-(double)h;
+                continue;
+            }
+            const float x = (float)(m % w), y = (float)(m / w);
+            float X[3];
+            orc::wfd_transfer(c, c, u, d, x + 0.5f, y + 0.5f, X);
+            const float txf = X[0] / X[2], tyf = X[1] / X[2];
+            tv[m] = txf;
+            tv[n + m] = tv[2 * n + m] = tyf;
+            for (int i = 0; i < dsf; ++i)
+                for (int j = 0; j < dsf; ++j) {
+                    const int px = (int)txf - dsf / 2 + j, py = (int)tyf - dsf / 2 + i;
+                    if (0 <= px && px <= W - 1 && 0 <= py && py <= H - 1) {
+                        float &slot = ud[(size_t)py * W + px];
+                        if (X[2] < slot) slot = X[2];
+                    }
+                }
+        }
+    }
+    for (int v = 0; v < V; ++v) {
+        const orc::GlmCam c = orc::glm_cam(cams[v]);
+        const orc::GlmCam &rc = faithful ? c : u;
+        float *tv = tau + (size_t)v * 3 * n;
+        for (size_t m = 0; m < n; ++m) {
+            const double tx = tv[m], ty = tv[n + m];
+            float u_d = 0.f, u_norm = 0.f;
+            for (int i = 0; i < dsf + 1; ++i)
+                for (int j = 0; j < dsf + 1; ++j) {
+                    const int px = (int)std::floor(tx - (double)(float)dsf * 0.5 + 0.5) + j;
+                    const int py = (int)std::floor(ty - (double)(float)dsf * 0.5 + 0.5) + i;
+                    if (!(0 <= px && px <= W - 1 && 0 <= py && py <= H - 1)) continue;
+                    const float zu = ud[(size_t)py * W + px];
+                    if (zu == (float)kInvalid) continue;
+                    float dx = 1.0f, dy = 1.0f;
+                    if (j == 0) dx = (float)(((double)(float)px + 0.5) - (tx - 0.5 * (double)(float)dsf));
+                    else if (j == dsf) dx = (float)((tx + 0.5 * (double)(float)dsf) - ((double)(float)px - 0.5));
+                    if (i == 0) dy = (float)(((double)(float)py + 0.5) - (ty - 0.5 * (double)(float)dsf));
+                    else if (i == dsf) dy = (float)((ty + 0.5 * (double)(float)dsf) - ((double)(float)py - 0.5));
+                    u_d += dx * dy * zu;
+                    u_norm += dx * dy;
+                }
+            if (u_norm == 0.0f) {
+                tv[m] = (float)-(double)w;
+                tv[n + m] = tv[2 * n + m] = (float)-(double)h;
+                continue;
+            }
+            u_d /= u_norm;
+            float X[3];
+            orc::wfd_transfer(u, rc, c, u_d, (float)((int)tx) + 0.5f, (float)((int)ty) + 0.5f, X);
+            const int ox = (int)(X[0] / X[2]), oy = (int)(X[1] / X[2]);
+            const int x = (int)(m % w), y = (int)(m / w);
+            if (ox - x < -10 || 10 < ox - x || oy - y < -10 || 10 < oy - y) {
+                tv[m] = (float)(-(double)w * 2.0);
+                tv[n + m] = tv[2 * n + m] = (float)(-(double)h * 2.0);
+            }
+        }
+    }
+    return 0;
+}
+
 // fromRadial2Ortho.frag:10-23 (FrameBuffer::fromRadial2Ortho, sources/openGL/frameBuffer.cpp:263-300), in
 // place on V x 3 x n depth maps (radial depth and its x / y derivatives): with X = K^-1 (x + 1/2, y + 1/2, 1)
 // and d = |X|, z_o = z / d, dz_o/dx = dz/dx / d - z (X . K^-1 column 0) / d^3, and likewise for y with column 1.

@@ -167,6 +167,16 @@ def warp(depth, cams, target):
     return tau, dpart, zbuf
 
 
+def warp_from_depth(depth, cams, target, dsf, faithful=1):
+    """import_warps_from_depth: V x 3 x h x w warps from V x C x h x w depth maps (plane 0 = z)."""
+    depth = f32(depth)
+    V, ch, h, w = depth.shape
+    tau = np.zeros((V, 3, h, w), np.float32)
+    LIB.orc_warp_from_depth(V, w, h, dsf, fptr(depth), ch, lfrv.cameras_array(cams), C.byref(target), int(faithful),
+                            fptr(tau))
+    return tau
+
+
 def depth_radial_to_ortho(depth, cams):
     """fromRadial2Ortho.frag on V x 3 x h x w depth maps (returns a converted copy)."""
     d = f32(depth).copy()

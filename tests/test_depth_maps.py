@@ -50,3 +50,43 @@ def test_gpu_matches_oracle(preset, w):
         got = ctx.depth_radial_to_ortho(radial, sc.cams)
     tol = 2e-6 * np.abs(want).max(axis=(0, 2, 3), keepdims=True) + 1e-8
     assert np.all(np.abs(got - want) <= tol)
+
+
+# ------------------------------------------------------------------ warps from depth maps (import.cpp:243-450)
+def _holey_depth(sc):
+    d = sc.depth.copy()
+    d[0, 0, :3, :] = 0.0      # below 1/INVALID_DEPTH: no warp
+    d[1, 0, 5, 5] = 2000.0    # above INVALID_DEPTH
+    return d
+
+
+@pytest.mark.parametrize("preset,w", [(1, 48), (2, 40)])
+def test_oracle_warp_from_depth_matches_projection(preset, w):
+    """Pass 1 is the projection the GL path computes; invalid depths give (-w, -h)."""
+    sc = scene(preset, w)
+    d = _holey_depth(sc)
+    tau = pyoracle.warp_from_depth(d, sc.cams, sc.target, sc.params.dsf, faithful=1)
+    gl, _, _ = pyoracle.warp(sc.depth, sc.cams, sc.target)
+    ok = (tau[:, 0] >= 0) & (gl[:, 0] >= 0)
+    assert ok.mean() > 0.9
+    assert np.max(np.abs(tau[:, 0][ok] - gl[:, 0][ok])) < 1e-4
+    assert np.max(np.abs(tau[:, 1][ok] - gl[:, 1][ok])) < 1e-4
+    assert np.all(tau[0, 0, :3, :] == -w) and np.all(tau[0, 1, :3, :] == -w)
+    assert tau[1, 0, 5, 5] == -w
+    assert np.array_equal(tau[:, 1], tau[:, 2])  # written as (tau_x, tau_y, tau_y)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("preset,w", [(1, 48), (2, 40)])
+@pytest.mark.parametrize("faithful", [1, 0])
+def test_gpu_warp_from_depth_matches_oracle(preset, w, faithful):
+    sc = scene(preset, w)
+    d = _holey_depth(sc)
+    want = pyoracle.warp_from_depth(d, sc.cams, sc.target, sc.params.dsf, faithful=faithful)
+    with lfrv.Context(0) as ctx:
+        got = ctx.warp_from_depth(d, sc.cams, sc.target, sc.params.dsf, faithful=bool(faithful))
+    code = np.where(got[:, 0] < 0, got[:, 0], 0)
+    rcode = np.where(want[:, 0] < 0, want[:, 0], 0)
+    assert np.mean(code != rcode) < 1e-3
+    ok = (code == 0) & (rcode == 0)
+    assert np.max(np.abs(got[:, :2][np.stack([ok, ok], 1)] - want[:, :2][np.stack([ok, ok], 1)])) < 1e-4
