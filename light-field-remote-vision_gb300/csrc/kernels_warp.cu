@@ -292,16 +292,25 @@ __device__ __forceinline__ float fkey_inv(unsigned int k) {
 // X = d K^-1 (px, py, 1) with kc's K; world = R^T X + C with rc's R, C; out = P (world, 1) with pc's P.
 __device__ __forceinline__ void wfd_transfer(const float *kc, const float *rc, const float *pc, float d, float px,
                                              float py, float out[3]) {
+    // every product and sum rounded on its own (no FMA contraction), as the host arithmetic of the reference
     const float i00 = (float)(1.0 / (double)kc[0]), i11 = (float)(1.0 / (double)kc[1]);
-    const float i20 = -kc[2] / kc[0], i21 = -kc[3] / kc[1];
-    const float X0 = d * i00 * px + d * i20, X1 = d * i11 * py + d * i21, X2 = d;
+    const float i20 = -__fdiv_rn(kc[2], kc[0]), i21 = -__fdiv_rn(kc[3], kc[1]);
+    const float X0 = __fadd_rn(__fmul_rn(__fmul_rn(d, i00), px), __fmul_rn(d, i20));
+    const float X1 = __fadd_rn(__fmul_rn(__fmul_rn(d, i11), py), __fmul_rn(d, i21));
+    const float X2 = d;
     const float *R = rc + 4, *C = rc + 13;
     float Xw[3];
 #pragma unroll
-    for (int r = 0; r < 3; ++r) Xw[r] = R[0 * 3 + r] * X0 + R[1 * 3 + r] * X1 + R[2 * 3 + r] * X2 + C[r];
+    for (int r = 0; r < 3; ++r)
+        Xw[r] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(R[0 * 3 + r], X0), __fmul_rn(R[1 * 3 + r], X1)),
+                                    __fmul_rn(R[2 * 3 + r], X2)),
+                          C[r]);
     const float *P = pc + 16;
 #pragma unroll
-    for (int r = 0; r < 3; ++r) out[r] = P[r * 4 + 0] * Xw[0] + P[r * 4 + 1] * Xw[1] + P[r * 4 + 2] * Xw[2] + P[r * 4 + 3];
+    for (int r = 0; r < 3; ++r)
+        out[r] = __fadd_rn(__fadd_rn(__fadd_rn(__fmul_rn(P[r * 4 + 0], Xw[0]), __fmul_rn(P[r * 4 + 1], Xw[1])),
+                                     __fmul_rn(P[r * 4 + 2], Xw[2])),
+                           P[r * 4 + 3]);
 }
 
 __global__ void k_wfd_clear(size_t N, unsigned int *ukey) {
@@ -359,8 +368,8 @@ __global__ void k_wfd_visibility(int V, int w, int h, int dsf, const WfdCams cam
             else if (j == dsf) dx = (float)((tx + hd) - ((double)(float)px - 0.5));
             if (i == 0) dy = (float)(((double)(float)py + 0.5) - (ty - hd));
             else if (i == dsf) dy = (float)((ty + hd) - ((double)(float)py - 0.5));
-            u_d += dx * dy * zu;
-            u_norm += dx * dy;
+            u_d = __fadd_rn(u_d, __fmul_rn(__fmul_rn(dx, dy), zu));
+            u_norm = __fadd_rn(u_norm, __fmul_rn(dx, dy));
         }
     if (u_norm == 0.0f) {
         tv[m] = (float)-(double)w;
