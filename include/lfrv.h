@@ -209,6 +209,25 @@ int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm,
                          const lfrv_camera *cams, const lfrv_camera *target,
                          float *d_out, lfrv_stats *stats);
 
+/* ---------------------------------------------------------------- batched targets
+ * No single reference counterpart: the reference renders one target per process run (main, sources/main.cpp:
+ * 349-357). A batch renders many target views, each with its own light field, sizes and options, on device
+ * buffers and the context's stream. IBR_gradient jobs with faithful = 0 run warp, set-up and hole filling one
+ * after another, then share one persistent CG launch (k_cg_batch) in which every job keeps its own tiles,
+ * dot products, stop rule and statistics; other jobs run as lfrv_render_view_dev would. The call returns when
+ * every output is written. */
+typedef struct lfrv_view_job {
+    const lfrv_config *cfg;    /* sizes (w, h, dsf, nviews) and solver options of this target */
+    int algorithm;             /* 0 IBR_color, 1 IBR_gradient */
+    const float *d_views;      /* nviews x 3 x h x w, device */
+    const float *d_depth;      /* nviews x 3 x h x w (z, dz/dx, dz/dy), device */
+    const lfrv_camera *cams;   /* nviews input cameras, host */
+    const lfrv_camera *target; /* host */
+    float *d_out;              /* 3 x H x W, device */
+    lfrv_stats *stats;         /* optional */
+} lfrv_view_job;
+int lfrv_render_views_dev(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count);
+
 /* ---------------------------------------------------------------- stage calls
  * Fine-grained entry points mirroring the cocolib stage functions, used by the parity tests.
  * All take host buffers. "views/tau/dpart" as above; U, G etc. are 3 x H x W.

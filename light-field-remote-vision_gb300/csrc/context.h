@@ -37,6 +37,8 @@ struct Workspace {
     DevBuf lapU, resg, ugrad;
     // target depth keys of the warps-from-depth path
     DevBuf ukey;
+    // batched targets: per-job buffers and the launch descriptors
+    DevBuf batch, batch_meta;
     // CG
     DevBuf r, d, q, U0, holes, hole_count;
     // reductions and persistent-solver state

@@ -616,11 +616,10 @@ static void cg_persistent_async(lfrv_ctx *c, int W, int H, int max_iter, double 
     c->pending.cg = true;
 }
 
-static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
-                           const float *init, float *out, lfrv_stats *st) {
-    check_solver_options(cfg);
-    const Geometry G = geometry(cfg);
-    if (G.W < 2 || G.H < 2) raise(LFRV_E_ARG, "IBR_gradient needs a target of at least 2 x 2 pixels");
+// IBR_gradient up to the CG (sources/gradientIBR.cpp:12-120): weights, the set-up pass (visibility, weighted
+// average, gradient splat) into U, gx, gy, then hole filling of U (or U = init).
+static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry &G, const float *img,
+                             const float *tau2, const float *dp2, const float *init, float *U, float *gx, float *gy) {
     const size_t N = G.N;
     cudaStream_t s = c->stream;
     Workspace &ws = c->ws;
@@ -634,12 +633,24 @@ static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img
     check_launch("weights");
     // visibility, weighted average and gradient splat in one pass of the inverse map
     float *vg = view_gradients(c, G, img);
-    float *U = ws.U.as<float>();
-    launch_gradient_setup(G, B, tau2, img, vg, b.wgt, s2, b.vis, U, b.gx, b.gy, ws.mask.as<float>(), s, c->launches);
+    launch_gradient_setup(G, B, tau2, img, vg, b.wgt, s2, b.vis, U, gx, gy, ws.mask.as<float>(), s, c->launches);
     check_launch("gradient set-up");
-    c->pending = Pending{};
     if (init) LFRV_CUDA(cudaMemcpyAsync(U, init, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
     else hole_fill_async(c, G.W, G.H, b.vis, U, cfg.hole_fill_iter);
+}
+
+static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
+                           const float *init, float *out, lfrv_stats *st) {
+    check_solver_options(cfg);
+    const Geometry G = geometry(cfg);
+    if (G.W < 2 || G.H < 2) raise(LFRV_E_ARG, "IBR_gradient needs a target of at least 2 x 2 pixels");
+    const size_t N = G.N;
+    cudaStream_t s = c->stream;
+    Workspace &ws = c->ws;
+    ColorBuffers b = color_buffers(c, G);
+    float *U = ws.U.as<float>();
+    c->pending = Pending{};
+    gradient_prepare(c, cfg, G, img, tau2, dp2, init, U, b.gx, b.gy);
     int it_faithful = 0;
     if (cfg.faithful) it_faithful = cg_faithful(c, G.W, G.H, b.gx, b.gy, U);
     else cg_persistent_async(c, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U);
@@ -1165,6 +1176,159 @@ extern "C" int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int a
     CTX_CHECK(ctx);
     if (!cfg || !d_views || !d_depth || !cams || !target || !d_out) return fail(LFRV_E_ARG, "null argument");
     render_view_impl(ctx, *cfg, algorithm, d_views, d_depth, cams, target, d_out, stats, nullptr, nullptr);
+    LFRV_API_END
+}
+
+// ====================================================================== batched targets
+// IBR_gradient jobs with the corrected CG share one k_cg_batch launch (per launch at most as many jobs as resident
+// blocks); every other job runs on its own. Per gradient job the batch pool holds U, gx, gy, r, dA, dB (14 N
+// floats) and 8 doubles of state.
+static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
+    if (count <= 0 || !jobs) raise(LFRV_E_ARG, "empty batch");
+    cudaStream_t s = c->stream;
+    Workspace &ws = c->ws;
+    struct Slot {
+        int job;
+        Geometry G;
+        size_t off;  // float offset of the job's buffers in the pool
+    };
+    std::vector<Slot> batched;
+    size_t pool = 0;
+    for (int j = 0; j < count; ++j) {
+        const lfrv_view_job &J = jobs[j];
+        if (!J.cfg || !J.d_views || !J.d_depth || !J.cams || !J.target || !J.d_out)
+            raise(LFRV_E_ARG, "job %d: null argument", j);
+        const Geometry G = geometry(*J.cfg);
+        if (J.target->width != G.W || J.target->height != G.H) raise(LFRV_E_ARG, "job %d: target size mismatch", j);
+        if (J.stats) std::memset(J.stats, 0, sizeof(*J.stats));
+        if (J.algorithm == 1 && !J.cfg->faithful) {
+            check_solver_options(*J.cfg);
+            if (G.W < 2 || G.H < 2) raise(LFRV_E_ARG, "job %d: target smaller than 2 x 2", j);
+            batched.push_back({j, G, pool});
+            pool += 14 * G.N + 16;  // + 8 doubles of state, kept 64-byte aligned by the 16-float pad
+        }
+    }
+    ws.batch.ensure(sizeof(float) * std::max<size_t>(pool, 16));
+    float *base = ws.batch.as<float>();
+    c->pending = Pending{};
+    // every job's warp stage; gradient jobs stop before the CG, the others run to the end
+    for (int j = 0; j < count; ++j) {
+        const lfrv_view_job &J = jobs[j];
+        const Geometry G = geometry(*J.cfg);
+        ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+        ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+        warp(c, G.V, G.w, G.h, J.d_depth, J.cams, J.target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(),
+             nullptr);
+        const Slot *sl = nullptr;
+        for (const Slot &b : batched)
+            if (b.job == j) sl = &b;
+        if (sl) {
+            float *U = base + sl->off;
+            gradient_prepare(c, *J.cfg, G, J.d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, U, U + 3 * G.N,
+                             U + 4 * G.N);
+            // keep this job's hole-fill iteration count (state slot 8) beside its CG state
+            double *st = reinterpret_cast<double *>(U + 14 * G.N);
+            LFRV_CUDA(cudaMemcpyAsync(st + 6, ws.state.as<double>() + 8, sizeof(double), cudaMemcpyDeviceToDevice, s));
+        } else {
+            // a job outside the batched CG: report what is pending first, then run it to the end and collect its
+            // statistics and barrier status before the next job reuses the state slots
+            sync(c);
+            finish_stats(c);
+            if (J.algorithm == 0)
+                color_solve(c, *J.cfg, J.d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, J.d_out, J.stats);
+            else
+                gradient_solve(c, *J.cfg, J.d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, J.d_out, J.stats);
+            sync(c);
+            finish_stats(c);
+        }
+    }
+    // the CG of all gradient jobs, in launches of at most `resident` jobs
+    const int resident = cg_batch_resident_blocks();
+    for (size_t first = 0; first < batched.size(); first += (size_t)resident) {
+        const size_t cnt = std::min(batched.size() - first, (size_t)resident);
+        std::vector<CgProblem> probs(cnt);
+        std::vector<int> tiles(cnt);
+        long long total = 0;
+        for (size_t q = 0; q < cnt; ++q) {
+            const Geometry &G = batched[first + q].G;
+            tiles[q] = ((G.W + 63) / 64) * ((G.H + 15) / 16);
+            total += tiles[q];
+        }
+        // blocks in proportion to the tiles, at least one each, no more than resident in all
+        std::vector<int> nb(cnt);
+        int used = 0;
+        for (size_t q = 0; q < cnt; ++q) {
+            nb[q] = std::max(1, (int)((long long)resident * tiles[q] / std::max(1LL, total)));
+            nb[q] = std::min(nb[q], tiles[q]);
+            used += nb[q];
+        }
+        while (used > resident) {  // trim the largest allocations
+            size_t big = 0;
+            for (size_t q = 1; q < cnt; ++q)
+                if (nb[q] > nb[big]) big = q;
+            --nb[big];
+            --used;
+        }
+        std::vector<int> block_prob(used);
+        int b0 = 0;
+        for (size_t q = 0; q < cnt; ++q) {
+            const Slot &sl = batched[first + q];
+            const lfrv_config &cfg = *jobs[sl.job].cfg;
+            float *U = base + sl.off;
+            CgProblem &P = probs[q];
+            P.W = sl.G.W;
+            P.H = sl.G.H;
+            P.tiles_x = (sl.G.W + 63) / 64;
+            P.ntiles = tiles[q];
+            P.b0 = b0;
+            P.nb = nb[q];
+            P.max_iter = cfg.cg_max_iter;
+            P.gap_tol = cfg.cg_gap_tol;
+            P.gx = U + 3 * sl.G.N;
+            P.gy = U + 4 * sl.G.N;
+            P.U = U;
+            P.r = U + 5 * sl.G.N;
+            P.dA = U + 8 * sl.G.N;
+            P.dB = U + 11 * sl.G.N;
+            P.state = reinterpret_cast<double *>(U + 14 * sl.G.N);
+            for (int k = 0; k < nb[q]; ++k) block_prob[b0 + k] = (int)q;
+            b0 += nb[q];
+        }
+        ws.batch_meta.ensure(sizeof(CgProblem) * cnt + sizeof(int) * (used + cnt) + 64);
+        char *meta = ws.batch_meta.as<char>();
+        CgProblem *d_probs = reinterpret_cast<CgProblem *>(meta);
+        int *d_block_prob = reinterpret_cast<int *>(meta + sizeof(CgProblem) * cnt);
+        int *d_done = d_block_prob + used;
+        LFRV_CUDA(cudaMemcpyAsync(d_probs, probs.data(), sizeof(CgProblem) * cnt, cudaMemcpyHostToDevice, s));
+        LFRV_CUDA(cudaMemcpyAsync(d_block_prob, block_prob.data(), sizeof(int) * used, cudaMemcpyHostToDevice, s));
+        double *part = partial_buf(c, (size_t)8 * used);
+        const GridBarrier gb = fresh_barrier(c);
+        LFRV_CUDA(launch_cg_batch(d_probs, d_block_prob, (int)cnt, used, part, part + 4 * (size_t)used, d_done, gb, s,
+                                  c->launches));
+        LFRV_CUDA(cudaStreamSynchronize(s));  // the host vectors above go out of scope
+    }
+    for (const Slot &sl : batched)
+        LFRV_CUDA(cudaMemcpyAsync(jobs[sl.job].d_out, base + sl.off, sizeof(float) * 3 * sl.G.N,
+                                  cudaMemcpyDeviceToDevice, s));
+    sync(c);
+    for (const Slot &sl : batched) {
+        lfrv_stats *st = jobs[sl.job].stats;
+        if (!st) continue;
+        double state[8];
+        LFRV_CUDA(cudaMemcpy(state, base + sl.off + 14 * sl.G.N, sizeof(state), cudaMemcpyDeviceToHost));
+        st->outer_iterations = (int)state[5];
+        st->gap = state[4];
+        st->energy = state[3];
+        st->hole_fill_iterations = (int)state[6];
+        st->stop_reason = (jobs[sl.job].cfg->cg_gap_tol > 0 && state[4] <= jobs[sl.job].cfg->cg_gap_tol) ? 4 : 0;
+    }
+    finish_stats(c);
+}
+
+extern "C" int lfrv_render_views_dev(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    render_views(ctx, jobs, count);
     LFRV_API_END
 }
 

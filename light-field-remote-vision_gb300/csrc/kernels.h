@@ -148,11 +148,28 @@ struct GridBarrier {
     unsigned int *count;
     int *err;
 };
-int persistent_partials();
+int persistent_partials();  // upper bound of blocks (partials per slot)
+
+// One target of a batched CG launch (k_cg_batch): its image, buffers and the contiguous range of blocks that
+// work on it. state: [0..2] delta, [3] E, [4] gap, [5] iterations (written by the problem's first block).
+struct CgProblem {
+    int W, H, tiles_x, ntiles;
+    int b0, nb;
+    int max_iter;
+    double gap_tol;
+    const float *gx, *gy;
+    float *U, *r, *dA, *dB;
+    double *state;
+};
+// Blocks of a batched launch: as many as can be resident with k_cg_batch's shape.
+int cg_batch_resident_blocks();
+cudaError_t launch_cg_batch(const CgProblem *d_probs, const int *d_block_prob, int nprob, int blocks, double *partA,
+                            double *partB, int *done, GridBarrier gb, cudaStream_t st, LaunchCounter &lc);
+
 int rof_persistent_steps(int niter);
 cudaError_t launch_rof_persistent(int W, int H, int niter, float tau, float sigma, float lam, float *U0, float *P0,
                                   float *U1, float *P1, const float *F, const float *g, GridBarrier gb, cudaStream_t st,
-                                  LaunchCounter &lc);  // upper bound of blocks (partials per slot)
+                                  LaunchCounter &lc);
 cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
                                  float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
                                  double *state, cudaStream_t st, LaunchCounter &lc);

@@ -686,6 +686,212 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
     }
 }
 
+// Batched corrected CG: many targets (CgProblem) in one cooperative launch. Each problem owns the blocks
+// [b0, b0 + nb) (block_prob maps a block to its problem), so its tiles, block partials and FP64 scalars never mix
+// with another problem's; all problems share the grid barriers. A problem that has met its stop rule idles;
+// done[p] (written by the problem's first block at the top of every iteration) tells every block, after the next
+// barrier, whether all problems have stopped, and then the whole grid leaves together. Per problem the
+// arithmetic is k_cg_persistent<false>'s.
+__global__ void __launch_bounds__(kPersistThreads) k_cg_batch(const CgProblem *__restrict__ probs,
+                                                              const int *__restrict__ block_prob, int nprob,
+                                                              double *partA, double *partB, int *done,
+                                                              GridBarrier gb) {
+    __shared__ double sh[8];
+    __shared__ float tile[3][kHaloY][kHaloX];
+    __shared__ float s_coef[3];
+    __shared__ int s_stop, s_all;
+    const int pid = block_prob[blockIdx.x];
+    const CgProblem P = probs[pid];
+    const int W = P.W, H = P.H;
+    const size_t N = (size_t)W * H;
+    const int lb = (int)blockIdx.x - P.b0;  // block index within the problem
+    const int G = (int)gridDim.x;
+    const float lambda = 1.0f;
+    float *U = P.U, *r = P.r;
+    unsigned int gen = 0;
+    // ---- phase 0 (as k_cg_persistent): r = b - A u0 and E(u0)
+    {
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (size_t o = (size_t)lb * blockDim.x + threadIdx.x; o < N; o += (size_t)P.nb * blockDim.x) {
+            const int x = (int)(o % W), y = (int)(o / W);
+            const float gxo = __ldg(P.gx + o), gyo = __ldg(P.gy + o);
+            const float gxl = (x > 0) ? __ldg(P.gx + o - 1) : 0.f, gyu = (y > 0) ? __ldg(P.gy + o - W) : 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float *u = U + c * N;
+                const float uc = __ldcg(u + o);
+                float lx, ly;
+                if (x == 0) lx = uc - __ldcg(u + o + 1) + gxo;
+                else if (x < W - 1) lx = 2.f * uc - __ldcg(u + o - 1) - __ldcg(u + o + 1) + gxo - gxl;
+                else lx = uc - __ldcg(u + o - 1) - gxl;
+                if (y == 0) ly = uc - __ldcg(u + o + W) + gyo;
+                else if (y < H - 1) ly = 2.f * uc - __ldcg(u + o - W) - __ldcg(u + o + W) + gyo - gyu;
+                else ly = uc - __ldcg(u + o - W) - gyu;
+                const float rv = -(lx + ly);
+                r[c * N + o] = rv;
+                acc[c] += rv * rv;
+                float e = 0.f;
+                if (x < W - 1) {
+                    const float a = __ldcg(u + o + 1) - uc - gxo;
+                    e += a * a;
+                }
+                if (y < H - 1) {
+                    const float a = __ldcg(u + o + W) - uc - gyo;
+                    e += a * a;
+                }
+                acc[3] += 0.5f * e;
+            }
+        }
+        block_partials_f(acc, 4, partB, G);
+    }
+    if (!grid_sync(gb, gen)) return;
+    // the problem's partials sit at [slot * G + b0, slot * G + b0 + nb): one warp sums them in a fixed order
+    auto reduce_own = [&](const double *part, int nslots) {
+        if (threadIdx.x < 32) {
+            for (int sl = 0; sl < nslots; ++sl) {
+                double acc = 0.0;
+                for (int i = threadIdx.x; i < P.nb; i += 32) acc += __ldcg(part + (size_t)sl * G + P.b0 + i);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+                if (threadIdx.x == 0) sh[sl] = acc;
+            }
+        }
+        __syncthreads();
+    };
+    reduce_own(partB, 4);
+    double delta[3] = {sh[0], sh[1], sh[2]};
+    double E = sh[3];
+    double gap = 1e300;
+    float beta[3] = {0.f, 0.f, 0.f};
+    const float *dold = r;
+    float *dnew = P.dA;
+    int it = 0, stopped_at = -1;
+    const int tiles_x = P.tiles_x, ntiles = P.ntiles;
+    for (;; ++it) {
+        if (threadIdx.x == 0) {
+            if (stopped_at < 0) {
+                const double bound = (delta[0] + delta[1] + delta[2]) / (2.0 * (double)lambda);
+                gap = (E - bound) > 0 ? bound / (E - bound) : 1e300;
+                if (it >= P.max_iter || (P.gap_tol > 0 && gap <= P.gap_tol)) stopped_at = it;
+            }
+            s_stop = stopped_at >= 0 ? 1 : 0;
+            if (lb == 0) done[pid] = s_stop;
+        }
+        __syncthreads();
+        const bool idle = s_stop != 0;
+        // ---- phase A (skipped by a stopped problem)
+        {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            if (!idle) {
+                for (int t = lb; t < ntiles; t += P.nb) {
+                    const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
+                    for (int k = threadIdx.x; k < 3 * kHaloY * kHaloX; k += blockDim.x) {
+                        const int c = k / (kHaloY * kHaloX), rem = k % (kHaloY * kHaloX);
+                        const int gx = x0 - 1 + rem % kHaloX, gy = y0 - 1 + rem / kHaloX;
+                        float v = 0.f;
+                        if (gx >= 0 && gx < W && gy >= 0 && gy < H) {
+                            const size_t o = c * N + (size_t)gy * W + gx;
+                            v = __ldcg(r + o) + beta[c] * __ldcg(dold + o);
+                        }
+                        tile[c][rem / kHaloX][rem % kHaloX] = v;
+                    }
+                    __syncthreads();
+                    for (int p = threadIdx.x; p < kTileX * kTileY; p += blockDim.x) {
+                        const int lx = p % kTileX, ly = p / kTileX, x = x0 + lx, y = y0 + ly;
+                        if (x >= W || y >= H) continue;
+                        const size_t o = (size_t)y * W + x;
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            const float qv = tile_op(tile[c], lx + 1, ly + 1, x, y, W, H, lambda);
+                            const float dcv = tile[c][ly + 1][lx + 1];
+                            dnew[c * N + o] = dcv;
+                            acc[c] += dcv * qv;
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            block_partials_f(acc, 3, partA, G);
+        }
+        if (!grid_sync(gb, gen)) return;
+        // every problem wrote done[] before this barrier: leave together once all have stopped
+        if (threadIdx.x == 0) {
+            int all = 1;
+            for (int q = 0; q < nprob; ++q) all &= __ldcg(done + q);
+            s_all = all;
+        }
+        __syncthreads();
+        if (s_all) break;
+        if (!idle) reduce_own(partA, 3);
+        if (threadIdx.x == 0 && !idle) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const double alpha_d = (sh[c] > 0) ? delta[c] / sh[c] : 0.0;
+                s_coef[c] = (float)alpha_d;
+                E -= 0.5 * alpha_d * delta[c];
+            }
+        }
+        __syncthreads();
+        const float alpha[3] = {s_coef[0], s_coef[1], s_coef[2]};
+        // ---- phase B
+        {
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            if (!idle) {
+                for (int t = lb; t < ntiles; t += P.nb) {
+                    const int x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
+                    for (int k = threadIdx.x; k < 3 * kHaloY * kHaloX; k += blockDim.x) {
+                        const int c = k / (kHaloY * kHaloX), rem = k % (kHaloY * kHaloX);
+                        const int gx = x0 - 1 + rem % kHaloX, gy = y0 - 1 + rem / kHaloX;
+                        tile[c][rem / kHaloX][rem % kHaloX] =
+                            (gx >= 0 && gx < W && gy >= 0 && gy < H) ? __ldcg(dnew + c * N + (size_t)gy * W + gx) : 0.f;
+                    }
+                    __syncthreads();
+                    for (int p = threadIdx.x; p < kTileX * kTileY; p += blockDim.x) {
+                        const int lx = p % kTileX, ly = p / kTileX, x = x0 + lx, y = y0 + ly;
+                        if (x >= W || y >= H) continue;
+                        const size_t o = (size_t)y * W + x;
+#pragma unroll
+                        for (int c = 0; c < 3; ++c) {
+                            const float qv = tile_op(tile[c], lx + 1, ly + 1, x, y, W, H, lambda);
+                            const float dv = tile[c][ly + 1][lx + 1];
+                            U[c * N + o] = __ldcg(U + c * N + o) + alpha[c] * dv;
+                            const float rv = __ldcg(r + c * N + o) - alpha[c] * qv;
+                            r[c * N + o] = rv;
+                            acc[c] += rv * rv;
+                        }
+                    }
+                    __syncthreads();
+                }
+            }
+            block_partials_f(acc, 3, partB, G);
+        }
+        if (!grid_sync(gb, gen)) return;
+        if (!idle) {
+            reduce_own(partB, 3);
+            if (threadIdx.x == 0) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    s_coef[c] = (delta[c] > 0) ? (float)(sh[c] / delta[c]) : 0.f;
+                    delta[c] = sh[c];
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int c = 0; c < 3; ++c) beta[c] = s_coef[c];
+            dold = dnew;
+            dnew = (dnew == P.dA) ? P.dB : P.dA;
+        }
+    }
+    if (lb == 0 && threadIdx.x == 0) {
+        P.state[0] = delta[0];
+        P.state[1] = delta[1];
+        P.state[2] = delta[2];
+        P.state[3] = E;
+        P.state[4] = gap;
+        P.state[5] = (double)(stopped_at >= 0 ? stopped_at : it);
+    }
+}
+
 // Hole filling for at most kSmallHoles holes, in one block and in shared memory. The visible pixels never change,
 // so every hole keeps, per direction (left, up, right, down: the summation order of compute_laplacian), either
 // the index of the neighbouring hole or the neighbour's fixed value; the iterations then touch shared memory
@@ -932,6 +1138,16 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
                     &maps[2], &maps[3], &maps[4]};
     lc.add(1);
     return cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(kPersistThreads), args, smem, st);
+}
+
+int cg_batch_resident_blocks() { return coop_blocks((const void *)k_cg_batch, 1 << 30); }
+
+cudaError_t launch_cg_batch(const CgProblem *d_probs, const int *d_block_prob, int nprob, int blocks, double *partA,
+                            double *partB, int *done, GridBarrier gb, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "cg_batch", st);
+    void *args[] = {(void *)&d_probs, (void *)&d_block_prob, &nprob, &partA, &partB, &done, &gb};
+    lc.add(1);
+    return cudaLaunchCooperativeKernel((const void *)k_cg_batch, dim3(blocks), dim3(kPersistThreads), args, 0, st);
 }
 
 bool encode_tensor_map_3d(CUtensorMap *map, const float *base, int cols, int rows, int planes, int box_x, int box_y,

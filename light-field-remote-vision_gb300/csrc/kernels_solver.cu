@@ -717,7 +717,7 @@ __device__ __forceinline__ void rof_project(float p[6], float r) {
 // place, then the primal in place), and writes back its kRofTX x kRofTY tile, whose values depend only on
 // the region (the halo absorbs one pixel of staleness per iteration from each side). Super-steps read one
 // global (U, P) pair and write the other, with a bounded grid barrier between them.
-constexpr int kRofTX = 32, kRofTY = 16, kRofK = 4, kRofThreads = 256;
+constexpr int kRofTX = 32, kRofTY = 16, kRofK = 4, kRofThreads = 1024;
 constexpr int kRofRX = kRofTX + 2 * kRofK, kRofRY = kRofTY + 2 * kRofK, kRofRN = kRofRX * kRofRY;
 constexpr size_t kRofSmem = (size_t)13 * kRofRN * sizeof(float);  // U 3, P 6, F 3, g 1 planes
 

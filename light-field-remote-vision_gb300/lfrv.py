@@ -64,6 +64,13 @@ class SceneParams(C.Structure):
                 ("focal_per_256", C.c_double), ("seed", C.c_uint64)]
 
 
+class ViewJob(C.Structure):
+    """lfrv_view_job: one target of a batch (device buffers, host cameras)."""
+    _fields_ = [("cfg", C.POINTER(Config)), ("algorithm", C.c_int), ("d_views", C.c_void_p), ("d_depth", C.c_void_p),
+                ("cams", C.POINTER(Camera)), ("target", C.POINTER(Camera)), ("d_out", C.c_void_p),
+                ("stats", C.POINTER(Stats))]
+
+
 _F = C.POINTER(C.c_float)
 _U8 = C.POINTER(C.c_uint8)
 _D = C.POINTER(C.c_double)
@@ -89,7 +96,8 @@ EXPORTED = [
     "lfrv_config_get_string", "lfrv_config_get_int", "lfrv_ctx_create", "lfrv_ctx_destroy", "lfrv_ctx_set_stream",
     "lfrv_ctx_launch_count", "lfrv_ctx_profile", "lfrv_ctx_profile_read", "lfrv_depth_radial_to_ortho",
     "lfrv_depth_radial_to_ortho_dev", "lfrv_warp_from_depth", "lfrv_warp_from_depth_dev", "lfrv_warp", "lfrv_warp_dev", "lfrv_ibr_color", "lfrv_ibr_color_dev",
-    "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_stage_weights",
+    "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_render_views_dev",
+    "lfrv_stage_weights",
     "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
     "lfrv_stage_u_gradient", "lfrv_stage_cg", "lfrv_cg_solve_static", "lfrv_pfm_read", "lfrv_pfm_write", "lfrv_png_read", "lfrv_png_write",
@@ -351,6 +359,23 @@ class Context:
                                         cameras_array(cams), C.byref(target), C.c_void_p(d_out), C.byref(st)))
         return st
 
+    def render_views_dev(self, jobs) -> list:
+        """Batched targets: jobs is a list of dicts with cfg, algorithm, d_views, d_depth, cams, target, d_out
+        (device pointers as ints). Returns one Stats per job."""
+        arr = (ViewJob * len(jobs))()
+        keep = []
+        stats = [Stats() for _ in jobs]
+        for i, j in enumerate(jobs):
+            cams = cameras_array(j["cams"])
+            tgt = Camera()
+            C.pointer(tgt)[0] = j["target"]
+            keep += [cams, tgt, j["cfg"]]
+            arr[i] = ViewJob(C.pointer(j["cfg"]), int(j["algorithm"]), C.c_void_p(j["d_views"]), C.c_void_p(j["d_depth"]),
+                             C.cast(cams, C.POINTER(Camera)), C.pointer(tgt), C.c_void_p(j["d_out"]),
+                             C.pointer(stats[i]))
+        _check(LIB.lfrv_render_views_dev(self._h, arr, len(jobs)))
+        return stats
+
     def render_view(self, cfg: Config, algorithm: int, views, depth, cams, target: Camera, out=None):
         """Host-buffer pipeline (copies inside the call). views/depth/out may be numpy arrays or host pointers."""
         st = Stats()
@@ -493,6 +518,7 @@ def _declare() -> None:
                                              C.POINTER(Camera), C.c_int, vp]
     LIB.lfrv_depth_radial_to_ortho.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(Camera), _F]
     LIB.lfrv_depth_radial_to_ortho_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(Camera), vp]
+    LIB.lfrv_render_views_dev.argtypes = [vp, C.POINTER(ViewJob), C.c_int]
     LIB.lfrv_cg_solve_static.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp, _I, _D]
     LIB.lfrv_png_read.argtypes = [C.c_char_p, _I, _I, _F, C.c_size_t]
     LIB.lfrv_png_write.argtypes = [C.c_char_p, C.c_int, C.c_int, _F]
