@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -39,6 +40,8 @@ struct Workspace {
     DevBuf ukey;
     // batched targets: per-job buffers and the launch descriptors
     DevBuf batch, batch_meta;
+    // scratch state of the autotuner's trial launches
+    DevBuf tune;
     // CG
     DevBuf r, d, q, U0, holes, hole_count;
     // reductions and persistent-solver state
@@ -85,6 +88,7 @@ struct lfrv_ctx {
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t up_start = nullptr, up_depth[4] = {}, up_views = nullptr;
     lfrv::Pending pending;
+    std::map<long long, int> rof_tuned;  // autotuned persistent-ROF variant per image size (W << 32 | H)
     lfrv::KernelProfiler prof;
     bool profiling = false;
     int device = 0;

@@ -271,6 +271,50 @@ static void residual(lfrv_ctx *c, const Geometry &G, const float *U, const float
     reduce_to(c, np, part, slot);
 }
 
+// ------------------------------------------------------------------ autotuner
+// Picks the persistent-ROF instantiation (iterations per super-step, block size) for a W x H image: each candidate
+// runs 16 iterations on a scratch copy of the state (U, P, F, g), timed with CUDA events on the context stream;
+// the fastest is cached per image size in the context. The solver's own buffers are not touched.
+static int rof_autotune(lfrv_ctx *c, int W, int H, float tau, float sigma, float lam, const float *U, const float *P,
+                        const float *F, const float *g) {
+    const long long key = ((long long)W << 32) | (unsigned)H;
+    auto it = c->rof_tuned.find(key);
+    if (it != c->rof_tuned.end()) return it->second;
+    const size_t N = (size_t)W * H;
+    c->ws.tune.ensure(sizeof(float) * 18 * N);
+    float *U0 = c->ws.tune.as<float>(), *U1 = U0 + 3 * N, *P0 = U1 + 3 * N, *P1 = P0 + 6 * N;
+    cudaStream_t s = c->stream;
+    cudaEvent_t e0, e1;
+    LFRV_CUDA(cudaEventCreate(&e0));
+    LFRV_CUDA(cudaEventCreate(&e1));
+    int best = rof_default_variant();
+    float best_ms = 1e30f;
+    LaunchCounter quiet;  // trial launches are not the caller's kernels
+    for (int v = 0; v < rof_variant_count(); ++v) {
+        LFRV_CUDA(cudaMemcpyAsync(U0, U, sizeof(float) * 3 * N, cudaMemcpyDeviceToDevice, s));
+        LFRV_CUDA(cudaMemcpyAsync(P0, P, sizeof(float) * 6 * N, cudaMemcpyDeviceToDevice, s));
+        const GridBarrier gb = fresh_barrier(c);
+        LFRV_CUDA(cudaEventRecord(e0, s));
+        const cudaError_t e = launch_rof_persistent(W, H, 16, tau, sigma, lam, U0, P0, U1, P1, F, g, gb, v, s, quiet);
+        LFRV_CUDA(cudaEventRecord(e1, s));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            continue;  // a variant that cannot launch here (occupancy) is skipped
+        }
+        LFRV_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        LFRV_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->rof_tuned[key] = best;
+    return best;
+}
+
 // ------------------------------------------------------------------ gradient data term (dt_beta)
 // Buffers of the gradient data term (vtv_sr_dataterm_gradients, sources/optimization.cu:1969-2116) and of the
 // gradient term of the energy (:1610-1700); empty when dt_beta == 0.
@@ -439,11 +483,13 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
             // niter inner ROF iterations from Uq = U in one persistent launch over (Ua, P) <-> (Ub, Pa);
             // U itself stays the previous iterate (the moving-pixel test compares against it)
             LFRV_CUDA(cudaMemcpyAsync(ws.Ua.p, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+            const int rv = rof_autotune(c, G.W, G.H, tau_pd, sigma_pd, lam_prox, ws.Ua.as<float>(), ws.P.as<float>(),
+                                        b.F, b.g);
             const GridBarrier gb = fresh_barrier(c);
             LFRV_CUDA(launch_rof_persistent(G.W, G.H, cfg.niter, tau_pd, sigma_pd, lam_prox, ws.Ua.as<float>(),
-                                            ws.P.as<float>(), ws.Ub.as<float>(), ws.Pa.as<float>(), b.F, b.g, gb, s,
+                                            ws.P.as<float>(), ws.Ub.as<float>(), ws.Pa.as<float>(), b.F, b.g, gb, rv, s,
                                             c->launches));
-            const bool odd = (rof_persistent_steps(cfg.niter) & 1) != 0;
+            const bool odd = (rof_persistent_steps(cfg.niter, rv) & 1) != 0;
             const float *Ucur = odd ? ws.Ub.as<float>() : ws.Ua.as<float>();
             if (odd) swap_buf(ws.P, ws.Pa);
             int nM = 0;
@@ -1494,11 +1540,13 @@ extern "C" int lfrv_stage_rof(lfrv_ctx *ctx, int W, int H, int niter, float tau,
     ws.Ua.ensure(3 * N * sizeof(float));
     ws.Pa.ensure(6 * N * sizeof(float));
     ctx->pending = Pending{};
+    const int rv = rof_autotune(ctx, W, H, tau, sigma, lambda, ws.U.as<float>(), ws.P.as<float>(), ws.F.as<float>(),
+                                ws.g.as<float>());
     const GridBarrier gb = fresh_barrier(ctx);
     LFRV_CUDA(launch_rof_persistent(W, H, niter, tau, sigma, lambda, ws.U.as<float>(), ws.P.as<float>(),
-                                    ws.Ua.as<float>(), ws.Pa.as<float>(), ws.F.as<float>(), ws.g.as<float>(), gb,
+                                    ws.Ua.as<float>(), ws.Pa.as<float>(), ws.F.as<float>(), ws.g.as<float>(), gb, rv,
                                     ctx->stream, ctx->launches));
-    const bool odd = (rof_persistent_steps(niter) & 1) != 0;
+    const bool odd = (rof_persistent_steps(niter, rv) & 1) != 0;
     io.down(U, odd ? ws.Ua.as<float>() : ws.U.as<float>(), 3 * N);
     io.down(P, odd ? ws.Pa.as<float>() : ws.P.as<float>(), 6 * N);
     sync(ctx);

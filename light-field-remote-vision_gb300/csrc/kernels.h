@@ -166,10 +166,14 @@ int cg_batch_resident_blocks();
 cudaError_t launch_cg_batch(const CgProblem *d_probs, const int *d_block_prob, int nprob, int blocks, double *partA,
                             double *partB, int *done, GridBarrier gb, cudaStream_t st, LaunchCounter &lc);
 
-int rof_persistent_steps(int niter);
+// Persistent ROF instantiations (iterations per super-step x block size), chosen per image size by the host's
+// autotuner; v indexes them.
+int rof_variant_count();
+int rof_default_variant();
+int rof_persistent_steps(int niter, int v);
 cudaError_t launch_rof_persistent(int W, int H, int niter, float tau, float sigma, float lam, float *U0, float *P0,
-                                  float *U1, float *P1, const float *F, const float *g, GridBarrier gb, cudaStream_t st,
-                                  LaunchCounter &lc);
+                                  float *U1, float *P1, const float *F, const float *g, GridBarrier gb, int v,
+                                  cudaStream_t st, LaunchCounter &lc);
 cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
                                  float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
                                  double *state, cudaStream_t st, LaunchCounter &lc);

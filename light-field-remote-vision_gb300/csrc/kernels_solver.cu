@@ -717,14 +717,20 @@ __device__ __forceinline__ void rof_project(float p[6], float r) {
 // place, then the primal in place), and writes back its kRofTX x kRofTY tile, whose values depend only on
 // the region (the halo absorbs one pixel of staleness per iteration from each side). Super-steps read one
 // global (U, P) pair and write the other, with a bounded grid barrier between them.
-constexpr int kRofTX = 32, kRofTY = 16, kRofK = 4, kRofThreads = 1024;
-constexpr int kRofRX = kRofTX + 2 * kRofK, kRofRY = kRofTY + 2 * kRofK, kRofRN = kRofRX * kRofRY;
-constexpr size_t kRofSmem = (size_t)13 * kRofRN * sizeof(float);  // U 3, P 6, F 3, g 1 planes
+// K (iterations per super-step) and the block size are template parameters; the host picks an instantiation
+// per image size with a timing autotuner (rof_autotune).
+constexpr int kRofTX = 32, kRofTY = 16;
+template <int K>
+constexpr size_t rof_smem() {
+    return (size_t)13 * (kRofTX + 2 * K) * (kRofTY + 2 * K) * sizeof(float);  // U 3, P 6, F 3, g 1 planes
+}
 
+template <int kRofK, int kRofThreads>
 __global__ void __launch_bounds__(kRofThreads) k_rof_persistent(int W, int H, int niter, float tau, float sigma,
                                                                 float lam, float *U0, float *P0, float *U1,
                                                                 float *P1, const float *__restrict__ F,
                                                                 const float *__restrict__ g, GridBarrier gb) {
+    constexpr int kRofRX = kRofTX + 2 * kRofK, kRofRY = kRofTY + 2 * kRofK, kRofRN = kRofRX * kRofRY;
     extern __shared__ float sm[];
     float *sU = sm, *sP = sm + 3 * kRofRN, *sF = sm + 9 * kRofRN, *sG = sm + 12 * kRofRN;
     const int tiles_x = (W + kRofTX - 1) / kRofTX, ntiles = tiles_x * ((H + kRofTY - 1) / kRofTY);
@@ -1180,27 +1186,43 @@ void launch_sobel(int W, int H, int count, const float *rgb, size_t in_stride, s
 }
 int sobel_partials(int W, int H) { return ((W + 31) / 32) * ((H + 7) / 8); }
 
-// Number of super-steps of k_rof_persistent for niter iterations: the result is in (U1, P1) when it is odd.
-int rof_persistent_steps(int niter) { return (niter + kRofK - 1) / kRofK; }
+// Instantiations the autotuner chooses from: (iterations per super-step, threads per block).
+struct RofVariant {
+    int K, threads;
+    const void *kernel;
+    size_t smem;
+};
+static const RofVariant kRofVariants[] = {
+    {2, 512, (const void *)k_rof_persistent<2, 512>, rof_smem<2>()},
+    {2, 1024, (const void *)k_rof_persistent<2, 1024>, rof_smem<2>()},
+    {4, 512, (const void *)k_rof_persistent<4, 512>, rof_smem<4>()},
+    {4, 1024, (const void *)k_rof_persistent<4, 1024>, rof_smem<4>()},
+    {8, 1024, (const void *)k_rof_persistent<8, 1024>, rof_smem<8>()},
+};
+int rof_variant_count() { return (int)(sizeof(kRofVariants) / sizeof(kRofVariants[0])); }
+int rof_default_variant() { return 3; }
+
+// Number of super-steps of variant v for niter iterations: the result is in (U1, P1) when it is odd.
+int rof_persistent_steps(int niter, int v) { return (niter + kRofVariants[v].K - 1) / kRofVariants[v].K; }
 
 cudaError_t launch_rof_persistent(int W, int H, int niter, float tau, float sigma, float lam, float *U0, float *P0,
-                                  float *U1, float *P1, const float *F, const float *g, GridBarrier gb, cudaStream_t st,
-                                  LaunchCounter &lc) {
+                                  float *U1, float *P1, const float *F, const float *g, GridBarrier gb, int v,
+                                  cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "rof_persistent", st);
-    cudaError_t e = cudaFuncSetAttribute(k_rof_persistent, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kRofSmem);
+    const RofVariant &R = kRofVariants[v];
+    cudaError_t e = cudaFuncSetAttribute(R.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)R.smem);
     if (e != cudaSuccess) return e;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_rof_persistent, kRofThreads, kRofSmem);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, R.kernel, R.threads, R.smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const int ntiles = ((W + kRofTX - 1) / kRofTX) * ((H + kRofTY - 1) / kRofTY);
     const int blocks = std::min(ntiles, sms * per_sm);
     void *args[] = {&W, &H, &niter, &tau, &sigma, &lam, &U0, &P0, &U1, &P1, (void *)&F, (void *)&g, &gb};
     lc.add(1);
-    return cudaLaunchCooperativeKernel((const void *)k_rof_persistent, dim3(blocks), dim3(kRofThreads), args, kRofSmem,
-                                       st);
+    return cudaLaunchCooperativeKernel(R.kernel, dim3(blocks), dim3(R.threads), args, R.smem, st);
 }
 
 void launch_moving(size_t N, const float *A, const float *B, float thr, double *partial, cudaStream_t st,
