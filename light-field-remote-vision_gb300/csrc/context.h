@@ -96,4 +96,8 @@ struct lfrv_ctx {
     lfrv::LaunchCounter launches;
     lfrv::Workspace ws;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // helper contexts (own stream and workspace) that prepare batched targets concurrently; created on first use
+    std::vector<lfrv_ctx *> lanes;
+    std::vector<cudaEvent_t> lane_done;
+    bool owns_stream = false;
 };

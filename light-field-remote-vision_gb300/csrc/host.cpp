@@ -937,6 +937,13 @@ extern "C" int lfrv_ctx_destroy(lfrv_ctx *ctx) {
     else cudaDeviceSynchronize();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    for (lfrv_ctx *l : ctx->lanes) {
+        cudaStreamSynchronize(l->stream);
+        cudaStreamDestroy(l->stream);
+        l->prof.destroy();
+        delete l;
+    }
+    for (cudaEvent_t e : ctx->lane_done) cudaEventDestroy(e);
     if (ctx->copy_stream) {
         cudaStreamSynchronize(ctx->copy_stream);
         cudaStreamDestroy(ctx->copy_stream);
@@ -1257,25 +1264,61 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
     ws.batch.ensure(sizeof(float) * std::max<size_t>(pool, 16));
     float *base = ws.batch.as<float>();
     c->pending = Pending{};
-    // every job's warp stage; gradient jobs stop before the CG, the others run to the end
+    // the batched jobs' warp stage, set-up and hole filling run on kLanes helper contexts (own stream and
+    // workspace each, round robin), so small targets overlap; the context stream waits for all of them
+    constexpr int kLanes = 4;
+    while ((int)c->lanes.size() < kLanes) {
+        lfrv_ctx *l = new lfrv_ctx;
+        l->device = c->device;
+        LFRV_CUDA(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking));
+        l->owns_stream = true;
+        c->lanes.push_back(l);
+        cudaEvent_t e;
+        LFRV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->lane_done.push_back(e);
+    }
+    LFRV_CUDA(cudaEventRecord(c->ev0, s));  // lanes start after what the caller queued on the context stream
+    for (int k = 0; k < kLanes; ++k) {
+        lfrv_ctx *l = c->lanes[k];
+        l->launches.n = 0;
+        l->launches.prof = nullptr;  // the profiler folds events per stream; lane kernels are counted, not timed
+        l->pending = Pending{};
+        LFRV_CUDA(cudaStreamWaitEvent(l->stream, c->ev0, 0));
+    }
+    for (size_t q = 0; q < batched.size(); ++q) {
+        const Slot &sl = batched[q];
+        const lfrv_view_job &J = jobs[sl.job];
+        lfrv_ctx *l = c->lanes[q % kLanes];
+        const Geometry &G = sl.G;
+        Workspace &lw = l->ws;
+        lw.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+        lw.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+        warp(l, G.V, G.w, G.h, J.d_depth, J.cams, J.target, nullptr, nullptr, lw.tau.as<float>(), lw.dp.as<float>(),
+             nullptr);
+        float *U = base + sl.off;
+        gradient_prepare(l, *J.cfg, G, J.d_views, lw.tau.as<float>(), lw.dp.as<float>(), nullptr, U, U + 3 * G.N,
+                         U + 4 * G.N);
+        // keep this job's hole-fill iteration count (state slot 8) beside its CG state
+        double *st = reinterpret_cast<double *>(U + 14 * G.N);
+        LFRV_CUDA(cudaMemcpyAsync(st + 6, lw.state.as<double>() + 8, sizeof(double), cudaMemcpyDeviceToDevice,
+                                  l->stream));
+    }
+    for (int k = 0; k < kLanes; ++k) {
+        LFRV_CUDA(cudaEventRecord(c->lane_done[k], c->lanes[k]->stream));
+        LFRV_CUDA(cudaStreamWaitEvent(s, c->lane_done[k], 0));
+    }
+    // the other jobs, one after another on the context stream
     for (int j = 0; j < count; ++j) {
         const lfrv_view_job &J = jobs[j];
         const Geometry G = geometry(*J.cfg);
+        bool is_batched = false;
+        for (const Slot &b : batched) is_batched = is_batched || b.job == j;
+        if (is_batched) continue;
         ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
         ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
         warp(c, G.V, G.w, G.h, J.d_depth, J.cams, J.target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(),
              nullptr);
-        const Slot *sl = nullptr;
-        for (const Slot &b : batched)
-            if (b.job == j) sl = &b;
-        if (sl) {
-            float *U = base + sl->off;
-            gradient_prepare(c, *J.cfg, G, J.d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, U, U + 3 * G.N,
-                             U + 4 * G.N);
-            // keep this job's hole-fill iteration count (state slot 8) beside its CG state
-            double *st = reinterpret_cast<double *>(U + 14 * G.N);
-            LFRV_CUDA(cudaMemcpyAsync(st + 6, ws.state.as<double>() + 8, sizeof(double), cudaMemcpyDeviceToDevice, s));
-        } else {
+        {
             // a job outside the batched CG: report what is pending first, then run it to the end and collect its
             // statistics and barrier status before the next job reuses the state slots
             sync(c);
@@ -1357,6 +1400,10 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
         LFRV_CUDA(cudaMemcpyAsync(jobs[sl.job].d_out, base + sl.off, sizeof(float) * 3 * sl.G.N,
                                   cudaMemcpyDeviceToDevice, s));
     sync(c);
+    for (lfrv_ctx *l : c->lanes) {
+        c->launches.add((int)l->launches.n);
+        finish_stats(l);  // the lanes' barrier status (hole filling)
+    }
     for (const Slot &sl : batched) {
         lfrv_stats *st = jobs[sl.job].stats;
         if (!st) continue;
