@@ -228,6 +228,55 @@ typedef struct lfrv_view_job {
 } lfrv_view_job;
 int lfrv_render_views_dev(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count);
 
+/* ---------------------------------------------------------------- learned warm start
+ * No reference counterpart: an addition beside the plain method, which stays unchanged. A 4-scale
+ * encoder-decoder convolutional network (~1.23 M parameters, BF16 weights and activations, FP32 accumulation
+ * on the tensor cores, FP32 master weights and Adam state) predicts the converged IBR_gradient solution from
+ * LFRV_WARMSTART_CHANNELS per-pixel inputs; the prediction only seeds the CG iterate of the corrected solver
+ * (faithful = 0). The anchor u0 of the normal equations (lambda I - Delta) u = lambda u0 + grad^T g
+ * (sources/solver.cu:526-699) stays the hole-filled weighted average, so the solution, the energy and the
+ * certified-gap stop are those of the plain solver: a poor prediction costs iterations, never accuracy.
+ * Targets (H, W) must be multiples of 8.
+ *
+ * Input channels (NHWC BF16, per target pixel): [0..2] u0, [3..5] gx, [6..8] gy (zero in the last column /
+ * row, clamped to [-1, 1]), [9] visibility,
+ * [10 + 3v .. 12 + 3v] view v splatted alone, [34 + v] view v's share of the splat weight (views v < 8),
+ * [42..44] the CG's initial residual at u0 (grad^T g + Delta u0, clamped to [-4, 4]), [45..47] zero. Parameters (lfrv_warmstart_get_params): flat FP32, per layer W[cout][ky][kx][cin] then
+ * bias[cout], layers in the order of the network description in learn.cpp. */
+#define LFRV_WARMSTART_CHANNELS 48
+typedef struct lfrv_warmstart lfrv_warmstart;
+long long lfrv_warmstart_param_count(void);
+int lfrv_warmstart_create(lfrv_ctx *ctx, unsigned long long seed, lfrv_warmstart **net);
+void lfrv_warmstart_destroy(lfrv_warmstart *net);
+int lfrv_warmstart_get_params(lfrv_warmstart *net, float *params);
+int lfrv_warmstart_set_params(lfrv_warmstart *net, const float *params);  /* also resets the Adam state */
+/* Training data of one target: the network input (H x W x 48 BF16), the anchor u0 (3 x H x W) and, when
+ * d_solution is not NULL, the plain solver's solution from u0 to cfg->cg_gap_tol (3 x H x W). */
+int lfrv_warmstart_features_dev(lfrv_ctx *ctx, const lfrv_config *cfg, const float *d_views,
+                                const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target,
+                                void *d_input, float *d_u0, float *d_solution, lfrv_stats *stats);
+/* Batched tensors: input batch x H x W x 48 (BF16), u0 / target / prediction batch x 3 x H x W (FP32). */
+int lfrv_warmstart_forward_dev(lfrv_warmstart *net, int batch, int H, int W, const void *d_input,
+                               const float *d_u0, float *d_pred);
+/* One Adam step (beta 0.9 / 0.999, eps 1e-8) on the mean squared error of u0 + net(input) against target;
+ * *loss = the loss before the step. */
+int lfrv_warmstart_train_step_dev(lfrv_warmstart *net, int batch, int H, int W, const void *d_input,
+                                  const float *d_u0, const float *d_target, float lr, double *loss);
+/* Loss and its gradient with respect to every parameter (host, lfrv_warmstart_param_count floats), no update. */
+int lfrv_warmstart_gradients_dev(lfrv_warmstart *net, int batch, int H, int W, const void *d_input,
+                                 const float *d_u0, const float *d_target, double *loss, float *grads);
+/* IBR_gradient of one target (as lfrv_render_view_dev with algorithm 1) with the CG seeded by the network. */
+int lfrv_render_view_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_config *cfg,
+                              const float *d_views, const float *d_depth, const lfrv_camera *cams,
+                              const lfrv_camera *target, float *d_out, lfrv_stats *stats);
+/* One convolution through the tensor-core kernels: x NHWC BF16 (batch x H x W x Cin), dy NHWC BF16
+ * (batch x H/stride x W/stride x Cout), w FP32 Cout x ks x ks x Cin (rounded to BF16 inside), out FP32.
+ * mode 0: out = conv(x) (batch x H/s x W/s x Cout); 1: out = the data gradient (batch x H x W x Cin);
+ * 2: out = the weight gradient (Cout x ks x ks x Cin). ks 1 or 3 (padding 1), stride 1 or 2, Cin a multiple of
+ * 8, Cout (and Cin for mode 1) one of 16, 32, 64, 128, 256. */
+int lfrv_conv_bf16_dev(lfrv_ctx *ctx, int mode, int batch, int H, int W, int Cin, int Cout, int ks, int stride,
+                       const void *d_x, const void *d_dy, const float *d_w, float *d_out);
+
 /* ---------------------------------------------------------------- stage calls
  * Fine-grained entry points mirroring the cocolib stage functions, used by the parity tests.
  * All take host buffers. "views/tau/dpart" as above; U, G etc. are 3 x H x W.

@@ -32,8 +32,8 @@ ORACLE_LIB = ROOT / "oracle" / "liblfrv_oracle.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-std=c++17", "-O3", "-lineinfo", f"-I{INCLUDE}", f"-I{CSRC}",
                "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp"]
-LIB_SOURCES = ["errors.cpp", "io.cpp", "png.cpp", "synth.cpp", "host.cpp",
-               "kernels_solver.cu", "kernels_warp.cu", "kernels_pushpull.cu", "kernels_cg.cu"]
+LIB_SOURCES = ["errors.cpp", "io.cpp", "png.cpp", "synth.cpp", "host.cpp", "learn.cpp",
+               "kernels_solver.cu", "kernels_warp.cu", "kernels_pushpull.cu", "kernels_cg.cu", "kernels_learn.cu"]
 
 
 def _have_zlib() -> bool:

@@ -42,6 +42,8 @@ struct Workspace {
     DevBuf batch, batch_meta;
     // scratch state of the autotuner's trial launches
     DevBuf tune;
+    // learned warm start: network input (NHWC BF16) and the seeded CG iterate
+    DevBuf learn_in, seed;
     // CG
     DevBuf r, d, q, U0, holes, hole_count;
     // reductions and persistent-solver state

@@ -648,7 +648,7 @@ static int cg_faithful(lfrv_ctx *c, int W, int H, const float *gx, const float *
 
 // Corrected CG: one persistent launch (FP32 iterates, FP64 dot products, certified-gap stop on the device).
 static void cg_persistent_async(lfrv_ctx *c, int W, int H, int max_iter, double gap_tol, const float *gx,
-                                const float *gy, float *U) {
+                                const float *gy, float *U, const float *U0 = nullptr) {
     Workspace &ws = c->ws;
     const size_t N = (size_t)W * H;
     ws.r.ensure(3 * N * sizeof(float));
@@ -658,14 +658,16 @@ static void cg_persistent_async(lfrv_ctx *c, int W, int H, int max_iter, double 
     double *part = partial_buf(c, 8 * np);
     const GridBarrier gb = fresh_barrier(c);
     LFRV_CUDA(launch_cg_persistent(W, H, gx, gy, U, ws.r.as<float>(), ws.d.as<float>(), ws.q.as<float>(), part,
-                                   part + 4 * np, gb, max_iter, gap_tol, solver_state(c), c->stream, c->launches));
+                                   part + 4 * np, gb, max_iter, gap_tol, solver_state(c), c->stream, c->launches,
+                                   U0));
     c->pending.cg = true;
 }
 
 // IBR_gradient up to the CG (sources/gradientIBR.cpp:12-120): weights, the set-up pass (visibility, weighted
 // average, gradient splat) into U, gx, gy, then hole filling of U (or U = init).
 static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry &G, const float *img,
-                             const float *tau2, const float *dp2, const float *init, float *U, float *gx, float *gy) {
+                             const float *tau2, const float *dp2, const float *init, float *U, float *gx, float *gy,
+                             void *learn_in = nullptr) {
     const size_t N = G.N;
     cudaStream_t s = c->stream;
     Workspace &ws = c->ws;
@@ -683,6 +685,11 @@ static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
     check_launch("gradient set-up");
     if (init) LFRV_CUDA(cudaMemcpyAsync(U, init, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
     else hole_fill_async(c, G.W, G.H, b.vis, U, cfg.hole_fill_iter);
+    // the learned warm start's input: the set-up products and the first views splatted one at a time
+    if (learn_in) {
+        launch_learn_input(G, B, tau2, img, b.wgt, U, gx, gy, b.vis, learn_in, s, c->launches);
+        check_launch("learned input");
+    }
 }
 
 static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
@@ -1232,6 +1239,99 @@ extern "C" int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int a
     LFRV_API_END
 }
 
+// ====================================================================== learned warm start
+// Training data and warm-started solves of IBR_gradient with the corrected CG. The network sees the set-up
+// products (anchor u0, gx, gy, visibility) and the first views splatted one at a time; its prediction only seeds
+// the CG iterate, while the anchor u0 keeps the problem, its energy and the certified-gap stop unchanged.
+namespace lfrv {
+void warmstart_predict_async(lfrv_warmstart *net, int H, int W, const void *d_input, const float *d_u0, float *d_pred);
+void warmstart_check(lfrv_warmstart *net);
+}  // namespace lfrv
+
+static Geometry warm_geometry(const lfrv_config &cfg, const lfrv_camera *target) {
+    if (cfg.faithful) raise(LFRV_E_ARG, "the learned warm start seeds the corrected CG (faithful = 0)");
+    check_solver_options(cfg);
+    const Geometry G = geometry(cfg);
+    if (target->width != G.W || target->height != G.H) raise(LFRV_E_ARG, "target size mismatch");
+    if (G.W % 8 || G.H % 8 || G.W < 8 || G.H < 8)
+        raise(LFRV_E_ARG, "the learned warm start needs a target of multiples of 8 pixels (got %d x %d)", G.W, G.H);
+    return G;
+}
+
+static void warm_features(lfrv_ctx *ctx, const lfrv_config &cfg, const float *d_views, const float *d_depth,
+                          const lfrv_camera *cams, const lfrv_camera *target, void *d_input, float *d_u0,
+                          float *d_solution, lfrv_stats *stats) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    const Geometry G = warm_geometry(cfg, target);
+    const long long l0 = ctx->launches.n;
+    begin_timing(ctx);
+    Workspace &ws = ctx->ws;
+    ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr,
+         nullptr);
+    ColorBuffers b = color_buffers(ctx, G);
+    float *U = ws.U.as<float>();
+    ctx->pending = Pending{};
+    gradient_prepare(ctx, cfg, G, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, U, b.gx, b.gy, d_input);
+    if (d_u0) LFRV_CUDA(cudaMemcpyAsync(d_u0, U, 3 * G.N * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    if (d_solution) {
+        cg_persistent_async(ctx, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U);
+        LFRV_CUDA(cudaMemcpyAsync(d_solution, U, 3 * G.N * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    ctx->pending.stats = stats;
+    ctx->pending.gap_tol = cfg.cg_gap_tol;
+    end_timing(ctx, stats, l0);
+}
+
+static void render_view_warm(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_config &cfg, const float *d_views,
+                             const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target, float *d_out,
+                             lfrv_stats *stats) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    const Geometry G = warm_geometry(cfg, target);
+    const long long l0 = ctx->launches.n;
+    begin_timing(ctx);
+    Workspace &ws = ctx->ws;
+    ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+    ws.learn_in.ensure(G.N * kLearnChannels * 2);
+    ws.seed.ensure(3 * G.N * sizeof(float));
+    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr,
+         nullptr);
+    ColorBuffers b = color_buffers(ctx, G);
+    float *U = ws.U.as<float>(), *X = ws.seed.as<float>();
+    ctx->pending = Pending{};
+    gradient_prepare(ctx, cfg, G, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, U, b.gx, b.gy,
+                     ws.learn_in.p);
+    warmstart_predict_async(net, G.H, G.W, ws.learn_in.p, U, X);
+    cg_persistent_async(ctx, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, X, U);
+    LFRV_CUDA(cudaMemcpyAsync(d_out, X, 3 * G.N * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->pending.stats = stats;
+    ctx->pending.gap_tol = cfg.cg_gap_tol;
+    end_timing(ctx, stats, l0);
+    warmstart_check(net);
+}
+
+extern "C" int lfrv_warmstart_features_dev(lfrv_ctx *ctx, const lfrv_config *cfg, const float *d_views,
+                                           const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target,
+                                           void *d_input, float *d_u0, float *d_solution, lfrv_stats *stats) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!cfg || !d_views || !d_depth || !cams || !target || !d_input) return fail(LFRV_E_ARG, "null argument");
+    warm_features(ctx, *cfg, d_views, d_depth, cams, target, d_input, d_u0, d_solution, stats);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_render_view_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_config *cfg,
+                                         const float *d_views, const float *d_depth, const lfrv_camera *cams,
+                                         const lfrv_camera *target, float *d_out, lfrv_stats *stats) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!net || !cfg || !d_views || !d_depth || !cams || !target || !d_out) return fail(LFRV_E_ARG, "null argument");
+    render_view_warm(ctx, net, *cfg, d_views, d_depth, cams, target, d_out, stats);
+    LFRV_API_END
+}
+
 // ====================================================================== batched targets
 // IBR_gradient jobs with the corrected CG share one k_cg_batch launch (per launch at most as many jobs as resident
 // blocks); every other job runs on its own. Per gradient job the batch pool holds U, gx, gy, r, dA, dB (14 N
@@ -1380,6 +1480,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
             P.dA = U + 8 * sl.G.N;
             P.dB = U + 11 * sl.G.N;
             P.state = reinterpret_cast<double *>(U + 14 * sl.G.N);
+            P.U0 = nullptr;
             for (int k = 0; k < nb[q]; ++k) block_prob[b0 + k] = (int)q;
             b0 += nb[q];
         }

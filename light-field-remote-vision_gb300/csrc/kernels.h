@@ -81,6 +81,12 @@ void launch_vis_any(const Geometry &G, const Buckets &B, const float *tau, uint8
                     LaunchCounter &lc);
 void launch_initial_image(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *wgt,
                           float *U, float *norm, cudaStream_t st, LaunchCounter &lc);
+// Learned warm start input (NHWC BF16, kLearnChannels per target pixel) from the IBR_gradient set-up products
+// and the first kLearnViews views splatted one at a time.
+constexpr int kLearnChannels = 48, kLearnViews = 8;
+void launch_learn_input(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *wgt,
+                        const float *U, const float *gx, const float *gy, const uint8_t *vis, void *out,
+                        cudaStream_t st, LaunchCounter &lc);
 // Gradient data term of the ISTA step (dt_beta > 0): per-view residuals resg (3 x n each) and their weights.
 struct GradTerm {
     const float *resg;  // nullptr: no gradient term
@@ -160,6 +166,7 @@ struct CgProblem {
     const float *gx, *gy;
     float *U, *r, *dA, *dB;
     double *state;
+    const float *U0;  // anchor when U holds a seed (nullptr: U is the anchor)
 };
 // Blocks of a batched launch: as many as can be resident with k_cg_batch's shape.
 int cg_batch_resident_blocks();
@@ -176,11 +183,59 @@ cudaError_t launch_rof_persistent(int W, int H, int niter, float tau, float sigm
                                   cudaStream_t st, LaunchCounter &lc);
 cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
                                  float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
-                                 double *state, cudaStream_t st, LaunchCounter &lc);
+                                 double *state, cudaStream_t st, LaunchCounter &lc, const float *U0 = nullptr);
 cudaError_t launch_hole_fill_persistent(int W, int H, const int *holes, const int *count, float *A, float *B,
                                         double *part, GridBarrier gb, int max_iter, double *state, cudaStream_t st,
                                         LaunchCounter &lc);
 void launch_cg_energy(int W, int H, const float *U, const float *U0, const float *gx, const float *gy, double *partial,
                       cudaStream_t st, LaunchCounter &lc);
+
+// ------------------------------------------------------------------ learned warm start (tcgen05 convolutions)
+// Implicit-GEMM convolution: rows are the batch x Ho x Wo pixels of the output (forward) or of the forward input
+// (dgrad); the gathered tensor src is NHWC BF16 with C channels over batch x Hs x Ws; B is the BF16 weight matrix
+// [N][ldw] (K contiguous, zero padded to ldw, a multiple of 64). Epilogue: + bias, + add, ReLU, zero where
+// mask <= 0; outputs [rows][N] in FP32 and/or BF16.
+struct ConvGemm {
+    const void *src;
+    int C, Hs, Ws;
+    int batch, Ho, Wo;
+    int ks, stride, dgrad;
+    int K;
+    const void *wt;
+    int ldw, N;
+    const float *bias;
+    int relu;
+    const void *add, *mask;
+    float *outf;
+    void *outb;
+};
+// Weight gradient of a convolution with input x (Cin channels, Hx x Wx) and output gradient dy (Cout stored
+// channels, Ho x Wo): rows (tap, ci) of dW^T padded to Mpad, the pixels split into chunks (a multiple of 64),
+// FP32 partial[split][Mpad][Cout].
+struct WgradGemm {
+    const void *x;
+    int Cin, Hx, Wx;
+    const void *dy;
+    int Cout, Ho, Wo;
+    int batch, ks, stride;
+    int Kf, Mpad, chunk;
+    float *partial;
+};
+cudaError_t launch_conv_tc(const ConvGemm &g, int *err, cudaStream_t st, LaunchCounter &lc);
+cudaError_t launch_wgrad_tc(const WgradGemm &g, int splits, int Cout_real, float *grad, int *err, cudaStream_t st,
+                            LaunchCounter &lc);
+cudaError_t launch_bias_grad(int P, int C, int Creal, const void *dy, float *partial, int blocks, float *out,
+                             cudaStream_t st, LaunchCounter &lc);
+cudaError_t launch_upsample_add_relu(int batch, int Hl, int Wl, int C, const void *t, const void *skip, void *s,
+                                     cudaStream_t st, LaunchCounter &lc);
+cudaError_t launch_down_sum(int batch, int Hl, int Wl, int C, const void *ds, void *dt, cudaStream_t st,
+                            LaunchCounter &lc);
+cudaError_t launch_output_head(int batch, int HW, int Cy, const float *y, const float *u0, const float *target,
+                               float *pred, void *dy, double *loss_partial, int blocks, cudaStream_t st,
+                               LaunchCounter &lc);
+cudaError_t launch_adam(size_t n, float *w, const float *grad, float *m, float *v, float lr_t, float b1, float b2,
+                        float eps_t, cudaStream_t st, LaunchCounter &lc);
+cudaError_t launch_pack_weights(int Cout, int Cst, int Cin, int taps, int Kpad, int Kdpad, const float *w, void *Wb,
+                                void *Wt, cudaStream_t st, LaunchCounter &lc);
 
 }  // namespace lfrv

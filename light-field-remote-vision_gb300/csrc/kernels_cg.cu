@@ -120,6 +120,51 @@ __global__ void __launch_bounds__(256) k_hole_iter(int W, int H, const int *__re
 // ------------------------------------------------------------------ conjugate gradient
 constexpr int kCgBX = 32, kCgBY = 8;
 
+// Phase 0 of the corrected CG at pixel o: the initial residual r = b - A x with b = lambda u0 + grad^T g
+// (initConjGrad, solver.cu:383-467) for the starting iterate x = U, and the energy
+// F(x) = lambda/2 |x - u0|^2 + 1/2 |grad x - g|^2 there (the loop lowers it by each step's decrease, so the
+// certified gap always refers to the current iterate). Without a separate anchor (U0 == nullptr) x = u0, as in
+// the reference; with one, U holds a seed (the learned warm start) while u0 keeps the problem unchanged.
+// acc[0..2] += r^2 per channel, acc[3] += the energy.
+__device__ __forceinline__ void cg_start_pixel(int W, int H, size_t N, size_t o, const float *__restrict__ gX,
+                                               const float *__restrict__ gY, const float *U, const float *U0,
+                                               float *r, float lambda, float acc[4]) {
+    const int x = (int)(o % W), y = (int)(o / W);
+    const float gxo = __ldg(gX + o), gyo = __ldg(gY + o);
+    const float gxl = (x > 0) ? __ldg(gX + o - 1) : 0.f, gyu = (y > 0) ? __ldg(gY + o - W) : 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float *u = U + c * N;
+        const float uc = __ldcg(u + o);
+        float lx, ly;
+        if (x == 0) lx = uc - __ldcg(u + o + 1) + gxo;
+        else if (x < W - 1) lx = 2.f * uc - __ldcg(u + o - 1) - __ldcg(u + o + 1) + gxo - gxl;
+        else lx = uc - __ldcg(u + o - 1) - gxl;
+        if (y == 0) ly = uc - __ldcg(u + o + W) + gyo;
+        else if (y < H - 1) ly = 2.f * uc - __ldcg(u + o - W) - __ldcg(u + o + W) + gyo - gyu;
+        else ly = uc - __ldcg(u + o - W) - gyu;
+        float rv = -(lx + ly);
+        float e = 0.f;
+        if (U0) {
+            const float dv = __ldcg(U0 + c * N + o) - uc;
+            rv += lambda * dv;
+            e = lambda * dv * dv;
+        }
+        r[c * N + o] = rv;
+        acc[c] += rv * rv;
+        if (x < W - 1) {
+            const float a = __ldcg(u + o + 1) - uc - gxo;
+            e += a * a;
+        }
+        if (y < H - 1) {
+            const float a = __ldcg(u + o + W) - uc - gyo;
+            e += a * a;
+        }
+        acc[3] += 0.5f * e;
+    }
+}
+
+
 __device__ __forceinline__ float cg_op(const float *d, int W, int H, int x, int y, size_t o, float lambda) {
     float lx, ly;
     if (x == 0) lx = d[o] - d[o + 1];
@@ -405,7 +450,8 @@ __device__ __forceinline__ bool block_wait_box(uint64_t *bar, unsigned parity, i
 // TMA = true reads the operator phases' tiles through the tensor maps of r, dA and dB (W a multiple of 4).
 template <bool TMA>
 __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H, const float *__restrict__ gX,
-                                                                   const float *__restrict__ gY, float *U, float *r,
+                                                                   const float *__restrict__ gY, float *U,
+                                                                   const float *U0, float *r,
                                                                    float *dA, float *dB, double *partA,
                                                                    double *partB, GridBarrier gb, int max_iter,
                                                                    double gap_tol, double *state,
@@ -460,38 +506,11 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
             if (k + 1 < nk) mbar_wait(&bars[(k + 1) & 1], par[(k + 1) & 1], kSpinLimit);
         }
     };
-    // ---- phase 0: r = b - A x (initConjGrad, solver.cu:383-467) and E(x0) = 1/2 ||grad x0 - g||^2 (x0 = u0)
+    // ---- phase 0: r = b - A x (initConjGrad, solver.cu:383-467) and the energy F(x)
     {
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
         for (size_t o = tid; o < N; o += nthr) {
-            const int x = (int)(o % W), y = (int)(o / W);
-            const float gxo = __ldg(gX + o), gyo = __ldg(gY + o);
-            const float gxl = (x > 0) ? __ldg(gX + o - 1) : 0.f, gyu = (y > 0) ? __ldg(gY + o - W) : 0.f;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float *u = U + c * N;
-                const float uc = __ldcg(u + o);
-                float lx, ly;
-                if (x == 0) lx = uc - __ldcg(u + o + 1) + gxo;
-                else if (x < W - 1) lx = 2.f * uc - __ldcg(u + o - 1) - __ldcg(u + o + 1) + gxo - gxl;
-                else lx = uc - __ldcg(u + o - 1) - gxl;
-                if (y == 0) ly = uc - __ldcg(u + o + W) + gyo;
-                else if (y < H - 1) ly = 2.f * uc - __ldcg(u + o - W) - __ldcg(u + o + W) + gyo - gyu;
-                else ly = uc - __ldcg(u + o - W) - gyu;
-                const float rv = -(lx + ly);
-                r[c * N + o] = rv;
-                acc[c] += rv * rv;
-                float e = 0.f;
-                if (x < W - 1) {
-                    const float a = __ldcg(u + o + 1) - uc - gxo;
-                    e += a * a;
-                }
-                if (y < H - 1) {
-                    const float a = __ldcg(u + o + W) - uc - gyo;
-                    e += a * a;
-                }
-                acc[3] += 0.5f * e;
-            }
+            cg_start_pixel(W, H, N, o, gX, gY, U, U0, r, lambda, acc);
         }
         block_partials_f(acc, 4, partB, gridDim.x);
     }
@@ -709,38 +728,11 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_batch(const CgProblem *_
     const float lambda = 1.0f;
     float *U = P.U, *r = P.r;
     unsigned int gen = 0;
-    // ---- phase 0 (as k_cg_persistent): r = b - A u0 and E(u0)
+    // ---- phase 0 (as k_cg_persistent): r = b - A x and F(x)
     {
         float acc[4] = {0.f, 0.f, 0.f, 0.f};
         for (size_t o = (size_t)lb * blockDim.x + threadIdx.x; o < N; o += (size_t)P.nb * blockDim.x) {
-            const int x = (int)(o % W), y = (int)(o / W);
-            const float gxo = __ldg(P.gx + o), gyo = __ldg(P.gy + o);
-            const float gxl = (x > 0) ? __ldg(P.gx + o - 1) : 0.f, gyu = (y > 0) ? __ldg(P.gy + o - W) : 0.f;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                const float *u = U + c * N;
-                const float uc = __ldcg(u + o);
-                float lx, ly;
-                if (x == 0) lx = uc - __ldcg(u + o + 1) + gxo;
-                else if (x < W - 1) lx = 2.f * uc - __ldcg(u + o - 1) - __ldcg(u + o + 1) + gxo - gxl;
-                else lx = uc - __ldcg(u + o - 1) - gxl;
-                if (y == 0) ly = uc - __ldcg(u + o + W) + gyo;
-                else if (y < H - 1) ly = 2.f * uc - __ldcg(u + o - W) - __ldcg(u + o + W) + gyo - gyu;
-                else ly = uc - __ldcg(u + o - W) - gyu;
-                const float rv = -(lx + ly);
-                r[c * N + o] = rv;
-                acc[c] += rv * rv;
-                float e = 0.f;
-                if (x < W - 1) {
-                    const float a = __ldcg(u + o + 1) - uc - gxo;
-                    e += a * a;
-                }
-                if (y < H - 1) {
-                    const float a = __ldcg(u + o + W) - uc - gyo;
-                    e += a * a;
-                }
-                acc[3] += 0.5f * e;
-            }
+            cg_start_pixel(W, H, N, o, P.gx, P.gy, U, P.U0, r, lambda, acc);
         }
         block_partials_f(acc, 4, partB, G);
     }
@@ -1110,7 +1102,7 @@ int persistent_partials() {
 
 cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
                                  float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
-                                 double *state, cudaStream_t st, LaunchCounter &lc) {
+                                 double *state, cudaStream_t st, LaunchCounter &lc, const float *U0) {
     ProfScope _ps(lc, "cg_persistent", st);
     const size_t N = (size_t)W * H;
     const int ntiles = ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
@@ -1133,7 +1125,7 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
     const int resident = coop_blocks(kern, 1 << 30, smem);
     const int per_block = (ntiles + resident - 1) / resident;
     const int blocks = std::max(1, (ntiles + per_block - 1) / per_block);
-    void *args[] = {&W,       &H,       (void *)&gx, (void *)&gy, &U,       &r,       &dA,      &dB,
+    void *args[] = {&W,       &H,       (void *)&gx, (void *)&gy, &U,       (void *)&U0, &r,     &dA,      &dB,
                     &partA,   &partB,   &gb,         &max_iter,   &gap_tol, &state,   &maps[0], &maps[1],
                     &maps[2], &maps[3], &maps[4]};
     lc.add(1);

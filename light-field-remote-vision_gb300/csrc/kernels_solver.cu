@@ -12,6 +12,8 @@
 // the footprint weights from tau instead of storing A (the reference stores ks^2 floats per source pixel).
 #include <algorithm>
 
+#include <cuda_bf16.h>
+
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -550,6 +552,92 @@ __global__ void k_initial_image(int W, int H, int n, int dsf, int BW, const unsi
     if (norm_out) norm_out[o] = norm;
 }
 
+// Input of the learned warm start, NHWC BF16 with kLearnChannels (48) channels per target pixel:
+// [0..2] the anchor u0 (hole-filled weighted average), [3..5] gx, [6..8] gy (zero in the last column / row,
+// which the normal equations never read, and clamped to [-1, 1], the range of finite differences of [0, 1]
+// images), [9] visibility, [10 + 3 v ..]
+// view v splatted alone (sum A w v / sum A w over its own footprints), [34 + v] view v's share of the total splat
+// weight, for the first kLearnViews views; [42..44] the CG's initial residual at u0, r0 = grad^T g + Delta u0
+// (computed in FP32 with the operator's boundary rules, clamped to [-4, 4]); [45..47] zero. Per-view accumulators
+// live in shared
+// memory (one column per thread), so the view index of an entry needs no register indexing.
+template <int KS>
+__global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int dsf, int BW,
+                                                     const unsigned int *__restrict__ start,
+                                                     const unsigned int *__restrict__ entries,
+                                                     const float *__restrict__ tau, const float *__restrict__ img,
+                                                     const float *__restrict__ wgt, const float *__restrict__ U,
+                                                     const float *__restrict__ gx, const float *__restrict__ gy,
+                                                     const uint8_t *__restrict__ vis, __nv_bfloat16 *__restrict__ out) {
+    __shared__ float acc[kLearnViews * 4][256];
+    const int t = threadIdx.y * blockDim.x + threadIdx.x;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+#pragma unroll
+    for (int i = 0; i < kLearnViews * 4; ++i) acc[i][t] = 0.f;
+    if (x >= W || y >= H) return;
+#pragma unroll
+    for (int i = 0; i < KS; ++i) {
+#pragma unroll
+        for (int j = 0; j < KS; ++j) {
+            const int ax = x - j, ay = y - i;
+            const size_t b = (size_t)(ay + KS - 1) * BW + (ax + KS - 1);
+            const unsigned int s0 = __ldg(start + b), e0 = __ldg(start + b + 1);
+            for (unsigned int k = s0; k < e0; ++k) {
+                const unsigned int ent = __ldg(entries + k);
+                const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
+                if (v >= kLearnViews) continue;
+                const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
+                float raw;
+                const float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw) * __ldg(wgt + (size_t)v * n + m);
+                acc[v * 4 + 3][t] += A;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) acc[v * 4 + c][t] += A * __ldg(img + ((size_t)v * 3 + c) * n + m);
+            }
+        }
+    }
+    const size_t o = (size_t)y * W + x, N = (size_t)W * H;
+    float f[kLearnChannels];
+#pragma unroll
+    for (int c = 0; c < kLearnChannels; ++c) f[c] = 0.f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float *u = U + c * N, *gxc = gx + c * N, *gyc = gy + c * N;
+        const float uc = u[o], gxo = gxc[o], gyo = gyc[o];
+        const float gxl = x > 0 ? gxc[o - 1] : 0.f, gyu = y > 0 ? gyc[o - W] : 0.f;
+        float lx, ly;
+        if (x == 0) lx = uc - u[o + 1] + gxo;
+        else if (x < W - 1) lx = 2.f * uc - u[o - 1] - u[o + 1] + gxo - gxl;
+        else lx = uc - u[o - 1] - gxl;
+        if (y == 0) ly = uc - u[o + W] + gyo;
+        else if (y < H - 1) ly = 2.f * uc - u[o - W] - u[o + W] + gyo - gyu;
+        else ly = uc - u[o - W] - gyu;
+        f[c] = uc;
+        f[3 + c] = x < W - 1 ? fminf(fmaxf(gxo, -1.f), 1.f) : 0.f;
+        f[6 + c] = y < H - 1 ? fminf(fmaxf(gyo, -1.f), 1.f) : 0.f;
+        f[42 + c] = fminf(fmaxf(-(lx + ly), -4.f), 4.f);
+    }
+    f[9] = vis[o] ? 1.f : 0.f;
+    float total = 0.f;
+#pragma unroll
+    for (int v = 0; v < kLearnViews; ++v) total += acc[v * 4 + 3][t];
+#pragma unroll
+    for (int v = 0; v < kLearnViews; ++v) {
+        const float a = acc[v * 4 + 3][t];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f[10 + 3 * v + c] = a > 0.f ? acc[v * 4 + c][t] / a : 0.f;
+        f[10 + 3 * kLearnViews + v] = total > 0.f ? a / total : 0.f;
+    }
+    uint4 *dst = reinterpret_cast<uint4 *>(out + o * kLearnChannels);
+#pragma unroll
+    for (int q = 0; q < kLearnChannels / 8; ++q) {
+        uint4 u;
+        __nv_bfloat162 *h = reinterpret_cast<__nv_bfloat162 *>(&u);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) h[i] = __floats2bfloat162_rn(f[8 * q + 2 * i], f[8 * q + 2 * i + 1]);
+        dst[q] = u;
+    }
+}
+
 // Data-term gradient and the proximal data F (vtv_sr_dataterm_intensities :1953-1963 and
 // vtv_sr_ista_step_unstructured :1785-1812): G = alpha sigma^2 sum A e / sum A, F = clamp(U + fs clamp(G)).
 // With a gradient term (gt.resg set, vtv_sr_dataterm_gradients sources/optimization.cu:1969-2116) the
@@ -975,6 +1063,15 @@ void launch_initial_image(const Geometry &G, const Buckets &B, const float *tau,
     SplatSrc src{{img, img + G.n, img + 2 * (size_t)G.n}, {s3, s3, s3}, wgt};
     LFRV_KS_DISPATCH(G.dsf + 1, k_initial_image, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW,
                      B.start, B.entries, tau, src, U, norm);
+    lc.add(1);
+}
+
+void launch_learn_input(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *wgt,
+                        const float *U, const float *gx, const float *gy, const uint8_t *vis, void *out,
+                        cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "learn_input", st);
+    LFRV_KS_DISPATCH(G.dsf + 1, k_learn_input, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW, B.start,
+                     B.entries, tau, img, wgt, U, gx, gy, vis, static_cast<__nv_bfloat16 *>(out));
     lc.add(1);
 }
 

@@ -97,6 +97,9 @@ EXPORTED = [
     "lfrv_ctx_launch_count", "lfrv_ctx_profile", "lfrv_ctx_profile_read", "lfrv_depth_radial_to_ortho",
     "lfrv_depth_radial_to_ortho_dev", "lfrv_warp_from_depth", "lfrv_warp_from_depth_dev", "lfrv_warp", "lfrv_warp_dev", "lfrv_ibr_color", "lfrv_ibr_color_dev",
     "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_render_views_dev",
+    "lfrv_warmstart_param_count", "lfrv_warmstart_create", "lfrv_warmstart_destroy", "lfrv_warmstart_get_params",
+    "lfrv_warmstart_set_params", "lfrv_warmstart_features_dev", "lfrv_warmstart_forward_dev",
+    "lfrv_warmstart_train_step_dev", "lfrv_warmstart_gradients_dev", "lfrv_render_view_warm_dev", "lfrv_conv_bf16_dev",
     "lfrv_stage_weights",
     "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
@@ -388,6 +391,20 @@ class Context:
                                     cameras_array(cams), C.byref(target), C.c_void_p(out_p), C.byref(st)))
         return out, st
 
+    def warmstart_features_dev(self, cfg: Config, d_views: int, d_depth: int, cams, target: Camera, d_input: int,
+                               d_u0: int, d_solution: int = 0) -> Stats:
+        st = Stats()
+        _check(LIB.lfrv_warmstart_features_dev(self._h, C.byref(cfg), C.c_void_p(d_views), C.c_void_p(d_depth),
+                                               cameras_array(cams), C.byref(target), C.c_void_p(d_input),
+                                               C.c_void_p(d_u0 or None), C.c_void_p(d_solution or None),
+                                               C.byref(st)))
+        return st
+
+    def conv_bf16_dev(self, mode: int, batch: int, H: int, W: int, Cin: int, Cout: int, ks: int, stride: int,
+                      d_x: int, d_dy: int, d_w: int, d_out: int) -> None:
+        _check(LIB.lfrv_conv_bf16_dev(self._h, mode, batch, H, W, Cin, Cout, ks, stride, C.c_void_p(d_x or None),
+                                      C.c_void_p(d_dy or None), C.c_void_p(d_w), C.c_void_p(d_out)))
+
     # ---- stage calls (parity tests)
     def stage_visibility(self, cfg: Config, tau):
         tau = f32(tau)
@@ -485,6 +502,71 @@ class Context:
         return U, it.value, gap.value
 
 
+# ------------------------------------------------------------------ learned warm start
+WARMSTART_CHANNELS = 48
+
+
+def warmstart_param_count() -> int:
+    return int(LIB.lfrv_warmstart_param_count())
+
+
+class WarmStart:
+    """The learned warm start of IBR_gradient (lfrv_warmstart_*). Tensors are device pointers (ints): inputs
+    batch x H x W x 48 BF16, u0 / targets / predictions batch x 3 x H x W float32."""
+
+    def __init__(self, ctx: "Context", seed: int = 0):
+        self.ctx = ctx
+        h = C.c_void_p()
+        _check(LIB.lfrv_warmstart_create(ctx._h, C.c_ulonglong(seed), C.byref(h)))
+        self._h = h
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            LIB.lfrv_warmstart_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(warmstart_param_count(), np.float32)
+        _check(LIB.lfrv_warmstart_get_params(self._h, fptr(out)))
+        return out
+
+    def set_params(self, params: np.ndarray) -> None:
+        params = f32(params)
+        assert params.size == warmstart_param_count()
+        _check(LIB.lfrv_warmstart_set_params(self._h, fptr(params)))
+
+    def forward_dev(self, batch: int, H: int, W: int, d_input: int, d_u0: int, d_pred: int) -> None:
+        _check(LIB.lfrv_warmstart_forward_dev(self._h, batch, H, W, C.c_void_p(d_input), C.c_void_p(d_u0),
+                                              C.c_void_p(d_pred)))
+
+    def train_step_dev(self, batch: int, H: int, W: int, d_input: int, d_u0: int, d_target: int,
+                       lr: float) -> float:
+        loss = C.c_double()
+        _check(LIB.lfrv_warmstart_train_step_dev(self._h, batch, H, W, C.c_void_p(d_input), C.c_void_p(d_u0),
+                                                 C.c_void_p(d_target), C.c_float(lr), C.byref(loss)))
+        return loss.value
+
+    def gradients_dev(self, batch: int, H: int, W: int, d_input: int, d_u0: int, d_target: int):
+        loss = C.c_double()
+        g = np.zeros(warmstart_param_count(), np.float32)
+        _check(LIB.lfrv_warmstart_gradients_dev(self._h, batch, H, W, C.c_void_p(d_input), C.c_void_p(d_u0),
+                                                C.c_void_p(d_target), C.byref(loss), fptr(g)))
+        return loss.value, g
+
+    def render_view_dev(self, cfg: Config, d_views: int, d_depth: int, cams, target: Camera, d_out: int) -> Stats:
+        st = Stats()
+        _check(LIB.lfrv_render_view_warm_dev(self.ctx._h, self._h, C.byref(cfg), C.c_void_p(d_views),
+                                             C.c_void_p(d_depth), cameras_array(cams), C.byref(target),
+                                             C.c_void_p(d_out), C.byref(st)))
+        return st
+
+
 def _declare() -> None:
     vp = C.c_void_p
     LIB.lfrv_ctx_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
@@ -522,6 +604,22 @@ def _declare() -> None:
     LIB.lfrv_cg_solve_static.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp, _I, _D]
     LIB.lfrv_png_read.argtypes = [C.c_char_p, _I, _I, _F, C.c_size_t]
     LIB.lfrv_png_write.argtypes = [C.c_char_p, C.c_int, C.c_int, _F]
+    LIB.lfrv_warmstart_param_count.restype = C.c_longlong
+    LIB.lfrv_warmstart_param_count.argtypes = []
+    LIB.lfrv_warmstart_create.argtypes = [vp, C.c_ulonglong, C.POINTER(C.c_void_p)]
+    LIB.lfrv_warmstart_destroy.argtypes = [vp]
+    LIB.lfrv_warmstart_destroy.restype = None
+    LIB.lfrv_warmstart_get_params.argtypes = [vp, _F]
+    LIB.lfrv_warmstart_set_params.argtypes = [vp, _F]
+    LIB.lfrv_warmstart_features_dev.argtypes = [vp, C.POINTER(Config), vp, vp, C.POINTER(Camera), C.POINTER(Camera),
+                                                vp, vp, vp, C.POINTER(Stats)]
+    LIB.lfrv_warmstart_forward_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp]
+    LIB.lfrv_warmstart_train_step_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, C.c_float, _D]
+    LIB.lfrv_warmstart_gradients_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, _D, _F]
+    LIB.lfrv_render_view_warm_dev.argtypes = [vp, vp, C.POINTER(Config), vp, vp, C.POINTER(Camera),
+                                              C.POINTER(Camera), vp, C.POINTER(Stats)]
+    LIB.lfrv_conv_bf16_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       vp, vp, vp, vp]
 
 
 _declare()
