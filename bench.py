@@ -41,6 +41,9 @@ WORKLOADS = {
                                             "(dsf 1 or 2), IBR_gradient + CG to gap 1e-4, one lfrv_render_views_dev call"),
     "c2": dict(preset=2, algorithm=1, name="5x5 LF 512^2 -> 1024^2 (dsf 2), 24 views, IBR_gradient + CG to gap 1e-4"),
     "c1": dict(preset=1, algorithm=0, name="3x3 LF 256^2, 8 views, IBR_color primal-dual TV, 300 x 300 iterations"),
+    "c4": dict(preset=1, algorithm=1, name="learned warm start: 3x3 LF 512^2 (8 views, 3 planes + 20 bumps), "
+                                            "IBR_gradient + CG to gap 1e-4 seeded by the encoder-decoder trained in "
+                                            "the run, 16 held-out targets per step, batched"),
 }
 
 
@@ -282,6 +285,158 @@ def run_batch(args, rank: int, world: int) -> None:
     ctx.close()
 
 
+def warm_scenes(lfrv, seeds, w, targets_per_field):
+    """Seeded 3x3 light fields (planes 1.0 / 1.5 / 2.5 plus 20 Gaussian depth bumps), each seen from
+    `targets_per_field` target cameras (the centre camera shifted by fractions of the baseline)."""
+    import copy
+    out = []
+    for sd in seeds:
+        p = lfrv.scene_params(1, w=w, h=w, seed=int(sd), nbumps=20, bump_amp=0.1, bump_sigma_px=30.0)
+        sc = lfrv.synth_scene(p)
+        for k in range(targets_per_field):
+            t = copy.copy(sc.target)
+            t.t[0] = sc.target.t[0] + ((k % 2) - 0.5) * 0.5 * p.baseline * (k > 0)
+            t.t[1] = sc.target.t[1] + ((k // 2) - 0.5) * 0.5 * p.baseline * (k > 0)
+            out.append((sc, t))
+    return out
+
+
+def run_warm(args, rank: int, world: int) -> None:
+    """Learned warm start (c4): generate and solve training scenes, train the network on the GPU (untimed, bounded),
+    then time converged views/sec on held-out targets: plain start vs warm start, one at a time and batched."""
+    import torch
+    import lfrv
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    wl = WORKLOADS[args.workload]
+    W = 512
+    t_gen = time.time()
+    train = warm_scenes(lfrv, range(1000, 1012), W, 4)      # 12 light fields x 4 targets = 48 samples
+    test = warm_scenes(lfrv, range(5000, 5008), W, 2)       # 8 held-out light fields x 2 targets = 16 views
+    t_gen = time.time() - t_gen
+    ctx = lfrv.Context(dev)
+
+    def cfg_of(sc, tol):
+        p = sc.params
+        return lfrv.default_config(w=p.w, h=p.h, dsf=p.dsf, nviews=sc.views.shape[0], nchannels=3,
+                                   sigma_sensor=0.005, lambda_=0.05, faithful=0, cg_gap_tol=tol, cg_max_iter=500,
+                                   hole_fill_iter=500)
+
+    dev_views = {}
+
+    def dv(sc):
+        k = id(sc)
+        if k not in dev_views:
+            dev_views[k] = (torch.from_numpy(sc.views).cuda(), torch.from_numpy(sc.depth).cuda())
+        return dev_views[k]
+
+    # training data: network input, anchor and the plain solution converged to gap 1e-6
+    t_feat = time.time()
+    X = torch.zeros((len(train), W, W, 48), dtype=torch.bfloat16, device="cuda")
+    U0 = torch.zeros((len(train), 3, W, W), device="cuda")
+    S = torch.zeros((len(train), 3, W, W), device="cuda")
+    torch.cuda.synchronize()
+    for i, (sc, t) in enumerate(train):
+        v, d = dv(sc)
+        ctx.warmstart_features_dev(cfg_of(sc, 1e-6), v.data_ptr(), d.data_ptr(), sc.cams, t, X[i].data_ptr(),
+                                   U0[i].data_ptr(), S[i].data_ptr())
+    torch.cuda.synchronize()
+    t_feat = time.time() - t_feat
+    net = lfrv.WarmStart(ctx, seed=1)
+    g = torch.Generator().manual_seed(0)
+    steps, bs = 1500, 4
+    t_train = time.time()
+    losses = []
+    for step in range(steps):
+        idx = torch.randperm(len(train), generator=g)[:bs].cuda()
+        xb, ub, sb = X[idx].contiguous(), U0[idx].contiguous(), S[idx].contiguous()
+        torch.cuda.synchronize()
+        losses.append(net.train_step_dev(bs, W, W, xb.data_ptr(), ub.data_ptr(), sb.data_ptr(), 5e-4))
+    torch.cuda.synchronize()
+    t_train = time.time() - t_train
+    del X, U0, S
+    # held-out targets
+    outs = [torch.empty((3, W, W), device="cuda") for _ in test]
+    cfgs = [cfg_of(sc, 1e-4) for sc, _ in test]
+    jobs = [dict(cfg=cfgs[i], algorithm=1, d_views=dv(sc)[0].data_ptr(), d_depth=dv(sc)[1].data_ptr(), cams=sc.cams,
+                 target=t, d_out=outs[i].data_ptr()) for i, (sc, t) in enumerate(test)]
+    torch.cuda.synchronize()
+
+    def plain_single():
+        return [ctx.render_view_dev(j["cfg"], 1, j["d_views"], j["d_depth"], j["cams"], j["target"], j["d_out"])
+                for j in jobs]
+
+    def warm_single():
+        return [net.render_view_dev(j["cfg"], j["d_views"], j["d_depth"], j["cams"], j["target"], j["d_out"])
+                for j in jobs]
+
+    def plain_batched():
+        return ctx.render_views_dev(jobs)
+
+    def warm_batched():
+        return ctx.render_views_dev(jobs, net)
+
+    # prediction quality on the held-out targets (mean squared distance to the converged solution)
+    mse_plain = mse_warm = 0.0
+    for i, (sc, t) in enumerate(test):
+        v, d = dv(sc)
+        xi = torch.zeros((W, W, 48), dtype=torch.bfloat16, device="cuda")
+        ui, si, pi = (torch.zeros((3, W, W), device="cuda") for _ in range(3))
+        torch.cuda.synchronize()
+        ctx.warmstart_features_dev(cfg_of(sc, 1e-6), v.data_ptr(), d.data_ptr(), sc.cams, t, xi.data_ptr(),
+                                   ui.data_ptr(), si.data_ptr())
+        net.forward_dev(1, W, W, xi.data_ptr(), ui.data_ptr(), pi.data_ptr())
+        torch.cuda.synchronize()
+        mse_plain += float(((ui - si) ** 2).mean()) / len(test)
+        mse_warm += float(((pi - si) ** 2).mean()) / len(test)
+    results = {}
+    for name, fn in (("plain_single", plain_single), ("warm_single", warm_single), ("plain_batched", plain_batched),
+                     ("warm_batched", warm_batched)):
+        for _ in range(max(args.warmup, 3)):
+            st = fn()
+        torch.cuda.synchronize()
+        if name == "warm_batched":
+            clk_path = tempfile.mktemp(prefix="lfrv_clocks_")
+            clk = sample_clocks(clk_path)
+            l0 = ctx.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            st = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        if name == "warm_batched":
+            launches = ctx.launch_count() - l0
+            clk.terminate()
+            clk.wait()
+            clocks = summarize_clocks(clk_path)
+        results[name] = dict(views_per_s=len(jobs) * args.steps / sec,
+                             cg_iterations=int(sum(s.outer_iterations for s in st)),
+                             max_gap=float(max(s.gap for s in st)))
+    if rank == 0:
+        wb = results["warm_batched"]
+        line = {"metric": "views/sec to energy gap <=1e-4", "value": world * wb["views_per_s"], "unit": "views/s",
+                "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+                "ms_per_step": 1e3 * len(jobs) / wb["views_per_s"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32 iterates, bf16 network",
+                "data": "synthetic (seeded planes + bumps light fields)",
+                "config": {"workload": wl["name"], "targets_per_step": len(jobs), "target": [W, W],
+                           "train_samples": 48, "train_steps": steps, "train_batch": bs,
+                           "train_seconds": round(t_train, 2), "features_seconds": round(t_feat, 2),
+                           "scene_generation_seconds": round(t_gen, 2),
+                           "train_loss_first_last": [losses[0], float(np.mean(losses[-20:]))],
+                           "heldout_mse_plain_start": mse_plain, "heldout_mse_warm_start": mse_warm,
+                           "modes": results,
+                           "learned_batched_vs_plain_single": wb["views_per_s"] / results["plain_single"]["views_per_s"],
+                           "l2": "16 targets of 512^2 with 8 views each exceed L2 (no flush needed)"},
+                "clocks": clocks, "gpu_launches": launches, "roofline": None, "cpu_baseline": None}
+        print(json.dumps(line), flush=True)
+    net.close()
+    ctx.close()
+
+
 def run_ours(args, rank: int, world: int) -> None:
     import torch
     import lfrv
@@ -424,6 +579,8 @@ def main() -> None:
         torch.distributed.init_process_group("nccl")
     if args.workload == "c3":
         run_batch(args, rank, world)
+    elif args.workload == "c4":
+        run_warm(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:

@@ -238,10 +238,11 @@ int lfrv_render_views_dev(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count);
  * certified-gap stop are those of the plain solver: a poor prediction costs iterations, never accuracy.
  * Targets (H, W) must be multiples of 8.
  *
- * Input channels (NHWC BF16, per target pixel): [0..2] u0, [3..5] gx, [6..8] gy (zero in the last column /
- * row, clamped to [-1, 1]), [9] visibility,
- * [10 + 3v .. 12 + 3v] view v splatted alone, [34 + v] view v's share of the splat weight (views v < 8),
- * [42..44] the CG's initial residual at u0 (grad^T g + Delta u0, clamped to [-4, 4]), [45..47] zero. Parameters (lfrv_warmstart_get_params): flat FP32, per layer W[cout][ky][kx][cin] then
+ * Input channels (NHWC BF16, per target pixel): [0..2] u0, [3] gx, [4] gy (the luminance gradient constraint,
+ * zero in the last column / row, clamped to [-1, 1]), [5] visibility, [6 + 3v .. 8 + 3v] view v splatted alone,
+ * [30 + v] view v's share of the splat weight (views v < 8), [38..40] the CG's initial residual at u0
+ * (grad^T g + Delta u0 per channel, clamped to [-4, 4]), [41..47] zero. Parameters (lfrv_warmstart_get_params):
+ * flat FP32, per layer W[cout][ky][kx][cin] then
  * bias[cout], layers in the order of the network description in learn.cpp. */
 #define LFRV_WARMSTART_CHANNELS 48
 typedef struct lfrv_warmstart lfrv_warmstart;
@@ -269,6 +270,11 @@ int lfrv_warmstart_gradients_dev(lfrv_warmstart *net, int batch, int H, int W, c
 int lfrv_render_view_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_config *cfg,
                               const float *d_views, const float *d_depth, const lfrv_camera *cams,
                               const lfrv_camera *target, float *d_out, lfrv_stats *stats);
+/* Batched targets (as lfrv_render_views_dev) with every IBR_gradient job of faithful = 0 and a target of
+ * multiples of 8 pixels seeded by the network, which must belong to ctx: the jobs' inputs are built on the helper
+ * lanes with their set-up, the network predicts each seed on the context stream, and the shared CG launch starts
+ * every seeded job from its prediction with its own anchor. */
+int lfrv_render_views_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_view_job *jobs, int count);
 /* One convolution through the tensor-core kernels: x NHWC BF16 (batch x H x W x Cin), dy NHWC BF16
  * (batch x H/stride x W/stride x Cout), w FP32 Cout x ks x ks x Cin (rounded to BF16 inside), out FP32.
  * mode 0: out = conv(x) (batch x H/s x W/s x Cout); 1: out = the data gradient (batch x H x W x Cin);

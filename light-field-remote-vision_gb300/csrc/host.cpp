@@ -1239,14 +1239,16 @@ extern "C" int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int a
     LFRV_API_END
 }
 
+namespace lfrv {
+void warmstart_predict_async(lfrv_warmstart *net, int H, int W, const void *d_input, const float *d_u0, float *d_pred);
+void warmstart_check(lfrv_warmstart *net);
+lfrv_ctx *warmstart_ctx(lfrv_warmstart *net);
+}  // namespace lfrv
+
 // ====================================================================== learned warm start
 // Training data and warm-started solves of IBR_gradient with the corrected CG. The network sees the set-up
 // products (anchor u0, gx, gy, visibility) and the first views splatted one at a time; its prediction only seeds
 // the CG iterate, while the anchor u0 keeps the problem, its energy and the certified-gap stop unchanged.
-namespace lfrv {
-void warmstart_predict_async(lfrv_warmstart *net, int H, int W, const void *d_input, const float *d_u0, float *d_pred);
-void warmstart_check(lfrv_warmstart *net);
-}  // namespace lfrv
 
 static Geometry warm_geometry(const lfrv_config &cfg, const lfrv_camera *target) {
     if (cfg.faithful) raise(LFRV_E_ARG, "the learned warm start seeds the corrected CG (faithful = 0)");
@@ -1336,7 +1338,7 @@ extern "C" int lfrv_render_view_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, con
 // IBR_gradient jobs with the corrected CG share one k_cg_batch launch (per launch at most as many jobs as resident
 // blocks); every other job runs on its own. Per gradient job the batch pool holds U, gx, gy, r, dA, dB (14 N
 // floats) and 8 doubles of state.
-static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
+static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv_warmstart *net = nullptr) {
     if (count <= 0 || !jobs) raise(LFRV_E_ARG, "empty batch");
     cudaStream_t s = c->stream;
     Workspace &ws = c->ws;
@@ -1344,7 +1346,9 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
         int job;
         Geometry G;
         size_t off;  // float offset of the job's buffers in the pool
+        bool seeded;  // the learned warm start seeds its CG (seed at 14 N + 16, network input after it)
     };
+    if (net && warmstart_ctx(net) != c) raise(LFRV_E_ARG, "the warm-start network belongs to another context");
     std::vector<Slot> batched;
     size_t pool = 0;
     for (int j = 0; j < count; ++j) {
@@ -1357,8 +1361,10 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
         if (J.algorithm == 1 && !J.cfg->faithful) {
             check_solver_options(*J.cfg);
             if (G.W < 2 || G.H < 2) raise(LFRV_E_ARG, "job %d: target smaller than 2 x 2", j);
-            batched.push_back({j, G, pool});
+            const bool seeded = net && G.W % 8 == 0 && G.H % 8 == 0;
+            batched.push_back({j, G, pool, seeded});
             pool += 14 * G.N + 16;  // + 8 doubles of state, kept 64-byte aligned by the 16-float pad
+            if (seeded) pool += 3 * G.N + (G.N * kLearnChannels * 2 + 63) / 64 * 16;  // seed + BF16 input
         }
     }
     ws.batch.ensure(sizeof(float) * std::max<size_t>(pool, 16));
@@ -1397,7 +1403,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
              nullptr);
         float *U = base + sl.off;
         gradient_prepare(l, *J.cfg, G, J.d_views, lw.tau.as<float>(), lw.dp.as<float>(), nullptr, U, U + 3 * G.N,
-                         U + 4 * G.N);
+                         U + 4 * G.N, sl.seeded ? U + 17 * G.N + 16 : nullptr);
         // keep this job's hole-fill iteration count (state slot 8) beside its CG state
         double *st = reinterpret_cast<double *>(U + 14 * G.N);
         LFRV_CUDA(cudaMemcpyAsync(st + 6, lw.state.as<double>() + 8, sizeof(double), cudaMemcpyDeviceToDevice,
@@ -1431,6 +1437,12 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
             finish_stats(c);
         }
     }
+    // seeds of the warm-started jobs: the network, one target after another on the context stream
+    for (const Slot &sl : batched)
+        if (sl.seeded) {
+            float *U = base + sl.off;
+            warmstart_predict_async(net, sl.G.H, sl.G.W, U + 17 * sl.G.N + 16, U, U + 14 * sl.G.N + 16);
+        }
     // the CG of all gradient jobs, in launches of at most `resident` jobs
     const int resident = cg_batch_resident_blocks();
     for (size_t first = 0; first < batched.size(); first += (size_t)resident) {
@@ -1475,12 +1487,12 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
             P.gap_tol = cfg.cg_gap_tol;
             P.gx = U + 3 * sl.G.N;
             P.gy = U + 4 * sl.G.N;
-            P.U = U;
+            P.U = sl.seeded ? U + 14 * sl.G.N + 16 : U;
             P.r = U + 5 * sl.G.N;
             P.dA = U + 8 * sl.G.N;
             P.dB = U + 11 * sl.G.N;
             P.state = reinterpret_cast<double *>(U + 14 * sl.G.N);
-            P.U0 = nullptr;
+            P.U0 = sl.seeded ? U : nullptr;
             for (int k = 0; k < nb[q]; ++k) block_prob[b0 + k] = (int)q;
             b0 += nb[q];
         }
@@ -1498,8 +1510,8 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count) {
         LFRV_CUDA(cudaStreamSynchronize(s));  // the host vectors above go out of scope
     }
     for (const Slot &sl : batched)
-        LFRV_CUDA(cudaMemcpyAsync(jobs[sl.job].d_out, base + sl.off, sizeof(float) * 3 * sl.G.N,
-                                  cudaMemcpyDeviceToDevice, s));
+        LFRV_CUDA(cudaMemcpyAsync(jobs[sl.job].d_out, base + sl.off + (sl.seeded ? 14 * sl.G.N + 16 : 0),
+                                  sizeof(float) * 3 * sl.G.N, cudaMemcpyDeviceToDevice, s));
     sync(c);
     for (lfrv_ctx *l : c->lanes) {
         c->launches.add((int)l->launches.n);
@@ -1523,6 +1535,16 @@ extern "C" int lfrv_render_views_dev(lfrv_ctx *ctx, const lfrv_view_job *jobs, i
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
     render_views(ctx, jobs, count);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_render_views_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_view_job *jobs,
+                                          int count) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!net) return fail(LFRV_E_ARG, "null network");
+    render_views(ctx, jobs, count, net);
+    warmstart_check(net);
     LFRV_API_END
 }
 

@@ -553,14 +553,13 @@ __global__ void k_initial_image(int W, int H, int n, int dsf, int BW, const unsi
 }
 
 // Input of the learned warm start, NHWC BF16 with kLearnChannels (48) channels per target pixel:
-// [0..2] the anchor u0 (hole-filled weighted average), [3..5] gx, [6..8] gy (zero in the last column / row,
-// which the normal equations never read, and clamped to [-1, 1], the range of finite differences of [0, 1]
-// images), [9] visibility, [10 + 3 v ..]
-// view v splatted alone (sum A w v / sum A w over its own footprints), [34 + v] view v's share of the total splat
-// weight, for the first kLearnViews views; [42..44] the CG's initial residual at u0, r0 = grad^T g + Delta u0
-// (computed in FP32 with the operator's boundary rules, clamped to [-4, 4]); [45..47] zero. Per-view accumulators
-// live in shared
-// memory (one column per thread), so the view index of an entry needs no register indexing.
+// [0..2] the anchor u0 (hole-filled weighted average), [3] gx, [4] gy (the splatted luminance gradient, one plane
+// each; zero in the last column / row, which the normal equations never read, and clamped to [-1, 1], the range
+// of finite differences of [0, 1] images), [5] visibility, [6 + 3 v .. 8 + 3 v] view v splatted alone
+// (sum A w v / sum A w over its own footprints), [30 + v] view v's share of the total splat weight, for the first
+// kLearnViews views; [38..40] the CG's initial residual at u0 per channel, r0 = grad^T g + Delta u0 (FP32, the
+// operator's boundary rules, clamped to [-4, 4]); [41..47] zero. Per-view accumulators live in shared memory (one
+// column per thread), so the view index of an entry needs no register indexing.
 template <int KS>
 __global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int dsf, int BW,
                                                      const unsigned int *__restrict__ start,
@@ -599,11 +598,15 @@ __global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int ds
     float f[kLearnChannels];
 #pragma unroll
     for (int c = 0; c < kLearnChannels; ++c) f[c] = 0.f;
+    const float gxo = gx[o], gyo = gy[o];
+    const float gxl = x > 0 ? gx[o - 1] : 0.f, gyu = y > 0 ? gy[o - W] : 0.f;
+    f[3] = x < W - 1 ? fminf(fmaxf(gxo, -1.f), 1.f) : 0.f;
+    f[4] = y < H - 1 ? fminf(fmaxf(gyo, -1.f), 1.f) : 0.f;
+    f[5] = vis[o] ? 1.f : 0.f;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float *u = U + c * N, *gxc = gx + c * N, *gyc = gy + c * N;
-        const float uc = u[o], gxo = gxc[o], gyo = gyc[o];
-        const float gxl = x > 0 ? gxc[o - 1] : 0.f, gyu = y > 0 ? gyc[o - W] : 0.f;
+        const float *u = U + c * N;
+        const float uc = u[o];
         float lx, ly;
         if (x == 0) lx = uc - u[o + 1] + gxo;
         else if (x < W - 1) lx = 2.f * uc - u[o - 1] - u[o + 1] + gxo - gxl;
@@ -612,11 +615,8 @@ __global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int ds
         else if (y < H - 1) ly = 2.f * uc - u[o - W] - u[o + W] + gyo - gyu;
         else ly = uc - u[o - W] - gyu;
         f[c] = uc;
-        f[3 + c] = x < W - 1 ? fminf(fmaxf(gxo, -1.f), 1.f) : 0.f;
-        f[6 + c] = y < H - 1 ? fminf(fmaxf(gyo, -1.f), 1.f) : 0.f;
-        f[42 + c] = fminf(fmaxf(-(lx + ly), -4.f), 4.f);
+        f[38 + c] = fminf(fmaxf(-(lx + ly), -4.f), 4.f);
     }
-    f[9] = vis[o] ? 1.f : 0.f;
     float total = 0.f;
 #pragma unroll
     for (int v = 0; v < kLearnViews; ++v) total += acc[v * 4 + 3][t];
@@ -624,8 +624,8 @@ __global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int ds
     for (int v = 0; v < kLearnViews; ++v) {
         const float a = acc[v * 4 + 3][t];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) f[10 + 3 * v + c] = a > 0.f ? acc[v * 4 + c][t] / a : 0.f;
-        f[10 + 3 * kLearnViews + v] = total > 0.f ? a / total : 0.f;
+        for (int c = 0; c < 3; ++c) f[6 + 3 * v + c] = a > 0.f ? acc[v * 4 + c][t] / a : 0.f;
+        f[6 + 3 * kLearnViews + v] = total > 0.f ? a / total : 0.f;
     }
     uint4 *dst = reinterpret_cast<uint4 *>(out + o * kLearnChannels);
 #pragma unroll

@@ -357,6 +357,8 @@ void warmstart_predict_async(lfrv_warmstart *net, int H, int W, const void *d_in
 
 void warmstart_check(lfrv_warmstart *net) { check_err(net); }
 
+lfrv_ctx *warmstart_ctx(lfrv_warmstart *net) { return net ? net->ctx : nullptr; }
+
 // Single convolution through the tensor-core kernels (tests of the GEMM paths in isolation). mode 0: forward
 // out[b][y][x][co]; 1: data gradient out[b][y][x][ci] of the input; 2: weight gradient out[co][tap][ci].
 static void conv_single(lfrv_ctx *c, int mode, int batch, int Hin, int Win, int Cin, int Cout, int ks, int stride,

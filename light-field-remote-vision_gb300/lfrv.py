@@ -99,7 +99,7 @@ EXPORTED = [
     "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_render_views_dev",
     "lfrv_warmstart_param_count", "lfrv_warmstart_create", "lfrv_warmstart_destroy", "lfrv_warmstart_get_params",
     "lfrv_warmstart_set_params", "lfrv_warmstart_features_dev", "lfrv_warmstart_forward_dev",
-    "lfrv_warmstart_train_step_dev", "lfrv_warmstart_gradients_dev", "lfrv_render_view_warm_dev", "lfrv_conv_bf16_dev",
+    "lfrv_warmstart_train_step_dev", "lfrv_warmstart_gradients_dev", "lfrv_render_view_warm_dev", "lfrv_render_views_warm_dev", "lfrv_conv_bf16_dev",
     "lfrv_stage_weights",
     "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
@@ -362,9 +362,10 @@ class Context:
                                         cameras_array(cams), C.byref(target), C.c_void_p(d_out), C.byref(st)))
         return st
 
-    def render_views_dev(self, jobs) -> list:
+    def render_views_dev(self, jobs, net: "WarmStart | None" = None) -> list:
         """Batched targets: jobs is a list of dicts with cfg, algorithm, d_views, d_depth, cams, target, d_out
-        (device pointers as ints). Returns one Stats per job."""
+        (device pointers as ints). With a warm-start network the IBR_gradient jobs are seeded by it
+        (lfrv_render_views_warm_dev). Returns one Stats per job."""
         arr = (ViewJob * len(jobs))()
         keep = []
         stats = [Stats() for _ in jobs]
@@ -376,7 +377,10 @@ class Context:
             arr[i] = ViewJob(C.pointer(j["cfg"]), int(j["algorithm"]), C.c_void_p(j["d_views"]), C.c_void_p(j["d_depth"]),
                              C.cast(cams, C.POINTER(Camera)), C.pointer(tgt), C.c_void_p(j["d_out"]),
                              C.pointer(stats[i]))
-        _check(LIB.lfrv_render_views_dev(self._h, arr, len(jobs)))
+        if net is None:
+            _check(LIB.lfrv_render_views_dev(self._h, arr, len(jobs)))
+        else:
+            _check(LIB.lfrv_render_views_warm_dev(self._h, net._h, arr, len(jobs)))
         return stats
 
     def render_view(self, cfg: Config, algorithm: int, views, depth, cams, target: Camera, out=None):
@@ -618,6 +622,7 @@ def _declare() -> None:
     LIB.lfrv_warmstart_gradients_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, vp, vp, vp, _D, _F]
     LIB.lfrv_render_view_warm_dev.argtypes = [vp, vp, C.POINTER(Config), vp, vp, C.POINTER(Camera),
                                               C.POINTER(Camera), vp, C.POINTER(Stats)]
+    LIB.lfrv_render_views_warm_dev.argtypes = [vp, vp, C.POINTER(ViewJob), C.c_int]
     LIB.lfrv_conv_bf16_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        vp, vp, vp, vp]
 
