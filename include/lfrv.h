@@ -72,6 +72,9 @@ typedef struct lfrv_config {
     double cg_gap_tol;       /* IBR_gradient, corrected CG: stop when the certified relative energy
                                 gap ||r||^2 / (2 lambda_cg) / |E(u)| falls to this value (0: run the cap) */
     int   hole_fill_iter;    /* IBR_gradient hole filling: Jacobi iteration cap (reference: 500)     */
+    int   bf16_storage;      /* IBR_gradient, device entry points: 1 = d_views holds BF16 values (V x 3 x h x w
+                                bfloat16), and the view gradients and weights are stored in BF16 too; every
+                                accumulation stays FP32 and the CG's dot products and energy FP64 (default 0) */
 } lfrv_config;
 
 /* Fills *cfg with Config_data's defaults (sources/config.cpp:11-64) and this library's option defaults

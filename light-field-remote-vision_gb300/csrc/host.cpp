@@ -140,6 +140,7 @@ static void check_solver_options(const lfrv_config &cfg) {
     if (cfg.dw_type != 0) raise(LFRV_E_ARG, "dw_type %d: only 0 exists upstream (optimization.cu:1141-1147)", cfg.dw_type);
     if (cfg.niter < 0 || cfg.nmeta_iter < 0) raise(LFRV_E_ARG, "negative iteration count");
     if (!(cfg.lambda > 0.0f)) raise(LFRV_E_ARG, "lambda must be > 0");
+    if (cfg.bf16_storage != 0 && cfg.bf16_storage != 1) raise(LFRV_E_ARG, "bf16_storage must be 0 or 1");
 }
 
 // ------------------------------------------------------------------ reductions
@@ -373,6 +374,7 @@ static void energy_gradients(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
 static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
                         const float *init, float *out, lfrv_stats *st) {
     check_solver_options(cfg);
+    if (cfg.bf16_storage) raise(LFRV_E_ARG, "bf16_storage applies to IBR_gradient only");
     const Geometry G = geometry(cfg);
     const size_t N = G.N;
     cudaStream_t s = c->stream;
@@ -591,6 +593,17 @@ static float *view_gradients(lfrv_ctx *c, const Geometry &G, const float *img) {
     return vg;
 }
 
+// BF16 views: their luminance Sobel into a BF16 stack (V x 2 x n), in the same workspace buffer.
+static void *view_gradients_bf16(lfrv_ctx *c, const Geometry &G, const void *img) {
+    Workspace &ws = c->ws;
+    ws.vgrad.ensure(sizeof(uint16_t) * 2 * (size_t)G.V * G.n);
+    uint16_t *vg = ws.vgrad.as<uint16_t>();
+    launch_view_sobel_bf16(G.w, G.h, G.V, img, (size_t)3 * G.n, (size_t)G.n, vg, vg + G.n, (size_t)2 * G.n, c->stream,
+                           c->launches);
+    check_launch("view sobel (bf16)");
+    return vg;
+}
+
 static void u_gradient(lfrv_ctx *c, const Geometry &G, const Buckets &B, const float *img, const float *tau2,
                        const float *wgt, float s2, float *gx, float *gy, float *mask) {
     float *vg = view_gradients(c, G, img);
@@ -675,19 +688,21 @@ static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
     const Buckets B = build_buckets(c, G, tau2);
     ColorBuffers b = color_buffers(c, G);
     ws.mask.ensure(N * sizeof(float));
+    // BF16 storage: img holds BF16 views, and the view gradients and weights are written in BF16
+    const bool bf = cfg.bf16_storage != 0;
     // compute_weights with U = 0 (sources/gradientIBR.cu:575-577): the unmasked Sobel of 0 is 0, so the
     // gathered gradient is 0 and the weights reduce to the deformation weights over sigma^2
-    launch_weights(G, nullptr, nullptr, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, s, c->launches);
+    launch_weights(G, nullptr, nullptr, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, s, c->launches, bf);
     check_launch("weights");
     // visibility, weighted average and gradient splat in one pass of the inverse map
-    float *vg = view_gradients(c, G, img);
-    launch_gradient_setup(G, B, tau2, img, vg, b.wgt, s2, b.vis, U, gx, gy, ws.mask.as<float>(), s, c->launches);
+    const void *vg = bf ? view_gradients_bf16(c, G, img) : (const void *)view_gradients(c, G, img);
+    launch_gradient_setup(G, B, tau2, img, vg, b.wgt, s2, b.vis, U, gx, gy, ws.mask.as<float>(), s, c->launches, bf);
     check_launch("gradient set-up");
     if (init) LFRV_CUDA(cudaMemcpyAsync(U, init, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
     else hole_fill_async(c, G.W, G.H, b.vis, U, cfg.hole_fill_iter);
     // the learned warm start's input: the set-up products and the first views splatted one at a time
     if (learn_in) {
-        launch_learn_input(G, B, tau2, img, b.wgt, U, gx, gy, b.vis, learn_in, s, c->launches);
+        launch_learn_input(G, B, tau2, img, b.wgt, U, gx, gy, b.vis, learn_in, s, c->launches, bf);
         check_launch("learned input");
     }
 }
@@ -1171,6 +1186,7 @@ static int solve_host(lfrv_ctx *ctx, const lfrv_config *cfg, bool color, const f
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
     if (!cfg || !views || !tau || !out) return fail(LFRV_E_ARG, "null argument");
+    if (cfg->bf16_storage) return fail(LFRV_E_ARG, "bf16_storage needs device views (the *_dev entry points)");
     const Geometry G = geometry(*cfg);
     HostIO io{ctx};
     const size_t n = G.n, V = G.V;
@@ -1564,6 +1580,7 @@ extern "C" int lfrv_render_view(lfrv_ctx *ctx, const lfrv_config *cfg, int algor
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
     if (!cfg || !views || !depth || !out || !cams || !target) return fail(LFRV_E_ARG, "null argument");
+    if (cfg->bf16_storage) return fail(LFRV_E_ARG, "bf16_storage needs device views (the *_dev entry points)");
     const Geometry G = geometry(*cfg);
     if (G.V < 1 || G.V > kMaxViews) return fail(LFRV_E_ARG, "bad view count");
     const size_t n = G.n, V = G.V, per_view = 3 * n * sizeof(float);

@@ -119,6 +119,7 @@ extern "C" int lfrv_config_default(lfrv_config *cfg) {
     cfg->cg_max_iter = 500;
     cfg->cg_gap_tol = 1e-4;
     cfg->hole_fill_iter = 500;
+    cfg->bf16_storage = 0;
     return LFRV_OK;
 }
 

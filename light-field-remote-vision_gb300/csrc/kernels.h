@@ -73,8 +73,9 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
 void launch_residual(const Geometry &G, const float *U, const float *img, const float *tau, const float *wgt, float s2,
                      float *res, double *partial, cudaStream_t st, LaunchCounter &lc);
 int residual_partials(const Geometry &G);
+// wgt: FP32, or BF16 with bf16 = true (the BF16 storage mode of IBR_gradient).
 void launch_weights(const Geometry &G, const float *gx, const float *gy, const float *tau, const float *dp, float sigma,
-                    float thr, float *wgt, cudaStream_t st, LaunchCounter &lc);
+                    float thr, void *wgt, cudaStream_t st, LaunchCounter &lc, bool bf16 = false);
 void launch_coverage(const Geometry &G, const Buckets &B, const float *tau, float *cov, uint8_t *vis, cudaStream_t st,
                      LaunchCounter &lc);
 void launch_vis_any(const Geometry &G, const Buckets &B, const float *tau, uint8_t *vis, cudaStream_t st,
@@ -84,9 +85,9 @@ void launch_initial_image(const Geometry &G, const Buckets &B, const float *tau,
 // Learned warm start input (NHWC BF16, kLearnChannels per target pixel) from the IBR_gradient set-up products
 // and the first kLearnViews views splatted one at a time.
 constexpr int kLearnChannels = 48, kLearnViews = 8;
-void launch_learn_input(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *wgt,
+void launch_learn_input(const Geometry &G, const Buckets &B, const float *tau, const void *img, const void *wgt,
                         const float *U, const float *gx, const float *gy, const uint8_t *vis, void *out,
-                        cudaStream_t st, LaunchCounter &lc);
+                        cudaStream_t st, LaunchCounter &lc, bool bf16 = false);
 // Gradient data term of the ISTA step (dt_beta > 0): per-view residuals resg (3 x n each) and their weights.
 struct GradTerm {
     const float *resg;  // nullptr: no gradient term
@@ -107,9 +108,13 @@ void launch_regweight(const Geometry &G, const Buckets &B, const float *tau, con
                       LaunchCounter &lc);
 void launch_u_gradient(const Geometry &G, const Buckets &B, const float *tau, const float *vgrad, const float *wgt,
                        float s2, float *gx, float *gy, float *mask, cudaStream_t st, LaunchCounter &lc);
-void launch_gradient_setup(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *vgrad,
-                           const float *wgt, float s2, uint8_t *vis, float *U, float *gx, float *gy, float *mask,
-                           cudaStream_t st, LaunchCounter &lc);
+// img, vgrad, wgt: FP32, or BF16 with bf16 = true; U, gx, gy, mask FP32 either way.
+void launch_gradient_setup(const Geometry &G, const Buckets &B, const float *tau, const void *img, const void *vgrad,
+                           const void *wgt, float s2, uint8_t *vis, float *U, float *gx, float *gy, float *mask,
+                           cudaStream_t st, LaunchCounter &lc, bool bf16 = false);
+// Luminance Sobel of BF16 views into BF16 gradients.
+void launch_view_sobel_bf16(int W, int H, int count, const void *rgb, size_t in_stride, size_t ch_stride, void *gx,
+                            void *gy, size_t out_stride, cudaStream_t st, LaunchCounter &lc);
 void launch_sobel(int W, int H, int count, const float *rgb, size_t in_stride, size_t ch_stride, float *gx, float *gy,
                   size_t out_stride, const uint8_t *vis, double *abs_partial, cudaStream_t st, LaunchCounter &lc);
 int sobel_partials(int W, int H);

@@ -15,6 +15,8 @@
 // ((r / 8) * 8 + k / 8) * 128 + (r % 8) * 16 + (k % 8) * 2: core matrices adjacent in K are 128 B apart (leading
 // byte offset), 8-row groups 1 KB apart (stride byte offset); one MMA (K = 16) reads two core matrices along K, so
 // the descriptor start advances 256 B per MMA.
+#include <algorithm>
+
 #include <cuda_bf16.h>
 #include <stdint.h>
 
@@ -30,8 +32,7 @@ constexpr int kBM = 128, kBK = 64, kThreads = 128, kStages = 4, kWgStages = 2;
 
 // Shared-memory matrix descriptor: start >> 4 in bits 0-13, leading byte offset >> 4 in 16-29, stride byte
 // offset >> 4 in 32-45, the fixed version field (1) in 46-47, base offset 0, layout type 0 (no swizzle).
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr) {
-    constexpr uint32_t lbo = 128, sbo = 1024;
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo = 128, uint32_t sbo = 1024) {
     uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
     d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
     d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
@@ -150,7 +151,7 @@ __device__ __forceinline__ bool conv_src(const ConvGemm &g, int y, int x, int ky
 
 }  // namespace
 
-// One CTA: 128 GEMM rows (pixels) x all N output channels (N = BN), K in 64-wide stages through a kStages-deep
+// One CTA: 128 GEMM rows (pixels) x BN output channels (columns n0 = blockIdx.y * BN ..), K in 64-wide stages through a kStages-deep
 // cp.async ring. Thread 0 issues the four K = 16 MMAs of a stage once the stage has landed and commits them to
 // the stage's mbarrier; a slot is refilled only after the mbarrier shows that the MMAs reading it completed.
 template <int BN>
@@ -164,7 +165,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvGemm g, int *err
     uint8_t *base = align1024(dsm);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int M = g.batch * g.Ho * g.Wo, HWo = g.Ho * g.Wo;
-    const int m0 = blockIdx.x * kBM;
+    const int m0 = blockIdx.x * kBM, n0 = blockIdx.y * BN;
     if (warp == 0) tmem_alloc(&tmem_slot, kCols);
     if (tid == 0) {
         for (int s = 0; s < kStages; ++s) mbar_init(&bars[s], 1);
@@ -211,7 +212,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvGemm g, int *err
 #pragma unroll
         for (int j = 0; j < BN / 16; ++j) {
             const int r = (rhi + 2 * j) * 8 + rlo;
-            cp_async16(sb + tile_off(r, kc), wt + (size_t)r * g.ldw + kt * kBK + kc * 8, 16);
+            cp_async16(sb + tile_off(r, kc), wt + (size_t)(n0 + r) * g.ldw + kt * kBK + kc * 8, 16);
         }
     };
     tc_fence_before();
@@ -274,10 +275,10 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvGemm g, int *err
             float v[16];
             tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
             if (!row_ok) continue;
-            const size_t o = (size_t)m * BN + c0;
+            const size_t o = (size_t)m * g.N + n0 + c0;
             if (g.bias) {
 #pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] += __ldg(g.bias + c0 + i);
+                for (int i = 0; i < 16; ++i) v[i] += __ldg(g.bias + n0 + c0 + i);
             }
             if (g.add) {
                 const uint4 *ap = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.add) + o);
@@ -312,6 +313,173 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvGemm g, int *err
                 uint4 *bp = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(g.outb) + o);
                 bp[0] = pack8(v);
                 bp[1] = pack8(v + 8);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_free(tmem, kCols);
+}
+
+// Stride-1 3 x 3 convolution (or its data gradient, taps mirrored) with the input tile resident in shared memory.
+// A CTA computes R output rows x 128 columns (x0 .. x0 + 127) x BN channels: it loads the (R + 2) x 130 input pixels
+// around them once, in a layout where consecutive pixels are consecutive 16-byte rows of the core matrices
+// (stride byte offset 128) and the 8-channel chunks are kLboA apart (leading byte offset), so the A operand of
+// tap (ky, kx) for output row i is the same tile read from pixel (i + ky) * 130 + kx on: nine shifted descriptors
+// instead of nine gathers. The weights stream per tap through a 3-slot cp.async ring. TMEM: R accumulators of BN
+// columns. Needs W % 128 == 0, H % R == 0, C % 16 == 0.
+constexpr int kTileW = 130, kTapStages = 3;
+
+__host__ __device__ constexpr int tile_lbo_px(int R) { return ((R + 2) * kTileW) | 1; }  // odd: spreads the banks
+
+template <int BN, int R>
+__global__ void __launch_bounds__(kThreads) k_conv_tile_tc(const ConvGemm g, int *err) {
+    extern __shared__ uint8_t dsm[];
+    constexpr int kCols = (R * BN) < 32 ? 32 : (R * BN);
+    constexpr int npix = (R + 2) * kTileW, lbo_px = tile_lbo_px(R);
+    __shared__ __align__(8) uint64_t bars[kTapStages];
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_fail;
+    uint8_t *base = align1024(dsm);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int C = g.C, chunks = C >> 3;
+    const int strips = g.Wo >> 7, yblocks = g.Ho / R;
+    int blk = blockIdx.x;
+    const int strip = blk % strips;
+    blk /= strips;
+    const int yb = blk % yblocks, b = blk / yblocks;
+    const int x0 = strip << 7, y0 = yb * R, n0 = blockIdx.y * BN;
+    const uint32_t lboA = (uint32_t)lbo_px * 16u;
+    const uint32_t sA = smem_u32(base), sB = sA + (uint32_t)chunks * lboA;
+    const uint32_t bstage = (uint32_t)BN * (uint32_t)C * 2u;  // bytes of one tap's weights
+    if (warp == 0) tmem_alloc(&tmem_slot, kCols);
+    if (tid == 0) {
+        for (int s = 0; s < kTapStages; ++s) mbar_init(&bars[s], 1);
+        s_fail = 0;
+        fence_proxy_async_smem();
+    }
+    const __nv_bfloat16 *src = static_cast<const __nv_bfloat16 *>(g.src);
+    const __nv_bfloat16 *wt = static_cast<const __nv_bfloat16 *>(g.wt);
+    // the input tile (zero outside the image): thread q -> pixel q / chunks, chunk q % chunks (coalesced reads)
+    const size_t img = (size_t)b * g.Hs * g.Ws;
+    for (int q = tid; q < npix * chunks; q += kThreads) {
+        const int p = q / chunks, j = q - p * chunks;
+        const int rr = p / kTileW, cc = p - rr * kTileW;
+        const int iy = y0 - 1 + rr, ix = x0 - 1 + cc;
+        const bool ok = iy >= 0 && iy < g.Hs && ix >= 0 && ix < g.Ws;
+        const __nv_bfloat16 *gp = ok ? src + (img + (size_t)iy * g.Ws + ix) * C + j * 8 : src;
+        cp_async16(sA + (uint32_t)j * lboA + (uint32_t)p * 16u, gp, ok ? 16 : 0);
+    }
+    cp_async_commit();
+    // one tap's weights: B[n][c] = wt[n0 + n][tap * C + c], chunk-major (chunk j at j * BN * 16, row n at n * 16)
+    auto load_tap = [&](int t, int slot) {
+        const uint32_t dst = sB + (uint32_t)slot * bstage;
+        for (int q = tid; q < BN * chunks; q += kThreads) {
+            const int n = q % BN, j = q / BN;
+            cp_async16(dst + (uint32_t)(j * BN + n) * 16u, wt + (size_t)(n0 + n) * g.ldw + t * C + j * 8, 16);
+        }
+    };
+    load_tap(0, 0);
+    cp_async_commit();
+    load_tap(1, 1);
+    cp_async_commit();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    const uint32_t idesc = idesc_bf16_f32(kBM, BN);
+    int issued = 0;
+#pragma unroll 1
+    for (int t = 0; t < 9; ++t) {
+        cp_async_wait<1>();  // the tile and this tap's weights have landed
+        fence_proxy_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+        if (s_fail) break;
+        if (tid == 0) {
+            const int ky = t / 3, kx = t - 3 * (t / 3);
+            const int sy = g.dgrad ? 2 - ky : ky, sx = g.dgrad ? 2 - kx : kx;
+            const uint32_t bb = sB + (uint32_t)(t % kTapStages) * bstage;
+            for (int i = 0; i < R; ++i) {
+                const uint32_t a0 = sA + (uint32_t)((i + sy) * kTileW + sx) * 16u;
+                for (int s = 0; s < C / 16; ++s)
+                    tc_mma(tmem + (uint32_t)(i * BN), smem_desc(a0 + (uint32_t)(2 * s) * lboA, lboA, 128),
+                           smem_desc(bb + (uint32_t)(2 * s) * (uint32_t)BN * 16u, (uint32_t)BN * 16u, 128), idesc,
+                           (t > 0 || s > 0) ? 1 : 0);
+            }
+            tc_commit(&bars[t % kTapStages]);
+        }
+        issued = t + 1;
+        if (t + 2 < 9) {
+            bool ok = true;
+            if (t >= 1) ok = mbar_wait(&bars[(t - 1) % kTapStages], ((t - 1) / kTapStages) & 1, kSpinLimit);
+            if (ok) load_tap(t + 2, (t + 2) % kTapStages);
+            else {
+                s_fail = 1;
+                atomicExch(err, 1);
+            }
+        }
+        cp_async_commit();
+    }
+    cp_async_wait<0>();
+    bool done = true;
+    if (issued > 0) done = mbar_wait(&bars[(issued - 1) % kTapStages], ((issued - 1) / kTapStages) & 1, kSpinLimit);
+    if (!done) {
+        s_fail = 1;
+        atomicExch(err, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (!s_fail && issued == 9) {
+        const int m = warp * 32 + lane;
+#pragma unroll 1
+        for (int i = 0; i < R; ++i) {
+            const size_t row = ((size_t)b * g.Ho + y0 + i) * g.Wo + x0 + m;
+#pragma unroll 1
+            for (int c0 = 0; c0 < BN; c0 += 16) {
+                float v[16];
+                tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * BN + c0), v);
+                const size_t o = row * g.N + n0 + c0;
+                if (g.bias) {
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) v[k] += __ldg(g.bias + n0 + c0 + k);
+                }
+                if (g.add) {
+                    const uint4 *ap = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.add) + o);
+                    float tt[8];
+                    unpack8(ap[0], tt);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) v[k] += tt[k];
+                    unpack8(ap[1], tt);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) v[8 + k] += tt[k];
+                }
+                if (g.relu) {
+#pragma unroll
+                    for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.f);
+                }
+                if (g.mask) {
+                    const uint4 *mp = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.mask) + o);
+                    float tt[8];
+                    unpack8(mp[0], tt);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) v[k] = tt[k] > 0.f ? v[k] : 0.f;
+                    unpack8(mp[1], tt);
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) v[8 + k] = tt[k] > 0.f ? v[8 + k] : 0.f;
+                }
+                if (g.outf) {
+                    float4 *fp = reinterpret_cast<float4 *>(g.outf + o);
+#pragma unroll
+                    for (int k = 0; k < 4; ++k) fp[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+                }
+                if (g.outb) {
+                    uint4 *bp = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(g.outb) + o);
+                    bp[0] = pack8(v);
+                    bp[1] = pack8(v + 8);
+                }
             }
         }
     }
@@ -625,16 +793,79 @@ static cudaError_t conv_launch(const ConvGemm &g, int *err, cudaStream_t st) {
         attr = true;
     }
     const int M = g.batch * g.Ho * g.Wo;
-    k_conv_tc<BN><<<(M + kBM - 1) / kBM, kThreads, smem, st>>>(g, err);
+    k_conv_tc<BN><<<dim3((M + kBM - 1) / kBM, g.N / BN), kThreads, smem, st>>>(g, err);
     return cudaGetLastError();
+}
+
+template <int BN, int R>
+static cudaError_t tile_launch(const ConvGemm &g, int smem, int *err, cudaStream_t st) {
+    static int attr = 0;
+    if (smem > attr) {
+        const cudaError_t e =
+            cudaFuncSetAttribute(k_conv_tile_tc<BN, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = smem;
+    }
+    const dim3 grid(g.batch * (g.Ho / R) * (g.Wo >> 7), g.N / BN);
+    k_conv_tile_tc<BN, R><<<grid, kThreads, smem, st>>>(g, err);
+    return cudaGetLastError();
+}
+
+// The resident-tile kernel's shape for a stride-1 3 x 3 layer (forward, or data gradient of a stride-1 layer), or
+// false when it does not apply (rows not a multiple of 128, channels not a multiple of 16, no shape that fits).
+static bool tile_shape(const ConvGemm &g, int &R, int &BN, int &smem) {
+    if (g.ks != 3 || g.stride != 1 || g.Wo % 128 || g.C % 16 || g.Hs != g.Ho || g.Ws != g.Wo) return false;
+    if (g.ldw < 9 * g.C) return false;
+    int best = -1;
+    for (int r : {4, 2, 1}) {
+        if (g.Ho % r) continue;
+        for (int bn = g.N; bn >= 16 && bn >= g.N / 2; bn >>= 1) {
+            if (r * bn > 256 || bn > 128) continue;
+            const int sm = (g.C / 8) * tile_lbo_px(r) * 16 + kTapStages * bn * g.C * 2 + 1024;
+            if (sm > 200 * 1024) continue;
+            const int ctas = g.batch * (g.Ho / r) * (g.Wo / 128) * (g.N / bn);
+            const int score = std::min(ctas, 2 * 148);
+            if (score > best) {
+                best = score;
+                R = r;
+                BN = bn;
+                smem = sm;
+            }
+        }
+    }
+    return best > 0;
+}
+
+static cudaError_t launch_tile(const ConvGemm &g, int R, int BN, int smem, int *err, cudaStream_t st) {
+#define LFRV_TILE_CASE(bn, r) \
+    if (BN == bn && R == r) return tile_launch<bn, r>(g, smem, err, st);
+    LFRV_TILE_CASE(16, 1) LFRV_TILE_CASE(16, 2) LFRV_TILE_CASE(16, 4)
+    LFRV_TILE_CASE(32, 1) LFRV_TILE_CASE(32, 2) LFRV_TILE_CASE(32, 4)
+    LFRV_TILE_CASE(64, 1) LFRV_TILE_CASE(64, 2) LFRV_TILE_CASE(64, 4)
+    LFRV_TILE_CASE(128, 1) LFRV_TILE_CASE(128, 2)
+#undef LFRV_TILE_CASE
+    return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_conv_tc(const ConvGemm &g, int *err, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, g.dgrad ? "conv_dgrad_tc" : "conv_fwd_tc", st);
+    {
+        int R = 0, BN = 0, smem = 0;
+        if (tile_shape(g, R, BN, smem)) {
+            const cudaError_t e = launch_tile(g, R, BN, smem, err, st);
+            lc.add(1);
+            return e;
+        }
+    }
     if (g.C % 8 || g.ldw % kBK || g.ldw < ((g.K + kBK - 1) / kBK) * kBK || g.K <= 0) return cudaErrorInvalidValue;
     if (g.stride != 1 && g.stride != 2) return cudaErrorInvalidValue;
+    if (g.N != 16 && g.N != 32 && g.N != 64 && g.N != 128 && g.N != 256) return cudaErrorInvalidValue;
+    // output columns per CTA: all N, halved while the grid would not fill the SMs (the low-resolution layers)
+    const int mtiles = (g.batch * g.Ho * g.Wo + kBM - 1) / kBM;
+    int bn = g.N;
+    while (bn > 32 && mtiles * (g.N / bn) < 120) bn >>= 1;
     cudaError_t e;
-    switch (g.N) {
+    switch (bn) {
         case 16: e = conv_launch<16>(g, err, st); break;
         case 32: e = conv_launch<32>(g, err, st); break;
         case 64: e = conv_launch<64>(g, err, st); break;

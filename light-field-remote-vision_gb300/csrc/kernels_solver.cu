@@ -19,6 +19,14 @@
 
 namespace lfrv {
 
+// Storage of the per-view stacks: FP32, or BF16 when the configuration asks for it (loads widen to FP32, and
+// every accumulation stays FP32).
+__device__ __forceinline__ float ldv(const float *p) { return __ldg(p); }
+__device__ __forceinline__ float ldv(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
+__device__ __forceinline__ void stv(float *p, float v) { *p = v; }
+__device__ __forceinline__ void stv(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
+
+
 // ====================================================================== inverse footprint map
 __global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
                                unsigned int *__restrict__ cnt) {
@@ -140,11 +148,11 @@ __global__ void __launch_bounds__(256) k_residual(int V, int n, int W, int H, in
 // Angular and deformation weights of every source pixel (coco_vtv_sr_compute_weights_unstructured,
 // sources/optimization.cu:1094-1163; vtv_sr_angular_weights_device and vtv_sr_gold_deform_weights_device,
 // vtv_sr_kernels_unstructured.cu:174-266): w = 1/(sg^2 + sigma^2) * deform with sg = clamp(A_i grad) . dpart.
-template <int KS>
+template <int KS, typename TW>
 __global__ void __launch_bounds__(256) k_weights(int V, int n, int w, int h, int W, int H, int dsf,
                                                  const float *__restrict__ gx, const float *__restrict__ gy,
                                                  const float *__restrict__ tau, const float *__restrict__ dp,
-                                                 float sigma, float thr, float *__restrict__ wgt) {
+                                                 float sigma, float thr, TW *__restrict__ wgt) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     const int v = blockIdx.y;
     if (m >= n) return;
@@ -191,7 +199,7 @@ __global__ void __launch_bounds__(256) k_weights(int V, int n, int w, int h, int
         const float N = fabsf(Dxx * Dyy - Dxy * Dyx);
         def = (N > 1.0f) ? 1.0f / N : 1.0f;
     }
-    wgt[(size_t)v * n + m] = ang * def;
+    stv(wgt + (size_t)v * n + m, ang * def);
 }
 
 // ====================================================================== A^T gathers (per target pixel)
@@ -320,12 +328,12 @@ struct SetupAcc {
 };
 
 // The set-up of one target pixel reading every entry straight from global memory.
-template <int KS>
+template <int KS, typename TS>
 __device__ __forceinline__ void gradient_setup_global(int x, int y, int W, int H, int n, int dsf, int BW,
                                                       const unsigned int *__restrict__ start,
                                                       const unsigned int *__restrict__ entries,
-                                                      const float *__restrict__ tau, const float *__restrict__ img,
-                                                      const float *__restrict__ vgrad, const float *__restrict__ wgt,
+                                                      const float *__restrict__ tau, const TS *__restrict__ img,
+                                                      const TS *__restrict__ vgrad, const TS *__restrict__ wgt,
                                                       SetupAcc &acc) {
 #pragma unroll
     for (int i = 0; i < KS; ++i) {
@@ -340,10 +348,10 @@ __device__ __forceinline__ void gradient_setup_global(int x, int y, int W, int H
                 const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
                 float raw;
                 const float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw);
-                const float *iv = img + (size_t)v * 3 * n;
-                const float *gv = vgrad + (size_t)v * 2 * n;
-                acc.add(A, raw, __ldg(wgt + (size_t)v * n + m), __ldg(iv + m), __ldg(iv + n + m), __ldg(iv + 2 * n + m),
-                        __ldg(gv + m), __ldg(gv + n + m));
+                const TS *iv = img + (size_t)v * 3 * n;
+                const TS *gv = vgrad + (size_t)v * 2 * n;
+                acc.add(A, raw, ldv(wgt + (size_t)v * n + m), ldv(iv + m), ldv(iv + n + m), ldv(iv + 2 * n + m),
+                        ldv(gv + m), ldv(gv + n + m));
             }
         }
     }
@@ -359,14 +367,14 @@ __device__ __forceinline__ void gradient_setup_global(int x, int y, int W, int H
 // are deterministic. Fields: 0 w A, 1-3 w A v, 4 A, 5-6 A Sobel, 7 A w, 8 visibility (raw overlap != 0).
 constexpr int kGrWarps = 8;
 
-template <int KS>
+template <int KS, typename TS>
 __global__ void __launch_bounds__(kGrWarps * 32, 2) k_gradient_setup_rows(int W, int H, int n, int dsf, int BW,
                                                                        const unsigned int *__restrict__ start,
                                                                        const unsigned int *__restrict__ entries,
                                                                        const float *__restrict__ tau,
-                                                                       const float *__restrict__ img,
-                                                                       const float *__restrict__ vgrad,
-                                                                       const float *__restrict__ wgt, float s2,
+                                                                       const TS *__restrict__ img,
+                                                                       const TS *__restrict__ vgrad,
+                                                                       const TS *__restrict__ wgt, float s2,
                                                                        uint8_t *__restrict__ vis,
                                                                        float *__restrict__ U, float *__restrict__ gx,
                                                                        float *__restrict__ gy,
@@ -404,17 +412,17 @@ __global__ void __launch_bounds__(kGrWarps * 32, 2) k_gradient_setup_rows(int W,
             };
             auto fetch = [&](unsigned int ent) {
                 const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
-                const float *iv = img + (size_t)v * 3 * n;
-                const float *gv = vgrad + (size_t)v * 2 * n;
+                const TS *iv = img + (size_t)v * 3 * n;
+                const TS *gv = vgrad + (size_t)v * 2 * n;
                 Src d;
                 d.tx = __ldg(tau + (size_t)v * 2 * n + m);
                 d.ty = __ldg(tau + (size_t)v * 2 * n + n + m);
-                d.w = __ldg(wgt + (size_t)v * n + m);
-                d.c0 = __ldg(iv + m);
-                d.c1 = __ldg(iv + n + m);
-                d.c2 = __ldg(iv + 2 * n + m);
-                d.s0 = __ldg(gv + m);
-                d.s1 = __ldg(gv + n + m);
+                d.w = ldv(wgt + (size_t)v * n + m);
+                d.c0 = ldv(iv + m);
+                d.c1 = ldv(iv + n + m);
+                d.c2 = ldv(iv + 2 * n + m);
+                d.s0 = ldv(gv + m);
+                d.s1 = ldv(gv + n + m);
                 return d;
             };
             Src cur = {};
@@ -519,20 +527,20 @@ __global__ void __launch_bounds__(kGrWarps * 32, 2) k_gradient_setup_rows(int W,
 }
 
 // Per-pixel form for KS > 3 (too many register partials for the anchor-row form).
-template <int KS>
+template <int KS, typename TS>
 __global__ void __launch_bounds__(256) k_gradient_setup_px(int W, int H, int n, int dsf, int BW,
                                                            const unsigned int *__restrict__ start,
                                                            const unsigned int *__restrict__ entries,
-                                                           const float *__restrict__ tau, const float *__restrict__ img,
-                                                           const float *__restrict__ vgrad,
-                                                           const float *__restrict__ wgt, float s2,
+                                                           const float *__restrict__ tau, const TS *__restrict__ img,
+                                                           const TS *__restrict__ vgrad,
+                                                           const TS *__restrict__ wgt, float s2,
                                                            uint8_t *__restrict__ vis, float *__restrict__ U,
                                                            float *__restrict__ gx, float *__restrict__ gy,
                                                            float *__restrict__ mask) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= W || y >= H) return;
     SetupAcc acc;
-    gradient_setup_global<KS>(x, y, W, H, n, dsf, BW, start, entries, tau, img, vgrad, wgt, acc);
+    gradient_setup_global<KS, TS>(x, y, W, H, n, dsf, BW, start, entries, tau, img, vgrad, wgt, acc);
     acc.store((size_t)y * W + x, (size_t)W * H, s2, vis, U, gx, gy, mask);
 }
 
@@ -560,12 +568,12 @@ __global__ void k_initial_image(int W, int H, int n, int dsf, int BW, const unsi
 // kLearnViews views; [38..40] the CG's initial residual at u0 per channel, r0 = grad^T g + Delta u0 (FP32, the
 // operator's boundary rules, clamped to [-4, 4]); [41..47] zero. Per-view accumulators live in shared memory (one
 // column per thread), so the view index of an entry needs no register indexing.
-template <int KS>
+template <int KS, typename TS>
 __global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int dsf, int BW,
                                                      const unsigned int *__restrict__ start,
                                                      const unsigned int *__restrict__ entries,
-                                                     const float *__restrict__ tau, const float *__restrict__ img,
-                                                     const float *__restrict__ wgt, const float *__restrict__ U,
+                                                     const float *__restrict__ tau, const TS *__restrict__ img,
+                                                     const TS *__restrict__ wgt, const float *__restrict__ U,
                                                      const float *__restrict__ gx, const float *__restrict__ gy,
                                                      const uint8_t *__restrict__ vis, __nv_bfloat16 *__restrict__ out) {
     __shared__ float acc[kLearnViews * 4][256];
@@ -587,10 +595,10 @@ __global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int ds
                 if (v >= kLearnViews) continue;
                 const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
                 float raw;
-                const float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw) * __ldg(wgt + (size_t)v * n + m);
+                const float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw) * ldv(wgt + (size_t)v * n + m);
                 acc[v * 4 + 3][t] += A;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) acc[v * 4 + c][t] += A * __ldg(img + ((size_t)v * 3 + c) * n + m);
+                for (int c = 0; c < 3; ++c) acc[v * 4 + c][t] += A * ldv(img + ((size_t)v * 3 + c) * n + m);
             }
         }
     }
@@ -1031,12 +1039,24 @@ void launch_residual(const Geometry &G, const float *U, const float *img, const 
 }
 int residual_partials(const Geometry &G) { return ((G.n + 255) / 256) * G.V; }
 
-void launch_weights(const Geometry &G, const float *gx, const float *gy, const float *tau, const float *dp, float sigma,
-                    float thr, float *wgt, cudaStream_t st, LaunchCounter &lc) {
-    ProfScope _ps(lc, "weights", st);
+template <typename TW>
+static void weights_typed(const Geometry &G, const float *gx, const float *gy, const float *tau, const float *dp,
+                          float sigma, float thr, TW *wgt, cudaStream_t st) {
     const dim3 b(256), g((G.n + 255) / 256, G.V);
-    LFRV_KS_DISPATCH(G.dsf + 1, k_weights, g, b, st, G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr,
-                     wgt);
+    switch (G.dsf + 1) {
+        case 2: k_weights<2, TW><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt); break;
+        case 3: k_weights<3, TW><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt); break;
+        case 4: k_weights<4, TW><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt); break;
+        case 5: k_weights<5, TW><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt); break;
+        default: break;
+    }
+}
+
+void launch_weights(const Geometry &G, const float *gx, const float *gy, const float *tau, const float *dp, float sigma,
+                    float thr, void *wgt, cudaStream_t st, LaunchCounter &lc, bool bf16) {
+    ProfScope _ps(lc, "weights", st);
+    if (bf16) weights_typed(G, gx, gy, tau, dp, sigma, thr, static_cast<__nv_bfloat16 *>(wgt), st);
+    else weights_typed(G, gx, gy, tau, dp, sigma, thr, static_cast<float *>(wgt), st);
     lc.add(1);
 }
 
@@ -1066,12 +1086,31 @@ void launch_initial_image(const Geometry &G, const Buckets &B, const float *tau,
     lc.add(1);
 }
 
-void launch_learn_input(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *wgt,
+template <typename TS>
+static void learn_input_typed(const Geometry &G, const Buckets &B, const float *tau, const TS *img, const TS *wgt,
+                              const float *U, const float *gx, const float *gy, const uint8_t *vis,
+                              __nv_bfloat16 *out, cudaStream_t st) {
+    const dim3 g = grid2(G.W, G.H, kTile);
+    switch (G.dsf + 1) {
+        case 2: k_learn_input<2, TS><<<g, kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau, img, wgt, U, gx, gy, vis, out); break;
+        case 3: k_learn_input<3, TS><<<g, kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau, img, wgt, U, gx, gy, vis, out); break;
+        case 4: k_learn_input<4, TS><<<g, kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau, img, wgt, U, gx, gy, vis, out); break;
+        case 5: k_learn_input<5, TS><<<g, kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau, img, wgt, U, gx, gy, vis, out); break;
+        default: break;
+    }
+}
+
+void launch_learn_input(const Geometry &G, const Buckets &B, const float *tau, const void *img, const void *wgt,
                         const float *U, const float *gx, const float *gy, const uint8_t *vis, void *out,
-                        cudaStream_t st, LaunchCounter &lc) {
+                        cudaStream_t st, LaunchCounter &lc, bool bf16) {
     ProfScope _ps(lc, "learn_input", st);
-    LFRV_KS_DISPATCH(G.dsf + 1, k_learn_input, grid2(G.W, G.H, kTile), kTile, st, G.W, G.H, G.n, G.dsf, B.BW, B.start,
-                     B.entries, tau, img, wgt, U, gx, gy, vis, static_cast<__nv_bfloat16 *>(out));
+    __nv_bfloat16 *o = static_cast<__nv_bfloat16 *>(out);
+    if (bf16)
+        learn_input_typed(G, B, tau, static_cast<const __nv_bfloat16 *>(img), static_cast<const __nv_bfloat16 *>(wgt),
+                          U, gx, gy, vis, o, st);
+    else
+        learn_input_typed(G, B, tau, static_cast<const float *>(img), static_cast<const float *>(wgt), U, gx, gy, vis,
+                          o, st);
     lc.add(1);
 }
 
@@ -1244,33 +1283,80 @@ void launch_u_gradient(const Geometry &G, const Buckets &B, const float *tau, co
     lc.add(1);
 }
 
-template <int KS>
-static void gradient_setup_ks(const Geometry &G, const Buckets &B, const float *tau, const float *img,
-                              const float *vgrad, const float *wgt, float s2, uint8_t *vis, float *U, float *gx,
+template <int KS, typename TS>
+static void gradient_setup_ks(const Geometry &G, const Buckets &B, const float *tau, const TS *img,
+                              const TS *vgrad, const TS *wgt, float s2, uint8_t *vis, float *U, float *gx,
                               float *gy, float *mask, cudaStream_t st) {
     if constexpr (KS <= 3) {
         constexpr int TXO = 33 - KS, TY = kGrWarps * 2 - (KS - 1);
         const dim3 g((G.W + TXO - 1) / TXO, (G.H + TY - 1) / TY);
-        k_gradient_setup_rows<KS><<<g, kGrWarps * 32, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau,
-                                                             img, vgrad, wgt, s2, vis, U, gx, gy, mask);
+        k_gradient_setup_rows<KS, TS><<<g, kGrWarps * 32, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries,
+                                                                 tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask);
     } else {
-        k_gradient_setup_px<KS><<<grid2(G.W, G.H, kTile), kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start,
-                                                                        B.entries, tau, img, vgrad, wgt, s2, vis, U,
-                                                                        gx, gy, mask);
+        k_gradient_setup_px<KS, TS><<<grid2(G.W, G.H, kTile), kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start,
+                                                                            B.entries, tau, img, vgrad, wgt, s2, vis,
+                                                                            U, gx, gy, mask);
     }
 }
 
-void launch_gradient_setup(const Geometry &G, const Buckets &B, const float *tau, const float *img, const float *vgrad,
-                           const float *wgt, float s2, uint8_t *vis, float *U, float *gx, float *gy, float *mask,
-                           cudaStream_t st, LaunchCounter &lc) {
-    ProfScope _ps(lc, "gradient_setup", st);
+template <typename TS>
+static void gradient_setup_typed(const Geometry &G, const Buckets &B, const float *tau, const TS *img, const TS *vgrad,
+                                 const TS *wgt, float s2, uint8_t *vis, float *U, float *gx, float *gy, float *mask,
+                                 cudaStream_t st) {
     switch (G.dsf + 1) {
-        case 2: gradient_setup_ks<2>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
-        case 3: gradient_setup_ks<3>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
-        case 4: gradient_setup_ks<4>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
-        case 5: gradient_setup_ks<5>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
+        case 2: gradient_setup_ks<2, TS>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
+        case 3: gradient_setup_ks<3, TS>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
+        case 4: gradient_setup_ks<4, TS>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
+        case 5: gradient_setup_ks<5, TS>(G, B, tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask, st); break;
         default: break;
     }
+}
+
+void launch_gradient_setup(const Geometry &G, const Buckets &B, const float *tau, const void *img, const void *vgrad,
+                           const void *wgt, float s2, uint8_t *vis, float *U, float *gx, float *gy, float *mask,
+                           cudaStream_t st, LaunchCounter &lc, bool bf16) {
+    ProfScope _ps(lc, "gradient_setup", st);
+    if (bf16)
+        gradient_setup_typed(G, B, tau, static_cast<const __nv_bfloat16 *>(img),
+                             static_cast<const __nv_bfloat16 *>(vgrad), static_cast<const __nv_bfloat16 *>(wgt), s2,
+                             vis, U, gx, gy, mask, st);
+    else
+        gradient_setup_typed(G, B, tau, static_cast<const float *>(img), static_cast<const float *>(vgrad),
+                             static_cast<const float *>(wgt), s2, vis, U, gx, gy, mask, st);
+    lc.add(1);
+}
+
+// Luminance Sobel of BF16 views into BF16 gradients (the view path of k_sobel: no mask, zero on the border).
+__global__ void k_view_sobel_bf16(int W, int H, const __nv_bfloat16 *__restrict__ rgb, size_t in_stride,
+                                  size_t ch_stride, __nv_bfloat16 *__restrict__ gx, __nv_bfloat16 *__restrict__ gy,
+                                  size_t out_stride) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    if (x >= W || y >= H) return;
+    const __nv_bfloat16 *r = rgb + (size_t)z * in_stride, *g = r + ch_stride, *b = g + ch_stride;
+    const size_t o = (size_t)y * W + x;
+    float gX = 0.f, gY = 0.f;
+    if (0 < x && x < W - 1 && 0 < y && y < H - 1) {
+        auto L = [&](int dx, int dy) {
+            const size_t q = o + (ptrdiff_t)dy * W + dx;
+            return lum(ldv(r + q), ldv(g + q), ldv(b + q));
+        };
+        const float Ypp = L(-1, -1), Ypc = L(0, -1), Ypn = L(1, -1);
+        const float Ycp = L(-1, 0), Ycn = L(1, 0);
+        const float Ynp = L(-1, 1), Ync = L(0, 1), Ynn = L(1, 1);
+        gX = (Ypn + 2.f * Ycn + Ynn - Ypp - 2.f * Ycp - Ynp) / 8.f;
+        gY = (Ynp + 2.f * Ync + Ynn - Ypp - 2.f * Ypc - Ypn) / 8.f;
+    }
+    stv(gx + (size_t)z * out_stride + o, gX);
+    stv(gy + (size_t)z * out_stride + o, gY);
+}
+
+void launch_view_sobel_bf16(int W, int H, int count, const void *rgb, size_t in_stride, size_t ch_stride, void *gx,
+                            void *gy, size_t out_stride, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "sobel", st);
+    const dim3 b(32, 8), g((W + 31) / 32, (H + 7) / 8, count);
+    k_view_sobel_bf16<<<g, b, 0, st>>>(W, H, static_cast<const __nv_bfloat16 *>(rgb), in_stride, ch_stride,
+                                       static_cast<__nv_bfloat16 *>(gx), static_cast<__nv_bfloat16 *>(gy), out_stride);
     lc.add(1);
 }
 

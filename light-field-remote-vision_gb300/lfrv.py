@@ -35,7 +35,8 @@ class Config(C.Structure):
                 ("lambda_max_factor", C.c_float), ("dw_type", C.c_int), ("gw_type", C.c_int),
                 ("dt_alpha", C.c_float), ("dt_beta", C.c_float), ("gradient_step", C.c_float),
                 ("niter", C.c_int), ("nmeta_iter", C.c_int), ("faithful", C.c_int), ("early_exit", C.c_int),
-                ("cg_max_iter", C.c_int), ("cg_gap_tol", C.c_double), ("hole_fill_iter", C.c_int)]
+                ("cg_max_iter", C.c_int), ("cg_gap_tol", C.c_double), ("hole_fill_iter", C.c_int),
+                ("bf16_storage", C.c_int)]
 
     def copy(self) -> "Config":
         c = Config()

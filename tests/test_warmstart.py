@@ -74,6 +74,13 @@ CONV_CASES = [
     (32, 16, 3, 1, 1, 24, 16),
     (64, 64, 3, 1, 1, 20, 12),
     (128, 256, 3, 2, 2, 16, 16),
+    # rows of 128 pixels: stride-1 3 x 3 forward and data gradient take the resident-tile kernel
+    (48, 32, 3, 1, 1, 8, 128),
+    (32, 32, 3, 1, 2, 4, 256),
+    (64, 64, 3, 1, 1, 6, 128),
+    (128, 128, 3, 1, 1, 4, 128),
+    (32, 16, 3, 1, 1, 4, 128),
+    (16, 32, 3, 1, 1, 2, 128),
 ]
 
 
@@ -126,7 +133,7 @@ def _rel_l2(a, b):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("B,H,W", [(2, 16, 16), (1, 24, 32)])
+@pytest.mark.parametrize("B,H,W", [(2, 16, 16), (1, 24, 32), (1, 8, 128)])
 def test_network_gradients_match_oracle(net, B, H, W):
     torch = _cuda()
     rng = np.random.default_rng(B * 100 + H)
