@@ -41,6 +41,9 @@ WORKLOADS = {
                                             "(dsf 1 or 2), IBR_gradient + CG to gap 1e-4, one lfrv_render_views_dev call"),
     "c2": dict(preset=2, algorithm=1, name="5x5 LF 512^2 -> 1024^2 (dsf 2), 24 views, IBR_gradient + CG to gap 1e-4"),
     "c1": dict(preset=1, algorithm=0, name="3x3 LF 256^2, 8 views, IBR_color primal-dual TV, 300 x 300 iterations"),
+    "c5": dict(preset=2, algorithm=1, name="full pipeline: 9x9 LF of 1024^2 views (80 inputs, point-sampled renders, "
+                                            "5 planes + 20 bumps) -> 32 targets of 2048^2 (dsf 2), IBR_gradient + CG to "
+                                            "gap 1e-4; BF16 stacks + learned warm start + batched vs plain FP32"),
     "c4": dict(preset=1, algorithm=1, name="learned warm start: 3x3 LF 512^2 (8 views, 3 planes + 20 bumps), "
                                             "IBR_gradient + CG to gap 1e-4 seeded by the encoder-decoder trained in "
                                             "the run, 16 held-out targets per step, batched"),
@@ -437,6 +440,144 @@ def run_warm(args, rank: int, world: int) -> None:
     ctx.close()
 
 
+def run_full(args, rank: int, world: int) -> None:
+    """Full pipeline (c5): one 9x9 light field, 32 target cameras around the centre, every arm timed over the 32
+    targets: plain FP32 one at a time, plain FP32 batched, BF16 stacks batched, BF16 + learned warm start batched.
+    The network is trained in the run on 512^2 crops of 4 other targets' 2048^2 features (untimed)."""
+    import copy
+    import torch
+    import lfrv
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    wl = WORKLOADS[args.workload]
+    t_gen = time.time()
+    p = lfrv.scene_params(2, w=1024, h=1024, grid=9, dsf=2, ss=1, seed=7000)
+    sc = lfrv.synth_scene(p)
+    t_gen = time.time() - t_gen
+    V = sc.views.shape[0]
+    H, W = sc.gt.shape[1], sc.gt.shape[2]
+
+    def shifted(i, n_side, scale):
+        t = copy.copy(sc.target)
+        t.t[0] = sc.target.t[0] + ((i % n_side) - (n_side - 1) / 2) * scale * p.baseline
+        t.t[1] = sc.target.t[1] + ((i // n_side) - (n_side - 1) / 2) * scale * p.baseline
+        return t
+
+    targets = [copy.copy(sc.target)] + [shifted(i, 6, 0.08) for i in range(31)]  # the rendered centre first
+    train_targets = [shifted(i, 2, 0.37) for i in range(4)]
+    ctx = lfrv.Context(dev)
+
+    def cfg_of(tol, bf16):
+        return lfrv.default_config(w=p.w, h=p.h, dsf=p.dsf, nviews=V, nchannels=3, sigma_sensor=0.005, lambda_=0.05,
+                                   faithful=0, cg_gap_tol=tol, cg_max_iter=500, hole_fill_iter=500,
+                                   bf16_storage=1 if bf16 else 0)
+
+    views = torch.from_numpy(sc.views).cuda()
+    views_bf16 = views.to(torch.bfloat16)
+    depth = torch.from_numpy(sc.depth).cuda()
+    sc.views = None  # the host copy is no longer needed
+    # training data for the network: features of 4 targets at 2048^2, random 512^2 crops
+    t_feat = time.time()
+    X = torch.zeros((len(train_targets), H, W, 48), dtype=torch.bfloat16, device="cuda")
+    U0 = torch.zeros((len(train_targets), 3, H, W), device="cuda")
+    S = torch.zeros((len(train_targets), 3, H, W), device="cuda")
+    torch.cuda.synchronize()
+    for i, t in enumerate(train_targets):
+        ctx.warmstart_features_dev(cfg_of(1e-6, True), views_bf16.data_ptr(), depth.data_ptr(), sc.cams, t,
+                                   X[i].data_ptr(), U0[i].data_ptr(), S[i].data_ptr())
+    torch.cuda.synchronize()
+    t_feat = time.time() - t_feat
+    net = lfrv.WarmStart(ctx, seed=1)
+    rng = np.random.default_rng(0)
+    steps, bs, crop = 1000, 4, 512
+    t_train = time.time()
+    for step in range(steps):
+        ii = rng.integers(0, len(train_targets), bs)
+        ys = rng.integers(0, (H - crop) // 8 + 1, bs) * 8
+        xs = rng.integers(0, (W - crop) // 8 + 1, bs) * 8
+        xb = torch.stack([X[i, y:y + crop, x:x + crop] for i, y, x in zip(ii, ys, xs)]).contiguous()
+        ub = torch.stack([U0[i, :, y:y + crop, x:x + crop] for i, y, x in zip(ii, ys, xs)]).contiguous()
+        sb = torch.stack([S[i, :, y:y + crop, x:x + crop] for i, y, x in zip(ii, ys, xs)]).contiguous()
+        torch.cuda.synchronize()
+        net.train_step_dev(bs, crop, crop, xb.data_ptr(), ub.data_ptr(), sb.data_ptr(), 5e-4)
+    torch.cuda.synchronize()
+    t_train = time.time() - t_train
+    del X, U0, S
+    cfg32, cfg16 = cfg_of(1e-4, False), cfg_of(1e-4, True)
+    outs = {k: [torch.empty((3, H, W), device="cuda") for _ in targets]
+            for k in ("plain_single", "plain_batched", "bf16_batched", "bf16_warm_batched")}
+
+    def jobs(name, cfg, vp):
+        return [dict(cfg=cfg, algorithm=1, d_views=vp, d_depth=depth.data_ptr(), cams=sc.cams, target=t,
+                     d_out=outs[name][i].data_ptr()) for i, t in enumerate(targets)]
+
+    j_ps = jobs("plain_single", cfg32, views.data_ptr())
+    j_pb = jobs("plain_batched", cfg32, views.data_ptr())
+    j_bb = jobs("bf16_batched", cfg16, views_bf16.data_ptr())
+    j_wb = jobs("bf16_warm_batched", cfg16, views_bf16.data_ptr())
+    arms = (("plain_single", lambda: [ctx.render_view_dev(j["cfg"], 1, j["d_views"], j["d_depth"], j["cams"],
+                                                          j["target"], j["d_out"]) for j in j_ps]),
+            ("plain_batched", lambda: ctx.render_views_dev(j_pb)),
+            ("bf16_batched", lambda: ctx.render_views_dev(j_bb)),
+            ("bf16_warm_batched", lambda: ctx.render_views_dev(j_wb, net)))
+    results = {}
+    torch.cuda.synchronize()
+    for name, fn in arms:
+        for _ in range(max(args.warmup, 3)):
+            st = fn()
+        torch.cuda.synchronize()
+        if name == "bf16_warm_batched":
+            clk_path = tempfile.mktemp(prefix="lfrv_clocks_")
+            clk = sample_clocks(clk_path)
+            l0 = ctx.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            st = fn()
+        e1.record()
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        if name == "bf16_warm_batched":
+            launches = ctx.launch_count() - l0
+            clk.terminate()
+            clk.wait()
+            clocks = summarize_clocks(clk_path)
+        results[name] = dict(views_per_s=len(targets) * args.steps / sec,
+                             cg_iterations=int(sum(s.outer_iterations for s in st)),
+                             max_gap=float(max(s.gap for s in st)))
+    # per-target error of each arm against the plain FP32 solution, and the centre target's PSNR to the render
+    ref = [o.cpu().numpy() for o in outs["plain_single"]]
+    for name in ("plain_batched", "bf16_batched", "bf16_warm_batched"):
+        got = [o.cpu().numpy() for o in outs[name]]
+        results[name]["max_abs_vs_plain_fp32"] = float(max(np.abs(a - b).max() for a, b in zip(got, ref)))
+        results[name]["psnr_vs_plain_fp32_min_db"] = float(min(lfrv.psnr(a, b) for a, b in zip(got, ref)))
+    psnr_gt = {name: lfrv.psnr(outs[name][0].cpu().numpy(), sc.gt) for name in outs}
+    if rank == 0:
+        wb = results["bf16_warm_batched"]
+        line = {"metric": "views/sec to energy gap <=1e-4", "value": world * wb["views_per_s"], "unit": "views/s",
+                "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+                "ms_per_step": 1e3 * len(targets) / wb["views_per_s"], "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "bf16 stacks, f32 iterates, f64 dots",
+                "data": "synthetic (seeded planes + bumps light field)",
+                "config": {"workload": wl["name"], "views": V, "input": [p.h, p.w], "target": [H, W],
+                           "targets_per_step": len(targets), "scene_generation_seconds": round(t_gen, 1),
+                           "features_seconds": round(t_feat, 2), "train_seconds": round(t_train, 2),
+                           "train": f"{steps} Adam steps of {bs} random {crop}^2 crops of 4 other targets' features",
+                           "modes": results, "psnr_to_render_centre_target": psnr_gt,
+                           "warm_bf16_batched_vs_plain_fp32_single":
+                               wb["views_per_s"] / results["plain_single"]["views_per_s"],
+                           "bf16_batched_vs_plain_fp32_single":
+                               results["bf16_batched"]["views_per_s"] / results["plain_single"]["views_per_s"],
+                           "inputs": "1024^2 views rendered point-sampled (no 2x supersampling) to bound the host "
+                                     "scene generation",
+                           "l2": "32 targets of 2048^2 from 80 views of 1024^2 exceed L2 (no flush needed)"},
+                "clocks": clocks, "gpu_launches": launches, "roofline": None, "cpu_baseline": None}
+        print(json.dumps(line), flush=True)
+    net.close()
+    ctx.close()
+
+
 def run_ours(args, rank: int, world: int) -> None:
     import torch
     import lfrv
@@ -581,6 +722,8 @@ def main() -> None:
         run_batch(args, rank, world)
     elif args.workload == "c4":
         run_warm(args, rank, world)
+    elif args.workload == "c5":
+        run_full(args, rank, world)
     else:
         run_ours(args, rank, world)
     if world > 1:
