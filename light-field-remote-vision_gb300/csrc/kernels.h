@@ -227,6 +227,9 @@ struct WgradGemm {
     float *partial;
 };
 cudaError_t launch_conv_tc(const ConvGemm &g, int *err, cudaStream_t st, LaunchCounter &lc);
+// Kernel choice of launch_conv_tc: 0 TMA / resident tile / gather as they apply, 1 without the TMA kernel, 2 the
+// gather kernel only (process-wide).
+void set_conv_kernel_pref(int pref);
 cudaError_t launch_wgrad_tc(const WgradGemm &g, int splits, int Cout_real, float *grad, int *err, cudaStream_t st,
                             LaunchCounter &lc);
 cudaError_t launch_bias_grad(int P, int C, int Creal, const void *dy, float *partial, int blocks, float *out,

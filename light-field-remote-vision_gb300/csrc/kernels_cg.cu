@@ -1142,9 +1142,8 @@ cudaError_t launch_cg_batch(const CgProblem *d_probs, const int *d_block_prob, i
     return cudaLaunchCooperativeKernel((const void *)k_cg_batch, dim3(blocks), dim3(kPersistThreads), args, 0, st);
 }
 
-bool encode_tensor_map_3d(CUtensorMap *map, const float *base, int cols, int rows, int planes, int box_x, int box_y,
-                          int box_z) {
-    static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+void *tensor_map_encoder() {
+    static void *encode = nullptr;
     static std::once_flag once;
     std::call_once(once, [] {
         void *fn = nullptr;
@@ -1152,9 +1151,15 @@ bool encode_tensor_map_3d(CUtensorMap *map, const float *base, int cols, int row
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
-            encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+            encode = fn;
         cudaGetLastError();
     });
+    return encode;
+}
+
+bool encode_tensor_map_3d(CUtensorMap *map, const float *base, int cols, int rows, int planes, int box_x, int box_y,
+                          int box_z) {
+    const auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tensor_map_encoder());
     if (!encode || !base || cols <= 0 || rows <= 0 || planes <= 0) return false;
     if (((size_t)cols * sizeof(float)) % 16 != 0 || reinterpret_cast<uintptr_t>(base) % 16 != 0) return false;
     const cuuint64_t dims[3] = {(cuuint64_t)cols, (cuuint64_t)rows, (cuuint64_t)planes};

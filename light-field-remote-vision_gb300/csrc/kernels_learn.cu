@@ -16,8 +16,10 @@
 // byte offset), 8-row groups 1 KB apart (stride byte offset); one MMA (K = 16) reads two core matrices along K, so
 // the descriptor start advances 256 B per MMA.
 #include <algorithm>
+#include <atomic>
 
 #include <cuda_bf16.h>
+#include <cudaTypedefs.h>
 #include <stdint.h>
 
 #include "device_common.cuh"
@@ -488,6 +490,167 @@ __global__ void __launch_bounds__(kThreads) k_conv_tile_tc(const ConvGemm g, int
     if (warp == 0) tmem_free(tmem, kCols);
 }
 
+// TMA-fed convolution with warp-specialised roles. A CTA owns a patch of bh x bw = 128 output pixels of one image
+// (one row of 128, or 128 / Wo whole rows) and BN output channels. The K loop runs over (tap, 64-channel block):
+// per stage, one thread issues a strided 4-D TMA box of the activations (64 channels x the patch's input pixels,
+// element stride = the convolution stride; padding and channels past C arrive as zeros) and a 2-D box of the
+// weights, both 128-byte swizzled, onto a full mbarrier with the stage's byte count. A second thread waits for the
+// stage, issues its four K = 16 MMAs and commits them to the stage's empty mbarrier, which releases the slot to the
+// producer. After the last stage the MMA thread commits to `done`, and the four warps read the accumulator.
+// Forward convolutions of stride 1 or 2 (3 x 3 or 1 x 1) and the data gradient of stride-1 layers (taps mirrored).
+constexpr int kTmaStages = 4;
+
+// K-major operand in the 128-byte swizzle: 128-byte rows (64 bf16), 8-row atoms of 1 KB (stride byte offset),
+// layout type 2 in bits 61-63; successive K = 16 slices start 32 B apart inside the atom.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)1 << 16;
+    d |= (uint64_t)(1024 >> 4) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+template <int BN>
+__global__ void __launch_bounds__(kThreads) k_conv_tma(const ConvGemm g, const __grid_constant__ CUtensorMap mapA,
+                                                       const __grid_constant__ CUtensorMap mapB, int bw, int bh,
+                                                       int cblocks, int *err) {
+    extern __shared__ uint8_t dsm[];
+    constexpr int kA = kBM * 128, kStage = kA + BN * 128;
+    constexpr int kCols = BN < 32 ? 32 : BN;
+    __shared__ __align__(8) uint64_t full[kTmaStages], empty[kTmaStages], done;
+    __shared__ uint32_t tmem_slot;
+    __shared__ int s_fail;
+    uint8_t *base = align1024(dsm);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int pxn = g.Wo / bw, pyn = g.Ho / bh;
+    int blk = blockIdx.x;
+    const int pxi = blk % pxn;
+    blk /= pxn;
+    const int pyi = blk % pyn, b = blk / pyn;
+    const int ox0 = pxi * bw, oy0 = pyi * bh, n0 = blockIdx.y * BN;
+    const int nk = g.ks * g.ks * cblocks;
+    if (warp == 0) tmem_alloc(&tmem_slot, kCols);
+    if (tid == 0) {
+        for (int s = 0; s < kTmaStages; ++s) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(&done, 1);
+        s_fail = 0;
+        fence_proxy_async_smem();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_slot;
+    if (warp == 0 && lane == 0) {
+        // producer
+        for (int kt = 0; kt < nk; ++kt) {
+            const int slot = kt % kTmaStages, use = kt / kTmaStages;
+            if (kt >= kTmaStages && !mbar_wait(&empty[slot], (use - 1) & 1, kSpinLimit)) {
+                s_fail = 1;
+                atomicExch(err, 1);
+                break;
+            }
+            const int tap = kt / cblocks, cb = kt - tap * cblocks;
+            int sx = ox0 * g.stride, sy = oy0 * g.stride;
+            if (g.ks == 3) {
+                const int ky = tap / 3, kx = tap - 3 * (tap / 3);
+                if (!g.dgrad) {
+                    sx += kx - 1;
+                    sy += ky - 1;
+                } else {
+                    sx = ox0 + 1 - kx;
+                    sy = oy0 + 1 - ky;
+                }
+            }
+            uint8_t *sa = base + slot * kStage;
+            mbar_arrive_expect_tx(&full[slot], (unsigned)kStage);
+            tma_load_4d(sa, &mapA, cb * 64, sx, sy, b, &full[slot]);
+            tma_load_2d(sa + kA, &mapB, tap * g.C + cb * 64, n0, &full[slot]);
+        }
+    } else if (warp == 1 && lane == 0) {
+        // MMA issuer
+        const uint32_t idesc = idesc_bf16_f32(kBM, BN);
+        for (int kt = 0; kt < nk; ++kt) {
+            const int slot = kt % kTmaStages, use = kt / kTmaStages;
+            if (!mbar_wait(&full[slot], use & 1, kSpinLimit)) {
+                s_fail = 1;
+                atomicExch(err, 1);
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a = smem_u32(base + slot * kStage), bb = a + kA;
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                tc_mma(tmem, smem_desc_sw128(a + 32 * k), smem_desc_sw128(bb + 32 * k), idesc, (kt > 0 || k > 0) ? 1 : 0);
+            tc_commit(&empty[slot]);
+        }
+        tc_commit(&done);  // arrives once every MMA issued above has completed
+    }
+    __syncthreads();
+    if (!mbar_wait(&done, 0, kSpinLimit)) {
+        s_fail = 1;
+        atomicExch(err, 1);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (!s_fail) {
+        const int m = warp * 32 + lane;
+        const int oy = oy0 + m / bw, ox = ox0 + m % bw;
+        const size_t row = ((size_t)b * g.Ho + oy) * g.Wo + ox;
+#pragma unroll 1
+        for (int c0 = 0; c0 < BN; c0 += 16) {
+            float v[16];
+            tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+            const size_t o = row * g.N + n0 + c0;
+            if (g.bias) {
+#pragma unroll
+                for (int k = 0; k < 16; ++k) v[k] += __ldg(g.bias + n0 + c0 + k);
+            }
+            if (g.add) {
+                const uint4 *ap = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.add) + o);
+                float tt[8];
+                unpack8(ap[0], tt);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) v[k] += tt[k];
+                unpack8(ap[1], tt);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) v[8 + k] += tt[k];
+            }
+            if (g.relu) {
+#pragma unroll
+                for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.f);
+            }
+            if (g.mask) {
+                const uint4 *mp = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.mask) + o);
+                float tt[8];
+                unpack8(mp[0], tt);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) v[k] = tt[k] > 0.f ? v[k] : 0.f;
+                unpack8(mp[1], tt);
+#pragma unroll
+                for (int k = 0; k < 8; ++k) v[8 + k] = tt[k] > 0.f ? v[8 + k] : 0.f;
+            }
+            if (g.outf) {
+                float4 *fp = reinterpret_cast<float4 *>(g.outf + o);
+#pragma unroll
+                for (int k = 0; k < 4; ++k) fp[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+            }
+            if (g.outb) {
+                uint4 *bp = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(g.outb) + o);
+                bp[0] = pack8(v);
+                bp[1] = pack8(v + 8);
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0) tmem_free(tmem, kCols);
+}
+
 // Weight gradient: GEMM rows are the (tap, ci) rows of dW^T (padded to 128), N = the stored output channels, the
 // reduction runs over the output pixels of this split. Both operands are pixel-major in global memory, so each
 // 16-byte load (8 channels of one pixel) is written transposed into a column of a core matrix. Double-buffered:
@@ -847,9 +1010,99 @@ static cudaError_t launch_tile(const ConvGemm &g, int R, int BN, int smem, int *
     return cudaErrorInvalidValue;
 }
 
+// Patch of the TMA kernel (bw x bh = 128 output pixels), or false when the layer does not tile that way or is a
+// data gradient of stride 2.
+static bool tma_shape(const ConvGemm &g, int &bw, int &bh) {
+    if (g.ks != 1 && g.ks != 3) return false;
+    if (g.dgrad && g.stride != 1) return false;
+    if (g.C % 8 || g.C < 8) return false;
+    if (g.Wo >= 128) {
+        if (g.Wo % 128) return false;
+        bw = 128;
+        bh = 1;
+    } else {
+        if (128 % g.Wo) return false;
+        bw = g.Wo;
+        bh = 128 / g.Wo;
+        if (g.Ho % bh) return false;
+    }
+    const int s = g.dgrad ? 1 : g.stride;
+    return bw * s <= 256 && bh * s <= 256;
+}
+
+// Activation map: dims (C, W, H, batch) of NHWC BF16, box (64, bw s, bh s, 1) with element strides (1, s, s, 1);
+// weight map: dims (ldw, N), box (64, BN). Both with the 128-byte swizzle and zero fill outside the tensor.
+static bool encode_conv_maps(const ConvGemm &g, int bw, int bh, int BN, CUtensorMap *mA, CUtensorMap *mB) {
+    const auto encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(tensor_map_encoder());
+    if (!encode) return false;
+    const int s = g.dgrad ? 1 : g.stride;
+    const cuuint64_t adims[4] = {(cuuint64_t)g.C, (cuuint64_t)g.Ws, (cuuint64_t)g.Hs, (cuuint64_t)g.batch};
+    const cuuint64_t astr[3] = {(cuuint64_t)g.C * 2, (cuuint64_t)g.Ws * g.C * 2, (cuuint64_t)g.Hs * g.Ws * g.C * 2};
+    const cuuint32_t abox[4] = {64, (cuuint32_t)(bw * s), (cuuint32_t)(bh * s), 1};
+    const cuuint32_t aes[4] = {1, (cuuint32_t)s, (cuuint32_t)s, 1};
+    if (encode(mA, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4, const_cast<void *>(g.src), adims, astr, abox, aes,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return false;
+    const cuuint64_t bdims[2] = {(cuuint64_t)g.ldw, (cuuint64_t)g.N};
+    const cuuint64_t bstr[1] = {(cuuint64_t)g.ldw * 2};
+    const cuuint32_t bbox[2] = {64, (cuuint32_t)BN};
+    const cuuint32_t bes[2] = {1, 1};
+    return encode(mB, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void *>(g.wt), bdims, bstr, bbox, bes,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+template <int BN>
+static cudaError_t tma_launch(const ConvGemm &g, int bw, int bh, const CUtensorMap &mA, const CUtensorMap &mB, int *err,
+                              cudaStream_t st) {
+    constexpr int smem = kTmaStages * (kBM * 128 + BN * 128) + 1024;
+    static bool attr = false;
+    if (!attr) {
+        const cudaError_t e = cudaFuncSetAttribute(k_conv_tma<BN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
+    const int cblocks = (g.C + 63) / 64;
+    const dim3 grid(g.batch * (g.Ho / bh) * (g.Wo / bw), g.N / BN);
+    k_conv_tma<BN><<<grid, kThreads, smem, st>>>(g, mA, mB, bw, bh, cblocks, err);
+    return cudaGetLastError();
+}
+
+// Which convolution kernel a layer uses: the TMA kernel where its patch tiling applies, else the resident-tile
+// kernel (stride-1 3 x 3 on 128-pixel rows), else the cp.async gather. The preference (0 all, 1 no TMA kernel,
+// 2 the gather only) restricts the choice; a kernel that does not apply falls through to the next.
+static std::atomic<int> g_conv_pref{1};
+void set_conv_kernel_pref(int pref) { g_conv_pref.store(pref); }
+static int conv_kernel_pref() { return g_conv_pref.load(); }
+
 cudaError_t launch_conv_tc(const ConvGemm &g, int *err, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, g.dgrad ? "conv_dgrad_tc" : "conv_fwd_tc", st);
+    if (g.N != 16 && g.N != 32 && g.N != 64 && g.N != 128 && g.N != 256) return cudaErrorInvalidValue;
+    const int pref = conv_kernel_pref();
     {
+        int bw = 0, bh = 0;
+        CUtensorMap mA, mB;
+        int bn = g.N;
+        if (pref == 0 && tma_shape(g, bw, bh)) {
+            const int mtiles = g.batch * (g.Ho / bh) * (g.Wo / bw);
+            while (bn > 32 && mtiles * (g.N / bn) < 120) bn >>= 1;
+        }
+        // a map the driver does not accept sends the layer to the other kernels
+        if (pref == 0 && bw > 0 && encode_conv_maps(g, bw, bh, bn, &mA, &mB)) {
+            cudaError_t e;
+            switch (bn) {
+                case 16: e = tma_launch<16>(g, bw, bh, mA, mB, err, st); break;
+                case 32: e = tma_launch<32>(g, bw, bh, mA, mB, err, st); break;
+                case 64: e = tma_launch<64>(g, bw, bh, mA, mB, err, st); break;
+                case 128: e = tma_launch<128>(g, bw, bh, mA, mB, err, st); break;
+                default: e = tma_launch<256>(g, bw, bh, mA, mB, err, st); break;
+            }
+            lc.add(1);
+            return e;
+        }
+    }
+    if (pref <= 1) {
         int R = 0, BN = 0, smem = 0;
         if (tile_shape(g, R, BN, smem)) {
             const cudaError_t e = launch_tile(g, R, BN, smem, err, st);

@@ -554,6 +554,12 @@ extern "C" int lfrv_warmstart_train_step_dev(lfrv_warmstart *net, int batch, int
     LFRV_API_END
 }
 
+extern "C" int lfrv_set_conv_kernel(int which) {
+    if (which < 0 || which > 2) return fail(LFRV_E_ARG, "conv kernel choice must be 0, 1 or 2 (got %d)", which);
+    set_conv_kernel_pref(which);
+    return LFRV_OK;
+}
+
 extern "C" int lfrv_conv_bf16_dev(lfrv_ctx *ctx, int mode, int batch, int H, int W, int Cin, int Cout, int ks,
                                   int stride, const void *d_x, const void *d_dy, const float *d_w, float *d_out) {
     LFRV_API_BEGIN

@@ -101,6 +101,7 @@ EXPORTED = [
     "lfrv_warmstart_param_count", "lfrv_warmstart_create", "lfrv_warmstart_destroy", "lfrv_warmstart_get_params",
     "lfrv_warmstart_set_params", "lfrv_warmstart_features_dev", "lfrv_warmstart_forward_dev",
     "lfrv_warmstart_train_step_dev", "lfrv_warmstart_gradients_dev", "lfrv_render_view_warm_dev", "lfrv_render_views_warm_dev", "lfrv_conv_bf16_dev",
+    "lfrv_set_conv_kernel",
     "lfrv_stage_weights",
     "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
@@ -511,6 +512,11 @@ class Context:
 WARMSTART_CHANNELS = 48
 
 
+def set_conv_kernel(which: int) -> None:
+    """0: TMA, resident-tile or gather kernel as they apply; 1 (default): no TMA kernel; 2: gather only."""
+    _check(LIB.lfrv_set_conv_kernel(which))
+
+
 def warmstart_param_count() -> int:
     return int(LIB.lfrv_warmstart_param_count())
 
@@ -624,6 +630,7 @@ def _declare() -> None:
     LIB.lfrv_render_view_warm_dev.argtypes = [vp, vp, C.POINTER(Config), vp, vp, C.POINTER(Camera),
                                               C.POINTER(Camera), vp, C.POINTER(Stats)]
     LIB.lfrv_render_views_warm_dev.argtypes = [vp, vp, C.POINTER(ViewJob), C.c_int]
+    LIB.lfrv_set_conv_kernel.argtypes = [C.c_int]
     LIB.lfrv_conv_bf16_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                        vp, vp, vp, vp]
 

@@ -81,13 +81,26 @@ CONV_CASES = [
     (128, 128, 3, 1, 1, 4, 128),
     (32, 16, 3, 1, 1, 4, 128),
     (16, 32, 3, 1, 1, 2, 128),
+    # patches of 128 pixels over several rows (W < 128): the TMA kernel, stride 1 and 2, 3 x 3 and 1 x 1
+    (32, 64, 3, 2, 1, 32, 32),
+    (64, 128, 3, 2, 1, 64, 32),
+    (256, 128, 1, 1, 1, 16, 8),
+    (128, 32, 3, 1, 2, 16, 8),
+    (16, 32, 3, 1, 1, 32, 4),
 ]
+
+
+@pytest.fixture(params=[0, 1, 2], ids=["tma", "tile", "gather"])
+def conv_kernel(request):
+    lfrv.set_conv_kernel(request.param)
+    yield request.param
+    lfrv.set_conv_kernel(1)
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("case", CONV_CASES)
 @pytest.mark.parametrize("mode", [0, 1, 2])
-def test_conv_matches_oracle(ctx, case, mode):
+def test_conv_matches_oracle(ctx, case, mode, conv_kernel):
     torch = _cuda()
     Cin, Cout, ks, s, B, H, W = case
     if mode == 1 and Cin not in (16, 32, 64, 128, 256):
