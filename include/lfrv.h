@@ -286,9 +286,9 @@ int lfrv_render_views_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_vi
 int lfrv_conv_bf16_dev(lfrv_ctx *ctx, int mode, int batch, int H, int W, int Cin, int Cout, int ks, int stride,
                        const void *d_x, const void *d_dy, const float *d_w, float *d_out);
 /* Which tensor-core convolution kernels the network's layers may use (process-wide; all give the same results to
- * within FP32 summation order): 0 the TMA-fed kernel where its 128-pixel patch tiling applies, else the
- * resident-tile kernel (stride-1 3 x 3 on rows of a multiple of 128), else the cp.async gather; 1 (default) the
- * last two; 2 the gather only. */
+ * within FP32 summation order): 0 (default) the TMA-fed kernel where its 128-pixel patch tiling applies, else
+ * the resident-tile kernel (stride-1 3 x 3 on rows of a multiple of 128), else the cp.async gather; 1 the last
+ * two; 2 the gather only. */
 int lfrv_set_conv_kernel(int which);
 
 /* ---------------------------------------------------------------- stage calls

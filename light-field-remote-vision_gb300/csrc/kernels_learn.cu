@@ -1072,7 +1072,7 @@ static cudaError_t tma_launch(const ConvGemm &g, int bw, int bh, const CUtensorM
 // Which convolution kernel a layer uses: the TMA kernel where its patch tiling applies, else the resident-tile
 // kernel (stride-1 3 x 3 on 128-pixel rows), else the cp.async gather. The preference (0 all, 1 no TMA kernel,
 // 2 the gather only) restricts the choice; a kernel that does not apply falls through to the next.
-static std::atomic<int> g_conv_pref{1};
+static std::atomic<int> g_conv_pref{0};
 void set_conv_kernel_pref(int pref) { g_conv_pref.store(pref); }
 static int conv_kernel_pref() { return g_conv_pref.load(); }
 
@@ -1084,12 +1084,13 @@ cudaError_t launch_conv_tc(const ConvGemm &g, int *err, cudaStream_t st, LaunchC
         int bw = 0, bh = 0;
         CUtensorMap mA, mB;
         int bn = g.N;
-        if (pref == 0 && tma_shape(g, bw, bh)) {
+        const bool tma = pref == 0 && tma_shape(g, bw, bh);
+        if (tma) {
             const int mtiles = g.batch * (g.Ho / bh) * (g.Wo / bw);
             while (bn > 32 && mtiles * (g.N / bn) < 120) bn >>= 1;
         }
         // a map the driver does not accept sends the layer to the other kernels
-        if (pref == 0 && bw > 0 && encode_conv_maps(g, bw, bh, bn, &mA, &mB)) {
+        if (tma && encode_conv_maps(g, bw, bh, bn, &mA, &mB)) {
             cudaError_t e;
             switch (bn) {
                 case 16: e = tma_launch<16>(g, bw, bh, mA, mB, err, st); break;

@@ -513,7 +513,7 @@ WARMSTART_CHANNELS = 48
 
 
 def set_conv_kernel(which: int) -> None:
-    """0: TMA, resident-tile or gather kernel as they apply; 1 (default): no TMA kernel; 2: gather only."""
+    """0 (default): TMA, resident-tile or gather kernel as they apply; 1: no TMA kernel; 2: gather only."""
     _check(LIB.lfrv_set_conv_kernel(which))
 
 

@@ -20,10 +20,13 @@ def main() -> None:
     ap.add_argument("--batch", type=int, default=4)
     ap.add_argument("--reps", type=int, default=10)
     ap.add_argument("--no-train", action="store_true")
+    ap.add_argument("--conv-kernel", type=int, default=None, help="lfrv_set_conv_kernel choice (0, 1, 2)")
     args = ap.parse_args()
     import torch
     import lfrv
 
+    if args.conv_kernel is not None:
+        lfrv.set_conv_kernel(args.conv_kernel)
     ctx = lfrv.Context(0)
     net = lfrv.WarmStart(ctx, seed=1)
     H = W = args.size
