@@ -213,6 +213,9 @@ struct ConvGemm {
     const void *add, *mask;
     float *outf;
     void *outb;
+    // nearest-upsampling fusion (1 x 1 decoder layers): with upskip set, each output pixel's value v is written as
+    // relu(v + upskip) to its 2 x 2 block of outb at (2 Ho) x (2 Wo), upskip being a BF16 tensor of that size
+    const void *upskip;
 };
 // Weight gradient of a convolution with input x (Cin channels, Hx x Wx) and output gradient dy (Cout stored
 // channels, Ho x Wo): rows (tap, ci) of dW^T padded to Mpad, the pixels split into chunks (a multiple of 64),

@@ -151,6 +151,84 @@ __device__ __forceinline__ bool conv_src(const ConvGemm &g, int y, int x, int ky
     return iy >= 0 && iy < g.Hs && ix >= 0 && ix < g.Ws;
 }
 
+// Epilogue of 16 accumulator columns (col .. col + 15) of GEMM row `row` (an output pixel, row-major over batch,
+// Ho, Wo): + bias, + add, ReLU, zero where mask <= 0, then the FP32 and / or BF16 stores. With upskip the row's
+// value goes, as relu(v + skip), to its 2 x 2 block of the doubled-resolution BF16 output.
+__device__ __forceinline__ void conv_store16(const ConvGemm &g, size_t row, int col, float v[16]) {
+    const size_t o = row * g.N + col;
+    if (g.bias) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] += __ldg(g.bias + col + k);
+    }
+    if (g.add) {
+        const uint4 *ap = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.add) + o);
+        float tt[8];
+        unpack8(ap[0], tt);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] += tt[k];
+        unpack8(ap[1], tt);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[8 + k] += tt[k];
+    }
+    if (g.upskip) {
+        const size_t HW = (size_t)g.Ho * g.Wo;
+        const size_t b = row / HW, rem = row - b * HW;
+        const int y = (int)(rem / g.Wo), x = (int)(rem - (size_t)y * g.Wo);
+        const __nv_bfloat16 *sk = static_cast<const __nv_bfloat16 *>(g.upskip);
+        __nv_bfloat16 *out = static_cast<__nv_bfloat16 *>(g.outb);
+        size_t oo[4];
+        uint4 sv[8];
+        // all eight skip loads in flight before the first store
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            const size_t hr = (b * 2 * g.Ho + 2 * y + (d >> 1)) * (size_t)(2 * g.Wo) + 2 * x + (d & 1);
+            oo[d] = hr * g.N + col;
+            const uint4 *sp = reinterpret_cast<const uint4 *>(sk + oo[d]);
+            sv[2 * d] = __ldg(sp);
+            sv[2 * d + 1] = __ldg(sp + 1);
+        }
+#pragma unroll
+        for (int d = 0; d < 4; ++d) {
+            float a[8], c[8], w0[8], w1[8];
+            unpack8(sv[2 * d], a);
+            unpack8(sv[2 * d + 1], c);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+                w0[k] = fmaxf(v[k] + a[k], 0.f);
+                w1[k] = fmaxf(v[8 + k] + c[k], 0.f);
+            }
+            uint4 *bp = reinterpret_cast<uint4 *>(out + oo[d]);
+            bp[0] = pack8(w0);
+            bp[1] = pack8(w1);
+        }
+        return;
+    }
+    if (g.relu) {
+#pragma unroll
+        for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.f);
+    }
+    if (g.mask) {
+        const uint4 *mp = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.mask) + o);
+        float tt[8];
+        unpack8(mp[0], tt);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[k] = tt[k] > 0.f ? v[k] : 0.f;
+        unpack8(mp[1], tt);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) v[8 + k] = tt[k] > 0.f ? v[8 + k] : 0.f;
+    }
+    if (g.outf) {
+        float4 *fp = reinterpret_cast<float4 *>(g.outf + o);
+#pragma unroll
+        for (int k = 0; k < 4; ++k) fp[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
+    }
+    if (g.outb) {
+        uint4 *bp = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(g.outb) + o);
+        bp[0] = pack8(v);
+        bp[1] = pack8(v + 8);
+    }
+}
+
 }  // namespace
 
 // One CTA: 128 GEMM rows (pixels) x BN output channels (columns n0 = blockIdx.y * BN ..), K in 64-wide stages through a kStages-deep
@@ -277,45 +355,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_tc(const ConvGemm g, int *err
             float v[16];
             tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
             if (!row_ok) continue;
-            const size_t o = (size_t)m * g.N + n0 + c0;
-            if (g.bias) {
-#pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] += __ldg(g.bias + n0 + c0 + i);
-            }
-            if (g.add) {
-                const uint4 *ap = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.add) + o);
-                float t[8];
-                unpack8(ap[0], t);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) v[i] += t[i];
-                unpack8(ap[1], t);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) v[8 + i] += t[i];
-            }
-            if (g.relu) {
-#pragma unroll
-                for (int i = 0; i < 16; ++i) v[i] = fmaxf(v[i], 0.f);
-            }
-            if (g.mask) {
-                const uint4 *mp = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.mask) + o);
-                float t[8];
-                unpack8(mp[0], t);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) v[i] = t[i] > 0.f ? v[i] : 0.f;
-                unpack8(mp[1], t);
-#pragma unroll
-                for (int i = 0; i < 8; ++i) v[8 + i] = t[i] > 0.f ? v[8 + i] : 0.f;
-            }
-            if (g.outf) {
-                float4 *fp = reinterpret_cast<float4 *>(g.outf + o);
-#pragma unroll
-                for (int i = 0; i < 4; ++i) fp[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-            }
-            if (g.outb) {
-                uint4 *bp = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(g.outb) + o);
-                bp[0] = pack8(v);
-                bp[1] = pack8(v + 8);
-            }
+            conv_store16(g, (size_t)m, n0 + c0, v);
         }
     }
     tc_fence_before();
@@ -443,45 +483,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_tile_tc(const ConvGemm g, int
             for (int c0 = 0; c0 < BN; c0 += 16) {
                 float v[16];
                 tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(i * BN + c0), v);
-                const size_t o = row * g.N + n0 + c0;
-                if (g.bias) {
-#pragma unroll
-                    for (int k = 0; k < 16; ++k) v[k] += __ldg(g.bias + n0 + c0 + k);
-                }
-                if (g.add) {
-                    const uint4 *ap = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.add) + o);
-                    float tt[8];
-                    unpack8(ap[0], tt);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) v[k] += tt[k];
-                    unpack8(ap[1], tt);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) v[8 + k] += tt[k];
-                }
-                if (g.relu) {
-#pragma unroll
-                    for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.f);
-                }
-                if (g.mask) {
-                    const uint4 *mp = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.mask) + o);
-                    float tt[8];
-                    unpack8(mp[0], tt);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) v[k] = tt[k] > 0.f ? v[k] : 0.f;
-                    unpack8(mp[1], tt);
-#pragma unroll
-                    for (int k = 0; k < 8; ++k) v[8 + k] = tt[k] > 0.f ? v[8 + k] : 0.f;
-                }
-                if (g.outf) {
-                    float4 *fp = reinterpret_cast<float4 *>(g.outf + o);
-#pragma unroll
-                    for (int k = 0; k < 4; ++k) fp[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-                }
-                if (g.outb) {
-                    uint4 *bp = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(g.outb) + o);
-                    bp[0] = pack8(v);
-                    bp[1] = pack8(v + 8);
-                }
+                conv_store16(g, row, n0 + c0, v);
             }
         }
     }
@@ -605,45 +607,7 @@ __global__ void __launch_bounds__(kThreads) k_conv_tma(const ConvGemm g, const _
         for (int c0 = 0; c0 < BN; c0 += 16) {
             float v[16];
             tc_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
-            const size_t o = row * g.N + n0 + c0;
-            if (g.bias) {
-#pragma unroll
-                for (int k = 0; k < 16; ++k) v[k] += __ldg(g.bias + n0 + c0 + k);
-            }
-            if (g.add) {
-                const uint4 *ap = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.add) + o);
-                float tt[8];
-                unpack8(ap[0], tt);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) v[k] += tt[k];
-                unpack8(ap[1], tt);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) v[8 + k] += tt[k];
-            }
-            if (g.relu) {
-#pragma unroll
-                for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k], 0.f);
-            }
-            if (g.mask) {
-                const uint4 *mp = reinterpret_cast<const uint4 *>(static_cast<const __nv_bfloat16 *>(g.mask) + o);
-                float tt[8];
-                unpack8(mp[0], tt);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) v[k] = tt[k] > 0.f ? v[k] : 0.f;
-                unpack8(mp[1], tt);
-#pragma unroll
-                for (int k = 0; k < 8; ++k) v[8 + k] = tt[k] > 0.f ? v[8 + k] : 0.f;
-            }
-            if (g.outf) {
-                float4 *fp = reinterpret_cast<float4 *>(g.outf + o);
-#pragma unroll
-                for (int k = 0; k < 4; ++k) fp[k] = make_float4(v[4 * k], v[4 * k + 1], v[4 * k + 2], v[4 * k + 3]);
-            }
-            if (g.outb) {
-                uint4 *bp = reinterpret_cast<uint4 *>(static_cast<__nv_bfloat16 *>(g.outb) + o);
-                bp[0] = pack8(v);
-                bp[1] = pack8(v + 8);
-            }
+            conv_store16(g, row, n0 + c0, v);
         }
     }
     tc_fence_before();
@@ -1080,6 +1044,16 @@ cudaError_t launch_conv_tc(const ConvGemm &g, int *err, cudaStream_t st, LaunchC
     ProfScope _ps(lc, g.dgrad ? "conv_dgrad_tc" : "conv_fwd_tc", st);
     if (g.N != 16 && g.N != 32 && g.N != 64 && g.N != 128 && g.N != 256) return cudaErrorInvalidValue;
     const int pref = conv_kernel_pref();
+    // the resident-tile kernel reads each input pixel ~1.5 times, the TMA kernel once per tap in 64-channel boxes:
+    // with fewer than 64 channels the tile kernel moves fewer bytes
+    {
+        int R = 0, BN = 0, smem = 0;
+        if (pref <= 1 && g.C < 64 && tile_shape(g, R, BN, smem)) {
+            const cudaError_t e = launch_tile(g, R, BN, smem, err, st);
+            lc.add(1);
+            return e;
+        }
+    }
     {
         int bw = 0, bh = 0;
         CUtensorMap mA, mB;

@@ -165,7 +165,9 @@ void net_shape(lfrv_warmstart *net, int batch, int H, int W) {
 
 int *net_err(lfrv_warmstart *net) { return net->err.as<int>(); }
 
-void conv_forward(lfrv_warmstart *net, int l, const void *x, int level, void *outb, float *outf) {
+// Forward of layer l (input at `level`); with upskip, outb receives relu(up2(conv) + upskip) at level - 1.
+void conv_forward(lfrv_warmstart *net, int l, const void *x, int level, void *outb, float *outf,
+                  const void *upskip = nullptr) {
     const Layer &L = net->L[l];
     const int Hin = net->H >> level, Win = net->W >> level;
     ConvGemm g{};
@@ -187,6 +189,7 @@ void conv_forward(lfrv_warmstart *net, int l, const void *x, int level, void *ou
     g.relu = L.d.relu;
     g.outb = outb;
     g.outf = outf;
+    g.upskip = upskip;
     LFRV_CUDA(launch_conv_tc(g, net_err(net), net->ctx->stream, net->ctx->launches));
 }
 
@@ -255,15 +258,12 @@ void forward(lfrv_warmstart *net, const void *in) {
     conv_forward(net, 2, b(A1), 1, b(A2), nullptr);
     conv_forward(net, 3, b(A2), 2, b(A3), nullptr);
     conv_forward(net, 4, b(A3), 3, b(A4), nullptr);
-    conv_forward(net, 5, b(A4), 3, b(T5), nullptr);
-    const int B = net->batch, H = net->H, W = net->W;
-    LFRV_CUDA(launch_upsample_add_relu(B, H >> 3, W >> 3, 128, b(T5), b(A2), b(S5), c->stream, c->launches));
+    // decoder: the 1 x 1 convolution's epilogue upsamples, adds the skip and applies the ReLU (s = relu(up2(t) + e))
+    conv_forward(net, 5, b(A4), 3, b(S5), nullptr, b(A2));
     conv_forward(net, 6, b(S5), 2, b(A6), nullptr);
-    conv_forward(net, 7, b(A6), 2, b(T7), nullptr);
-    LFRV_CUDA(launch_upsample_add_relu(B, H >> 2, W >> 2, 64, b(T7), b(A1), b(S7), c->stream, c->launches));
+    conv_forward(net, 7, b(A6), 2, b(S7), nullptr, b(A1));
     conv_forward(net, 8, b(S7), 1, b(A8), nullptr);
-    conv_forward(net, 9, b(A8), 1, b(T9), nullptr);
-    LFRV_CUDA(launch_upsample_add_relu(B, H >> 1, W >> 1, 32, b(T9), b(A0), b(S9), c->stream, c->launches));
+    conv_forward(net, 9, b(A8), 1, b(S9), nullptr, b(A0));
     conv_forward(net, 10, b(S9), 0, b(A10), nullptr);
     conv_forward(net, 11, b(A10), 0, nullptr, net->y.as<float>());
 }

@@ -126,9 +126,10 @@ def forward_backward(theta: np.ndarray, x: np.ndarray, u0: np.ndarray, target: n
         return relu(y) if r else y
 
     a0 = q(f(0, x)); a1 = q(f(1, a0)); a2 = q(f(2, a1)); a3 = q(f(3, a2)); a4 = q(f(4, a3))
-    t5 = q(f(5, a4)); s5 = q(relu(up2(t5) + a2))
-    a6 = q(f(6, s5)); t7 = q(f(7, a6)); s7 = q(relu(up2(t7) + a1))
-    a8 = q(f(8, s7)); t9 = q(f(9, a8)); s9 = q(relu(up2(t9) + a0))
+    # the 1 x 1 decoder layers keep t in FP32: the device adds it to the skip in the same epilogue
+    t5 = f(5, a4); s5 = q(relu(up2(t5) + a2))
+    a6 = q(f(6, s5)); t7 = f(7, a6); s7 = q(relu(up2(t7) + a1))
+    a8 = q(f(8, s7)); t9 = f(9, a8); s9 = q(relu(up2(t9) + a0))
     a10 = q(f(10, s9))
     y = f(11, a10)                                          # FP32 on the device
     pred = u0 + y.transpose(0, 3, 1, 2)
