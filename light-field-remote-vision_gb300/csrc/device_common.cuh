@@ -187,12 +187,14 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &g
     generation += 1;
     bool ok = true;
     if (threadIdx.x == 0 && threadIdx.y == 0) {
-        __threadfence();
+        // release: the block's writes (ordered before this thread by the __syncthreads above) become visible to
+        // every block that acquires the count after it; acquire: the other blocks' writes are visible here
         const unsigned int target = generation * nblocks;
-        atomicAdd(gb.count, 1u);
+        asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(gb.count) : "memory");
         long long spins = 0;
         while (true) {
-            const unsigned int seen = *((volatile unsigned int *)gb.count);
+            unsigned int seen;
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(gb.count) : "memory");
             if ((int)(seen - target) >= 0) break;
             if (*((volatile int *)gb.err)) {
                 ok = false;
@@ -205,7 +207,6 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &g
             }
             __nanosleep(32);
         }
-        __threadfence();
     }
     __shared__ int s_ok;
     if (threadIdx.x == 0 && threadIdx.y == 0) s_ok = ok ? 1 : 0;

@@ -331,12 +331,19 @@ __device__ void block_reduce_partials(const double *partial, int count, int nslo
     // one warp: lane-strided sums then a shuffle tree, in FP64 and a fixed order (the FP64 pipe is narrow on
     // this part, so the other warps stay out of it)
     if (threadIdx.x < 32) {
-        for (int sl = 0; sl < nslots; ++sl) {
-            double s = 0.0;
-            for (int i = threadIdx.x; i < count; i += 32) s += __ldcg(partial + (size_t)sl * count + i);
+        // the slots' loads interleaved (independent, in flight together); each slot keeps its summation order
+        double s[4] = {0.0, 0.0, 0.0, 0.0};
+#pragma unroll 4
+        for (int i = threadIdx.x; i < count; i += 32) {
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            if (threadIdx.x == 0) out_smem[sl] = s;
+            for (int sl = 0; sl < 4; ++sl)
+                if (sl < nslots) s[sl] += __ldcg(partial + (size_t)sl * count + i);
+        }
+#pragma unroll
+        for (int sl = 0; sl < 4; ++sl) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s[sl] += __shfl_down_sync(0xffffffffu, s[sl], o);
+            if (threadIdx.x == 0 && sl < nslots) out_smem[sl] = s[sl];
         }
     }
     __syncthreads();
@@ -889,7 +896,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_batch(const CgProblem *_
 // the index of the neighbouring hole or the neighbour's fixed value; the iterations then touch shared memory
 // only. Each update is the same float expression as k_hole_fill_persistent's. holes must be in ascending pixel
 // order (k_hole_write): neighbours are found by binary search.
-constexpr int kSmallHoles = 2048, kSmallThreads = 256;
+constexpr int kSmallHoles = 2048, kSmallThreads = 1024;
 constexpr size_t kSmallHoleSmem = (size_t)kSmallHoles * (6 * 4 + 12 * 4 + 4 * 2 + 4);
 
 __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H, const int *__restrict__ holes,
@@ -902,8 +909,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
     float *fixedv = hsm + 6 * kSmallHoles;                      // [4 dirs][3][kSmallHoles]
     float *wts = hsm + 18 * kSmallHoles;                        // [kSmallHoles]
     short *nb = reinterpret_cast<short *>(hsm + 19 * kSmallHoles);  // [4][kSmallHoles]: hole index, -1 fixed, -2 none
-    __shared__ double red[kSmallThreads / 32];
-    __shared__ float s_energy;
+    __shared__ float wsum[2][kSmallThreads / 32];
     __shared__ int s_holes[kSmallHoles];
     const size_t N = (size_t)W * H;
     for (int h = threadIdx.x; h < nh; h += kSmallThreads) s_holes[h] = __ldg(holes + h);
@@ -943,7 +949,9 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
     int k;
     for (k = 0; k < max_iter; ++k) {
         previous = energy;
-        double acc = 0.0;
+        // the energy in FP32 (a handful of terms per thread, fixed shuffle trees): the FP64 pipe of this part is
+        // narrow, and the stop test compares single-precision energies
+        float acc = 0.f;
         for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
@@ -959,20 +967,20 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
                 const float lap = v - uc;
                 const float un = uc + lap;
                 nxt[c * kSmallHoles + h] = un;
-                if (c == 2) acc += (double)(lap * un);
+                if (c == 2) acc += lap * un;
             }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        // one barrier per iteration: the warp sums alternate between two slots, and every warp sums the 32 of
+        // this iteration with the same fixed tree (down-shuffles, then lane 0's value), so all agree
+        const int lane = threadIdx.x & 31;
+        if (lane == 0) wsum[k & 1][threadIdx.x >> 5] = acc;
         __syncthreads();
-        if (threadIdx.x == 0) {
-            double t = 0.0;
-            for (int w = 0; w < kSmallThreads / 32; ++w) t += red[w];
-            s_energy = (float)t;
-        }
-        __syncthreads();
-        energy = s_energy;
+        float tot = (lane < kSmallThreads / 32) ? wsum[k & 1][lane] : 0.f;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
+        energy = __shfl_sync(0xffffffffu, tot, 0);
         float *t = cur;
         cur = nxt;
         nxt = t;
