@@ -91,11 +91,27 @@ __global__ void k_scan_blocks(int nb, const unsigned int *__restrict__ in, unsig
     if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = s[threadIdx.x];
 }
 
-__global__ void k_scan_add(int nb, unsigned int *__restrict__ out, const unsigned int *__restrict__ block_offsets,
-                           const unsigned int *__restrict__ block_sums_total, unsigned int *__restrict__ out_last) {
+// Adds to block b's exclusive scan the sum of the totals of blocks 0 .. b - 1; out[nb] = the grand total.
+__global__ void __launch_bounds__(kScanBlock) k_scan_finish(int nb, unsigned int *__restrict__ out,
+                                                            const unsigned int *__restrict__ block_sums) {
+    __shared__ unsigned int red[kScanBlock / 32];
+    unsigned int s = 0;
+    for (int j = threadIdx.x; j < (int)blockIdx.x; j += kScanBlock) s += block_sums[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        unsigned int t = (threadIdx.x < kScanBlock / 32) ? red[threadIdx.x] : 0u;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (threadIdx.x == 0) red[0] = t;
+    }
+    __syncthreads();
+    const unsigned int off = red[0];
     const int i = blockIdx.x * kScanBlock + threadIdx.x;
-    if (i < nb) out[i] += block_offsets[blockIdx.x];
-    if (i == 0) *out_last = *block_sums_total;
+    if (i < nb) out[i] += off;
+    if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[nb] = off + block_sums[blockIdx.x];
 }
 
 // ====================================================================== per-source gathers (v = A u)
@@ -157,7 +173,15 @@ __global__ void __launch_bounds__(256) k_weights(int V, int n, int w, int h, int
     const int v = blockIdx.y;
     if (m >= n) return;
     const float *tx = tau + (size_t)v * 2 * n, *ty = tx + n;
-    const float txm = tx[m], tym = ty[m];
+    // every load the pixel can need, issued together (neighbour indices clamped to the view; the clamped values
+    // are read only where the neighbour exists)
+    const int mx = m % w, my = m / w;
+    const int ml = mx > 0 ? m - 1 : m, mr = mx < w - 1 ? m + 1 : m;
+    const int mu = my > 0 ? m - w : m, md = my < h - 1 ? m + w : m;
+    const float txm = __ldg(tx + m), tym = __ldg(ty + m);
+    const float txl = __ldg(tx + ml), tyl = __ldg(ty + ml), txr = __ldg(tx + mr), tyr = __ldg(ty + mr);
+    const float txu = __ldg(tx + mu), tyu = __ldg(ty + mu), txd = __ldg(tx + md), tyd = __ldg(ty + md);
+    const float dpx = __ldg(dp + (size_t)v * 2 * n + m), dpy = __ldg(dp + (size_t)v * 2 * n + n + m);
     float ax = 0.f, ay = 0.f;
     if (gx && in_gather(txm, tym, W, H)) {  // gx == nullptr: the target gradient is identically zero
         Footprint fp;
@@ -181,21 +205,20 @@ __global__ void __launch_bounds__(256) k_weights(int V, int n, int w, int h, int
         ax = ax / norm * thr;
         ay = ay / norm * thr;
     }
-    float sg = ax * dp[(size_t)v * 2 * n + m] + ay * dp[(size_t)v * 2 * n + n + m];
+    float sg = ax * dpx + ay * dpy;
     if (sg > 0.5f) sg = 0.5f;
     const float ang = 1.0f / (sg * sg + sigma * sigma);
     // deformation weight
-    const int mx = m % w, my = m / w;
-    auto out = [&](int k) { return tx[k] < 0.f || tx[k] > (float)W || ty[k] < 0.f || ty[k] > (float)H; };
+    auto out = [&](float x, float y) { return x < 0.f || x > (float)W || y < 0.f || y > (float)H; };
     float def;
-    if (out(m)) def = 0.0f;
+    if (out(txm, tym)) def = 0.0f;
     else if (mx == 0 || my == 0 || mx == w - 1 || my == h - 1) def = 1.0f;
-    else if (out(m - 1) || out(m + 1) || out(m - w) || out(m + w)) def = 1.0f;
+    else if (out(txl, tyl) || out(txr, tyr) || out(txu, tyu) || out(txd, tyd)) def = 1.0f;
     else {
-        const float Dxx = 0.5f * (tx[m + 1] - tx[m - 1]);
-        const float Dyx = 0.5f * (ty[m + 1] - ty[m - 1]);
-        const float Dxy = 0.5f * (tx[m + w] - tx[m - w]);
-        const float Dyy = 0.5f * (ty[m + w] - ty[m - w]);
+        const float Dxx = 0.5f * (txr - txl);
+        const float Dyx = 0.5f * (tyr - tyl);
+        const float Dxy = 0.5f * (txd - txu);
+        const float Dyy = 0.5f * (tyd - tyu);
         const float N = fabsf(Dxx * Dyy - Dxy * Dyx);
         def = (N > 1.0f) ? 1.0f / N : 1.0f;
     }
@@ -1006,23 +1029,12 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
     cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
     k_bucket_count<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.count);
     lc.add(1);
+    // exclusive scan of the counts: block-local scans, then every block adds the sum of the block totals before
+    // it (integer sums, so the result does not depend on the order) and the last block writes the total
     const int nblk = (B.nb + kScanBlock - 1) / kScanBlock;
     k_scan_blocks<<<nblk, kScanBlock, 0, st>>>(B.nb, B.count, B.start, B.block_sums);
-    lc.add(1);
-    // scan of block sums (nblk <= kScanBlock^2 covers 2^20 * 1024 buckets)
-    const int nblk2 = (nblk + kScanBlock - 1) / kScanBlock;
-    k_scan_blocks<<<nblk2, kScanBlock, 0, st>>>(nblk, B.block_sums, B.block_offsets, B.block_sums2);
-    lc.add(1);
-    if (nblk2 > 1) {
-        // third level: at most kScanBlock entries
-        k_scan_blocks<<<1, kScanBlock, 0, st>>>(nblk2, B.block_sums2, B.block_offsets2, B.total2);
-        k_scan_add<<<nblk2, kScanBlock, 0, st>>>(nblk, B.block_offsets, B.block_offsets2, B.total2, B.total);
-        lc.add(2);
-    } else {
-        cudaMemcpyAsync(B.total, B.block_sums2, sizeof(unsigned int), cudaMemcpyDeviceToDevice, st);
-    }
-    k_scan_add<<<nblk, kScanBlock, 0, st>>>(B.nb, B.start, B.block_offsets, B.total, B.start + B.nb);
-    lc.add(1);
+    k_scan_finish<<<nblk, kScanBlock, 0, st>>>(B.nb, B.start, B.block_sums);
+    lc.add(2);
     cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
     k_bucket_fill<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.start, B.count, B.entries);
     k_bucket_sort<<<(B.nb + 255) / 256, 256, 0, st>>>(B.nb, B.start, B.entries);
