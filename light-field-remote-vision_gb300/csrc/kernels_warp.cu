@@ -143,7 +143,7 @@ __device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigne
         }
 }
 
-__global__ void __launch_bounds__(256) k_zsplat(int V, int w, int h, const float *__restrict__ depth,
+__global__ void __launch_bounds__(256, 6) k_zsplat(int V, int w, int h, const float *__restrict__ depth,
                                                 const WarpCams cams, int W, int H,
                                                 unsigned long long *__restrict__ zkey) {
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
