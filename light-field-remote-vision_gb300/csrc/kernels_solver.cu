@@ -164,8 +164,10 @@ __global__ void __launch_bounds__(256) k_residual(int V, int n, int W, int H, in
 // Angular and deformation weights of every source pixel (coco_vtv_sr_compute_weights_unstructured,
 // sources/optimization.cu:1094-1163; vtv_sr_angular_weights_device and vtv_sr_gold_deform_weights_device,
 // vtv_sr_kernels_unstructured.cu:174-266): w = 1/(sg^2 + sigma^2) * deform with sg = clamp(A_i grad) . dpart.
-template <int KS, typename TW>
-__global__ void __launch_bounds__(256) k_weights(int V, int n, int w, int h, int W, int H, int dsf,
+// GATHER = false: the target gradient is identically zero (gx == nullptr), so the gather through A is skipped
+// at compile time and the kernel keeps few registers.
+template <int KS, typename TW, bool GATHER>
+__global__ void __launch_bounds__(256, GATHER ? 1 : 8) k_weights(int V, int n, int w, int h, int W, int H, int dsf,
                                                  const float *__restrict__ gx, const float *__restrict__ gy,
                                                  const float *__restrict__ tau, const float *__restrict__ dp,
                                                  float sigma, float thr, TW *__restrict__ wgt) {
@@ -183,7 +185,7 @@ __global__ void __launch_bounds__(256) k_weights(int V, int n, int w, int h, int
     const float txu = __ldg(tx + mu), tyu = __ldg(ty + mu), txd = __ldg(tx + md), tyd = __ldg(ty + md);
     const float dpx = __ldg(dp + (size_t)v * 2 * n + m), dpy = __ldg(dp + (size_t)v * 2 * n + n + m);
     float ax = 0.f, ay = 0.f;
-    if (gx && in_gather(txm, tym, W, H)) {  // gx == nullptr: the target gradient is identically zero
+    if (GATHER && in_gather(txm, tym, W, H)) {
         Footprint fp;
         footprint<KS>(txm, tym, dsf, W, H, fp);
 #pragma unroll
@@ -1055,13 +1057,19 @@ template <typename TW>
 static void weights_typed(const Geometry &G, const float *gx, const float *gy, const float *tau, const float *dp,
                           float sigma, float thr, TW *wgt, cudaStream_t st) {
     const dim3 b(256), g((G.n + 255) / 256, G.V);
+#define LFRV_WEIGHTS(KS_)                                                                                          \
+    if (gx)                                                                                                        \
+        k_weights<KS_, TW, true><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt); \
+    else                                                                                                           \
+        k_weights<KS_, TW, false><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt);
     switch (G.dsf + 1) {
-        case 2: k_weights<2, TW><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt); break;
-        case 3: k_weights<3, TW><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt); break;
-        case 4: k_weights<4, TW><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt); break;
-        case 5: k_weights<5, TW><<<g, b, 0, st>>>(G.V, G.n, G.w, G.h, G.W, G.H, G.dsf, gx, gy, tau, dp, sigma, thr, wgt); break;
+        case 2: LFRV_WEIGHTS(2) break;
+        case 3: LFRV_WEIGHTS(3) break;
+        case 4: LFRV_WEIGHTS(4) break;
+        case 5: LFRV_WEIGHTS(5) break;
         default: break;
     }
+#undef LFRV_WEIGHTS
 }
 
 void launch_weights(const Geometry &G, const float *gx, const float *gy, const float *tau, const float *dp, float sigma,
@@ -1338,27 +1346,39 @@ void launch_gradient_setup(const Geometry &G, const Buckets &B, const float *tau
     lc.add(1);
 }
 
-// Luminance Sobel of BF16 views into BF16 gradients (the view path of k_sobel: no mask, zero on the border).
-__global__ void k_view_sobel_bf16(int W, int H, const __nv_bfloat16 *__restrict__ rgb, size_t in_stride,
-                                  size_t ch_stride, __nv_bfloat16 *__restrict__ gx, __nv_bfloat16 *__restrict__ gy,
-                                  size_t out_stride) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
+// Luminance Sobel of the views (the view path of k_sobel: no mask, zero on the border), FP32 or BF16 in and out.
+// The luminance of a 32 x 8 tile and its one-pixel halo is computed once into shared memory (three loads per
+// pixel instead of 27); the arithmetic is k_sobel's, so the results are the same bit for bit.
+template <typename T>
+__global__ void __launch_bounds__(256) k_view_sobel(int W, int H, const T *__restrict__ rgb, size_t in_stride,
+                                                    size_t ch_stride, T *__restrict__ gx, T *__restrict__ gy,
+                                                    size_t out_stride) {
+    __shared__ float Ls[10][35];
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 8, z = blockIdx.z;
+    const T *r = rgb + (size_t)z * in_stride, *g = r + ch_stride, *b = g + ch_stride;
+    const int t = threadIdx.y * 32 + threadIdx.x;
+    for (int k = t; k < 10 * 34; k += 256) {
+        const int ly = k / 34, lx = k - ly * 34, xx = x0 - 1 + lx, yy = y0 - 1 + ly;
+        float L = 0.f;
+        if (xx >= 0 && xx < W && yy >= 0 && yy < H) {
+            const size_t q = (size_t)yy * W + xx;
+            L = lum(ldv(r + q), ldv(g + q), ldv(b + q));
+        }
+        Ls[ly][lx] = L;
+    }
+    __syncthreads();
+    const int x = x0 + threadIdx.x, y = y0 + threadIdx.y;
     if (x >= W || y >= H) return;
-    const __nv_bfloat16 *r = rgb + (size_t)z * in_stride, *g = r + ch_stride, *b = g + ch_stride;
-    const size_t o = (size_t)y * W + x;
+    const int tx = threadIdx.x + 1, ty = threadIdx.y + 1;
     float gX = 0.f, gY = 0.f;
     if (0 < x && x < W - 1 && 0 < y && y < H - 1) {
-        auto L = [&](int dx, int dy) {
-            const size_t q = o + (ptrdiff_t)dy * W + dx;
-            return lum(ldv(r + q), ldv(g + q), ldv(b + q));
-        };
-        const float Ypp = L(-1, -1), Ypc = L(0, -1), Ypn = L(1, -1);
-        const float Ycp = L(-1, 0), Ycn = L(1, 0);
-        const float Ynp = L(-1, 1), Ync = L(0, 1), Ynn = L(1, 1);
+        const float Ypp = Ls[ty - 1][tx - 1], Ypc = Ls[ty - 1][tx], Ypn = Ls[ty - 1][tx + 1];
+        const float Ycp = Ls[ty][tx - 1], Ycn = Ls[ty][tx + 1];
+        const float Ynp = Ls[ty + 1][tx - 1], Ync = Ls[ty + 1][tx], Ynn = Ls[ty + 1][tx + 1];
         gX = (Ypn + 2.f * Ycn + Ynn - Ypp - 2.f * Ycp - Ynp) / 8.f;
         gY = (Ynp + 2.f * Ync + Ynn - Ypp - 2.f * Ypc - Ypn) / 8.f;
     }
+    const size_t o = (size_t)y * W + x;
     stv(gx + (size_t)z * out_stride + o, gX);
     stv(gy + (size_t)z * out_stride + o, gY);
 }
@@ -1367,8 +1387,9 @@ void launch_view_sobel_bf16(int W, int H, int count, const void *rgb, size_t in_
                             void *gy, size_t out_stride, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "sobel", st);
     const dim3 b(32, 8), g((W + 31) / 32, (H + 7) / 8, count);
-    k_view_sobel_bf16<<<g, b, 0, st>>>(W, H, static_cast<const __nv_bfloat16 *>(rgb), in_stride, ch_stride,
-                                       static_cast<__nv_bfloat16 *>(gx), static_cast<__nv_bfloat16 *>(gy), out_stride);
+    k_view_sobel<__nv_bfloat16><<<g, b, 0, st>>>(W, H, static_cast<const __nv_bfloat16 *>(rgb), in_stride, ch_stride,
+                                                 static_cast<__nv_bfloat16 *>(gx), static_cast<__nv_bfloat16 *>(gy),
+                                                 out_stride);
     lc.add(1);
 }
 
@@ -1376,7 +1397,8 @@ void launch_sobel(int W, int H, int count, const float *rgb, size_t in_stride, s
                   size_t out_stride, const uint8_t *vis, double *abs_partial, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "sobel", st);
     const dim3 b(32, 8), g((W + 31) / 32, (H + 7) / 8, count);
-    k_sobel<<<g, b, 0, st>>>(W, H, rgb, in_stride, ch_stride, gx, gy, out_stride, vis, abs_partial);
+    if (!vis && !abs_partial) k_view_sobel<float><<<g, b, 0, st>>>(W, H, rgb, in_stride, ch_stride, gx, gy, out_stride);
+    else k_sobel<<<g, b, 0, st>>>(W, H, rgb, in_stride, ch_stride, gx, gy, out_stride, vis, abs_partial);
     lc.add(1);
 }
 int sobel_partials(int W, int H) { return ((W + 31) / 32) * ((H + 7) / 8); }
