@@ -282,8 +282,7 @@ def run_batch(args, rank: int, world: int) -> None:
                            "batching_gain": sec_single / sec,
                            "l2": "the 32 targets' buffers exceed L2 (no flush needed)"},
                 "clocks": clocks, "gpu_launches": launches, "roofline": None, "cpu_baseline": None,
-                "e2e": {"value": world * nv / sec, "unit": "views/s", "h2d_bytes_per_step": 0,
-                        "d2h_bytes_per_step": 0}}
+                "e2e": None}  # device-pointer batch API only: no host-buffer leg for this workload
         print(json.dumps(line), flush=True)
     ctx.close()
 
