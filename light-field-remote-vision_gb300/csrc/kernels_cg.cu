@@ -127,9 +127,12 @@ constexpr int kCgBX = 32, kCgBY = 8;
 // the reference; with one, U holds a seed (the learned warm start) while u0 keeps the problem unchanged.
 // acc[0..2] += r^2 per channel, acc[3] += the energy.
 __device__ __forceinline__ void cg_start_pixel(int W, int H, size_t N, size_t o, const float *__restrict__ gX,
-                                               const float *__restrict__ gY, const float *U, const float *U0,
-                                               float *r, float lambda, float acc[4]) {
-    const int x = (int)(o % W), y = (int)(o / W);
+                                               const float *__restrict__ gY, const float *__restrict__ U,
+                                               const float *__restrict__ U0, float *__restrict__ r, float lambda,
+                                               float acc[4]) {
+    // 32-bit index arithmetic: images have fewer than 2^31 pixels
+    const unsigned int ou = (unsigned int)o;
+    const int y = (int)(ou / (unsigned int)W), x = (int)(ou - (unsigned int)y * (unsigned int)W);
     const float gxo = __ldg(gX + o), gyo = __ldg(gY + o);
     const float gxl = (x > 0) ? __ldg(gX + o - 1) : 0.f, gyu = (y > 0) ? __ldg(gY + o - W) : 0.f;
 #pragma unroll
