@@ -11,6 +11,7 @@
 // (view, pixel)), and every target pixel reads the ks x ks anchor buckets that can reach it, recomputing
 // the footprint weights from tau instead of storing A (the reference stores ks^2 floats per source pixel).
 #include <algorithm>
+#include <mutex>
 
 #include <cuda_bf16.h>
 
@@ -383,14 +384,28 @@ __device__ __forceinline__ void gradient_setup_global(int x, int y, int W, int H
 }
 
 // Anchor-row form (KS <= 3). The entries of one anchor bucket reach a KS x KS block of target pixels, so
-// instead of every target pixel re-reading the entries of its KS^2 buckets, a lane owns one bucket, reads
-// each of its entries once and accumulates all KS^2 taps in registers (partials P[i][j][field]). A warp owns
-// 32 consecutive anchors of one anchor row; pixel x of tap row i sums P[i][0] of anchor x, P[i][1] of anchor
-// x-1, ... (warp shuffles, fixed order), and the block adds the KS tap rows of each pixel from shared memory
-// in fixed order. Lanes 0 .. KS-2 only feed their right neighbours, so a warp outputs 33 - KS pixels.
-// The summation order differs from the per-pixel form (per-bucket partials first) but is fixed, so results
-// are deterministic. Fields: 0 w A, 1-3 w A v, 4 A, 5-6 A Sobel, 7 A w, 8 visibility (raw overlap != 0).
+// instead of every target pixel re-reading the entries of its KS^2 buckets, a lane reads each entry of its
+// buckets once and accumulates all KS^2 taps in registers (partials P[i][j][field]).
+// A warp owns 64 consecutive anchors of one anchor row, starting at an even column: lane l takes anchor 2l in
+// pass 0 and anchor 2l + 1 in pass 1, and owns pixel columns 2l and 2l + 1. With dsf 2 most source pixels of a
+// box-decimated view land on even anchors, so one pass per parity makes a warp wait for its longest even bucket
+// plus its longest odd bucket, not twice the longest of both. Pixel x of tap row i sums tap j of anchor x - j:
+//   column 2l:      (P0[0] of 2l + P0[2] of 2l - 2) + P1[1] of 2l - 1
+//   column 2l + 1:   P0[1] of 2l + (P1[0] of 2l + 1 + P1[2] of 2l - 1)
+// (P0 / P1: the pass-0 / pass-1 partials; the left terms come from lane l - 1 by shuffle). The block then adds
+// the KS tap rows of each pixel from shared memory. Every sum has a fixed order, so results are deterministic.
+// Lane 0's columns lack their left anchors, so a warp outputs 62 pixels. The footprint norm is the product of
+// the row and column overlap sums (the KS^2 taps are an outer product), and a tap is visible when both of its
+// overlaps are non-zero. Fields: 0 w A, 1-3 w A v, 4 A, 5-6 A Sobel, 7 visibility. The mask sum (A w) is
+// field 0: the same products added in the same order.
 constexpr int kGrWarps = 8;
+constexpr int kGrTXO = 62;  // output pixels per warp row
+constexpr int kGrNF = 8;    // fields per tap-row partial
+
+template <int KS>
+constexpr size_t gradient_rows_smem() {
+    return sizeof(float) * (kGrWarps * 2 - (KS - 1)) * KS * kGrNF * kGrTXO;
+}
 
 template <int KS, typename TS>
 __global__ void __launch_bounds__(kGrWarps * 32, 2) k_gradient_setup_rows(int W, int H, int n, int dsf, int BW,
@@ -404,148 +419,174 @@ __global__ void __launch_bounds__(kGrWarps * 32, 2) k_gradient_setup_rows(int W,
                                                                        float *__restrict__ U, float *__restrict__ gx,
                                                                        float *__restrict__ gy,
                                                                        float *__restrict__ mask) {
-    constexpr int TXO = 33 - KS;                 // output pixels per warp row
-    constexpr int ROWS = kGrWarps * 2;           // anchor rows per block (2 per warp: 2w, 2w + 1)
-    constexpr int TY = ROWS - (KS - 1);          // output pixel rows per block
-    constexpr int NF = 9;
-    __shared__ float part[TY][KS][TXO][NF];      // (pixel row, tap row, pixel, field)
+    constexpr int TY = kGrWarps * 2 - (KS - 1);  // output pixel rows per block
+    constexpr int NA = 7;                        // accumulated fields
+    extern __shared__ float gr_part[];           // [TY][KS][kGrNF][kGrTXO]: (pixel row, tap row, field, pixel)
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int x0 = blockIdx.x * TXO, y0 = blockIdx.y * TY;
+    const int x0 = blockIdx.x * kGrTXO, y0 = blockIdx.y * TY;
     const int BH = H + KS - 1;
-    const int bx = x0 + lane;                    // bucket column = anchor x + KS - 1
-    const int ax = bx - (KS - 1);
-    // warp w takes anchor rows 2w and 2w + 1: one of each parity (with dsf = 2 the populated anchors often
-    // sit on every other row, so rows w and w + 8 would leave half the warps idle)
+    const int lx = 2 * lane - 2;  // this lane's first pixel column inside the tile
+    // warp w takes anchor rows 2w and 2w + 1: one of each parity (with dsf = 2 the populated anchors mostly sit
+    // on even rows, so rows w and w + 8 would leave half the warps idle)
     for (int q = 0; q < 2; ++q) {
         const int rr = 2 * warp + q;
         const int ay = y0 - (KS - 1) + rr, by = ay + KS - 1;
-        float P[KS][KS][8];
+        bool iny[KS];
 #pragma unroll
-        for (int i = 0; i < KS; ++i)
+        for (int i = 0; i < KS; ++i) iny[i] = (0 <= ay + i && ay + i <= H - 1);
+#pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+            const int ax = x0 - 2 + 2 * lane + pass, bx = ax + KS - 1;
+            bool inx[KS];
 #pragma unroll
-            for (int j = 0; j < KS; ++j)
+            for (int j = 0; j < KS; ++j) inx[j] = (0 <= ax + j && ax + j <= W - 1);
+            float P[KS][KS][NA];
 #pragma unroll
-                for (int f = 0; f < 8; ++f) P[i][j][f] = 0.f;
-        unsigned int anyb = 0;
-        if (bx < BW && by < BH) {
-            const size_t b = (size_t)by * BW + bx;
-            const unsigned int s = __ldg(start + b), e = __ldg(start + b + 1);
-            // software pipeline: the entry index two ahead and the source data one ahead are in flight while
-            // the current entry is accumulated
-            struct Src {
-                float tx, ty, w, c0, c1, c2, s0, s1;
-            };
-            auto fetch = [&](unsigned int ent) {
-                const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
-                const TS *iv = img + (size_t)v * 3 * n;
-                const TS *gv = vgrad + (size_t)v * 2 * n;
-                Src d;
-                d.tx = __ldg(tau + (size_t)v * 2 * n + m);
-                d.ty = __ldg(tau + (size_t)v * 2 * n + n + m);
-                d.w = ldv(wgt + (size_t)v * n + m);
-                d.c0 = ldv(iv + m);
-                d.c1 = ldv(iv + n + m);
-                d.c2 = ldv(iv + 2 * n + m);
-                d.s0 = ldv(gv + m);
-                d.s1 = ldv(gv + n + m);
-                return d;
-            };
-            Src cur = {};
-            unsigned int ent_next = 0;
-            if (s < e) cur = fetch(__ldg(entries + s));
-            if (s + 1 < e) ent_next = __ldg(entries + s + 1);
-            for (unsigned int k = s; k < e; ++k) {
-                Src nxt = {};
-                if (k + 1 < e) nxt = fetch(ent_next);
-                if (k + 2 < e) ent_next = __ldg(entries + k + 2);
-                const float tx = cur.tx, ty = cur.ty, w = cur.w, c0 = cur.c0, c1 = cur.c1, c2 = cur.c2;
-                const float s0 = cur.s0, s1 = cur.s1;
-                cur = nxt;
-                const float px = tx - 0.5f, py = ty - 0.5f;
-                float dxs[KS], dys[KS];
-#pragma unroll
-                for (int q = 0; q < KS; ++q) {
-                    dxs[q] = fp_overlap(q, KS, ax + q, px, dsf);
-                    dys[q] = fp_overlap(q, KS, ay + q, py, dsf);
-                }
-                bool inx[KS], iny[KS];
-#pragma unroll
-                for (int q = 0; q < KS; ++q) {
-                    inx[q] = (0 <= ax + q && ax + q <= W - 1);
-                    iny[q] = (0 <= ay + q && ay + q <= H - 1);
-                }
-                float a[KS][KS], norm = 0.f;
+            for (int i = 0; i < KS; ++i)
 #pragma unroll
                 for (int j = 0; j < KS; ++j)
 #pragma unroll
+                    for (int f = 0; f < NA; ++f) P[i][j][f] = 0.f;
+            unsigned int anyb = 0;
+            if (bx >= 0 && bx < BW && by < BH) {
+                const size_t b = (size_t)by * BW + bx;
+                const unsigned int s = __ldg(start + b), e = __ldg(start + b + 1);
+                // software pipeline: the entry index three ahead and the source data of the next two entries
+                // are in flight while the current entry is accumulated
+                struct Src {
+                    float tx, ty, w, c0, c1, c2, s0, s1;
+                };
+                auto fetch = [&](unsigned int ent) {
+                    const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
+                    const TS *iv = img + (size_t)v * 3 * n;
+                    const TS *gv = vgrad + (size_t)v * 2 * n;
+                    Src d;
+                    d.tx = __ldg(tau + (size_t)v * 2 * n + m);
+                    d.ty = __ldg(tau + (size_t)v * 2 * n + n + m);
+                    d.w = ldv(wgt + (size_t)v * n + m);
+                    d.c0 = ldv(iv + m);
+                    d.c1 = ldv(iv + n + m);
+                    d.c2 = ldv(iv + 2 * n + m);
+                    d.s0 = ldv(gv + m);
+                    d.s1 = ldv(gv + n + m);
+                    return d;
+                };
+                Src cur = {}, nx1 = {};
+                unsigned int ent_next = 0;
+                if (s < e) cur = fetch(__ldg(entries + s));
+                if (s + 1 < e) nx1 = fetch(__ldg(entries + s + 1));
+                if (s + 2 < e) ent_next = __ldg(entries + s + 2);
+                for (unsigned int k = s; k < e; ++k) {
+                    Src nx2 = {};
+                    if (k + 2 < e) nx2 = fetch(ent_next);
+                    if (k + 3 < e) ent_next = __ldg(entries + k + 3);
+                    const float w = cur.w, c0 = cur.c0, c1 = cur.c1, c2 = cur.c2, s0 = cur.s0, s1 = cur.s1;
+                    const float px = cur.tx - 0.5f, py = cur.ty - 0.5f;
+                    cur = nx1;
+                    nx1 = nx2;
+                    float dx[KS], dy[KS], sx = 0.f, sy = 0.f;
+                    unsigned int xb = 0;
+#pragma unroll
+                    for (int t = 0; t < KS; ++t) {
+                        dx[t] = inx[t] ? fp_overlap(t, KS, ax + t, px, dsf) : 0.0f;
+                        dy[t] = iny[t] ? fp_overlap(t, KS, ay + t, py, dsf) : 0.0f;
+                        sx = __fadd_rn(sx, dx[t]);
+                        sy = __fadd_rn(sy, dy[t]);
+                        xb |= (dx[t] != 0.0f) ? 1u << t : 0u;
+                    }
+                    // one reciprocal per entry; A = (dx * (1 / norm)) * dy is within a few ulps of dx dy / norm
+                    const float norm = __fmul_rn(sx, sy);
+                    const float inv = (norm != 0.0f) ? __frcp_rn(norm) : 1.0f;
+                    const float w0 = w * c0, w1 = w * c1, w2 = w * c2;
+#pragma unroll
                     for (int i = 0; i < KS; ++i) {
-                        a[i][j] = (inx[j] && iny[i]) ? __fmul_rn(dxs[j], dys[i]) : 0.0f;
-                        norm = __fadd_rn(norm, a[i][j]);
+                        anyb |= (dy[i] != 0.0f) ? xb << (i * KS) : 0u;
+                        const float yi = __fmul_rn(dy[i], inv);
+#pragma unroll
+                        for (int j = 0; j < KS; ++j) {
+                            const float A = __fmul_rn(dx[j], yi);
+                            P[i][j][0] += w * A;
+                            P[i][j][1] += A * w0;
+                            P[i][j][2] += A * w1;
+                            P[i][j][3] += A * w2;
+                            P[i][j][4] += A;
+                            P[i][j][5] += A * s0;
+                            P[i][j][6] += A * s1;
+                        }
                     }
-                // one reciprocal per entry: A = a * (1 / norm) is within an ulp of the reference's a / norm
-                const float inv = (norm != 0.0f) ? __frcp_rn(norm) : 1.0f;
+                }
+            }
+            // tap rows of this pass into shared memory: pass 0 stores, pass 1 adds (same lane, same slots)
 #pragma unroll
-                for (int i = 0; i < KS; ++i)
+            for (int i = 0; i < KS; ++i) {
+                const int py = ay + i - y0;  // output pixel row inside the tile
+                float c0[NA], c1[NA];
+                unsigned int v0, v1;
+                const unsigned int bi = anyb >> (i * KS);
+                const unsigned int bl = __shfl_up_sync(0xffffffffu, bi, 1);
+                if (pass == 0) {
 #pragma unroll
-                    for (int j = 0; j < KS; ++j) {
-                        const float A = __fmul_rn(a[i][j], inv);
-                        if (a[i][j] != 0.0f) anyb |= 1u << (i * KS + j);
-                        const float wA = w * A;
-                        P[i][j][0] += wA;
-                        P[i][j][1] += wA * c0;
-                        P[i][j][2] += wA * c1;
-                        P[i][j][3] += wA * c2;
-                        P[i][j][4] += A;
-                        P[i][j][5] += A * s0;
-                        P[i][j][6] += A * s1;
-                        P[i][j][7] += A * w;
+                    for (int f = 0; f < NA; ++f) {
+                        const float left = (KS == 3) ? __shfl_up_sync(0xffffffffu, P[i][KS - 1][f], 1) : 0.0f;
+                        c0[f] = (KS == 3) ? P[i][0][f] + left : P[i][0][f];
+                        c1[f] = P[i][1][f];
                     }
-            }
-        }
-        // merge along x: pixel ax (this lane) takes tap j of anchor ax - j (lane - j)
+                    v0 = (bi & 1u) | ((KS == 3) ? (bl >> 2) & 1u : 0u);
+                    v1 = (bi >> 1) & 1u;
+                } else {
 #pragma unroll
-        for (int i = 0; i < KS; ++i) {
-            const int py = ay + i - y0;  // output pixel row inside the tile
-            float sum[8];
-            unsigned int anyp = 0;
+                    for (int f = 0; f < NA; ++f) {
+                        c0[f] = __shfl_up_sync(0xffffffffu, P[i][1][f], 1);
+                        const float left = (KS == 3) ? __shfl_up_sync(0xffffffffu, P[i][KS - 1][f], 1) : 0.0f;
+                        c1[f] = (KS == 3) ? P[i][0][f] + left : P[i][0][f];
+                    }
+                    v0 = (bl >> 1) & 1u;
+                    v1 = (bi & 1u) | ((KS == 3) ? (bl >> 2) & 1u : 0u);
+                }
+                if (lane >= 1 && py >= 0 && py < TY) {
+                    float *row = gr_part + (size_t)(py * KS + i) * kGrNF * kGrTXO + lx;
 #pragma unroll
-            for (int f = 0; f < 8; ++f) sum[f] = P[i][0][f];
-            anyp |= (anyb >> (i * KS)) & 1u;
-#pragma unroll
-            for (int j = 1; j < KS; ++j) {
-#pragma unroll
-                for (int f = 0; f < 8; ++f) sum[f] += __shfl_up_sync(0xffffffffu, P[i][j][f], j);
-                anyp |= (__shfl_up_sync(0xffffffffu, anyb, j) >> (i * KS + j)) & 1u;
-            }
-            if (lane >= KS - 1 && py >= 0 && py < TY) {
-                float *dst = part[py][i][lane - (KS - 1)];
-#pragma unroll
-                for (int f = 0; f < 8; ++f) dst[f] = sum[f];
-                dst[8] = anyp ? 1.f : 0.f;
+                    for (int f = 0; f < NA; ++f) {
+                        float2 *d = reinterpret_cast<float2 *>(row + f * kGrTXO);
+                        if (pass == 0) {
+                            *d = make_float2(c0[f], c1[f]);
+                        } else {
+                            const float2 o = *d;
+                            *d = make_float2(o.x + c0[f], o.y + c1[f]);
+                        }
+                    }
+                    float2 *dv = reinterpret_cast<float2 *>(row + NA * kGrTXO);
+                    if (pass == 0) {
+                        *dv = make_float2(v0 ? 1.f : 0.f, v1 ? 1.f : 0.f);
+                    } else {
+                        const float2 o = *dv;
+                        *dv = make_float2((o.x != 0.f || v0) ? 1.f : 0.f, (o.y != 0.f || v1) ? 1.f : 0.f);
+                    }
+                }
             }
         }
     }
     __syncthreads();
     // add the tap rows of every pixel in order and normalise (as SetupAcc::store)
     const size_t N = (size_t)W * H;
-    for (int p = threadIdx.x; p < TY * TXO; p += kGrWarps * 32) {
-        const int lx = p % TXO, ly = p / TXO, x = x0 + lx, y = y0 + ly;
+    for (int p = threadIdx.x; p < TY * kGrTXO; p += kGrWarps * 32) {
+        const int px = p % kGrTXO, ly = p / kGrTXO, x = x0 + px, y = y0 + ly;
         if (x >= W || y >= H) continue;
         SetupAcc acc;
         float any = 0.f;
 #pragma unroll
         for (int i = 0; i < KS; ++i) {
-            const float *c = part[ly][i][lx];
-            acc.wn += c[0];
-            acc.u0 += c[1];
-            acc.u1 += c[2];
-            acc.u2 += c[3];
-            acc.nrm += c[4];
-            acc.g0 += c[5];
-            acc.g1 += c[6];
-            acc.g2 += c[7];
-            any += c[8];
+            const float *c = gr_part + (size_t)(ly * KS + i) * kGrNF * kGrTXO + px;
+            acc.wn += c[0 * kGrTXO];
+            acc.u0 += c[1 * kGrTXO];
+            acc.u1 += c[2 * kGrTXO];
+            acc.u2 += c[3 * kGrTXO];
+            acc.nrm += c[4 * kGrTXO];
+            acc.g0 += c[5 * kGrTXO];
+            acc.g1 += c[6 * kGrTXO];
+            any += c[7 * kGrTXO];
         }
+        acc.g2 = acc.wn;
         acc.any = any != 0.f;
         acc.store((size_t)y * W + x, N, s2, vis, U, gx, gy, mask);
     }
@@ -1308,10 +1349,15 @@ static void gradient_setup_ks(const Geometry &G, const Buckets &B, const float *
                               const TS *vgrad, const TS *wgt, float s2, uint8_t *vis, float *U, float *gx,
                               float *gy, float *mask, cudaStream_t st) {
     if constexpr (KS <= 3) {
-        constexpr int TXO = 33 - KS, TY = kGrWarps * 2 - (KS - 1);
-        const dim3 g((G.W + TXO - 1) / TXO, (G.H + TY - 1) / TY);
-        k_gradient_setup_rows<KS, TS><<<g, kGrWarps * 32, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries,
-                                                                 tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask);
+        constexpr int TY = kGrWarps * 2 - (KS - 1);
+        constexpr size_t smem = gradient_rows_smem<KS>();
+        static std::once_flag once;
+        std::call_once(once, [] {
+            cudaFuncSetAttribute(k_gradient_setup_rows<KS, TS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        });
+        const dim3 g((G.W + kGrTXO - 1) / kGrTXO, (G.H + TY - 1) / TY);
+        k_gradient_setup_rows<KS, TS><<<g, kGrWarps * 32, smem, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries,
+                                                                    tau, img, vgrad, wgt, s2, vis, U, gx, gy, mask);
     } else {
         k_gradient_setup_px<KS, TS><<<grid2(G.W, G.H, kTile), kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start,
                                                                             B.entries, tau, img, vgrad, wgt, s2, vis,

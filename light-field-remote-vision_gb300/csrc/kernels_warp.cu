@@ -127,6 +127,31 @@ __device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigne
     const int ymin = A.live ? (B.live ? min(A.ymin, B.ymin) : A.ymin) : B.ymin;
     const int ymax = A.live ? (B.live ? max(A.ymax, B.ymax) : A.ymax) : B.ymax;
     const unsigned int zlow = ~__float_as_uint(zc);
+    if (A.live && B.live && A.sgn != B.sgn) {
+        // Opposite windings (a strip quad that does not fold): the shared edge splits the quad, and a pixel
+        // centre on the edge belongs to the triangle whose edge is top-left (the two flags are complementary),
+        // so only the triangle on the pixel's side is tested. With o = v0 (A) or v3 (B), its other edges are
+        // v2 -> o and o -> v1, and its depth (e12 z_o + e2o z_1 + eo1 z_2) / (e12 + e2o + eo1) equals
+        // tri_cover's (the winding sign cancels in the quotient).
+        for (int y = ymin; y <= ymax; ++y)
+            for (int x = xmin; x <= xmax; ++x) {
+                const float px = x + 0.5f, py = y + 0.5f;
+                const float e12 = edgef(v[1][0], v[1][1], v[2][0], v[2][1], px, py);
+                const float a12 = A.sgn * e12;
+                const bool inA = a12 > 0.f || (a12 == 0.f && A.tl0);
+                const float ox = inA ? v[0][0] : v[3][0], oy = inA ? v[0][1] : v[3][1];
+                const float oz = inA ? v[0][2] : v[3][2], sg = inA ? A.sgn : B.sgn;
+                const bool tla = inA ? A.tl1 : B.tl0, tlb = inA ? A.tl2 : B.tl1;
+                const float ea = edgef(v[2][0], v[2][1], ox, oy, px, py);
+                const float eb = edgef(ox, oy, v[1][0], v[1][1], px, py);
+                const float wa = sg * ea, wb = sg * eb;
+                if (wa < 0.f || wb < 0.f || (wa == 0.f && !tla) || (wb == 0.f && !tlb)) continue;
+                const float w0 = sg * e12;
+                const float iz = (w0 * oz + wa * v[1][2] + wb * v[2][2]) / (w0 + wa + wb);
+                depth_test(x, y, W, iz, zlow, zkey);
+            }
+        return;
+    }
     for (int y = ymin; y <= ymax; ++y)
         for (int x = xmin; x <= xmax; ++x) {
             const float px = x + 0.5f, py = y + 0.5f;
