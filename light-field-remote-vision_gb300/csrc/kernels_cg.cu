@@ -329,47 +329,59 @@ __global__ void __launch_bounds__(256) k_cg_energy(int W, int H, const float *__
 // device_common.cuh. Values written by other blocks inside the launch are read through L2 (__ldcg).
 constexpr int kPersistThreads = 512;
 
-// Sums `count` FP64 partials per slot in a fixed order (identical in every block).
-__device__ void block_reduce_partials(const double *partial, int count, int nslots, double *out_smem) {
-    // one warp: lane-strided sums then a shuffle tree, in FP64 and a fixed order (the FP64 pipe is narrow on
-    // this part, so the other warps stay out of it)
-    if (threadIdx.x < 32) {
-        // the slots' loads interleaved (independent, in flight together); each slot keeps its summation order
-        double s[4] = {0.0, 0.0, 0.0, 0.0};
-#pragma unroll 4
-        for (int i = threadIdx.x; i < count; i += 32) {
+// Sums of nslots slots of count FP64 values (slot s at p + s * stride) into out_smem[s], in FP64 and a fixed order:
+// warp s takes slot s (lane l adds elements l, l + 32, ... in order, eight loads in flight at a time, then a
+// shuffle tree). One warp per slot keeps each slot to one round trip to L2 and puts the slots' FP64 trees on
+// separate warp schedulers (the FP64 pipe is narrow on this part). Needs a block of at least 32 * nslots threads.
+__device__ void reduce_slots(const double *p, int count, size_t stride, int nslots, double *out_smem) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (wid < nslots) {
+        const double *q = p + (size_t)wid * stride;
+        double s = 0.0;
+        for (int base = 0; base < count; base += 256) {
+            double v[8];
 #pragma unroll
-            for (int sl = 0; sl < 4; ++sl)
-                if (sl < nslots) s[sl] += __ldcg(partial + (size_t)sl * count + i);
+            for (int j = 0; j < 8; ++j) {
+                const int i = base + lane + 32 * j;
+                v[j] = i < count ? __ldcg(q + i) : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < 8; ++j) s += v[j];
         }
 #pragma unroll
-        for (int sl = 0; sl < 4; ++sl) {
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s[sl] += __shfl_down_sync(0xffffffffu, s[sl], o);
-            if (threadIdx.x == 0 && sl < nslots) out_smem[sl] = s[sl];
-        }
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) out_smem[wid] = s;
     }
     __syncthreads();
 }
 
-// Block sum of up to 4 per-thread FP32 values: warp trees in FP32 (each lane holds a handful of terms),
-// the warp sums added in FP64 in a fixed order into partial[slot * stride + blockIdx.x].
+__device__ void block_reduce_partials(const double *partial, int count, int nslots, double *out_smem) {
+    reduce_slots(partial, count, (size_t)count, nslots, out_smem);
+}
+
+// Block sum of up to 4 per-thread FP32 values into partial[slot * stride + blockIdx.x]: warp trees in FP32 (each
+// lane holds a handful of terms, the slots interleaved), then warp s adds the warp sums of slot s in FP64 (a
+// shuffle tree, fixed order). Every call site reaches a grid barrier next, whose leading block barrier orders
+// these stores before the barrier's release and the shared buffer before its next use.
 __device__ void block_partials_f(const float v[4], int nslots, double *partial, int stride) {
-    __shared__ float red[kPersistThreads / 32][4];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    for (int sl = 0; sl < nslots; ++sl) {
-        float s = v[sl];
+    __shared__ float red[4][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)(blockDim.x >> 5);
+    float s[4] = {v[0], v[1], v[2], v[3]};
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-        if (lane == 0) red[wid][sl] = s;
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int sl = 0; sl < 4; ++sl) s[sl] += __shfl_down_sync(0xffffffffu, s[sl], o);
+    if (lane == 0) {
+#pragma unroll
+        for (int sl = 0; sl < 4; ++sl) red[sl][wid] = s[sl];
     }
     __syncthreads();
-    if (threadIdx.x < nslots) {
-        double t = 0.0;
-        for (int w = 0; w < (int)(blockDim.x / 32); ++w) t += (double)red[w][threadIdx.x];
-        partial[(size_t)threadIdx.x * stride + blockIdx.x] = t;
+    if (wid < nslots) {
+        double t = lane < nw ? (double)red[wid][lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+        if (lane == 0) partial[(size_t)wid * stride + blockIdx.x] = t;
     }
-    __syncthreads();
 }
 
 // Block sum of up to 4 per-thread values into partial[slot * stride + blockIdx.x] (stride: gridDim.x, or
@@ -747,19 +759,8 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_batch(const CgProblem *_
         block_partials_f(acc, 4, partB, G);
     }
     if (!grid_sync(gb, gen)) return;
-    // the problem's partials sit at [slot * G + b0, slot * G + b0 + nb): one warp sums them in a fixed order
-    auto reduce_own = [&](const double *part, int nslots) {
-        if (threadIdx.x < 32) {
-            for (int sl = 0; sl < nslots; ++sl) {
-                double acc = 0.0;
-                for (int i = threadIdx.x; i < P.nb; i += 32) acc += __ldcg(part + (size_t)sl * G + P.b0 + i);
-#pragma unroll
-                for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-                if (threadIdx.x == 0) sh[sl] = acc;
-            }
-        }
-        __syncthreads();
-    };
+    // the problem's partials sit at [slot * G + b0, slot * G + b0 + nb): one warp per slot sums them in a fixed order
+    auto reduce_own = [&](const double *part, int nslots) { reduce_slots(part + P.b0, P.nb, (size_t)G, nslots, sh); };
     reduce_own(partB, 4);
     double delta[3] = {sh[0], sh[1], sh[2]};
     double E = sh[3];
