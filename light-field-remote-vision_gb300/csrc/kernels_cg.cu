@@ -125,14 +125,12 @@ constexpr int kCgBX = 32, kCgBY = 8;
 // F(x) = lambda/2 |x - u0|^2 + 1/2 |grad x - g|^2 there (the loop lowers it by each step's decrease, so the
 // certified gap always refers to the current iterate). Without a separate anchor (U0 == nullptr) x = u0, as in
 // the reference; with one, U holds a seed (the learned warm start) while u0 keeps the problem unchanged.
-// acc[0..2] += r^2 per channel, acc[3] += the energy.
-__device__ __forceinline__ void cg_start_pixel(int W, int H, size_t N, size_t o, const float *__restrict__ gX,
-                                               const float *__restrict__ gY, const float *__restrict__ U,
-                                               const float *__restrict__ U0, float *__restrict__ r, float lambda,
-                                               float acc[4]) {
-    // 32-bit index arithmetic: images have fewer than 2^31 pixels
-    const unsigned int ou = (unsigned int)o;
-    const int y = (int)(ou / (unsigned int)W), x = (int)(ou - (unsigned int)y * (unsigned int)W);
+// acc[0..2] += r^2 per channel, acc[3] += the energy. cg_start_values returns the residual of pixel (x, y)
+// (o = y W + x) per channel in rv3; cg_start_pixel stores it in r.
+__device__ __forceinline__ void cg_start_values(int W, int H, size_t N, size_t o, int x, int y,
+                                                const float *__restrict__ gX, const float *__restrict__ gY,
+                                                const float *__restrict__ U, const float *__restrict__ U0,
+                                                float lambda, float rv3[3], float acc[4]) {
     const float gxo = __ldg(gX + o), gyo = __ldg(gY + o);
     const float gxl = (x > 0) ? __ldg(gX + o - 1) : 0.f, gyu = (y > 0) ? __ldg(gY + o - W) : 0.f;
 #pragma unroll
@@ -153,7 +151,7 @@ __device__ __forceinline__ void cg_start_pixel(int W, int H, size_t N, size_t o,
             rv += lambda * dv;
             e = lambda * dv * dv;
         }
-        r[c * N + o] = rv;
+        rv3[c] = rv;
         acc[c] += rv * rv;
         if (x < W - 1) {
             const float a = __ldcg(u + o + 1) - uc - gxo;
@@ -165,6 +163,19 @@ __device__ __forceinline__ void cg_start_pixel(int W, int H, size_t N, size_t o,
         }
         acc[3] += 0.5f * e;
     }
+}
+
+__device__ __forceinline__ void cg_start_pixel(int W, int H, size_t N, size_t o, const float *__restrict__ gX,
+                                               const float *__restrict__ gY, const float *__restrict__ U,
+                                               const float *__restrict__ U0, float *__restrict__ r, float lambda,
+                                               float acc[4]) {
+    // 32-bit index arithmetic: images have fewer than 2^31 pixels
+    const unsigned int ou = (unsigned int)o;
+    const int y = (int)(ou / (unsigned int)W), x = (int)(ou - (unsigned int)y * (unsigned int)W);
+    float rv[3];
+    cg_start_values(W, H, N, o, x, y, gX, gY, U, U0, lambda, rv, acc);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) r[c * N + o] = rv[c];
 }
 
 
@@ -443,17 +454,17 @@ constexpr unsigned kIntBytes = 3u * kTileX * kTileY * sizeof(float);  // interio
 constexpr int kBoxStride = ((kBoxBytes + 127) / 128) * 128 / sizeof(float);  // floats between box buffers
 constexpr size_t kCgTmaSmem = 6 * (size_t)kBoxStride * sizeof(float) + 128;   // 2 stages x 3 slots + alignment
 
-// Operator of updateAlpha on a box in shared memory: f(i) is the value at box index i.
-template <class F>
+// Operator of updateAlpha on a box in shared memory: f(i) is the value at box index i, ROW floats per box row.
+template <int ROW = kBoxX, class F>
 __device__ __forceinline__ float box_op(F f, int i, int x, int y, int W, int H, float lambda) {
     const float c = f(i);
     float lx, ly;
     if (x == 0) lx = c - f(i + 1);
     else if (x < W - 1) lx = 2.f * c - f(i - 1) - f(i + 1);
     else lx = c - f(i - 1);
-    if (y == 0) ly = c - f(i + kBoxX);
-    else if (y < H - 1) ly = 2.f * c - f(i - kBoxX) - f(i + kBoxX);
-    else ly = c - f(i - kBoxX);
+    if (y == 0) ly = c - f(i + ROW);
+    else if (y < H - 1) ly = 2.f * c - f(i - ROW) - f(i + ROW);
+    else ly = c - f(i - ROW);
     return lambda * c + lx + ly;
 }
 
@@ -723,6 +734,291 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
         state[2] = delta[2];
         state[3] = E;
         state[4] = gap;
+        state[5] = (double)it;
+    }
+}
+
+// Shared-memory resident form of the corrected CG (the iteration of k_cg_persistent) for images of at most
+// kResMaxTiles tiles per SM. Block b owns tiles b, b + G, ... and keeps r (3 planes) and d (3 planes with a
+// one-pixel halo) of each in shared memory for the whole solve; only u stays in global memory. The phases
+// exchange tile borders alone, through `bord` (set 0: r; sets 1, 2: d by iteration parity, since phase A still
+// reads the previous iteration's d as d_old):
+//   phase A: d = r + beta d_old on the interior; the halo's d from the neighbours' published r and d_old
+//            borders; q = A d, d . q; publish the border rows and columns of d;
+//   phase B: the halo's d from the neighbours' new borders; q = A d; u += alpha d; r -= alpha q, r . r;
+//            publish the borders of r.
+// Per pixel the arithmetic is k_cg_persistent's. Borders written by other blocks are read through L2 (__ldcg)
+// after the grid barrier that follows their writing.
+constexpr int kResThreads = kTileX * kTileY;          // one tile pixel per thread
+constexpr int kResMaxTiles = 7;                       // tiles per block: 7 x 26.5 KB of shared memory
+constexpr int kResPix = kTileX * kTileY;              // r plane (interior only)
+constexpr int kResPlane = kHaloY * kHaloX;            // d plane with its halo: 18 x 66 floats
+constexpr int kResBorder = 2 * kTileX + 2 * kTileY;   // border values per plane: top, bottom, left, right rows
+constexpr size_t kResTileBytes = (size_t)3 * (kResPix + kResPlane) * sizeof(float);
+
+// a / b in FP64 for the solver's scalars: an FP32 reciprocal refined by Newton steps in FP64 (a few dependent
+// FMAs instead of the full division sequence, whose latency sits on the path every block waits for). The
+// result is within a few units in the last place of the rounded quotient; b outside the FP32 range takes
+// the division.
+__device__ __forceinline__ double res_div(double a, double b) {
+    const double ab = fabs(b);
+    if (!(ab > 1e-30 && ab < 1e30)) return a / b;
+    double r = (double)__frcp_rn((float)b);
+    r = fma(r, fma(-b, r, 1.0), r);  // ~46 bits
+    r = fma(r, fma(-b, r, 1.0), r);  // full precision
+    const double q = a * r;
+    return fma(r, fma(-b, q, a), q);
+}
+
+// Halo slot p (in [0, kResBorder)) of a tile at tile coordinates (tx, ty): its index in a d plane, and the
+// neighbour tile and border slot it is read from (nt = -1: outside the image, the value is 0). Border slots:
+// top row [0, 64), bottom row [64, 128), left column [128, 144), right column [144, 160).
+__device__ __forceinline__ void res_halo_slot(int p, int t, int tx, int ty, int tiles_x, int tiles_y, int &si,
+                                              int &nt, int &np) {
+    nt = -1;
+    np = 0;
+    if (p < kTileX) {  // row above <- bottom row of the tile above
+        si = p + 1;
+        if (ty > 0) nt = t - tiles_x, np = kTileX + p;
+    } else if (p < 2 * kTileX) {  // row below <- top row of the tile below
+        const int q = p - kTileX;
+        si = (kTileY + 1) * kHaloX + q + 1;
+        if (ty + 1 < tiles_y) nt = t + tiles_x, np = q;
+    } else if (p < 2 * kTileX + kTileY) {  // left column <- right column of the tile to the left
+        const int q = p - 2 * kTileX;
+        si = (q + 1) * kHaloX;
+        if (tx > 0) nt = t - 1, np = 2 * kTileX + kTileY + q;
+    } else {  // right column <- left column of the tile to the right
+        const int q = p - 2 * kTileX - kTileY;
+        si = (q + 1) * kHaloX + kHaloX - 1;
+        if (tx + 1 < tiles_x) nt = t + 1, np = 2 * kTileX + q;
+    }
+}
+
+__global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(int W, int H, const float *__restrict__ gX,
+                                                                const float *__restrict__ gY, float *__restrict__ U,
+                                                                const float *__restrict__ U0,
+                                                                float *__restrict__ bord, double *__restrict__ partA,
+                                                                double *__restrict__ partB, GridBarrier gb,
+                                                                int max_iter, double gap_tol,
+                                                                double *__restrict__ state) {
+    extern __shared__ __align__(16) float res_smem[];
+    __shared__ double sh[4], s_delta[3], s_dE[3];
+    __shared__ float s_coef[3];
+    __shared__ int s_stop;
+    __shared__ int s_x0[kResMaxTiles], s_y0[kResMaxTiles], s_inner[kResMaxTiles];
+    __shared__ short s_slotD[kResBorder], s_slotR[kResBorder];  // border slot -> index in a d / r plane
+    const size_t N = (size_t)W * H;
+    const int tiles_x = (W + kTileX - 1) / kTileX, tiles_y = (H + kTileY - 1) / kTileY, ntiles = tiles_x * tiles_y;
+    const int nk = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+    const int lx = threadIdx.x % kTileX, ly = threadIdx.x / kTileX;
+    const int si = (ly + 1) * kHaloX + lx + 1;  // this thread's pixel in a d plane
+    float *Rs = res_smem;                       // [tile][plane][kResPix]
+    float *Ds = res_smem + (size_t)nk * 3 * kResPix;  // [tile][plane][kResPlane]
+    const float lambda = 1.0f;
+    unsigned int gen = 0;
+    auto tile_of = [&](int k) { return (int)blockIdx.x + k * (int)gridDim.x; };
+    auto border = [&](int set, int t, int c) { return bord + ((size_t)(set * ntiles + t) * 3 + c) * kResBorder; };
+    if ((int)threadIdx.x < nk) {
+        const int t = tile_of(threadIdx.x), x0 = (t % tiles_x) * kTileX, y0 = (t / tiles_x) * kTileY;
+        s_x0[threadIdx.x] = x0;
+        s_y0[threadIdx.x] = y0;
+        // no pixel of an inner tile sits on the image border: its operator needs no one-sided differences
+        s_inner[threadIdx.x] = (x0 > 0 && y0 > 0 && x0 + kTileX < W && y0 + kTileY < H) ? 1 : 0;
+    }
+    if ((int)threadIdx.x < kResBorder) {
+        const int p = threadIdx.x;
+        int px, py;  // tile pixel of border slot p
+        if (p < kTileX) px = p, py = 0;
+        else if (p < 2 * kTileX) px = p - kTileX, py = kTileY - 1;
+        else if (p < 2 * kTileX + kTileY) px = 0, py = p - 2 * kTileX;
+        else px = kTileX - 1, py = p - 2 * kTileX - kTileY;
+        s_slotD[p] = (short)((py + 1) * kHaloX + px + 1);
+        s_slotR[p] = (short)(py * kTileX + px);
+    }
+    __syncthreads();
+    // Border values of every own tile, one (tile, plane, slot) item at a time: d from the interior of the
+    // shared d planes (D = true) or r from the r planes, into border set `set`.
+    // (item j = (k * 3 + c) * kResBorder + p lands at border(set, tile k, c)[p], i.e. at
+    // bord + (set * ntiles + blockIdx.x) * 3 kResBorder + j + k (gridDim.x - 1) 3 kResBorder)
+    auto publish = [&](int set, bool D) {
+        float *base = bord + ((size_t)set * ntiles + blockIdx.x) * 3 * kResBorder;
+        const size_t kstep = (size_t)(gridDim.x - 1) * 3 * kResBorder;
+        for (int j = threadIdx.x; j < nk * 3 * kResBorder; j += kResThreads) {
+            const int q = j / kResBorder, p = j - q * kResBorder, k = q / 3;  // q = k * 3 + c
+            const float v = D ? Ds[q * kResPlane + s_slotD[p]] : Rs[q * kResPix + s_slotR[p]];
+            base[j + k * kstep] = v;
+        }
+    };
+    // Halo of every own tile's d planes from the neighbours' borders: border(sa) + b_c border(sb) (sb < 0:
+    // border(sa) alone; 0 outside the image). load_halo issues all of a thread's loads into hv / hi,
+    // store_halo writes them to the planes, so other work can run while the loads are in flight.
+    constexpr int kItems = (kResMaxTiles * 3 * kResBorder + kResThreads - 1) / kResThreads;
+    float hv[kItems];
+    int hi[kItems];
+    auto load_halo = [&](int sa, int sb, float b0, float b1, float b2) {
+#pragma unroll
+        for (int u = 0; u < kItems; ++u) {
+            const int j = (int)threadIdx.x + u * kResThreads;
+            hv[u] = 0.f;
+            hi[u] = -1;
+            if (j < nk * 3 * kResBorder) {
+                const int k = j / (3 * kResBorder), rem = j - k * 3 * kResBorder, c = rem / kResBorder;
+                const int t = tile_of(k);
+                int hs, nt, np;
+                res_halo_slot(rem - c * kResBorder, t, t % tiles_x, t / tiles_x, tiles_x, tiles_y, hs, nt, np);
+                hi[u] = (k * 3 + c) * kResPlane + hs;
+                if (nt >= 0) {
+                    hv[u] = __ldcg(border(sa, nt, c) + np);
+                    if (sb >= 0) hv[u] += (c == 0 ? b0 : (c == 1 ? b1 : b2)) * __ldcg(border(sb, nt, c) + np);
+                }
+            }
+        }
+    };
+    auto store_halo = [&]() {
+#pragma unroll
+        for (int u = 0; u < kItems; ++u)
+            if (hi[u] >= 0) Ds[hi[u]] = hv[u];
+    };
+    // q = A d at this thread's pixel of plane Dc (inner tiles: the interior formula of box_op, same arithmetic)
+    auto op_at = [&](const float *Dc, bool inner, int x, int y) {
+        if (inner) {
+            const float c = Dc[si];
+            const float lxv = 2.f * c - Dc[si - 1] - Dc[si + 1];
+            const float lyv = 2.f * c - Dc[si - kHaloX] - Dc[si + kHaloX];
+            return lambda * c + lxv + lyv;
+        }
+        return box_op<kHaloX>([&](int i) { return Dc[i]; }, si, x, y, W, H, lambda);
+    };
+    // ---- phase 0: r = b - A x and the energy F(x); d_old = 0 (interior and published borders)
+    {
+        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int k = 0; k < nk; ++k) {
+            const int x = s_x0[k] + lx, y = s_y0[k] + ly;
+            float rv[3] = {0.f, 0.f, 0.f};
+            if (x < W && y < H) cg_start_values(W, H, N, (size_t)y * W + x, x, y, gX, gY, U, U0, lambda, rv, acc);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                Rs[(k * 3 + c) * kResPix + threadIdx.x] = rv[c];
+                Ds[(k * 3 + c) * kResPlane + si] = 0.f;
+            }
+        }
+        __syncthreads();
+        publish(0, false);
+        publish(2, true);
+        block_partials_f(acc, 4, partB, gridDim.x);
+    }
+    if (!grid_sync(gb, gen)) return;
+    block_reduce_partials(partB, gridDim.x, 4, sh);
+    if (threadIdx.x < 3) s_delta[threadIdx.x] = sh[threadIdx.x];
+    double E = sh[3];  // thread 0's copy is the one in use
+    float beta[3] = {0.f, 0.f, 0.f};
+    int it = 0;
+    __syncthreads();
+    for (;; ++it) {
+        if (threadIdx.x == 0) {
+            // gap = bound / (E - bound) <= gap_tol, tested without the division
+            const double bound = (s_delta[0] + s_delta[1] + s_delta[2]) / (2.0 * (double)lambda);
+            const double room = E - bound;
+            s_stop = (it >= max_iter || (gap_tol > 0 && room > 0 && bound <= gap_tol * room)) ? 1 : 0;
+        }
+        __syncthreads();
+        if (s_stop) break;
+        const int dold = 1 + ((it + 1) & 1), dnew = 1 + (it & 1);
+        // ---- phase A: d = r + beta d_old (halo from the neighbours' borders, interior in place); publish d's
+        // borders; q = A d and d . q
+        load_halo(0, dold, beta[0], beta[1], beta[2]);
+        for (int k = 0; k < nk; ++k)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float *d = Ds + (k * 3 + c) * kResPlane + si;
+                *d = Rs[(k * 3 + c) * kResPix + threadIdx.x] + beta[c] * *d;
+            }
+        store_halo();
+        __syncthreads();
+        publish(dnew, true);
+        float accA[4] = {0.f, 0.f, 0.f, 0.f};
+        for (int k = 0; k < nk; ++k) {
+            const int x = s_x0[k] + lx, y = s_y0[k] + ly;
+            if (x >= W || y >= H) continue;
+            const bool inner = s_inner[k] != 0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const float *Dc = Ds + (k * 3 + c) * kResPlane;
+                accA[c] += Dc[si] * op_at(Dc, inner, x, y);
+            }
+        }
+        block_partials_f(accA, 3, partA, gridDim.x);
+        if (!grid_sync(gb, gen)) return;
+        block_reduce_partials(partA, gridDim.x, 3, sh);
+        // the three step lengths on three threads (the FP64 divisions side by side)
+        if (threadIdx.x < 3) {
+            const int c = threadIdx.x;
+            const double alpha_d = (sh[c] > 0) ? res_div(s_delta[c], sh[c]) : 0.0;
+            s_coef[c] = (float)alpha_d;
+            s_dE[c] = 0.5 * alpha_d * s_delta[c];
+        }
+        __syncthreads();
+        const float alpha[3] = {s_coef[0], s_coef[1], s_coef[2]};
+        if (threadIdx.x == 0) E = E - s_dE[0] - s_dE[1] - s_dE[2];
+        // ---- phase B: the halo's d from the neighbours' new borders; u += alpha d, r -= alpha A d, r . r;
+        // publish r's borders
+        load_halo(dnew, -1, 0.f, 0.f, 0.f);
+        store_halo();
+        __syncthreads();
+        float accB[4] = {0.f, 0.f, 0.f, 0.f};
+        // u of the next tile is loaded while the current one is updated
+        auto load_u = [&](int k, float u3[3]) {
+            const int x = s_x0[k] + lx, y = s_y0[k] + ly;
+            const bool in = x < W && y < H;
+            const size_t o = (size_t)y * W + x;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) u3[c] = in ? __ldcg(U + c * N + o) : 0.f;
+        };
+        float ucur[3] = {0.f, 0.f, 0.f};
+        if (nk > 0) load_u(0, ucur);
+        for (int k = 0; k < nk; ++k) {
+            float unext[3] = {0.f, 0.f, 0.f};
+            if (k + 1 < nk) load_u(k + 1, unext);
+            const int x = s_x0[k] + lx, y = s_y0[k] + ly;
+            if (x < W && y < H) {
+                const bool inner = s_inner[k] != 0;
+                const size_t o = (size_t)y * W + x;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    const float *Dc = Ds + (k * 3 + c) * kResPlane;
+                    float *Rc = Rs + (k * 3 + c) * kResPix + threadIdx.x;
+                    const float qv = op_at(Dc, inner, x, y);
+                    U[c * N + o] = ucur[c] + alpha[c] * Dc[si];
+                    const float rv = *Rc - alpha[c] * qv;
+                    *Rc = rv;
+                    accB[c] += rv * rv;
+                }
+            }
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ucur[c] = unext[c];
+        }
+        __syncthreads();
+        publish(0, false);
+        block_partials_f(accB, 3, partB, gridDim.x);
+        if (!grid_sync(gb, gen)) return;
+        block_reduce_partials(partB, gridDim.x, 3, sh);
+        if (threadIdx.x < 3) {
+            const int c = threadIdx.x;
+            s_coef[c] = (s_delta[c] > 0) ? (float)res_div(sh[c], s_delta[c]) : 0.f;
+            s_delta[c] = sh[c];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int c = 0; c < 3; ++c) beta[c] = s_coef[c];
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const double bound = (s_delta[0] + s_delta[1] + s_delta[2]) / (2.0 * (double)lambda);
+        state[0] = s_delta[0];
+        state[1] = s_delta[1];
+        state[2] = s_delta[2];
+        state[3] = E;
+        state[4] = (E - bound) > 0 ? bound / (E - bound) : 1e300;
         state[5] = (double)it;
     }
 }
@@ -1118,6 +1414,30 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
     ProfScope _ps(lc, "cg_persistent", st);
     const size_t N = (size_t)W * H;
     const int ntiles = ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
+    // shared-memory resident form when every block can hold its tiles (one block per SM) and the tile borders
+    // (3 sets x 3 planes x 160 floats per tile) fit in dA
+    {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        static std::once_flag once;
+        std::call_once(once, [] {
+            cudaFuncSetAttribute(k_cg_resident, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)(kResMaxTiles * kResTileBytes));
+        });
+        const int per = (ntiles + sms - 1) / std::max(sms, 1);
+        const size_t smem = (size_t)per * kResTileBytes;
+        if (per <= kResMaxTiles && (size_t)9 * kResBorder * ntiles <= 3 * N &&
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cg_resident, kResThreads, smem) == cudaSuccess &&
+            per_sm >= 1) {
+            const int blocks = (ntiles + per - 1) / per;
+            void *args[] = {&W, &H, (void *)&gx, (void *)&gy, &U, (void *)&U0, &dA, &partA, &partB, &gb,
+                            &max_iter, &gap_tol, &state};
+            lc.add(1);
+            return cudaLaunchCooperativeKernel((const void *)k_cg_resident, dim3(blocks), dim3(kResThreads), args,
+                                               smem, st);
+        }
+    }
     // the TMA form needs row pitches of a multiple of 16 bytes (W % 4 == 0) and the driver's encoder
     CUtensorMap maps[5];
     const bool tma = encode_tensor_map_3d(&maps[0], r, W, H, 3, kBoxX, kBoxY, 3) &&
