@@ -168,17 +168,90 @@ __device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigne
         }
 }
 
-__global__ void __launch_bounds__(256, 6) k_zsplat(int V, int w, int h, const float *__restrict__ depth,
-                                                const WarpCams cams, int W, int H,
-                                                unsigned long long *__restrict__ zkey) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    const int v = blockIdx.y;
-    const int n = w * h;
-    if (m >= n) return;
-    const float *dz = depth + (size_t)v * 3 * n;
-    const float z = dz[m], zx = dz[n + m], zy = dz[2 * n + m];
+// raster_quad for the common quad: its two triangles have opposite windings (the strip does not fold) and its
+// box holds at most 3 x 3 pixel centres. Coverage and depth are tri_cover's for each triangle:
+//   - a centre is tested against the triangle on its side of the shared edge v1v2 only (a centre on that edge
+//     belongs to the triangle for which the edge is top-left; the two flags are complementary);
+//   - edge values are taken relative to the box's first centre (the same differences as edgef's) and scaled
+//     by the triangle's winding sign, so "inside" is w >= thr on every edge, with thr = 0 on a top-left edge
+//     and the smallest positive float elsewhere (the library is built without flush-to-zero);
+//   - the depth is tri_cover's quotient, its terms in the same order.
+// The 3 x 3 window is unrolled. Returns false when the quad needs raster_quad.
+__device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc, int W, int H,
+                                                  unsigned long long *zkey) {
+    const float areaA = edgef(v[0][0], v[0][1], v[1][0], v[1][1], v[2][0], v[2][1]);
+    const float areaB = edgef(v[1][0], v[1][1], v[2][0], v[2][1], v[3][0], v[3][1]);
+    if (!(areaA != 0.f && areaB != 0.f && ((areaA > 0.f) != (areaB > 0.f)))) return false;
+    const float x_lo = fminf(fminf(v[0][0], v[1][0]), fminf(v[2][0], v[3][0]));
+    const float x_hi = fmaxf(fmaxf(v[0][0], v[1][0]), fmaxf(v[2][0], v[3][0]));
+    const float y_lo = fminf(fminf(v[0][1], v[1][1]), fminf(v[2][1], v[3][1]));
+    const float y_hi = fmaxf(fmaxf(v[0][1], v[1][1]), fmaxf(v[2][1], v[3][1]));
+    const int xmin = max(0, (int)ceilf(x_lo - 0.5f)), xmax = min(W - 1, (int)floorf(x_hi - 0.5f));
+    const int ymin = max(0, (int)ceilf(y_lo - 0.5f)), ymax = min(H - 1, (int)floorf(y_hi - 0.5f));
+    if (xmax < xmin || ymax < ymin) return true;  // no pixel centre in the box
+    if (xmax - xmin > 2 || ymax - ymin > 2) return false;
+    const float ox = (float)xmin + 0.5f, oy = (float)ymin + 0.5f;
+    float qx[4], qy[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        qx[k] = v[k][0] - ox;
+        qy[k] = v[k][1] - oy;
+    }
+    const bool ccwA = areaA > 0.f;
+    const float sA = ccwA ? 1.f : -1.f;
+    constexpr float kTiny = 1.40129846e-45f;  // smallest positive float: w >= kTiny is w > 0
+    // edge a -> b scaled by s: w(i, j) = (s dx)(j - qy[a]) - (s dy)(i - qx[a])
+    struct Edge {
+        float ax, ay, dx, dy, thr;
+    };
+    auto edge = [&](int a, int b, float s, bool ccw) {
+        Edge e;
+        e.ax = qx[a];
+        e.ay = qy[a];
+        e.dx = s * (qx[b] - qx[a]);
+        e.dy = s * (qy[b] - qy[a]);
+        e.thr = top_left(qx[a], qy[a], qx[b], qy[b], ccw) ? 0.f : kTiny;
+        return e;
+    };
+    const Edge e12 = edge(1, 2, sA, ccwA), a1 = edge(2, 0, sA, ccwA), a2 = edge(0, 1, sA, ccwA);
+    const Edge b0 = edge(2, 3, -sA, !ccwA), b1 = edge(3, 1, -sA, !ccwA);
+    auto w = [](const Edge &e, float i, float j) { return e.dx * (j - e.ay) - e.dy * (i - e.ax); };
+    const unsigned int zlow = ~__float_as_uint(zc);
+    // one row of the window at a time: the three cells' keys, then their depth-buffer loads together (the
+    // depth test of depth_test, its loads not serialised behind each other's branches)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+        if (j > ymax - ymin) break;
+        unsigned long long *row = zkey + (size_t)(ymin + j) * W + xmin;
+        unsigned long long key[3], cur[3];
+        bool hit[3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+            const float fi = (float)i, fj = (float)j;
+            const float w12 = w(e12, fi, fj);
+            const bool inA = w12 >= e12.thr;
+            const float wa1 = w(a1, fi, fj), wa2 = w(a2, fi, fj), wb0 = w(b0, fi, fj), wb1 = w(b1, fi, fj);
+            const bool cov = inA ? (wa1 >= a1.thr && wa2 >= a2.thr) : (wb0 >= b0.thr && wb1 >= b1.thr);
+            // A = (v0, v1, v2) with weights (w12, wa1, wa2); B = (v1, v2, v3) with (wb0, wb1, -w12)
+            const float w0 = inA ? w12 : wb0, w1 = inA ? wa1 : wb1, w2 = inA ? wa2 : -w12;
+            const float z0 = inA ? v[0][2] : v[1][2], z1 = inA ? v[1][2] : v[2][2], z2 = inA ? v[2][2] : v[3][2];
+            const float iz = (w0 * z0 + w1 * z1 + w2 * z2) / (w0 + w1 + w2);
+            hit[i] = i <= xmax - xmin && cov && iz > 0.f;
+            key[i] = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
+        }
+#pragma unroll
+        for (int i = 0; i < 3; ++i) cur[i] = hit[i] ? __ldcg(row + i) : ~0ull;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+            if (hit[i] && cur[i] < key[i]) atomicMax(row + i, key[i]);
+    }
+    return true;
+}
+
+// One input pixel m of view cam c: its tilted quad into the depth buffer.
+__device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int m, int w, float z, float zx, float zy, int W,
+                                             int H, unsigned long long *zkey) {
     if (z >= 1000.0f * 0.5f) return;  // INVALID_DEPTH / 2 (depthSplatting.geom:21)
-    const ViewCam c = view_cam(cams, v);
     const float cx = (m % w) + 0.5f, cy = (m / w) + 0.5f;
     float xh[3];
     warp_point(c, cx, cy, z, xh);
@@ -195,7 +268,27 @@ __global__ void __launch_bounds__(256, 6) k_zsplat(int V, int w, int h, const fl
         vert[k][1] = xh[1] * iw;
         vert[k][2] = iw;
     }
-    raster_quad(vert, zc, W, H, zkey);
+    if (!raster_quad_small(vert, zc, W, H, zkey)) raster_quad(vert, zc, W, H, zkey);
+}
+
+// Two input pixels per thread (m and m + blockDim.x): the second pixel's depth is loaded before the first is
+// rasterised, so its latency hides behind that work.
+constexpr int kZsplatPerThread = 2;
+
+__global__ void __launch_bounds__(256, 4) k_zsplat(int V, int w, int h, const float *__restrict__ depth,
+                                                const WarpCams cams, int W, int H,
+                                                unsigned long long *__restrict__ zkey) {
+    const int m0 = blockIdx.x * blockDim.x * kZsplatPerThread + threadIdx.x, m1 = m0 + blockDim.x;
+    const int v = blockIdx.y;
+    const int n = w * h;
+    if (m0 >= n) return;
+    const float *dz = depth + (size_t)v * 3 * n;
+    const float z0 = dz[m0], zx0 = dz[n + m0], zy0 = dz[2 * n + m0];
+    float z1 = 0.f, zx1 = 0.f, zy1 = 0.f;
+    if (m1 < n) z1 = dz[m1], zx1 = dz[n + m1], zy1 = dz[2 * n + m1];
+    const ViewCam c = view_cam(cams, v);
+    zsplat_pixel(c, m0, w, z0, zx0, zy0, W, H, zkey);
+    if (m1 < n) zsplat_pixel(c, m1, w, z1, zx1, zy1, W, H, zkey);
 }
 
 __global__ void k_zresolve(size_t N, const unsigned long long *__restrict__ zkey, float *__restrict__ zbuf) {
@@ -298,7 +391,8 @@ void launch_zbuffer_splat(int V, int w, int h, const float *depth, const WarpCam
                           unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "zbuffer_splat", st);
     const int n = w * h;
-    k_zsplat<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zkey);
+    const int per_block = 256 * kZsplatPerThread;
+    k_zsplat<<<dim3((n + per_block - 1) / per_block, V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zkey);
     lc.add(1);
 }
 
