@@ -56,19 +56,37 @@ __global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const
     entries[slot] = ((unsigned int)v << 24) | (unsigned int)m;
 }
 
-// Orders each bucket by (view, pixel) so the gathers sum in a fixed order.
-__global__ void k_bucket_sort(int nb, const unsigned int *__restrict__ start, unsigned int *__restrict__ entries) {
-    const int b = blockIdx.x * blockDim.x + threadIdx.x;
-    if (b >= nb) return;
-    const unsigned int s = start[b], e = start[b + 1];
+// Orders each bucket by (view, pixel) so the gathers sum in a fixed order. A block takes 256 consecutive buckets,
+// whose entries are contiguous: when they fit, the block stages them in shared memory with coalesced loads,
+// each thread insertion-sorts its bucket there, and the block writes them back coalesced; a larger group
+// sorts in global memory, one bucket per thread.
+constexpr int kSortBuckets = 256, kSortCap = 8192;
+
+__device__ __forceinline__ void insertion_sort(unsigned int *a, unsigned int s, unsigned int e) {
     for (unsigned int i = s + 1; i < e; ++i) {
-        const unsigned int key = entries[i];
+        const unsigned int key = a[i];
         unsigned int j = i;
-        while (j > s && entries[j - 1] > key) {
-            entries[j] = entries[j - 1];
+        while (j > s && a[j - 1] > key) {
+            a[j] = a[j - 1];
             --j;
         }
-        entries[j] = key;
+        a[j] = key;
+    }
+}
+
+__global__ void __launch_bounds__(kSortBuckets) k_bucket_sort(int nb, const unsigned int *__restrict__ start,
+                                                              unsigned int *__restrict__ entries) {
+    __shared__ unsigned int buf[kSortCap];
+    const int b0 = blockIdx.x * kSortBuckets, b1 = min(b0 + kSortBuckets, nb), b = b0 + (int)threadIdx.x;
+    const unsigned int S = start[b0], E = start[b1];
+    if (E - S <= (unsigned int)kSortCap) {
+        for (unsigned int i = threadIdx.x; i < E - S; i += kSortBuckets) buf[i] = entries[S + i];
+        __syncthreads();
+        if (b < b1) insertion_sort(buf, start[b] - S, start[b + 1] - S);
+        __syncthreads();
+        for (unsigned int i = threadIdx.x; i < E - S; i += kSortBuckets) entries[S + i] = buf[i];
+    } else if (b < b1) {
+        insertion_sort(entries, start[b], start[b + 1]);
     }
 }
 
@@ -1080,7 +1098,7 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
     lc.add(2);
     cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
     k_bucket_fill<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.start, B.count, B.entries);
-    k_bucket_sort<<<(B.nb + 255) / 256, 256, 0, st>>>(B.nb, B.start, B.entries);
+    k_bucket_sort<<<(B.nb + kSortBuckets - 1) / kSortBuckets, kSortBuckets, 0, st>>>(B.nb, B.start, B.entries);
     lc.add(2);
     (void)ks;
 }
