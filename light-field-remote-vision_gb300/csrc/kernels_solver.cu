@@ -29,31 +29,64 @@ __device__ __forceinline__ void stv(__nv_bfloat16 *p, float v) { *p = __float2bf
 
 
 // ====================================================================== inverse footprint map
-__global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
-                               unsigned int *__restrict__ cnt) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    const int v = blockIdx.y;
-    if (m >= n) return;
-    const float tx = tau[(size_t)v * 2 * n + m], ty = tau[(size_t)v * 2 * n + n + m];
-    if (!in_splat(tx, ty, W, H)) return;
+// Count and fill take kBucketPer source pixels per thread (m, m + blockDim.x, ...): each stage's loads and atomics
+// for all of them are issued before any result is used, so their round trips to L2 overlap. Bucket of a
+// splatted source pixel: its footprint anchor, offset by ks - 1 (-1: not splatted).
+constexpr int kBucketPer = 4;
+
+__device__ __forceinline__ long long bucket_of(float tx, float ty, int W, int H, int dsf, int BW) {
+    if (!in_splat(tx, ty, W, H)) return -1;
     const int ks = dsf + 1;
     const int x0 = fp_anchor(tx - 0.5f, dsf), y0 = fp_anchor(ty - 0.5f, dsf);
-    atomicAdd(&cnt[(size_t)(y0 + ks - 1) * BW + (x0 + ks - 1)], 1u);
+    return (long long)(y0 + ks - 1) * BW + (x0 + ks - 1);
+}
+
+__global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
+                               unsigned int *__restrict__ cnt) {
+    const int m0 = blockIdx.x * blockDim.x * kBucketPer + threadIdx.x;
+    const float *tv = tau + (size_t)blockIdx.y * 2 * n;
+    float tx[kBucketPer], ty[kBucketPer];
+#pragma unroll
+    for (int j = 0; j < kBucketPer; ++j) {
+        const int m = min(m0 + j * (int)blockDim.x, n - 1);
+        tx[j] = tv[m];
+        ty[j] = tv[n + m];
+    }
+#pragma unroll
+    for (int j = 0; j < kBucketPer; ++j) {
+        const long long b = bucket_of(tx[j], ty[j], W, H, dsf, BW);
+        if (m0 + j * (int)blockDim.x < n && b >= 0) atomicAdd(&cnt[b], 1u);
+    }
 }
 
 __global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
                               const unsigned int *__restrict__ start, unsigned int *__restrict__ cursor,
                               unsigned int *__restrict__ entries) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
     const int v = blockIdx.y;
-    if (m >= n) return;
-    const float tx = tau[(size_t)v * 2 * n + m], ty = tau[(size_t)v * 2 * n + n + m];
-    if (!in_splat(tx, ty, W, H)) return;
-    const int ks = dsf + 1;
-    const int x0 = fp_anchor(tx - 0.5f, dsf), y0 = fp_anchor(ty - 0.5f, dsf);
-    const size_t b = (size_t)(y0 + ks - 1) * BW + (x0 + ks - 1);
-    const unsigned int slot = start[b] + atomicAdd(&cursor[b], 1u);
-    entries[slot] = ((unsigned int)v << 24) | (unsigned int)m;
+    const int m0 = blockIdx.x * blockDim.x * kBucketPer + threadIdx.x;
+    const float *tv = tau + (size_t)v * 2 * n;
+    float tx[kBucketPer], ty[kBucketPer];
+#pragma unroll
+    for (int j = 0; j < kBucketPer; ++j) {
+        const int m = min(m0 + j * (int)blockDim.x, n - 1);
+        tx[j] = tv[m];
+        ty[j] = tv[n + m];
+    }
+    long long b[kBucketPer];
+    unsigned int slot[kBucketPer], base[kBucketPer];
+#pragma unroll
+    for (int j = 0; j < kBucketPer; ++j) {
+        b[j] = m0 + j * (int)blockDim.x < n ? bucket_of(tx[j], ty[j], W, H, dsf, BW) : -1;
+        slot[j] = 0u;
+        base[j] = 0u;
+        if (b[j] >= 0) {
+            slot[j] = atomicAdd(&cursor[b[j]], 1u);
+            base[j] = start[b[j]];
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < kBucketPer; ++j)
+        if (b[j] >= 0) entries[base[j] + slot[j]] = ((unsigned int)v << 24) | (unsigned int)(m0 + j * (int)blockDim.x);
 }
 
 // Orders each bucket by (view, pixel) so the gathers sum in a fixed order. A block takes 256 consecutive buckets,
@@ -1086,7 +1119,7 @@ static inline dim3 grid2(int W, int H, dim3 b) { return dim3((W + b.x - 1) / b.x
 void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "bucket_build", st);
     const int ks = G.dsf + 1;
-    const dim3 b1(256), gs((G.n + 255) / 256, G.V);
+    const dim3 b1(256), gs((G.n + 256 * kBucketPer - 1) / (256 * kBucketPer), G.V);
     cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
     k_bucket_count<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.count);
     lc.add(1);
