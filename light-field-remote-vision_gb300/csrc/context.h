@@ -31,7 +31,7 @@ struct Workspace {
     // per view
     DevBuf img, tau, dp, wgt, res, vgrad, depth, tau_in, dpart_in, cams;
     // inverse footprint map
-    DevBuf b_count, b_start, b_entries, b_aux;
+    DevBuf b_count, b_start, b_entries, b_aux, b_mask;
     // target
     DevBuf U, Ua, Ub, Uprev, P, Pa, F, G, g, g0, tmp, cov, norm, vis, Xq, gx, gy, mask, zkey, zbuf;
     // gradient data term (dt_beta)

@@ -178,6 +178,11 @@ static Buckets build_buckets(lfrv_ctx *c, const Geometry &G, const float *tau2) 
     B.count = ws.b_count.as<unsigned int>();
     B.start = ws.b_start.as<unsigned int>();
     B.entries = ws.b_entries.as<unsigned int>();
+    B.mask = nullptr;
+    if (G.V <= 64) {
+        ws.b_mask.ensure(sizeof(unsigned long long) * B.nb);
+        B.mask = ws.b_mask.as<unsigned long long>();
+    }
     B.block_sums = aux;
     B.block_offsets = aux + nblk;
     B.block_sums2 = aux + 2 * nblk;

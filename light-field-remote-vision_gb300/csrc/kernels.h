@@ -36,6 +36,7 @@ struct Buckets {
     int BW, BH, nb;                     // bucket grid (W + ks - 1) x (H + ks - 1)
     unsigned int *count, *start;        // nb, nb + 1
     unsigned int *entries;              // V * n capacity, (view << 24) | pixel
+    unsigned long long *mask;           // nb: bit v set when view v lands in the bucket (V <= 64), else null
     unsigned int *block_sums, *block_offsets, *block_sums2, *block_offsets2, *total, *total2;
 };
 

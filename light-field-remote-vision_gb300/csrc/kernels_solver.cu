@@ -32,6 +32,10 @@ __device__ __forceinline__ void stv(__nv_bfloat16 *p, float v) { *p = __float2bf
 // Count and fill take kBucketPer source pixels per thread (m, m + blockDim.x, ...): each stage's loads and atomics
 // for all of them are issued before any result is used, so their round trips to L2 overlap. Bucket of a
 // splatted source pixel: its footprint anchor, offset by ks - 1 (-1: not splatted).
+// With a view mask (V <= 64) the count also sets bit v of its bucket's mask. A bucket whose count equals the
+// mask's population holds one entry per view, and the entry of view v goes to slot popc(mask & (2^v - 1)):
+// already in (view, pixel) order, with no atomic in the fill and nothing for the sort to do. Only buckets with
+// two entries of one view take slots from the cursor (in arrival order) and need the sort.
 constexpr int kBucketPer = 4;
 
 __device__ __forceinline__ long long bucket_of(float tx, float ty, int W, int H, int dsf, int BW) {
@@ -42,7 +46,7 @@ __device__ __forceinline__ long long bucket_of(float tx, float ty, int W, int H,
 }
 
 __global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
-                               unsigned int *__restrict__ cnt) {
+                               unsigned int *__restrict__ cnt, unsigned long long *__restrict__ mask) {
     const int m0 = blockIdx.x * blockDim.x * kBucketPer + threadIdx.x;
     const float *tv = tau + (size_t)blockIdx.y * 2 * n;
     float tx[kBucketPer], ty[kBucketPer];
@@ -55,13 +59,21 @@ __global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, cons
 #pragma unroll
     for (int j = 0; j < kBucketPer; ++j) {
         const long long b = bucket_of(tx[j], ty[j], W, H, dsf, BW);
-        if (m0 + j * (int)blockDim.x < n && b >= 0) atomicAdd(&cnt[b], 1u);
+        if (m0 + j * (int)blockDim.x < n && b >= 0) {
+            atomicAdd(&cnt[b], 1u);
+            if (mask) atomicOr(&mask[b], 1ull << blockIdx.y);
+        }
     }
+}
+
+// Whether bucket b's entries must come from the cursor and be sorted (see above).
+__device__ __forceinline__ bool bucket_dup(const unsigned int *start, const unsigned long long *mask, long long b) {
+    return !mask || start[b + 1] - start[b] != (unsigned int)__popcll(mask[b]);
 }
 
 __global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
                               const unsigned int *__restrict__ start, unsigned int *__restrict__ cursor,
-                              unsigned int *__restrict__ entries) {
+                              const unsigned long long *__restrict__ mask, unsigned int *__restrict__ entries) {
     const int v = blockIdx.y;
     const int m0 = blockIdx.x * blockDim.x * kBucketPer + threadIdx.x;
     const float *tv = tau + (size_t)v * 2 * n;
@@ -80,8 +92,9 @@ __global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const
         slot[j] = 0u;
         base[j] = 0u;
         if (b[j] >= 0) {
-            slot[j] = atomicAdd(&cursor[b[j]], 1u);
             base[j] = start[b[j]];
+            if (bucket_dup(start, mask, b[j])) slot[j] = atomicAdd(&cursor[b[j]], 1u);
+            else slot[j] = (unsigned int)__popcll(mask[b[j]] & ((1ull << v) - 1ull));
         }
     }
 #pragma unroll
@@ -89,10 +102,11 @@ __global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const
         if (b[j] >= 0) entries[base[j] + slot[j]] = ((unsigned int)v << 24) | (unsigned int)(m0 + j * (int)blockDim.x);
 }
 
-// Orders each bucket by (view, pixel) so the gathers sum in a fixed order. A block takes 256 consecutive buckets,
-// whose entries are contiguous: when they fit, the block stages them in shared memory with coalesced loads,
-// each thread insertion-sorts its bucket there, and the block writes them back coalesced; a larger group
-// sorts in global memory, one bucket per thread.
+// Orders each bucket by (view, pixel) so the gathers sum in a fixed order. With a view mask, the buckets that
+// hold two entries of one view (the only ones filled out of order) sort themselves in global memory. Without
+// one, a block takes 256 consecutive buckets, whose entries are contiguous: when they fit, the block stages them
+// in shared memory with coalesced loads, each thread insertion-sorts its bucket there, and the block writes
+// them back coalesced; a larger group sorts in global memory, one bucket per thread.
 constexpr int kSortBuckets = 256, kSortCap = 8192;
 
 __device__ __forceinline__ void insertion_sort(unsigned int *a, unsigned int s, unsigned int e) {
@@ -108,9 +122,15 @@ __device__ __forceinline__ void insertion_sort(unsigned int *a, unsigned int s, 
 }
 
 __global__ void __launch_bounds__(kSortBuckets) k_bucket_sort(int nb, const unsigned int *__restrict__ start,
+                                                              const unsigned long long *__restrict__ mask,
                                                               unsigned int *__restrict__ entries) {
     __shared__ unsigned int buf[kSortCap];
     const int b0 = blockIdx.x * kSortBuckets, b1 = min(b0 + kSortBuckets, nb), b = b0 + (int)threadIdx.x;
+    // with a view mask only the buckets with two entries of one view need the sort: each sorts itself in place
+    if (mask) {
+        if (b < b1 && bucket_dup(start, mask, b)) insertion_sort(entries, start[b], start[b + 1]);
+        return;
+    }
     const unsigned int S = start[b0], E = start[b1];
     if (E - S <= (unsigned int)kSortCap) {
         for (unsigned int i = threadIdx.x; i < E - S; i += kSortBuckets) buf[i] = entries[S + i];
@@ -1121,7 +1141,8 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
     const int ks = G.dsf + 1;
     const dim3 b1(256), gs((G.n + 256 * kBucketPer - 1) / (256 * kBucketPer), G.V);
     cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
-    k_bucket_count<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.count);
+    if (B.mask) cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb, st);
+    k_bucket_count<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.count, B.mask);
     lc.add(1);
     // exclusive scan of the counts: block-local scans, then every block adds the sum of the block totals before
     // it (integer sums, so the result does not depend on the order) and the last block writes the total
@@ -1130,8 +1151,9 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
     k_scan_finish<<<nblk, kScanBlock, 0, st>>>(B.nb, B.start, B.block_sums);
     lc.add(2);
     cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
-    k_bucket_fill<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.start, B.count, B.entries);
-    k_bucket_sort<<<(B.nb + kSortBuckets - 1) / kSortBuckets, kSortBuckets, 0, st>>>(B.nb, B.start, B.entries);
+    k_bucket_fill<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.start, B.count, B.mask, B.entries);
+    k_bucket_sort<<<(B.nb + kSortBuckets - 1) / kSortBuckets, kSortBuckets, 0, st>>>(B.nb, B.start, B.mask,
+                                                                                      B.entries);
     lc.add(2);
     (void)ks;
 }
