@@ -314,69 +314,102 @@ __device__ __forceinline__ float bilinear_clamp(const float *img, int W, int H, 
            ay * ((1.f - ax) * at(x0, y0 + 1) + ax * at(x0 + 1, y0 + 1));
 }
 
-__global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *__restrict__ depth,
-                                             const WarpCams cams, int W, int H,
-                                             const float *__restrict__ zbuf, float *__restrict__ tau3,
-                                             float *__restrict__ dpart3, float *__restrict__ tau2,
-                                             float *__restrict__ dp2) {
-    const int m = blockIdx.x * blockDim.x + threadIdx.x;
-    const int v = blockIdx.y;
-    const int n = w * h;
-    if (m >= n) return;
-    const float *dz = depth + (size_t)v * 3 * n;
-    const float z = dz[m], zx = dz[n + m], zy = dz[2 * n + m];
-    const ViewCam c = view_cam(cams, v);
+// k_tau takes kTauPer source pixels per thread (m, m + blockDim.x): both are projected, then both bilinear
+// samples of the target depth map are issued, then both are finished, so the dependent loads overlap.
+constexpr int kTauPer = 2;
+
+struct TauPix {
+    float z, xu, yu, zt, deform, rx, ry;  // zt: the point's depth in the target camera
+};
+
+__device__ __forceinline__ TauPix tau_project(const ViewCam &c, int m, int w, float z, float zx, float zy) {
+    TauPix p;
+    p.z = z;
     const float x = (m % w) + 0.5f, y = (m / w) + 0.5f;
     float xuh[3];
     warp_point(c, x, y, z, xuh);
-    float xu = 0.f, yu = 0.f;
+    p.xu = 0.f;
+    p.yu = 0.f;
     if (xuh[2] != 0.f) {
-        xu = xuh[0] / xuh[2];
-        yu = xuh[1] / xuh[2];
+        p.xu = xuh[0] / xuh[2];
+        p.yu = xuh[1] / xuh[2];
     }
+    p.zt = xuh[2];
     // Jacobian of the euclidean normalisation applied to M columns (tauWarp.frag:41-50)
     float m0[3], m1[3], mk[3];
     mv3(c.M, x * zx + z, y * zx, zx, m0);
     mv3(c.M, x * zy, y * zy + z, zy, m1);
     mv3(c.M, x, y, 1.0f, mk);
     const float iz = 1.0f / xuh[2];
-    const float d00 = (m0[0] - xu * m0[2]) * iz, d01 = (m0[1] - yu * m0[2]) * iz;
-    const float d10 = (m1[0] - xu * m1[2]) * iz, d11 = (m1[1] - yu * m1[2]) * iz;
-    float deform = 1.0f / fabsf(d00 * d11 - d01 * d10);
-    if (deform >= 30.0f) deform = 30.0f;
-    const float rx = (mk[0] - xu * mk[2]) * iz, ry = (mk[1] - yu * mk[2]) * iz;
-    float t0, t1, t2;
-    if (xu <= 0.f || (float)W <= xu || yu <= 0.f || (float)H <= yu || z >= 500.0f) {
-        t0 = -2.0f;
-        t1 = -2.0f;
-        t2 = 0.0f;
-    } else if (xuh[2] > bilinear_clamp(zbuf, W, H, xu, yu) + 0.10f) {
-        t0 = -1.0f;
-        t1 = -1.0f;
-        t2 = 0.0f;
-    } else {
-        t0 = xu;
-        t1 = yu;
-        t2 = deform;
+    const float d00 = (m0[0] - p.xu * m0[2]) * iz, d01 = (m0[1] - p.yu * m0[2]) * iz;
+    const float d10 = (m1[0] - p.xu * m1[2]) * iz, d11 = (m1[1] - p.yu * m1[2]) * iz;
+    p.deform = 1.0f / fabsf(d00 * d11 - d01 * d10);
+    if (p.deform >= 30.0f) p.deform = 30.0f;
+    p.rx = (mk[0] - p.xu * mk[2]) * iz;
+    p.ry = (mk[1] - p.yu * mk[2]) * iz;
+    return p;
+}
+
+__global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *__restrict__ depth,
+                                             const WarpCams cams, int W, int H,
+                                             const float *__restrict__ zbuf, float *__restrict__ tau3,
+                                             float *__restrict__ dpart3, float *__restrict__ tau2,
+                                             float *__restrict__ dp2) {
+    const int v = blockIdx.y;
+    const int n = w * h;
+    const int m0 = blockIdx.x * blockDim.x * kTauPer + threadIdx.x;
+    if (m0 >= n) return;
+    const float *dz = depth + (size_t)v * 3 * n;
+    const ViewCam c = view_cam(cams, v);
+    TauPix px[kTauPer];
+    float zs[kTauPer];
+#pragma unroll
+    for (int j = 0; j < kTauPer; ++j) {
+        const int m = min(m0 + j * (int)blockDim.x, n - 1);
+        px[j] = tau_project(c, m, w, dz[m], dz[n + m], dz[2 * n + m]);
     }
-    const size_t b3 = (size_t)v * 3 * n, b2 = (size_t)v * 2 * n;
-    if (tau3) {
-        tau3[b3 + m] = t0;
-        tau3[b3 + n + m] = t1;
-        tau3[b3 + 2 * n + m] = t2;
-    }
-    if (dpart3) {
-        dpart3[b3 + m] = 10.0f;
-        dpart3[b3 + n + m] = rx;
-        dpart3[b3 + 2 * n + m] = ry;
-    }
-    if (tau2) {
-        tau2[b2 + m] = t0;
-        tau2[b2 + n + m] = t1;
-    }
-    if (dp2) {
-        dp2[b2 + m] = 10.0f * rx;
-        dp2[b2 + n + m] = 10.0f * ry;
+    // the target depth map at every projection (clamped, so every sample is in bounds; out-of-range points
+    // do not use it)
+#pragma unroll
+    for (int j = 0; j < kTauPer; ++j) zs[j] = bilinear_clamp(zbuf, W, H, px[j].xu, px[j].yu);
+#pragma unroll
+    for (int j = 0; j < kTauPer; ++j) {
+        const int m = m0 + j * (int)blockDim.x;
+        if (m >= n) break;
+        const TauPix &p = px[j];
+        float t0, t1, t2;
+        if (p.xu <= 0.f || (float)W <= p.xu || p.yu <= 0.f || (float)H <= p.yu || p.z >= 500.0f) {
+            t0 = -2.0f;
+            t1 = -2.0f;
+            t2 = 0.0f;
+        } else if (p.zt > zs[j] + 0.10f) {
+            t0 = -1.0f;
+            t1 = -1.0f;
+            t2 = 0.0f;
+        } else {
+            t0 = p.xu;
+            t1 = p.yu;
+            t2 = p.deform;
+        }
+        const size_t b3 = (size_t)v * 3 * n, b2 = (size_t)v * 2 * n;
+        if (tau3) {
+            tau3[b3 + m] = t0;
+            tau3[b3 + n + m] = t1;
+            tau3[b3 + 2 * n + m] = t2;
+        }
+        if (dpart3) {
+            dpart3[b3 + m] = 10.0f;
+            dpart3[b3 + n + m] = p.rx;
+            dpart3[b3 + 2 * n + m] = p.ry;
+        }
+        if (tau2) {
+            tau2[b2 + m] = t0;
+            tau2[b2 + n + m] = t1;
+        }
+        if (dp2) {
+            dp2[b2 + m] = 10.0f * p.rx;
+            dp2[b2 + n + m] = 10.0f * p.ry;
+        }
     }
 }
 
@@ -558,7 +591,8 @@ void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, i
                 float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "tau", st);
     const int n = w * h;
-    k_tau<<<dim3((n + 255) / 256, V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zbuf, tau3, dpart3, tau2, dp2);
+    k_tau<<<dim3((n + 256 * kTauPer - 1) / (256 * kTauPer), V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zbuf, tau3,
+                                                                               dpart3, tau2, dp2);
     lc.add(1);
 }
 
