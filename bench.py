@@ -99,9 +99,9 @@ def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: in
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu --set full capture of the
 # C2 step; the captures and their commands are summarised in profiles/*_c2.md.
 NCU_TRAFFIC_BYTES = {
-    "zbuffer_splat": 83.906816e6 + 2.437376e6,
-    "gradient_setup": 223.385600e6 + 20.086528e6,
-    "cg_persistent": 21.064704e6 + 18.125056e6,
+    "zbuffer_splat": 83.943168e6 + 2.374144e6,
+    "gradient_setup": 224.255488e6 + 18.407424e6,
+    "cg_persistent": 21.044736e6 + 0.005632e6,
 }
 
 
