@@ -70,7 +70,7 @@ struct KernelProfiler {
     void init(int slots);
     void destroy();
     void reset();
-    void fold(cudaStream_t st);  // synchronises st, adds the recorded pairs to the totals, frees the pool
+    void fold();  // waits for the recorded pairs (on any stream), adds them to the totals, frees the pool
     int begin(const char *name, cudaStream_t st);
     void end(int slot, cudaStream_t st);
 };
@@ -89,6 +89,9 @@ struct lfrv_ctx {
     // host-buffer calls upload on a second stream so the copies overlap the warp stage (created on first use)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t up_start = nullptr, up_depth[4] = {}, up_views = nullptr;
+    // work that depends only on a call's inputs runs on a side stream, joined by event (created on first use)
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t side_fork = nullptr, side_join = nullptr;
     lfrv::Pending pending;
     std::map<long long, int> rof_tuned;  // autotuned persistent-ROF variant per image size (W << 32 | H)
     lfrv::KernelProfiler prof;

@@ -63,10 +63,10 @@ void KernelProfiler::reset() {
     count.clear();
 }
 
-void KernelProfiler::fold(cudaStream_t st) {
-    LFRV_CUDA(cudaStreamSynchronize(st));
+void KernelProfiler::fold() {
     for (const auto &r : recs) {
         float t = 0.f;
+        LFRV_CUDA(cudaEventSynchronize(ev[2 * r.slot + 1]));
         LFRV_CUDA(cudaEventElapsedTime(&t, ev[2 * r.slot], ev[2 * r.slot + 1]));
         size_t k = 0;
         while (k < names.size() && names[k] != r.name) ++k;
@@ -83,7 +83,7 @@ void KernelProfiler::fold(cudaStream_t st) {
 }
 
 int KernelProfiler::begin(const char *name, cudaStream_t st) {
-    if (2 * (size_t)(next + 1) > ev.size()) fold(st);
+    if (2 * (size_t)(next + 1) > ev.size()) fold();
     const int slot = next++;
     cudaEventRecord(ev[2 * slot], st);
     recs.push_back({name, slot});
@@ -108,7 +108,27 @@ static void swap_buf(DevBuf &a, DevBuf &b) {
 }
 
 static GridBarrier fresh_barrier(lfrv_ctx *c);
-static float *view_gradients(lfrv_ctx *c, const Geometry &G, const float *img);
+static float *view_gradients(lfrv_ctx *c, const Geometry &G, const float *img, cudaStream_t st);
+
+// The side stream: work of a call that depends only on its inputs runs there, between an event recorded on the
+// context stream (fork) and one the context stream waits for (join). Created on first use.
+static cudaStream_t side_stream(lfrv_ctx *c) {
+    if (!c->side_stream) {
+        LFRV_CUDA(cudaStreamCreateWithFlags(&c->side_stream, cudaStreamNonBlocking));
+        LFRV_CUDA(cudaEventCreateWithFlags(&c->side_fork, cudaEventDisableTiming));
+        LFRV_CUDA(cudaEventCreateWithFlags(&c->side_join, cudaEventDisableTiming));
+    }
+    return c->side_stream;
+}
+
+static void destroy_side_stream(lfrv_ctx *c) {
+    if (!c->side_stream) return;
+    cudaStreamSynchronize(c->side_stream);
+    cudaStreamDestroy(c->side_stream);
+    cudaEventDestroy(c->side_fork);
+    cudaEventDestroy(c->side_join);
+    c->side_stream = nullptr;
+}
 
 static void check_launch(const char *what) {
     const cudaError_t e = cudaGetLastError();
@@ -339,7 +359,7 @@ static GradientTermBuffers gradient_term_buffers(lfrv_ctx *c, const lfrv_config 
     ws.resg.ensure(sizeof(float) * 3 * (size_t)G.V * G.n);
     ws.ugrad.ensure(sizeof(float) * 2 * G.N);
     t.on = true;
-    t.vgrad = view_gradients(c, G, img);
+    t.vgrad = view_gradients(c, G, img, c->stream);
     t.lapU = ws.lapU.as<float>();
     t.resg = ws.resg.as<float>();
     t.ugrad = ws.ugrad.as<float>();
@@ -588,22 +608,22 @@ static void hole_fill_async(lfrv_ctx *c, int W, int H, const uint8_t *vis, float
 }
 
 // Sobel of every input view's luminance (compute_gradient, sources/gradientIBR_kernels.cuh:57-100).
-static float *view_gradients(lfrv_ctx *c, const Geometry &G, const float *img) {
+static float *view_gradients(lfrv_ctx *c, const Geometry &G, const float *img, cudaStream_t st) {
     Workspace &ws = c->ws;
     ws.vgrad.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
     float *vg = ws.vgrad.as<float>();
     launch_sobel(G.w, G.h, G.V, img, (size_t)3 * G.n, (size_t)G.n, vg, vg + G.n, (size_t)2 * G.n, nullptr, nullptr,
-                 c->stream, c->launches);
+                 st, c->launches);
     check_launch("view sobel");
     return vg;
 }
 
 // BF16 views: their luminance Sobel into a BF16 stack (V x 2 x n), in the same workspace buffer.
-static void *view_gradients_bf16(lfrv_ctx *c, const Geometry &G, const void *img) {
+static void *view_gradients_bf16(lfrv_ctx *c, const Geometry &G, const void *img, cudaStream_t st) {
     Workspace &ws = c->ws;
     ws.vgrad.ensure(sizeof(uint16_t) * 2 * (size_t)G.V * G.n);
     uint16_t *vg = ws.vgrad.as<uint16_t>();
-    launch_view_sobel_bf16(G.w, G.h, G.V, img, (size_t)3 * G.n, (size_t)G.n, vg, vg + G.n, (size_t)2 * G.n, c->stream,
+    launch_view_sobel_bf16(G.w, G.h, G.V, img, (size_t)3 * G.n, (size_t)G.n, vg, vg + G.n, (size_t)2 * G.n, st,
                            c->launches);
     check_launch("view sobel (bf16)");
     return vg;
@@ -611,7 +631,7 @@ static void *view_gradients_bf16(lfrv_ctx *c, const Geometry &G, const void *img
 
 static void u_gradient(lfrv_ctx *c, const Geometry &G, const Buckets &B, const float *img, const float *tau2,
                        const float *wgt, float s2, float *gx, float *gy, float *mask) {
-    float *vg = view_gradients(c, G, img);
+    float *vg = view_gradients(c, G, img, c->stream);
     launch_u_gradient(G, B, tau2, vg, wgt, s2, gx, gy, mask, c->stream, c->launches);
     check_launch("gradient splat");
 }
@@ -690,17 +710,25 @@ static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
     cudaStream_t s = c->stream;
     Workspace &ws = c->ws;
     const float s2 = cfg.sigma_sensor * cfg.sigma_sensor;
-    const Buckets B = build_buckets(c, G, tau2);
     ColorBuffers b = color_buffers(c, G);
     ws.mask.ensure(N * sizeof(float));
     // BF16 storage: img holds BF16 views, and the view gradients and weights are written in BF16
     const bool bf = cfg.bf16_storage != 0;
+    // The weights and the view gradients depend only on tau, dp and the views: they run on the side stream
+    // while the inverse map is built on the context stream, which waits for them before the set-up pass.
+    cudaStream_t side = side_stream(c);
+    LFRV_CUDA(cudaEventRecord(c->side_fork, s));
+    LFRV_CUDA(cudaStreamWaitEvent(side, c->side_fork, 0));
     // compute_weights with U = 0 (sources/gradientIBR.cu:575-577): the unmasked Sobel of 0 is 0, so the
     // gathered gradient is 0 and the weights reduce to the deformation weights over sigma^2
-    launch_weights(G, nullptr, nullptr, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, s, c->launches, bf);
+    launch_weights(G, nullptr, nullptr, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, side, c->launches,
+                   bf);
     check_launch("weights");
+    const void *vg = bf ? view_gradients_bf16(c, G, img, side) : (const void *)view_gradients(c, G, img, side);
+    LFRV_CUDA(cudaEventRecord(c->side_join, side));
+    const Buckets B = build_buckets(c, G, tau2);
+    LFRV_CUDA(cudaStreamWaitEvent(s, c->side_join, 0));
     // visibility, weighted average and gradient splat in one pass of the inverse map
-    const void *vg = bf ? view_gradients_bf16(c, G, img) : (const void *)view_gradients(c, G, img);
     launch_gradient_setup(G, B, tau2, img, vg, b.wgt, s2, b.vis, U, gx, gy, ws.mask.as<float>(), s, c->launches, bf);
     check_launch("gradient set-up");
     if (init) LFRV_CUDA(cudaMemcpyAsync(U, init, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
@@ -966,10 +994,12 @@ extern "C" int lfrv_ctx_destroy(lfrv_ctx *ctx) {
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
     for (lfrv_ctx *l : ctx->lanes) {
         cudaStreamSynchronize(l->stream);
+        destroy_side_stream(l);
         cudaStreamDestroy(l->stream);
         l->prof.destroy();
         delete l;
     }
+    destroy_side_stream(ctx);
     for (cudaEvent_t e : ctx->lane_done) cudaEventDestroy(e);
     if (ctx->copy_stream) {
         cudaStreamSynchronize(ctx->copy_stream);
@@ -1015,7 +1045,7 @@ extern "C" int lfrv_ctx_profile_read(lfrv_ctx *ctx, int index, char *name, size_
                                      long long *launches) {
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
-    ctx->prof.fold(ctx->stream);
+    ctx->prof.fold();
     const KernelProfiler &p = ctx->prof;
     if (index < 0 || index >= (int)p.names.size()) return fail(LFRV_E_ARG, "profile index %d out of range", index);
     if (name && name_len) std::snprintf(name, name_len, "%s", p.names[index].c_str());
