@@ -7,6 +7,7 @@
 
 #include <cuda_runtime.h>
 
+#include <atomic>
 #include <map>
 #include <string>
 #include <vector>
@@ -83,6 +84,29 @@ struct Pending {
     double gap_tol = 0.0;
 };
 
+// Bumped by every workspace allocation and release: a captured graph holds workspace pointers and is replayed
+// only while the epoch it was captured at is current.
+extern std::atomic<unsigned long long> g_alloc_epoch;
+
+// One captured render call (lfrv_render_view_dev): the call's argument bytes, and once the same call has run
+// uncaptured, its executable graph with the host-side state the capture left (pending statistics, launches).
+struct RenderGraph {
+    std::vector<unsigned char> key;
+    bool seen = false;     // this key ran once uncaptured (its workspace is allocated)
+    bool failed = false;   // capturing this key failed: it runs uncaptured
+    cudaGraphExec_t exec = nullptr;
+    unsigned long long epoch = 0;
+    Pending pending;
+    long long launches = 0;
+    void reset(std::vector<unsigned char> k) {
+        if (exec) cudaGraphExecDestroy(exec);
+        exec = nullptr;
+        key = std::move(k);
+        seen = false;
+        failed = false;
+    }
+};
+
 }  // namespace lfrv
 
 struct lfrv_ctx {
@@ -101,6 +125,7 @@ struct lfrv_ctx {
     lfrv::LaunchCounter launches;
     lfrv::Workspace ws;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    lfrv::RenderGraph graph;  // replay of a repeated lfrv_render_view_dev call
     // helper contexts (own stream and workspace) that prepare batched targets concurrently; created on first use
     std::vector<lfrv_ctx *> lanes;
     std::vector<cudaEvent_t> lane_done;

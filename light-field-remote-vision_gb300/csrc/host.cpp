@@ -28,16 +28,22 @@ void check_cuda(cudaError_t e, const char *what) {
                                 cudaGetErrorString(e));
 }
 
+std::atomic<unsigned long long> g_alloc_epoch{0};
+
 void DevBuf::ensure(size_t b) {
     if (b <= bytes && p) return;
     release();
     if (b == 0) b = 16;
     LFRV_CUDA(cudaMalloc(&p, b));
     bytes = b;
+    ++g_alloc_epoch;
 }
 
 void DevBuf::release() {
-    if (p) cudaFree(p);
+    if (p) {
+        cudaFree(p);
+        ++g_alloc_epoch;
+    }
     p = nullptr;
     bytes = 0;
 }
@@ -716,18 +722,23 @@ static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
     const bool bf = cfg.bf16_storage != 0;
     // The weights and the view gradients depend only on tau, dp and the views: they run on the side stream
     // while the inverse map is built on the context stream, which waits for them before the set-up pass.
-    cudaStream_t side = side_stream(c);
-    LFRV_CUDA(cudaEventRecord(c->side_fork, s));
-    LFRV_CUDA(cudaStreamWaitEvent(side, c->side_fork, 0));
+    // With per-kernel profiling on, everything stays on the context stream, so that each kernel's event time
+    // is its own and not shared with a concurrent one.
+    const bool fork = c->launches.prof == nullptr;
+    cudaStream_t side = fork ? side_stream(c) : s;
+    if (fork) {
+        LFRV_CUDA(cudaEventRecord(c->side_fork, s));
+        LFRV_CUDA(cudaStreamWaitEvent(side, c->side_fork, 0));
+    }
     // compute_weights with U = 0 (sources/gradientIBR.cu:575-577): the unmasked Sobel of 0 is 0, so the
     // gathered gradient is 0 and the weights reduce to the deformation weights over sigma^2
     launch_weights(G, nullptr, nullptr, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, side, c->launches,
                    bf);
     check_launch("weights");
     const void *vg = bf ? view_gradients_bf16(c, G, img, side) : (const void *)view_gradients(c, G, img, side);
-    LFRV_CUDA(cudaEventRecord(c->side_join, side));
+    if (fork) LFRV_CUDA(cudaEventRecord(c->side_join, side));
     const Buckets B = build_buckets(c, G, tau2);
-    LFRV_CUDA(cudaStreamWaitEvent(s, c->side_join, 0));
+    if (fork) LFRV_CUDA(cudaStreamWaitEvent(s, c->side_join, 0));
     // visibility, weighted average and gradient splat in one pass of the inverse map
     launch_gradient_setup(G, B, tau2, img, vg, b.wgt, s2, b.vis, U, gx, gy, ws.mask.as<float>(), s, c->launches, bf);
     check_launch("gradient set-up");
@@ -1000,6 +1011,7 @@ extern "C" int lfrv_ctx_destroy(lfrv_ctx *ctx) {
         delete l;
     }
     destroy_side_stream(ctx);
+    ctx->graph.reset({});
     for (cudaEvent_t e : ctx->lane_done) cudaEventDestroy(e);
     if (ctx->copy_stream) {
         cudaStreamSynchronize(ctx->copy_stream);
@@ -1259,14 +1271,11 @@ extern "C" int lfrv_ibr_gradient(lfrv_ctx *ctx, const lfrv_config *cfg, const fl
 
 // Warp stage + solve of one target view on device buffers; with a plan the inputs are still arriving on the
 // copy stream, and with host_out the result is copied back before the call synchronises.
-static void render_view_impl(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const float *d_views,
+// The stream work of one render call (between the call's timing events).
+static void render_view_body(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const float *d_views,
                              const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target, float *d_out,
                              lfrv_stats *stats, const UploadPlan *plan, float *host_out) {
-    if (stats) std::memset(stats, 0, sizeof(*stats));
     const Geometry G = geometry(cfg);
-    if (target->width != G.W || target->height != G.H) raise(LFRV_E_ARG, "target size mismatch");
-    const long long l0 = ctx->launches.n;
-    begin_timing(ctx);
     Workspace &ws = ctx->ws;
     ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
     ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
@@ -1277,7 +1286,98 @@ static void render_view_impl(lfrv_ctx *ctx, const lfrv_config &cfg, int algorith
     else gradient_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
     if (host_out)
         LFRV_CUDA(cudaMemcpyAsync(host_out, d_out, sizeof(float) * 3 * G.N, cudaMemcpyDeviceToHost, ctx->stream));
+}
+
+static void render_view_impl(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const float *d_views,
+                             const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target, float *d_out,
+                             lfrv_stats *stats, const UploadPlan *plan, float *host_out) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    const Geometry G = geometry(cfg);
+    if (target->width != G.W || target->height != G.H) raise(LFRV_E_ARG, "target size mismatch");
+    const long long l0 = ctx->launches.n;
+    begin_timing(ctx);
+    render_view_body(ctx, cfg, algorithm, d_views, d_depth, cams, target, d_out, stats, plan, host_out);
     end_timing(ctx, stats, l0);
+}
+
+// lfrv_render_view_dev through a CUDA graph. A call whose arguments (config, pointers, cameras, target, stream)
+// repeat the previous call's is captured once, the second time it is seen (the first run allocated its
+// workspace), and replayed from then on: one graph launch instead of the ~25 launches, memsets and events of
+// the call, so the device does not idle while the host enqueues them. Only IBR_gradient with the corrected CG
+// qualifies (no host synchronisation inside the call), and not while per-kernel profiling is on. The host state
+// the call leaves (pending solver statistics, launch count) is recorded at capture and restored at each replay;
+// any workspace reallocation since the capture invalidates the graph. Returns false when the call must run
+// uncaptured.
+static bool render_view_graph(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const float *d_views,
+                              const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target, float *d_out,
+                              lfrv_stats *stats) {
+    if (algorithm != 1 || cfg.faithful || ctx->launches.prof) return false;
+    const Geometry G = geometry(cfg);
+    if (target->width != G.W || target->height != G.H) return false;
+    std::vector<unsigned char> key;
+    auto put = [&](const void *p, size_t n) {
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        key.insert(key.end(), c, c + n);
+    };
+    put(&cfg, sizeof(cfg));
+    put(&d_views, sizeof(d_views));
+    put(&d_depth, sizeof(d_depth));
+    put(&d_out, sizeof(d_out));
+    put(cams, sizeof(lfrv_camera) * (size_t)G.V);
+    put(target, sizeof(*target));
+    put(&ctx->stream, sizeof(ctx->stream));
+    RenderGraph &g = ctx->graph;
+    if (g.key != key) {
+        g.reset(std::move(key));
+        g.seen = true;
+        return false;
+    }
+    if (g.failed) return false;
+    if (g.exec && g.epoch != g_alloc_epoch) {
+        cudaGraphExecDestroy(g.exec);
+        g.exec = nullptr;
+        return false;  // rerun uncaptured; the next identical call captures again
+    }
+    if (!g.exec) {
+        const unsigned long long e0 = g_alloc_epoch;
+        const long long l0 = ctx->launches.n;
+        ctx->pending = Pending{};
+        cudaGraph_t graph = nullptr;
+        bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
+        if (ok) {
+            try {
+                render_view_body(ctx, cfg, algorithm, d_views, d_depth, cams, target, d_out, nullptr, nullptr,
+                                 nullptr);
+            } catch (...) {
+                ok = false;
+            }
+            ok = cudaStreamEndCapture(ctx->stream, &graph) == cudaSuccess && ok && graph && e0 == g_alloc_epoch;
+            if (ok) ok = cudaGraphInstantiate(&g.exec, graph, 0) == cudaSuccess;
+        }
+        if (graph) cudaGraphDestroy(graph);
+        cudaGetLastError();  // a failed capture leaves its error here; the call reruns uncaptured
+        if (!ok) {
+            g.exec = nullptr;
+            g.failed = true;
+            ctx->launches.n = l0;
+            ctx->pending = Pending{};
+            return false;
+        }
+        g.epoch = e0;
+        g.pending = ctx->pending;
+        g.pending.stats = nullptr;
+        g.launches = ctx->launches.n - l0;
+        ctx->launches.n = l0;
+    }
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    const long long l0 = ctx->launches.n;
+    begin_timing(ctx);
+    LFRV_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
+    ctx->launches.n += g.launches;
+    ctx->pending = g.pending;
+    ctx->pending.stats = stats;
+    end_timing(ctx, stats, l0);
+    return true;
 }
 
 extern "C" int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm, const float *d_views,
@@ -1286,7 +1386,8 @@ extern "C" int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int a
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
     if (!cfg || !d_views || !d_depth || !cams || !target || !d_out) return fail(LFRV_E_ARG, "null argument");
-    render_view_impl(ctx, *cfg, algorithm, d_views, d_depth, cams, target, d_out, stats, nullptr, nullptr);
+    if (!render_view_graph(ctx, *cfg, algorithm, d_views, d_depth, cams, target, d_out, stats))
+        render_view_impl(ctx, *cfg, algorithm, d_views, d_depth, cams, target, d_out, stats, nullptr, nullptr);
     LFRV_API_END
 }
 

@@ -52,3 +52,49 @@ def test_render_view_repeated_calls_are_identical(ctx):
     a, _ = ctx.render_view(cfg, 1, sc.views, sc.depth, sc.cams, sc.target)
     b, _ = ctx.render_view(cfg, 1, sc.views, sc.depth, sc.cams, sc.target)
     np.testing.assert_array_equal(a, b)
+
+
+def test_render_view_dev_graph_replay(ctx):
+    """Repeated identical lfrv_render_view_dev calls are captured once and replayed as a CUDA graph: every call
+    gives the uncaptured call's result bit for bit and the same statistics, new input contents behind the same
+    pointers are picked up, and changed arguments fall back to an uncaptured run."""
+    import torch
+
+    sc = scene(2, 32)
+    cfg = gradient_config(sc, cg_gap_tol=1e-6, faithful=0)
+    d_views = torch.from_numpy(sc.views.copy()).cuda()
+    d_depth = torch.from_numpy(sc.depth.copy()).cuda()
+    H, W = sc.target.height, sc.target.width
+    d_out = torch.empty((3, H, W), dtype=torch.float32, device="cuda")
+
+    def run(c, cams=sc.cams):
+        torch.cuda.synchronize()
+        st = c.render_view_dev(cfg, 1, d_views.data_ptr(), d_depth.data_ptr(), cams, sc.target, d_out.data_ptr())
+        torch.cuda.synchronize()
+        return d_out.cpu().numpy().copy(), st
+
+    with lfrv.Context(0) as fresh:
+        want, st0 = run(fresh)
+    outs = [run(ctx) for _ in range(4)]  # uncaptured, captured + replayed, replayed, replayed
+    for out, st in outs:
+        np.testing.assert_array_equal(out, want)
+        assert st.outer_iterations == st0.outer_iterations
+        assert st.hole_fill_iterations == st0.hole_fill_iterations
+        assert st.gap == st0.gap
+        assert st.kernel_launches == st0.kernel_launches
+
+    # new view contents behind the same pointers: the replay reads them
+    d_views.mul_(0.5)
+    got, _ = run(ctx)
+    with lfrv.Context(0) as fresh:
+        want2, _ = run(fresh)
+    np.testing.assert_array_equal(got, want2)
+    assert not np.array_equal(want2, want)
+
+    # different cameras: a new key, run uncaptured
+    cams2 = [c for c in sc.cams]
+    cams2[0], cams2[1] = cams2[1], cams2[0]
+    got3, _ = run(ctx, cams2)
+    with lfrv.Context(0) as fresh:
+        want3, _ = run(fresh, cams2)
+    np.testing.assert_array_equal(got3, want3)
