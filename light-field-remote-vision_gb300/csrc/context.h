@@ -130,4 +130,5 @@ struct lfrv_ctx {
     std::vector<lfrv_ctx *> lanes;
     std::vector<cudaEvent_t> lane_done;
     bool owns_stream = false;
+    bool lane = false;  // a helper context of a batched call (its stream already runs beside the others)
 };

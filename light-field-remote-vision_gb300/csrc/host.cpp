@@ -723,8 +723,9 @@ static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
     // The weights and the view gradients depend only on tau, dp and the views: they run on the side stream
     // while the inverse map is built on the context stream, which waits for them before the set-up pass.
     // With per-kernel profiling on, everything stays on the context stream, so that each kernel's event time
-    // is its own and not shared with a concurrent one.
-    const bool fork = c->launches.prof == nullptr;
+    // is its own and not shared with a concurrent one; so it does in the helper lanes of a batched call, whose
+    // streams already run beside each other.
+    const bool fork = c->launches.prof == nullptr && !c->lane;
     cudaStream_t side = fork ? side_stream(c) : s;
     if (fork) {
         LFRV_CUDA(cudaEventRecord(c->side_fork, s));
@@ -1300,32 +1301,16 @@ static void render_view_impl(lfrv_ctx *ctx, const lfrv_config &cfg, int algorith
     end_timing(ctx, stats, l0);
 }
 
-// lfrv_render_view_dev through a CUDA graph. A call whose arguments (config, pointers, cameras, target, stream)
-// repeat the previous call's is captured once, the second time it is seen (the first run allocated its
-// workspace), and replayed from then on: one graph launch instead of the ~25 launches, memsets and events of
-// the call, so the device does not idle while the host enqueues them. Only IBR_gradient with the corrected CG
-// qualifies (no host synchronisation inside the call), and not while per-kernel profiling is on. The host state
-// the call leaves (pending solver statistics, launch count) is recorded at capture and restored at each replay;
-// any workspace reallocation since the capture invalidates the graph. Returns false when the call must run
-// uncaptured.
-static bool render_view_graph(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const float *d_views,
-                              const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target, float *d_out,
-                              lfrv_stats *stats) {
-    if (algorithm != 1 || cfg.faithful || ctx->launches.prof) return false;
-    const Geometry G = geometry(cfg);
-    if (target->width != G.W || target->height != G.H) return false;
-    std::vector<unsigned char> key;
-    auto put = [&](const void *p, size_t n) {
-        const unsigned char *c = static_cast<const unsigned char *>(p);
-        key.insert(key.end(), c, c + n);
-    };
-    put(&cfg, sizeof(cfg));
-    put(&d_views, sizeof(d_views));
-    put(&d_depth, sizeof(d_depth));
-    put(&d_out, sizeof(d_out));
-    put(cams, sizeof(lfrv_camera) * (size_t)G.V);
-    put(target, sizeof(*target));
-    put(&ctx->stream, sizeof(ctx->stream));
+// Repeated render calls through a CUDA graph. A call whose key (its arguments: config, pointers, cameras,
+// target, stream) repeats the previous call's is captured once, the second time it is seen (the first run
+// allocated its workspace), and replayed from then on: one graph launch instead of the ~25 launches, memsets,
+// copies and events of the call, so the device does not idle while the host enqueues them. Only IBR_gradient
+// with the corrected CG qualifies (no host synchronisation inside the call), and not while per-kernel profiling
+// is on. The host state the call leaves (pending solver statistics, launch count) is recorded at capture and
+// restored at each replay; any workspace reallocation since the capture invalidates the graph. body() enqueues
+// the call's stream work. Returns false when the call must run uncaptured.
+template <class Body>
+static bool render_graph(lfrv_ctx *ctx, std::vector<unsigned char> key, lfrv_stats *stats, Body body) {
     RenderGraph &g = ctx->graph;
     if (g.key != key) {
         g.reset(std::move(key));
@@ -1346,8 +1331,7 @@ static bool render_view_graph(lfrv_ctx *ctx, const lfrv_config &cfg, int algorit
         bool ok = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed) == cudaSuccess;
         if (ok) {
             try {
-                render_view_body(ctx, cfg, algorithm, d_views, d_depth, cams, target, d_out, nullptr, nullptr,
-                                 nullptr);
+                body();
             } catch (...) {
                 ok = false;
             }
@@ -1380,13 +1364,44 @@ static bool render_view_graph(lfrv_ctx *ctx, const lfrv_config &cfg, int algorit
     return true;
 }
 
+// The key of a render call: its argument bytes.
+static std::vector<unsigned char> render_key(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const void *views,
+                                             const void *depth, const void *out, const lfrv_camera *cams,
+                                             const lfrv_camera *target) {
+    std::vector<unsigned char> key;
+    auto put = [&](const void *p, size_t n) {
+        const unsigned char *c = static_cast<const unsigned char *>(p);
+        key.insert(key.end(), c, c + n);
+    };
+    put(&cfg, sizeof(cfg));
+    put(&algorithm, sizeof(algorithm));
+    put(&views, sizeof(views));
+    put(&depth, sizeof(depth));
+    put(&out, sizeof(out));
+    put(cams, sizeof(lfrv_camera) * (size_t)cfg.nviews);
+    put(target, sizeof(*target));
+    put(&ctx->stream, sizeof(ctx->stream));
+    return key;
+}
+
+static bool graph_eligible(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const lfrv_camera *target) {
+    if (algorithm != 1 || cfg.faithful || ctx->launches.prof) return false;
+    const Geometry G = geometry(cfg);
+    return target->width == G.W && target->height == G.H;
+}
+
 extern "C" int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm, const float *d_views,
                                     const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target,
                                     float *d_out, lfrv_stats *stats) {
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
     if (!cfg || !d_views || !d_depth || !cams || !target || !d_out) return fail(LFRV_E_ARG, "null argument");
-    if (!render_view_graph(ctx, *cfg, algorithm, d_views, d_depth, cams, target, d_out, stats))
+    const bool replayed =
+        graph_eligible(ctx, *cfg, algorithm, target) &&
+        render_graph(ctx, render_key(ctx, *cfg, algorithm, d_views, d_depth, d_out, cams, target), stats, [&] {
+            render_view_body(ctx, *cfg, algorithm, d_views, d_depth, cams, target, d_out, nullptr, nullptr, nullptr);
+        });
+    if (!replayed)
         render_view_impl(ctx, *cfg, algorithm, d_views, d_depth, cams, target, d_out, stats, nullptr, nullptr);
     LFRV_API_END
 }
@@ -1530,6 +1545,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         l->device = c->device;
         LFRV_CUDA(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking));
         l->owns_stream = true;
+        l->lane = true;
         c->lanes.push_back(l);
         cudaEvent_t e;
         LFRV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -1727,25 +1743,40 @@ extern "C" int lfrv_render_view(lfrv_ctx *ctx, const lfrv_config *cfg, int algor
     // uploads on the copy stream, after whatever the context stream has queued on these buffers; the depth
     // maps first, in up to 4 chunks of views, then the colour views
     cudaStream_t cs = copy_stream(ctx);
-    LFRV_CUDA(cudaEventRecord(ctx->up_start, ctx->stream));
-    LFRV_CUDA(cudaStreamWaitEvent(cs, ctx->up_start, 0));
     UploadPlan plan;
-    plan.chunks = G.V < 4 ? G.V : 4;
-    int v0 = 0;
-    for (int k = 0; k < plan.chunks; ++k) {
-        const int v1 = (int)((V * (size_t)(k + 1)) / plan.chunks);
-        LFRV_CUDA(cudaMemcpyAsync(ws.depth.as<char>() + v0 * per_view, reinterpret_cast<const char *>(depth) + v0 * per_view,
-                                  (size_t)(v1 - v0) * per_view, cudaMemcpyHostToDevice, cs));
-        LFRV_CUDA(cudaEventRecord(ctx->up_depth[k], cs));
-        plan.v_end[k] = v1;
-        plan.depth_ready[k] = ctx->up_depth[k];
-        v0 = v1;
+    auto upload = [&] {
+        LFRV_CUDA(cudaEventRecord(ctx->up_start, ctx->stream));
+        LFRV_CUDA(cudaStreamWaitEvent(cs, ctx->up_start, 0));
+        plan.chunks = G.V < 4 ? G.V : 4;
+        int v0 = 0;
+        for (int k = 0; k < plan.chunks; ++k) {
+            const int v1 = (int)((V * (size_t)(k + 1)) / plan.chunks);
+            LFRV_CUDA(cudaMemcpyAsync(ws.depth.as<char>() + v0 * per_view,
+                                      reinterpret_cast<const char *>(depth) + v0 * per_view,
+                                      (size_t)(v1 - v0) * per_view, cudaMemcpyHostToDevice, cs));
+            LFRV_CUDA(cudaEventRecord(ctx->up_depth[k], cs));
+            plan.v_end[k] = v1;
+            plan.depth_ready[k] = ctx->up_depth[k];
+            v0 = v1;
+        }
+        LFRV_CUDA(cudaMemcpyAsync(ws.in_views.p, views, V * per_view, cudaMemcpyHostToDevice, cs));
+        LFRV_CUDA(cudaEventRecord(ctx->up_views, cs));
+        plan.views_ready = ctx->up_views;
+    };
+    // a repeated call (same host buffers and arguments) replays its captured graph: uploads, warp, solve and
+    // the download in one launch
+    const bool replayed =
+        graph_eligible(ctx, *cfg, algorithm, target) &&
+        render_graph(ctx, render_key(ctx, *cfg, algorithm, views, depth, out, cams, target), stats, [&] {
+            upload();
+            render_view_body(ctx, *cfg, algorithm, ws.in_views.as<float>(), ws.depth.as<float>(), cams, target,
+                             ws.out_img.as<float>(), nullptr, &plan, out);
+        });
+    if (!replayed) {
+        upload();
+        render_view_impl(ctx, *cfg, algorithm, ws.in_views.as<float>(), ws.depth.as<float>(), cams, target,
+                         ws.out_img.as<float>(), stats, &plan, out);
     }
-    LFRV_CUDA(cudaMemcpyAsync(ws.in_views.p, views, V * per_view, cudaMemcpyHostToDevice, cs));
-    LFRV_CUDA(cudaEventRecord(ctx->up_views, cs));
-    plan.views_ready = ctx->up_views;
-    render_view_impl(ctx, *cfg, algorithm, ws.in_views.as<float>(), ws.depth.as<float>(), cams, target,
-                     ws.out_img.as<float>(), stats, &plan, out);
     LFRV_API_END
 }
 
