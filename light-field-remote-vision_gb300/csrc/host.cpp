@@ -711,7 +711,7 @@ static void cg_persistent_async(lfrv_ctx *c, int W, int H, int max_iter, double 
 // average, gradient splat) into U, gx, gy, then hole filling of U (or U = init).
 static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry &G, const float *img,
                              const float *tau2, const float *dp2, const float *init, float *U, float *gx, float *gy,
-                             void *learn_in = nullptr) {
+                             void *learn_in = nullptr, cudaEvent_t views_ready = nullptr) {
     const size_t N = G.N;
     cudaStream_t s = c->stream;
     Workspace &ws = c->ws;
@@ -736,6 +736,8 @@ static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
     launch_weights(G, nullptr, nullptr, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, side, c->launches,
                    bf);
     check_launch("weights");
+    // views still uploading (views_ready): only the view gradients wait for them, and the set-up through the join
+    if (views_ready) LFRV_CUDA(cudaStreamWaitEvent(side, views_ready, 0));
     const void *vg = bf ? view_gradients_bf16(c, G, img, side) : (const void *)view_gradients(c, G, img, side);
     if (fork) LFRV_CUDA(cudaEventRecord(c->side_join, side));
     const Buckets B = build_buckets(c, G, tau2);
@@ -753,7 +755,7 @@ static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
 }
 
 static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
-                           const float *init, float *out, lfrv_stats *st) {
+                           const float *init, float *out, lfrv_stats *st, cudaEvent_t views_ready = nullptr) {
     check_solver_options(cfg);
     const Geometry G = geometry(cfg);
     if (G.W < 2 || G.H < 2) raise(LFRV_E_ARG, "IBR_gradient needs a target of at least 2 x 2 pixels");
@@ -763,7 +765,7 @@ static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img
     ColorBuffers b = color_buffers(c, G);
     float *U = ws.U.as<float>();
     c->pending = Pending{};
-    gradient_prepare(c, cfg, G, img, tau2, dp2, init, U, b.gx, b.gy);
+    gradient_prepare(c, cfg, G, img, tau2, dp2, init, U, b.gx, b.gy, nullptr, views_ready);
     int it_faithful = 0;
     if (cfg.faithful) it_faithful = cg_faithful(c, G.W, G.H, b.gx, b.gy, U);
     else cg_persistent_async(c, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U);
@@ -1282,9 +1284,14 @@ static void render_view_body(lfrv_ctx *ctx, const lfrv_config &cfg, int algorith
     ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
     warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr,
          plan);
-    if (plan) LFRV_CUDA(cudaStreamWaitEvent(ctx->stream, plan->views_ready, 0));
-    if (algorithm == 0) color_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
-    else gradient_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
+    if (algorithm == 0) {
+        if (plan) LFRV_CUDA(cudaStreamWaitEvent(ctx->stream, plan->views_ready, 0));
+        color_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
+    } else {
+        // the inverse map and the weights need only the warps: they do not wait for the colour views' upload
+        gradient_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats,
+                       plan ? plan->views_ready : nullptr);
+    }
     if (host_out)
         LFRV_CUDA(cudaMemcpyAsync(host_out, d_out, sizeof(float) * 3 * G.N, cudaMemcpyDeviceToHost, ctx->stream));
 }
