@@ -175,7 +175,8 @@ __device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigne
 //   - edge values are taken relative to the box's first centre (the same differences as edgef's) and scaled
 //     by the triangle's winding sign, so "inside" is w >= thr on every edge, with thr = 0 on a top-left edge
 //     and the smallest positive float elsewhere (the library is built without flush-to-zero);
-//   - the depth is tri_cover's quotient, its terms in the same order.
+//   - the depth is tri_cover's barycentric quotient with its terms in the same order, divided approximately
+//     (__fdividef, within 2 ulp; the key only orders surfaces whose depths differ by far more).
 // The 3 x 3 window is unrolled. Returns false when the quad needs raster_quad.
 __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc, int W, int H,
                                                   unsigned long long *zkey) {
@@ -235,7 +236,8 @@ __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc,
             // A = (v0, v1, v2) with weights (w12, wa1, wa2); B = (v1, v2, v3) with (wb0, wb1, -w12)
             const float w0 = inA ? w12 : wb0, w1 = inA ? wa1 : wb1, w2 = inA ? wa2 : -w12;
             const float z0 = inA ? v[0][2] : v[1][2], z1 = inA ? v[1][2] : v[2][2], z2 = inA ? v[2][2] : v[3][2];
-            const float iz = (w0 * z0 + w1 * z1 + w2 * z2) / (w0 + w1 + w2);
+            // the approximate quotient (within 2 ulp): a depth key, compared at 1e-4 and far coarser downstream
+            const float iz = __fdividef(w0 * z0 + w1 * z1 + w2 * z2, w0 + w1 + w2);
             hit[i] = i <= xmax - xmin && cov && iz > 0.f;
             key[i] = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
         }
@@ -263,7 +265,7 @@ __device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int m, int w, flo
         const float dx = off[k][0], dy = off[k][1];
         warp_point(c, cx + dx, cy + dy, z + dx * zx + dy * zy, xh);
         if (!(xh[2] > 1e-2f)) return;  // behind the near plane (zNear = 1e-2, sources/pinholeCamera.cpp:133)
-        const float iw = 1.0f / xh[2];
+        const float iw = __fdividef(1.0f, xh[2]);  // approximate reciprocal: vertex positions within 2 ulp
         vert[k][0] = xh[0] * iw;
         vert[k][1] = xh[1] * iw;
         vert[k][2] = iw;
