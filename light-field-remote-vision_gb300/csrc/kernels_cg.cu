@@ -23,14 +23,35 @@ namespace lfrv {
 
 // Hole list in raster order: one warp per row counts its holes (ballot), one block scans the row counts,
 // one warp per row writes its holes in order.
+// Zero bytes of 16 visibility bytes (as a 16-bit mask, bit j = byte j) and their count.
+__device__ __forceinline__ unsigned int zero_mask16(uint4 v) {
+    const unsigned int w[4] = {v.x, v.y, v.z, v.w};
+    unsigned int m = 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        const unsigned int e = __vcmpeq4(w[i], 0u);  // 0xff in every zero byte
+#pragma unroll
+        for (int j = 0; j < 4; ++j) m |= ((e >> (8 * j)) & 1u) << (4 * i + j);
+    }
+    return m;
+}
+
 __global__ void k_hole_rows(int W, int H, const uint8_t *__restrict__ vis, int *__restrict__ row_count) {
     const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (y >= H) return;
     int c = 0;
-    for (int x0 = 0; x0 < W; x0 += 32) {
-        const int x = x0 + lane;
-        const bool hole = (x < W) && !vis[(size_t)y * W + x];
-        c += __popc(__ballot_sync(0xffffffffu, hole));
+    if (W % 16 == 0) {
+        // 16 pixels per lane and load (rows start on 16-byte boundaries)
+        const uint8_t *row = vis + (size_t)y * W;
+        for (int x = lane * 16; x < W; x += 512) c += __popc(zero_mask16(*reinterpret_cast<const uint4 *>(row + x)));
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    } else {
+        for (int x0 = 0; x0 < W; x0 += 32) {
+            const int x = x0 + lane;
+            const bool hole = (x < W) && !vis[(size_t)y * W + x];
+            c += __popc(__ballot_sync(0xffffffffu, hole));
+        }
     }
     if (lane == 0) row_count[y] = c;
 }
@@ -77,6 +98,25 @@ __global__ void k_hole_write(int W, int H, const uint8_t *__restrict__ vis, cons
     const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (y >= H) return;
     int k = row_start[y];
+    if (W % 16 == 0) {
+        // 16 pixels per lane and load; a lane's holes go after the holes of the lanes before it
+        const uint8_t *row = vis + (size_t)y * W;
+        for (int x0 = 0; x0 < W; x0 += 512) {
+            const int x = x0 + lane * 16;
+            const unsigned int m = (x < W) ? zero_mask16(*reinterpret_cast<const uint4 *>(row + x)) : 0u;
+            const int c = __popc(m);
+            int incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= o) incl += t;
+            }
+            int at = k + incl - c;
+            for (unsigned int r = m; r; r &= r - 1) holes[at++] = y * W + x + (__ffs(r) - 1);
+            k += __shfl_sync(0xffffffffu, incl, 31);
+        }
+        return;
+    }
     for (int x0 = 0; x0 < W; x0 += 32) {
         const int x = x0 + lane;
         const bool hole = (x < W) && !vis[(size_t)y * W + x];
@@ -1194,8 +1234,9 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_batch(const CgProblem *_
 // Hole filling for at most kSmallHoles holes, in one block and in shared memory. The visible pixels never change,
 // so every hole keeps, per direction (left, up, right, down: the summation order of compute_laplacian), either
 // the index of the neighbouring hole or the neighbour's fixed value; the iterations then touch shared memory
-// only. Each update is the same float expression as k_hole_fill_persistent's. holes must be in ascending pixel
-// order (k_hole_write): neighbours are found by binary search.
+// only. Each update gives k_hole_fill_persistent's value bit for bit (its division by the neighbour count is a
+// corrected reciprocal product). holes must be in ascending pixel order with the row starts behind them
+// (launch_hole_list).
 constexpr int kSmallHoles = 2048, kSmallThreads = 1024;
 constexpr size_t kSmallHoleSmem = (size_t)kSmallHoles * (6 * 4 + 12 * 4 + 4 * 2 + 4);
 
@@ -1208,43 +1249,67 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
     float *cur = hsm, *nxt = hsm + 3 * kSmallHoles;            // [3][kSmallHoles] each
     float *fixedv = hsm + 6 * kSmallHoles;                      // [4 dirs][3][kSmallHoles]
     float *wts = hsm + 18 * kSmallHoles;                        // [kSmallHoles]
+    __shared__ float rws[kSmallHoles];                          // 1 / wts
     short *nb = reinterpret_cast<short *>(hsm + 19 * kSmallHoles);  // [4][kSmallHoles]: hole index, -1 fixed, -2 none
     __shared__ float wsum[2][kSmallThreads / 32];
     __shared__ int s_holes[kSmallHoles];
     const size_t N = (size_t)W * H;
     for (int h = threadIdx.x; h < nh; h += kSmallThreads) s_holes[h] = __ldg(holes + h);
     __syncthreads();
+    // row starts of the hole list (launch_hole_list keeps them in holes[N .. N + H)): a vertical neighbour is
+    // searched in its row's few holes only, a horizontal one is the adjacent entry of the sorted list
+    const int *row_start = holes + N;
     for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
         const int o = s_holes[h];
         const int ox = o % W, oy = o / W;
         const bool has[4] = {ox > 0, oy > 0, ox < W - 1, oy < H - 1};
         const int q[4] = {o - 1, o - W, o + 1, o + W};
+        int lo[4] = {h - 1, 0, h + 1, 0}, hi[4] = {h - 1, -1, min(h + 1, nh - 1), -1};
+        if (has[1]) {
+            lo[1] = __ldg(row_start + oy - 1);
+            hi[1] = __ldg(row_start + oy) - 1;
+        }
+        if (has[3]) {
+            lo[3] = __ldg(row_start + oy + 1);
+            hi[3] = (oy + 2 < H ? __ldg(row_start + oy + 2) : nh) - 1;
+        }
         float wt = 0.f;
+        short idx4[4];
 #pragma unroll
         for (int d = 0; d < 4; ++d) {
             short idx = -2;
             if (has[d]) {
                 wt += 1.f;
-                int lo = 0, hi = nh - 1;  // binary search of q[d] among the holes
                 idx = -1;
-                while (lo <= hi) {
-                    const int mid = (lo + hi) >> 1, v = s_holes[mid];
+                int l = max(lo[d], 0), r = hi[d];
+                while (l <= r) {
+                    const int mid = (l + r) >> 1, v = s_holes[mid];
                     if (v == q[d]) {
                         idx = (short)mid;
                         break;
                     }
-                    if (v < q[d]) lo = mid + 1;
-                    else hi = mid - 1;
+                    if (v < q[d]) l = mid + 1;
+                    else r = mid - 1;
                 }
-                if (idx == -1)
-                    for (int c = 0; c < 3; ++c) fixedv[(d * 3 + c) * kSmallHoles + h] = A[c * N + q[d]];
             }
+            idx4[d] = idx;
             nb[d * kSmallHoles + h] = idx;
         }
         wts[h] = wt;
+        rws[h] = 1.0f / wt;
+        // the fixed neighbours' values and the hole's own, all loads issued together
+#pragma unroll
+        for (int d = 0; d < 4; ++d)
+            if (idx4[d] == -1)
+                for (int c = 0; c < 3; ++c) fixedv[(d * 3 + c) * kSmallHoles + h] = A[c * N + q[d]];
         for (int c = 0; c < 3; ++c) cur[c * kSmallHoles + h] = A[c * N + o];
     }
     __syncthreads();
+    // only the warps that hold holes iterate (at least one, so that an empty hole set reports its one iteration
+    // as the reference does): the others leave, and the iterations synchronise on named barrier 1 with the
+    // iterating threads' count
+    const int active = max(32, min(kSmallThreads, (nh + 31) & ~31));
+    if ((int)threadIdx.x >= active) return;
     float energy = 0.0f, previous = 0.0f;
     int k;
     for (k = 0; k < max_iter; ++k) {
@@ -1262,7 +1327,14 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
                     if (idx == -2) continue;
                     v += (idx >= 0) ? cur[c * kSmallHoles + idx] : fixedv[(d * 3 + c) * kSmallHoles + h];
                 }
-                v /= wts[h];
+                // v / wt as the reciprocal product with one residual correction (Markstein): with rw the
+                // rounded reciprocal and q within an ulp of the quotient, q + rw (v - wt q) is the correctly
+                // rounded quotient, i.e. the division's result bit for bit (no underflow at these magnitudes)
+                {
+                    const float wt = wts[h], rw = rws[h];
+                    const float q = v * rw;
+                    v = fmaf(fmaf(-q, wt, v), rw, q);
+                }
                 const float uc = cur[c * kSmallHoles + h];
                 const float lap = v - uc;
                 const float un = uc + lap;
@@ -1276,8 +1348,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
         // this iteration with the same fixed tree (down-shuffles, then lane 0's value), so all agree
         const int lane = threadIdx.x & 31;
         if (lane == 0) wsum[k & 1][threadIdx.x >> 5] = acc;
-        __syncthreads();
-        float tot = (lane < kSmallThreads / 32) ? wsum[k & 1][lane] : 0.f;
+        asm volatile("bar.sync 1, %0;" ::"r"(active) : "memory");
+        float tot = (lane < active / 32) ? wsum[k & 1][lane] : 0.f;
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
         energy = __shfl_sync(0xffffffffu, tot, 0);
