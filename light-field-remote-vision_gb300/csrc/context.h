@@ -126,6 +126,11 @@ struct lfrv_ctx {
     lfrv::Workspace ws;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     lfrv::RenderGraph graph;  // replay of a repeated lfrv_render_view_dev call
+    // the warp stage counted the inverse map's buckets for this geometry (W, H, dsf, V, n): the next bucket build
+    // of the same geometry skips its count pass
+    bool buckets_counted = false;
+    long long counted_geometry[5] = {};
+    const float *counted_tau = nullptr;  // the tau2 the counts were taken from
     // helper contexts (own stream and workspace) that prepare batched targets concurrently; created on first use
     std::vector<lfrv_ctx *> lanes;
     std::vector<cudaEvent_t> lane_done;

@@ -153,6 +153,15 @@ __device__ __forceinline__ bool in_splat(float tx, float ty, int W, int H) {
     return !(px < 0 || py < 0 || px > W - 1 || py > H - 1);
 }
 
+// Inverse-map bucket of a source pixel with warp (tx, ty): its footprint anchor offset by ks - 1 on a grid of
+// BW columns (-1: the pixel is not splatted).
+__device__ __forceinline__ long long bucket_of(float tx, float ty, int W, int H, int dsf, int BW) {
+    if (!in_splat(tx, ty, W, H)) return -1;
+    const int ks = dsf + 1;
+    const int x0 = fp_anchor(tx - 0.5f, dsf), y0 = fp_anchor(ty - 0.5f, dsf);
+    return (long long)(y0 + ks - 1) * BW + (x0 + ks - 1);
+}
+
 // Luminance of the Sobel kernels (vtv_sr_kernels_unstructured.cu:121-130).
 __device__ __forceinline__ float lum(float r, float g, float b) { return 0.2126f * r + 0.7152f * g + 0.0722f * b; }
 

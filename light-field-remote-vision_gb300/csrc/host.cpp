@@ -188,7 +188,16 @@ static void read_sums(lfrv_ctx *c, double *host, int count) {
 }
 
 // ------------------------------------------------------------------ inverse footprint map
-static Buckets build_buckets(lfrv_ctx *c, const Geometry &G, const float *tau2) {
+static void geometry_key(const Geometry &G, long long key[5]) {
+    key[0] = G.W;
+    key[1] = G.H;
+    key[2] = G.dsf;
+    key[3] = G.V;
+    key[4] = G.n;
+}
+
+// The inverse map's buffers for geometry G (allocated on first use).
+static Buckets bucket_buffers(lfrv_ctx *c, const Geometry &G) {
     Workspace &ws = c->ws;
     const int ks = G.dsf + 1;
     Buckets B;
@@ -215,7 +224,17 @@ static Buckets build_buckets(lfrv_ctx *c, const Geometry &G, const float *tau2) 
     B.block_offsets2 = aux + 2 * nblk + 1024;
     B.total = aux + 2 * nblk + 2048;
     B.total2 = aux + 2 * nblk + 2049;
-    launch_bucket_build(G, tau2, B, c->stream, c->launches);
+    return B;
+}
+
+static Buckets build_buckets(lfrv_ctx *c, const Geometry &G, const float *tau2) {
+    Buckets B = bucket_buffers(c, G);
+    long long key[5];
+    geometry_key(G, key);
+    const bool counted = c->buckets_counted && c->counted_tau == tau2 &&
+                         std::memcmp(key, c->counted_geometry, sizeof(key)) == 0;
+    c->buckets_counted = false;
+    launch_bucket_build(G, tau2, B, c->stream, c->launches, counted);
     check_launch("bucket build");
     return B;
 }
@@ -871,7 +890,7 @@ struct UploadPlan {
 
 static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfrv_camera *cams,
                  const lfrv_camera *target, float *tau3, float *dpart3, float *tau2, float *dp2, float *zbuf_out,
-                 const UploadPlan *plan = nullptr) {
+                 const UploadPlan *plan = nullptr, const Geometry *count_for = nullptr) {
     if (V < 1 || V > kMaxViews || w <= 0 || h <= 0 || !depth || !cams || !target)
         raise(LFRV_E_ARG, "bad warp arguments");
     Workspace &ws = c->ws;
@@ -906,8 +925,26 @@ static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfr
     }
     launch_zbuffer_resolve(W, H, ws.zkey.as<unsigned long long>(), ws.zbuf.as<float>(), c->stream, c->launches);
     check_launch("z-buffer");
-    launch_tau(V, w, h, depth, wc, W, H, ws.zbuf.as<float>(), tau3, dpart3, tau2, dp2, c->stream, c->launches);
+    // count_for (the solve's geometry, whose inverse map is built next from tau2): k_tau counts its buckets
+    BucketCount bc;
+    c->buckets_counted = false;
+    if (count_for && tau2) {
+        const Buckets B = bucket_buffers(c, *count_for);
+        LFRV_CUDA(cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, c->stream));
+        if (B.mask) LFRV_CUDA(cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb, c->stream));
+        bc.count = B.count;
+        bc.mask = B.mask;
+        bc.dsf = count_for->dsf;
+        bc.BW = B.BW;
+    }
+    launch_tau(V, w, h, depth, wc, W, H, ws.zbuf.as<float>(), tau3, dpart3, tau2, dp2, c->stream, c->launches,
+               bc.count ? &bc : nullptr);
     check_launch("tau");
+    if (bc.count) {
+        c->buckets_counted = true;
+        geometry_key(*count_for, c->counted_geometry);
+        c->counted_tau = tau2;
+    }
     if (zbuf_out)
         LFRV_CUDA(cudaMemcpyAsync(zbuf_out, ws.zbuf.p, sizeof(float) * N, cudaMemcpyDeviceToDevice, c->stream));
 }
@@ -962,9 +999,11 @@ static void end_timing(lfrv_ctx *c, lfrv_stats *st, long long launches0) {
 
 using namespace lfrv;
 
+// (every call starts without counted buckets: a count the warp stage took belongs to the call that took it)
 #define CTX_CHECK(ctx)                                                   \
     if (!(ctx)) return lfrv::fail(LFRV_E_ARG, "null context");           \
-    LFRV_CUDA(cudaSetDevice((ctx)->device));
+    LFRV_CUDA(cudaSetDevice((ctx)->device));                             \
+    (ctx)->buckets_counted = false;
 
 // ====================================================================== contexts
 extern "C" int lfrv_ctx_create(lfrv_ctx **out, int device) {
@@ -1283,7 +1322,7 @@ static void render_view_body(lfrv_ctx *ctx, const lfrv_config &cfg, int algorith
     ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
     ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
     warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr,
-         plan);
+         plan, &G);
     if (algorithm == 0) {
         if (plan) LFRV_CUDA(cudaStreamWaitEvent(ctx->stream, plan->views_ready, 0));
         color_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);

@@ -66,11 +66,20 @@ void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float 
                             LaunchCounter &lc);
 // tau3/dpart3: reference format (V x 3 x n); tau2/dp2: solver format (V x 2 x n), dp2 premultiplied by sigma_z.
 // Any output may be null.
+// The inverse map's per-bucket counts (and view masks) that k_tau can accumulate while it writes tau, so the
+// bucket build needs no count pass of its own (count and mask zeroed beforehand).
+struct BucketCount {
+    unsigned int *count = nullptr;
+    unsigned long long *mask = nullptr;  // null when V > 64
+    int dsf = 0, BW = 0;
+};
 void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H, const float *zbuf,
-                float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc);
+                float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc,
+                const BucketCount *bc = nullptr);
 
 // ---- solver stage (kernels_solver.cu)
-void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc);
+void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc,
+                         bool counted = false);
 void launch_residual(const Geometry &G, const float *U, const float *img, const float *tau, const float *wgt, float s2,
                      float *res, double *partial, cudaStream_t st, LaunchCounter &lc);
 int residual_partials(const Geometry &G);

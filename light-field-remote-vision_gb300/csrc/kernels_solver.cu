@@ -38,12 +38,6 @@ __device__ __forceinline__ void stv(__nv_bfloat16 *p, float v) { *p = __float2bf
 // two entries of one view take slots from the cursor (in arrival order) and need the sort.
 constexpr int kBucketPer = 4;
 
-__device__ __forceinline__ long long bucket_of(float tx, float ty, int W, int H, int dsf, int BW) {
-    if (!in_splat(tx, ty, W, H)) return -1;
-    const int ks = dsf + 1;
-    const int x0 = fp_anchor(tx - 0.5f, dsf), y0 = fp_anchor(ty - 0.5f, dsf);
-    return (long long)(y0 + ks - 1) * BW + (x0 + ks - 1);
-}
 
 __global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
                                unsigned int *__restrict__ cnt, unsigned long long *__restrict__ mask) {
@@ -1136,14 +1130,17 @@ static inline dim3 grid2(int W, int H, dim3 b) { return dim3((W + b.x - 1) / b.x
         default: break;                                                                 \
     }
 
-void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc) {
+void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc,
+                         bool counted) {
     ProfScope _ps(lc, "bucket_build", st);
     const int ks = G.dsf + 1;
     const dim3 b1(256), gs((G.n + 256 * kBucketPer - 1) / (256 * kBucketPer), G.V);
-    cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
-    if (B.mask) cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb, st);
-    k_bucket_count<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.count, B.mask);
-    lc.add(1);
+    if (!counted) {  // else k_tau has counted while writing tau
+        cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
+        if (B.mask) cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb, st);
+        k_bucket_count<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.count, B.mask);
+        lc.add(1);
+    }
     // exclusive scan of the counts: block-local scans, then every block adds the sum of the block totals before
     // it (integer sums, so the result does not depend on the order) and the last block writes the total
     const int nblk = (B.nb + kScanBlock - 1) / kScanBlock;

@@ -356,7 +356,7 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
                                              const WarpCams cams, int W, int H,
                                              const float *__restrict__ zbuf, float *__restrict__ tau3,
                                              float *__restrict__ dpart3, float *__restrict__ tau2,
-                                             float *__restrict__ dp2) {
+                                             float *__restrict__ dp2, BucketCount bc) {
     const int v = blockIdx.y;
     const int n = w * h;
     const int m0 = blockIdx.x * blockDim.x * kTauPer + threadIdx.x;
@@ -411,6 +411,14 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
         if (dp2) {
             dp2[b2 + m] = 10.0f * p.rx;
             dp2[b2 + n + m] = 10.0f * p.ry;
+        }
+        // the inverse map's count of this pixel's bucket, from the tau just written (k_bucket_count's rule)
+        if (bc.count) {
+            const long long b = bucket_of(t0, t1, W, H, bc.dsf, bc.BW);
+            if (b >= 0) {
+                atomicAdd(&bc.count[b], 1u);
+                if (bc.mask) atomicOr(&bc.mask[b], 1ull << v);
+            }
         }
     }
 }
@@ -590,11 +598,13 @@ void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float 
 }
 
 void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H, const float *zbuf,
-                float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc) {
+                float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc,
+                const BucketCount *bc) {
     ProfScope _ps(lc, "tau", st);
     const int n = w * h;
+    const BucketCount count = bc ? *bc : BucketCount{};
     k_tau<<<dim3((n + 256 * kTauPer - 1) / (256 * kTauPer), V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zbuf, tau3,
-                                                                               dpart3, tau2, dp2);
+                                                                               dpart3, tau2, dp2, count);
     lc.add(1);
 }
 
