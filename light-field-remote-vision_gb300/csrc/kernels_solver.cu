@@ -137,24 +137,49 @@ __global__ void __launch_bounds__(kSortBuckets) k_bucket_sort(int nb, const unsi
     }
 }
 
-// Exclusive scan of unsigned counts (three-phase: block scans, scan of block sums, add back).
-constexpr int kScanBlock = 1024;
+// Exclusive scan of unsigned counts: each block scans kScanPer * kScanBlock counts (kScanPer per thread: a
+// thread's own prefix, then warp shuffles over the thread totals and one warp over the warp totals) and writes its
+// total; k_scan_finish then adds to every block the totals of the blocks before it. Integer sums: the result does
+// not depend on the order.
+constexpr int kScanBlock = 1024, kScanPer = 4, kScanSpan = kScanBlock * kScanPer;
 
-__global__ void k_scan_blocks(int nb, const unsigned int *__restrict__ in, unsigned int *__restrict__ out,
-                              unsigned int *__restrict__ block_sums) {
-    __shared__ unsigned int s[kScanBlock];
-    const int i = blockIdx.x * kScanBlock + threadIdx.x;
-    const unsigned int v = (i < nb) ? in[i] : 0u;
-    s[threadIdx.x] = v;
-    __syncthreads();
-    for (int off = 1; off < kScanBlock; off <<= 1) {
-        const unsigned int t = (threadIdx.x >= off) ? s[threadIdx.x - off] : 0u;
-        __syncthreads();
-        s[threadIdx.x] += t;
-        __syncthreads();
+__global__ void __launch_bounds__(kScanBlock) k_scan_blocks(int nb, const unsigned int *__restrict__ in,
+                                                            unsigned int *__restrict__ out,
+                                                            unsigned int *__restrict__ block_sums) {
+    __shared__ unsigned int warp_tot[kScanBlock / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int i0 = blockIdx.x * kScanSpan + threadIdx.x * kScanPer;
+    unsigned int v[kScanPer];
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j) v[j] = (i0 + j < nb) ? in[i0 + j] : 0u;
+    unsigned int t = 0;
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j) t += v[j];
+    unsigned int incl = t;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int u = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += u;
     }
-    if (i < nb) out[i] = s[threadIdx.x] - v;  // exclusive
-    if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = s[threadIdx.x];
+    if (lane == 31) warp_tot[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        unsigned int w = warp_tot[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const unsigned int u = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= o) w += u;
+        }
+        warp_tot[lane] = w;  // inclusive over warps
+    }
+    __syncthreads();
+    unsigned int run = (wid > 0 ? warp_tot[wid - 1] : 0u) + incl - t;  // exclusive prefix of this thread
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j) {
+        if (i0 + j < nb) out[i0 + j] = run;
+        run += v[j];
+    }
+    if (threadIdx.x == kScanBlock - 1) block_sums[blockIdx.x] = warp_tot[31];
 }
 
 // Adds to block b's exclusive scan the sum of the totals of blocks 0 .. b - 1; out[nb] = the grand total.
@@ -175,8 +200,10 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_finish(int nb, unsigned int
     }
     __syncthreads();
     const unsigned int off = red[0];
-    const int i = blockIdx.x * kScanBlock + threadIdx.x;
-    if (i < nb) out[i] += off;
+    const int i0 = blockIdx.x * kScanSpan + threadIdx.x * kScanPer;
+#pragma unroll
+    for (int j = 0; j < kScanPer; ++j)
+        if (i0 + j < nb) out[i0 + j] += off;
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[nb] = off + block_sums[blockIdx.x];
 }
 
@@ -1143,7 +1170,7 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
     }
     // exclusive scan of the counts: block-local scans, then every block adds the sum of the block totals before
     // it (integer sums, so the result does not depend on the order) and the last block writes the total
-    const int nblk = (B.nb + kScanBlock - 1) / kScanBlock;
+    const int nblk = (B.nb + kScanSpan - 1) / kScanSpan;
     k_scan_blocks<<<nblk, kScanBlock, 0, st>>>(B.nb, B.count, B.start, B.block_sums);
     k_scan_finish<<<nblk, kScanBlock, 0, st>>>(B.nb, B.start, B.block_sums);
     lc.add(2);
