@@ -1321,14 +1321,17 @@ static void render_view_body(lfrv_ctx *ctx, const lfrv_config &cfg, int algorith
     Workspace &ws = ctx->ws;
     ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
     ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
-    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr,
-         plan, &G);
+    // IBR_gradient uses dtau/dz only in its weights, multiplied by the gradient of U = 0 (compute_weights with
+    // U = 0): the warp stage does not write it and the weights take it as 0 (the same weights wherever they are
+    // read: a pixel whose dtau/dz is not finite is outside the view and in no bucket)
+    float *dp2 = algorithm == 0 ? ws.dp.as<float>() : nullptr;
+    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), dp2, nullptr, plan, &G);
     if (algorithm == 0) {
         if (plan) LFRV_CUDA(cudaStreamWaitEvent(ctx->stream, plan->views_ready, 0));
-        color_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats);
+        color_solve(ctx, cfg, d_views, ws.tau.as<float>(), dp2, nullptr, d_out, stats);
     } else {
         // the inverse map and the weights need only the warps: they do not wait for the colour views' upload
-        gradient_solve(ctx, cfg, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, d_out, stats,
+        gradient_solve(ctx, cfg, d_views, ws.tau.as<float>(), nullptr, nullptr, d_out, stats,
                        plan ? plan->views_ready : nullptr);
     }
     if (host_out)

@@ -276,7 +276,9 @@ __global__ void __launch_bounds__(256, GATHER ? 1 : 8) k_weights(int V, int n, i
     const float txm = __ldg(tx + m), tym = __ldg(ty + m);
     const float txl = __ldg(tx + ml), tyl = __ldg(ty + ml), txr = __ldg(tx + mr), tyr = __ldg(ty + mr);
     const float txu = __ldg(tx + mu), tyu = __ldg(ty + mu), txd = __ldg(tx + md), tyd = __ldg(ty + md);
-    const float dpx = __ldg(dp + (size_t)v * 2 * n + m), dpy = __ldg(dp + (size_t)v * 2 * n + n + m);
+    // (no dp: dtau/dz taken as 0, for callers whose gathered gradient is 0 anyway)
+    const float dpx = dp ? __ldg(dp + (size_t)v * 2 * n + m) : 0.f;
+    const float dpy = dp ? __ldg(dp + (size_t)v * 2 * n + n + m) : 0.f;
     float ax = 0.f, ay = 0.f;
     if (GATHER && in_gather(txm, tym, W, H)) {
         Footprint fp;
