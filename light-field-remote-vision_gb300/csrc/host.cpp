@@ -923,7 +923,9 @@ static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfr
     } else {
         launch_zbuffer_splat(V, w, h, depth, wc, W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
     }
-    launch_zbuffer_resolve(W, H, ws.zkey.as<unsigned long long>(), ws.zbuf.as<float>(), c->stream, c->launches);
+    // the resolved depth map only when the caller wants it; otherwise k_tau samples the keys themselves
+    if (zbuf_out)
+        launch_zbuffer_resolve(W, H, ws.zkey.as<unsigned long long>(), ws.zbuf.as<float>(), c->stream, c->launches);
     check_launch("z-buffer");
     // count_for (the solve's geometry, whose inverse map is built next from tau2): k_tau counts its buckets
     BucketCount bc;
@@ -937,8 +939,8 @@ static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfr
         bc.dsf = count_for->dsf;
         bc.BW = B.BW;
     }
-    launch_tau(V, w, h, depth, wc, W, H, ws.zbuf.as<float>(), tau3, dpart3, tau2, dp2, c->stream, c->launches,
-               bc.count ? &bc : nullptr);
+    launch_tau(V, w, h, depth, wc, W, H, zbuf_out ? ws.zbuf.as<float>() : nullptr, tau3, dpart3, tau2, dp2, c->stream,
+               c->launches, bc.count ? &bc : nullptr, ws.zkey.as<unsigned long long>());
     check_launch("tau");
     if (bc.count) {
         c->buckets_counted = true;

@@ -75,7 +75,7 @@ struct BucketCount {
 };
 void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H, const float *zbuf,
                 float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc,
-                const BucketCount *bc = nullptr);
+                const BucketCount *bc = nullptr, const unsigned long long *zkey = nullptr);  // zbuf null: read zkey
 
 // ---- solver stage (kernels_solver.cu)
 void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc,

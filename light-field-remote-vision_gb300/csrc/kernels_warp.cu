@@ -42,11 +42,6 @@ __device__ __forceinline__ void warp_point(const ViewCam &c, float px, float py,
 }
 
 // ------------------------------------------------------------------ target depth map
-__global__ void k_zclear(size_t N, unsigned long long *zkey) {
-    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < N) zkey[i] = 0ull;
-}
-
 __device__ __forceinline__ float edgef(float ax, float ay, float bx, float by, float px, float py) {
     return (bx - ax) * (py - ay) - (by - ay) * (px - ax);
 }
@@ -293,15 +288,33 @@ __global__ void __launch_bounds__(256, 4) k_zsplat(int V, int w, int h, const fl
     if (m1 < n) zsplat_pixel(c, m1, w, z1, zx1, zy1, W, H, zkey);
 }
 
+// The target depth a z-buffer key holds (its centre depth; 0 where nothing was splatted).
+__device__ __forceinline__ float zkey_depth(unsigned long long k) {
+    return k ? __uint_as_float(~(unsigned int)(k & 0xFFFFFFFFull)) : 0.0f;
+}
+
 __global__ void k_zresolve(size_t N, const unsigned long long *__restrict__ zkey, float *__restrict__ zbuf) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= N) return;
-    const unsigned long long k = zkey[i];
-    zbuf[i] = k ? __uint_as_float(~(unsigned int)(k & 0xFFFFFFFFull)) : 0.0f;
+    zbuf[i] = zkey_depth(zkey[i]);
 }
 
 // ------------------------------------------------------------------ tau and dtau/dz
-// GL_LINEAR on a sampler2DRect with CLAMP_TO_EDGE (sources/openGL/texture.cpp:153-156).
+// GL_LINEAR on a sampler2DRect with CLAMP_TO_EDGE (sources/openGL/texture.cpp:153-156) of the target depth map,
+// read from the resolved map or straight from the z-buffer keys (zkey_depth of each tap).
+__device__ __forceinline__ float bilinear_clamp(const unsigned long long *zkey, int W, int H, float u, float v) {
+    const float fx = u - 0.5f, fy = v - 0.5f;
+    const float flx = floorf(fx), fly = floorf(fy);
+    const float ax = fx - flx, ay = fy - fly;
+    const int x0 = (int)flx, y0 = (int)fly;
+    auto at = [&](int x, int y) {
+        x = min(max(x, 0), W - 1);
+        y = min(max(y, 0), H - 1);
+        return zkey_depth(__ldg(zkey + (size_t)y * W + x));
+    };
+    return (1.f - ay) * ((1.f - ax) * at(x0, y0) + ax * at(x0 + 1, y0)) +
+           ay * ((1.f - ax) * at(x0, y0 + 1) + ax * at(x0 + 1, y0 + 1));
+}
 __device__ __forceinline__ float bilinear_clamp(const float *img, int W, int H, float u, float v) {
     const float fx = u - 0.5f, fy = v - 0.5f;
     const float flx = floorf(fx), fly = floorf(fy);
@@ -356,7 +369,8 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
                                              const WarpCams cams, int W, int H,
                                              const float *__restrict__ zbuf, float *__restrict__ tau3,
                                              float *__restrict__ dpart3, float *__restrict__ tau2,
-                                             float *__restrict__ dp2, BucketCount bc) {
+                                             float *__restrict__ dp2, BucketCount bc,
+                                             const unsigned long long *__restrict__ zkey) {
     const int v = blockIdx.y;
     const int n = w * h;
     const int m0 = blockIdx.x * blockDim.x * kTauPer + threadIdx.x;
@@ -373,7 +387,8 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
     // the target depth map at every projection (clamped, so every sample is in bounds; out-of-range points
     // do not use it)
 #pragma unroll
-    for (int j = 0; j < kTauPer; ++j) zs[j] = bilinear_clamp(zbuf, W, H, px[j].xu, px[j].yu);
+    for (int j = 0; j < kTauPer; ++j)
+        zs[j] = zbuf ? bilinear_clamp(zbuf, W, H, px[j].xu, px[j].yu) : bilinear_clamp(zkey, W, H, px[j].xu, px[j].yu);
 #pragma unroll
     for (int j = 0; j < kTauPer; ++j) {
         const int m = m0 + j * (int)blockDim.x;
@@ -425,9 +440,7 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
 
 void launch_zbuffer_clear(int W, int H, unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "zbuffer_clear", st);
-    const size_t N = (size_t)W * H;
-    k_zclear<<<(unsigned)((N + 255) / 256), 256, 0, st>>>(N, zkey);
-    lc.add(1);
+    cudaMemsetAsync(zkey, 0, sizeof(unsigned long long) * (size_t)W * H, st);  // key 0: nothing splatted
 }
 
 void launch_zbuffer_splat(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H,
@@ -599,12 +612,12 @@ void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float 
 
 void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H, const float *zbuf,
                 float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc,
-                const BucketCount *bc) {
+                const BucketCount *bc, const unsigned long long *zkey) {
     ProfScope _ps(lc, "tau", st);
     const int n = w * h;
     const BucketCount count = bc ? *bc : BucketCount{};
     k_tau<<<dim3((n + 256 * kTauPer - 1) / (256 * kTauPer), V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zbuf, tau3,
-                                                                               dpart3, tau2, dp2, count);
+                                                                               dpart3, tau2, dp2, count, zkey);
     lc.add(1);
 }
 
