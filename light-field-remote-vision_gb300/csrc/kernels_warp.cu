@@ -170,8 +170,9 @@ __device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigne
 //   - edge values are taken relative to the box's first centre (the same differences as edgef's) and scaled
 //     by the triangle's winding sign, so "inside" is w >= thr on every edge, with thr = 0 on a top-left edge
 //     and the smallest positive float elsewhere (the library is built without flush-to-zero);
-//   - the depth is tri_cover's barycentric quotient with its terms in the same order, divided approximately
-//     (__fdividef, within 2 ulp; the key only orders surfaces whose depths differ by far more).
+//   - the depth is the triangle's 1/z plane (tri_cover's barycentric interpolation, which is affine over the
+//     triangle) evaluated at the centre: within a few ulp of tri_cover's quotient, and the key only orders
+//     surfaces whose depths differ by far more.
 // The 3 x 3 window is unrolled. Returns false when the quad needs raster_quad.
 __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc, int W, int H,
                                                   unsigned long long *zkey) {
@@ -212,6 +213,20 @@ __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc,
     const Edge e12 = edge(1, 2, sA, ccwA), a1 = edge(2, 0, sA, ccwA), a2 = edge(0, 1, sA, ccwA);
     const Edge b0 = edge(2, 3, -sA, !ccwA), b1 = edge(3, 1, -sA, !ccwA);
     auto w = [](const Edge &e, float i, float j) { return e.dx * (j - e.ay) - e.dy * (i - e.ax); };
+    // 1/z is affine over each triangle: iz(i, j) = P0 + Px i + Py j, from the barycentric numerator (the edge
+    // values weighting the vertices' 1/z, each edge value affine in (i, j)) over the triangle's doubled area
+    // (the sum of its sign-scaled edge values)
+    auto plane = [&](const Edge &e0, float za, const Edge &e1, float zb, const Edge &e2, float zc2, float s0,
+                     float area, float &P0, float &Px, float &Py) {
+        const float inv = __fdividef(1.0f, fabsf(area));
+        P0 = (s0 * w(e0, 0.f, 0.f) * za + w(e1, 0.f, 0.f) * zb + w(e2, 0.f, 0.f) * zc2) * inv;
+        Px = -(s0 * e0.dy * za + e1.dy * zb + e2.dy * zc2) * inv;
+        Py = (s0 * e0.dx * za + e1.dx * zb + e2.dx * zc2) * inv;
+    };
+    // A = (v0, v1, v2): weights (w12, wa1, wa2); B = (v1, v2, v3): weights (wb0, wb1, -w12)
+    float PA0, PAx, PAy, PB0, PBx, PBy;
+    plane(e12, v[0][2], a1, v[1][2], a2, v[2][2], 1.f, areaA, PA0, PAx, PAy);
+    plane(e12, v[3][2], b0, v[1][2], b1, v[2][2], -1.f, areaB, PB0, PBx, PBy);
     const unsigned int zlow = ~__float_as_uint(zc);
     // one row of the window at a time: the three cells' keys, then their depth-buffer loads together (the
     // depth test of depth_test, its loads not serialised behind each other's branches)
@@ -228,11 +243,7 @@ __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc,
             const bool inA = w12 >= e12.thr;
             const float wa1 = w(a1, fi, fj), wa2 = w(a2, fi, fj), wb0 = w(b0, fi, fj), wb1 = w(b1, fi, fj);
             const bool cov = inA ? (wa1 >= a1.thr && wa2 >= a2.thr) : (wb0 >= b0.thr && wb1 >= b1.thr);
-            // A = (v0, v1, v2) with weights (w12, wa1, wa2); B = (v1, v2, v3) with (wb0, wb1, -w12)
-            const float w0 = inA ? w12 : wb0, w1 = inA ? wa1 : wb1, w2 = inA ? wa2 : -w12;
-            const float z0 = inA ? v[0][2] : v[1][2], z1 = inA ? v[1][2] : v[2][2], z2 = inA ? v[2][2] : v[3][2];
-            // the approximate quotient (within 2 ulp): a depth key, compared at 1e-4 and far coarser downstream
-            const float iz = __fdividef(w0 * z0 + w1 * z1 + w2 * z2, w0 + w1 + w2);
+            const float iz = inA ? fmaf(PAy, fj, fmaf(PAx, fi, PA0)) : fmaf(PBy, fj, fmaf(PBx, fi, PB0));
             hit[i] = i <= xmax - xmin && cov && iz > 0.f;
             key[i] = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
         }
