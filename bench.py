@@ -99,9 +99,9 @@ def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: in
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu --set full capture of the
 # C2 step; the captures and their commands are summarised in profiles/*_c2.md.
 NCU_TRAFFIC_BYTES = {
-    "zbuffer_splat": 83.936512e6 + 2.556160e6,
-    "gradient_setup": 224.133632e6 + 18.189056e6,
-    "cg_persistent": 21.045248e6 + 0.014336e6,
+    "zbuffer_splat": 83.937280e6 + 2.382336e6,
+    "gradient_setup": 224.049664e6 + 18.143744e6,
+    "cg_persistent": 21.045248e6 + 0.008192e6,
 }
 
 
