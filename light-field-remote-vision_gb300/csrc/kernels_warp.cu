@@ -167,12 +167,13 @@ __device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigne
 // box holds at most 3 x 3 pixel centres. Coverage and depth are tri_cover's for each triangle:
 //   - a centre is tested against the triangle on its side of the shared edge v1v2 only (a centre on that edge
 //     belongs to the triangle for which the edge is top-left; the two flags are complementary);
-//   - edge values are taken relative to the box's first centre (the same differences as edgef's) and scaled
-//     by the triangle's winding sign, so "inside" is w >= thr on every edge, with thr = 0 on a top-left edge
-//     and the smallest positive float elsewhere (the library is built without flush-to-zero);
+//   - edge values are affine in the centre's offset (i, j) from the box's first centre: each edge keeps its
+//     value there and its steps along i and j, scaled by the triangle's winding sign, so "inside" is w >= thr
+//     on every edge, with thr = 0 on a top-left edge and the smallest positive float elsewhere (the library
+//     is built without flush-to-zero). A row's values are its base plus the column steps;
 //   - the depth is the triangle's 1/z plane (tri_cover's barycentric interpolation, which is affine over the
-//     triangle) evaluated at the centre: within a few ulp of tri_cover's quotient, and the key only orders
-//     surfaces whose depths differ by far more.
+//     triangle) evaluated at the centre the same way; it differs from tri_cover's quotient by float rounding
+//     only.
 // The 3 x 3 window is unrolled. Returns false when the quad needs raster_quad.
 __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc, int W, int H,
                                                   unsigned long long *zkey) {
@@ -197,53 +198,58 @@ __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc,
     const bool ccwA = areaA > 0.f;
     const float sA = ccwA ? 1.f : -1.f;
     constexpr float kTiny = 1.40129846e-45f;  // smallest positive float: w >= kTiny is w > 0
-    // edge a -> b scaled by s: w(i, j) = (s dx)(j - qy[a]) - (s dy)(i - qx[a])
+    // edge a -> b scaled by s: w(i, j) = (s dx)(j - qy[a]) - (s dy)(i - qx[a]) = c0 + gi i + gj j
     struct Edge {
-        float ax, ay, dx, dy, thr;
+        float c0, gi, gj, thr;
     };
     auto edge = [&](int a, int b, float s, bool ccw) {
         Edge e;
-        e.ax = qx[a];
-        e.ay = qy[a];
-        e.dx = s * (qx[b] - qx[a]);
-        e.dy = s * (qy[b] - qy[a]);
+        const float dx = s * (qx[b] - qx[a]), dy = s * (qy[b] - qy[a]);
+        e.c0 = dy * qx[a] - dx * qy[a];
+        e.gi = -dy;
+        e.gj = dx;
         e.thr = top_left(qx[a], qy[a], qx[b], qy[b], ccw) ? 0.f : kTiny;
         return e;
     };
     const Edge e12 = edge(1, 2, sA, ccwA), a1 = edge(2, 0, sA, ccwA), a2 = edge(0, 1, sA, ccwA);
     const Edge b0 = edge(2, 3, -sA, !ccwA), b1 = edge(3, 1, -sA, !ccwA);
-    auto w = [](const Edge &e, float i, float j) { return e.dx * (j - e.ay) - e.dy * (i - e.ax); };
-    // 1/z is affine over each triangle: iz(i, j) = P0 + Px i + Py j, from the barycentric numerator (the edge
-    // values weighting the vertices' 1/z, each edge value affine in (i, j)) over the triangle's doubled area
-    // (the sum of its sign-scaled edge values)
+    // 1/z is affine over each triangle: iz(i, j) = P0 + Pi i + Pj j, from the barycentric numerator (the edge
+    // values weighting the vertices' 1/z) over the triangle's doubled area (the sum of its sign-scaled edge
+    // values)
     auto plane = [&](const Edge &e0, float za, const Edge &e1, float zb, const Edge &e2, float zc2, float s0,
-                     float area, float &P0, float &Px, float &Py) {
+                     float area) {
         const float inv = __fdividef(1.0f, fabsf(area));
-        P0 = (s0 * w(e0, 0.f, 0.f) * za + w(e1, 0.f, 0.f) * zb + w(e2, 0.f, 0.f) * zc2) * inv;
-        Px = -(s0 * e0.dy * za + e1.dy * zb + e2.dy * zc2) * inv;
-        Py = (s0 * e0.dx * za + e1.dx * zb + e2.dx * zc2) * inv;
+        Edge p;
+        p.c0 = (s0 * e0.c0 * za + e1.c0 * zb + e2.c0 * zc2) * inv;
+        p.gi = (s0 * e0.gi * za + e1.gi * zb + e2.gi * zc2) * inv;
+        p.gj = (s0 * e0.gj * za + e1.gj * zb + e2.gj * zc2) * inv;
+        p.thr = 0.f;
+        return p;
     };
     // A = (v0, v1, v2): weights (w12, wa1, wa2); B = (v1, v2, v3): weights (wb0, wb1, -w12)
-    float PA0, PAx, PAy, PB0, PBx, PBy;
-    plane(e12, v[0][2], a1, v[1][2], a2, v[2][2], 1.f, areaA, PA0, PAx, PAy);
-    plane(e12, v[3][2], b0, v[1][2], b1, v[2][2], -1.f, areaB, PB0, PBx, PBy);
+    const Edge pA = plane(e12, v[0][2], a1, v[1][2], a2, v[2][2], 1.f, areaA);
+    const Edge pB = plane(e12, v[3][2], b0, v[1][2], b1, v[2][2], -1.f, areaB);
     const unsigned int zlow = ~__float_as_uint(zc);
+    // value of an affine function at row base r (its value at (0, j)) stepped i columns
+    auto at = [](const Edge &e, float r, int i) { return i == 0 ? r : fmaf(e.gi, (float)i, r); };
     // one row of the window at a time: the three cells' keys, then their depth-buffer loads together (the
     // depth test of depth_test, its loads not serialised behind each other's branches)
 #pragma unroll
     for (int j = 0; j < 3; ++j) {
         if (j > ymax - ymin) break;
         unsigned long long *row = zkey + (size_t)(ymin + j) * W + xmin;
+        auto base = [j](const Edge &e) { return j == 0 ? e.c0 : fmaf(e.gj, (float)j, e.c0); };
+        const float r12 = base(e12), ra1 = base(a1), ra2 = base(a2), rb0 = base(b0), rb1 = base(b1);
+        const float rA = base(pA), rB = base(pB);
         unsigned long long key[3], cur[3];
         bool hit[3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-            const float fi = (float)i, fj = (float)j;
-            const float w12 = w(e12, fi, fj);
+            const float w12 = at(e12, r12, i);
             const bool inA = w12 >= e12.thr;
-            const float wa1 = w(a1, fi, fj), wa2 = w(a2, fi, fj), wb0 = w(b0, fi, fj), wb1 = w(b1, fi, fj);
+            const float wa1 = at(a1, ra1, i), wa2 = at(a2, ra2, i), wb0 = at(b0, rb0, i), wb1 = at(b1, rb1, i);
             const bool cov = inA ? (wa1 >= a1.thr && wa2 >= a2.thr) : (wb0 >= b0.thr && wb1 >= b1.thr);
-            const float iz = inA ? fmaf(PAy, fj, fmaf(PAx, fi, PA0)) : fmaf(PBy, fj, fmaf(PBx, fi, PB0));
+            const float iz = inA ? at(pA, rA, i) : at(pB, rB, i);
             hit[i] = i <= xmax - xmin && cov && iz > 0.f;
             key[i] = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
         }
@@ -261,15 +267,21 @@ __device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int m, int w, flo
                                              int H, unsigned long long *zkey) {
     if (z >= 1000.0f * 0.5f) return;  // INVALID_DEPTH / 2 (depthSplatting.geom:21)
     const float cx = (m % w) + 0.5f, cy = (m / w) + 0.5f;
-    float xh[3];
-    warp_point(c, cx, cy, z, xh);
-    const float zc = xh[2];
+    // x_h is linear in the pixel-space point scaled by its depth: with q = M (cx, cy, 1), the centre maps to
+    // z q + b and the corner (cx + dx, cy + dy) at depth z + dx zx + dy zy to (z + dx zx + dy zy)(q + dx M_0 +
+    // dy M_1) + b, M_0 and M_1 the first two columns of M
+    float q[3];
+    mv3(c.M, cx, cy, 1.f, q);
+    const float zc = fmaf(z, q[2], c.b[2]);
     const float off[4][2] = {{-0.5f, -0.5f}, {-0.5f, 0.5f}, {0.5f, -0.5f}, {0.5f, 0.5f}};  // BL TL BR TR
     float vert[4][3];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const float dx = off[k][0], dy = off[k][1];
-        warp_point(c, cx + dx, cy + dy, z + dx * zx + dy * zy, xh);
+        const float zk = fmaf(dy, zy, fmaf(dx, zx, z));
+        float xh[3];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) xh[r] = fmaf(zk, fmaf(dy, c.M[3 * r + 1], fmaf(dx, c.M[3 * r], q[r])), c.b[r]);
         if (!(xh[2] > 1e-2f)) return;  // behind the near plane (zNear = 1e-2, sources/pinholeCamera.cpp:133)
         const float iw = __fdividef(1.0f, xh[2]);  // approximate reciprocal: vertex positions within 2 ulp
         vert[k][0] = xh[0] * iw;
