@@ -20,7 +20,7 @@ __device__ __forceinline__ void mv3(const float *M, float x, float y, float z, f
     o[2] = M[6] * x + M[7] * y + M[8] * z;
 }
 
-// x_h of the point at pixel-space (px, py) with depth z seen from view cam.
+// One input view's fold of the cameras: the target homogeneous point of pixel (x, y) at depth z is M (z x, z y, z) + b.
 struct ViewCam {
     float M[9], b[3];
 };
@@ -32,13 +32,6 @@ __device__ __forceinline__ ViewCam view_cam(const WarpCams &cams, int v) {
 #pragma unroll
     for (int i = 0; i < 3; ++i) c.b[i] = cams.b[v][i];
     return c;
-}
-
-__device__ __forceinline__ void warp_point(const ViewCam &c, float px, float py, float z, float *xh) {
-    mv3(c.M, z * px, z * py, z, xh);
-    xh[0] += c.b[0];
-    xh[1] += c.b[1];
-    xh[2] += c.b[2];
 }
 
 // ------------------------------------------------------------------ target depth map
@@ -364,8 +357,16 @@ __device__ __forceinline__ TauPix tau_project(const ViewCam &c, int m, int w, fl
     TauPix p;
     p.z = z;
     const float x = (m % w) + 0.5f, y = (m / w) + 0.5f;
-    float xuh[3];
-    warp_point(c, x, y, z, xuh);
+    // with mk = M (x, y, 1): x_h = z mk + b, and the Jacobian's columns M (x zx + z, y zx, zx) = zx mk + z M_0
+    // and M (x zy, y zy + z, zy) = zy mk + z M_1 (M_0, M_1 the first two columns of M)
+    float mk[3], xuh[3], m0[3], m1[3];
+    mv3(c.M, x, y, 1.0f, mk);
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        xuh[r] = fmaf(z, mk[r], c.b[r]);
+        m0[r] = fmaf(zx, mk[r], z * c.M[3 * r]);
+        m1[r] = fmaf(zy, mk[r], z * c.M[3 * r + 1]);
+    }
     p.xu = 0.f;
     p.yu = 0.f;
     if (xuh[2] != 0.f) {
@@ -374,10 +375,6 @@ __device__ __forceinline__ TauPix tau_project(const ViewCam &c, int m, int w, fl
     }
     p.zt = xuh[2];
     // Jacobian of the euclidean normalisation applied to M columns (tauWarp.frag:41-50)
-    float m0[3], m1[3], mk[3];
-    mv3(c.M, x * zx + z, y * zx, zx, m0);
-    mv3(c.M, x * zy, y * zy + z, zy, m1);
-    mv3(c.M, x, y, 1.0f, mk);
     const float iz = 1.0f / xuh[2];
     const float d00 = (m0[0] - p.xu * m0[2]) * iz, d01 = (m0[1] - p.yu * m0[2]) * iz;
     const float d10 = (m1[0] - p.xu * m1[2]) * iz, d11 = (m1[1] - p.yu * m1[2]) * iz;
