@@ -730,7 +730,8 @@ static void cg_persistent_async(lfrv_ctx *c, int W, int H, int max_iter, double 
 // average, gradient splat) into U, gx, gy, then hole filling of U (or U = init).
 static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry &G, const float *img,
                              const float *tau2, const float *dp2, const float *init, float *U, float *gx, float *gy,
-                             void *learn_in = nullptr, cudaEvent_t views_ready = nullptr) {
+                             void *learn_in = nullptr, cudaEvent_t views_ready = nullptr,
+                             const void *vg_early = nullptr) {
     const size_t N = G.N;
     cudaStream_t s = c->stream;
     Workspace &ws = c->ws;
@@ -755,9 +756,12 @@ static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
     launch_weights(G, nullptr, nullptr, tau2, dp2, cfg.sigma_sensor, cfg.ugrad_threshold, b.wgt, side, c->launches,
                    bf);
     check_launch("weights");
-    // views still uploading (views_ready): only the view gradients wait for them, and the set-up through the join
-    if (views_ready) LFRV_CUDA(cudaStreamWaitEvent(side, views_ready, 0));
-    const void *vg = bf ? view_gradients_bf16(c, G, img, side) : (const void *)view_gradients(c, G, img, side);
+    // views still uploading (views_ready): only the view gradients wait for them, and the set-up through the join.
+    // vg_early: the caller already launched them on the side stream, ahead of the weights
+    if (views_ready && !vg_early) LFRV_CUDA(cudaStreamWaitEvent(side, views_ready, 0));
+    const void *vg = vg_early ? vg_early
+                     : bf     ? view_gradients_bf16(c, G, img, side)
+                              : (const void *)view_gradients(c, G, img, side);
     if (fork) LFRV_CUDA(cudaEventRecord(c->side_join, side));
     const Buckets B = build_buckets(c, G, tau2);
     if (fork) LFRV_CUDA(cudaStreamWaitEvent(s, c->side_join, 0));
@@ -774,7 +778,8 @@ static void gradient_prepare(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
 }
 
 static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
-                           const float *init, float *out, lfrv_stats *st, cudaEvent_t views_ready = nullptr) {
+                           const float *init, float *out, lfrv_stats *st, cudaEvent_t views_ready = nullptr,
+                           const void *vg_early = nullptr) {
     check_solver_options(cfg);
     const Geometry G = geometry(cfg);
     if (G.W < 2 || G.H < 2) raise(LFRV_E_ARG, "IBR_gradient needs a target of at least 2 x 2 pixels");
@@ -784,7 +789,7 @@ static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img
     ColorBuffers b = color_buffers(c, G);
     float *U = ws.U.as<float>();
     c->pending = Pending{};
-    gradient_prepare(c, cfg, G, img, tau2, dp2, init, U, b.gx, b.gy, nullptr, views_ready);
+    gradient_prepare(c, cfg, G, img, tau2, dp2, init, U, b.gx, b.gy, nullptr, views_ready, vg_early);
     int it_faithful = 0;
     if (cfg.faithful) it_faithful = cg_faithful(c, G.W, G.H, b.gx, b.gy, U);
     else cg_persistent_async(c, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U);
@@ -1327,6 +1332,17 @@ static void render_view_body(lfrv_ctx *ctx, const lfrv_config &cfg, int algorith
     // U = 0): the warp stage does not write it and the weights take it as 0 (the same weights wherever they are
     // read: a pixel whose dtau/dz is not finite is outside the view and in no bucket)
     float *dp2 = algorithm == 0 ? ws.dp.as<float>() : nullptr;
+    // IBR_gradient from device-resident views: their Sobel needs only the views, so it starts on the side stream
+    // beside the warp stage (gradient_prepare's join after the weights also covers it). Not with per-kernel
+    // profiling or in a helper lane, where gradient_prepare keeps its work on one stream.
+    const void *vg_early = nullptr;
+    if (algorithm == 1 && !plan && ctx->launches.prof == nullptr && !ctx->lane) {
+        cudaStream_t side = side_stream(ctx);
+        LFRV_CUDA(cudaEventRecord(ctx->side_fork, ctx->stream));
+        LFRV_CUDA(cudaStreamWaitEvent(side, ctx->side_fork, 0));
+        vg_early = cfg.bf16_storage ? view_gradients_bf16(ctx, G, d_views, side)
+                                    : (const void *)view_gradients(ctx, G, d_views, side);
+    }
     warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), dp2, nullptr, plan, &G);
     if (algorithm == 0) {
         if (plan) LFRV_CUDA(cudaStreamWaitEvent(ctx->stream, plan->views_ready, 0));
@@ -1334,7 +1350,7 @@ static void render_view_body(lfrv_ctx *ctx, const lfrv_config &cfg, int algorith
     } else {
         // the inverse map and the weights need only the warps: they do not wait for the colour views' upload
         gradient_solve(ctx, cfg, d_views, ws.tau.as<float>(), nullptr, nullptr, d_out, stats,
-                       plan ? plan->views_ready : nullptr);
+                       plan ? plan->views_ready : nullptr, vg_early);
     }
     if (host_out)
         LFRV_CUDA(cudaMemcpyAsync(host_out, d_out, sizeof(float) * 3 * G.N, cudaMemcpyDeviceToHost, ctx->stream));
