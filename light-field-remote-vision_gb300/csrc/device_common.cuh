@@ -8,6 +8,29 @@
 
 namespace lfrv {
 
+// Programmatic dependent launch. A kernel launched by launch_pdl may be scheduled while the kernel before it in
+// the stream is finishing; pdl_wait() returns once that kernel has completed and its writes are visible, so a
+// kernel calls it before touching anything earlier work wrote. pdl_trigger() lets the next such kernel be
+// scheduled once every block of this one has issued it. Both are no-ops in a kernel launched the ordinary way.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <typename... Params, typename... Args>
+inline cudaError_t launch_pdl(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t st,
+                              Args... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kernel, static_cast<Params>(args)...);
+}
+
 constexpr int kMaxKs = 5;  // ks = dsf + 1, dsf <= 4
 
 // ------------------------------------------------------------------ footprint of a source pixel

@@ -623,8 +623,7 @@ static void hole_fill_async(lfrv_ctx *c, int W, int H, const uint8_t *vis, float
     ws.hole_count.ensure(sizeof(int) * 4);
     launch_hole_list(W, H, vis, ws.holes.as<int>(), ws.hole_count.as<int>(), s, c->launches);
     check_launch("hole list");
-    ws.Ua.ensure(3 * N * sizeof(float));
-    LFRV_CUDA(cudaMemcpyAsync(ws.Ua.p, U, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    ws.Ua.ensure(3 * N * sizeof(float));  // the grid-wide kernel's second buffer (it fills what it reads)
     double *part = partial_buf(c, 2 * (size_t)persistent_partials());
     const GridBarrier gb = fresh_barrier(c);
     LFRV_CUDA(launch_hole_fill_persistent(W, H, ws.holes.as<int>(), ws.hole_count.as<int>(), U, ws.Ua.as<float>(),
@@ -909,6 +908,19 @@ static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfr
     ws.zkey.ensure(sizeof(unsigned long long) * N);
     ws.zbuf.ensure(sizeof(float) * N);
     launch_zbuffer_clear(W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
+    // count_for (the solve's geometry, whose inverse map is built next from tau2): k_tau counts its buckets. The
+    // counts are cleared here, ahead of the splat, so that k_tau directly follows the z-buffer kernels
+    BucketCount bc;
+    c->buckets_counted = false;
+    if (count_for && tau2) {
+        const Buckets B = bucket_buffers(c, *count_for);
+        LFRV_CUDA(cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, c->stream));
+        if (B.mask) LFRV_CUDA(cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb, c->stream));
+        bc.count = B.count;
+        bc.mask = B.mask;
+        bc.dsf = count_for->dsf;
+        bc.BW = B.BW;
+    }
     if (plan) {
         // splat each chunk of views as soon as its depth maps have arrived
         int v0 = 0;
@@ -932,18 +944,6 @@ static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfr
     if (zbuf_out)
         launch_zbuffer_resolve(W, H, ws.zkey.as<unsigned long long>(), ws.zbuf.as<float>(), c->stream, c->launches);
     check_launch("z-buffer");
-    // count_for (the solve's geometry, whose inverse map is built next from tau2): k_tau counts its buckets
-    BucketCount bc;
-    c->buckets_counted = false;
-    if (count_for && tau2) {
-        const Buckets B = bucket_buffers(c, *count_for);
-        LFRV_CUDA(cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, c->stream));
-        if (B.mask) LFRV_CUDA(cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb, c->stream));
-        bc.count = B.count;
-        bc.mask = B.mask;
-        bc.dsf = count_for->dsf;
-        bc.BW = B.BW;
-    }
     launch_tau(V, w, h, depth, wc, W, H, zbuf_out ? ws.zbuf.as<float>() : nullptr, tau3, dpart3, tau2, dp2, c->stream,
                c->launches, bc.count ? &bc : nullptr, ws.zkey.as<unsigned long long>());
     check_launch("tau");

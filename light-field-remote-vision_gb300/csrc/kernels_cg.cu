@@ -37,6 +37,8 @@ __device__ __forceinline__ unsigned int zero_mask16(uint4 v) {
 }
 
 __global__ void k_hole_rows(int W, int H, const uint8_t *__restrict__ vis, int *__restrict__ row_count) {
+    pdl_wait();
+    pdl_trigger();
     const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (y >= H) return;
     int c = 0;
@@ -58,6 +60,8 @@ __global__ void k_hole_rows(int W, int H, const uint8_t *__restrict__ vis, int *
 
 // Exclusive scan of H row counts in one block of 1024 threads (chunks of 1024 rows).
 __global__ void k_hole_scan(int H, int *__restrict__ row_count, int *__restrict__ total) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ int warp_tot[32];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
@@ -95,6 +99,7 @@ __global__ void k_hole_scan(int H, int *__restrict__ row_count, int *__restrict_
 
 __global__ void k_hole_write(int W, int H, const uint8_t *__restrict__ vis, const int *__restrict__ row_start,
                              int *__restrict__ holes) {
+    pdl_wait();
     const int y = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
     if (y >= H) return;
     int k = row_start[y];
@@ -1370,7 +1375,8 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
 }
 
 // Hole filling with the whole iteration loop in one launch (hole_filling, sources/gradientIBR.cu:87-152).
-// count: device pointer to the number of holes. A holds the initial image (and the result); B is a copy.
+// count: device pointer to the number of holes. A holds the initial image (and the result); B is scratch, into
+// which the kernel first copies every hole's value and its neighbours' (the pixels the iterations read).
 // state: [0] iterations.
 // Only as many blocks as the hole count needs take part (kHoleFillPerBlock holes each; the others return at
 // once), so the grid barrier of each iteration spans few blocks, and none is needed when one block suffices. The energy partials alternate between two
@@ -1390,6 +1396,25 @@ __global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W,
     if ((int)blockIdx.x >= active) return;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = active * blockDim.x;
     unsigned int gen = 0;
+    // B = A at the holes and their neighbours; every copy of one pixel writes the same value
+    for (int h = tid; h < nh; h += nthr) {
+        const int o = __ldg(holes + h);
+        const int ox = o % W, oy = o / W;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const size_t p = (size_t)c * N + o;
+            B[p] = __ldcg(A + p);
+            if (ox > 0) B[p - 1] = __ldcg(A + p - 1);
+            if (oy > 0) B[p - W] = __ldcg(A + p - W);
+            if (ox < W - 1) B[p + 1] = __ldcg(A + p + 1);
+            if (oy < H - 1) B[p + W] = __ldcg(A + p + W);
+        }
+    }
+    if (active > 1) {
+        if (!grid_sync(gb, gen, active)) return;
+    } else {
+        __syncthreads();
+    }
     float *src = A, *dst = B;
     float energy = 0.0f, previous = 0.0f;
     int k;
@@ -1454,9 +1479,11 @@ void launch_hole_list(int W, int H, const uint8_t *vis, int *holes, int *count, 
     // row starts are kept in holes[N .. N + H) scratch supplied by the caller (holes has N + H entries)
     int *row = holes + (size_t)W * H;
     const int rows_per_block = 256 / 32;
-    k_hole_rows<<<(H + rows_per_block - 1) / rows_per_block, 256, 0, st>>>(W, H, vis, row);
-    k_hole_scan<<<1, 1024, 0, st>>>(H, row, count);
-    k_hole_write<<<(H + rows_per_block - 1) / rows_per_block, 256, 0, st>>>(W, H, vis, row, holes);
+    // programmatic launches: each kernel's launch overlaps the tail of the one before it
+    const dim3 rows_grid((H + rows_per_block - 1) / rows_per_block);
+    launch_pdl(k_hole_rows, rows_grid, dim3(256), 0, st, W, H, vis, row);
+    launch_pdl(k_hole_scan, dim3(1), dim3(1024), 0, st, H, row, count);
+    launch_pdl(k_hole_write, rows_grid, dim3(256), 0, st, W, H, vis, row, holes);
     lc.add(3);
 }
 

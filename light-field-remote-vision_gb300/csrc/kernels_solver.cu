@@ -68,6 +68,8 @@ __device__ __forceinline__ bool bucket_dup(const unsigned int *start, const unsi
 __global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
                               const unsigned int *__restrict__ start, unsigned int *__restrict__ cursor,
                               const unsigned long long *__restrict__ mask, unsigned int *__restrict__ entries) {
+    pdl_wait();
+    pdl_trigger();
     const int v = blockIdx.y;
     const int m0 = blockIdx.x * blockDim.x * kBucketPer + threadIdx.x;
     const float *tv = tau + (size_t)v * 2 * n;
@@ -118,6 +120,7 @@ __device__ __forceinline__ void insertion_sort(unsigned int *a, unsigned int s, 
 __global__ void __launch_bounds__(kSortBuckets) k_bucket_sort(int nb, const unsigned int *__restrict__ start,
                                                               const unsigned long long *__restrict__ mask,
                                                               unsigned int *__restrict__ entries) {
+    pdl_wait();
     __shared__ unsigned int buf[kSortCap];
     const int b0 = blockIdx.x * kSortBuckets, b1 = min(b0 + kSortBuckets, nb), b = b0 + (int)threadIdx.x;
     // with a view mask only the buckets with two entries of one view need the sort: each sorts itself in place
@@ -146,6 +149,8 @@ constexpr int kScanBlock = 1024, kScanPer = 4, kScanSpan = kScanBlock * kScanPer
 __global__ void __launch_bounds__(kScanBlock) k_scan_blocks(int nb, const unsigned int *__restrict__ in,
                                                             unsigned int *__restrict__ out,
                                                             unsigned int *__restrict__ block_sums) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ unsigned int warp_tot[kScanBlock / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int i0 = blockIdx.x * kScanSpan + threadIdx.x * kScanPer;
@@ -183,8 +188,12 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_blocks(int nb, const unsign
 }
 
 // Adds to block b's exclusive scan the sum of the totals of blocks 0 .. b - 1; out[nb] = the grand total.
+// zero (optional): the scanned counts, cleared here for their next use as cursors (k_scan_blocks has read them)
 __global__ void __launch_bounds__(kScanBlock) k_scan_finish(int nb, unsigned int *__restrict__ out,
-                                                            const unsigned int *__restrict__ block_sums) {
+                                                            const unsigned int *__restrict__ block_sums,
+                                                            unsigned int *__restrict__ zero) {
+    pdl_wait();
+    pdl_trigger();
     __shared__ unsigned int red[kScanBlock / 32];
     unsigned int s = 0;
     for (int j = threadIdx.x; j < (int)blockIdx.x; j += kScanBlock) s += block_sums[j];
@@ -203,7 +212,10 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_finish(int nb, unsigned int
     const int i0 = blockIdx.x * kScanSpan + threadIdx.x * kScanPer;
 #pragma unroll
     for (int j = 0; j < kScanPer; ++j)
-        if (i0 + j < nb) out[i0 + j] += off;
+        if (i0 + j < nb) {
+            out[i0 + j] += off;
+            if (zero) zero[i0 + j] = 0u;
+        }
     if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[nb] = off + block_sums[blockIdx.x];
 }
 
@@ -516,6 +528,7 @@ __global__ void __launch_bounds__(kGrWarps * 32, 2) k_gradient_setup_rows(int W,
     constexpr int TY = kGrWarps * 2 - (KS - 1);  // output pixel rows per block
     constexpr int NA = 7;                        // accumulated fields
     extern __shared__ float gr_part[];           // [TY][KS][kGrNF][kGrTXO]: (pixel row, tap row, field, pixel)
+    pdl_trigger();                               // the hole list, launched next, waits for this grid's completion
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int x0 = blockIdx.x * kGrTXO, y0 = blockIdx.y * TY;
     const int BH = H + KS - 1;
@@ -1173,13 +1186,15 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
     // exclusive scan of the counts: block-local scans, then every block adds the sum of the block totals before
     // it (integer sums, so the result does not depend on the order) and the last block writes the total
     const int nblk = (B.nb + kScanSpan - 1) / kScanSpan;
-    k_scan_blocks<<<nblk, kScanBlock, 0, st>>>(B.nb, B.count, B.start, B.block_sums);
-    k_scan_finish<<<nblk, kScanBlock, 0, st>>>(B.nb, B.start, B.block_sums);
+    // programmatic launches: each kernel's launch overlaps the tail of the one before it; k_scan_finish clears
+    // the counts for their use as k_bucket_fill's cursors
+    launch_pdl(k_scan_blocks, dim3(nblk), dim3(kScanBlock), 0, st, B.nb, B.count, B.start, B.block_sums);
+    launch_pdl(k_scan_finish, dim3(nblk), dim3(kScanBlock), 0, st, B.nb, B.start, B.block_sums, B.count);
     lc.add(2);
-    cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
-    k_bucket_fill<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.start, B.count, B.mask, B.entries);
-    k_bucket_sort<<<(B.nb + kSortBuckets - 1) / kSortBuckets, kSortBuckets, 0, st>>>(B.nb, B.start, B.mask,
-                                                                                      B.entries);
+    launch_pdl(k_bucket_fill, gs, b1, 0, st, G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.start, B.count, B.mask,
+               B.entries);
+    launch_pdl(k_bucket_sort, dim3((B.nb + kSortBuckets - 1) / kSortBuckets), dim3(kSortBuckets), 0, st, B.nb,
+               B.start, B.mask, B.entries);
     lc.add(2);
     (void)ks;
 }

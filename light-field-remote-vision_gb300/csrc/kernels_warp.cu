@@ -291,6 +291,7 @@ constexpr int kZsplatPerThread = 2;
 __global__ void __launch_bounds__(256, 4) k_zsplat(int V, int w, int h, const float *__restrict__ depth,
                                                 const WarpCams cams, int W, int H,
                                                 unsigned long long *__restrict__ zkey) {
+    pdl_trigger();  // k_tau, launched next, waits for this grid's completion
     const int m0 = blockIdx.x * blockDim.x * kZsplatPerThread + threadIdx.x, m1 = m0 + blockDim.x;
     const int v = blockIdx.y;
     const int n = w * h;
@@ -391,6 +392,8 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
                                              float *__restrict__ dpart3, float *__restrict__ tau2,
                                              float *__restrict__ dp2, BucketCount bc,
                                              const unsigned long long *__restrict__ zkey) {
+    pdl_wait();
+    pdl_trigger();
     const int v = blockIdx.y;
     const int n = w * h;
     const int m0 = blockIdx.x * blockDim.x * kTauPer + threadIdx.x;
@@ -636,8 +639,9 @@ void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, i
     ProfScope _ps(lc, "tau", st);
     const int n = w * h;
     const BucketCount count = bc ? *bc : BucketCount{};
-    k_tau<<<dim3((n + 256 * kTauPer - 1) / (256 * kTauPer), V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zbuf, tau3,
-                                                                               dpart3, tau2, dp2, count, zkey);
+    // programmatic launch: its launch overlaps the tail of the z-buffer kernel before it
+    launch_pdl(k_tau, dim3((n + 256 * kTauPer - 1) / (256 * kTauPer), V), dim3(256), 0, st, V, w, h, depth, cams, W,
+               H, zbuf, tau3, dpart3, tau2, dp2, count, zkey);
     lc.add(1);
 }
 
