@@ -255,11 +255,22 @@ __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc,
     return true;
 }
 
+// Column x and row y of pixel m of a w-wide view of n pixels, rw = RN(1/w). For n <= 2^21 the row is the float
+// quotient (m + 1/2) rw truncated: its rounding error, below (m + 1/2) / w * 2^-23, is smaller than the distance
+// 1/(2w) from (m + 1/2) / w to the nearest integer, so it equals the integer quotient, without the integer
+// division's instruction sequence.
+__device__ __forceinline__ void pixel_of(int m, int w, int n, float rw, int &x, int &y) {
+    y = n <= (1 << 21) ? (int)(((float)m + 0.5f) * rw) : m / w;
+    x = m - y * w;
+}
+
 // One input pixel m of view cam c: its tilted quad into the depth buffer.
-__device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int m, int w, float z, float zx, float zy, int W,
-                                             int H, unsigned long long *zkey) {
+__device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int m, int w, int n, float rw, float z, float zx,
+                                             float zy, int W, int H, unsigned long long *zkey) {
     if (z >= 1000.0f * 0.5f) return;  // INVALID_DEPTH / 2 (depthSplatting.geom:21)
-    const float cx = (m % w) + 0.5f, cy = (m / w) + 0.5f;
+    int px, py;
+    pixel_of(m, w, n, rw, px, py);
+    const float cx = px + 0.5f, cy = py + 0.5f;
     // x_h is linear in the pixel-space point scaled by its depth: with q = M (cx, cy, 1), the centre maps to
     // z q + b and the corner (cx + dx, cy + dy) at depth z + dx zx + dy zy to (z + dx zx + dy zy)(q + dx M_0 +
     // dy M_1) + b, M_0 and M_1 the first two columns of M
@@ -301,8 +312,9 @@ __global__ void __launch_bounds__(256, 4) k_zsplat(int V, int w, int h, const fl
     float z1 = 0.f, zx1 = 0.f, zy1 = 0.f;
     if (m1 < n) z1 = dz[m1], zx1 = dz[n + m1], zy1 = dz[2 * n + m1];
     const ViewCam c = view_cam(cams, v);
-    zsplat_pixel(c, m0, w, z0, zx0, zy0, W, H, zkey);
-    if (m1 < n) zsplat_pixel(c, m1, w, z1, zx1, zy1, W, H, zkey);
+    const float rw = __frcp_rn((float)w);
+    zsplat_pixel(c, m0, w, n, rw, z0, zx0, zy0, W, H, zkey);
+    if (m1 < n) zsplat_pixel(c, m1, w, n, rw, z1, zx1, zy1, W, H, zkey);
 }
 
 // The target depth a z-buffer key holds (its centre depth; 0 where nothing was splatted).
@@ -354,10 +366,13 @@ struct TauPix {
     float z, xu, yu, zt, deform, rx, ry;  // zt: the point's depth in the target camera
 };
 
-__device__ __forceinline__ TauPix tau_project(const ViewCam &c, int m, int w, float z, float zx, float zy) {
+__device__ __forceinline__ TauPix tau_project(const ViewCam &c, int m, int w, int n, float rw, float z, float zx,
+                                              float zy) {
     TauPix p;
     p.z = z;
-    const float x = (m % w) + 0.5f, y = (m / w) + 0.5f;
+    int px, py;
+    pixel_of(m, w, n, rw, px, py);
+    const float x = px + 0.5f, y = py + 0.5f;
     // with mk = M (x, y, 1): x_h = z mk + b, and the Jacobian's columns M (x zx + z, y zx, zx) = zx mk + z M_0
     // and M (x zy, y zy + z, zy) = zy mk + z M_1 (M_0, M_1 the first two columns of M)
     float mk[3], xuh[3], m0[3], m1[3];
@@ -400,12 +415,13 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
     if (m0 >= n) return;
     const float *dz = depth + (size_t)v * 3 * n;
     const ViewCam c = view_cam(cams, v);
+    const float rw = __frcp_rn((float)w);
     TauPix px[kTauPer];
     float zs[kTauPer];
 #pragma unroll
     for (int j = 0; j < kTauPer; ++j) {
         const int m = min(m0 + j * (int)blockDim.x, n - 1);
-        px[j] = tau_project(c, m, w, dz[m], dz[n + m], dz[2 * n + m]);
+        px[j] = tau_project(c, m, w, n, rw, dz[m], dz[n + m], dz[2 * n + m]);
     }
     // the target depth map at every projection (clamped, so every sample is in bounds; out-of-range points
     // do not use it)
