@@ -176,6 +176,15 @@ __device__ __forceinline__ bool in_splat(float tx, float ty, int W, int H) {
     return !(px < 0 || py < 0 || px > W - 1 || py > H - 1);
 }
 
+// Column x and row y of pixel m of a w-wide view of n pixels, rw = RN(1/w). For n <= 2^21 the row is the float
+// quotient (m + 1/2) rw truncated: its rounding error, below (m + 1/2) / w * 2^-23, is smaller than the distance
+// 1/(2w) from (m + 1/2) / w to the nearest integer, so it equals the integer quotient, without the integer
+// division's instruction sequence.
+__device__ __forceinline__ void pixel_of(int m, int w, int n, float rw, int &x, int &y) {
+    y = n <= (1 << 21) ? (int)(((float)m + 0.5f) * rw) : m / w;
+    x = m - y * w;
+}
+
 // Inverse-map bucket of a source pixel with warp (tx, ty): its footprint anchor offset by ks - 1 on a grid of
 // BW columns (-1: the pixel is not splatted).
 __device__ __forceinline__ long long bucket_of(float tx, float ty, int W, int H, int dsf, int BW) {

@@ -282,7 +282,8 @@ __global__ void __launch_bounds__(256, GATHER ? 1 : 8) k_weights(int V, int n, i
     const float *tx = tau + (size_t)v * 2 * n, *ty = tx + n;
     // every load the pixel can need, issued together (neighbour indices clamped to the view; the clamped values
     // are read only where the neighbour exists)
-    const int mx = m % w, my = m / w;
+    int mx, my;
+    pixel_of(m, w, n, __frcp_rn((float)w), mx, my);
     const int ml = mx > 0 ? m - 1 : m, mr = mx < w - 1 ? m + 1 : m;
     const int mu = my > 0 ? m - w : m, md = my < h - 1 ? m + w : m;
     const float txm = __ldg(tx + m), tym = __ldg(ty + m);
@@ -1352,7 +1353,8 @@ __global__ void __launch_bounds__(256) k_residual_grad(int V, int w, int h, int 
             }
     }
     const float dsf2 = (float)(dsf * dsf);
-    const int mx = m % w, my = m / w;
+    int mx, my;
+    pixel_of(m, w, n, __frcp_rn((float)w), mx, my);
     const float *iv = img + (size_t)v * 3 * n;
     float *rv = resg + (size_t)v * 3 * n;
 #pragma unroll

@@ -255,15 +255,6 @@ __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc,
     return true;
 }
 
-// Column x and row y of pixel m of a w-wide view of n pixels, rw = RN(1/w). For n <= 2^21 the row is the float
-// quotient (m + 1/2) rw truncated: its rounding error, below (m + 1/2) / w * 2^-23, is smaller than the distance
-// 1/(2w) from (m + 1/2) / w to the nearest integer, so it equals the integer quotient, without the integer
-// division's instruction sequence.
-__device__ __forceinline__ void pixel_of(int m, int w, int n, float rw, int &x, int &y) {
-    y = n <= (1 << 21) ? (int)(((float)m + 0.5f) * rw) : m / w;
-    x = m - y * w;
-}
-
 // One input pixel m of view cam c: its tilted quad into the depth buffer.
 __device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int m, int w, int n, float rw, float z, float zx,
                                              float zy, int W, int H, unsigned long long *zkey) {
