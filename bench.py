@@ -97,7 +97,7 @@ def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: in
 
 
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu --set full capture of the
-# C2 step; the captures and their commands are summarised in profiles/*_c2.md.
+# C2 step (5x5 light field of 512^2 views -> the 1024^2 target).
 NCU_TRAFFIC_BYTES = {
     "zbuffer_splat": 83.937536e6 + 2.530560e6,
     "gradient_setup": 224.049664e6 + 18.143744e6,

@@ -111,6 +111,16 @@ typedef struct lfrv_stats {
     double gap;                  /* last certified relative gap (CG), else 0 */
     double seconds;              /* device time of the solve (CUDA events) */
     int    kernel_launches;      /* kernels this library launched for the call */
+    /* Optional energy trace (the reference prints the energy of every FISTA iteration,
+     * sources/super-resolution.cpp:221-260). The caller sets energy_trace to a host buffer of trace_capacity
+     * doubles (or NULL / 0 for none) before the call; the solver writes one entry per outer iteration, in order:
+     * IBR_color: the energy of coco_vtv_sr_primal_energy_unstructured (sources/optimization.cu:1477-1717) after
+     * each FISTA iteration, across meta iterations; IBR_gradient: the quadratic energy
+     * 1/2 ||u - u0||^2 + 1/2 ||grad u - g||^2 after each CG iteration (FP64). trace_length receives the number of
+     * entries written (at most trace_capacity). Zero-initialise the struct: the library reads these two fields. */
+    double *energy_trace;
+    int    trace_capacity;
+    int    trace_length;
 } lfrv_stats;
 
 /* ---------------------------------------------------------------- contexts */
@@ -354,8 +364,12 @@ int lfrv_stage_cg(lfrv_ctx *ctx, int W, int H, int faithful, int max_iter, doubl
  * 9.5 MB per device, for W * H <= LFRV_CG_STATIC_MAX_PIXELS. No call allocates or frees device memory,
  * and none creates a context or a stream: this is the entry point for callers that cannot allocate.
  * - Larger images are rejected with LFRV_E_ARG, before any device work.
- * - First call on a device: it looks up the array's address with that device current. Later calls
- *   reuse the cached address. This setup must happen before any stream capture that includes the call.
+ * - First call on a device (per driver context of that device): it looks up the array's address with the
+ *   device current, and later calls reuse it. Under lazy module loading (CUDA's default since 12.2) that first
+ *   lookup also loads the library's device code and so reserves the array's memory on the device: make one call
+ *   (any valid size) during start-up, outside the section that must not allocate and before any stream capture
+ *   that includes the call. Setting CUDA_MODULE_LOADING=EAGER loads it when the context is created instead.
+ *   After cudaDeviceReset, or under another context of the same device, the address is looked up again.
  * - The barrier words are cleared on `stream` before each launch. Nothing else needs to start at zero.
  * - There is one array per device. Calls that overlap on the same device race on it, even from different
  *   streams or threads. Order such calls, for example on one stream.

@@ -106,12 +106,15 @@ def build_oracle(force: bool = False, verbose: bool = False) -> Path:
 
 
 def build_reference_kernels(verbose: bool = False) -> Path | None:
-    """Builds oracle/_ref from the read-only reference tree when it is present on this machine."""
+    """Builds oracle/_ref from the reference tree when the recipe finds one (oracle/build_ref.sh --probe prints
+    its location; LFRV_REFERENCE_ROOT overrides the recipe's default)."""
     script = ROOT / "oracle" / "build_ref.sh"
-    ref_root = Path(os.environ.get("LFRV_REFERENCE_ROOT", "/root/reference"))
-    if not script.exists() or not ref_root.exists():
+    if not script.exists():
         return None
-    _run(["bash", str(script), str(ref_root)], verbose)
+    probe = subprocess.run(["bash", str(script), "--probe"], capture_output=True, text=True)
+    if probe.returncode != 0:
+        return None  # no reference tree on this machine
+    _run(["bash", str(script)], verbose)
     out = ROOT / "oracle" / "_ref" / "libref_kernels.so"
     return out if out.exists() else None
 

@@ -47,8 +47,8 @@ struct Workspace {
     DevBuf learn_in, seed;
     // CG
     DevBuf r, d, q, U0, holes, hole_count;
-    // reductions and persistent-solver state
-    DevBuf partial, sums, state, barrier;
+    // reductions and persistent-solver state; per-iteration energies of the current call (energy trace)
+    DevBuf partial, sums, state, barrier, trace;
     // push-pull pyramid
     DevBuf pp_img, pp_vis, pp_tmp, pp_orig;
     // host staging for the host-buffer entry points
@@ -82,6 +82,12 @@ struct Pending {
     bool barrier = false;  // a persistent kernel used the grid barrier since the last check (error word armed)
     lfrv_stats *stats = nullptr;
     double gap_tol = 0.0;
+    // energy trace requested by the caller: entries kept in ws.trace on the device, copied to trace_host once the
+    // stream has completed. trace_len >= 0 is the entry count known on the host; -1 takes the CG's iteration
+    // count from the device state
+    double *trace_host = nullptr;
+    int trace_cap = 0;
+    int trace_len = -1;
 };
 
 // Bumped by every workspace allocation and release: a captured graph holds workspace pointers and is replayed

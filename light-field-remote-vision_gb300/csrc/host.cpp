@@ -143,6 +143,26 @@ static void check_launch(const char *what) {
 
 static void sync(lfrv_ctx *c) { LFRV_CUDA(cudaStreamSynchronize(c->stream)); }
 
+// Clears a caller's statistics, keeping its energy-trace request (buffer and capacity).
+static void reset_stats(lfrv_stats *st) {
+    if (!st) return;
+    double *buf = st->energy_trace;
+    const int cap = st->trace_capacity;
+    std::memset(st, 0, sizeof(*st));
+    st->energy_trace = buf;
+    st->trace_capacity = cap;
+}
+
+// The caller's energy-trace request of this call: the device buffer (ws.trace) for its entries, or nullptr.
+static double *trace_request(lfrv_ctx *c, lfrv_stats *st) {
+    if (!st || !st->energy_trace || st->trace_capacity <= 0) return nullptr;
+    c->ws.trace.ensure(sizeof(double) * (size_t)st->trace_capacity);
+    c->pending.trace_host = st->energy_trace;
+    c->pending.trace_cap = st->trace_capacity;
+    c->pending.trace_len = -1;
+    return c->ws.trace.as<double>();
+}
+
 // ------------------------------------------------------------------ geometry and validation
 static Geometry geometry(const lfrv_config &cfg) {
     if (cfg.nchannels != 3) raise(LFRV_E_ARG, "nchannels must be 3 (sources/config.cpp:116), got %d", cfg.nchannels);
@@ -493,12 +513,22 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
     const float EPS = 1e-4f, MAX_DIFF = 1e-3f, PERCENT_MOVING = 0.01f;
     const int mp = moving_partials(N);
 
-    auto energy = [&](bool need_tv) -> float {
+    // energy trace: one entry per FISTA iteration, written on the device (no host read per iteration)
+    double *trace = trace_request(c, st);
+    const int trace_cap = trace ? st->trace_capacity : 0;
+    auto energy = [&](bool need_tv, int trace_slot = -1) -> float {
         // residual pass (also the data term input of the next iteration) + TV term of the reference energy
         residual(c, G, ws.U.as<float>(), img, tau2, b.wgt, s2, b.res, 1);
-        if (!need_tv) return 0.0f;
+        const bool want_trace = trace_slot >= 0 && trace_slot < trace_cap;
+        if (!need_tv && !want_trace) return 0.0f;
         sobel_target(c, G, ws.U.as<float>(), b.Xq, b.Xq + N, b.vis, 0);
         if (gtb.on) energy_gradients(c, cfg, G, gtb, ws.U.as<float>(), tau2, b.wgt, 3);
+        if (want_trace) {
+            launch_trace_energy(ws.sums.as<double>(), cfg.lambda, cfg.dt_alpha, cfg.dt_beta, gtb.on,
+                                trace + trace_slot, s, c->launches);
+            check_launch("trace energy");
+        }
+        if (!need_tv) return 0.0f;
         double sums[4] = {0, 0, 0, 0};
         read_sums(c, sums, gtb.on ? 4 : 2);
         const float e_tv = (float)sums[0], e_int = (float)sums[1], e_grad = (float)sums[3];
@@ -550,7 +580,7 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
             if (Ucur == ws.Ua.as<float>()) swap_buf(ws.U, ws.Ua);
             else if (Ucur == ws.Ub.as<float>()) swap_buf(ws.U, ws.Ub);
             ++total_k;
-            E = energy(track);
+            E = energy(track, total_k - 1);
             if (!track) continue;
             if (E < EPS) {
                 reason = 1;
@@ -585,6 +615,7 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         LFRV_CUDA(cudaMemcpyAsync(b.Uprev_meta, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
     }
     LFRV_CUDA(cudaMemcpyAsync(out, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    if (trace) c->pending.trace_len = std::min(total_k, trace_cap);
     if (st) {
         st->outer_iterations = total_k;
         st->meta_iterations = std::min(r + 1, cfg.nmeta_iter);
@@ -662,7 +693,8 @@ static void u_gradient(lfrv_ctx *c, const Geometry &G, const Buckets &B, const f
 
 // possion_conj_grad with the reference's loop (faithful, defect D1): 5 iterations, host-side scalars as the
 // reference computes them (sources/solver.cu:612-676).
-static int cg_faithful(lfrv_ctx *c, int W, int H, const float *gx, const float *gy, float *U) {
+static int cg_faithful(lfrv_ctx *c, int W, int H, const float *gx, const float *gy, float *U,
+                       double *trace = nullptr) {
     Workspace &ws = c->ws;
     const size_t N = (size_t)W * H;
     cudaStream_t s = c->stream;
@@ -672,6 +704,12 @@ static int cg_faithful(lfrv_ctx *c, int W, int H, const float *gx, const float *
     float *r = ws.r.as<float>(), *d = ws.d.as<float>(), *q = ws.q.as<float>();
     const int np = cg_partials(W, H);
     double *part = partial_buf(c, 3 * (size_t)np);
+    // energy trace: the quadratic energy of each iterate against the starting image u0
+    const int trace_cap = trace ? c->pending.trace_cap : 0;
+    if (trace) {
+        ws.U0.ensure(3 * N * sizeof(float));
+        LFRV_CUDA(cudaMemcpyAsync(ws.U0.p, U, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    }
     ws.sums.ensure(sizeof(double) * 64);
     double *sums = ws.sums.as<double>();
     auto reduce3 = [&](double out[3]) {
@@ -704,13 +742,19 @@ static int cg_faithful(lfrv_ctx *c, int W, int H, const float *gx, const float *
         for (int ch = 0; ch < 3; ++ch) dAlpha[ch] = (double)alpha[ch] + rr[ch];
         launch_cg_dir(W, H, beta, r, d, s, c->launches);
         check_launch("cg dir");
+        if (it < trace_cap) {
+            launch_cg_energy(W, H, U, ws.U0.as<float>(), gx, gy, part, s, c->launches);
+            launch_reduce_final(np, part, trace + it, s, c->launches);
+            check_launch("cg energy trace");
+        }
     }
     return it;
 }
 
 // Corrected CG: one persistent launch (FP32 iterates, FP64 dot products, certified-gap stop on the device).
 static void cg_persistent_async(lfrv_ctx *c, int W, int H, int max_iter, double gap_tol, const float *gx,
-                                const float *gy, float *U, const float *U0 = nullptr) {
+                                const float *gy, float *U, const float *U0 = nullptr, double *trace = nullptr,
+                                int trace_cap = 0) {
     Workspace &ws = c->ws;
     const size_t N = (size_t)W * H;
     ws.r.ensure(3 * N * sizeof(float));
@@ -721,7 +765,7 @@ static void cg_persistent_async(lfrv_ctx *c, int W, int H, int max_iter, double 
     const GridBarrier gb = fresh_barrier(c);
     LFRV_CUDA(launch_cg_persistent(W, H, gx, gy, U, ws.r.as<float>(), ws.d.as<float>(), ws.q.as<float>(), part,
                                    part + 4 * np, gb, max_iter, gap_tol, solver_state(c), c->stream, c->launches,
-                                   U0));
+                                   U0, trace, trace_cap));
     c->pending.cg = true;
 }
 
@@ -788,10 +832,16 @@ static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img
     ColorBuffers b = color_buffers(c, G);
     float *U = ws.U.as<float>();
     c->pending = Pending{};
+    double *trace = trace_request(c, st);
     gradient_prepare(c, cfg, G, img, tau2, dp2, init, U, b.gx, b.gy, nullptr, views_ready, vg_early);
     int it_faithful = 0;
-    if (cfg.faithful) it_faithful = cg_faithful(c, G.W, G.H, b.gx, b.gy, U);
-    else cg_persistent_async(c, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U);
+    if (cfg.faithful) {
+        it_faithful = cg_faithful(c, G.W, G.H, b.gx, b.gy, U, trace);
+        if (trace) c->pending.trace_len = std::min(it_faithful, st->trace_capacity);
+    } else {
+        cg_persistent_async(c, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U, nullptr, trace,
+                            trace ? st->trace_capacity : 0);
+    }
     LFRV_CUDA(cudaMemcpyAsync(out, U, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
     c->pending.stats = st;
     c->pending.gap_tol = cfg.cg_gap_tol;
@@ -806,7 +856,7 @@ static void gradient_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img
 // After the stream has completed: solver statistics kept on the device, and the barrier status.
 void finish_stats(lfrv_ctx *c) {
     Pending &p = c->pending;
-    if (!p.cg && !p.hole_fill && !p.barrier) return;
+    if (!p.cg && !p.hole_fill && !p.barrier && !p.trace_host) return;
     double state[16];
     int bar[8] = {0, 0, 0, 0, 0, 0, 0, 0};
     if (p.cg || p.hole_fill) LFRV_CUDA(cudaMemcpy(state, c->ws.state.p, sizeof(state), cudaMemcpyDeviceToHost));
@@ -820,6 +870,13 @@ void finish_stats(lfrv_ctx *c) {
             p.stats->energy = state[3];
             p.stats->stop_reason = (p.gap_tol > 0 && state[4] <= p.gap_tol) ? 4 : 0;
         }
+    }
+    if (p.trace_host) {
+        int len = p.trace_len >= 0 ? p.trace_len : (p.cg ? (int)state[5] : 0);
+        len = std::max(0, std::min(len, p.trace_cap));
+        if (len > 0)
+            LFRV_CUDA(cudaMemcpy(p.trace_host, c->ws.trace.p, sizeof(double) * len, cudaMemcpyDeviceToHost));
+        if (p.stats) p.stats->trace_length = len;
     }
     p = Pending{};
     if (timeout) raise(LFRV_E_TIMEOUT, "a device-side grid barrier gave up waiting (persistent solver)");
@@ -1264,7 +1321,7 @@ static int solve_dev(lfrv_ctx *ctx, const lfrv_config *cfg, bool color, const fl
     LFRV_API_BEGIN
     CTX_CHECK(ctx);
     if (!cfg || !d_views || !d_tau || !d_out) return fail(LFRV_E_ARG, "null argument");
-    if (stats) std::memset(stats, 0, sizeof(*stats));
+    reset_stats(stats);
     const Geometry G = geometry(*cfg);
     const long long l0 = ctx->launches.n;
     begin_timing(ctx);
@@ -1359,7 +1416,7 @@ static void render_view_body(lfrv_ctx *ctx, const lfrv_config &cfg, int algorith
 static void render_view_impl(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const float *d_views,
                              const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target, float *d_out,
                              lfrv_stats *stats, const UploadPlan *plan, float *host_out) {
-    if (stats) std::memset(stats, 0, sizeof(*stats));
+    reset_stats(stats);
     const Geometry G = geometry(cfg);
     if (target->width != G.W || target->height != G.H) raise(LFRV_E_ARG, "target size mismatch");
     const long long l0 = ctx->launches.n;
@@ -1420,7 +1477,7 @@ static bool render_graph(lfrv_ctx *ctx, std::vector<unsigned char> key, lfrv_sta
         g.launches = ctx->launches.n - l0;
         ctx->launches.n = l0;
     }
-    if (stats) std::memset(stats, 0, sizeof(*stats));
+    reset_stats(stats);
     const long long l0 = ctx->launches.n;
     begin_timing(ctx);
     LFRV_CUDA(cudaGraphLaunch(g.exec, ctx->stream));
@@ -1451,8 +1508,10 @@ static std::vector<unsigned char> render_key(lfrv_ctx *ctx, const lfrv_config &c
     return key;
 }
 
-static bool graph_eligible(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const lfrv_camera *target) {
+static bool graph_eligible(lfrv_ctx *ctx, const lfrv_config &cfg, int algorithm, const lfrv_camera *target,
+                           const lfrv_stats *stats) {
     if (algorithm != 1 || cfg.faithful || ctx->launches.prof) return false;
+    if (stats && stats->energy_trace && stats->trace_capacity > 0) return false;  // traced calls run uncaptured
     const Geometry G = geometry(cfg);
     return target->width == G.W && target->height == G.H;
 }
@@ -1464,7 +1523,7 @@ extern "C" int lfrv_render_view_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int a
     CTX_CHECK(ctx);
     if (!cfg || !d_views || !d_depth || !cams || !target || !d_out) return fail(LFRV_E_ARG, "null argument");
     const bool replayed =
-        graph_eligible(ctx, *cfg, algorithm, target) &&
+        graph_eligible(ctx, *cfg, algorithm, target, stats) &&
         render_graph(ctx, render_key(ctx, *cfg, algorithm, d_views, d_depth, d_out, cams, target), stats, [&] {
             render_view_body(ctx, *cfg, algorithm, d_views, d_depth, cams, target, d_out, nullptr, nullptr, nullptr);
         });
@@ -1497,7 +1556,7 @@ static Geometry warm_geometry(const lfrv_config &cfg, const lfrv_camera *target)
 static void warm_features(lfrv_ctx *ctx, const lfrv_config &cfg, const float *d_views, const float *d_depth,
                           const lfrv_camera *cams, const lfrv_camera *target, void *d_input, float *d_u0,
                           float *d_solution, lfrv_stats *stats) {
-    if (stats) std::memset(stats, 0, sizeof(*stats));
+    reset_stats(stats);
     const Geometry G = warm_geometry(cfg, target);
     const long long l0 = ctx->launches.n;
     begin_timing(ctx);
@@ -1523,7 +1582,7 @@ static void warm_features(lfrv_ctx *ctx, const lfrv_config &cfg, const float *d_
 static void render_view_warm(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_config &cfg, const float *d_views,
                              const float *d_depth, const lfrv_camera *cams, const lfrv_camera *target, float *d_out,
                              lfrv_stats *stats) {
-    if (stats) std::memset(stats, 0, sizeof(*stats));
+    reset_stats(stats);
     const Geometry G = warm_geometry(cfg, target);
     const long long l0 = ctx->launches.n;
     begin_timing(ctx);
@@ -1591,7 +1650,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
             raise(LFRV_E_ARG, "job %d: null argument", j);
         const Geometry G = geometry(*J.cfg);
         if (J.target->width != G.W || J.target->height != G.H) raise(LFRV_E_ARG, "job %d: target size mismatch", j);
-        if (J.stats) std::memset(J.stats, 0, sizeof(*J.stats));
+        reset_stats(J.stats);
         if (J.algorithm == 1 && !J.cfg->faithful) {
             check_solver_options(*J.cfg);
             if (G.W < 2 || G.H < 2) raise(LFRV_E_ARG, "job %d: target smaller than 2 x 2", j);
@@ -1678,6 +1737,15 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
             float *U = base + sl.off;
             warmstart_predict_async(net, sl.G.H, sl.G.W, U + 17 * sl.G.N + 16, U, U + 14 * sl.G.N + 16);
         }
+    // energy traces of the batched jobs: one region of ws.trace per job that asks for one
+    std::vector<size_t> trace_off(batched.size(), 0);
+    size_t trace_total = 0;
+    for (size_t q = 0; q < batched.size(); ++q) {
+        const lfrv_stats *st = jobs[batched[q].job].stats;
+        trace_off[q] = trace_total;
+        if (st && st->energy_trace && st->trace_capacity > 0) trace_total += (size_t)st->trace_capacity;
+    }
+    if (trace_total) ws.trace.ensure(sizeof(double) * trace_total);
     // the CG of all gradient jobs, in launches of at most `resident` jobs
     const int resident = cg_batch_resident_blocks();
     for (size_t first = 0; first < batched.size(); first += (size_t)resident) {
@@ -1728,6 +1796,10 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
             P.dB = U + 11 * sl.G.N;
             P.state = reinterpret_cast<double *>(U + 14 * sl.G.N);
             P.U0 = sl.seeded ? U : nullptr;
+            const lfrv_stats *jst = jobs[sl.job].stats;
+            const bool traced = jst && jst->energy_trace && jst->trace_capacity > 0;
+            P.trace = traced ? ws.trace.as<double>() + trace_off[first + q] : nullptr;
+            P.trace_cap = traced ? jst->trace_capacity : 0;
             for (int k = 0; k < nb[q]; ++k) block_prob[b0 + k] = (int)q;
             b0 += nb[q];
         }
@@ -1762,6 +1834,13 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         st->energy = state[3];
         st->hole_fill_iterations = (int)state[6];
         st->stop_reason = (jobs[sl.job].cfg->cg_gap_tol > 0 && state[4] <= jobs[sl.job].cfg->cg_gap_tol) ? 4 : 0;
+        if (st->energy_trace && st->trace_capacity > 0) {
+            const size_t q = (size_t)(&sl - batched.data());
+            st->trace_length = std::min(st->outer_iterations, st->trace_capacity);
+            if (st->trace_length > 0)
+                LFRV_CUDA(cudaMemcpy(st->energy_trace, ws.trace.as<double>() + trace_off[q],
+                                     sizeof(double) * st->trace_length, cudaMemcpyDeviceToHost));
+        }
     }
     finish_stats(c);
 }
@@ -1833,7 +1912,7 @@ extern "C" int lfrv_render_view(lfrv_ctx *ctx, const lfrv_config *cfg, int algor
     // a repeated call (same host buffers and arguments) replays its captured graph: uploads, warp, solve and
     // the download in one launch
     const bool replayed =
-        graph_eligible(ctx, *cfg, algorithm, target) &&
+        graph_eligible(ctx, *cfg, algorithm, target, stats) &&
         render_graph(ctx, render_key(ctx, *cfg, algorithm, views, depth, out, cams, target), stats, [&] {
             upload();
             render_view_body(ctx, *cfg, algorithm, ws.in_views.as<float>(), ws.depth.as<float>(), cams, target,

@@ -134,6 +134,10 @@ int moving_partials(size_t N);
 void set_gaussian(const float k[11]);
 void launch_blur(int W, int H, const float *in, float *tmp, float *out, cudaStream_t st, LaunchCounter &lc);
 void launch_reduce_final(int count, const double *partial, double *out, cudaStream_t st, LaunchCounter &lc);
+// One energy-trace entry of IBR_color: *dst = lambda (float)sums[0] + alpha (float)sums[1] (+ beta (float)sums[3]
+// when grad), evaluated in float as the reference's host sums it (coco_vtv_sr_primal_energy_unstructured).
+void launch_trace_energy(const double *sums, float lambda, float alpha, float beta, bool grad, double *dst,
+                         cudaStream_t st, LaunchCounter &lc);
 void launch_premultiply_dpart(int V, int n, const float *dpart3, int ch, float *dp, cudaStream_t st, LaunchCounter &lc);
 void launch_copy_tau(int V, int n, const float *tau_in, int ch, float *tau, cudaStream_t st, LaunchCounter &lc);
 
@@ -182,6 +186,8 @@ struct CgProblem {
     float *U, *r, *dA, *dB;
     double *state;
     const float *U0;  // anchor when U holds a seed (nullptr: U is the anchor)
+    double *trace;    // energy after each iteration (nullptr: none), at most trace_cap entries
+    int trace_cap;
 };
 // Blocks of a batched launch: as many as can be resident with k_cg_batch's shape.
 int cg_batch_resident_blocks();
@@ -198,7 +204,8 @@ cudaError_t launch_rof_persistent(int W, int H, int niter, float tau, float sigm
                                   cudaStream_t st, LaunchCounter &lc);
 cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
                                  float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
-                                 double *state, cudaStream_t st, LaunchCounter &lc, const float *U0 = nullptr);
+                                 double *state, cudaStream_t st, LaunchCounter &lc, const float *U0 = nullptr,
+                                 double *trace = nullptr, int trace_cap = 0);
 cudaError_t launch_hole_fill_persistent(int W, int H, const int *holes, const int *count, float *A, float *B,
                                         double *part, GridBarrier gb, int max_iter, double *state, cudaStream_t st,
                                         LaunchCounter &lc);

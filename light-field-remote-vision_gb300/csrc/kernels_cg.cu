@@ -533,6 +533,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                                                                    float *dA, float *dB, double *partA,
                                                                    double *partB, GridBarrier gb, int max_iter,
                                                                    double gap_tol, double *state,
+                                                                   double *trace, int trace_cap,
                                                                    const __grid_constant__ CUtensorMap mapR,
                                                                    const __grid_constant__ CUtensorMap mapA,
                                                                    const __grid_constant__ CUtensorMap mapB,
@@ -690,6 +691,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_persistent(int W, int H,
                 s_coef[c] = (float)alpha_d;
                 E -= 0.5 * alpha_d * delta[c];
             }
+            if (blockIdx.x == 0 && trace && it < trace_cap) trace[it] = E;
         }
         __syncthreads();
         const float alpha[3] = {s_coef[0], s_coef[1], s_coef[2]};
@@ -846,7 +848,8 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(int W, int H, co
                                                                 float *__restrict__ bord, double *__restrict__ partA,
                                                                 double *__restrict__ partB, GridBarrier gb,
                                                                 int max_iter, double gap_tol,
-                                                                double *__restrict__ state) {
+                                                                double *__restrict__ state,
+                                                                double *__restrict__ trace, int trace_cap) {
     extern __shared__ __align__(16) float res_smem[];
     __shared__ double sh[4], s_delta[3], s_dE[3];
     __shared__ float s_coef[3];
@@ -1005,7 +1008,10 @@ __global__ void __launch_bounds__(kResThreads, 1) k_cg_resident(int W, int H, co
         }
         __syncthreads();
         const float alpha[3] = {s_coef[0], s_coef[1], s_coef[2]};
-        if (threadIdx.x == 0) E = E - s_dE[0] - s_dE[1] - s_dE[2];
+        if (threadIdx.x == 0) {
+            E = E - s_dE[0] - s_dE[1] - s_dE[2];
+            if (blockIdx.x == 0 && trace && it < trace_cap) trace[it] = E;
+        }
         // ---- phase B: the halo's d from the neighbours' new borders; u += alpha d, r -= alpha A d, r . r;
         // publish r's borders
         load_halo(dnew, -1, 0.f, 0.f, 0.f);
@@ -1174,6 +1180,7 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_batch(const CgProblem *_
                 s_coef[c] = (float)alpha_d;
                 E -= 0.5 * alpha_d * delta[c];
             }
+            if (lb == 0 && P.trace && it < P.trace_cap) P.trace[it] = E;
         }
         __syncthreads();
         const float alpha[3] = {s_coef[0], s_coef[1], s_coef[2]};
@@ -1509,7 +1516,8 @@ int persistent_partials() {
 
 cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
                                  float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
-                                 double *state, cudaStream_t st, LaunchCounter &lc, const float *U0) {
+                                 double *state, cudaStream_t st, LaunchCounter &lc, const float *U0,
+                                 double *trace, int trace_cap) {
     ProfScope _ps(lc, "cg_persistent", st);
     const size_t N = (size_t)W * H;
     const int ntiles = ((W + kTileX - 1) / kTileX) * ((H + kTileY - 1) / kTileY);
@@ -1519,11 +1527,17 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        static std::once_flag once;
-        std::call_once(once, [] {
-            cudaFuncSetAttribute(k_cg_resident, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)(kResMaxTiles * kResTileBytes));
-        });
+        // the attribute is per device: set it the first time each device launches here
+        static std::mutex attr_mu;
+        static bool attr_set[64] = {};
+        if (dev >= 0 && dev < 64) {
+            std::lock_guard<std::mutex> lock(attr_mu);
+            if (!attr_set[dev]) {
+                cudaFuncSetAttribute(k_cg_resident, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(kResMaxTiles * kResTileBytes));
+                attr_set[dev] = true;
+            }
+        }
         const int per = (ntiles + sms - 1) / std::max(sms, 1);
         const size_t smem = (size_t)per * kResTileBytes;
         if (per <= kResMaxTiles && (size_t)9 * kResBorder * ntiles <= 3 * N &&
@@ -1531,7 +1545,7 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
             per_sm >= 1) {
             const int blocks = (ntiles + per - 1) / per;
             void *args[] = {&W, &H, (void *)&gx, (void *)&gy, &U, (void *)&U0, &dA, &partA, &partB, &gb,
-                            &max_iter, &gap_tol, &state};
+                            &max_iter, &gap_tol, &state, &trace, &trace_cap};
             lc.add(1);
             return cudaLaunchCooperativeKernel((const void *)k_cg_resident, dim3(blocks), dim3(kResThreads), args,
                                                smem, st);
@@ -1556,9 +1570,9 @@ cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy,
     const int resident = coop_blocks(kern, 1 << 30, smem);
     const int per_block = (ntiles + resident - 1) / resident;
     const int blocks = std::max(1, (ntiles + per_block - 1) / per_block);
-    void *args[] = {&W,       &H,       (void *)&gx, (void *)&gy, &U,       (void *)&U0, &r,     &dA,      &dB,
-                    &partA,   &partB,   &gb,         &max_iter,   &gap_tol, &state,   &maps[0], &maps[1],
-                    &maps[2], &maps[3], &maps[4]};
+    void *args[] = {&W,     &H,       (void *)&gx, (void *)&gy, &U,       (void *)&U0, &r,        &dA,
+                    &dB,    &partA,   &partB,      &gb,         &max_iter, &gap_tol,   &state,    &trace,
+                    &trace_cap, &maps[0], &maps[1], &maps[2], &maps[3], &maps[4]};
     lc.add(1);
     return cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(kPersistThreads), args, smem, st);
 }
@@ -1696,16 +1710,40 @@ __device__ __align__(256) unsigned char g_cg_scratch[kStaticBytes];
 
 std::mutex g_scratch_mu;
 unsigned char *g_scratch_addr[kMaxDevices] = {};
+void *g_scratch_ctx[kMaxDevices] = {};  // the driver context the cached address belongs to
 
-// Address of this device's copy of g_cg_scratch, looked up once per device with that device current.
+// The calling thread's current driver context (cuCtxGetCurrent through the runtime's entry-point query, so the
+// library does not link the driver library directly); nullptr when it cannot be asked.
+void *current_driver_context() {
+    using Fn = int (*)(void **);
+    static Fn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<Fn>(f);
+        cudaGetLastError();
+    });
+    void *ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
+// Address of this device's copy of g_cg_scratch, looked up with that device current the first time a driver
+// context of the device calls here. Keyed by the context: after a cudaDeviceReset, or under another context of the
+// same ordinal, the module is loaded again and the array moves, so the address is looked up again.
 unsigned char *static_scratch(int dev) {
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch_addr[dev]) {
+    void *ctx = current_driver_context();
+    if (!g_scratch_addr[dev] || !ctx || ctx != g_scratch_ctx[dev]) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_cg_scratch);
         if (e != cudaSuccess || !p)
             lfrv::raise(LFRV_E_CUDA, "cudaGetSymbolAddress(g_cg_scratch): %s", cudaGetErrorString(e));
         g_scratch_addr[dev] = static_cast<unsigned char *>(p);
+        g_scratch_ctx[dev] = current_driver_context();  // the runtime has made the primary context current by now
     }
     return g_scratch_addr[dev];
 }

@@ -1134,6 +1134,15 @@ __global__ void k_reduce_final(int count, const double *__restrict__ partial, do
     if (threadIdx.x == 0) *out = t;
 }
 
+// One energy-trace entry: the host's float expression lambda e_tv + alpha e_int (+ beta e_grad), without
+// contraction (the host code is compiled with -ffp-contract=off).
+__global__ void k_trace_energy(const double *__restrict__ sums, float lambda, float alpha, float beta, int grad,
+                               double *__restrict__ dst) {
+    float e = __fadd_rn(__fmul_rn(lambda, (float)sums[0]), __fmul_rn(alpha, (float)sums[1]));
+    if (grad) e = __fadd_rn(e, __fmul_rn(beta, (float)sums[3]));
+    *dst = (double)e;
+}
+
 // Elementwise helpers.
 __global__ void k_fill_u8(size_t n, uint8_t *p, uint8_t v) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -1635,6 +1644,13 @@ void launch_blur(int W, int H, const float *in, float *tmp, float *out, cudaStre
 void launch_reduce_final(int count, const double *partial, double *out, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "reduce_final", st);
     k_reduce_final<<<1, 1024, 0, st>>>(count, partial, out);
+    lc.add(1);
+}
+
+void launch_trace_energy(const double *sums, float lambda, float alpha, float beta, bool grad, double *dst,
+                         cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "trace_energy", st);
+    k_trace_energy<<<1, 1, 0, st>>>(sums, lambda, alpha, beta, grad ? 1 : 0, dst);
     lc.add(1);
 }
 

@@ -140,7 +140,7 @@ int main(int argc, char **argv) {
     lfrv_ctx *ctx = nullptr;
     if (lfrv_ctx_create(&ctx, device) != LFRV_OK) die("device");
     std::vector<float> out(3 * (size_t)W * H);
-    lfrv_stats st;
+    lfrv_stats st = {};
     const int rc = (algorithm == "IBR_color")
                        ? lfrv_ibr_color(ctx, &cfg, views.data(), tau.data(), 3, dpart.data(),
                                         init.empty() ? nullptr : init.data(), out.data(), &st)

@@ -52,10 +52,26 @@ class Camera(C.Structure):
 class Stats(C.Structure):
     _fields_ = [("outer_iterations", C.c_int), ("meta_iterations", C.c_int), ("hole_fill_iterations", C.c_int),
                 ("stop_reason", C.c_int), ("energy", C.c_double), ("gap", C.c_double), ("seconds", C.c_double),
-                ("kernel_launches", C.c_int)]
+                ("kernel_launches", C.c_int), ("energy_trace", C.POINTER(C.c_double)), ("trace_capacity", C.c_int),
+                ("trace_length", C.c_int)]
+
+    @classmethod
+    def with_trace(cls, capacity: int = 0) -> "Stats":
+        """Statistics that also record the energy of every outer iteration (up to `capacity` entries)."""
+        st = cls()
+        if capacity > 0:
+            st._trace_buf = np.zeros(capacity, np.float64)
+            st.energy_trace = st._trace_buf.ctypes.data_as(C.POINTER(C.c_double))
+            st.trace_capacity = capacity
+        return st
+
+    def trace(self) -> np.ndarray:
+        """The recorded energy trace (empty when none was requested)."""
+        buf = getattr(self, "_trace_buf", None)
+        return np.zeros(0) if buf is None else buf[: self.trace_length].copy()
 
     def as_dict(self) -> dict:
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "energy_trace"}
 
 
 class SceneParams(C.Structure):
@@ -332,45 +348,45 @@ class Context:
                                  C.c_void_p(d_tau), C.c_void_p(d_dpart), C.c_void_p(d_zbuf or None)))
 
     # ---- solvers
-    def _solve(self, fn, cfg: Config, views, tau, dpart, init=None):
+    def _solve(self, fn, cfg: Config, views, tau, dpart, init=None, trace: int = 0):
         views, tau = f32(views), f32(tau)
         dpart = None if dpart is None else f32(dpart)
         init = None if init is None else f32(init)
         H, W = cfg.h * cfg.dsf, cfg.w * cfg.dsf
         out = np.zeros((3, H, W), np.float32)
-        st = Stats()
+        st = Stats.with_trace(trace)
         _check(fn(self._h, C.byref(cfg), fptr(views), fptr(tau), tau.shape[1], fptr(dpart), fptr(init), fptr(out),
                   C.byref(st)))
         return out, st
 
-    def ibr_color(self, cfg: Config, views, tau, dpart, init=None):
-        return self._solve(LIB.lfrv_ibr_color, cfg, views, tau, dpart, init)
+    def ibr_color(self, cfg: Config, views, tau, dpart, init=None, trace: int = 0):
+        return self._solve(LIB.lfrv_ibr_color, cfg, views, tau, dpart, init, trace)
 
-    def ibr_gradient(self, cfg: Config, views, tau, dpart, init=None):
-        return self._solve(LIB.lfrv_ibr_gradient, cfg, views, tau, dpart, init)
+    def ibr_gradient(self, cfg: Config, views, tau, dpart, init=None, trace: int = 0):
+        return self._solve(LIB.lfrv_ibr_gradient, cfg, views, tau, dpart, init, trace)
 
     def solve_dev(self, algorithm: int, cfg: Config, d_views: int, d_tau: int, tau_channels: int, d_dpart: int,
-                  d_out: int, d_init: int = 0) -> Stats:
-        st = Stats()
+                  d_out: int, d_init: int = 0, trace: int = 0) -> Stats:
+        st = Stats.with_trace(trace)
         fn = LIB.lfrv_ibr_color_dev if algorithm == 0 else LIB.lfrv_ibr_gradient_dev
         _check(fn(self._h, C.byref(cfg), C.c_void_p(d_views), C.c_void_p(d_tau), tau_channels,
                   C.c_void_p(d_dpart or None), C.c_void_p(d_init or None), C.c_void_p(d_out), C.byref(st)))
         return st
 
     def render_view_dev(self, cfg: Config, algorithm: int, d_views: int, d_depth: int, cams, target: Camera,
-                        d_out: int) -> Stats:
-        st = Stats()
+                        d_out: int, trace: int = 0) -> Stats:
+        st = Stats.with_trace(trace)
         _check(LIB.lfrv_render_view_dev(self._h, C.byref(cfg), algorithm, C.c_void_p(d_views), C.c_void_p(d_depth),
                                         cameras_array(cams), C.byref(target), C.c_void_p(d_out), C.byref(st)))
         return st
 
-    def render_views_dev(self, jobs, net: "WarmStart | None" = None) -> list:
+    def render_views_dev(self, jobs, net: "WarmStart | None" = None, trace: int = 0) -> list:
         """Batched targets: jobs is a list of dicts with cfg, algorithm, d_views, d_depth, cams, target, d_out
         (device pointers as ints). With a warm-start network the IBR_gradient jobs are seeded by it
-        (lfrv_render_views_warm_dev). Returns one Stats per job."""
+        (lfrv_render_views_warm_dev). Returns one Stats per job (with `trace` entries of energy trace each)."""
         arr = (ViewJob * len(jobs))()
         keep = []
-        stats = [Stats() for _ in jobs]
+        stats = [Stats.with_trace(trace) for _ in jobs]
         for i, j in enumerate(jobs):
             cams = cameras_array(j["cams"])
             tgt = Camera()
@@ -385,9 +401,10 @@ class Context:
             _check(LIB.lfrv_render_views_warm_dev(self._h, net._h, arr, len(jobs)))
         return stats
 
-    def render_view(self, cfg: Config, algorithm: int, views, depth, cams, target: Camera, out=None):
+    def render_view(self, cfg: Config, algorithm: int, views, depth, cams, target: Camera, out=None,
+                    trace: int = 0):
         """Host-buffer pipeline (copies inside the call). views/depth/out may be numpy arrays or host pointers."""
-        st = Stats()
+        st = Stats.with_trace(trace)
         views_p = views if isinstance(views, int) else f32(views).ctypes.data
         depth_p = depth if isinstance(depth, int) else f32(depth).ctypes.data
         if out is None:

@@ -7,9 +7,16 @@
 # translation units under oracle/_ref/ (git-ignored) #include the reference files where they lie, or
 # extract line ranges of files that also contain host-side launch code.
 #
-# usage: oracle/build_ref.sh <reference root>
+# usage: oracle/build_ref.sh [<reference root>]    (default: $LFRV_REFERENCE_ROOT, else /root/reference)
+#        oracle/build_ref.sh --probe               (exit 0 and print the root if a reference tree is there)
 set -euo pipefail
-REF="${1:?reference root}"
+if [ "${1:-}" = "--probe" ]; then
+    ROOT_DIR="${LFRV_REFERENCE_ROOT:-/root/reference}"
+    [ -f "$ROOT_DIR/sources/optimization.cu" ] || exit 1
+    echo "$ROOT_DIR"
+    exit 0
+fi
+REF="${1:-${LFRV_REFERENCE_ROOT:-/root/reference}}"
 HERE="$(cd "$(dirname "$0")" && pwd)"
 OUT="$HERE/_ref"
 mkdir -p "$OUT"

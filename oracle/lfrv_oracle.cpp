@@ -862,6 +862,7 @@ void ibr_color(const lfrv_config &cfg, const T *views, const T *tau, int tau_ch,
                T *out, lfrv_stats *st) {
     ColorState<T> S;
     S.init(cfg, views, tau, tau_ch, dpart);
+    if (st) st->trace_length = 0;
     color_compute_weights(S);   // super-resolution.cpp:157 (U = 0, visibility all false)
     color_visibility(S);        // :160
     if (init) {
@@ -886,6 +887,10 @@ void ibr_color(const lfrv_config &cfg, const T *views, const T *tau, int tau_ch,
             color_fista_iteration(S);
             ++total_k;
             energy = color_energy(S);
+            if (st && st->energy_trace && total_k - 1 < st->trace_capacity) {
+                st->energy_trace[total_k - 1] = (double)energy;
+                st->trace_length = total_k;
+            }
             if (!cfg.early_exit) continue;
             if ((double)energy < EPS) {
                 reason = 1;
@@ -1067,9 +1072,11 @@ double cg_energy(int W, int H, const T *U, const T *U0, const T *gX, const T *gY
 //             second count uses the row's correct residual, and alpha is read before any addition.
 //   corrected: conjugate gradient per channel with double dot products, stopping when the certified
 //             relative gap ||r||^2/(2 lambda) / (E(u) - ||r||^2/(2 lambda)) <= gap_tol or at max_iter.
+// trace (optional, trace_cap entries): the energy after each iteration -- the FP64 quadratic energy of the
+// iterate (faithful) or the energy lowered by each step's decrease (corrected), as the device solvers record it.
 template <class T>
 int cg_solve(int W, int H, bool faithful, int max_iter, double gap_tol, const T *gX, const T *gY, T *U,
-             double *gap_out) {
+             double *gap_out, double *trace = nullptr, int trace_cap = 0) {
     const size_t N = (size_t)W * H;
     const T lambda = 1;
     Vec<T> U0(U, U + 3 * N);
@@ -1115,6 +1122,7 @@ int cg_solve(int W, int H, bool faithful, int max_iter, double gap_tol, const T 
                 dAlpha[c] = (double)alpha + rr;  // updateSolution adds r.r into the alpha slot
                 for (size_t o = 0; o < N; ++o) dc[o] = rc[o] + (T)1 * dc[o];  // beta = deltaNew/deltaOld = 1
             }
+            if (trace && it < trace_cap) trace[it] = cg_energy(W, H, U, U0.data(), gX, gY);
         }
         if (gap_out) *gap_out = 0;
         return it;
@@ -1150,6 +1158,7 @@ int cg_solve(int W, int H, bool faithful, int max_iter, double gap_tol, const T 
             delta[c] = rr;
             for (size_t o = 0; o < N; ++o) dc[o] = rc[o] + (T)beta * dc[o];
         }
+        if (trace && it < trace_cap) trace[it] = E;
     }
     if (gap_out) *gap_out = gap;
     return it;
@@ -1184,10 +1193,12 @@ void ibr_gradient(const lfrv_config &cfg, const T *views, const T *tau, int tau_
     Vec<T> gx(N), gy(N), mask(N);
     u_gradient(P, cfg, gx.data(), gy.data(), mask.data());
     double gap = 0;
+    const bool traced = st && st->energy_trace && st->trace_capacity > 0;
     const int it = cg_solve(P.W, P.H, cfg.faithful != 0, cfg.cg_max_iter, cfg.cg_gap_tol, gx.data(), gy.data(),
-                            U.data(), &gap);
+                            U.data(), &gap, traced ? st->energy_trace : nullptr, traced ? st->trace_capacity : 0);
     std::copy(U.begin(), U.end(), out);
     if (st) {
+        st->trace_length = traced ? std::min(it, st->trace_capacity) : 0;
         st->outer_iterations = it;
         st->hole_fill_iterations = hf;
         st->gap = gap;

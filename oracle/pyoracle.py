@@ -28,19 +28,19 @@ def _cfg(cfg):
     return C.byref(cfg)
 
 
-def ibr_color(cfg, views, tau, dpart, init=None, prec=0):
+def ibr_color(cfg, views, tau, dpart, init=None, prec=0, trace=0):
     views, tau = f32(views), f32(tau)
     out = np.zeros((3, cfg.h * cfg.dsf, cfg.w * cfg.dsf), np.float32)
-    st = lfrv.Stats()
+    st = lfrv.Stats.with_trace(trace)
     LIB.orc_ibr_color(prec, _cfg(cfg), fptr(views), fptr(tau), tau.shape[1], fptr(None if dpart is None else f32(dpart)),
                       fptr(None if init is None else f32(init)), fptr(out), C.byref(st))
     return out, st
 
 
-def ibr_gradient(cfg, views, tau, dpart, init=None, prec=0):
+def ibr_gradient(cfg, views, tau, dpart, init=None, prec=0, trace=0):
     views, tau = f32(views), f32(tau)
     out = np.zeros((3, cfg.h * cfg.dsf, cfg.w * cfg.dsf), np.float32)
-    st = lfrv.Stats()
+    st = lfrv.Stats.with_trace(trace)
     LIB.orc_ibr_gradient(prec, _cfg(cfg), fptr(views), fptr(tau), tau.shape[1],
                          fptr(None if dpart is None else f32(dpart)), fptr(None if init is None else f32(init)),
                          fptr(out), C.byref(st))

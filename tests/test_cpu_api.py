@@ -134,3 +134,38 @@ def test_psnr_border():
     b[:, 5, 5] = 0.1
     mse = (0.01 * 3 / 3) / 36.0
     assert lfrv.psnr(a, b) == pytest.approx(10 * np.log10(1.0 / mse))
+
+
+def test_stats_layout_matches_header():
+    """lfrv_stats as ctypes sees it is the C struct of include/lfrv.h (the trace fields sit at the end)."""
+    import ctypes as C
+
+    import lfrv
+
+    assert C.sizeof(lfrv.Stats) == 64
+    assert lfrv.Stats.energy_trace.offset == 48 and lfrv.Stats.trace_length.offset == 60
+
+
+def test_oracle_energy_traces():
+    """The oracle records one energy per outer iteration: the reference energy after each FISTA iteration
+    (IBR_color), the quadratic energy after each CG iteration (IBR_gradient, both CG modes)."""
+    import numpy as np
+
+    import pyoracle
+    from scenes import color_config, gradient_config, scene
+
+    sc = scene(1, 32)
+    tau, dpart, _ = pyoracle.warp(sc.depth, sc.cams, sc.target)
+    cfg = color_config(sc, niter=5, early_exit=0)
+    _, st = pyoracle.ibr_color(cfg, sc.views, tau, dpart, prec=0, trace=8)
+    assert st.trace_length == 5 and st.trace()[-1] == st.energy
+    _, st = pyoracle.ibr_color(cfg, sc.views, tau, dpart, prec=0, trace=3)  # a shorter buffer keeps the first 3
+    assert st.trace_length == 3
+    g = gradient_config(sc, faithful=0, cg_gap_tol=1e-8)
+    _, st = pyoracle.ibr_gradient(g, sc.views, tau, dpart, prec=0, trace=200)
+    tr = st.trace()
+    assert st.trace_length == st.outer_iterations > 3
+    assert np.all(np.diff(tr) <= 1e-12 * abs(tr[0]))  # CG lowers the energy at every step
+    g = gradient_config(sc, faithful=1)
+    _, st = pyoracle.ibr_gradient(g, sc.views, tau, dpart, prec=0, trace=10)
+    assert st.trace_length == 5

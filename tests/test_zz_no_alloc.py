@@ -20,12 +20,18 @@ def test_static_cg_rejects_oversized_images():
     assert e.value.status == lfrv.E_ARG
 
 
+# (H, W) and the kernel the call takes: 200 x 296 fits the shared-memory resident CG; images narrower than 30
+# pixels do not (their partial 64 x 16 tiles cannot hold the published borders), so 8192 x 28 runs the TMA-fed
+# streaming kernel (W a multiple of 4) and 8192 x 26 the streaming kernel with plain loads.
+SHAPES = [(200, 296, "resident"), (8192, 28, "streaming, TMA"), (8192, 26, "streaming, plain loads")]
+
+
 @pytest.mark.gpu
-def test_static_cg_matches_stage_cg_twice():
+@pytest.mark.parametrize("H,W,path", SHAPES)
+def test_static_cg_matches_stage_cg_twice(H, W, path):
     import torch
 
     rng = np.random.default_rng(21)
-    H, W = 200, 296
     U0 = rng.uniform(0, 1, (3, H, W)).astype(np.float32)
     gx = rng.normal(0, 0.05, (H, W)).astype(np.float32)
     gy = rng.normal(0, 0.05, (H, W)).astype(np.float32)
@@ -44,3 +50,14 @@ def test_static_cg_matches_stage_cg_twice():
         assert it == wit and 0 < gap <= 1e-7
         assert abs(gap - wgap) <= 1e-12 + 1e-6 * wgap
         np.testing.assert_allclose(got, want, rtol=0, atol=1e-6)
+    # without iterations / gap the call only enqueues its work on the stream; the caller synchronises. A warmed-up
+    # call leaves the device's free memory unchanged: it allocates nothing.
+    d_U = torch.from_numpy(U0).cuda()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    lfrv.cg_solve_static(stream.cuda_stream, W, H, 500, 1e-7, d_gx.data_ptr(), d_gy.data_ptr(), d_U.data_ptr(),
+                         want_stats=False)
+    stream.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    np.testing.assert_allclose(d_U.cpu().numpy(), want, rtol=0, atol=1e-6)
