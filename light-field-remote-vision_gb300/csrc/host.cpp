@@ -157,6 +157,7 @@ static void reset_stats(lfrv_stats *st) {
 static double *trace_request(lfrv_ctx *c, lfrv_stats *st) {
     if (!st || !st->energy_trace || st->trace_capacity <= 0) return nullptr;
     c->ws.trace.ensure(sizeof(double) * (size_t)st->trace_capacity);
+    c->pending.stats = st;
     c->pending.trace_host = st->energy_trace;
     c->pending.trace_cap = st->trace_capacity;
     c->pending.trace_len = -1;

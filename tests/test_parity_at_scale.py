@@ -8,8 +8,11 @@ Two comparisons per configuration:
   * end to end: the oracle's own FP64 warp feeds its solver. The GPU evaluates the projections in float, so a
     few source pixels on depth edges get another visibility code or a tau that differs by more than 1e-3 px, and
     a tau that lies within float rounding of a pixel boundary can take another discrete footprint decision
-    (anchor, splat set, a tap of weight exactly 0). Target pixels within the footprints of those source pixels,
-    dilated by DILATE pixels, are excluded and counted; everywhere else the 1e-4 bar holds.
+    (anchor, splat set, a tap of weight exactly 0), which can change a target pixel's visibility. The excluded
+    target pixels are counted: IBR_gradient excludes the pixels whose visibility differs between the two warps
+    and the footprints of source pixels with another code or tau, dilated by DILATE pixels; IBR_color excludes
+    the footprints of every source pixel with another code, tau or footprint decision, dilated the same way.
+    Everywhere else the 1e-4 bar holds.
 
 Set LFRV_PARITY_REPORT to a file path to record the measured errors and the excluded pixel counts as JSON.
 """
@@ -76,7 +79,15 @@ def _footprint_decisions(t, W, H, dsf):
                      ((y0 + 0.5) - (py - 0.5 * dsf)) == 0, ((py + 0.5 * dsf) - (y0 + dsf - 0.5)) == 0])
 
 
-def _affected_mask(tau_a, tau_b, dsf, H, W, tol=1e-3):
+def _dilate(m, r):
+    out = m.copy()
+    ys, xs = np.nonzero(m)
+    for y, x in zip(ys, xs):
+        out[max(0, y - r):y + r + 1, max(0, x - r):x + r + 1] = True
+    return out
+
+
+def _affected_mask(tau_a, tau_b, dsf, H, W, tol=1e-3, flips=True):
     """Target pixels near the footprints of source pixels whose warps differ between tau_a and tau_b: another
     visibility code, a tau more than `tol` px apart, or another discrete footprint decision (a tau within float
     rounding of a pixel boundary). Returns the mask and the counts of the two kinds of source pixels."""
@@ -85,8 +96,11 @@ def _affected_mask(tau_a, tau_b, dsf, H, W, tol=1e-3):
     differ = code_a != code_b
     both = (code_a == 0) & (code_b == 0)
     differ |= both & ((np.abs(tau_a[:, 0] - tau_b[:, 0]) > tol) | (np.abs(tau_a[:, 1] - tau_b[:, 1]) > tol))
-    flips = np.any(_footprint_decisions(tau_a, W, H, dsf) != _footprint_decisions(tau_b, W, H, dsf), axis=0)
-    flips &= ~differ
+    if flips:
+        flips = np.any(_footprint_decisions(tau_a, W, H, dsf) != _footprint_decisions(tau_b, W, H, dsf), axis=0)
+        flips &= ~differ
+    else:
+        flips = np.zeros_like(differ)
     mask = np.zeros((H, W), bool)
     r = dsf + 1 + DILATE
     for t in (tau_a, tau_b):
@@ -119,7 +133,18 @@ def _compare(ctx, name, sc, cfg, algorithm, trace):
     tau_o, dpart_o, _ = pyoracle.warp(sc.depth, sc.cams, sc.target)
     ref_e2e, rst_e2e = solve(cfg, sc.views, tau_o, dpart_o, prec=0)
     H, W = out.shape[1:]
-    mask, ndiff, nflip, nsrc = _affected_mask(tau_g, tau_o, cfg.dsf, H, W)
+    fmask, ndiff, nflip, nsrc = _affected_mask(tau_g, tau_o, cfg.dsf, H, W)
+    # the discrete decision that moves the result is a target pixel's visibility (IBR_gradient: some splatted tap
+    # of nonzero weight; IBR_color: splatted coverage >= 1); pixels whose visibility differs between the two warps,
+    # dilated by DILATE, and the footprints of source pixels with another code or tau form the excluded set
+    if algorithm == 1:
+        va = pyoracle.stage_gradient_visibility(cfg, tau_g)
+        vb = pyoracle.stage_gradient_visibility(cfg, tau_o)
+        cmask, _, _, _ = _affected_mask(tau_g, tau_o, cfg.dsf, H, W, flips=False)
+        mask = cmask | _dilate(va != vb, DILATE)
+    else:
+        mask = fmask
+    vis_flips = int((va != vb).sum()) if algorithm == 1 else None
     holes_differ = algorithm == 1 and rst_e2e.hole_fill_iterations != st.hole_fill_iterations
     if holes_differ:  # another stop iteration of the hole filling changes every hole pixel: exclude the holes
         vis = pyoracle.stage_gradient_visibility(cfg, tau_o)
@@ -133,7 +158,9 @@ def _compare(ctx, name, sc, cfg, algorithm, trace):
            "max_rel_err_same_warps": err_same, "trace_entries": n, "trace_max_rel_err": trace_err,
            "source_pixels_with_other_warp": ndiff, "source_pixels_with_other_footprint_decision": nflip,
            "source_pixels": nsrc, "hole_fill_iterations_oracle_own_warps": rst_e2e.hole_fill_iterations,
-           "holes_excluded": bool(holes_differ),
+           "holes_excluded": bool(holes_differ), "target_pixels_with_other_visibility": vis_flips,
+           "footprint_mask_pixels": int(fmask.sum()),
+           "max_rel_err_outside_footprint_mask": float(rmap[~fmask].max()) if (~fmask).any() else 0.0,
            "target_pixels_excluded": int(mask.sum()), "target_pixels": int(H * W),
            "max_rel_err_end_to_end_outside_excluded": err_e2e_kept,
            "max_rel_err_end_to_end_all": float(rmap.max()),
