@@ -1,23 +1,29 @@
-"""Benchmark: converged views/sec of the depth-to-view pipeline on one GB300.
+"""Benchmark: converged views/sec of the depth-to-view pipeline on one GB300 -- BASELINE's metric, "views/sec to
+energy gap <= 1e-4: learned + batched vs plain solver, same GB300".
 
-Workload (default "c2"): the super-resolution configuration -- a synthetic 5x5 light field of 512x512 RGB
-float32 views (rendered at 1024^2 and box-decimated, 5 planes + 20 Gaussian depth bumps, baseline 0.03,
-noise 0.005), 24 inputs warped to the 1024x1024 centre view and reconstructed with the gradient-constraint
-formulation (IBR_gradient) solved by conjugate gradient with FP32 iterates and FP64 dot products until the
-certified relative energy gap is <= 1e-4 (cap 500 iterations). One step = one full view: warp stage (target
-depth map, tau, dtau/dz), inverse footprint map, visibility, weights, weighted average, hole filling,
-gradient splatting and the CG solve.
+Workload (default "c5", the full pipeline the metric is quoted on): one synthetic 9x9 light field of 1024x1024
+RGB float32 views (rendered at 2048^2 and box-decimated 2x, 5 planes + 20 Gaussian depth bumps, baseline 0.03,
+noise 0.005), its 80 inputs warped to 32 target cameras of 2048x2048 (2x super-resolution) and reconstructed with
+the gradient-constraint formulation (IBR_gradient) solved by conjugate gradient with FP32 iterates and FP64 dot
+products until the certified relative energy gap is <= 1e-4. One step = the 32 targets.
 
-  value : views/sec with inputs resident in HBM (device pointers, lfrv_render_view_dev)
-  e2e   : views/sec through the host-buffer C ABI call (lfrv_render_view) from pinned host memory, with the
-          host->device copy of the views and depth maps and the device->host copy of the result inside
-  roofline : the dominant kernel of the step (by device time), algorithmic bytes per launch / its average
+  value : views/sec of the learned + batched arm (BF16 view stacks, the encoder-decoder's warm start, all 32
+          targets in one lfrv_render_views_warm_dev call) with inputs resident in HBM
+  config.modes / speedup_vs_plain : every arm (plain FP32 one target at a time -- the plain solver --, plain
+          batched, BF16 batched, learned + BF16 batched) on the same targets and the same GPU
+  e2e   : the learned + batched arm through the host-buffer C ABI call (lfrv_render_views_warm), from pinned host
+          memory, with the light field's upload and the 32 outputs' download inside the timed region
+  roofline : the dominant kernel of the plain step (by device time), algorithmic bytes per launch / its average
           CUDA-event duration on the launch stream
-  cpu_baseline : the FP32 CPU restatement of the reference path (oracle port, OpenMP over the host cores) on
-          one full view of the same workload
+  cpu_baseline : the FP32 CPU restatement of the reference path (oracle port, OpenMP over the host cores) on the
+          centre target
+  vs_fp64 : the centre target against the FP64 CPU oracle run on the GPU's warps
 
-`--impl reference` times that CPU restatement alone as the reference arm (the reference's own path needs
-Qt, glm, OpenGL and its CUDA runtime and cannot run here).
+Other workloads (--workload): c1 (3x3 256^2, IBR_color 300 x 300 iterations), c2 (5x5 512^2 -> 1024^2, one target),
+c3 (batched targets of uneven size), c4 (learned warm start trained in the run, 512^2), net (the network alone).
+
+`--impl reference` times the CPU restatement alone as the reference arm (the reference's own path needs Qt, glm,
+OpenGL and its CUDA runtime and cannot run here).
 """
 from __future__ import annotations
 
@@ -37,16 +43,22 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "light-field-remote-vision_gb300"))
 
 WORKLOADS = {
-    "c3": dict(preset=2, algorithm=1, name="batched: 32 targets of 256^2..1024^2 from 8 seeded 5x5 light fields "
-                                            "(dsf 1 or 2), IBR_gradient + CG to gap 1e-4, one lfrv_render_views_dev call"),
-    "c2": dict(preset=2, algorithm=1, name="5x5 LF 512^2 -> 1024^2 (dsf 2), 24 views, IBR_gradient + CG to gap 1e-4"),
-    "c1": dict(preset=1, algorithm=0, name="3x3 LF 256^2, 8 views, IBR_color primal-dual TV, 300 x 300 iterations"),
-    "c5": dict(preset=2, algorithm=1, name="full pipeline: 9x9 LF of 1024^2 views (80 inputs, point-sampled renders, "
-                                            "5 planes + 20 bumps) -> 32 targets of 2048^2 (dsf 2), IBR_gradient + CG to "
-                                            "gap 1e-4; BF16 stacks + learned warm start + batched vs plain FP32"),
-    "c4": dict(preset=1, algorithm=1, name="learned warm start: 3x3 LF 512^2 (8 views, 3 planes + 20 bumps), "
-                                            "IBR_gradient + CG to gap 1e-4 seeded by the encoder-decoder trained in "
-                                            "the run, 16 held-out targets per step, batched"),
+    "c5": dict(preset=2, algorithm=1, steps=5, warmup=3,
+               name="full pipeline: 9x9 LF of 1024^2 views (80 inputs rendered at 2048^2 and box-decimated, 5 planes + "
+                    "20 bumps) -> 32 targets of 2048^2 (dsf 2), IBR_gradient + CG to gap 1e-4; learned warm start + BF16 "
+                    "stacks + batched vs the plain FP32 solver one target at a time"),
+    "c3": dict(preset=2, algorithm=1, steps=5, warmup=3,
+               name="batched: 32 targets of 256^2..1024^2 from 8 seeded 5x5 light fields (dsf 1 or 2), IBR_gradient + "
+                    "CG to gap 1e-4, one lfrv_render_views_dev call"),
+    "c2": dict(preset=2, algorithm=1, steps=200, warmup=5,
+               name="5x5 LF 512^2 -> 1024^2 (dsf 2), 24 views, IBR_gradient + CG to gap 1e-4"),
+    "c1": dict(preset=1, algorithm=0, steps=10, warmup=3,
+               name="3x3 LF 256^2, 8 views, IBR_color primal-dual TV, 300 x 300 iterations"),
+    "c4": dict(preset=1, algorithm=1, steps=10, warmup=3,
+               name="learned warm start: 3x3 LF 512^2 (8 views, 3 planes + 20 bumps), IBR_gradient + CG to gap 1e-4 "
+                    "seeded by the encoder-decoder trained in the run, 16 held-out targets per step, batched"),
+    "net": dict(preset=0, algorithm=-1, steps=10, warmup=3,
+                name="learned warm start network alone: one 512^2 inference and one training step of 4"),
 }
 
 
@@ -66,9 +78,9 @@ def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: in
                       rof_iters: int = 0) -> float | None:
     """Compulsory DRAM bytes of one launch of `kernel` (FP32 = 4 B; V views of n pixels, N target pixels)."""
     table = {
-        # r = b - A u0 (g_x, g_y, u read, r written), then per iteration: r, d_old read, d written (phase A);
-        # d, u, r read, u, r written (phase B)
-        "cg_persistent": 32 * N + cg_iters * 96 * N,
+        # per CG iteration the state vectors x, r, d are each read and written once: 72 B per pixel (q is not
+        # materialised; the FP64 scalars are negligible)
+        "cg_persistent": cg_iters * 72 * N,
         # inverse map (bucket starts + 4 B entries), per source pixel tau 8 B + colour 12 B + Sobel 8 B +
         # weight 4 B; vis 1 B, U 12 B, g_x, g_y, mask 12 B written per target pixel
         "gradient_setup": 4 * N + 4 * V * n + 32 * V * n + 25 * N,
@@ -99,9 +111,9 @@ def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: in
 # DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu --set full capture of the
 # C2 step (5x5 light field of 512^2 views -> the 1024^2 target).
 NCU_TRAFFIC_BYTES = {
-    "zbuffer_splat": 83.937536e6 + 2.530560e6,
-    "gradient_setup": 224.049664e6 + 18.143744e6,
-    "cg_persistent": 21.045248e6 + 0.008192e6,
+    ("zbuffer_splat", 1024 * 1024): 83.937536e6 + 2.530560e6,
+    ("gradient_setup", 1024 * 1024): 224.049664e6 + 18.143744e6,
+    ("cg_persistent", 1024 * 1024): 21.045248e6 + 0.008192e6,
 }
 
 
@@ -162,31 +174,95 @@ def run_reference(args, rank: int) -> None:
     import pyoracle
 
     wl = WORKLOADS[args.workload]
-    sc = lfrv.synth_scene(lfrv.scene_params(wl["preset"]))
-    cfg = make_config(lfrv, args.workload, sc)
+    if args.workload == "net":
+        print(json.dumps({"impl": "reference", "unavailable": "the learned network has no reference counterpart"}))
+        return
+    if args.workload == "c5":
+        p, sc, targets, _ = c5_scene(lfrv)
+        sc.target = targets[0]
+        cfg = c5_config(lfrv, p, sc.views.shape[0])
+        sample = "the centre target of the 32 per step"
+        metric = "views/sec to energy gap <=1e-4 (learned+batched vs plain solver, same GB300)"
+    else:
+        sc = lfrv.synth_scene(lfrv.scene_params(wl["preset"]))
+        cfg = make_config(lfrv, args.workload, sc)
+        sample = "one full view per step"
+        metric = "views/sec to energy gap <=1e-4"
     if args.workload == "c1":
         cfg.niter = 30  # bounded sample: 30 x 30 iterations; the value is scaled to the 300 x 300 step below
-    # Bounded sample: one warm-up view at most, then full views until K views or a ~150 s budget is used.
-    if args.warmup > 0:
-        cpu_step(pyoracle, args.workload, cfg, sc, wl["algorithm"])
-    times = []
+    algorithm = 0 if args.workload == "c1" else 1
+    # Bounded sample: one warm-up view at most, then full views until K views or a ~150 s budget (warm-up included)
+    # is used; at least one view is timed.
     t_start = time.perf_counter()
+    if args.warmup > 0:
+        cpu_step(pyoracle, args.workload, cfg, sc, algorithm)
+    times = []
     while len(times) < args.steps and (not times or time.perf_counter() - t_start + times[-1] < 150.0):
-        times.append(cpu_step(pyoracle, args.workload, cfg, sc, wl["algorithm"]))
+        times.append(cpu_step(pyoracle, args.workload, cfg, sc, algorithm))
     sec = sum(times) / len(times)
     if args.workload == "c1":
         sec *= 100.0  # ROF work scales with niter^2
     cores = os.cpu_count()
     v = 1.0 / sec
-    line = {"impl": "reference", "metric": "views/sec to energy gap <=1e-4", "value": v, "unit": "views/s",
+    line = {"impl": "reference", "metric": metric, "value": v, "unit": "views/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": {"workload": wl["name"]},
             "cpu_baseline": {"value": v, "unit": "views/s", "cores": cores, "kind": "port",
-                             "sample": f"{len(times)} full views (warp + solve) timed of {args.steps} requested "
-                                       f"(150 s budget), FP32 CPU restatement, OpenMP"},
+                             "sample": f"{len(times)} full views (warp + solve; {sample}) timed of {args.steps} "
+                                       f"requested (150 s budget), FP32 CPU restatement, OpenMP"},
             "e2e": {"value": v, "unit": "views/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def run_net(args, rank: int, world: int) -> None:
+    """The learned warm start network alone: one 512^2 inference and one training step of 4 images, random inputs
+    of the network's shape, CUDA events on the library's stream after warm-up."""
+    import torch
+    import lfrv
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()
+    ctx = lfrv.Context(dev, stream.cuda_stream)
+    net = lfrv.WarmStart(ctx, seed=1)
+    H = W = 512
+    B = 4
+    g = torch.Generator(device="cuda").manual_seed(0)
+    x = torch.rand((B, H, W, lfrv.WARMSTART_CHANNELS), device="cuda", generator=g).to(torch.bfloat16)
+    u0 = torch.rand((B, 3, H, W), device="cuda", generator=g)
+    tg = u0 + 0.01 * torch.randn((B, 3, H, W), device="cuda", generator=g)
+    pred = torch.zeros_like(u0)
+    torch.cuda.synchronize()
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    train_ms = timed(lambda: net.train_step_dev(B, H, W, x.data_ptr(), u0.data_ptr(), tg.data_ptr(), 1e-4))
+    l0 = ctx.launch_count()
+    fwd_ms = timed(lambda: net.forward_dev(1, H, W, x[0].data_ptr(), u0[0].data_ptr(), pred[0].data_ptr()))
+    launches = ctx.launch_count() - l0
+    gflop = 34.6  # 2 M N K of the 12 convolutions and the head at 512^2 (unpadded K)
+    if rank == 0:
+        print(json.dumps({"metric": "learned warm start inference images/sec", "value": 1e3 / fwd_ms,
+                          "unit": "images/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                          "ms_per_step": fwd_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "bf16 (fp32 accumulation)", "data": "random inputs of the network's shape",
+                          "config": {"workload": WORKLOADS["net"]["name"], "forward_ms": fwd_ms,
+                                     "train_step_ms_batch4": train_ms, "forward_tflops": gflop / fwd_ms,
+                                     "forward_launches": launches // max(1, args.warmup + args.steps)}}),
+              flush=True)
+    net.close()
+    ctx.close()
 
 
 def batch_scenes(lfrv):
@@ -439,23 +515,13 @@ def run_warm(args, rank: int, world: int) -> None:
     ctx.close()
 
 
-def run_full(args, rank: int, world: int) -> None:
-    """Full pipeline (c5): one 9x9 light field, 32 target cameras around the centre, every arm timed over the 32
-    targets: plain FP32 one at a time, plain FP32 batched, BF16 stacks batched, BF16 + learned warm start batched.
-    The network is trained in the run on 512^2 crops of 4 other targets' 2048^2 features (untimed)."""
+def c5_scene(lfrv):
+    """The c5 light field and its 32 target cameras (the rendered centre camera first, then 31 shifted by fractions
+    of the baseline), plus 4 other cameras whose features train the network."""
     import copy
-    import torch
-    import lfrv
 
-    dev = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(dev)
-    wl = WORKLOADS[args.workload]
-    t_gen = time.time()
-    p = lfrv.scene_params(2, w=1024, h=1024, grid=9, dsf=2, ss=1, seed=7000)
+    p = lfrv.scene_params(2, w=1024, h=1024, grid=9, dsf=2, ss=2, seed=7000)
     sc = lfrv.synth_scene(p)
-    t_gen = time.time() - t_gen
-    V = sc.views.shape[0]
-    H, W = sc.gt.shape[1], sc.gt.shape[2]
 
     def shifted(i, n_side, scale):
         t = copy.copy(sc.target)
@@ -463,19 +529,40 @@ def run_full(args, rank: int, world: int) -> None:
         t.t[1] = sc.target.t[1] + ((i // n_side) - (n_side - 1) / 2) * scale * p.baseline
         return t
 
-    targets = [copy.copy(sc.target)] + [shifted(i, 6, 0.08) for i in range(31)]  # the rendered centre first
+    targets = [copy.copy(sc.target)] + [shifted(i, 6, 0.08) for i in range(31)]
     train_targets = [shifted(i, 2, 0.37) for i in range(4)]
-    ctx = lfrv.Context(dev)
+    return p, sc, targets, train_targets
 
-    def cfg_of(tol, bf16):
-        return lfrv.default_config(w=p.w, h=p.h, dsf=p.dsf, nviews=V, nchannels=3, sigma_sensor=0.005, lambda_=0.05,
-                                   faithful=0, cg_gap_tol=tol, cg_max_iter=500, hole_fill_iter=500,
-                                   bf16_storage=1 if bf16 else 0)
 
+def c5_config(lfrv, p, V, tol=1e-4, bf16=False):
+    return lfrv.default_config(w=p.w, h=p.h, dsf=p.dsf, nviews=V, nchannels=3, sigma_sensor=0.005, lambda_=0.05,
+                               faithful=0, cg_gap_tol=tol, cg_max_iter=500, hole_fill_iter=500,
+                               bf16_storage=1 if bf16 else 0)
+
+
+def run_full(args, rank: int, world: int) -> None:
+    """Full pipeline (c5), BASELINE's metric: one 9x9 light field, 32 target cameras, every arm timed over the 32
+    targets on the same GPU: plain FP32 one at a time (the plain solver), plain FP32 batched, BF16 stacks batched,
+    and learned + batched (BF16 stacks, warm start, one batched call) -- the headline value. The network is trained
+    in the run on 512^2 crops of 4 other targets' 2048^2 features (untimed)."""
+    import torch
+    import lfrv
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    wl = WORKLOADS["c5"]
+    t_gen = time.time()
+    p, sc, targets, train_targets = c5_scene(lfrv)
+    t_gen = time.time() - t_gen
+    V = sc.views.shape[0]
+    H, W = sc.gt.shape[1], sc.gt.shape[2]
+    stream = torch.cuda.Stream()
+    ctx = lfrv.Context(dev, stream.cuda_stream)
+    cfg32, cfg16 = c5_config(lfrv, p, V), c5_config(lfrv, p, V, bf16=True)
     views = torch.from_numpy(sc.views).cuda()
     views_bf16 = views.to(torch.bfloat16)
     depth = torch.from_numpy(sc.depth).cuda()
-    sc.views = None  # the host copy is no longer needed
+    torch.cuda.synchronize()
     # training data for the network: features of 4 targets at 2048^2, random 512^2 crops
     t_feat = time.time()
     X = torch.zeros((len(train_targets), H, W, 48), dtype=torch.bfloat16, device="cuda")
@@ -483,15 +570,15 @@ def run_full(args, rank: int, world: int) -> None:
     S = torch.zeros((len(train_targets), 3, H, W), device="cuda")
     torch.cuda.synchronize()
     for i, t in enumerate(train_targets):
-        ctx.warmstart_features_dev(cfg_of(1e-6, True), views_bf16.data_ptr(), depth.data_ptr(), sc.cams, t,
-                                   X[i].data_ptr(), U0[i].data_ptr(), S[i].data_ptr())
+        ctx.warmstart_features_dev(c5_config(lfrv, p, V, tol=1e-6, bf16=True), views_bf16.data_ptr(), depth.data_ptr(),
+                                   sc.cams, t, X[i].data_ptr(), U0[i].data_ptr(), S[i].data_ptr())
     torch.cuda.synchronize()
     t_feat = time.time() - t_feat
     net = lfrv.WarmStart(ctx, seed=1)
     rng = np.random.default_rng(0)
     steps, bs, crop = 1000, 4, 512
     t_train = time.time()
-    for step in range(steps):
+    for _ in range(steps):
         ii = rng.integers(0, len(train_targets), bs)
         ys = rng.integers(0, (H - crop) // 8 + 1, bs) * 8
         xs = rng.integers(0, (W - crop) // 8 + 1, bs) * 8
@@ -503,9 +590,8 @@ def run_full(args, rank: int, world: int) -> None:
     torch.cuda.synchronize()
     t_train = time.time() - t_train
     del X, U0, S
-    cfg32, cfg16 = cfg_of(1e-4, False), cfg_of(1e-4, True)
     outs = {k: [torch.empty((3, H, W), device="cuda") for _ in targets]
-            for k in ("plain_single", "plain_batched", "bf16_batched", "bf16_warm_batched")}
+            for k in ("plain_single", "plain_batched", "bf16_batched", "learned_batched")}
 
     def jobs(name, cfg, vp):
         return [dict(cfg=cfg, algorithm=1, d_views=vp, d_depth=depth.data_ptr(), cams=sc.cams, target=t,
@@ -514,30 +600,32 @@ def run_full(args, rank: int, world: int) -> None:
     j_ps = jobs("plain_single", cfg32, views.data_ptr())
     j_pb = jobs("plain_batched", cfg32, views.data_ptr())
     j_bb = jobs("bf16_batched", cfg16, views_bf16.data_ptr())
-    j_wb = jobs("bf16_warm_batched", cfg16, views_bf16.data_ptr())
+    j_wb = jobs("learned_batched", cfg16, views_bf16.data_ptr())
     arms = (("plain_single", lambda: [ctx.render_view_dev(j["cfg"], 1, j["d_views"], j["d_depth"], j["cams"],
                                                           j["target"], j["d_out"]) for j in j_ps]),
             ("plain_batched", lambda: ctx.render_views_dev(j_pb)),
             ("bf16_batched", lambda: ctx.render_views_dev(j_bb)),
-            ("bf16_warm_batched", lambda: ctx.render_views_dev(j_wb, net)))
+            ("learned_batched", lambda: ctx.render_views_dev(j_wb, net)))
     results = {}
+    clocks, launches = None, None
     torch.cuda.synchronize()
     for name, fn in arms:
-        for _ in range(max(args.warmup, 3)):
+        for _ in range(args.warmup):
             st = fn()
         torch.cuda.synchronize()
-        if name == "bf16_warm_batched":
+        headline = name == "learned_batched"
+        if headline:
             clk_path = tempfile.mktemp(prefix="lfrv_clocks_")
             clk = sample_clocks(clk_path)
             l0 = ctx.launch_count()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
+        e0.record(stream)
         for _ in range(args.steps):
             st = fn()
-        e1.record()
+        e1.record(stream)
         torch.cuda.synchronize()
         sec = e0.elapsed_time(e1) / 1e3
-        if name == "bf16_warm_batched":
+        if headline:
             launches = ctx.launch_count() - l0
             clk.terminate()
             clk.wait()
@@ -545,36 +633,122 @@ def run_full(args, rank: int, world: int) -> None:
         results[name] = dict(views_per_s=len(targets) * args.steps / sec,
                              cg_iterations=int(sum(s.outer_iterations for s in st)),
                              max_gap=float(max(s.gap for s in st)))
-    # per-target error of each arm against the plain FP32 solution, and the centre target's PSNR to the render
+    if world > 1:
+        t = torch.tensor([len(targets) * args.steps / results["learned_batched"]["views_per_s"]], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        results["learned_batched"]["views_per_s"] = len(targets) * args.steps / float(t.item())
+    # every arm against the plain FP32 solver's outputs (same targets)
     ref = [o.cpu().numpy() for o in outs["plain_single"]]
-    for name in ("plain_batched", "bf16_batched", "bf16_warm_batched"):
+    for name in ("plain_batched", "bf16_batched", "learned_batched"):
         got = [o.cpu().numpy() for o in outs[name]]
         results[name]["max_abs_vs_plain_fp32"] = float(max(np.abs(a - b).max() for a, b in zip(got, ref)))
         results[name]["psnr_vs_plain_fp32_min_db"] = float(min(lfrv.psnr(a, b) for a, b in zip(got, ref)))
-    psnr_gt = {name: lfrv.psnr(outs[name][0].cpu().numpy(), sc.gt) for name in outs}
+    centre = {name: outs[name][0].cpu().numpy() for name in outs}
+    psnr_gt = {name: lfrv.psnr(centre[name], sc.gt) for name in outs}
+
+    # the dominant kernel of the plain step: per-kernel device time over one pass of the 32 targets
+    ctx.profile_enable(True)
+    st_prof = [ctx.render_view_dev(j["cfg"], 1, j["d_views"], j["d_depth"], j["cams"], j["target"], j["d_out"])
+               for j in j_ps]
+    prof = ctx.profile()
+    ctx.profile_enable(False)
+    n, N = p.w * p.h, H * W
+    roof, kernels_ms = roofline_of(prof, V, n, N, p.dsf + 1, st_prof, None, len(targets))
+
+    # end to end: the learned + batched arm from pinned host buffers through lfrv_render_views_warm
+    hv = views_bf16.cpu().pin_memory()
+    hd = torch.from_numpy(sc.depth).pin_memory()
+    hos = [torch.empty((3, H, W), dtype=torch.float32).pin_memory() for _ in targets]
+    hjobs = [dict(cfg=cfg16, algorithm=1, d_views=hv.data_ptr(), d_depth=hd.data_ptr(), cams=sc.cams, target=t,
+                  d_out=o.data_ptr()) for t, o in zip(targets, hos)]
+    for _ in range(max(1, args.warmup // 2)):
+        ctx.render_views(hjobs, net)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        ctx.render_views(hjobs, net)
+    e2e_sec = time.perf_counter() - t0  # the call returns after its outputs are in host memory
+    e2e = {"value": world * len(targets) * args.steps / e2e_sec, "unit": "views/s",
+           "h2d_bytes_per_step": int(hv.numel() * 2 + hd.numel() * 4),
+           "d2h_bytes_per_step": int(len(targets) * 3 * H * W * 4)}
+    e2e_match = bool(all(np.array_equal(o.numpy(), w.cpu().numpy()) for o, w in zip(hos, outs["learned_batched"])))
+    del hos
+
+    # CPU legs on the centre target: the FP32 port timed (cpu_baseline), the FP64 oracle on the GPU's warps
+    cpu, vs64 = None, None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        import pyoracle
+
+        tau_g, dpart_g, _ = ctx.warp(sc.depth, sc.cams, targets[0])
+        t0 = time.perf_counter()
+        tau_c, dpart_c, _ = pyoracle.warp(sc.depth, sc.cams, targets[0])
+        pyoracle.ibr_gradient(cfg32, sc.views, tau_c, dpart_c, prec=1)
+        t_cpu = time.perf_counter() - t0
+        del tau_c, dpart_c
+        cpu = {"value": 1.0 / t_cpu, "unit": "views/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "the centre target of the 32 (warp of 80 views + IBR_gradient to gap 1e-4), FP32 CPU "
+                         "restatement of the reference path, OpenMP"}
+        ref64, rst64 = pyoracle.ibr_gradient(cfg32, sc.views, tau_g, dpart_g, prec=0)
+        vs64 = {"target": "centre (rendered ground truth available)", "warps": "the GPU's (lfrv_warp_dev)",
+                "plain_fp32_max_rel_err": rel_err(centre["plain_single"], ref64),
+                "plain_fp32_cg_iterations": st_prof[0].outer_iterations, "fp64_cg_iterations": rst64.outer_iterations,
+                "learned_batched_max_abs_err": float(np.abs(centre["learned_batched"] - ref64).max()),
+                "psnr_to_render_fp64_db": lfrv.psnr(ref64, sc.gt),
+                "psnr_to_render_learned_batched_db": psnr_gt["learned_batched"],
+                "psnr_delta_learned_batched_db": psnr_gt["learned_batched"] - lfrv.psnr(ref64, sc.gt),
+                "psnr_to_render_plain_fp32_db": psnr_gt["plain_single"]}
     if rank == 0:
-        wb = results["bf16_warm_batched"]
-        line = {"metric": "views/sec to energy gap <=1e-4", "value": world * wb["views_per_s"], "unit": "views/s",
-                "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
-                "ms_per_step": 1e3 * len(targets) / wb["views_per_s"], "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "bf16 stacks, f32 iterates, f64 dots",
-                "data": "synthetic (seeded planes + bumps light field)",
+        wb = results["learned_batched"]
+        plain = results["plain_single"]["views_per_s"]
+        line = {"metric": "views/sec to energy gap <=1e-4 (learned+batched vs plain solver, same GB300)",
+                "value": world * wb["views_per_s"], "unit": "views/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * len(targets) / wb["views_per_s"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "bf16 stacks, f32 iterates, f64 dots", "data": "synthetic (seeded planes + bumps light field)",
                 "config": {"workload": wl["name"], "views": V, "input": [p.h, p.w], "target": [H, W],
                            "targets_per_step": len(targets), "scene_generation_seconds": round(t_gen, 1),
                            "features_seconds": round(t_feat, 2), "train_seconds": round(t_train, 2),
                            "train": f"{steps} Adam steps of {bs} random {crop}^2 crops of 4 other targets' features",
+                           "plain_views_per_s": plain, "speedup_vs_plain": wb["views_per_s"] / plain,
                            "modes": results, "psnr_to_render_centre_target": psnr_gt,
-                           "warm_bf16_batched_vs_plain_fp32_single":
-                               wb["views_per_s"] / results["plain_single"]["views_per_s"],
-                           "bf16_batched_vs_plain_fp32_single":
-                               results["bf16_batched"]["views_per_s"] / results["plain_single"]["views_per_s"],
-                           "inputs": "1024^2 views rendered point-sampled (no 2x supersampling) to bound the host "
-                                     "scene generation",
+                           "e2e_outputs_equal_device_call": e2e_match,
                            "l2": "32 targets of 2048^2 from 80 views of 1024^2 exceed L2 (no flush needed)"},
-                "clocks": clocks, "gpu_launches": launches, "roofline": None, "cpu_baseline": None}
+                "vs_fp64": vs64, "clocks": clocks, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+                "e2e": e2e, "kernels_ms_per_step": kernels_ms}
         print(json.dumps(line), flush=True)
     net.close()
     ctx.close()
+
+
+def rel_err(a, b, floor: float = 1e-2) -> float:
+    """Max over pixels of |a - b| / max(|b|, floor)."""
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), floor)))
+
+
+def roofline_of(prof: dict, V: int, n: int, N: int, ks: int, stats, rof_iters, targets: int):
+    """roofline of the dominant kernel in a per-kernel profile (launcher name -> (total ms, launches)) and the
+    per-step milliseconds of every kernel."""
+    dom = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_n = prof[dom]
+    avg_s = dom_ms / 1e3 / dom_n
+    cg_iters = float(np.mean([s.outer_iterations for s in stats])) if stats else 0
+    abytes = algorithmic_bytes(dom, V, n, N, ks, cg_iters=cg_iters, rof_iters=rof_iters or 0)
+    peak, peak_kind = measured_peak_hbm()
+    roof = None
+    if abytes:
+        ach = abytes / avg_s / 1e9
+        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "peak_source": peak_kind, "traffic": NCU_TRAFFIC_BYTES.get((dom, N)),
+                "avg_launch_us": avg_s * 1e6, "algorithmic_bytes_per_launch": abytes}
+        if dom == "cg_persistent" and roof["traffic"]:
+            roof["dram_frac"] = roof["traffic"] / avg_s / 1e9 / peak
+            roof["limiter"] = ("two grid barriers per iteration and the FP64 block sums before them; r and d stay in "
+                               "shared memory, so DRAM moves only the one-time read of g and u")
+    kernels_ms = {k: v[0] / targets for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    return roof, kernels_ms
 
 
 def run_ours(args, rank: int, world: int) -> None:
@@ -634,19 +808,7 @@ def run_ours(args, rank: int, world: int) -> None:
         step()
     prof = ctx.profile()
     ctx.profile_enable(False)
-    dom = max(prof, key=lambda k: prof[k][0])
-    dom_ms, dom_n = prof[dom]
-    avg_s = dom_ms / 1e3 / dom_n
-    abytes = algorithmic_bytes(dom, V, n, N, ks, cg_iters=int(st.outer_iterations), rof_iters=int(cfg.niter))
-    peak, peak_kind = measured_peak_hbm()
-    roof = None
-    if abytes:
-        ach = abytes / avg_s / 1e9
-        roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
-                "peak_source": peak_kind,
-                "traffic": NCU_TRAFFIC_BYTES.get(dom) if args.workload == "c2" else None,
-                "avg_launch_us": avg_s * 1e6,
-                "algorithmic_bytes_per_launch": abytes}
+    roof, kernels_ms = roofline_of(prof, V, n, N, ks, [st], int(cfg.niter), args.steps)
 
     # end to end through the host-buffer C ABI call, pinned host memory
     hv = torch.from_numpy(sc.views).pin_memory()
@@ -666,7 +828,7 @@ def run_ours(args, rank: int, world: int) -> None:
     wall = time.perf_counter() - t0
     e2e_value = world * args.steps / max(e2e_sec, wall)
 
-    cpu = None
+    cpu, vs64 = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
         sys.path.insert(0, str(ROOT / "oracle"))
         import pyoracle
@@ -678,7 +840,14 @@ def run_ours(args, rank: int, world: int) -> None:
         if args.workload == "c1":
             t *= 100.0
         cpu = {"value": 1.0 / t, "unit": "views/s", "cores": os.cpu_count(), "kind": "port",
-               "sample": "one full view (warp + solve) of the same workload, FP32 CPU restatement, OpenMP"}
+               "sample": "one full view (warp + solve) of the same workload, FP32 CPU restatement, OpenMP"
+                         + (" (30 x 30 of the 300 x 300 iterations, time x 100)" if args.workload == "c1" else "")}
+        # the timed step's result against the FP64 oracle on the GPU's warps (once, outside the timed region)
+        tau_g, dpart_g, _ = ctx.warp(sc.depth, sc.cams, sc.target)
+        solve = pyoracle.ibr_gradient if wl["algorithm"] == 1 else pyoracle.ibr_color
+        ref64, rst64 = solve(cfg, sc.views, tau_g, dpart_g, prec=0)
+        vs64 = {"warps": "the GPU's (lfrv_warp_dev)", "max_rel_err": rel_err(out.cpu().numpy(), ref64),
+                "iterations_gpu": stats[-1].outer_iterations, "iterations_fp64": rst64.outer_iterations}
 
     if rank == 0:
         line = {"metric": "views/sec to energy gap <=1e-4", "value": value, "unit": "views/s", "n_gpus": world,
@@ -691,10 +860,11 @@ def run_ours(args, rank: int, world: int) -> None:
                            "l2": "inputs and per-step buffers exceed L2 between steps (no flush needed)",
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "clocks": clocks, "gpu_launches": launches, "roofline": roof, "cpu_baseline": cpu,
+                "vs_fp64": vs64,
                 "e2e": {"value": e2e_value, "unit": "views/s",
                         "h2d_bytes_per_step": int(sc.views.nbytes + sc.depth.nbytes),
                         "d2h_bytes_per_step": int(3 * H * W * 4)},
-                "kernels_ms_per_step": {k: v[0] / args.steps for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}}
+                "kernels_ms_per_step": kernels_ms}
         print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -702,12 +872,16 @@ def run_ours(args, rank: int, world: int) -> None:
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
-    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=None, help="timed steps (default per workload; c5: 5)")
+    ap.add_argument("--warmup", type=int, default=None, help="untimed warm-up steps (>= 3; c5 default 3)")
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="c2", choices=sorted(WORKLOADS))
-    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--workload", default="c5", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline and FP64 error legs")
     args = ap.parse_args()
+    wl = WORKLOADS[args.workload]
+    if args.steps is None:
+        args.steps = wl["steps"]
+    args.warmup = max(3, wl["warmup"] if args.warmup is None else args.warmup)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if args.impl == "reference":
@@ -717,14 +891,8 @@ def main() -> None:
         import torch
 
         torch.distributed.init_process_group("nccl")
-    if args.workload == "c3":
-        run_batch(args, rank, world)
-    elif args.workload == "c4":
-        run_warm(args, rank, world)
-    elif args.workload == "c5":
-        run_full(args, rank, world)
-    else:
-        run_ours(args, rank, world)
+    runner = {"c3": run_batch, "c4": run_warm, "c5": run_full, "net": run_net}.get(args.workload, run_ours)
+    runner(args, rank, world)
     if world > 1:
         import torch
 

@@ -240,6 +240,10 @@ typedef struct lfrv_view_job {
     lfrv_stats *stats;         /* optional */
 } lfrv_view_job;
 int lfrv_render_views_dev(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count);
+/* The same batch from HOST buffers: each job's d_views, d_depth and d_out are host pointers (views BF16 when the
+ * job's cfg->bf16_storage is 1). Input buffers shared by several jobs (same pointer and size, e.g. one light field
+ * seen from many targets) are uploaded once; every output is copied back before the call returns. */
+int lfrv_render_views(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count);
 
 /* ---------------------------------------------------------------- learned warm start
  * No reference counterpart: an addition beside the plain method, which stays unchanged. A 4-scale
@@ -288,6 +292,8 @@ int lfrv_render_view_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_con
  * lanes with their set-up, the network predicts each seed on the context stream, and the shared CG launch starts
  * every seeded job from its prediction with its own anchor. */
 int lfrv_render_views_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_view_job *jobs, int count);
+/* lfrv_render_views_warm_dev from host buffers, as lfrv_render_views. */
+int lfrv_render_views_warm(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_view_job *jobs, int count);
 /* One convolution through the tensor-core kernels: x NHWC BF16 (batch x H x W x Cin), dy NHWC BF16
  * (batch x H/stride x W/stride x Cout), w FP32 Cout x ks x ks x Cin (rounded to BF16 inside), out FP32.
  * mode 0: out = conv(x) (batch x H/s x W/s x Cout); 1: out = the data gradient (batch x H x W x Cin);

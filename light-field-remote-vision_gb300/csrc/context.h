@@ -53,6 +53,8 @@ struct Workspace {
     DevBuf pp_img, pp_vis, pp_tmp, pp_orig;
     // host staging for the host-buffer entry points
     DevBuf in_views, in_tau, in_dpart, in_init, out_img;
+    // host-buffer batched calls: one device copy per distinct light field (views, depth) and the outputs
+    DevBuf hb_in, hb_out;
 };
 
 // Per-kernel CUDA-event timing: a fixed pool of event pairs recorded in-stream. When the pool is full the

@@ -1863,6 +1863,72 @@ extern "C" int lfrv_render_views_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, co
     LFRV_API_END
 }
 
+// Host-buffer batched targets: the jobs' views, depth maps and outputs are host pointers. Each distinct input
+// buffer (same pointer and size, as when many targets share one light field) is uploaded once into one device
+// pool; the batch runs as lfrv_render_views_dev would; the outputs are copied back before the call returns.
+static void render_views_host(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv_warmstart *net) {
+    if (count <= 0 || !jobs) raise(LFRV_E_ARG, "empty batch");
+    struct Input {
+        const void *host;
+        size_t bytes, off;
+    };
+    std::vector<Input> inputs;
+    auto place = [&](const void *p, size_t bytes) -> size_t {
+        for (const Input &in : inputs)
+            if (in.host == p && in.bytes == bytes) return in.off;
+        const size_t off = inputs.empty() ? 0 : (inputs.back().off + inputs.back().bytes + 255) / 256 * 256;
+        inputs.push_back({p, bytes, off});
+        return off;
+    };
+    std::vector<size_t> off_views(count), off_depth(count), off_out(count);
+    size_t out_bytes = 0;
+    for (int j = 0; j < count; ++j) {
+        const lfrv_view_job &J = jobs[j];
+        if (!J.cfg || !J.d_views || !J.d_depth || !J.d_out) raise(LFRV_E_ARG, "job %d: null argument", j);
+        const Geometry G = geometry(*J.cfg);
+        const size_t vb = (size_t)G.V * 3 * G.n * (J.cfg->bf16_storage ? 2 : 4);
+        off_views[j] = place(J.d_views, vb);
+        off_depth[j] = place(J.d_depth, (size_t)G.V * 3 * G.n * sizeof(float));
+        off_out[j] = out_bytes;
+        out_bytes += (3 * G.N * sizeof(float) + 255) / 256 * 256;
+    }
+    const size_t in_bytes = inputs.back().off + inputs.back().bytes;
+    c->ws.hb_in.ensure(in_bytes);
+    c->ws.hb_out.ensure(out_bytes);
+    char *din = c->ws.hb_in.as<char>(), *dout = c->ws.hb_out.as<char>();
+    for (const Input &in : inputs)
+        LFRV_CUDA(cudaMemcpyAsync(din + in.off, in.host, in.bytes, cudaMemcpyHostToDevice, c->stream));
+    std::vector<lfrv_view_job> dj(jobs, jobs + count);
+    for (int j = 0; j < count; ++j) {
+        dj[j].d_views = reinterpret_cast<const float *>(din + off_views[j]);
+        dj[j].d_depth = reinterpret_cast<const float *>(din + off_depth[j]);
+        dj[j].d_out = reinterpret_cast<float *>(dout + off_out[j]);
+    }
+    render_views(c, dj.data(), count, net);
+    for (int j = 0; j < count; ++j) {
+        const Geometry G = geometry(*jobs[j].cfg);
+        LFRV_CUDA(cudaMemcpyAsync(jobs[j].d_out, dout + off_out[j], 3 * G.N * sizeof(float), cudaMemcpyDeviceToHost,
+                                  c->stream));
+    }
+    sync(c);
+}
+
+extern "C" int lfrv_render_views(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    render_views_host(ctx, jobs, count, nullptr);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_render_views_warm(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_view_job *jobs, int count) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!net) return fail(LFRV_E_ARG, "null network");
+    render_views_host(ctx, jobs, count, net);
+    warmstart_check(net);
+    LFRV_API_END
+}
+
 static cudaStream_t copy_stream(lfrv_ctx *c) {
     if (!c->copy_stream) {
         LFRV_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));

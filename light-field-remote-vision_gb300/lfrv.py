@@ -114,6 +114,7 @@ EXPORTED = [
     "lfrv_ctx_launch_count", "lfrv_ctx_profile", "lfrv_ctx_profile_read", "lfrv_depth_radial_to_ortho",
     "lfrv_depth_radial_to_ortho_dev", "lfrv_warp_from_depth", "lfrv_warp_from_depth_dev", "lfrv_warp", "lfrv_warp_dev", "lfrv_ibr_color", "lfrv_ibr_color_dev",
     "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_render_views_dev",
+    "lfrv_render_views", "lfrv_render_views_warm",
     "lfrv_warmstart_param_count", "lfrv_warmstart_create", "lfrv_warmstart_destroy", "lfrv_warmstart_get_params",
     "lfrv_warmstart_set_params", "lfrv_warmstart_features_dev", "lfrv_warmstart_forward_dev",
     "lfrv_warmstart_train_step_dev", "lfrv_warmstart_gradients_dev", "lfrv_render_view_warm_dev", "lfrv_render_views_warm_dev", "lfrv_conv_bf16_dev",
@@ -380,7 +381,12 @@ class Context:
                                         cameras_array(cams), C.byref(target), C.c_void_p(d_out), C.byref(st)))
         return st
 
-    def render_views_dev(self, jobs, net: "WarmStart | None" = None, trace: int = 0) -> list:
+    def render_views(self, jobs, net: "WarmStart | None" = None, trace: int = 0) -> list:
+        """Batched targets from host buffers (lfrv_render_views / lfrv_render_views_warm): each job's d_views,
+        d_depth and d_out are HOST pointers (ints); shared inputs are uploaded once. Returns one Stats per job."""
+        return self.render_views_dev(jobs, net, trace, host=True)
+
+    def render_views_dev(self, jobs, net: "WarmStart | None" = None, trace: int = 0, host: bool = False) -> list:
         """Batched targets: jobs is a list of dicts with cfg, algorithm, d_views, d_depth, cams, target, d_out
         (device pointers as ints). With a warm-start network the IBR_gradient jobs are seeded by it
         (lfrv_render_views_warm_dev). Returns one Stats per job (with `trace` entries of energy trace each)."""
@@ -396,9 +402,10 @@ class Context:
                              C.cast(cams, C.POINTER(Camera)), C.pointer(tgt), C.c_void_p(j["d_out"]),
                              C.pointer(stats[i]))
         if net is None:
-            _check(LIB.lfrv_render_views_dev(self._h, arr, len(jobs)))
+            _check((LIB.lfrv_render_views if host else LIB.lfrv_render_views_dev)(self._h, arr, len(jobs)))
         else:
-            _check(LIB.lfrv_render_views_warm_dev(self._h, net._h, arr, len(jobs)))
+            fn = LIB.lfrv_render_views_warm if host else LIB.lfrv_render_views_warm_dev
+            _check(fn(self._h, net._h, arr, len(jobs)))
         return stats
 
     def render_view(self, cfg: Config, algorithm: int, views, depth, cams, target: Camera, out=None,
@@ -629,6 +636,8 @@ def _declare() -> None:
     LIB.lfrv_depth_radial_to_ortho.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(Camera), _F]
     LIB.lfrv_depth_radial_to_ortho_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(Camera), vp]
     LIB.lfrv_render_views_dev.argtypes = [vp, C.POINTER(ViewJob), C.c_int]
+    LIB.lfrv_render_views.argtypes = [vp, C.POINTER(ViewJob), C.c_int]
+    LIB.lfrv_render_views_warm.argtypes = [vp, vp, C.POINTER(ViewJob), C.c_int]
     LIB.lfrv_cg_solve_static.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp, _I, _D]
     LIB.lfrv_png_read.argtypes = [C.c_char_p, _I, _I, _F, C.c_size_t]
     LIB.lfrv_png_write.argtypes = [C.c_char_p, C.c_int, C.c_int, _F]

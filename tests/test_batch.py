@@ -49,3 +49,68 @@ def test_batch_matches_single_targets():
                 assert np.max(np.abs(got - want)) < 1e-5
             else:
                 np.testing.assert_array_equal(got, want)
+
+
+def test_batch_jobs_match_fp64_oracle():
+    """Every job of a batch (IBR_gradient with the batched CG, IBR_color run in the same call) against the FP64 CPU
+    oracle on the warps the GPU computed, at a fixed iteration count: 1e-4 max relative error per pixel (floor
+    1e-2), and the batched CG's energy trace against the oracle's to 1e-4 relative."""
+    import torch
+
+    import pyoracle
+    from scenes import rel_err
+
+    specs = [(2, 32, 1, dict(cg_gap_tol=0.0, cg_max_iter=12)), (1, 48, 1, dict(cg_gap_tol=0.0, cg_max_iter=9)),
+             (2, 24, 0, dict(niter=5)), (1, 40, 1, dict(cg_gap_tol=0.0, cg_max_iter=15))]
+    jobs, scenes = [], []
+    for preset, w, alg, kw in specs:
+        sc = scene(preset, w)
+        cfg = (gradient_config(sc, **kw) if alg == 1 else color_config(sc, **kw))
+        jobs.append(_job(torch, sc, cfg, alg))
+        scenes.append(sc)
+    with lfrv.Context(0) as ctx:
+        torch.cuda.synchronize()
+        stats = ctx.render_views_dev([dict(cfg=j["cfg"], algorithm=j["algorithm"], d_views=j["views"].data_ptr(),
+                                           d_depth=j["depth"].data_ptr(), cams=j["cams"], target=j["target"],
+                                           d_out=j["out"].data_ptr()) for j in jobs], trace=32)
+        torch.cuda.synchronize()
+        for j, st, sc in zip(jobs, stats, scenes):
+            tau, dpart, _ = ctx.warp(sc.depth, sc.cams, sc.target)
+            solve = pyoracle.ibr_gradient if j["algorithm"] == 1 else pyoracle.ibr_color
+            ref, rst = solve(j["cfg"], sc.views, tau, dpart, prec=0, trace=32)
+            assert st.outer_iterations == rst.outer_iterations
+            assert rel_err(j["out"].cpu().numpy(), ref) <= 1e-4
+            tr, rtr = st.trace(), rst.trace()
+            assert len(tr) == len(rtr) == st.outer_iterations
+            assert np.max(np.abs(tr - rtr) / np.abs(rtr)) <= 1e-4
+
+
+def test_host_buffer_batch_equals_device_batch():
+    """lfrv_render_views (host buffers, shared inputs uploaded once) gives lfrv_render_views_dev's outputs bit for
+    bit; two targets share one light field."""
+    import copy
+
+    import torch
+
+    sc = scene(2, 32)
+    cfg = gradient_config(sc, cg_gap_tol=1e-6)
+    t2 = copy.copy(sc.target)
+    t2.t[0] += 0.01
+    H, W = cfg.h * cfg.dsf, cfg.w * cfg.dsf
+    views = np.ascontiguousarray(sc.views)
+    depth = np.ascontiguousarray(sc.depth)
+    outs = [np.zeros((3, H, W), np.float32) for _ in range(2)]
+    dv, dd = torch.from_numpy(views).cuda(), torch.from_numpy(depth).cuda()
+    douts = [torch.zeros((3, H, W), device="cuda") for _ in range(2)]
+    with lfrv.Context(0) as ctx:
+        st_h = ctx.render_views([dict(cfg=cfg, algorithm=1, d_views=views.ctypes.data, d_depth=depth.ctypes.data,
+                                      cams=sc.cams, target=t, d_out=o.ctypes.data) for t, o in zip((sc.target, t2), outs)])
+        torch.cuda.synchronize()
+        st_d = ctx.render_views_dev([dict(cfg=cfg, algorithm=1, d_views=dv.data_ptr(), d_depth=dd.data_ptr(),
+                                          cams=sc.cams, target=t, d_out=o.data_ptr())
+                                     for t, o in zip((sc.target, t2), douts)])
+        torch.cuda.synchronize()
+    for o, d, a, b in zip(outs, douts, st_h, st_d):
+        np.testing.assert_array_equal(o, d.cpu().numpy())
+        assert a.outer_iterations == b.outer_iterations
+    assert not np.array_equal(outs[0], outs[1])
