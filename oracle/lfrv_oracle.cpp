@@ -19,6 +19,8 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -844,6 +846,231 @@ void color_fista_iteration(ColorState<T> &S) {
     S.alpha = alpha_new;
 }
 
+// ------------------------------------------------------------------ IBR_color, corrected mode
+// No reference counterpart: the objective the reference's ISTA step (sources/optimization.cu:1751-1832) aims at,
+// solved to a certified primal-dual gap.
+//   E(u) = f(u) + lambda J_g(u) over the box [0, 1]^{3N},
+//   f(u) = alpha sigma^2 / 2 sum_i sum_{m in S_i} w_im |A_i u - v_i|^2_m   (S_i: the splat set of view i, the same
+//          set the data term's gradient splats over, so that grad f = alpha sigma^2 sum_i A_i^T w_i (A_i u - v_i)),
+//   J_g(u) = sum_x g_x |grad u(x)|_F (forward differences with zero at the last column / row, Frobenius norm over
+//          the 3 channels and 2 directions: the weighted TV_F whose dual ball vtv_rof.cu:280-320 projects onto).
+// Solver: FISTA in the diagonal metric D = max(alpha sigma^2 sum_i A_i^T w_i, kTvDelta), which majorises the
+// Hessian of f (rows of A_i sum to 1, so by Cauchy-Schwarz (A_i u)^2 <= A_i (u^2)), with the momentum restarted
+// whenever the energy rises (function-value restart, O'Donoghue and Candes 2015). Each step is the weighted ROF
+// problem min_u lambda J_g(u) + 1/2 |u - F|^2_D over the box with F = y - grad f(y) / D, solved by kTvInner
+// iterations of the fast gradient projection on its dual (|p(x)| <= g_x), warm-started from the last dual.
+// Certificate: for |p| <= g and u in the box, with c = grad f(u) - lambda div p,
+//   E(u) - E* <= gap(u, p) = lambda sum_x [g_x |grad u(x)|_F - <grad u(x), p(x)>] + sum [u c - min(0, c)],
+// (the Fenchel dual of the problem with the data term's dual variable at its optimum for u). The solver stops
+// when gap / E <= cfg.cg_gap_tol or after cfg.niter outer iterations.
+constexpr int kTvInner = 200;
+constexpr double kTvDelta = 1.0;
+
+// grad f(u) (3 planes) and f(u): residuals over the splat set.
+template <class T>
+double tv_grad_f(const ColorState<T> &S, const Vec<T> *U, Vec<T> *gf) {
+    const size_t n = (size_t)S.P.w * S.P.h, N = S.N;
+    const double as2 = (double)S.cfg.dt_alpha * (double)S.cfg.sigma_sensor * (double)S.cfg.sigma_sensor;
+    for (int c = 0; c < 3; ++c) std::fill(gf[c].begin(), gf[c].end(), T(0));
+    double f = 0;
+    Vec<T> r0(n), r1(n), r2(n);
+    for (const auto &vw : S.P.views) {
+        T *r[3] = {r0.data(), r1.data(), r2.data()};
+#pragma omp parallel for reduction(+ : f)
+        for (long long mm = 0; mm < (long long)n; ++mm) {
+            const size_t m = (size_t)mm;
+            for (int c = 0; c < 3; ++c) r[c][m] = 0;
+            if (!in_splat(vw.tx[m], vw.ty[m], S.P.W, S.P.H)) continue;
+            const Footprint<T> &fp = vw.fp[m];
+            T a[3] = {0, 0, 0};
+            for (int j = 0; j < fp.ks; ++j)
+                for (int i = 0; i < fp.ks; ++i) {
+                    const int x = fp.x0 + j, y = fp.y0 + i;
+                    if (0 <= x && x <= S.P.W - 1 && 0 <= y && y <= S.P.H - 1)
+                        for (int c = 0; c < 3; ++c) a[c] += fp.A[fp.ks * i + j] * U[c][(size_t)y * S.P.W + x];
+                }
+            for (int c = 0; c < 3; ++c) {
+                const T d = a[c] - vw.img[c * n + m];
+                f += 0.5 * as2 * (double)vw.w[m] * (double)d * (double)d;
+                r[c][m] = vw.w[m] * d;
+            }
+        }
+        const T *in[3] = {r0.data(), r1.data(), r2.data()};
+        T *out[3] = {gf[0].data(), gf[1].data(), gf[2].data()};
+        splat(S.P, vw, 3, in, out, (T *)nullptr, (const T *)nullptr);
+    }
+    for (int c = 0; c < 3; ++c)
+        for (size_t o = 0; o < N; ++o) gf[c][o] = (T)(as2 * (double)gf[c][o]);
+    return f;
+}
+
+// div of a dual field (the negative adjoint of the forward gradient with zero at the last column / row).
+template <class T>
+inline T tv_div_at(const T *px, const T *py, int W, int H, int x, int y) {
+    const size_t o = (size_t)y * W + x;
+    T d = 0;
+    if (x < W - 1) d += px[o];
+    if (x > 0) d -= px[o - 1];
+    if (y < H - 1) d += py[o];
+    if (y > 0) d -= py[o - W];
+    return d;
+}
+
+// kTvInner iterations of FGP on the dual of min_u J_g(u) + sum_x (1 / (2 lam_x)) |u(x) - F(x)|^2 over the box,
+// lam_x = lambda / D_x: u(q) = clamp(F + lam div q, 0, 1), p <- proj_{|.| <= g}(q + grad u(q) / L_x),
+// q <- p + (s - 1) / s' (p - p_old). The step is per pixel: the dual's Hessian grad diag(lam) grad^T is at most
+// diag(L) with L_x = 8 max(lam_x, lam_{x+1}, lam_{x+W}) (each dual entry enters the divergence at two pixels, each
+// divergence has four terms), so the fast gradient projection converges in that metric; the ball projection stays
+// a radial scaling since L_x is one scalar for the six entries of pixel x. P: px (3 planes), py (3 planes).
+template <class T>
+void tv_fgp(int W, int H, const Vec<T> *F, const Vec<T> &lam, const Vec<T> &g, const Vec<T> &Linv, Vec<T> *P,
+            int iters, Vec<T> *U) {
+    const size_t N = (size_t)W * H;
+    Vec<T> Q[6], Pn[6], u[3];
+    for (int k = 0; k < 6; ++k) Q[k] = P[k], Pn[k].assign(N, 0);
+    for (int c = 0; c < 3; ++c) u[c].assign(N, 0);
+    double s = 1;
+    auto primal = [&](const Vec<T> *q, Vec<T> *out) {
+        for (int c = 0; c < 3; ++c) {
+#pragma omp parallel for
+            for (int y = 0; y < H; ++y)
+                for (int x = 0; x < W; ++x) {
+                    const size_t o = (size_t)y * W + x;
+                    const T v = F[c][o] + lam[o] * tv_div_at(q[c].data(), q[3 + c].data(), W, H, x, y);
+                    out[c][o] = std::min((T)1, std::max((T)0, v));
+                }
+        }
+    };
+    for (int it = 0; it < iters; ++it) {
+        primal(Q, u);
+        const double s1 = 0.5 * (1.0 + std::sqrt(1.0 + 4.0 * s * s));
+        const T beta = (T)((s - 1.0) / s1);
+#pragma omp parallel for
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) {
+                const size_t o = (size_t)y * W + x;
+                T v[6];
+                T nrm = 0;
+                for (int c = 0; c < 3; ++c) {
+                    const T gxv = x < W - 1 ? u[c][o + 1] - u[c][o] : T(0);
+                    const T gyv = y < H - 1 ? u[c][o + W] - u[c][o] : T(0);
+                    v[c] = Q[c][o] + gxv * Linv[o];
+                    v[3 + c] = Q[3 + c][o] + gyv * Linv[o];
+                    nrm += v[c] * v[c] + v[3 + c] * v[3 + c];
+                }
+                nrm = std::sqrt(nrm);
+                const T sc = nrm > g[o] ? g[o] / nrm : T(1);
+                for (int k = 0; k < 6; ++k) {
+                    const T pn = v[k] * sc;
+                    Q[k][o] = pn + beta * (pn - P[k][o]);
+                    Pn[k][o] = pn;
+                }
+            }
+        for (int k = 0; k < 6; ++k) std::swap(P[k], Pn[k]);
+        s = s1;
+    }
+    primal(P, U);
+}
+
+// E(u) and the certified gap for the dual p (see above); J_g(u) through *J.
+template <class T>
+double tv_gap(int W, int H, const Vec<T> *U, const Vec<T> *gf, const Vec<T> *P, const Vec<T> &g, double lambda,
+              double *J) {
+    double tv = 0, inner = 0, box = 0;
+#pragma omp parallel for reduction(+ : tv, inner, box)
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t o = (size_t)y * W + x;
+            double n2 = 0;
+            for (int c = 0; c < 3; ++c) {
+                const double gxv = x < W - 1 ? (double)U[c][o + 1] - (double)U[c][o] : 0.0;
+                const double gyv = y < H - 1 ? (double)U[c][o + W] - (double)U[c][o] : 0.0;
+                n2 += gxv * gxv + gyv * gyv;
+                inner += gxv * (double)P[c][o] + gyv * (double)P[3 + c][o];
+                const double cc =
+                    (double)gf[c][o] - lambda * (double)tv_div_at(P[c].data(), P[3 + c].data(), W, H, x, y);
+                box += (double)U[c][o] * cc - std::min(0.0, cc);
+            }
+            tv += (double)g[o] * std::sqrt(n2);
+        }
+    *J = tv;
+    return lambda * (tv - inner) + box;
+}
+
+// One meta iteration of the corrected IBR_color solve on S.U (weights and g already set). Returns the outer
+// iterations run; *E_out, *gap_out: energy and relative gap of the returned iterate. trace: E after each outer
+// iteration (and of the start), at most trace_cap entries from trace_pos on.
+template <class T>
+int tv_solve(ColorState<T> &S, int max_outer, double tol, double *E_out, double *gap_out, double *trace,
+             int trace_cap, int *trace_pos, const Vec<T> *P0 = nullptr) {
+    const int W = S.P.W, H = S.P.H;
+    const size_t N = S.N;
+    const double lambda = (double)S.cfg.lambda;
+    const double as2 = (double)S.cfg.dt_alpha * (double)S.cfg.sigma_sensor * (double)S.cfg.sigma_sensor;
+    // metric D and the per-pixel prox parameter lambda / D
+    Vec<T> Dm(N, T(0)), lam(N);
+    for (const auto &vw : S.P.views) {
+        const T *in[1] = {vw.w.data()};
+        T *out[1] = {Dm.data()};
+        splat(S.P, vw, 1, in, out, (T *)nullptr, (const T *)nullptr);
+    }
+    for (size_t o = 0; o < N; ++o) {
+        Dm[o] = (T)std::max(as2 * (double)Dm[o], kTvDelta);
+        lam[o] = (T)(lambda / (double)Dm[o]);
+    }
+    Vec<T> Linv(N);
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t o = (size_t)y * W + x;
+            T m = lam[o];
+            if (x < W - 1) m = std::max(m, lam[o + 1]);
+            if (y < H - 1) m = std::max(m, lam[o + W]);
+            Linv[o] = (T)(1.0 / (8.0 * (double)m));
+        }
+    Vec<T> u[3], up[3], gf[3], gfp[3], Fy[3], P[6];
+    for (int c = 0; c < 3; ++c) {
+        u[c].resize(N);
+        for (size_t o = 0; o < N; ++o) u[c][o] = std::min((T)1, std::max((T)0, S.U[c][o]));
+        up[c] = u[c];
+        gf[c].assign(N, 0);
+        gfp[c].assign(N, 0);
+        Fy[c].assign(N, 0);
+    }
+    for (int k = 0; k < 6; ++k) P[k] = P0 ? P0[k] : Vec<T>(N, T(0));
+    double t = 1.0, E = 0, gap = 1e300, E_prev = 1e300;
+    int k;
+    for (k = 0;; ++k) {
+        const double f = tv_grad_f(S, u, gf);
+        double J = 0;
+        const double g_abs = tv_gap(W, H, u, gf, P, S.g, lambda, &J);
+        E = f + lambda * J;
+        gap = E > 0 ? g_abs / E : 1e300;
+        if (trace && *trace_pos < trace_cap) trace[(*trace_pos)++] = E;
+        if (k >= max_outer || (tol > 0 && gap <= tol)) break;
+        if (E > E_prev) t = 1.0;  // function-value restart of the momentum (O'Donoghue and Candes)
+        E_prev = E;
+        // FISTA step: y = u + theta (u - u_prev); grad f(y) = (1 + theta) grad f(u) - theta grad f(u_prev)
+        const double t1 = 0.5 * (1.0 + std::sqrt(1.0 + 4.0 * t * t));
+        const double theta = k == 0 ? 0.0 : (t - 1.0) / t1;
+        for (int c = 0; c < 3; ++c)
+            for (size_t o = 0; o < N; ++o) {
+                const double y = (double)u[c][o] + theta * ((double)u[c][o] - (double)up[c][o]);
+                const double gy = (1.0 + theta) * (double)gf[c][o] - theta * (double)gfp[c][o];
+                Fy[c][o] = (T)(y - gy / (double)Dm[o]);
+            }
+        t = t1;
+        for (int c = 0; c < 3; ++c) {
+            std::swap(up[c], u[c]);
+            std::swap(gfp[c], gf[c]);
+        }
+        tv_fgp(W, H, Fy, lam, S.g, Linv, P, kTvInner, u);
+    }
+    for (int c = 0; c < 3; ++c) S.U[c] = u[c];
+    *E_out = E;
+    *gap_out = gap;
+    return k;
+}
+
 // sr_compare_images, sources/super-resolution.cpp:16-51
 template <class T>
 int moving_pixels(const ColorState<T> &S, const Vec<T> prev[3]) {
@@ -877,9 +1104,21 @@ void ibr_color(const lfrv_config &cfg, const T *views, const T *tau, int tau_ch,
     const float PERCENT_MOVING = (float)0.01;
     T energy = 0, previous_energy = 0, previous_energy_reweight = 0;
     int r, total_k = 0, reason = 0;
+    double tv_gap_last = 0;
+    int trace_pos = 0;
+    const bool traced = st && st->energy_trace && st->trace_capacity > 0;
     for (r = 0; r < cfg.nmeta_iter; ++r) {
         color_compute_weights(S);
         color_regularizer(S);
+        if (!cfg.faithful) {  // corrected mode: the true objective to a certified gap
+            double Ec = 0;
+            total_k += tv_solve(S, cfg.niter, cfg.cg_gap_tol, &Ec, &tv_gap_last, traced ? st->energy_trace : nullptr,
+                                traced ? st->trace_capacity : 0, &trace_pos);
+            energy = (T)Ec;
+            reason = (cfg.cg_gap_tol > 0 && tv_gap_last <= cfg.cg_gap_tol) ? 4 : 0;
+            if (traced) st->trace_length = trace_pos;
+            continue;
+        }
         energy = color_energy(S);
         previous_energy = energy;
         int k;
@@ -909,7 +1148,7 @@ void ibr_color(const lfrv_config &cfg, const T *views, const T *tau, int tau_ch,
             }
             for (int c = 0; c < 3; ++c) prev[c] = S.U[c];
         }
-        if (!cfg.early_exit) continue;
+        if (!cfg.early_exit || !cfg.faithful) continue;
         if ((double)energy < EPS) {
             if ((double)previous_energy_reweight < EPS) break;
             previous_energy_reweight = energy;
@@ -925,6 +1164,7 @@ void ibr_color(const lfrv_config &cfg, const T *views, const T *tau, int tau_ch,
         st->meta_iterations = std::min(r + 1, cfg.nmeta_iter);
         st->stop_reason = reason;
         st->energy = (double)energy;
+        st->gap = cfg.faithful ? 0.0 : tv_gap_last;
     }
 }
 
