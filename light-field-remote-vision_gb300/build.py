@@ -33,7 +33,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-std=c++17", "-O3", "-lineinfo", f"-I{INCLUDE}", f"-I{CSRC}",
                "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp"]
 LIB_SOURCES = ["errors.cpp", "io.cpp", "png.cpp", "synth.cpp", "host.cpp", "learn.cpp",
-               "kernels_solver.cu", "kernels_warp.cu", "kernels_pushpull.cu", "kernels_cg.cu", "kernels_learn.cu"]
+               "kernels_solver.cu", "kernels_tv.cu", "kernels_warp.cu", "kernels_pushpull.cu", "kernels_cg.cu", "kernels_learn.cu"]
 
 
 def _have_zlib() -> bool:

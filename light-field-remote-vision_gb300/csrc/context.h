@@ -55,6 +55,8 @@ struct Workspace {
     DevBuf in_views, in_tau, in_dpart, in_init, out_img;
     // host-buffer batched calls: one device copy per distinct light field (views, depth) and the outputs
     DevBuf hb_in, hb_out;
+    // corrected IBR_color: iterates, data gradients, metric and the dual / momentum fields (39 N floats)
+    DevBuf tv;
 };
 
 // Per-kernel CUDA-event timing: a fixed pool of event pairs recorded in-stream. When the pool is full the

@@ -259,4 +259,54 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &g
     return grid_sync(gb, generation, gridDim.x * gridDim.y);
 }
 
+// ---------------------------------------------------------------------- A^T gathers (per target pixel)
+struct SplatSrc {
+    const float *ch[3];   // payload channel c of view v at ch[c] + v * stride[c]
+    size_t stride[3];
+    const float *scale;   // optional per-source factor (weights), stride n per view
+};
+
+// Accumulates sum_entries A * payload and sum_entries A (times the optional scale) for target (x, y).
+template <int KS, int NCH>
+__device__ __forceinline__ void splat_accumulate(int x, int y, int W, int H, int n, int dsf, int BW,
+                                                 const unsigned int *__restrict__ start,
+                                                 const unsigned int *__restrict__ entries,
+                                                 const float *__restrict__ tau, const SplatSrc &src, float acc[3],
+                                                 float &norm) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) acc[c] = 0.f;
+    norm = 0.f;
+#pragma unroll
+    for (int i = 0; i < KS; ++i) {
+#pragma unroll
+        for (int j = 0; j < KS; ++j) {
+            const int ax = x - j, ay = y - i;  // anchor whose tap (j, i) lands on (x, y)
+            const size_t b = (size_t)(ay + KS - 1) * BW + (ax + KS - 1);
+            const unsigned int s = __ldg(start + b), e = __ldg(start + b + 1);
+            for (unsigned int k = s; k < e; ++k) {
+                const unsigned int ent = __ldg(entries + k);
+                const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
+                const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
+                float raw;
+                float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw);
+                if (src.scale) A = __ldg(src.scale + (size_t)v * n + m) * A;
+                norm += A;
+#pragma unroll
+                for (int c = 0; c < NCH; ++c) acc[c] += A * __ldg(src.ch[c] + (size_t)v * src.stride[c] + m);
+            }
+        }
+    }
+}
+
+
+// Instantiates a kernel template on the footprint size ks = dsf + 1 (2..5).
+#define LFRV_KS_DISPATCH(ks, KERNEL, GRID, BLOCK, STREAM, ...)                          \
+    switch (ks) {                                                                       \
+        case 2: KERNEL<2><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
+        case 3: KERNEL<3><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
+        case 4: KERNEL<4><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
+        case 5: KERNEL<5><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
+        default: break;                                                                 \
+    }
+
 }  // namespace lfrv

@@ -335,10 +335,10 @@ static void sobel_target(lfrv_ctx *c, const Geometry &G, const float *U, float *
 
 // Weighted residuals of every view at U (and the intensity energy into sums[slot]).
 static void residual(lfrv_ctx *c, const Geometry &G, const float *U, const float *img, const float *tau2,
-                     const float *wgt, float s2, float *res, int slot) {
+                     const float *wgt, float s2, float *res, int slot, bool splat_set = false) {
     const int np = residual_partials(G);
     double *part = partial_buf(c, np);
-    launch_residual(G, U, img, tau2, wgt, s2, res, part, c->stream, c->launches);
+    launch_residual(G, U, img, tau2, wgt, s2, res, part, c->stream, c->launches, splat_set);
     check_launch("residual");
     reduce_to(c, np, part, slot);
 }
@@ -446,6 +446,8 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
                         const float *init, float *out, lfrv_stats *st) {
     check_solver_options(cfg);
     if (cfg.bf16_storage) raise(LFRV_E_ARG, "bf16_storage applies to IBR_gradient only");
+    if (!cfg.faithful && cfg.dt_beta != 0.0f)
+        raise(LFRV_E_ARG, "corrected IBR_color solves the intensity objective: dt_beta must be 0");
     const Geometry G = geometry(cfg);
     const size_t N = G.N;
     cudaStream_t s = c->stream;
@@ -545,6 +547,60 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         return (int)v[2];
     };
 
+    // corrected mode: the true TV_F objective to a certified primal-dual gap (kernels_tv.cu); one call per meta
+    // iteration on ws.U, returning the outer iterations run. Trace entries (the energy of every iterate, the start
+    // included) are written to the caller's buffer from the host, where the energy is read for the stop test.
+    double tv_gap_last = 0.0, tv_E = 0.0;
+    int tv_trace_pos = 0;
+    auto tv_meta = [&](int meta) -> int {
+        const size_t N3 = 3 * N;
+        ws.tv.ensure(sizeof(float) * 39 * N);
+        float *u = ws.tv.as<float>(), *up = u + N3, *gf = up + N3, *gfp = gf + N3, *D = gfp + N3, *lam = D + N,
+              *linv = lam + N, *P0 = linv + N, *P1 = P0 + 6 * N, *Q0 = P1 + 6 * N, *Q1 = Q0 + 6 * N;
+        const float as2 = cfg.dt_alpha * s2;
+        launch_tv_metric(G, B, tau2, b.wgt, as2, cfg.lambda, D, lam, linv, s, c->launches);
+        check_launch("tv metric");
+        launch_tv_clamp(N3, ws.U.as<float>(), u, s, c->launches);
+        if (meta == 0) LFRV_CUDA(cudaMemsetAsync(P0, 0, sizeof(float) * 6 * N, s));
+        const int npart = tv_gap_partials(G.W, G.H);
+        const double tol = cfg.cg_gap_tol;
+        double t = 1.0, E_prev = 1e300;
+        int k;
+        for (k = 0;; ++k) {
+            residual(c, G, u, img, tau2, b.wgt, s2, b.res, 1, true);
+            launch_tv_gradf(G, B, tau2, b.res, as2, gf, s, c->launches);
+            check_launch("tv data gradient");
+            double *part = partial_buf(c, 3 * (size_t)npart);
+            launch_tv_gap(G.W, G.H, u, gf, P0, b.g, cfg.lambda, part, s, c->launches);
+            check_launch("tv gap");
+            for (int q = 0; q < 3; ++q) reduce_to(c, npart, part + (size_t)q * npart, 4 + q);
+            double sums[7];
+            read_sums(c, sums, 7);
+            const double f = 0.5 * (double)cfg.dt_alpha * sums[1];
+            tv_E = f + (double)cfg.lambda * sums[4];
+            const double gap_abs = (double)cfg.lambda * (sums[4] - sums[5]) + sums[6];
+            tv_gap_last = tv_E > 0 ? gap_abs / tv_E : 1e300;
+            if (trace && tv_trace_pos < trace_cap) st->energy_trace[tv_trace_pos++] = tv_E;
+            if (!std::isfinite(tv_E) || !std::isfinite(tv_gap_last))
+                raise(LFRV_E_NONFINITE, "non-finite energy in the corrected IBR_color solve");
+            if (k >= cfg.niter || (tol > 0 && tv_gap_last <= tol)) break;
+            if (tv_E > E_prev) t = 1.0;  // function-value restart of the momentum
+            E_prev = tv_E;
+            const double t1 = 0.5 * (1.0 + std::sqrt(1.0 + 4.0 * t * t));
+            const float theta = (float)((t - 1.0) / t1);
+            t = t1;
+            launch_tv_fstep(G.W, G.H, u, up, gf, gfp, D, theta, b.F, s, c->launches);
+            check_launch("tv step");
+            std::swap(u, up);
+            std::swap(gf, gfp);
+            const GridBarrier gb = fresh_barrier(c);
+            LFRV_CUDA(launch_tv_fgp(G.W, G.H, kTvInnerIterations, b.F, lam, linv, b.g, P0, P1, Q0, Q1, u, gb, s,
+                                    c->launches));
+        }
+        LFRV_CUDA(cudaMemcpyAsync(ws.U.p, u, sizeof(float) * N3, cudaMemcpyDeviceToDevice, s));
+        return k;
+    };
+
     float E = 0.0f, E_prev = 0.0f, E_prev_reweight = 0.0f;
     int total_k = 0, reason = 0, r = 0;
     const bool track = cfg.early_exit != 0;
@@ -555,6 +611,12 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         check_launch("regularizer weight");
         launch_blur(G.W, G.H, b.g0, b.tmp, b.g, s, c->launches);
         check_launch("blur");
+        if (!faithful) {
+            total_k += tv_meta(r);
+            E = (float)tv_E;
+            reason = (cfg.cg_gap_tol > 0 && tv_gap_last <= cfg.cg_gap_tol) ? 4 : 0;
+            continue;
+        }
         E = energy(true);
         E_prev = E;
         int k;
@@ -616,12 +678,17 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         LFRV_CUDA(cudaMemcpyAsync(b.Uprev_meta, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
     }
     LFRV_CUDA(cudaMemcpyAsync(out, ws.U.p, 3 * N * sizeof(float), cudaMemcpyDeviceToDevice, s));
-    if (trace) c->pending.trace_len = std::min(total_k, trace_cap);
+    if (trace && faithful) c->pending.trace_len = std::min(total_k, trace_cap);
+    if (trace && !faithful) {  // the corrected solve wrote its trace from the host
+        c->pending.trace_host = nullptr;
+        st->trace_length = tv_trace_pos;
+    }
     if (st) {
         st->outer_iterations = total_k;
         st->meta_iterations = std::min(r + 1, cfg.nmeta_iter);
         st->stop_reason = reason;
-        st->energy = (double)E;
+        st->energy = faithful ? (double)E : tv_E;
+        st->gap = faithful ? 0.0 : tv_gap_last;
     }
 }
 

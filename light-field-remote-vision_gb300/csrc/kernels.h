@@ -81,7 +81,7 @@ void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, i
 void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc,
                          bool counted = false);
 void launch_residual(const Geometry &G, const float *U, const float *img, const float *tau, const float *wgt, float s2,
-                     float *res, double *partial, cudaStream_t st, LaunchCounter &lc);
+                     float *res, double *partial, cudaStream_t st, LaunchCounter &lc, bool splat_set = false);
 int residual_partials(const Geometry &G);
 // wgt: FP32, or BF16 with bf16 = true (the BF16 storage mode of IBR_gradient).
 void launch_weights(const Geometry &G, const float *gx, const float *gy, const float *tau, const float *dp, float sigma,
@@ -174,6 +174,32 @@ struct GridBarrier {
     int *err;
 };
 int persistent_partials();  // upper bound of blocks (partials per slot)
+
+// ---------------------------------------------------------------- corrected IBR_color (kernels_tv.cu)
+constexpr int kTvInnerIterations = 200;  // FGP iterations per FISTA step (the oracle's kTvInner)
+// Metric D = max(alpha sigma^2 sum_i A_i^T w_i, 1), the prox parameter lam = lambda / D and the dual step
+// 1 / (8 max(lam_x, lam_{x+1}, lam_{x+W})) per target pixel.
+void launch_tv_metric(const Geometry &G, const Buckets &B, const float *tau, const float *wgt, float as2, float lambda,
+                      float *D, float *lam, float *linv, cudaStream_t st, LaunchCounter &lc);
+// grad f = as2 sum_i A_i^T res_i (3 planes) from the splat-set residuals of launch_residual.
+void launch_tv_gradf(const Geometry &G, const Buckets &B, const float *tau, const float *res, float as2, float *gf,
+                     cudaStream_t st, LaunchCounter &lc);
+// FP64 block partials of J_g(u), sum <grad u, p> and the box term of the certificate (c = gf - lambda div p),
+// three arrays of tv_gap_partials(W, H) entries each.
+int tv_gap_partials(int W, int H);
+void launch_tv_gap(int W, int H, const float *u, const float *gf, const float *P, const float *g, float lambda,
+                   double *partial, cudaStream_t st, LaunchCounter &lc);
+// F = y - grad f(y) / D, y = u + theta (u - u_prev), grad f(y) = (1 + theta) gf - theta gf_prev (3 planes).
+void launch_tv_fstep(int W, int H, const float *u, const float *up, const float *gf, const float *gfp, const float *D,
+                     float theta, float *F, cudaStream_t st, LaunchCounter &lc);
+// out = clamp(in, 0, 1) over n floats.
+void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, LaunchCounter &lc);
+// niter FGP iterations on the dual of the weighted ROF problem (one cooperative launch): P0 holds the starting
+// dual (6 planes: x parts of the 3 channels, then the y parts) and receives the final one; P1, Q0, Q1 are scratch
+// (6 planes each); U receives clamp(F + lam div p, 0, 1).
+cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *lam, const float *linv, const float *g,
+                          float *P0, float *P1, float *Q0, float *Q1, float *U, GridBarrier gb, cudaStream_t st,
+                          LaunchCounter &lc);
 
 // One target of a batched CG launch (k_cg_batch): its image, buffers and the contiguous range of blocks that
 // work on it. state: [0..2] delta, [3] E, [4] gap, [5] iterations (written by the problem's first block).

@@ -223,11 +223,14 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_finish(int nb, unsigned int
 // Weighted residual e = w * (A_i U - v_i) over the gather set, and the intensity energy
 // sum sigma^2 w (A_i U - v_i)^2 (vtv_sr_dataterm_intensities sources/optimization.cu:1871-1903 and
 // coco_vtv_sr_primal_energy_unstructured :1560-1608). Outside the gather set A_i U = 0.
+// splat_set: the residual over the splat set instead, zero elsewhere (the corrected IBR_color objective, whose
+// gradient splats over the same set).
 template <int KS>
 __global__ void __launch_bounds__(256) k_residual(int V, int n, int W, int H, int dsf, const float *__restrict__ U,
                                                   const float *__restrict__ img, const float *__restrict__ tau,
                                                   const float *__restrict__ wgt, float s2,
-                                                  float *__restrict__ res, double *__restrict__ partial) {
+                                                  float *__restrict__ res, double *__restrict__ partial,
+                                                  int splat_set) {
     __shared__ double red[8];
     const int m = blockIdx.x * blockDim.x + threadIdx.x;
     const int v = blockIdx.y;
@@ -254,7 +257,7 @@ __global__ void __launch_bounds__(256) k_residual(int V, int n, int W, int H, in
                 }
         }
         const float *iv = img + (size_t)v * 3 * n;
-        const float w = wgt[(size_t)v * n + m];
+        const float w = (splat_set && !in_splat(tx, ty, W, H)) ? 0.f : wgt[(size_t)v * n + m];
         const float d0 = a0 - iv[m], d1 = a1 - iv[n + m], d2 = a2 - iv[2 * n + m];
         float *rv = res + (size_t)v * 3 * n;
         rv[m] = d0 * w;
@@ -336,43 +339,7 @@ __global__ void __launch_bounds__(256, GATHER ? 1 : 8) k_weights(int V, int n, i
 }
 
 // ====================================================================== A^T gathers (per target pixel)
-struct SplatSrc {
-    const float *ch[3];   // payload channel c of view v at ch[c] + v * stride[c]
-    size_t stride[3];
-    const float *scale;   // optional per-source factor (weights), stride n per view
-};
-
-// Accumulates sum_entries A * payload and sum_entries A (times the optional scale) for target (x, y).
-template <int KS, int NCH>
-__device__ __forceinline__ void splat_accumulate(int x, int y, int W, int H, int n, int dsf, int BW,
-                                                 const unsigned int *__restrict__ start,
-                                                 const unsigned int *__restrict__ entries,
-                                                 const float *__restrict__ tau, const SplatSrc &src, float acc[3],
-                                                 float &norm) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) acc[c] = 0.f;
-    norm = 0.f;
-#pragma unroll
-    for (int i = 0; i < KS; ++i) {
-#pragma unroll
-        for (int j = 0; j < KS; ++j) {
-            const int ax = x - j, ay = y - i;  // anchor whose tap (j, i) lands on (x, y)
-            const size_t b = (size_t)(ay + KS - 1) * BW + (ax + KS - 1);
-            const unsigned int s = __ldg(start + b), e = __ldg(start + b + 1);
-            for (unsigned int k = s; k < e; ++k) {
-                const unsigned int ent = __ldg(entries + k);
-                const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
-                const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
-                float raw;
-                float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw);
-                if (src.scale) A = __ldg(src.scale + (size_t)v * n + m) * A;
-                norm += A;
-#pragma unroll
-                for (int c = 0; c < NCH; ++c) acc[c] += A * __ldg(src.ch[c] + (size_t)v * src.stride[c] + m);
-            }
-        }
-    }
-}
+// (SplatSrc and splat_accumulate live in device_common.cuh)
 
 // Coverage and visibility (coco_vtv_setup_visibility_mask sources/optimization.cu:33-135):
 // cov = sum A, vis = cov >= 1.
@@ -1173,14 +1140,6 @@ __global__ void k_copy_tau(int V, int n, const float *__restrict__ tau_in, int t
 // ====================================================================== host launchers
 static inline dim3 grid2(int W, int H, dim3 b) { return dim3((W + b.x - 1) / b.x, (H + b.y - 1) / b.y); }
 
-#define LFRV_KS_DISPATCH(ks, KERNEL, GRID, BLOCK, STREAM, ...)                          \
-    switch (ks) {                                                                       \
-        case 2: KERNEL<2><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
-        case 3: KERNEL<3><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
-        case 4: KERNEL<4><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
-        case 5: KERNEL<5><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); break;             \
-        default: break;                                                                 \
-    }
 
 void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaStream_t st, LaunchCounter &lc,
                          bool counted) {
@@ -1210,10 +1169,11 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
 }
 
 void launch_residual(const Geometry &G, const float *U, const float *img, const float *tau, const float *wgt, float s2,
-                     float *res, double *partial, cudaStream_t st, LaunchCounter &lc) {
+                     float *res, double *partial, cudaStream_t st, LaunchCounter &lc, bool splat_set) {
     ProfScope _ps(lc, "residual", st);
     const dim3 b(256), g((G.n + 255) / 256, G.V);
-    LFRV_KS_DISPATCH(G.dsf + 1, k_residual, g, b, st, G.V, G.n, G.W, G.H, G.dsf, U, img, tau, wgt, s2, res, partial);
+    LFRV_KS_DISPATCH(G.dsf + 1, k_residual, g, b, st, G.V, G.n, G.W, G.H, G.dsf, U, img, tau, wgt, s2, res, partial,
+                     splat_set ? 1 : 0);
     lc.add(1);
 }
 int residual_partials(const Geometry &G) { return ((G.n + 255) / 256) * G.V; }

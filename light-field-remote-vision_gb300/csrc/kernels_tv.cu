@@ -1,0 +1,335 @@
+// kernels_tv.cu -- corrected IBR_color: the weighted TV_F objective solved to a certified primal-dual gap.
+//
+// No reference counterpart. The reference's ISTA step (sources/optimization.cu:1751-1832) normalises the data
+// term's gradient by the coverage and clamps it, and reports an energy that is not its objective; in corrected mode
+// the library minimises
+//   E(u) = f(u) + lambda J_g(u) over [0, 1]^{3N},
+//   f(u) = alpha sigma^2 / 2 sum_i sum_{m in S_i} w_im |A_i u - v_i|^2_m        (S_i: view i's splat set),
+//   J_g(u) = sum_x g_x |grad u(x)|_F                                           (the TV_F of vtv_rof.cu:280-320),
+// by FISTA in the diagonal metric D = max(alpha sigma^2 sum_i A_i^T w_i, 1) (a majoriser of f's Hessian: the rows
+// of A_i sum to 1), each step a weighted ROF problem solved by the fast gradient projection (FGP) on its dual, and
+// certifies E(u) - E* <= lambda sum_x [g_x |grad u|_F - <grad u, p>] + sum [u c - min(0, c)], c = grad f(u) -
+// lambda div p. The host loop is color_solve_tv (host.cpp); the CPU restatement is oracle tv_solve.
+#include "device_common.cuh"
+#include "kernels.h"
+#include "lfrv_internal.h"
+
+#include <mutex>
+
+namespace lfrv {
+
+constexpr float kTvDelta = 1.0f;  // floor of the metric D (pixels without data keep a proximal term)
+
+// ------------------------------------------------------------------ per-pixel set-up
+template <int KS>
+__global__ void k_tv_metric(int W, int H, int n, int dsf, int BW, const unsigned int *__restrict__ start,
+                            const unsigned int *__restrict__ entries, const float *__restrict__ tau,
+                            const float *__restrict__ wgt, float as2, float lambda, float *__restrict__ D,
+                            float *__restrict__ lam) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const SplatSrc src{{wgt, wgt, wgt}, {(size_t)n, (size_t)n, (size_t)n}, nullptr};
+    float acc[3], norm;
+    splat_accumulate<KS, 1>(x, y, W, H, n, dsf, BW, start, entries, tau, src, acc, norm);
+    const size_t o = (size_t)y * W + x;
+    const float d = fmaxf(as2 * acc[0], kTvDelta);
+    D[o] = d;
+    lam[o] = lambda / d;
+}
+
+// Dual step 1 / L_x, L_x = 8 max(lam_x, lam_{x+1}, lam_{x+W}): the dual Hessian grad diag(lam) grad^T is at most
+// diag(L) (each dual entry enters the divergence at two pixels, each divergence has four terms).
+__global__ void k_tv_linv(int W, int H, const float *__restrict__ lam, float *__restrict__ linv) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t o = (size_t)y * W + x;
+    float m = lam[o];
+    if (x < W - 1) m = fmaxf(m, lam[o + 1]);
+    if (y < H - 1) m = fmaxf(m, lam[o + W]);
+    linv[o] = 1.0f / (8.0f * m);
+}
+
+template <int KS>
+__global__ void k_tv_gradf(int W, int H, int n, int dsf, int BW, const unsigned int *__restrict__ start,
+                           const unsigned int *__restrict__ entries, const float *__restrict__ tau,
+                           const float *__restrict__ res, float as2, float *__restrict__ gf) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    const size_t s3 = (size_t)3 * n;
+    const SplatSrc src{{res, res + n, res + 2 * (size_t)n}, {s3, s3, s3}, nullptr};
+    float acc[3], norm;
+    splat_accumulate<KS, 3>(x, y, W, H, n, dsf, BW, start, entries, tau, src, acc, norm);
+    const size_t o = (size_t)y * W + x, N = (size_t)W * H;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) gf[c * N + o] = as2 * acc[c];
+}
+
+// div of a dual field at (x, y): the negative adjoint of the forward gradient with zero at the last column / row.
+__device__ __forceinline__ float tv_div(const float *px, const float *py, int W, int H, int x, int y, size_t o) {
+    float d = 0.f;
+    if (x < W - 1) d += px[o];
+    if (x > 0) d -= px[o - 1];
+    if (y < H - 1) d += py[o];
+    if (y > 0) d -= py[o - W];
+    return d;
+}
+
+// ------------------------------------------------------------------ certificate
+constexpr int kGapBX = 32, kGapBY = 8;
+__global__ void __launch_bounds__(kGapBX * kGapBY) k_tv_gap(int W, int H, const float *__restrict__ u,
+                                                            const float *__restrict__ gf, const float *__restrict__ P,
+                                                            const float *__restrict__ g, float lambda,
+                                                            double *__restrict__ partial) {
+    __shared__ double red[kGapBX * kGapBY / 32];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const size_t N = (size_t)W * H;
+    double tv = 0.0, inner = 0.0, box = 0.0;
+    if (x < W && y < H) {
+        const size_t o = (size_t)y * W + x;
+        double n2 = 0.0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float *uc = u + c * N;
+            const double gxv = x < W - 1 ? (double)uc[o + 1] - (double)uc[o] : 0.0;
+            const double gyv = y < H - 1 ? (double)uc[o + W] - (double)uc[o] : 0.0;
+            n2 += gxv * gxv + gyv * gyv;
+            const float *px = P + c * N, *py = P + (3 + c) * N;
+            inner += gxv * (double)px[o] + gyv * (double)py[o];
+            const double cc = (double)gf[c * N + o] - (double)lambda * (double)tv_div(px, py, W, H, x, y, o);
+            box += (double)uc[o] * cc - fmin(0.0, cc);
+        }
+        tv = (double)g[o] * sqrt(n2);
+    }
+    const int b = blockIdx.y * gridDim.x + blockIdx.x, nb = gridDim.x * gridDim.y;
+    const double s0 = block_sum<kGapBX * kGapBY>(tv, red);
+    if (threadIdx.x == 0 && threadIdx.y == 0) partial[b] = s0;
+    const double s1 = block_sum<kGapBX * kGapBY>(inner, red);
+    if (threadIdx.x == 0 && threadIdx.y == 0) partial[nb + b] = s1;
+    const double s2 = block_sum<kGapBX * kGapBY>(box, red);
+    if (threadIdx.x == 0 && threadIdx.y == 0) partial[2 * nb + b] = s2;
+}
+
+__global__ void k_tv_fstep(size_t N, const float *__restrict__ u, const float *__restrict__ up,
+                           const float *__restrict__ gf, const float *__restrict__ gfp, const float *__restrict__ D,
+                           float theta, float *__restrict__ F) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 3 * N) return;
+    const float y = u[i] + theta * (u[i] - up[i]);
+    const float gy = (1.0f + theta) * gf[i] - theta * gfp[i];
+    F[i] = y - gy / D[i % N];
+}
+
+__global__ void k_tv_clamp(size_t n, const float *__restrict__ in, float *__restrict__ out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = fminf(1.0f, fmaxf(0.0f, in[i]));
+}
+
+// ------------------------------------------------------------------ FGP on the weighted ROF dual
+// One cooperative launch runs every inner iteration. Temporally blocked: a block stages its tile and a halo of
+// kFgpK pixels (q, p, F, lam, 1/L, g) in shared memory and runs kFgpK iterations there before it writes the tile
+// back and the grid synchronises (each iteration's dependence reaches one pixel in each direction, diagonals
+// included, so the tile stays exact). Per iteration, on the staged region:
+//   u = clamp(F + lam div q, 0, 1);  p' = proj_{|.|_F <= g}(q + grad u / L);  q = p' + beta_j (p' - p);  p = p'
+// with beta_j = (s_j - 1) / s_{j+1}, s_0 = 1, s_{j+1} = (1 + sqrt(1 + 4 s_j^2)) / 2 (Beck and Teboulle's FGP).
+constexpr int kFgpTX = 32, kFgpTY = 16, kFgpK = 4, kFgpThreads = 512;
+constexpr int kFgpRX = kFgpTX + 2 * kFgpK, kFgpRY = kFgpTY + 2 * kFgpK, kFgpRN = kFgpRX * kFgpRY;
+constexpr int kFgpPlanes = 21;  // q 6, p 6, u 3, F 3, lam, 1/L, g
+constexpr size_t kFgpSmem = (size_t)kFgpPlanes * kFgpRN * sizeof(float);
+
+__global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter, const float *__restrict__ F,
+                                                        const float *__restrict__ lam, const float *__restrict__ linv,
+                                                        const float *__restrict__ g, float *P0, float *P1, float *Q0,
+                                                        float *Q1, float *__restrict__ U, GridBarrier gb) {
+    extern __shared__ float sm[];
+    float *sQ = sm, *sP = sm + 6 * kFgpRN, *sU = sm + 12 * kFgpRN, *sF = sm + 15 * kFgpRN;
+    float *sL = sm + 18 * kFgpRN, *sI = sm + 19 * kFgpRN, *sG = sm + 20 * kFgpRN;
+    const int tiles_x = (W + kFgpTX - 1) / kFgpTX, ntiles = tiles_x * ((H + kFgpTY - 1) / kFgpTY);
+    const size_t N = (size_t)W * H;
+    unsigned int gen = 0;
+    float s_step = 1.0f;  // s_j at the start of the super-step (every thread follows the same sequence)
+    int step = 0;
+    for (int done = 0; done < niter; done += kFgpK, ++step) {
+        const int iters = min(kFgpK, niter - done);
+        const float *Pi = (step & 1) ? P1 : P0;
+        float *Po = (step & 1) ? P0 : P1;
+        const float *Qi = step == 0 ? P0 : ((step & 1) ? Q1 : Q0);  // q starts at p
+        float *Qo = (step & 1) ? Q0 : Q1;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            const int rx0 = (t % tiles_x) * kFgpTX - kFgpK, ry0 = (t / tiles_x) * kFgpTY - kFgpK;
+            for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
+                const int gx = rx0 + i % kFgpRX, gy = ry0 + i / kFgpRX;
+                const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+                const size_t o = in ? (size_t)gy * W + gx : 0;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    sQ[k * kFgpRN + i] = in ? __ldcg(Qi + k * N + o) : 0.f;
+                    sP[k * kFgpRN + i] = in ? __ldcg(Pi + k * N + o) : 0.f;
+                }
+#pragma unroll
+                for (int c = 0; c < 3; ++c) sF[c * kFgpRN + i] = in ? __ldg(F + c * N + o) : 0.f;
+                sL[i] = in ? __ldg(lam + o) : 0.f;
+                sI[i] = in ? __ldg(linv + o) : 0.f;
+                sG[i] = in ? __ldg(g + o) : 0.f;
+            }
+            __syncthreads();
+            float s = s_step;
+            for (int it = 0; it < iters; ++it) {
+                const float s1 = 0.5f * (1.0f + sqrtf(1.0f + 4.0f * s * s));
+                const float beta = (s - 1.0f) / s1;
+                // u(q) on the region (values next to the region's edge are stale and stay outside the tile)
+                for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
+                    const int lx = i % kFgpRX, ly = i / kFgpRX, gx = rx0 + lx, gy = ry0 + ly;
+                    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float *qx = sQ + c * kFgpRN, *qy = sQ + (3 + c) * kFgpRN;
+                        float d = 0.f;
+                        if (gx < W - 1) d += qx[i];
+                        if (gx > 0) d -= lx > 0 ? qx[i - 1] : 0.f;
+                        if (gy < H - 1) d += qy[i];
+                        if (gy > 0) d -= ly > 0 ? qy[i - kFgpRX] : 0.f;
+                        sU[c * kFgpRN + i] = fminf(1.0f, fmaxf(0.0f, sF[c * kFgpRN + i] + sL[i] * d));
+                    }
+                }
+                __syncthreads();
+                // p' = proj(q + grad u / L), q = p' + beta (p' - p), in place (own pixel only)
+                for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
+                    const int lx = i % kFgpRX, ly = i / kFgpRX, gx = rx0 + lx, gy = ry0 + ly;
+                    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+                    float v[6];
+                    float n2 = 0.f;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float *uc = sU + c * kFgpRN;
+                        const float ur = (lx + 1 < kFgpRX) ? uc[i + 1] : 0.f;
+                        const float ud = (ly + 1 < kFgpRY) ? uc[i + kFgpRX] : 0.f;
+                        const float gxv = gx < W - 1 ? ur - uc[i] : 0.f;
+                        const float gyv = gy < H - 1 ? ud - uc[i] : 0.f;
+                        v[c] = sQ[c * kFgpRN + i] + gxv * sI[i];
+                        v[3 + c] = sQ[(3 + c) * kFgpRN + i] + gyv * sI[i];
+                        n2 += v[c] * v[c] + v[3 + c] * v[3 + c];
+                    }
+                    const float nrm = sqrtf(n2);
+                    const float sc = nrm > sG[i] ? sG[i] / nrm : 1.0f;
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) {
+                        const float pn = v[k] * sc;
+                        sQ[k * kFgpRN + i] = pn + beta * (pn - sP[k * kFgpRN + i]);
+                        sP[k * kFgpRN + i] = pn;
+                    }
+                }
+                __syncthreads();
+                s = s1;
+            }
+            for (int i = threadIdx.x; i < kFgpTX * kFgpTY; i += kFgpThreads) {
+                const int lx = kFgpK + i % kFgpTX, ly = kFgpK + i / kFgpTX, gx = rx0 + lx, gy = ry0 + ly;
+                if (gx >= W || gy >= H) continue;
+                const size_t o = (size_t)gy * W + gx;
+                const int r = ly * kFgpRX + lx;
+#pragma unroll
+                for (int k = 0; k < 6; ++k) {
+                    Po[k * N + o] = sP[k * kFgpRN + r];
+                    Qo[k * N + o] = sQ[k * kFgpRN + r];
+                }
+            }
+            __syncthreads();  // the next tile overwrites the staged region
+        }
+        for (int it = 0; it < iters; ++it) s_step = 0.5f * (1.0f + sqrtf(1.0f + 4.0f * s_step * s_step));
+        if (!grid_sync(gb, gen)) return;
+    }
+    // the final dual sits in P0 after an even number of super-steps, else in P1; u = clamp(F + lam div p)
+    const int steps = (niter + kFgpK - 1) / kFgpK;
+    const float *Pf = (steps & 1) ? P1 : P0;
+    float *Pother = (steps & 1) ? P0 : P1;
+    for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < N; o += (size_t)gridDim.x * blockDim.x) {
+        const int x = (int)(o % W), y = (int)(o / W);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float d = tv_div(Pf + c * N, Pf + (3 + c) * N, W, H, x, y, o);
+            U[c * N + o] = fminf(1.0f, fmaxf(0.0f, F[c * N + o] + lam[o] * d));
+        }
+    }
+    // the caller keeps its dual in P0: copy it there when the last super-step wrote P1
+    if (steps & 1) {
+        if (!grid_sync(gb, gen)) return;  // every block has read P1's neighbours above
+        for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < 6 * N; i += (size_t)gridDim.x * blockDim.x)
+            Pother[i] = Pf[i];
+    }
+}
+
+// ------------------------------------------------------------------ launchers
+static inline dim3 tv_grid(int W, int H, dim3 b) { return dim3((W + b.x - 1) / b.x, (H + b.y - 1) / b.y); }
+
+void launch_tv_metric(const Geometry &G, const Buckets &B, const float *tau, const float *wgt, float as2, float lambda,
+                      float *D, float *lam, float *linv, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "tv_metric", st);
+    const dim3 b(32, 8), g = tv_grid(G.W, G.H, b);
+    LFRV_KS_DISPATCH(G.dsf + 1, k_tv_metric, g, b, st, G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau, wgt,
+                     as2, lambda, D, lam);
+    k_tv_linv<<<g, b, 0, st>>>(G.W, G.H, lam, linv);
+    lc.add(2);
+}
+
+void launch_tv_gradf(const Geometry &G, const Buckets &B, const float *tau, const float *res, float as2, float *gf,
+                     cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "tv_gradf", st);
+    const dim3 b(32, 8), g = tv_grid(G.W, G.H, b);
+    LFRV_KS_DISPATCH(G.dsf + 1, k_tv_gradf, g, b, st, G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau, res, as2,
+                     gf);
+    lc.add(1);
+}
+
+int tv_gap_partials(int W, int H) { return ((W + kGapBX - 1) / kGapBX) * ((H + kGapBY - 1) / kGapBY); }
+
+void launch_tv_gap(int W, int H, const float *u, const float *gf, const float *P, const float *g, float lambda,
+                   double *partial, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "tv_gap", st);
+    const dim3 b(kGapBX, kGapBY), gr = tv_grid(W, H, b);
+    k_tv_gap<<<gr, b, 0, st>>>(W, H, u, gf, P, g, lambda, partial);
+    lc.add(1);
+}
+
+void launch_tv_fstep(int W, int H, const float *u, const float *up, const float *gf, const float *gfp, const float *D,
+                     float theta, float *F, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "tv_fstep", st);
+    const size_t N = (size_t)W * H;
+    k_tv_fstep<<<(unsigned)((3 * N + 255) / 256), 256, 0, st>>>(N, u, up, gf, gfp, D, theta, F);
+    lc.add(1);
+}
+
+void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, LaunchCounter &lc) {
+    ProfScope _ps(lc, "tv_clamp", st);
+    k_tv_clamp<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, in, out);
+    lc.add(1);
+}
+
+cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *lam, const float *linv, const float *g,
+                          float *P0, float *P1, float *Q0, float *Q1, float *U, GridBarrier gb, cudaStream_t st,
+                          LaunchCounter &lc) {
+    ProfScope _ps(lc, "tv_fgp", st);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    static std::mutex mu;
+    static bool attr_set[64] = {};
+    if (dev >= 0 && dev < 64) {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!attr_set[dev]) {
+            cudaFuncSetAttribute(k_tv_fgp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFgpSmem);
+            attr_set[dev] = true;
+        }
+    }
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tv_fgp, kFgpThreads, kFgpSmem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int ntiles = ((W + kFgpTX - 1) / kFgpTX) * ((H + kFgpTY - 1) / kFgpTY);
+    const int resident = sms * per_sm;
+    // as few blocks as keep the per-block tile count at its minimum (no block waits for a straggler's extra tile)
+    const int per_block = (ntiles + resident - 1) / resident;
+    const int blocks = std::max(1, (ntiles + per_block - 1) / per_block);
+    void *args[] = {&W, &H, &niter, (void *)&F, (void *)&lam, (void *)&linv, (void *)&g, &P0, &P1, &Q0, &Q1, &U, &gb};
+    lc.add(1);
+    return cudaLaunchCooperativeKernel((const void *)k_tv_fgp, dim3(blocks), dim3(kFgpThreads), args, kFgpSmem, st);
+}
+
+}  // namespace lfrv

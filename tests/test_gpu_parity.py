@@ -253,12 +253,38 @@ def test_ibr_color_early_exit(ctx):
     assert rel_err(out, ref) <= 1e-4
 
 
-def test_ibr_color_corrected_mode(ctx):
-    sc, tau, dpart, _ = warped(1, 48)
-    cfg = color_config(sc, niter=10, faithful=0)
-    out, _ = ctx.ibr_color(cfg, sc.views, tau, dpart)
-    ref, _ = pyoracle.ibr_color(cfg, sc.views, tau, dpart, prec=0)
+@pytest.mark.parametrize("preset,w,niter", [(1, 48, 6), (2, 24, 4)])
+def test_ibr_color_corrected_mode(ctx, preset, w, niter):
+    """Corrected IBR_color (the TV_F objective by FISTA + FGP, kernels_tv.cu) against the FP64 oracle after a fixed
+    number of outer iterations (gap stop off): 1e-4 max relative error per pixel, energy trace and certified gap
+    to 1e-4 relative."""
+    sc, tau, dpart, _ = warped(preset, w)
+    cfg = color_config(sc, niter=niter, faithful=0, cg_gap_tol=0.0)
+    out, st = ctx.ibr_color(cfg, sc.views, tau, dpart, trace=16)
+    ref, rst = pyoracle.ibr_color(cfg, sc.views, tau, dpart, prec=0, trace=16)
+    assert st.outer_iterations == rst.outer_iterations == niter
     assert rel_err(out, ref) <= 1e-4
+    tr, rtr = st.trace(), rst.trace()
+    assert len(tr) == len(rtr) == niter + 1
+    assert np.max(np.abs(tr - rtr) / np.abs(rtr)) <= 1e-4
+    assert abs(st.gap - rst.gap) <= 1e-4 * rst.gap + 1e-7
+
+
+def test_ibr_color_corrected_certified_gap(ctx):
+    """The corrected solve stops at a certified relative gap of 1e-4, and the certificate holds: its energy is
+    within gap * E of the FP64 oracle's optimum (solved to a certified 1e-7)."""
+    sc, tau, dpart, _ = warped(1, 64)
+    cfg = color_config(sc, niter=400, faithful=0, cg_gap_tol=1e-4)
+    out, st = ctx.ibr_color(cfg, sc.views, tau, dpart, trace=512)
+    assert st.stop_reason == 4 and st.gap <= 1e-4
+    ref_cfg = color_config(sc, niter=2000, faithful=0, cg_gap_tol=1e-7)
+    _, rst = pyoracle.ibr_color(ref_cfg, sc.views, tau, dpart, prec=0)
+    assert rst.gap <= 1e-7
+    e_star = rst.energy
+    assert st.energy - e_star <= st.gap * st.energy + 1e-6 * e_star
+    assert st.energy >= e_star * (1 - 1e-6)
+    tr = st.trace()
+    assert len(tr) == st.outer_iterations + 1 and tr[-1] == st.energy
 
 
 @pytest.mark.parametrize("preset,w", [(1, 48), (2, 32)])
