@@ -361,6 +361,14 @@ int lfrv_stage_u_gradient(lfrv_ctx *ctx, const lfrv_config *cfg, const float *vi
 int lfrv_stage_cg(lfrv_ctx *ctx, int W, int H, int faithful, int max_iter, double gap_tol,
                   const float *gx, const float *gy, float *U, int *iterations, double *gap);
 
+/* poisson_jacobi (sources/gradientIBR.cu:923-1013), the Jacobi alternative to the CG that IBR_gradient leaves
+ * commented out (sources/gradientIBR.cpp:131): z = (m u0 - div g) / (4 + m) per channel with the central-difference
+ * divergence of (gx, gy), then `iterations` sweeps (200 upstream) u <- (sum of the 4 neighbours, the border pixel
+ * repeated) / (4 + m) + z. gx, gy, mask: H x W; U: 3 x H x W (in: u0, out: the result). All sweeps run in one
+ * persistent launch. */
+int lfrv_stage_poisson_jacobi(lfrv_ctx *ctx, int W, int H, int iterations, const float *gx, const float *gy,
+                              const float *mask, float *U);
+
 /* Allocation-free corrected CG. No reference counterpart.
  * The same solver as lfrv_stage_cg with faithful = 0, on caller-owned DEVICE buffers on `stream`
  * (a cudaStream_t of the current device, or NULL for the legacy default stream): gx, gy are H x W,

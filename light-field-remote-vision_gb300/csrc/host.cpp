@@ -234,11 +234,9 @@ static Buckets bucket_buffers(lfrv_ctx *c, const Geometry &G) {
     B.count = ws.b_count.as<unsigned int>();
     B.start = ws.b_start.as<unsigned int>();
     B.entries = ws.b_entries.as<unsigned int>();
-    B.mask = nullptr;
-    if (G.V <= 64) {
-        ws.b_mask.ensure(sizeof(unsigned long long) * B.nb);
-        B.mask = ws.b_mask.as<unsigned long long>();
-    }
+    B.mask_words = (G.V + 63) / 64;
+    ws.b_mask.ensure(sizeof(unsigned long long) * B.nb * B.mask_words);
+    B.mask = ws.b_mask.as<unsigned long long>();
     B.block_sums = aux;
     B.block_offsets = aux + nblk;
     B.block_sums2 = aux + 2 * nblk;
@@ -561,6 +559,9 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         launch_tv_metric(G, B, tau2, b.wgt, as2, cfg.lambda, D, lam, linv, s, c->launches);
         check_launch("tv metric");
         launch_tv_clamp(N3, ws.U.as<float>(), u, s, c->launches);
+        // u_prev = u and grad f(u_prev) = 0: the first step (theta = 0) reads them only through zero factors
+        LFRV_CUDA(cudaMemcpyAsync(up, u, sizeof(float) * N3, cudaMemcpyDeviceToDevice, s));
+        LFRV_CUDA(cudaMemsetAsync(gfp, 0, sizeof(float) * N3, s));
         if (meta == 0) LFRV_CUDA(cudaMemsetAsync(P0, 0, sizeof(float) * 6 * N, s));
         const int npart = tv_gap_partials(G.W, G.H);
         const double tol = cfg.cg_gap_tol;
@@ -1040,11 +1041,13 @@ static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfr
     if (count_for && tau2) {
         const Buckets B = bucket_buffers(c, *count_for);
         LFRV_CUDA(cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, c->stream));
-        if (B.mask) LFRV_CUDA(cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb, c->stream));
+        if (B.mask)
+            LFRV_CUDA(cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb * B.mask_words, c->stream));
         bc.count = B.count;
         bc.mask = B.mask;
         bc.dsf = count_for->dsf;
         bc.BW = B.BW;
+        bc.nb = B.nb;
     }
     if (plan) {
         // splat each chunk of views as soon as its depth maps have arrived
@@ -2342,6 +2345,31 @@ extern "C" int lfrv_stage_u_gradient(lfrv_ctx *ctx, const lfrv_config *cfg, cons
     io.down(gy, b.gy, G.N);
     io.down(mask, ctx->ws.mask.as<float>(), G.N);
     sync(ctx);
+    LFRV_API_END
+}
+
+extern "C" int lfrv_stage_poisson_jacobi(lfrv_ctx *ctx, int W, int H, int iterations, const float *gx,
+                                         const float *gy, const float *mask, float *U) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (W < 1 || H < 1 || iterations < 0 || !gx || !gy || !mask || !U) return fail(LFRV_E_ARG, "bad arguments");
+    const size_t N = (size_t)W * H;
+    HostIO io{ctx};
+    io.up(ctx->ws.gx, gx, N);
+    io.up(ctx->ws.gy, gy, N);
+    io.up(ctx->ws.mask, mask, N);
+    io.up(ctx->ws.U, U, 3 * N);
+    ctx->ws.Ua.ensure(sizeof(float) * 3 * N);
+    ctx->ws.r.ensure(sizeof(float) * 3 * N);
+    ctx->ws.tmp.ensure(sizeof(float) * N);
+    ctx->pending = Pending{};
+    const GridBarrier gb = fresh_barrier(ctx);
+    LFRV_CUDA(launch_poisson_jacobi(W, H, iterations, ctx->ws.gx.as<float>(), ctx->ws.gy.as<float>(),
+                                    ctx->ws.mask.as<float>(), ctx->ws.U.as<float>(), ctx->ws.Ua.as<float>(),
+                                    ctx->ws.r.as<float>(), ctx->ws.tmp.as<float>(), gb, ctx->stream, ctx->launches));
+    io.down(U, ctx->ws.U.as<float>(), 3 * N);
+    sync(ctx);
+    finish_stats(ctx);
     LFRV_API_END
 }
 

@@ -36,7 +36,9 @@ struct Buckets {
     int BW, BH, nb;                     // bucket grid (W + ks - 1) x (H + ks - 1)
     unsigned int *count, *start;        // nb, nb + 1
     unsigned int *entries;              // V * n capacity, (view << 24) | pixel
-    unsigned long long *mask;           // nb: bit v set when view v lands in the bucket (V <= 64), else null
+    unsigned long long *mask;           // mask_words x nb: bit v % 64 of word v / 64 set when view v lands in the
+                                        // bucket (word-major: word w of bucket b at mask[w * nb + b])
+    int mask_words;                     // ceil(V / 64)
     unsigned int *block_sums, *block_offsets, *block_sums2, *block_offsets2, *total, *total2;
 };
 
@@ -70,8 +72,8 @@ void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float 
 // bucket build needs no count pass of its own (count and mask zeroed beforehand).
 struct BucketCount {
     unsigned int *count = nullptr;
-    unsigned long long *mask = nullptr;  // null when V > 64
-    int dsf = 0, BW = 0;
+    unsigned long long *mask = nullptr;  // view masks: word w of bucket b at mask[w * nb + b]
+    int dsf = 0, BW = 0, nb = 0;
 };
 void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H, const float *zbuf,
                 float *tau3, float *dpart3, float *tau2, float *dp2, cudaStream_t st, LaunchCounter &lc,
@@ -228,6 +230,11 @@ int rof_persistent_steps(int niter, int v);
 cudaError_t launch_rof_persistent(int W, int H, int niter, float tau, float sigma, float lam, float *U0, float *P0,
                                   float *U1, float *P1, const float *F, const float *g, GridBarrier gb, int v,
                                   cudaStream_t st, LaunchCounter &lc);
+// poisson_jacobi (sources/gradientIBR.cu:923-1013): `iters` Jacobi sweeps on U (3 planes) in one cooperative launch;
+// U1 (3 planes), z (3 planes) and den (1 plane) are scratch.
+cudaError_t launch_poisson_jacobi(int W, int H, int iters, const float *gx, const float *gy, const float *mask,
+                                  float *U, float *U1, float *z, float *den, GridBarrier gb, cudaStream_t st,
+                                  LaunchCounter &lc);
 cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,
                                  float *dB, double *partA, double *partB, GridBarrier gb, int max_iter, double gap_tol,
                                  double *state, cudaStream_t st, LaunchCounter &lc, const float *U0 = nullptr,

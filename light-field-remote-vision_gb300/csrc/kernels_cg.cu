@@ -1474,6 +1474,102 @@ __global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W,
     if (blockIdx.x == 0 && threadIdx.x == 0) state[0] = (double)k;
 }
 
+// ------------------------------------------------------------------ Jacobi Poisson integration
+// poisson_jacobi (sources/gradientIBR.cu:923-1013): z = (m u0 - div g) / (4 + m) per channel (compute_divergence,
+// jacobi_z, sources/gradientIBR_kernels.cuh:553-598), then sweeps x <- (x_l + x_u + x_r + x_d) / (4 + m) + z with the
+// border pixel standing in for a missing neighbour (jacobi_B :600-643). The reference launches 2 kernels per channel
+// and sweep; here one cooperative launch runs every sweep of all three channels, kJacK sweeps per grid barrier: a
+// block stages its tile with a halo of kJacK pixels in shared memory (each sweep's stencil reaches one pixel) and
+// ping-pongs there. Every operation is the reference's float expression in its order, without contraction.
+constexpr int kJacTX = 32, kJacTY = 16, kJacK = 4, kJacThreads = 512;
+constexpr int kJacRX = kJacTX + 2 * kJacK, kJacRY = kJacTY + 2 * kJacK, kJacRN = kJacRX * kJacRY;
+constexpr size_t kJacSmem = (size_t)10 * kJacRN * sizeof(float);  // x (3 channels x 2 buffers), z (3), 4 + m
+
+__global__ void k_jacobi_setup(int W, int H, const float *__restrict__ gX, const float *__restrict__ gY,
+                               const float *__restrict__ mask, const float *__restrict__ U, float *__restrict__ z,
+                               float *__restrict__ den) {
+    const int ox = blockIdx.x * blockDim.x + threadIdx.x, oy = blockIdx.y * blockDim.y + threadIdx.y;
+    if (ox >= W || oy >= H) return;
+    const size_t o = (size_t)oy * W + ox, N = (size_t)W * H;
+    float dv = 0.0f;
+    if (ox != 0 && ox != W - 1) dv = __fadd_rn(dv, __fsub_rn(gX[o + 1], gX[o - 1]) / 2);
+    if (oy != 0 && oy != H - 1) dv = __fadd_rn(dv, __fsub_rn(gY[o + W], gY[o - W]) / 2);
+    const float data_w = __fmul_rn(1.0f, mask[o]);
+    const float d = __fadd_rn(4.0f, data_w);
+    den[o] = d;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) z[c * N + o] = __fsub_rn(__fmul_rn(data_w, U[c * N + o]), dv) / d;
+}
+
+__global__ void __launch_bounds__(kJacThreads) k_jacobi_persistent(int W, int H, int iters,
+                                                                   const float *__restrict__ z,
+                                                                   const float *__restrict__ den, float *U0, float *U1,
+                                                                   GridBarrier gb) {
+    extern __shared__ float jsm[];
+    float *sX = jsm, *sZ = jsm + 6 * kJacRN, *sD = jsm + 9 * kJacRN;  // sX: [buffer][channel][kJacRN]
+    const int tiles_x = (W + kJacTX - 1) / kJacTX, ntiles = tiles_x * ((H + kJacTY - 1) / kJacTY);
+    const size_t N = (size_t)W * H;
+    unsigned int gen = 0;
+    int step = 0;
+    for (int done = 0; done < iters; done += kJacK, ++step) {
+        const int n_it = min(kJacK, iters - done);
+        const float *Ui = (step & 1) ? U1 : U0;
+        float *Uo = (step & 1) ? U0 : U1;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
+            const int rx0 = (t % tiles_x) * kJacTX - kJacK, ry0 = (t / tiles_x) * kJacTY - kJacK;
+            for (int i = threadIdx.x; i < kJacRN; i += kJacThreads) {
+                const int gx = rx0 + i % kJacRX, gy = ry0 + i / kJacRX;
+                const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+                const size_t o = in ? (size_t)gy * W + gx : 0;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    sX[c * kJacRN + i] = in ? __ldcg(Ui + c * N + o) : 0.f;
+                    sZ[c * kJacRN + i] = in ? __ldg(z + c * N + o) : 0.f;
+                }
+                sD[i] = in ? __ldg(den + o) : 1.f;
+            }
+            __syncthreads();
+            for (int it = 0; it < n_it; ++it) {
+                const float *src = sX + (it & 1) * 3 * kJacRN;
+                float *dst = sX + ((it + 1) & 1) * 3 * kJacRN;
+                for (int i = threadIdx.x; i < kJacRN; i += kJacThreads) {
+                    const int lx = i % kJacRX, ly = i / kJacRX, gx = rx0 + lx, gy = ry0 + ly;
+                    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        const float *x = src + c * kJacRN;
+                        const float xc = x[i];
+                        // neighbours outside the staged region are stale only where the tile does not look
+                        const float xl = gx == 0 ? xc : (lx > 0 ? x[i - 1] : 0.f);
+                        const float xu = gy == 0 ? xc : (ly > 0 ? x[i - kJacRX] : 0.f);
+                        const float xr = gx == W - 1 ? xc : (lx + 1 < kJacRX ? x[i + 1] : 0.f);
+                        const float xd = gy == H - 1 ? xc : (ly + 1 < kJacRY ? x[i + kJacRX] : 0.f);
+                        float v = 0.0f;
+                        v = __fadd_rn(v, xl);
+                        v = __fadd_rn(v, xu);
+                        v = __fadd_rn(v, xr);
+                        v = __fadd_rn(v, xd);
+                        v = v / sD[i];
+                        dst[c * kJacRN + i] = __fadd_rn(v, sZ[c * kJacRN + i]);
+                    }
+                }
+                __syncthreads();
+            }
+            const float *res = sX + (n_it & 1) * 3 * kJacRN;
+            for (int i = threadIdx.x; i < kJacTX * kJacTY; i += kJacThreads) {
+                const int lx = kJacK + i % kJacTX, ly = kJacK + i / kJacTX, gx = rx0 + lx, gy = ry0 + ly;
+                if (gx >= W || gy >= H) continue;
+                const size_t o = (size_t)gy * W + gx;
+                const int r = ly * kJacRX + lx;
+#pragma unroll
+                for (int c = 0; c < 3; ++c) Uo[c * N + o] = res[c * kJacRN + r];
+            }
+            __syncthreads();  // the next tile overwrites the staged region
+        }
+        if (!grid_sync(gb, gen)) return;
+    }
+}
+
 // ------------------------------------------------------------------ launchers
 static inline dim3 cg_grid(int W, int H) { return dim3((W + kCgBX - 1) / kCgBX, (H + kCgBY - 1) / kCgBY); }
 int cg_partials(int W, int H) {
@@ -1512,6 +1608,35 @@ int persistent_partials() {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     return 2 * sms;
+}
+
+cudaError_t launch_poisson_jacobi(int W, int H, int iters, const float *gx, const float *gy, const float *mask,
+                                  float *U, float *U1, float *z, float *den, GridBarrier gb, cudaStream_t st,
+                                  LaunchCounter &lc) {
+    ProfScope _ps(lc, "poisson_jacobi", st);
+    const dim3 b(32, 8), g((W + 31) / 32, (H + 7) / 8);
+    k_jacobi_setup<<<g, b, 0, st>>>(W, H, gx, gy, mask, U, z, den);
+    lc.add(1);
+    if (iters <= 0) return cudaGetLastError();
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_jacobi_persistent, kJacThreads, kJacSmem);
+    if (e != cudaSuccess) return e;
+    if (per_sm < 1) return cudaErrorInvalidConfiguration;
+    const int ntiles = ((W + kJacTX - 1) / kJacTX) * ((H + kJacTY - 1) / kJacTY);
+    const int resident = sms * per_sm;
+    const int per_block = (ntiles + resident - 1) / resident;
+    const int blocks = std::max(1, (ntiles + per_block - 1) / per_block);
+    void *args[] = {&W, &H, &iters, (void *)&z, (void *)&den, &U, &U1, &gb};
+    e = cudaLaunchCooperativeKernel((const void *)k_jacobi_persistent, dim3(blocks), dim3(kJacThreads), args, kJacSmem,
+                                    st);
+    lc.add(1);
+    if (e != cudaSuccess) return e;
+    // an odd number of super-steps leaves the result in U1
+    const int steps = (iters + kJacK - 1) / kJacK;
+    if (steps & 1) return cudaMemcpyAsync(U, U1, sizeof(float) * 3 * (size_t)W * H, cudaMemcpyDeviceToDevice, st);
+    return cudaSuccess;
 }
 
 cudaError_t launch_cg_persistent(int W, int H, const float *gx, const float *gy, float *U, float *r, float *dA,

@@ -32,15 +32,15 @@ __device__ __forceinline__ void stv(__nv_bfloat16 *p, float v) { *p = __float2bf
 // Count and fill take kBucketPer source pixels per thread (m, m + blockDim.x, ...): each stage's loads and atomics
 // for all of them are issued before any result is used, so their round trips to L2 overlap. Bucket of a
 // splatted source pixel: its footprint anchor, offset by ks - 1 (-1: not splatted).
-// With a view mask (V <= 64) the count also sets bit v of its bucket's mask. A bucket whose count equals the
-// mask's population holds one entry per view, and the entry of view v goes to slot popc(mask & (2^v - 1)):
-// already in (view, pixel) order, with no atomic in the fill and nothing for the sort to do. Only buckets with
-// two entries of one view take slots from the cursor (in arrival order) and need the sort.
+// The count also sets bit v of its bucket's view mask (ceil(V / 64) 64-bit words per bucket, word-major). A bucket
+// whose count equals the mask's population holds one entry per view, and the entry of view v goes to slot
+// popc(mask & (2^v - 1)): already in (view, pixel) order, with no atomic in the fill and nothing for the sort to
+// do. Only buckets with two entries of one view take slots from the cursor (in arrival order) and need the sort.
 constexpr int kBucketPer = 4;
 
 
 __global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
-                               unsigned int *__restrict__ cnt, unsigned long long *__restrict__ mask) {
+                               unsigned int *__restrict__ cnt, unsigned long long *__restrict__ mask, int nb) {
     const int m0 = blockIdx.x * blockDim.x * kBucketPer + threadIdx.x;
     const float *tv = tau + (size_t)blockIdx.y * 2 * n;
     float tx[kBucketPer], ty[kBucketPer];
@@ -55,19 +55,28 @@ __global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, cons
         const long long b = bucket_of(tx[j], ty[j], W, H, dsf, BW);
         if (m0 + j * (int)blockDim.x < n && b >= 0) {
             atomicAdd(&cnt[b], 1u);
-            if (mask) atomicOr(&mask[b], 1ull << blockIdx.y);
+            if (mask) atomicOr(&mask[(size_t)(blockIdx.y >> 6) * nb + b], 1ull << (blockIdx.y & 63));
         }
     }
 }
 
+// Views in bucket b's mask (mw words).
+__device__ __forceinline__ unsigned int mask_pop(const unsigned long long *mask, int mw, int nb, long long b) {
+    unsigned int c = 0;
+    for (int w = 0; w < mw; ++w) c += (unsigned int)__popcll(mask[(size_t)w * nb + b]);
+    return c;
+}
+
 // Whether bucket b's entries must come from the cursor and be sorted (see above).
-__device__ __forceinline__ bool bucket_dup(const unsigned int *start, const unsigned long long *mask, long long b) {
-    return !mask || start[b + 1] - start[b] != (unsigned int)__popcll(mask[b]);
+__device__ __forceinline__ bool bucket_dup(const unsigned int *start, const unsigned long long *mask, int mw, int nb,
+                                           long long b) {
+    return !mask || start[b + 1] - start[b] != mask_pop(mask, mw, nb, b);
 }
 
 __global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
                               const unsigned int *__restrict__ start, unsigned int *__restrict__ cursor,
-                              const unsigned long long *__restrict__ mask, unsigned int *__restrict__ entries) {
+                              const unsigned long long *__restrict__ mask, int mw, int nb,
+                              unsigned int *__restrict__ entries) {
     pdl_wait();
     pdl_trigger();
     const int v = blockIdx.y;
@@ -89,8 +98,13 @@ __global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const
         base[j] = 0u;
         if (b[j] >= 0) {
             base[j] = start[b[j]];
-            if (bucket_dup(start, mask, b[j])) slot[j] = atomicAdd(&cursor[b[j]], 1u);
-            else slot[j] = (unsigned int)__popcll(mask[b[j]] & ((1ull << v) - 1ull));
+            if (bucket_dup(start, mask, mw, nb, b[j])) {
+                slot[j] = atomicAdd(&cursor[b[j]], 1u);
+            } else {
+                unsigned int below = 0;  // views before v in this bucket
+                for (int w = 0; w < (v >> 6); ++w) below += (unsigned int)__popcll(mask[(size_t)w * nb + b[j]]);
+                slot[j] = below + (unsigned int)__popcll(mask[(size_t)(v >> 6) * nb + b[j]] & ((1ull << (v & 63)) - 1ull));
+            }
         }
     }
 #pragma unroll
@@ -118,14 +132,14 @@ __device__ __forceinline__ void insertion_sort(unsigned int *a, unsigned int s, 
 }
 
 __global__ void __launch_bounds__(kSortBuckets) k_bucket_sort(int nb, const unsigned int *__restrict__ start,
-                                                              const unsigned long long *__restrict__ mask,
+                                                              const unsigned long long *__restrict__ mask, int mw,
                                                               unsigned int *__restrict__ entries) {
     pdl_wait();
     __shared__ unsigned int buf[kSortCap];
     const int b0 = blockIdx.x * kSortBuckets, b1 = min(b0 + kSortBuckets, nb), b = b0 + (int)threadIdx.x;
     // with a view mask only the buckets with two entries of one view need the sort: each sorts itself in place
     if (mask) {
-        if (b < b1 && bucket_dup(start, mask, b)) insertion_sort(entries, start[b], start[b + 1]);
+        if (b < b1 && bucket_dup(start, mask, mw, nb, b)) insertion_sort(entries, start[b], start[b + 1]);
         return;
     }
     const unsigned int S = start[b0], E = start[b1];
@@ -1148,8 +1162,8 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
     const dim3 b1(256), gs((G.n + 256 * kBucketPer - 1) / (256 * kBucketPer), G.V);
     if (!counted) {  // else k_tau has counted while writing tau
         cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
-        if (B.mask) cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb, st);
-        k_bucket_count<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.count, B.mask);
+        if (B.mask) cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb * B.mask_words, st);
+        k_bucket_count<<<gs, b1, 0, st>>>(G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.count, B.mask, B.nb);
         lc.add(1);
     }
     // exclusive scan of the counts: block-local scans, then every block adds the sum of the block totals before
@@ -1161,9 +1175,9 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
     launch_pdl(k_scan_finish, dim3(nblk), dim3(kScanBlock), 0, st, B.nb, B.start, B.block_sums, B.count);
     lc.add(2);
     launch_pdl(k_bucket_fill, gs, b1, 0, st, G.V, G.n, G.W, G.H, G.dsf, B.BW, tau, B.start, B.count, B.mask,
-               B.entries);
+               B.mask_words, B.nb, B.entries);
     launch_pdl(k_bucket_sort, dim3((B.nb + kSortBuckets - 1) / kSortBuckets), dim3(kSortBuckets), 0, st, B.nb,
-               B.start, B.mask, B.entries);
+               B.start, B.mask, B.mask_words, B.entries);
     lc.add(2);
     (void)ks;
 }

@@ -462,7 +462,7 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
             const long long b = bucket_of(t0, t1, W, H, bc.dsf, bc.BW);
             if (b >= 0) {
                 atomicAdd(&bc.count[b], 1u);
-                if (bc.mask) atomicOr(&bc.mask[b], 1ull << v);
+                if (bc.mask) atomicOr(&bc.mask[(size_t)(v >> 6) * bc.nb + b], 1ull << (v & 63));
             }
         }
     }

@@ -122,7 +122,7 @@ EXPORTED = [
     "lfrv_stage_weights",
     "lfrv_stage_visibility", "lfrv_stage_dataterm", "lfrv_stage_rof", "lfrv_stage_energy", "lfrv_stage_regularizer",
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
-    "lfrv_stage_u_gradient", "lfrv_stage_cg", "lfrv_cg_solve_static", "lfrv_pfm_read", "lfrv_pfm_write", "lfrv_png_read", "lfrv_png_write",
+    "lfrv_stage_u_gradient", "lfrv_stage_cg", "lfrv_stage_poisson_jacobi", "lfrv_cg_solve_static", "lfrv_pfm_read", "lfrv_pfm_write", "lfrv_png_read", "lfrv_png_write",
     "lfrv_scene_params_preset",
     "lfrv_synth_scene", "lfrv_psnr",
 ]
@@ -523,6 +523,14 @@ class Context:
                                          fptr(gx), fptr(gy), fptr(mask)))
         return gx, gy, mask
 
+    def stage_poisson_jacobi(self, gx, gy, mask, U, iterations: int = 200):
+        """poisson_jacobi: `iterations` Jacobi sweeps on a copy of U (3 x H x W)."""
+        gx, gy, mask = f32(gx), f32(gy), f32(mask)
+        U = f32(U).copy()
+        _check(LIB.lfrv_stage_poisson_jacobi(self._h, U.shape[2], U.shape[1], iterations, fptr(gx), fptr(gy),
+                                             fptr(mask), fptr(U)))
+        return U
+
     def stage_cg(self, gx, gy, U, faithful: bool, max_iter: int = 500, gap_tol: float = 1e-4):
         gx, gy = f32(gx), f32(gy)
         U = f32(U).copy()
@@ -622,6 +630,7 @@ def _declare() -> None:
                                      vp, C.POINTER(Stats)]
     LIB.lfrv_stage_rof.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, _F, _F, _F, _F]
     LIB.lfrv_stage_cg.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_double, _F, _F, _F, _I, _D]
+    LIB.lfrv_stage_poisson_jacobi.argtypes = [vp, C.c_int, C.c_int, C.c_int, _F, _F, _F, _F]
     LIB.lfrv_stage_push_pull.argtypes = [vp, C.c_int, C.c_int, C.c_int, _U8, _F]
     LIB.lfrv_stage_hole_fill.argtypes = [vp, C.c_int, C.c_int, C.c_int, _U8, _F, _I]
     LIB.lfrv_synth_scene.argtypes = [C.POINTER(SceneParams), _F, _F, C.POINTER(Camera), _F]

@@ -1404,6 +1404,46 @@ int cg_solve(int W, int H, bool faithful, int max_iter, double gap_tol, const T 
     return it;
 }
 
+// poisson_jacobi, sources/gradientIBR.cu:923-1013 (the Jacobi alternative to the CG, left commented out at
+// sources/gradientIBR.cpp:131): per channel z = (lambda m u0 - div g) / (4 + lambda m) with lambda = 1, m the target
+// mask and div the central-difference divergence of compute_divergence (sources/gradientIBR_kernels.cuh:553-575,
+// zero on the border rows / columns), jacobi_z (:577-598); then `iters` sweeps (200 upstream) of jacobi_B (:600-643):
+// x <- (x_left + x_up + x_right + x_down) / (4 + lambda m) + z, the border pixel standing in for a missing neighbour.
+template <class T>
+void poisson_jacobi(int W, int H, const T *gX, const T *gY, const T *mask, T *U, int iters) {
+    const size_t N = (size_t)W * H;
+    const T lambda = (T)1.0;
+    Vec<T> z(3 * N), tmp(N);
+    for (int c = 0; c < 3; ++c)
+        for (int oy = 0; oy < H; ++oy)
+            for (int ox = 0; ox < W; ++ox) {
+                const size_t o = (size_t)oy * W + ox;
+                T dv = 0;
+                if (ox != 0 && ox != W - 1) dv += (gX[o + 1] - gX[o - 1]) / 2;
+                if (oy != 0 && oy != H - 1) dv += (gY[o + W] - gY[o - W]) / 2;
+                const T data_w = lambda * mask[o];
+                z[c * N + o] = (data_w * U[c * N + o] - dv) / (4 + data_w);
+            }
+    for (int k = 0; k < iters; ++k)
+        for (int c = 0; c < 3; ++c) {
+            T *u = U + c * N;
+            std::copy(u, u + N, tmp.begin());
+#pragma omp parallel for
+            for (int oy = 0; oy < H; ++oy)
+                for (int ox = 0; ox < W; ++ox) {
+                    const size_t o = (size_t)oy * W + ox;
+                    T x = 0;
+                    x += ox == 0 ? tmp[o] : tmp[o - 1];
+                    x += oy == 0 ? tmp[o] : tmp[o - W];
+                    x += ox == W - 1 ? tmp[o] : tmp[o + 1];
+                    x += oy == H - 1 ? tmp[o] : tmp[o + W];
+                    x /= (4 + lambda * mask[o]);
+                    x += z[c * N + o];
+                    u[o] = x;
+                }
+        }
+}
+
 // IBR_gradient, sources/gradientIBR.cpp:12-150.
 template <class T>
 void ibr_gradient(const lfrv_config &cfg, const T *views, const T *tau, int tau_ch, const T *dpart, const T *init,
@@ -1968,6 +2008,19 @@ int orc_stage_cg(int prec, int W, int H, int faithful, int max_iter, double gap_
         std::vector<T> a = conv<T>(gx, N), b = conv<T>(gy, N), u = conv<T>(U, 3 * N);
         const int it = orc::cg_solve<T>(W, H, faithful != 0, max_iter, gap_tol, a.data(), b.data(), u.data(), gap);
         if (iterations) *iterations = it;
+        back(u, U);
+        return 0;
+    };
+    return prec == 0 ? run(double()) : run(float());
+}
+
+int orc_stage_poisson_jacobi(int prec, int W, int H, int iters, const float *gx, const float *gy, const float *mask,
+                             float *U) {
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        const size_t N = (size_t)W * H;
+        std::vector<T> a = conv<T>(gx, N), b = conv<T>(gy, N), m = conv<T>(mask, N), u = conv<T>(U, 3 * N);
+        orc::poisson_jacobi<T>(W, H, a.data(), b.data(), m.data(), u.data(), iters);
         back(u, U);
         return 0;
     };

@@ -152,6 +152,15 @@ def stage_cg(gx, gy, U, faithful, max_iter=500, gap_tol=1e-4, prec=0):
     return U, it.value, gap.value
 
 
+def stage_poisson_jacobi(gx, gy, mask, U, iters=200, prec=0):
+    """poisson_jacobi (sources/gradientIBR.cu:923-1013): `iters` Jacobi sweeps on U (3 x H x W) for the gradient
+    constraint (gx, gy) and the target mask."""
+    gx, gy, mask = f32(gx), f32(gy), f32(mask)
+    U = f32(U).copy()
+    LIB.orc_stage_poisson_jacobi(prec, U.shape[2], U.shape[1], iters, fptr(gx), fptr(gy), fptr(mask), fptr(U))
+    return U
+
+
 def cg_energy(U, U0, gx, gy):
     U, U0, gx, gy = f32(U), f32(U0), f32(gx), f32(gy)
     return LIB.orc_cg_energy(U.shape[2], U.shape[1], fptr(U), fptr(U0), fptr(gx), fptr(gy))

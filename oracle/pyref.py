@@ -311,6 +311,16 @@ def hole_fill(U, vis, max_iter=500):
     return u.reshape(3, H, W), it
 
 
+def poisson_jacobi(gx, gy, mask, U, iters=200):
+    """poisson_jacobi (sources/gradientIBR.cu:923-1013) through the reference's compute_divergence, jacobi_z and
+    jacobi_B kernels."""
+    U = np.ascontiguousarray(U, np.float32).copy()
+    H, W = U.shape[1], U.shape[2]
+    gx, gy, mask = (np.ascontiguousarray(a, np.float32).copy() for a in (gx, gy, mask))
+    LIB.refg_poisson_jacobi(W, H, iters, _f(gx), _f(gy), _f(mask), _f(U[0]), _f(U[1]), _f(U[2]))
+    return U
+
+
 if LIB is not None:
     LIB.ref_scale.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float), F]
     LIB.ref_clamp.argtypes = [C.c_int, C.c_int, C.POINTER(C.c_float), F, F]

@@ -305,3 +305,44 @@ def test_solve_is_deterministic(ctx):
     a, _ = ctx.ibr_color(cfg, sc.views, tau, dpart)
     b, _ = ctx.ibr_color(cfg, sc.views, tau, dpart)
     assert np.array_equal(a, b)
+
+
+def test_inverse_map_more_than_64_views(ctx):
+    """A 9x9 light field (80 input views, two 64-bit view-mask words per bucket of the inverse footprint map):
+    IBR_gradient against the FP64 oracle at a fixed CG iteration count, and IBR_color's data term."""
+    import lfrv
+
+    p = lfrv.scene_params(2, w=24, h=24, grid=9, seed=4)
+    sc = lfrv.synth_scene(p)
+    assert sc.views.shape[0] == 80
+    tau, dpart, _ = pyoracle.warp(sc.depth, sc.cams, sc.target)
+    cfg = gradient_config(sc, cg_gap_tol=0.0, cg_max_iter=10)
+    out, st = ctx.ibr_gradient(cfg, sc.views, tau, dpart)
+    ref, rst = pyoracle.ibr_gradient(cfg, sc.views, tau, dpart, prec=0)
+    assert st.outer_iterations == rst.outer_iterations == 10
+    assert rel_err(out, ref) <= 1e-4
+    ccfg = color_config(sc)
+    rng = np.random.default_rng(3)
+    H = W = 24 * p.dsf
+    U = rng.uniform(0, 1, (3, H, W)).astype(np.float32)
+    wg = rng.uniform(0.5e4, 1e4, (80, 24, 24)).astype(np.float32)
+    G, F = ctx.stage_dataterm(ccfg, sc.views, tau, wg, U)
+    rG, rF = pyoracle.stage_dataterm(ccfg, sc.views, tau, wg, U, prec=1)
+    assert rel_err(G, rG, floor=1e-2) < 1e-4
+
+
+@pytest.mark.parametrize("H,W,iters", [(48, 64, 200), (37, 53, 13), (200, 296, 200)])
+def test_poisson_jacobi(ctx, H, W, iters):
+    """poisson_jacobi (sources/gradientIBR.cu:923-1013) on the GPU: bit for bit against the FP32 mirror (which is
+    pinned to the reference's kernels), and within 1e-5 of the FP64 oracle; odd sweep counts end mid super-step."""
+    rng = np.random.default_rng(13)
+    U = rng.uniform(0.1, 0.9, (3, H, W)).astype(np.float32)
+    gx = rng.normal(0, 0.05, (H, W)).astype(np.float32)
+    gy = rng.normal(0, 0.05, (H, W)).astype(np.float32)
+    mask = rng.uniform(0, 1.5, (H, W)).astype(np.float32)
+    mask[H // 4:H // 2, W // 8:W // 2] = 0.0
+    out = ctx.stage_poisson_jacobi(gx, gy, mask, U, iters)
+    ref32 = pyoracle.stage_poisson_jacobi(gx, gy, mask, U, iters, prec=1)
+    ref64 = pyoracle.stage_poisson_jacobi(gx, gy, mask, U, iters, prec=0)
+    np.testing.assert_array_equal(out, ref32)
+    assert np.max(np.abs(out - ref64)) < 1e-5

@@ -131,3 +131,17 @@ def test_hole_fill_bitexact():
     u, it = pyref.hole_fill(U, vis)
     out, oit = pyoracle.stage_hole_fill(U, vis, 500, prec=1)
     assert oit == it and np.array_equal(u, out)
+
+
+def test_poisson_jacobi_bitexact():
+    """The Jacobi variant of the Poisson integration (poisson_jacobi, sources/gradientIBR.cu:923-1013)."""
+    rng = np.random.default_rng(12)
+    H, W = 37, 52
+    U = rng.uniform(0.1, 0.9, (3, H, W)).astype(np.float32)
+    gx = rng.normal(0, 0.05, (H, W)).astype(np.float32)
+    gy = rng.normal(0, 0.05, (H, W)).astype(np.float32)
+    mask = rng.uniform(0, 1.5, (H, W)).astype(np.float32)
+    mask[10:20, 5:25] = 0.0
+    ref = pyref.poisson_jacobi(gx, gy, mask, U, iters=40)
+    out = pyoracle.stage_poisson_jacobi(gx, gy, mask, U, iters=40, prec=1)
+    assert np.array_equal(ref, out)
