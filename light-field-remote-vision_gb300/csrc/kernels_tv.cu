@@ -75,13 +75,16 @@ __device__ __forceinline__ float tv_div(const float *px, const float *py, int W,
 }
 
 // ------------------------------------------------------------------ certificate
+// One-dimensional blocks of kGapBX * kGapBY threads (block_sum indexes warps by threadIdx.x), each covering a
+// kGapBX x kGapBY patch of pixels.
 constexpr int kGapBX = 32, kGapBY = 8;
 __global__ void __launch_bounds__(kGapBX * kGapBY) k_tv_gap(int W, int H, const float *__restrict__ u,
                                                             const float *__restrict__ gf, const float *__restrict__ P,
                                                             const float *__restrict__ g, float lambda,
                                                             double *__restrict__ partial) {
     __shared__ double red[kGapBX * kGapBY / 32];
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int x = blockIdx.x * kGapBX + (int)(threadIdx.x % kGapBX);
+    const int y = blockIdx.y * kGapBY + (int)(threadIdx.x / kGapBX);
     const size_t N = (size_t)W * H;
     double tv = 0.0, inner = 0.0, box = 0.0;
     if (x < W && y < H) {
@@ -102,11 +105,11 @@ __global__ void __launch_bounds__(kGapBX * kGapBY) k_tv_gap(int W, int H, const 
     }
     const int b = blockIdx.y * gridDim.x + blockIdx.x, nb = gridDim.x * gridDim.y;
     const double s0 = block_sum<kGapBX * kGapBY>(tv, red);
-    if (threadIdx.x == 0 && threadIdx.y == 0) partial[b] = s0;
+    if (threadIdx.x == 0) partial[b] = s0;
     const double s1 = block_sum<kGapBX * kGapBY>(inner, red);
-    if (threadIdx.x == 0 && threadIdx.y == 0) partial[nb + b] = s1;
+    if (threadIdx.x == 0) partial[nb + b] = s1;
     const double s2 = block_sum<kGapBX * kGapBY>(box, red);
-    if (threadIdx.x == 0 && threadIdx.y == 0) partial[2 * nb + b] = s2;
+    if (threadIdx.x == 0) partial[2 * nb + b] = s2;
 }
 
 __global__ void k_tv_fstep(size_t N, const float *__restrict__ u, const float *__restrict__ up,
@@ -284,8 +287,8 @@ int tv_gap_partials(int W, int H) { return ((W + kGapBX - 1) / kGapBX) * ((H + k
 void launch_tv_gap(int W, int H, const float *u, const float *gf, const float *P, const float *g, float lambda,
                    double *partial, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "tv_gap", st);
-    const dim3 b(kGapBX, kGapBY), gr = tv_grid(W, H, b);
-    k_tv_gap<<<gr, b, 0, st>>>(W, H, u, gf, P, g, lambda, partial);
+    const dim3 gr = tv_grid(W, H, dim3(kGapBX, kGapBY));
+    k_tv_gap<<<gr, kGapBX * kGapBY, 0, st>>>(W, H, u, gf, P, g, lambda, partial);
     lc.add(1);
 }
 
