@@ -55,7 +55,7 @@ struct Workspace {
     DevBuf in_views, in_tau, in_dpart, in_init, out_img;
     // host-buffer batched calls: one device copy per distinct light field (views, depth) and the outputs
     DevBuf hb_in, hb_out;
-    // corrected IBR_color: iterates, data gradients, metric and the dual / momentum fields (39 N floats)
+    // corrected IBR_color: iterates, data gradients and metric (15 N floats), the FP64 dual / momentum fields (24 N)
     DevBuf tv;
 };
 

@@ -552,9 +552,13 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
     int tv_trace_pos = 0;
     auto tv_meta = [&](int meta) -> int {
         const size_t N3 = 3 * N;
-        ws.tv.ensure(sizeof(float) * 39 * N);
+        // 15 N floats (u, u_prev, grad f, grad f_prev, D, lam, 1/L), then 24 N doubles (p, its ping-pong copy, q x 2)
+        const size_t fbytes = (sizeof(float) * 15 * N + 255) / 256 * 256;
+        ws.tv.ensure(fbytes + sizeof(double) * 24 * N);
         float *u = ws.tv.as<float>(), *up = u + N3, *gf = up + N3, *gfp = gf + N3, *D = gfp + N3, *lam = D + N,
-              *linv = lam + N, *P0 = linv + N, *P1 = P0 + 6 * N, *Q0 = P1 + 6 * N, *Q1 = Q0 + 6 * N;
+              *linv = lam + N;
+        double *P0 = reinterpret_cast<double *>(ws.tv.as<char>() + fbytes), *P1 = P0 + 6 * N, *Q0 = P1 + 6 * N,
+               *Q1 = Q0 + 6 * N;
         const float as2 = cfg.dt_alpha * s2;
         launch_tv_metric(G, B, tau2, b.wgt, as2, cfg.lambda, D, lam, linv, s, c->launches);
         check_launch("tv metric");
@@ -562,7 +566,7 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         // u_prev = u and grad f(u_prev) = 0: the first step (theta = 0) reads them only through zero factors
         LFRV_CUDA(cudaMemcpyAsync(up, u, sizeof(float) * N3, cudaMemcpyDeviceToDevice, s));
         LFRV_CUDA(cudaMemsetAsync(gfp, 0, sizeof(float) * N3, s));
-        if (meta == 0) LFRV_CUDA(cudaMemsetAsync(P0, 0, sizeof(float) * 6 * N, s));
+        if (meta == 0) LFRV_CUDA(cudaMemsetAsync(P0, 0, sizeof(double) * 6 * N, s));
         const int npart = tv_gap_partials(G.W, G.H);
         const double tol = cfg.cg_gap_tol;
         double t = 1.0, E_prev = 1e300;

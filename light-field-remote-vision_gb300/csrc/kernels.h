@@ -186,10 +186,10 @@ void launch_tv_metric(const Geometry &G, const Buckets &B, const float *tau, con
 // grad f = as2 sum_i A_i^T res_i (3 planes) from the splat-set residuals of launch_residual.
 void launch_tv_gradf(const Geometry &G, const Buckets &B, const float *tau, const float *res, float as2, float *gf,
                      cudaStream_t st, LaunchCounter &lc);
-// FP64 block partials of J_g(u), sum <grad u, p> and the box term of the certificate (c = gf - lambda div p),
+// FP64 block partials of J_g(u), sum <grad u, p> and the box term of the certificate (c = gf - lambda div p; p FP64),
 // three arrays of tv_gap_partials(W, H) entries each.
 int tv_gap_partials(int W, int H);
-void launch_tv_gap(int W, int H, const float *u, const float *gf, const float *P, const float *g, float lambda,
+void launch_tv_gap(int W, int H, const float *u, const float *gf, const double *P, const float *g, float lambda,
                    double *partial, cudaStream_t st, LaunchCounter &lc);
 // F = y - grad f(y) / D, y = u + theta (u - u_prev), grad f(y) = (1 + theta) gf - theta gf_prev (3 planes).
 void launch_tv_fstep(int W, int H, const float *u, const float *up, const float *gf, const float *gfp, const float *D,
@@ -197,10 +197,10 @@ void launch_tv_fstep(int W, int H, const float *u, const float *up, const float 
 // out = clamp(in, 0, 1) over n floats.
 void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, LaunchCounter &lc);
 // niter FGP iterations on the dual of the weighted ROF problem (one cooperative launch): P0 holds the starting
-// dual (6 planes: x parts of the 3 channels, then the y parts) and receives the final one; P1, Q0, Q1 are scratch
-// (6 planes each); U receives clamp(F + lam div p, 0, 1).
+// dual (6 FP64 planes: x parts of the 3 channels, then the y parts) and receives the final one; P1, Q0, Q1 are
+// scratch (6 FP64 planes each); U receives clamp(F + lam div p, 0, 1).
 cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *lam, const float *linv, const float *g,
-                          float *P0, float *P1, float *Q0, float *Q1, float *U, GridBarrier gb, cudaStream_t st,
+                          double *P0, double *P1, double *Q0, double *Q1, float *U, GridBarrier gb, cudaStream_t st,
                           LaunchCounter &lc);
 
 // One target of a batched CG launch (k_cg_batch): its image, buffers and the contiguous range of blocks that

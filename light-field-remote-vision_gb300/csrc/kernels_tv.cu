@@ -65,8 +65,9 @@ __global__ void k_tv_gradf(int W, int H, int n, int dsf, int BW, const unsigned 
 }
 
 // div of a dual field at (x, y): the negative adjoint of the forward gradient with zero at the last column / row.
-__device__ __forceinline__ float tv_div(const float *px, const float *py, int W, int H, int x, int y, size_t o) {
-    float d = 0.f;
+template <typename TD>
+__device__ __forceinline__ TD tv_div(const TD *px, const TD *py, int W, int H, int x, int y, size_t o) {
+    TD d = 0;
     if (x < W - 1) d += px[o];
     if (x > 0) d -= px[o - 1];
     if (y < H - 1) d += py[o];
@@ -79,7 +80,7 @@ __device__ __forceinline__ float tv_div(const float *px, const float *py, int W,
 // kGapBX x kGapBY patch of pixels.
 constexpr int kGapBX = 32, kGapBY = 8;
 __global__ void __launch_bounds__(kGapBX * kGapBY) k_tv_gap(int W, int H, const float *__restrict__ u,
-                                                            const float *__restrict__ gf, const float *__restrict__ P,
+                                                            const float *__restrict__ gf, const double *__restrict__ P,
                                                             const float *__restrict__ g, float lambda,
                                                             double *__restrict__ partial) {
     __shared__ double red[kGapBX * kGapBY / 32];
@@ -96,9 +97,9 @@ __global__ void __launch_bounds__(kGapBX * kGapBY) k_tv_gap(int W, int H, const 
             const double gxv = x < W - 1 ? (double)uc[o + 1] - (double)uc[o] : 0.0;
             const double gyv = y < H - 1 ? (double)uc[o + W] - (double)uc[o] : 0.0;
             n2 += gxv * gxv + gyv * gyv;
-            const float *px = P + c * N, *py = P + (3 + c) * N;
-            inner += gxv * (double)px[o] + gyv * (double)py[o];
-            const double cc = (double)gf[c * N + o] - (double)lambda * (double)tv_div(px, py, W, H, x, y, o);
+            const double *px = P + c * N, *py = P + (3 + c) * N;
+            inner += gxv * px[o] + gyv * py[o];
+            const double cc = (double)gf[c * N + o] - (double)lambda * tv_div(px, py, W, H, x, y, o);
             box += (double)uc[o] * cc - fmin(0.0, cc);
         }
         tv = (double)g[o] * sqrt(n2);
@@ -136,27 +137,31 @@ __global__ void k_tv_clamp(size_t n, const float *__restrict__ in, float *__rest
 // with beta_j = (s_j - 1) / s_{j+1}, s_0 = 1, s_{j+1} = (1 + sqrt(1 + 4 s_j^2)) / 2 (Beck and Teboulle's FGP).
 constexpr int kFgpTX = 32, kFgpTY = 16, kFgpK = 4, kFgpThreads = 512;
 constexpr int kFgpRX = kFgpTX + 2 * kFgpK, kFgpRY = kFgpTY + 2 * kFgpK, kFgpRN = kFgpRX * kFgpRY;
-constexpr int kFgpPlanes = 21;  // q 6, p 6, u 3, F 3, lam, 1/L, g
-constexpr size_t kFgpSmem = (size_t)kFgpPlanes * kFgpRN * sizeof(float);
+// The dual p and the momentum point q are FP64 (12 planes), everything else FP32 (u 3, F 3, lam, 1/L, g). In FP32
+// the dual's rounding (a few ulp of |p| <= g) leaves lambda div p, and with it the certificate's box term, a noise
+// floor near 4e-4 relative at 256^2; the FP64 dual certifies 1e-4 (the oracle's FP32 mirror shows the same).
+constexpr size_t kFgpSmem = (size_t)12 * kFgpRN * sizeof(double) + (size_t)9 * kFgpRN * sizeof(float);
 
 __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter, const float *__restrict__ F,
                                                         const float *__restrict__ lam, const float *__restrict__ linv,
-                                                        const float *__restrict__ g, float *P0, float *P1, float *Q0,
-                                                        float *Q1, float *__restrict__ U, GridBarrier gb) {
-    extern __shared__ float sm[];
-    float *sQ = sm, *sP = sm + 6 * kFgpRN, *sU = sm + 12 * kFgpRN, *sF = sm + 15 * kFgpRN;
-    float *sL = sm + 18 * kFgpRN, *sI = sm + 19 * kFgpRN, *sG = sm + 20 * kFgpRN;
+                                                        const float *__restrict__ g, double *P0, double *P1,
+                                                        double *Q0, double *Q1, float *__restrict__ U,
+                                                        GridBarrier gb) {
+    extern __shared__ __align__(16) unsigned char fgp_sm[];
+    double *sQ = reinterpret_cast<double *>(fgp_sm), *sP = sQ + 6 * kFgpRN;
+    float *sU = reinterpret_cast<float *>(sP + 6 * kFgpRN), *sF = sU + 3 * kFgpRN;
+    float *sL = sF + 3 * kFgpRN, *sI = sL + kFgpRN, *sG = sI + kFgpRN;
     const int tiles_x = (W + kFgpTX - 1) / kFgpTX, ntiles = tiles_x * ((H + kFgpTY - 1) / kFgpTY);
     const size_t N = (size_t)W * H;
     unsigned int gen = 0;
-    float s_step = 1.0f;  // s_j at the start of the super-step (every thread follows the same sequence)
+    double s_step = 1.0;  // s_j at the start of the super-step (every thread follows the same sequence)
     int step = 0;
     for (int done = 0; done < niter; done += kFgpK, ++step) {
         const int iters = min(kFgpK, niter - done);
-        const float *Pi = (step & 1) ? P1 : P0;
-        float *Po = (step & 1) ? P0 : P1;
-        const float *Qi = step == 0 ? P0 : ((step & 1) ? Q1 : Q0);  // q starts at p
-        float *Qo = (step & 1) ? Q0 : Q1;
+        const double *Pi = (step & 1) ? P1 : P0;
+        double *Po = (step & 1) ? P0 : P1;
+        const double *Qi = step == 0 ? P0 : ((step & 1) ? Q1 : Q0);  // q starts at p
+        double *Qo = (step & 1) ? Q0 : Q1;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
             const int rx0 = (t % tiles_x) * kFgpTX - kFgpK, ry0 = (t / tiles_x) * kFgpTY - kFgpK;
             for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
@@ -165,8 +170,8 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                 const size_t o = in ? (size_t)gy * W + gx : 0;
 #pragma unroll
                 for (int k = 0; k < 6; ++k) {
-                    sQ[k * kFgpRN + i] = in ? __ldcg(Qi + k * N + o) : 0.f;
-                    sP[k * kFgpRN + i] = in ? __ldcg(Pi + k * N + o) : 0.f;
+                    sQ[k * kFgpRN + i] = in ? __ldcg(Qi + k * N + o) : 0.0;
+                    sP[k * kFgpRN + i] = in ? __ldcg(Pi + k * N + o) : 0.0;
                 }
 #pragma unroll
                 for (int c = 0; c < 3; ++c) sF[c * kFgpRN + i] = in ? __ldg(F + c * N + o) : 0.f;
@@ -175,23 +180,23 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                 sG[i] = in ? __ldg(g + o) : 0.f;
             }
             __syncthreads();
-            float s = s_step;
+            double s = s_step;
             for (int it = 0; it < iters; ++it) {
-                const float s1 = 0.5f * (1.0f + sqrtf(1.0f + 4.0f * s * s));
-                const float beta = (s - 1.0f) / s1;
+                const double s1 = 0.5 * (1.0 + sqrt(1.0 + 4.0 * s * s));
+                const double beta = (s - 1.0) / s1;
                 // u(q) on the region (values next to the region's edge are stale and stay outside the tile)
                 for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
                     const int lx = i % kFgpRX, ly = i / kFgpRX, gx = rx0 + lx, gy = ry0 + ly;
                     if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const float *qx = sQ + c * kFgpRN, *qy = sQ + (3 + c) * kFgpRN;
-                        float d = 0.f;
+                        const double *qx = sQ + c * kFgpRN, *qy = sQ + (3 + c) * kFgpRN;
+                        double d = 0.0;
                         if (gx < W - 1) d += qx[i];
-                        if (gx > 0) d -= lx > 0 ? qx[i - 1] : 0.f;
+                        if (gx > 0) d -= lx > 0 ? qx[i - 1] : 0.0;
                         if (gy < H - 1) d += qy[i];
-                        if (gy > 0) d -= ly > 0 ? qy[i - kFgpRX] : 0.f;
-                        sU[c * kFgpRN + i] = fminf(1.0f, fmaxf(0.0f, sF[c * kFgpRN + i] + sL[i] * d));
+                        if (gy > 0) d -= ly > 0 ? qy[i - kFgpRX] : 0.0;
+                        sU[c * kFgpRN + i] = fminf(1.0f, fmaxf(0.0f, sF[c * kFgpRN + i] + sL[i] * (float)d));
                     }
                 }
                 __syncthreads();
@@ -199,8 +204,8 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                 for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
                     const int lx = i % kFgpRX, ly = i / kFgpRX, gx = rx0 + lx, gy = ry0 + ly;
                     if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
-                    float v[6];
-                    float n2 = 0.f;
+                    double v[6];
+                    double n2 = 0.0;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         const float *uc = sU + c * kFgpRN;
@@ -208,15 +213,16 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                         const float ud = (ly + 1 < kFgpRY) ? uc[i + kFgpRX] : 0.f;
                         const float gxv = gx < W - 1 ? ur - uc[i] : 0.f;
                         const float gyv = gy < H - 1 ? ud - uc[i] : 0.f;
-                        v[c] = sQ[c * kFgpRN + i] + gxv * sI[i];
-                        v[3 + c] = sQ[(3 + c) * kFgpRN + i] + gyv * sI[i];
+                        v[c] = sQ[c * kFgpRN + i] + (double)(gxv * sI[i]);
+                        v[3 + c] = sQ[(3 + c) * kFgpRN + i] + (double)(gyv * sI[i]);
                         n2 += v[c] * v[c] + v[3 + c] * v[3 + c];
                     }
-                    const float nrm = sqrtf(n2);
-                    const float sc = nrm > sG[i] ? sG[i] / nrm : 1.0f;
+                    const double nrm = sqrt(n2);
+                    const double gv = (double)sG[i];
+                    const double sc = nrm > gv ? gv / nrm : 1.0;
 #pragma unroll
                     for (int k = 0; k < 6; ++k) {
-                        const float pn = v[k] * sc;
+                        const double pn = v[k] * sc;
                         sQ[k * kFgpRN + i] = pn + beta * (pn - sP[k * kFgpRN + i]);
                         sP[k * kFgpRN + i] = pn;
                     }
@@ -237,19 +243,19 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
             }
             __syncthreads();  // the next tile overwrites the staged region
         }
-        for (int it = 0; it < iters; ++it) s_step = 0.5f * (1.0f + sqrtf(1.0f + 4.0f * s_step * s_step));
+        for (int it = 0; it < iters; ++it) s_step = 0.5 * (1.0 + sqrt(1.0 + 4.0 * s_step * s_step));
         if (!grid_sync(gb, gen)) return;
     }
     // the final dual sits in P0 after an even number of super-steps, else in P1; u = clamp(F + lam div p)
     const int steps = (niter + kFgpK - 1) / kFgpK;
-    const float *Pf = (steps & 1) ? P1 : P0;
-    float *Pother = (steps & 1) ? P0 : P1;
+    const double *Pf = (steps & 1) ? P1 : P0;
+    double *Pother = (steps & 1) ? P0 : P1;
     for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < N; o += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(o % W), y = (int)(o / W);
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-            const float d = tv_div(Pf + c * N, Pf + (3 + c) * N, W, H, x, y, o);
-            U[c * N + o] = fminf(1.0f, fmaxf(0.0f, F[c * N + o] + lam[o] * d));
+            const double d = tv_div(Pf + c * N, Pf + (3 + c) * N, W, H, x, y, o);
+            U[c * N + o] = fminf(1.0f, fmaxf(0.0f, F[c * N + o] + lam[o] * (float)d));
         }
     }
     // the caller keeps its dual in P0: copy it there when the last super-step wrote P1
@@ -284,7 +290,7 @@ void launch_tv_gradf(const Geometry &G, const Buckets &B, const float *tau, cons
 
 int tv_gap_partials(int W, int H) { return ((W + kGapBX - 1) / kGapBX) * ((H + kGapBY - 1) / kGapBY); }
 
-void launch_tv_gap(int W, int H, const float *u, const float *gf, const float *P, const float *g, float lambda,
+void launch_tv_gap(int W, int H, const float *u, const float *gf, const double *P, const float *g, float lambda,
                    double *partial, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "tv_gap", st);
     const dim3 gr = tv_grid(W, H, dim3(kGapBX, kGapBY));
@@ -307,7 +313,7 @@ void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, Lau
 }
 
 cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *lam, const float *linv, const float *g,
-                          float *P0, float *P1, float *Q0, float *Q1, float *U, GridBarrier gb, cudaStream_t st,
+                          double *P0, double *P1, double *Q0, double *Q1, float *U, GridBarrier gb, cudaStream_t st,
                           LaunchCounter &lc) {
     ProfScope _ps(lc, "tv_fgp", st);
     int dev = 0, sms = 0, per_sm = 0;

@@ -864,6 +864,10 @@ void color_fista_iteration(ColorState<T> &S) {
 // (the Fenchel dual of the problem with the data term's dual variable at its optimum for u). The solver stops
 // when gap / E <= cfg.cg_gap_tol or after cfg.niter outer iterations.
 constexpr int kTvInner = 200;
+// The dual field p and its momentum point are double in both builds: in float, their rounding (a few ulp of
+// |p| <= g) leaves lambda div p, and with it the certificate's box term, a noise floor near 4e-4 relative at 256^2.
+// The GPU keeps the same FP64 dual with FP32 iterates, so the FP32 mirror stays its like-for-like reference.
+using TvDual = double;
 constexpr double kTvDelta = 1.0;
 
 // grad f(u) (3 planes) and f(u): residuals over the splat set.
@@ -922,21 +926,22 @@ inline T tv_div_at(const T *px, const T *py, int W, int H, int x, int y) {
 // diag(L) with L_x = 8 max(lam_x, lam_{x+1}, lam_{x+W}) (each dual entry enters the divergence at two pixels, each
 // divergence has four terms), so the fast gradient projection converges in that metric; the ball projection stays
 // a radial scaling since L_x is one scalar for the six entries of pixel x. P: px (3 planes), py (3 planes).
-template <class T>
-void tv_fgp(int W, int H, const Vec<T> *F, const Vec<T> &lam, const Vec<T> &g, const Vec<T> &Linv, Vec<T> *P,
+template <class T, class TP>
+void tv_fgp(int W, int H, const Vec<T> *F, const Vec<T> &lam, const Vec<T> &g, const Vec<T> &Linv, Vec<TP> *P,
             int iters, Vec<T> *U) {
     const size_t N = (size_t)W * H;
-    Vec<T> Q[6], Pn[6], u[3];
+    Vec<TP> Q[6], Pn[6];
+    Vec<T> u[3];
     for (int k = 0; k < 6; ++k) Q[k] = P[k], Pn[k].assign(N, 0);
     for (int c = 0; c < 3; ++c) u[c].assign(N, 0);
     double s = 1;
-    auto primal = [&](const Vec<T> *q, Vec<T> *out) {
+    auto primal = [&](const Vec<TP> *q, Vec<T> *out) {
         for (int c = 0; c < 3; ++c) {
 #pragma omp parallel for
             for (int y = 0; y < H; ++y)
                 for (int x = 0; x < W; ++x) {
                     const size_t o = (size_t)y * W + x;
-                    const T v = F[c][o] + lam[o] * tv_div_at(q[c].data(), q[3 + c].data(), W, H, x, y);
+                    const T v = F[c][o] + lam[o] * (T)tv_div_at(q[c].data(), q[3 + c].data(), W, H, x, y);
                     out[c][o] = std::min((T)1, std::max((T)0, v));
                 }
         }
@@ -944,24 +949,24 @@ void tv_fgp(int W, int H, const Vec<T> *F, const Vec<T> &lam, const Vec<T> &g, c
     for (int it = 0; it < iters; ++it) {
         primal(Q, u);
         const double s1 = 0.5 * (1.0 + std::sqrt(1.0 + 4.0 * s * s));
-        const T beta = (T)((s - 1.0) / s1);
+        const TP beta = (TP)((s - 1.0) / s1);
 #pragma omp parallel for
         for (int y = 0; y < H; ++y)
             for (int x = 0; x < W; ++x) {
                 const size_t o = (size_t)y * W + x;
-                T v[6];
-                T nrm = 0;
+                TP v[6];
+                TP nrm = 0;
                 for (int c = 0; c < 3; ++c) {
                     const T gxv = x < W - 1 ? u[c][o + 1] - u[c][o] : T(0);
                     const T gyv = y < H - 1 ? u[c][o + W] - u[c][o] : T(0);
-                    v[c] = Q[c][o] + gxv * Linv[o];
-                    v[3 + c] = Q[3 + c][o] + gyv * Linv[o];
+                    v[c] = Q[c][o] + (TP)(gxv * Linv[o]);
+                    v[3 + c] = Q[3 + c][o] + (TP)(gyv * Linv[o]);
                     nrm += v[c] * v[c] + v[3 + c] * v[3 + c];
                 }
                 nrm = std::sqrt(nrm);
-                const T sc = nrm > g[o] ? g[o] / nrm : T(1);
+                const TP sc = nrm > (TP)g[o] ? (TP)g[o] / nrm : TP(1);
                 for (int k = 0; k < 6; ++k) {
-                    const T pn = v[k] * sc;
+                    const TP pn = v[k] * sc;
                     Q[k][o] = pn + beta * (pn - P[k][o]);
                     Pn[k][o] = pn;
                 }
@@ -973,8 +978,8 @@ void tv_fgp(int W, int H, const Vec<T> *F, const Vec<T> &lam, const Vec<T> &g, c
 }
 
 // E(u) and the certified gap for the dual p (see above); J_g(u) through *J.
-template <class T>
-double tv_gap(int W, int H, const Vec<T> *U, const Vec<T> *gf, const Vec<T> *P, const Vec<T> &g, double lambda,
+template <class T, class TP>
+double tv_gap(int W, int H, const Vec<T> *U, const Vec<T> *gf, const Vec<TP> *P, const Vec<T> &g, double lambda,
               double *J) {
     double tv = 0, inner = 0, box = 0;
 #pragma omp parallel for reduction(+ : tv, inner, box)
@@ -1027,7 +1032,8 @@ int tv_solve(ColorState<T> &S, int max_outer, double tol, double *E_out, double 
             if (y < H - 1) m = std::max(m, lam[o + W]);
             Linv[o] = (T)(1.0 / (8.0 * (double)m));
         }
-    Vec<T> u[3], up[3], gf[3], gfp[3], Fy[3], P[6];
+    Vec<T> u[3], up[3], gf[3], gfp[3], Fy[3];
+    Vec<TvDual> P[6];
     for (int c = 0; c < 3; ++c) {
         u[c].resize(N);
         for (size_t o = 0; o < N; ++o) u[c][o] = std::min((T)1, std::max((T)0, S.U[c][o]));
@@ -1036,7 +1042,7 @@ int tv_solve(ColorState<T> &S, int max_outer, double tol, double *E_out, double 
         gfp[c].assign(N, 0);
         Fy[c].assign(N, 0);
     }
-    for (int k = 0; k < 6; ++k) P[k] = P0 ? P0[k] : Vec<T>(N, T(0));
+    for (int k = 0; k < 6; ++k) P[k].assign(N, TvDual(0));
     double t = 1.0, E = 0, gap = 1e300, E_prev = 1e300;
     int k;
     for (k = 0;; ++k) {
