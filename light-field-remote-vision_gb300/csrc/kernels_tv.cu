@@ -217,9 +217,17 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                         v[3 + c] = sQ[(3 + c) * kFgpRN + i] + (double)(gyv * sI[i]);
                         n2 += v[c] * v[c] + v[3 + c] * v[3 + c];
                     }
-                    const double nrm = sqrt(n2);
+                    // projection onto |p| <= g without an FP64 square root or division (both are long sequences on
+                    // this GPU's narrow FP64 pipe): r = 1 / sqrt(n2) from the FP32 estimate and one FP64 Newton step
+                    // (relative error ~1e-14), applied only where the ball constraint is active
                     const double gv = (double)sG[i];
-                    const double sc = nrm > gv ? gv / nrm : 1.0;
+                    double sc = 1.0;
+                    if (n2 > gv * gv) {
+                        double r = (double)rsqrtf((float)n2);
+                        r = r * (1.5 - 0.5 * n2 * r * r);
+                        r = r * (1.5 - 0.5 * n2 * r * r);
+                        sc = gv * r;
+                    }
 #pragma unroll
                     for (int k = 0; k < 6; ++k) {
                         const double pn = v[k] * sc;
