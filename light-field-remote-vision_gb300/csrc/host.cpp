@@ -570,6 +570,7 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         const int npart = tv_gap_partials(G.W, G.H);
         const double tol = cfg.cg_gap_tol;
         double t = 1.0, E_prev = 1e300;
+        bool fp64 = false;
         int k;
         for (k = 0;; ++k) {
             residual(c, G, u, img, tau2, b.wgt, s2, b.res, 1, true);
@@ -599,8 +600,11 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
             std::swap(u, up);
             std::swap(gf, gfp);
             const GridBarrier gb = fresh_barrier(c);
+            // FP32 dual arithmetic while the gap is far above FP32's floor, FP64 once it nears it (the switch only
+            // changes rounding, not the iteration)
+            fp64 = fp64 || tv_gap_last < kTvFp64Below;
             LFRV_CUDA(launch_tv_fgp(G.W, G.H, kTvInnerIterations, b.F, lam, linv, b.g, P0, P1, Q0, Q1, u, gb, s,
-                                    c->launches));
+                                    c->launches, fp64));
         }
         LFRV_CUDA(cudaMemcpyAsync(ws.U.p, u, sizeof(float) * N3, cudaMemcpyDeviceToDevice, s));
         return k;

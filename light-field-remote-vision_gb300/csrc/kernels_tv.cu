@@ -137,18 +137,22 @@ __global__ void k_tv_clamp(size_t n, const float *__restrict__ in, float *__rest
 // with beta_j = (s_j - 1) / s_{j+1}, s_0 = 1, s_{j+1} = (1 + sqrt(1 + 4 s_j^2)) / 2 (Beck and Teboulle's FGP).
 constexpr int kFgpTX = 32, kFgpTY = 16, kFgpK = 4, kFgpThreads = 512;
 constexpr int kFgpRX = kFgpTX + 2 * kFgpK, kFgpRY = kFgpTY + 2 * kFgpK, kFgpRN = kFgpRX * kFgpRY;
-// The dual p and the momentum point q are FP64 (12 planes), everything else FP32 (u 3, F 3, lam, 1/L, g). In FP32
-// the dual's rounding (a few ulp of |p| <= g) leaves lambda div p, and with it the certificate's box term, a noise
-// floor near 4e-4 relative at 256^2; the FP64 dual certifies 1e-4 (the oracle's FP32 mirror shows the same).
-constexpr size_t kFgpSmem = (size_t)12 * kFgpRN * sizeof(double) + (size_t)9 * kFgpRN * sizeof(float);
+// The dual p and the momentum point q are stored in FP64 (12 planes); u, F, lam, 1/L and g are FP32. TD is the
+// dual's arithmetic (and shared-memory) type. In FP32 the dual's rounding (a few ulp of |p| <= g) leaves
+// lambda div p, and with it the certificate's box term, a noise floor near 4e-4 relative at 256^2; with TD = double
+// the certificate reaches 1e-4 (the oracle's FP32 mirror shows the same). FP64 is slow on this GPU's narrow FP64
+// pipe, so the host runs TD = float while the gap is far above its floor and TD = double to finish.
+template <typename TD>
+constexpr size_t fgp_smem() { return (size_t)12 * kFgpRN * sizeof(TD) + (size_t)9 * kFgpRN * sizeof(float); }
 
+template <typename TD>
 __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter, const float *__restrict__ F,
                                                         const float *__restrict__ lam, const float *__restrict__ linv,
                                                         const float *__restrict__ g, double *P0, double *P1,
                                                         double *Q0, double *Q1, float *__restrict__ U,
                                                         GridBarrier gb) {
     extern __shared__ __align__(16) unsigned char fgp_sm[];
-    double *sQ = reinterpret_cast<double *>(fgp_sm), *sP = sQ + 6 * kFgpRN;
+    TD *sQ = reinterpret_cast<TD *>(fgp_sm), *sP = sQ + 6 * kFgpRN;
     float *sU = reinterpret_cast<float *>(sP + 6 * kFgpRN), *sF = sU + 3 * kFgpRN;
     float *sL = sF + 3 * kFgpRN, *sI = sL + kFgpRN, *sG = sI + kFgpRN;
     const int tiles_x = (W + kFgpTX - 1) / kFgpTX, ntiles = tiles_x * ((H + kFgpTY - 1) / kFgpTY);
@@ -170,8 +174,8 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                 const size_t o = in ? (size_t)gy * W + gx : 0;
 #pragma unroll
                 for (int k = 0; k < 6; ++k) {
-                    sQ[k * kFgpRN + i] = in ? __ldcg(Qi + k * N + o) : 0.0;
-                    sP[k * kFgpRN + i] = in ? __ldcg(Pi + k * N + o) : 0.0;
+                    sQ[k * kFgpRN + i] = in ? (TD)__ldcg(Qi + k * N + o) : TD(0);
+                    sP[k * kFgpRN + i] = in ? (TD)__ldcg(Pi + k * N + o) : TD(0);
                 }
 #pragma unroll
                 for (int c = 0; c < 3; ++c) sF[c * kFgpRN + i] = in ? __ldg(F + c * N + o) : 0.f;
@@ -183,19 +187,19 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
             double s = s_step;
             for (int it = 0; it < iters; ++it) {
                 const double s1 = 0.5 * (1.0 + sqrt(1.0 + 4.0 * s * s));
-                const double beta = (s - 1.0) / s1;
+                const TD beta = (TD)((s - 1.0) / s1);
                 // u(q) on the region (values next to the region's edge are stale and stay outside the tile)
                 for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
                     const int lx = i % kFgpRX, ly = i / kFgpRX, gx = rx0 + lx, gy = ry0 + ly;
                     if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const double *qx = sQ + c * kFgpRN, *qy = sQ + (3 + c) * kFgpRN;
-                        double d = 0.0;
+                        const TD *qx = sQ + c * kFgpRN, *qy = sQ + (3 + c) * kFgpRN;
+                        TD d = 0;
                         if (gx < W - 1) d += qx[i];
-                        if (gx > 0) d -= lx > 0 ? qx[i - 1] : 0.0;
+                        if (gx > 0) d -= lx > 0 ? qx[i - 1] : TD(0);
                         if (gy < H - 1) d += qy[i];
-                        if (gy > 0) d -= ly > 0 ? qy[i - kFgpRX] : 0.0;
+                        if (gy > 0) d -= ly > 0 ? qy[i - kFgpRX] : TD(0);
                         sU[c * kFgpRN + i] = fminf(1.0f, fmaxf(0.0f, sF[c * kFgpRN + i] + sL[i] * (float)d));
                     }
                 }
@@ -204,8 +208,8 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                 for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
                     const int lx = i % kFgpRX, ly = i / kFgpRX, gx = rx0 + lx, gy = ry0 + ly;
                     if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
-                    double v[6];
-                    double n2 = 0.0;
+                    TD v[6];
+                    TD n2 = 0;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
                         const float *uc = sU + c * kFgpRN;
@@ -213,24 +217,26 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                         const float ud = (ly + 1 < kFgpRY) ? uc[i + kFgpRX] : 0.f;
                         const float gxv = gx < W - 1 ? ur - uc[i] : 0.f;
                         const float gyv = gy < H - 1 ? ud - uc[i] : 0.f;
-                        v[c] = sQ[c * kFgpRN + i] + (double)(gxv * sI[i]);
-                        v[3 + c] = sQ[(3 + c) * kFgpRN + i] + (double)(gyv * sI[i]);
+                        v[c] = sQ[c * kFgpRN + i] + (TD)(gxv * sI[i]);
+                        v[3 + c] = sQ[(3 + c) * kFgpRN + i] + (TD)(gyv * sI[i]);
                         n2 += v[c] * v[c] + v[3 + c] * v[3 + c];
                     }
                     // projection onto |p| <= g without an FP64 square root or division (both are long sequences on
                     // this GPU's narrow FP64 pipe): r = 1 / sqrt(n2) from the FP32 estimate and one FP64 Newton step
                     // (relative error ~1e-14), applied only where the ball constraint is active
-                    const double gv = (double)sG[i];
-                    double sc = 1.0;
+                    const TD gv = (TD)sG[i];
+                    TD sc = 1;
                     if (n2 > gv * gv) {
-                        double r = (double)rsqrtf((float)n2);
-                        r = r * (1.5 - 0.5 * n2 * r * r);
-                        r = r * (1.5 - 0.5 * n2 * r * r);
+                        TD r = (TD)rsqrtf((float)n2);
+                        if (sizeof(TD) == sizeof(double)) {
+                            r = r * (TD(1.5) - TD(0.5) * n2 * r * r);
+                            r = r * (TD(1.5) - TD(0.5) * n2 * r * r);
+                        }
                         sc = gv * r;
                     }
 #pragma unroll
                     for (int k = 0; k < 6; ++k) {
-                        const double pn = v[k] * sc;
+                        const TD pn = v[k] * sc;
                         sQ[k * kFgpRN + i] = pn + beta * (pn - sP[k * kFgpRN + i]);
                         sP[k * kFgpRN + i] = pn;
                     }
@@ -245,8 +251,8 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                 const int r = ly * kFgpRX + lx;
 #pragma unroll
                 for (int k = 0; k < 6; ++k) {
-                    Po[k * N + o] = sP[k * kFgpRN + r];
-                    Qo[k * N + o] = sQ[k * kFgpRN + r];
+                    Po[k * N + o] = (double)sP[k * kFgpRN + r];
+                    Qo[k * N + o] = (double)sQ[k * kFgpRN + r];
                 }
             }
             __syncthreads();  // the next tile overwrites the staged region
@@ -322,8 +328,10 @@ void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, Lau
 
 cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *lam, const float *linv, const float *g,
                           double *P0, double *P1, double *Q0, double *Q1, float *U, GridBarrier gb, cudaStream_t st,
-                          LaunchCounter &lc) {
-    ProfScope _ps(lc, "tv_fgp", st);
+                          LaunchCounter &lc, bool fp64) {
+    ProfScope _ps(lc, fp64 ? "tv_fgp_fp64" : "tv_fgp", st);
+    const void *kern = fp64 ? (const void *)k_tv_fgp<double> : (const void *)k_tv_fgp<float>;
+    const size_t smem = fp64 ? fgp_smem<double>() : fgp_smem<float>();
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -332,11 +340,13 @@ cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *
     if (dev >= 0 && dev < 64) {
         std::lock_guard<std::mutex> lock(mu);
         if (!attr_set[dev]) {
-            cudaFuncSetAttribute(k_tv_fgp, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kFgpSmem);
+            cudaFuncSetAttribute(k_tv_fgp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fgp_smem<float>());
+            cudaFuncSetAttribute(k_tv_fgp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fgp_smem<double>());
             attr_set[dev] = true;
         }
     }
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_tv_fgp, kFgpThreads, kFgpSmem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFgpThreads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const int ntiles = ((W + kFgpTX - 1) / kFgpTX) * ((H + kFgpTY - 1) / kFgpTY);
@@ -346,7 +356,7 @@ cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *
     const int blocks = std::max(1, (ntiles + per_block - 1) / per_block);
     void *args[] = {&W, &H, &niter, (void *)&F, (void *)&lam, (void *)&linv, (void *)&g, &P0, &P1, &Q0, &Q1, &U, &gb};
     lc.add(1);
-    return cudaLaunchCooperativeKernel((const void *)k_tv_fgp, dim3(blocks), dim3(kFgpThreads), args, kFgpSmem, st);
+    return cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(kFgpThreads), args, smem, st);
 }
 
 }  // namespace lfrv
