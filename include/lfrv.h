@@ -63,14 +63,17 @@ typedef struct lfrv_config {
     float dt_alpha;          /* intensity data term weight                                          */
     float dt_beta;           /* gradient data term weight                                           */
     float gradient_step;     /* step of the gradient data term                                      */
-    int   niter;             /* outer FISTA iterations AND inner ROF iterations (reference reuses it) */
+    int   niter;             /* outer FISTA iterations AND inner ROF iterations (reference reuses it); in
+                                corrected IBR_color (faithful = 0) the cap on outer FISTA steps */
     int   nmeta_iter;        /* re-weighting meta iterations                                         */
     /* --- options with no Config_data counterpart --- */
     int   faithful;          /* 1: reproduce the reference's control flow including its defects      */
     int   early_exit;        /* 1: the reference's convergence tests (energy / moving pixels) apply  */
     int   cg_max_iter;       /* IBR_gradient, corrected CG: iteration cap                             */
-    double cg_gap_tol;       /* IBR_gradient, corrected CG: stop when the certified relative energy
-                                gap ||r||^2 / (2 lambda_cg) / |E(u)| falls to this value (0: run the cap) */
+    double cg_gap_tol;       /* corrected mode (faithful = 0): stop when the certified relative energy gap falls
+                                to this value (0: run the cap). IBR_gradient: ||r||^2 / (2 lambda_cg) / |E(u)| of
+                                the CG. IBR_color: the primal-dual gap of the weighted TV_F objective over E(u)
+                                (kernels_tv.cu's certificate) */
     int   hole_fill_iter;    /* IBR_gradient hole filling: Jacobi iteration cap (reference: 500)     */
     int   bf16_storage;      /* IBR_gradient, device entry points: 1 = d_views holds BF16 values (V x 3 x h x w
                                 bfloat16), and the view gradients and weights are stored in BF16 too; every
@@ -107,15 +110,17 @@ typedef struct lfrv_stats {
     int    hole_fill_iterations;
     int    stop_reason;          /* 0 cap reached, 1 tiny energy, 2 relative energy change, 3 < 1% pixels moving,
                                     4 certified gap reached */
-    double energy;               /* last energy evaluated (reference formula for IBR_color, quadratic for CG) */
-    double gap;                  /* last certified relative gap (CG), else 0 */
+    double energy;               /* last energy evaluated: the reference formula for IBR_color (faithful), the TV_F
+                                    objective (corrected IBR_color), the quadratic energy for CG */
+    double gap;                  /* last certified relative gap (corrected modes), else 0 */
     double seconds;              /* device time of the solve (CUDA events) */
     int    kernel_launches;      /* kernels this library launched for the call */
     /* Optional energy trace (the reference prints the energy of every FISTA iteration,
      * sources/super-resolution.cpp:221-260). The caller sets energy_trace to a host buffer of trace_capacity
      * doubles (or NULL / 0 for none) before the call; the solver writes one entry per outer iteration, in order:
-     * IBR_color: the energy of coco_vtv_sr_primal_energy_unstructured (sources/optimization.cu:1477-1717) after
-     * each FISTA iteration, across meta iterations; IBR_gradient: the quadratic energy
+     * IBR_color (faithful): the energy of coco_vtv_sr_primal_energy_unstructured (sources/optimization.cu:1477-1717)
+     * after each FISTA iteration, across meta iterations; corrected IBR_color: the TV_F objective of the starting
+     * point and of every FISTA iterate; IBR_gradient: the quadratic energy
      * 1/2 ||u - u0||^2 + 1/2 ||grad u - g||^2 after each CG iteration (FP64). trace_length receives the number of
      * entries written (at most trace_capacity). Zero-initialise the struct: the library reads these two fields. */
     double *energy_trace;
@@ -244,6 +249,19 @@ int lfrv_render_views_dev(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count);
  * job's cfg->bf16_storage is 1). Input buffers shared by several jobs (same pointer and size, e.g. one light field
  * seen from many targets) are uploaded once; every output is copied back before the call returns. */
 int lfrv_render_views(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count);
+
+/* ---------------------------------------------------------------- IBR_video
+ * The reference's IBR_video loop (sources/main.cpp:359-403) renders frame after frame of one light field from a
+ * moving target camera (TargetView::move, sources/openGL/view.cpp:1744-1759): the centre goes from input view a's
+ * towards view b's by frame / 1000 of the way and the rotation is view a's turned about the y axis by frame * 0.0003
+ * rad (the reference takes views 5 and 3); K and the size stay the target's.
+ * lfrv_video_camera: that camera for one frame. lfrv_render_video_dev: frames first_frame .. first_frame + nframes - 1
+ * rendered as one batch (as lfrv_render_views_dev); d_out holds nframes x 3 x H x W, stats (optional) nframes entries. */
+int lfrv_video_camera(const lfrv_camera *a, const lfrv_camera *b, const lfrv_camera *target, int frame,
+                      lfrv_camera *out);
+int lfrv_render_video_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm, const float *d_views,
+                          const float *d_depth, const lfrv_camera *cams, int cam_a, int cam_b,
+                          const lfrv_camera *target, int first_frame, int nframes, float *d_out, lfrv_stats *stats);
 
 /* ---------------------------------------------------------------- learned warm start
  * No reference counterpart: an addition beside the plain method, which stays unchanged. A 4-scale
@@ -399,6 +417,17 @@ int lfrv_cg_solve_static(void *stream, int W, int H, int max_iter, double gap_to
  * flips on write. Buffers here are top-left origin, planar. */
 int lfrv_pfm_read(const char *path, int *w, int *h, int *channels, float *data, size_t capacity);
 int lfrv_pfm_write(const char *path, int w, int h, int channels, const float *data);
+/* MVE depth and normal maps (InputView::importMVEIFile, sources/openGL/view.cpp:279-325): a text header line, then
+ * width, height, channels, type as four little-endian uint32, then interleaved float32 pixels, row 0 first; returned
+ * planar (channels x h x w). A NULL data pointer returns only the sizes. */
+int lfrv_mvei_read(const char *path, int *w, int *h, int *channels, float *data, size_t capacity);
+/* InputView::setDepthAndNormals (sources/openGL/view.cpp:607-635) with Texture::loadFromData (sources/openGL/
+ * texture.cpp:207-290): the depth plane (h0 x w0) and the first two normal planes (2 x h0 x w0) become the three
+ * depth-map channels (out: 3 x h0*factor x w0*factor), upsampled by nearest neighbour; pixels whose three values are
+ * all 0 become (invalid_depth, 0, 0) (the reference uses INVALID_DEPTH = 1000). Feed the result to
+ * lfrv_depth_radial_to_ortho, as Scene::filterDepthMaps does. */
+int lfrv_depth_from_mve(int w0, int h0, int factor, const float *depth, const float *normal, float invalid_depth,
+                        float *out);
 /* 8-bit PNG as gsl_image_load / gsl_image_save read and write it through Qt (cocolib/cocolib/common/
  * gsl_image.cpp:539-640): channels scaled by 1/255 on read (grey replicated to RGB, alpha dropped), written
  * as clamp(int(v * 255), 0, 255). rgb is 3 x h x w. Needs zlib at build time, else LFRV_E_IO. */

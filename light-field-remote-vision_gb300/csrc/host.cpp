@@ -2007,6 +2007,58 @@ extern "C" int lfrv_render_views_warm(lfrv_ctx *ctx, lfrv_warmstart *net, const 
     LFRV_API_END
 }
 
+// ------------------------------------------------------------------ IBR_video
+// TargetView::move (sources/openGL/view.cpp:1744-1759), in its float arithmetic: the centre moves from camera a's
+// towards camera b's by frame / 1000 of the way, the rotation is camera a's turned about the y axis by frame * 0.0003
+// rad, K and the size stay the target's.
+extern "C" int lfrv_video_camera(const lfrv_camera *a, const lfrv_camera *b, const lfrv_camera *target, int frame,
+                                 lfrv_camera *out) {
+    if (!a || !b || !target || !out || frame < 0) return fail(LFRV_E_ARG, "bad arguments");
+    float Ca[3], Cb[3];
+    for (int i = 0; i < 3; ++i) {  // C = -R^T t
+        Ca[i] = -(a->R[0 * 3 + i] * a->t[0] + a->R[1 * 3 + i] * a->t[1] + a->R[2 * 3 + i] * a->t[2]);
+        Cb[i] = -(b->R[0 * 3 + i] * b->t[0] + b->R[1 * 3 + i] * b->t[1] + b->R[2 * 3 + i] * b->t[2]);
+    }
+    const float step = 1000.0f, angle = 0.0003f;
+    const float count = (float)frame;
+    float C[3];
+    for (int i = 0; i < 3; ++i) C[i] = Ca[i] + count * (Cb[i] - Ca[i]) / step;
+    const float cs = std::cos(count * angle), sn = std::sin(count * angle);
+    const float Ry[9] = {cs, 0.0f, sn, 0.0f, 1.0f, 0.0f, -sn, 0.0f, cs};
+    lfrv_camera o = *target;
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c)
+            o.R[r * 3 + c] = Ry[r * 3 + 0] * a->R[0 * 3 + c] + Ry[r * 3 + 1] * a->R[1 * 3 + c] + Ry[r * 3 + 2] * a->R[2 * 3 + c];
+    for (int r = 0; r < 3; ++r) o.t[r] = -(o.R[r * 3 + 0] * C[0] + o.R[r * 3 + 1] * C[1] + o.R[r * 3 + 2] * C[2]);
+    *out = o;
+    return LFRV_OK;
+}
+
+// The IBR_video loop (sources/main.cpp:359-403) over one static light field: frames first_frame .. first_frame +
+// nframes - 1, each a target camera moved by lfrv_video_camera from views cam_a and cam_b, all rendered as one batch.
+extern "C" int lfrv_render_video_dev(lfrv_ctx *ctx, const lfrv_config *cfg, int algorithm, const float *d_views,
+                                     const float *d_depth, const lfrv_camera *cams, int cam_a, int cam_b,
+                                     const lfrv_camera *target, int first_frame, int nframes, float *d_out,
+                                     lfrv_stats *stats) {
+    LFRV_API_BEGIN
+    CTX_CHECK(ctx);
+    if (!cfg || !d_views || !d_depth || !cams || !target || !d_out || nframes < 1 || first_frame < 0)
+        return fail(LFRV_E_ARG, "bad arguments");
+    if (cam_a < 0 || cam_a >= cfg->nviews || cam_b < 0 || cam_b >= cfg->nviews)
+        return fail(LFRV_E_ARG, "camera indices %d, %d outside the %d views", cam_a, cam_b, cfg->nviews);
+    const Geometry G = geometry(*cfg);
+    std::vector<lfrv_camera> tcams(nframes);
+    std::vector<lfrv_view_job> jobs(nframes);
+    for (int f = 0; f < nframes; ++f) {
+        const int rc = lfrv_video_camera(&cams[cam_a], &cams[cam_b], target, first_frame + f, &tcams[f]);
+        if (rc != LFRV_OK) return rc;
+        jobs[f] = lfrv_view_job{cfg, algorithm, d_views, d_depth, cams, &tcams[f], d_out + (size_t)f * 3 * G.N,
+                                stats ? &stats[f] : nullptr};
+    }
+    render_views(ctx, jobs.data(), nframes);
+    LFRV_API_END
+}
+
 static cudaStream_t copy_stream(lfrv_ctx *c) {
     if (!c->copy_stream) {
         LFRV_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));

@@ -8,6 +8,7 @@
 #include "lfrv.h"
 #include "lfrv_internal.h"
 
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -229,5 +230,71 @@ extern "C" int lfrv_pfm_write(const char *path, int w, int h, int channels, cons
         }
     }
     std::fclose(f);
+    return LFRV_OK;
+}
+
+// ------------------------------------------------------------------ MVE depth and normal maps
+// InputView::importMVEIFile (sources/openGL/view.cpp:279-325): a text header line, then width, height, channels and
+// type as four 32-bit unsigned integers, then height x width pixels of `channels` interleaved 32-bit floats (row 0
+// first). Returned planar, top-left origin, like every other image here.
+extern "C" int lfrv_mvei_read(const char *path, int *w, int *h, int *channels, float *data, size_t capacity) {
+    if (!path || !w || !h || !channels) return lfrv::fail(LFRV_E_ARG, "null argument");
+    FILE *f = std::fopen(path, "rb");
+    if (!f) return lfrv::fail(LFRV_E_IO, "cannot open %s", path);
+    auto bad = [&](const char *why) {
+        std::fclose(f);
+        return lfrv::fail(LFRV_E_FORMAT, "%s: %s", path, why);
+    };
+    int ch = 0;
+    while ((ch = std::fgetc(f)) != EOF && ch != '\n') {
+    }
+    if (ch == EOF) return bad("MVEI header line not terminated");
+    uint32_t hdr[4];
+    if (std::fread(hdr, sizeof(uint32_t), 4, f) != 4) return bad("truncated size fields");
+    if (!little_endian()) swap_bytes(reinterpret_cast<float *>(hdr), 4);
+    const uint32_t W = hdr[0], H = hdr[1], C = hdr[2];
+    if (W == 0 || H == 0 || C == 0 || C > 64 || (unsigned long long)W * H > (1ull << 30)) return bad("bad dimensions");
+    *w = (int)W;
+    *h = (int)H;
+    *channels = (int)C;
+    if (!data) {
+        std::fclose(f);
+        return LFRV_OK;
+    }
+    const size_t N = (size_t)W * H;
+    if (capacity < (size_t)C * N) {
+        std::fclose(f);
+        return lfrv::fail(LFRV_E_ARG, "%s: buffer holds %zu floats, need %zu", path, capacity, (size_t)C * N);
+    }
+    std::vector<float> row((size_t)C * W);
+    for (uint32_t y = 0; y < H; ++y) {
+        if (std::fread(row.data(), sizeof(float), row.size(), f) != row.size()) return bad("truncated data");
+        if (!little_endian()) swap_bytes(row.data(), row.size());
+        for (uint32_t x = 0; x < W; ++x)
+            for (uint32_t c = 0; c < C; ++c) data[(size_t)c * N + (size_t)y * W + x] = row[(size_t)x * C + c];
+    }
+    std::fclose(f);
+    return LFRV_OK;
+}
+
+// InputView::setDepthAndNormals (sources/openGL/view.cpp:607-635) with Texture::loadFromData (sources/openGL/
+// texture.cpp:207-290, no flip): the depth plane and the first two normal planes become the three depth-map channels,
+// upsampled by nearest neighbour from (w0, h0) to (w0 * factor, h0 * factor); a pixel whose three values are all 0
+// becomes (invalid_depth, 0, 0).
+extern "C" int lfrv_depth_from_mve(int w0, int h0, int factor, const float *depth, const float *normal,
+                                   float invalid_depth, float *out) {
+    if (w0 <= 0 || h0 <= 0 || factor < 1 || !depth || !normal || !out) return lfrv::fail(LFRV_E_ARG, "bad arguments");
+    const int W = w0 * factor, H = h0 * factor;
+    const size_t n0 = (size_t)w0 * h0, N = (size_t)W * H;
+    const float *src[3] = {depth, normal, normal + n0};
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const size_t o = (size_t)y * W + x, s = (size_t)(y / factor) * w0 + (x / factor);
+            const float a = src[0][s], b = src[1][s], c = src[2][s];
+            const bool empty = a == 0.0f && b == 0.0f && c == 0.0f;
+            out[o] = empty ? invalid_depth : a;
+            out[N + o] = empty ? 0.0f : b;
+            out[2 * N + o] = empty ? 0.0f : c;
+        }
     return LFRV_OK;
 }

@@ -115,6 +115,7 @@ EXPORTED = [
     "lfrv_depth_radial_to_ortho_dev", "lfrv_warp_from_depth", "lfrv_warp_from_depth_dev", "lfrv_warp", "lfrv_warp_dev", "lfrv_ibr_color", "lfrv_ibr_color_dev",
     "lfrv_ibr_gradient", "lfrv_ibr_gradient_dev", "lfrv_render_view", "lfrv_render_view_dev", "lfrv_render_views_dev",
     "lfrv_render_views", "lfrv_render_views_warm",
+    "lfrv_video_camera", "lfrv_render_video_dev", "lfrv_mvei_read", "lfrv_depth_from_mve",
     "lfrv_warmstart_param_count", "lfrv_warmstart_create", "lfrv_warmstart_destroy", "lfrv_warmstart_get_params",
     "lfrv_warmstart_set_params", "lfrv_warmstart_features_dev", "lfrv_warmstart_forward_dev",
     "lfrv_warmstart_train_step_dev", "lfrv_warmstart_gradients_dev", "lfrv_render_view_warm_dev", "lfrv_render_views_warm_dev", "lfrv_conv_bf16_dev",
@@ -246,6 +247,33 @@ def cg_solve_static(stream: int, W: int, H: int, max_iter: int, gap_tol: float, 
                                     C.c_void_p(d_gx), C.c_void_p(d_gy), C.c_void_p(d_U),
                                     C.byref(it) if want_stats else None, C.byref(gap) if want_stats else None))
     return it.value, gap.value
+
+
+def mvei_read(path: str) -> np.ndarray:
+    """MVE image (depth or normal map) as channels x h x w float32."""
+    w, h, c = C.c_int(), C.c_int(), C.c_int()
+    _check(LIB.lfrv_mvei_read(str(path).encode(), C.byref(w), C.byref(h), C.byref(c), None, C.c_size_t(0)))
+    out = np.zeros((c.value, h.value, w.value), np.float32)
+    _check(LIB.lfrv_mvei_read(str(path).encode(), C.byref(w), C.byref(h), C.byref(c), fptr(out),
+                              C.c_size_t(out.size)))
+    return out
+
+
+def depth_from_mve(depth: np.ndarray, normal: np.ndarray, factor: int, invalid_depth: float = 1000.0) -> np.ndarray:
+    """3 x (h0 factor) x (w0 factor) depth-map channels from an MVE depth plane (h0 x w0) and normal planes."""
+    depth = f32(np.asarray(depth).reshape(-1, *np.asarray(depth).shape[-2:])[0])
+    normal = f32(normal)
+    h0, w0 = depth.shape
+    out = np.zeros((3, h0 * factor, w0 * factor), np.float32)
+    _check(LIB.lfrv_depth_from_mve(w0, h0, factor, fptr(depth), fptr(normal), C.c_float(invalid_depth), fptr(out)))
+    return out
+
+
+def video_camera(a: "Camera", b: "Camera", target: "Camera", frame: int) -> "Camera":
+    """The IBR_video target camera of one frame (TargetView::move)."""
+    out = Camera()
+    _check(LIB.lfrv_video_camera(C.byref(a), C.byref(b), C.byref(target), frame, C.byref(out)))
+    return out
 
 
 def png_read(path: str) -> np.ndarray:
@@ -380,6 +408,15 @@ class Context:
         _check(LIB.lfrv_render_view_dev(self._h, C.byref(cfg), algorithm, C.c_void_p(d_views), C.c_void_p(d_depth),
                                         cameras_array(cams), C.byref(target), C.c_void_p(d_out), C.byref(st)))
         return st
+
+    def render_video_dev(self, cfg: Config, algorithm: int, d_views: int, d_depth: int, cams, cam_a: int, cam_b: int,
+                         target: Camera, first_frame: int, nframes: int, d_out: int) -> list:
+        """IBR_video frames first_frame .. first_frame + nframes - 1 as one batch; d_out: nframes x 3 x H x W."""
+        stats = (Stats * nframes)()
+        _check(LIB.lfrv_render_video_dev(self._h, C.byref(cfg), algorithm, C.c_void_p(d_views), C.c_void_p(d_depth),
+                                         cameras_array(cams), cam_a, cam_b, C.byref(target), first_frame, nframes,
+                                         C.c_void_p(d_out), stats))
+        return list(stats)
 
     def render_views(self, jobs, net: "WarmStart | None" = None, trace: int = 0) -> list:
         """Batched targets from host buffers (lfrv_render_views / lfrv_render_views_warm): each job's d_views,
@@ -646,6 +683,11 @@ def _declare() -> None:
     LIB.lfrv_depth_radial_to_ortho_dev.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.POINTER(Camera), vp]
     LIB.lfrv_render_views_dev.argtypes = [vp, C.POINTER(ViewJob), C.c_int]
     LIB.lfrv_render_views.argtypes = [vp, C.POINTER(ViewJob), C.c_int]
+    LIB.lfrv_video_camera.argtypes = [C.POINTER(Camera)] * 3 + [C.c_int, C.POINTER(Camera)]
+    LIB.lfrv_render_video_dev.argtypes = [vp, C.POINTER(Config), C.c_int, vp, vp, C.POINTER(Camera), C.c_int,
+                                          C.c_int, C.POINTER(Camera), C.c_int, C.c_int, vp, C.POINTER(Stats)]
+    LIB.lfrv_mvei_read.argtypes = [C.c_char_p, _I, _I, _I, _F, C.c_size_t]
+    LIB.lfrv_depth_from_mve.argtypes = [C.c_int, C.c_int, C.c_int, _F, _F, C.c_float, _F]
     LIB.lfrv_render_views_warm.argtypes = [vp, vp, C.POINTER(ViewJob), C.c_int]
     LIB.lfrv_cg_solve_static.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_double, vp, vp, vp, _I, _D]
     LIB.lfrv_png_read.argtypes = [C.c_char_p, _I, _I, _F, C.c_size_t]
