@@ -146,4 +146,7 @@ struct lfrv_ctx {
     std::vector<cudaEvent_t> lane_done;
     bool owns_stream = false;
     bool lane = false;  // a helper context of a batched call (its stream already runs beside the others)
+    double *host_sums = nullptr;  // pinned host copy of reduction sums (corrected IBR_color's stop test)
+    // contexts of the corrected IBR_color jobs of a batched call (one per job, own stream and workspace)
+    std::vector<lfrv_ctx *> tv_jobs;
 };

@@ -115,6 +115,11 @@ static void swap_buf(DevBuf &a, DevBuf &b) {
 
 static GridBarrier fresh_barrier(lfrv_ctx *c);
 static float *view_gradients(lfrv_ctx *c, const Geometry &G, const float *img, cudaStream_t st);
+// Pinned host copy of a context's first 8 reduction sums (allocated on first use, freed with the context).
+static double *host_sums(lfrv_ctx *c) {
+    if (!c->host_sums) LFRV_CUDA(cudaMallocHost(reinterpret_cast<void **>(&c->host_sums), sizeof(double) * 8));
+    return c->host_sums;
+}
 
 // The side stream: work of a call that depends only on its inputs runs there, between an event recorded on the
 // context stream (fork) and one the context stream waits for (join). Created on first use.
@@ -439,9 +444,116 @@ static void energy_gradients(lfrv_ctx *c, const lfrv_config &cfg, const Geometry
     reduce_to(c, np, part, slot);
 }
 
+// ------------------------------------------------------------------ IBR_color, corrected mode
+// The corrected IBR_color solve of one target (kernels_tv.cu), held in the workspace of context c and driven one
+// outer iteration at a time, so that several targets on their own contexts can advance in lockstep with one host
+// synchronisation per round: eval() enqueues the energy and certificate of the current iterate and their copy to
+// host memory; after the stream has completed, decide() reads them, records the trace and the stop decision; step()
+// enqueues one FISTA step (its FGP dual solve in one persistent launch).
+struct TvSolve {
+    lfrv_ctx *c = nullptr;
+    lfrv_config cfg{};
+    Geometry G{};
+    const float *img = nullptr, *tau2 = nullptr;
+    Buckets B{};
+    ColorBuffers b{};
+    float *u = nullptr, *up = nullptr, *gf = nullptr, *gfp = nullptr, *D = nullptr, *lam = nullptr, *linv = nullptr;
+    double *P0 = nullptr, *P1 = nullptr, *Q0 = nullptr, *Q1 = nullptr;
+    double t = 1.0, E_prev = 1e300, E = 0.0, gap = 1e300;
+    bool fp64 = false, done = false;
+    int k = 0, npart = 0;
+    lfrv_stats *st = nullptr;  // energy trace destination (optional)
+    int trace_pos = 0;
+
+    // set-up for one meta iteration on ws.U (weights and regulariser weight computed): the metric, u = clamp(U),
+    // the FISTA history and, for the first meta iteration, a zero dual
+    void begin(int meta) {
+        Workspace &ws = c->ws;
+        const size_t N = G.N, N3 = 3 * N;
+        cudaStream_t s = c->stream;
+        // 15 N floats (u, u_prev, grad f, grad f_prev, D, lam, 1/L), then 24 N doubles (p, its ping-pong copy, q x 2)
+        const size_t fbytes = (sizeof(float) * 15 * N + 255) / 256 * 256;
+        ws.tv.ensure(fbytes + sizeof(double) * 24 * N);
+        u = ws.tv.as<float>();
+        up = u + N3;
+        gf = up + N3;
+        gfp = gf + N3;
+        D = gfp + N3;
+        lam = D + N;
+        linv = lam + N;
+        P0 = reinterpret_cast<double *>(ws.tv.as<char>() + fbytes);
+        P1 = P0 + 6 * N;
+        Q0 = P1 + 6 * N;
+        Q1 = Q0 + 6 * N;
+        launch_tv_metric(G, B, tau2, b.wgt, as2(), cfg.lambda, D, lam, linv, s, c->launches);
+        check_launch("tv metric");
+        launch_tv_clamp(N3, ws.U.as<float>(), u, s, c->launches);
+        // u_prev = u and grad f(u_prev) = 0: the first step (theta = 0) reads them only through zero factors
+        LFRV_CUDA(cudaMemcpyAsync(up, u, sizeof(float) * N3, cudaMemcpyDeviceToDevice, s));
+        LFRV_CUDA(cudaMemsetAsync(gfp, 0, sizeof(float) * N3, s));
+        if (meta == 0) LFRV_CUDA(cudaMemsetAsync(P0, 0, sizeof(double) * 6 * N, s));
+        npart = tv_gap_partials(G.W, G.H);
+        t = 1.0;
+        E_prev = 1e300;
+        fp64 = false;
+        done = false;
+        k = 0;
+    }
+    float as2() const { return cfg.dt_alpha * cfg.sigma_sensor * cfg.sigma_sensor; }
+    void eval() {
+        const float s2 = cfg.sigma_sensor * cfg.sigma_sensor;
+        residual(c, G, u, img, tau2, b.wgt, s2, b.res, 1, true);
+        launch_tv_gradf(G, B, tau2, b.res, as2(), gf, c->stream, c->launches);
+        check_launch("tv data gradient");
+        double *part = partial_buf(c, 3 * (size_t)npart);
+        launch_tv_gap(G.W, G.H, u, gf, P0, b.g, cfg.lambda, part, c->stream, c->launches);
+        check_launch("tv gap");
+        for (int q = 0; q < 3; ++q) reduce_to(c, npart, part + (size_t)q * npart, 4 + q);
+        LFRV_CUDA(cudaMemcpyAsync(host_sums(c), c->ws.sums.p, sizeof(double) * 7, cudaMemcpyDeviceToHost, c->stream));
+    }
+    // after the stream has completed: true when the solve has stopped (gap reached or the cap)
+    bool decide() {
+        const double *sums = host_sums(c);
+        const double f = 0.5 * (double)cfg.dt_alpha * sums[1];
+        E = f + (double)cfg.lambda * sums[4];
+        const double gap_abs = (double)cfg.lambda * (sums[4] - sums[5]) + sums[6];
+        gap = E > 0 ? gap_abs / E : 1e300;
+        if (st && st->energy_trace && trace_pos < st->trace_capacity) st->energy_trace[trace_pos++] = E;
+        if (!std::isfinite(E) || !std::isfinite(gap))
+            raise(LFRV_E_NONFINITE, "non-finite energy in the corrected IBR_color solve");
+        done = k >= cfg.niter || (cfg.cg_gap_tol > 0 && gap <= cfg.cg_gap_tol);
+        return done;
+    }
+    void step() {
+        cudaStream_t s = c->stream;
+        if (E > E_prev) t = 1.0;  // function-value restart of the momentum
+        E_prev = E;
+        const double t1 = 0.5 * (1.0 + std::sqrt(1.0 + 4.0 * t * t));
+        const float theta = (float)((t - 1.0) / t1);
+        t = t1;
+        launch_tv_fstep(G.W, G.H, u, up, gf, gfp, D, theta, b.F, s, c->launches);
+        check_launch("tv step");
+        std::swap(u, up);
+        std::swap(gf, gfp);
+        const GridBarrier gb = fresh_barrier(c);
+        // FP32 dual arithmetic while the gap is far above FP32's floor, FP64 once it nears it (the switch only
+        // changes rounding, not the iteration)
+        fp64 = fp64 || gap < kTvFp64Below;
+        LFRV_CUDA(launch_tv_fgp(G.W, G.H, kTvInnerIterations, b.F, lam, linv, b.g, P0, P1, Q0, Q1, u, gb, s,
+                                c->launches, fp64));
+        ++k;
+    }
+    // the solution back into ws.U
+    void finish() {
+        LFRV_CUDA(cudaMemcpyAsync(c->ws.U.p, u, sizeof(float) * 3 * G.N, cudaMemcpyDeviceToDevice, c->stream));
+    }
+};
+
 // ------------------------------------------------------------------ IBR_color
+// defer (corrected mode with one meta iteration): the set-up runs, then *defer receives the solve, begun, and the
+// caller drives it and copies the result (TvSolve::finish puts it into the context's ws.U).
 static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, const float *tau2, const float *dp2,
-                        const float *init, float *out, lfrv_stats *st) {
+                        const float *init, float *out, lfrv_stats *st, TvSolve *defer = nullptr) {
     check_solver_options(cfg);
     if (cfg.bf16_storage) raise(LFRV_E_ARG, "bf16_storage applies to IBR_gradient only");
     if (!cfg.faithful && cfg.dt_beta != 0.0f)
@@ -550,66 +662,34 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
     // included) are written to the caller's buffer from the host, where the energy is read for the stop test.
     double tv_gap_last = 0.0, tv_E = 0.0;
     int tv_trace_pos = 0;
-    auto tv_meta = [&](int meta) -> int {
-        const size_t N3 = 3 * N;
-        // 15 N floats (u, u_prev, grad f, grad f_prev, D, lam, 1/L), then 24 N doubles (p, its ping-pong copy, q x 2)
-        const size_t fbytes = (sizeof(float) * 15 * N + 255) / 256 * 256;
-        ws.tv.ensure(fbytes + sizeof(double) * 24 * N);
-        float *u = ws.tv.as<float>(), *up = u + N3, *gf = up + N3, *gfp = gf + N3, *D = gfp + N3, *lam = D + N,
-              *linv = lam + N;
-        double *P0 = reinterpret_cast<double *>(ws.tv.as<char>() + fbytes), *P1 = P0 + 6 * N, *Q0 = P1 + 6 * N,
-               *Q1 = Q0 + 6 * N;
-        const float as2 = cfg.dt_alpha * s2;
-        launch_tv_metric(G, B, tau2, b.wgt, as2, cfg.lambda, D, lam, linv, s, c->launches);
-        check_launch("tv metric");
-        launch_tv_clamp(N3, ws.U.as<float>(), u, s, c->launches);
-        // u_prev = u and grad f(u_prev) = 0: the first step (theta = 0) reads them only through zero factors
-        LFRV_CUDA(cudaMemcpyAsync(up, u, sizeof(float) * N3, cudaMemcpyDeviceToDevice, s));
-        LFRV_CUDA(cudaMemsetAsync(gfp, 0, sizeof(float) * N3, s));
-        if (meta == 0) LFRV_CUDA(cudaMemsetAsync(P0, 0, sizeof(double) * 6 * N, s));
-        const int npart = tv_gap_partials(G.W, G.H);
-        const double tol = cfg.cg_gap_tol;
-        double t = 1.0, E_prev = 1e300;
-        bool fp64 = false;
-        int k;
-        for (k = 0;; ++k) {
-            residual(c, G, u, img, tau2, b.wgt, s2, b.res, 1, true);
-            launch_tv_gradf(G, B, tau2, b.res, as2, gf, s, c->launches);
-            check_launch("tv data gradient");
-            double *part = partial_buf(c, 3 * (size_t)npart);
-            launch_tv_gap(G.W, G.H, u, gf, P0, b.g, cfg.lambda, part, s, c->launches);
-            check_launch("tv gap");
-            for (int q = 0; q < 3; ++q) reduce_to(c, npart, part + (size_t)q * npart, 4 + q);
-            double sums[7];
-            read_sums(c, sums, 7);
-            const double f = 0.5 * (double)cfg.dt_alpha * sums[1];
-            tv_E = f + (double)cfg.lambda * sums[4];
-            const double gap_abs = (double)cfg.lambda * (sums[4] - sums[5]) + sums[6];
-            tv_gap_last = tv_E > 0 ? gap_abs / tv_E : 1e300;
-            if (trace && tv_trace_pos < trace_cap) st->energy_trace[tv_trace_pos++] = tv_E;
-            if (!std::isfinite(tv_E) || !std::isfinite(tv_gap_last))
-                raise(LFRV_E_NONFINITE, "non-finite energy in the corrected IBR_color solve");
-            if (k >= cfg.niter || (tol > 0 && tv_gap_last <= tol)) break;
-            if (tv_E > E_prev) t = 1.0;  // function-value restart of the momentum
-            E_prev = tv_E;
-            const double t1 = 0.5 * (1.0 + std::sqrt(1.0 + 4.0 * t * t));
-            const float theta = (float)((t - 1.0) / t1);
-            t = t1;
-            launch_tv_fstep(G.W, G.H, u, up, gf, gfp, D, theta, b.F, s, c->launches);
-            check_launch("tv step");
-            std::swap(u, up);
-            std::swap(gf, gfp);
-            const GridBarrier gb = fresh_barrier(c);
-            // FP32 dual arithmetic while the gap is far above FP32's floor, FP64 once it nears it (the switch only
-            // changes rounding, not the iteration)
-            fp64 = fp64 || tv_gap_last < kTvFp64Below;
-            LFRV_CUDA(launch_tv_fgp(G.W, G.H, kTvInnerIterations, b.F, lam, linv, b.g, P0, P1, Q0, Q1, u, gb, s,
-                                    c->launches, fp64));
-        }
-        LFRV_CUDA(cudaMemcpyAsync(ws.U.p, u, sizeof(float) * N3, cudaMemcpyDeviceToDevice, s));
-        return k;
+    auto tv_solver = [&]() {
+        TvSolve ts;
+        ts.c = c;
+        ts.cfg = cfg;
+        ts.G = G;
+        ts.img = img;
+        ts.tau2 = tau2;
+        ts.B = B;
+        ts.b = b;
+        ts.st = trace ? st : nullptr;
+        ts.trace_pos = tv_trace_pos;
+        return ts;
     };
-
+    auto tv_meta = [&](int meta) -> int {
+        TvSolve ts = tv_solver();
+        ts.begin(meta);
+        for (;;) {
+            ts.eval();
+            sync(c);
+            if (ts.decide()) break;
+            ts.step();
+        }
+        ts.finish();
+        tv_E = ts.E;
+        tv_gap_last = ts.gap;
+        tv_trace_pos = ts.trace_pos;
+        return ts.k;
+    };
     float E = 0.0f, E_prev = 0.0f, E_prev_reweight = 0.0f;
     int total_k = 0, reason = 0, r = 0;
     const bool track = cfg.early_exit != 0;
@@ -620,6 +700,11 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
         check_launch("regularizer weight");
         launch_blur(G.W, G.H, b.g0, b.tmp, b.g, s, c->launches);
         check_launch("blur");
+        if (!faithful && defer) {
+            *defer = tv_solver();
+            defer->begin(0);
+            return;
+        }
         if (!faithful) {
             total_k += tv_meta(r);
             E = (float)tv_E;
@@ -1188,13 +1273,17 @@ extern "C" int lfrv_ctx_destroy(lfrv_ctx *ctx) {
     else cudaDeviceSynchronize();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-    for (lfrv_ctx *l : ctx->lanes) {
-        cudaStreamSynchronize(l->stream);
-        destroy_side_stream(l);
-        cudaStreamDestroy(l->stream);
-        l->prof.destroy();
-        delete l;
-    }
+    for (std::vector<lfrv_ctx *> *group : {&ctx->lanes, &ctx->tv_jobs})
+        for (lfrv_ctx *l : *group) {
+            cudaStreamSynchronize(l->stream);
+            destroy_side_stream(l);
+            cudaStreamDestroy(l->stream);
+            if (l->host_sums) cudaFreeHost(l->host_sums);
+            if (l->ev0) cudaEventDestroy(l->ev0);
+            l->prof.destroy();
+            delete l;
+        }
+    if (ctx->host_sums) cudaFreeHost(ctx->host_sums);
     destroy_side_stream(ctx);
     ctx->graph.reset({});
     for (cudaEvent_t e : ctx->lane_done) cudaEventDestroy(e);
@@ -1722,6 +1811,8 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
     };
     if (net && warmstart_ctx(net) != c) raise(LFRV_E_ARG, "the warm-start network belongs to another context");
     std::vector<Slot> batched;
+    // corrected IBR_color jobs with one meta iteration: each on a context of its own, advanced in lockstep
+    std::vector<int> tv_idx;
     size_t pool = 0;
     for (int j = 0; j < count; ++j) {
         const lfrv_view_job &J = jobs[j];
@@ -1730,6 +1821,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         const Geometry G = geometry(*J.cfg);
         if (J.target->width != G.W || J.target->height != G.H) raise(LFRV_E_ARG, "job %d: target size mismatch", j);
         reset_stats(J.stats);
+        if (J.algorithm == 0 && !J.cfg->faithful && J.cfg->nmeta_iter == 1) tv_idx.push_back(j);
         if (J.algorithm == 1 && !J.cfg->faithful) {
             check_solver_options(*J.cfg);
             if (G.W < 2 || G.H < 2) raise(LFRV_E_ARG, "job %d: target smaller than 2 x 2", j);
@@ -1764,6 +1856,32 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         l->pending = Pending{};
         LFRV_CUDA(cudaStreamWaitEvent(l->stream, c->ev0, 0));
     }
+    // the corrected IBR_color jobs: warp stage and set-up on their own contexts (streams), up to the first step
+    while (c->tv_jobs.size() < tv_idx.size()) {
+        lfrv_ctx *l = new lfrv_ctx;
+        l->device = c->device;
+        LFRV_CUDA(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking));
+        l->owns_stream = true;
+        l->lane = true;
+        c->tv_jobs.push_back(l);
+    }
+    std::vector<TvSolve> tv(tv_idx.size());
+    for (size_t q = 0; q < tv_idx.size(); ++q) {
+        const lfrv_view_job &J = jobs[tv_idx[q]];
+        lfrv_ctx *l = c->tv_jobs[q];
+        l->launches.n = 0;
+        l->launches.prof = nullptr;
+        l->pending = Pending{};
+        LFRV_CUDA(cudaStreamWaitEvent(l->stream, c->ev0, 0));
+        const Geometry G = geometry(*J.cfg);
+        l->ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+        l->ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
+        warp(l, G.V, G.w, G.h, J.d_depth, J.cams, J.target, nullptr, nullptr, l->ws.tau.as<float>(),
+             l->ws.dp.as<float>(), nullptr);
+        color_solve(l, *J.cfg, J.d_views, l->ws.tau.as<float>(), l->ws.dp.as<float>(), nullptr, J.d_out, J.stats,
+                    &tv[q]);
+        l->pending.trace_host = nullptr;  // the solve writes its trace from the host
+    }
     for (size_t q = 0; q < batched.size(); ++q) {
         const Slot &sl = batched[q];
         const lfrv_view_job &J = jobs[sl.job];
@@ -1792,6 +1910,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         const Geometry G = geometry(*J.cfg);
         bool is_batched = false;
         for (const Slot &b : batched) is_batched = is_batched || b.job == j;
+        for (int t : tv_idx) is_batched = is_batched || t == j;
         if (is_batched) continue;
         ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
         ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
@@ -1893,7 +2012,47 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         const GridBarrier gb = fresh_barrier(c);
         LFRV_CUDA(launch_cg_batch(d_probs, d_block_prob, (int)cnt, used, part, part + 4 * (size_t)used, d_done, gb, s,
                                   c->launches));
-        LFRV_CUDA(cudaStreamSynchronize(s));  // the host vectors above go out of scope
+        // the next launch rewrites the descriptors in batch_meta (the host vectors were staged by the copies)
+        if (first + cnt < batched.size()) LFRV_CUDA(cudaStreamSynchronize(s));
+    }
+    // the corrected IBR_color jobs in lockstep (beside the batched CG on the context stream): every round enqueues
+    // each running job's certificate, waits once for all of them, then enqueues each job's next FISTA step
+    {
+        std::vector<size_t> running;
+        for (size_t q = 0; q < tv.size(); ++q) running.push_back(q);
+        while (!running.empty()) {
+            for (size_t q : running) tv[q].eval();
+            for (size_t q : running) LFRV_CUDA(cudaStreamSynchronize(c->tv_jobs[q]->stream));
+            std::vector<size_t> next;
+            for (size_t q : running) {
+                TvSolve &ts = tv[q];
+                if (!ts.decide()) {
+                    ts.step();
+                    next.push_back(q);
+                    continue;
+                }
+                ts.finish();
+                const lfrv_view_job &J = jobs[tv_idx[q]];
+                lfrv_ctx *l = c->tv_jobs[q];
+                LFRV_CUDA(cudaMemcpyAsync(J.d_out, l->ws.U.p, sizeof(float) * 3 * ts.G.N, cudaMemcpyDeviceToDevice,
+                                          l->stream));
+                if (J.stats) {
+                    J.stats->outer_iterations = ts.k;
+                    J.stats->meta_iterations = 1;
+                    J.stats->stop_reason = (J.cfg->cg_gap_tol > 0 && ts.gap <= J.cfg->cg_gap_tol) ? 4 : 0;
+                    J.stats->energy = ts.E;
+                    J.stats->gap = ts.gap;
+                    J.stats->trace_length = ts.st ? ts.trace_pos : 0;
+                }
+            }
+            running.swap(next);
+        }
+        for (lfrv_ctx *l : c->tv_jobs) {
+            LFRV_CUDA(cudaStreamSynchronize(l->stream));
+            c->launches.add((int)l->launches.n);
+            l->launches.n = 0;
+            finish_stats(l);  // barrier status of the FGP launches
+        }
     }
     for (const Slot &sl : batched)
         LFRV_CUDA(cudaMemcpyAsync(jobs[sl.job].d_out, base + sl.off + (sl.seeded ? 14 * sl.G.N + 16 : 0),

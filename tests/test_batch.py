@@ -24,7 +24,8 @@ def test_batch_matches_single_targets():
     import torch
 
     specs = [(2, 32, 1, {}), (1, 48, 1, {}), (2, 24, 0, dict(niter=5)), (1, 40, 1, dict(faithful=1)),
-             (2, 40, 1, dict(cg_gap_tol=1e-6))]
+             (2, 40, 1, dict(cg_gap_tol=1e-6)), (1, 48, 0, dict(faithful=0, niter=60, cg_gap_tol=1e-4)),
+             (2, 32, 0, dict(faithful=0, niter=6, cg_gap_tol=0.0))]
     jobs = []
     for preset, w, alg, kw in specs:
         sc = scene(preset, w)
@@ -61,7 +62,8 @@ def test_batch_jobs_match_fp64_oracle():
     from scenes import rel_err
 
     specs = [(2, 32, 1, dict(cg_gap_tol=0.0, cg_max_iter=12)), (1, 48, 1, dict(cg_gap_tol=0.0, cg_max_iter=9)),
-             (2, 24, 0, dict(niter=5)), (1, 40, 1, dict(cg_gap_tol=0.0, cg_max_iter=15))]
+             (2, 24, 0, dict(niter=5)), (1, 40, 1, dict(cg_gap_tol=0.0, cg_max_iter=15)),
+             (1, 48, 0, dict(faithful=0, niter=5, cg_gap_tol=0.0))]
     jobs, scenes = [], []
     for preset, w, alg, kw in specs:
         sc = scene(preset, w)
@@ -81,7 +83,9 @@ def test_batch_jobs_match_fp64_oracle():
             assert st.outer_iterations == rst.outer_iterations
             assert rel_err(j["out"].cpu().numpy(), ref) <= 1e-4
             tr, rtr = st.trace(), rst.trace()
-            assert len(tr) == len(rtr) == st.outer_iterations
+            # one entry per iteration; the corrected IBR_color trace also holds the starting point's energy
+            extra = 1 if (j["algorithm"] == 0 and not j["cfg"].faithful) else 0
+            assert len(tr) == len(rtr) == st.outer_iterations + extra
             assert np.max(np.abs(tr - rtr) / np.abs(rtr)) <= 1e-4
 
 
