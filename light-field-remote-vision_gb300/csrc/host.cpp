@@ -1836,7 +1836,10 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
     c->pending = Pending{};
     // the batched jobs' warp stage, set-up and hole filling run on kLanes helper contexts (own stream and
     // workspace each, round robin), so small targets overlap; the context stream waits for all of them
-    constexpr int kLanes = 4;
+#ifndef LFRV_BATCH_LANES
+#define LFRV_BATCH_LANES 4
+#endif
+    constexpr int kLanes = LFRV_BATCH_LANES;
     while ((int)c->lanes.size() < kLanes) {
         lfrv_ctx *l = new lfrv_ctx;
         l->device = c->device;
@@ -1944,15 +1947,41 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         if (st && st->energy_trace && st->trace_capacity > 0) trace_total += (size_t)st->trace_capacity;
     }
     if (trace_total) ws.trace.ensure(sizeof(double) * trace_total);
-    // the CG of all gradient jobs, in launches of at most `resident` jobs
+    // A job with at least as many 64 x 16 tiles as the batched launch has resident blocks fills the GPU on its own:
+    // it gains nothing from sharing a launch, so it runs the single-target persistent CG (shared-memory resident
+    // or TMA form) on its pool buffers, one after another on the context stream. The others share k_cg_batch.
     const int resident = cg_batch_resident_blocks();
-    for (size_t first = 0; first < batched.size(); first += (size_t)resident) {
-        const size_t cnt = std::min(batched.size() - first, (size_t)resident);
+    std::vector<size_t> grouped;
+    for (size_t q = 0; q < batched.size(); ++q) {
+        const Slot &sl = batched[q];
+        const long long ntiles = (long long)((sl.G.W + 63) / 64) * ((sl.G.H + 15) / 16);
+        if (ntiles < resident) {
+            grouped.push_back(q);
+            continue;
+        }
+        const lfrv_config &cfg = *jobs[sl.job].cfg;
+        const lfrv_stats *jst = jobs[sl.job].stats;
+        const bool traced = jst && jst->energy_trace && jst->trace_capacity > 0;
+        float *U = base + sl.off;
+        const size_t N = sl.G.N;
+        const size_t np = (size_t)persistent_partials();
+        double *part = partial_buf(c, 8 * np);
+        const GridBarrier gb = fresh_barrier(c);
+        LFRV_CUDA(launch_cg_persistent(sl.G.W, sl.G.H, U + 3 * N, U + 4 * N, sl.seeded ? U + 14 * N + 16 : U,
+                                       U + 5 * N, U + 8 * N, U + 11 * N, part, part + 4 * np, gb, cfg.cg_max_iter,
+                                       cfg.cg_gap_tol, reinterpret_cast<double *>(U + 14 * N), s, c->launches,
+                                       sl.seeded ? U : nullptr, traced ? ws.trace.as<double>() + trace_off[q] : nullptr,
+                                       traced ? jst->trace_capacity : 0));
+        check_launch("batched job CG");
+    }
+    // the CG of the other gradient jobs, in launches of at most `resident` jobs
+    for (size_t first = 0; first < grouped.size(); first += (size_t)resident) {
+        const size_t cnt = std::min(grouped.size() - first, (size_t)resident);
         std::vector<CgProblem> probs(cnt);
         std::vector<int> tiles(cnt);
         long long total = 0;
         for (size_t q = 0; q < cnt; ++q) {
-            const Geometry &G = batched[first + q].G;
+            const Geometry &G = batched[grouped[first + q]].G;
             tiles[q] = ((G.W + 63) / 64) * ((G.H + 15) / 16);
             total += tiles[q];
         }
@@ -1974,7 +2003,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         std::vector<int> block_prob(used);
         int b0 = 0;
         for (size_t q = 0; q < cnt; ++q) {
-            const Slot &sl = batched[first + q];
+            const Slot &sl = batched[grouped[first + q]];
             const lfrv_config &cfg = *jobs[sl.job].cfg;
             float *U = base + sl.off;
             CgProblem &P = probs[q];
@@ -1996,7 +2025,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
             P.U0 = sl.seeded ? U : nullptr;
             const lfrv_stats *jst = jobs[sl.job].stats;
             const bool traced = jst && jst->energy_trace && jst->trace_capacity > 0;
-            P.trace = traced ? ws.trace.as<double>() + trace_off[first + q] : nullptr;
+            P.trace = traced ? ws.trace.as<double>() + trace_off[grouped[first + q]] : nullptr;
             P.trace_cap = traced ? jst->trace_capacity : 0;
             for (int k = 0; k < nb[q]; ++k) block_prob[b0 + k] = (int)q;
             b0 += nb[q];
@@ -2013,7 +2042,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         LFRV_CUDA(launch_cg_batch(d_probs, d_block_prob, (int)cnt, used, part, part + 4 * (size_t)used, d_done, gb, s,
                                   c->launches));
         // the next launch rewrites the descriptors in batch_meta (the host vectors were staged by the copies)
-        if (first + cnt < batched.size()) LFRV_CUDA(cudaStreamSynchronize(s));
+        if (first + cnt < grouped.size()) LFRV_CUDA(cudaStreamSynchronize(s));
     }
     // the corrected IBR_color jobs in lockstep (beside the batched CG on the context stream): every round enqueues
     // each running job's certificate, waits once for all of them, then enqueues each job's next FISTA step

@@ -25,7 +25,8 @@ def test_batch_matches_single_targets():
 
     specs = [(2, 32, 1, {}), (1, 48, 1, {}), (2, 24, 0, dict(niter=5)), (1, 40, 1, dict(faithful=1)),
              (2, 40, 1, dict(cg_gap_tol=1e-6)), (1, 48, 0, dict(faithful=0, niter=60, cg_gap_tol=1e-4)),
-             (2, 32, 0, dict(faithful=0, niter=6, cg_gap_tol=0.0))]
+             (2, 32, 0, dict(faithful=0, niter=6, cg_gap_tol=0.0)), (2, 512, 1, {})]
+    # the 1024^2 job has more 64 x 16 tiles than the batched CG has resident blocks: it runs the single-target CG
     jobs = []
     for preset, w, alg, kw in specs:
         sc = scene(preset, w)

@@ -282,11 +282,12 @@ def test_training_gain_over_plain_start(ctx):
 @pytest.mark.gpu
 def test_batched_warm_start_matches_single_targets(ctx, net):
     """lfrv_render_views_warm_dev: seeded jobs converge like the one-target warm call; a target that is not a
-    multiple of 8 runs unseeded, as in the plain batch."""
+    multiple of 8 runs unseeded, as in the plain batch; the 1024^2 target fills the GPU and runs the single-target
+    CG from its seed."""
     torch = _cuda()
     net.set_params(wo.init_params(4))
     jobs, keep, singles = [], [], []
-    for seed, w in ((50, 64), (51, 40), (52, 36)):
+    for seed, w in ((50, 64), (51, 40), (52, 36), (53, 1024)):
         sc = scene(1, w, seed=seed)
         cfg = gradient_config(sc, cg_gap_tol=1e-6, cg_max_iter=500)
         views, depth = _f32_dev(torch, sc.views), _f32_dev(torch, sc.depth)
