@@ -41,8 +41,9 @@ constexpr int kBucketPer = 4;
 
 __global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, const float *__restrict__ tau,
                                unsigned int *__restrict__ cnt, unsigned long long *__restrict__ mask, int nb) {
-    const int m0 = blockIdx.x * blockDim.x * kBucketPer + threadIdx.x;
-    const float *tv = tau + (size_t)blockIdx.y * 2 * n;
+    const int v = (int)(blockIdx.x % (unsigned)V);
+    const int m0 = (int)(blockIdx.x / (unsigned)V) * blockDim.x * kBucketPer + threadIdx.x;
+    const float *tv = tau + (size_t)v * 2 * n;
     float tx[kBucketPer], ty[kBucketPer];
 #pragma unroll
     for (int j = 0; j < kBucketPer; ++j) {
@@ -55,7 +56,7 @@ __global__ void k_bucket_count(int V, int n, int W, int H, int dsf, int BW, cons
         const long long b = bucket_of(tx[j], ty[j], W, H, dsf, BW);
         if (m0 + j * (int)blockDim.x < n && b >= 0) {
             atomicAdd(&cnt[b], 1u);
-            if (mask) atomicOr(&mask[(size_t)(blockIdx.y >> 6) * nb + b], 1ull << (blockIdx.y & 63));
+            if (mask) atomicOr(&mask[(size_t)(v >> 6) * nb + b], 1ull << (v & 63));
         }
     }
 }
@@ -79,8 +80,8 @@ __global__ void k_bucket_fill(int V, int n, int W, int H, int dsf, int BW, const
                               unsigned int *__restrict__ entries) {
     pdl_wait();
     pdl_trigger();
-    const int v = blockIdx.y;
-    const int m0 = blockIdx.x * blockDim.x * kBucketPer + threadIdx.x;
+    const int v = (int)(blockIdx.x % (unsigned)V);
+    const int m0 = (int)(blockIdx.x / (unsigned)V) * blockDim.x * kBucketPer + threadIdx.x;
     const float *tv = tau + (size_t)v * 2 * n;
     float tx[kBucketPer], ty[kBucketPer];
 #pragma unroll
@@ -747,7 +748,7 @@ __global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int ds
             for (unsigned int k = s0; k < e0; ++k) {
                 const unsigned int ent = __ldg(entries + k);
                 const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
-                if (v >= kLearnViews) continue;
+                if (v >= kLearnViews) break;  // a bucket's entries ascend by view: the rest are later views
                 const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
                 float raw;
                 const float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw) * ldv(wgt + (size_t)v * n + m);
@@ -1159,7 +1160,10 @@ void launch_bucket_build(const Geometry &G, const float *tau, Buckets &B, cudaSt
                          bool counted) {
     ProfScope _ps(lc, "bucket_build", st);
     const int ks = G.dsf + 1;
-    const dim3 b1(256), gs((G.n + 256 * kBucketPer - 1) / (256 * kBucketPer), G.V);
+    // one block per (view, chunk of 256 * kBucketPer source pixels), views varying fastest: the blocks in flight
+    // cover one band of source rows in every view, so the buckets they count into and fill (whose entries
+    // interleave the views) stay in one band of the target, in L2, until every view's entry of a sector is in
+    const dim3 b1(256), gs((unsigned)((G.n + 256 * kBucketPer - 1) / (256 * kBucketPer)) * (unsigned)G.V);
     if (!counted) {  // else k_tau has counted while writing tau
         cudaMemsetAsync(B.count, 0, sizeof(unsigned int) * B.nb, st);
         if (B.mask) cudaMemsetAsync(B.mask, 0, sizeof(unsigned long long) * B.nb * B.mask_words, st);

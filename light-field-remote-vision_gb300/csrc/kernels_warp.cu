@@ -400,9 +400,11 @@ __global__ void __launch_bounds__(256) k_tau(int V, int w, int h, const float *_
                                              const unsigned long long *__restrict__ zkey) {
     pdl_wait();
     pdl_trigger();
-    const int v = blockIdx.y;
+    // views vary fastest along the grid: the blocks in flight cover one band of source rows in every view, so
+    // the inverse map's counters they update stay in one band of the target (and in L2)
+    const int v = (int)(blockIdx.x % (unsigned)V);
     const int n = w * h;
-    const int m0 = blockIdx.x * blockDim.x * kTauPer + threadIdx.x;
+    const int m0 = (int)(blockIdx.x / (unsigned)V) * blockDim.x * kTauPer + threadIdx.x;
     if (m0 >= n) return;
     const float *dz = depth + (size_t)v * 3 * n;
     const ViewCam c = view_cam(cams, v);
@@ -647,7 +649,8 @@ void launch_tau(int V, int w, int h, const float *depth, const WarpCams &cams, i
     const int n = w * h;
     const BucketCount count = bc ? *bc : BucketCount{};
     // programmatic launch: its launch overlaps the tail of the z-buffer kernel before it
-    launch_pdl(k_tau, dim3((n + 256 * kTauPer - 1) / (256 * kTauPer), V), dim3(256), 0, st, V, w, h, depth, cams, W,
+    launch_pdl(k_tau, dim3((unsigned)((n + 256 * kTauPer - 1) / (256 * kTauPer)) * (unsigned)V), dim3(256), 0, st, V, w,
+               h, depth, cams, W,
                H, zbuf, tau3, dpart3, tau2, dp2, count, zkey);
     lc.add(1);
 }

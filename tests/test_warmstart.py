@@ -311,3 +311,43 @@ def test_batched_warm_start_matches_single_targets(ctx, net):
         assert lfrv.psnr(out.cpu().numpy(), ref.cpu().numpy()) > 60.0
         assert abs(stats[k].outer_iterations - st1.outer_iterations) <= 1
 
+
+
+@pytest.mark.gpu
+def test_learned_input_views_match_oracle(ctx):
+    """The per-view channels of the network input on a 24-view light field (views past the first 8 end each bucket's
+    scan): view v splatted alone equals the FP64 oracle's weighted average of view v on the same warps and weights,
+    and its share of the splat weight the oracle's weight sums, to BF16 rounding."""
+    import pyoracle
+
+    torch = _cuda()
+    sc = scene(2, 32, seed=43)
+    cfg = gradient_config(sc, cg_gap_tol=1e-6, cg_max_iter=500)
+    H, W = sc.params.h * sc.params.dsf, sc.params.w * sc.params.dsf
+    views, depth = _f32_dev(torch, sc.views), _f32_dev(torch, sc.depth)
+    inp = torch.zeros((H, W, 48), dtype=torch.bfloat16, device="cuda")
+    u0 = torch.zeros((3, H, W), dtype=torch.float32, device="cuda")
+    sol = torch.zeros((3, H, W), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    ctx.warmstart_features_dev(cfg, views.data_ptr(), depth.data_ptr(), sc.cams, sc.target, inp.data_ptr(),
+                               u0.data_ptr(), sol.data_ptr())
+    torch.cuda.synchronize()
+    x = inp.float().cpu().numpy()
+    assert sc.views.shape[0] > 8
+    tau, dpart, _ = ctx.warp(sc.depth, sc.cams, sc.target)
+    zero = np.zeros((H, W), np.float32)
+    _, _, wgt = pyoracle.stage_weights(cfg, sc.views, tau, dpart, np.zeros((3, H, W), np.float32),
+                                       np.zeros((H, W), np.uint8), zero, zero, prec=0)
+    cfg1 = gradient_config(sc, cg_gap_tol=1e-6, cg_max_iter=500)
+    cfg1.nviews = 1
+    norms = []
+    for v in range(8):
+        Uv, nv = pyoracle.stage_initial_image(cfg1, sc.views[v:v + 1], tau[v:v + 1], wgt[v:v + 1], prec=0)
+        got = x[..., 6 + 3 * v:9 + 3 * v].transpose(2, 0, 1)
+        want = np.where(nv > 0, Uv, 0.0)
+        np.testing.assert_allclose(got, want, rtol=8e-3, atol=2e-3)
+        norms.append(nv)
+    norms = np.array(norms, np.float64)
+    total = norms.sum(0)
+    share = np.where(total > 0, norms / np.where(total > 0, total, 1), 0.0)
+    np.testing.assert_allclose(x[..., 30:38].transpose(2, 0, 1), share, rtol=8e-3, atol=2e-3)
