@@ -12,6 +12,7 @@
 #include <cstring>
 #include <mutex>
 
+#include <cooperative_groups.h>
 #include <cudaTypedefs.h>
 
 #include "device_common.cuh"
@@ -20,6 +21,8 @@
 #include "lfrv_internal.h"
 
 namespace lfrv {
+
+namespace cg = cooperative_groups;
 
 // Hole list in raster order: one warp per row counts its holes (ballot), one block scans the row counts,
 // one warp per row writes its holes in order.
@@ -1243,40 +1246,47 @@ __global__ void __launch_bounds__(kPersistThreads) k_cg_batch(const CgProblem *_
     }
 }
 
-// Hole filling for at most kSmallHoles holes, in one block and in shared memory. The visible pixels never change,
-// so every hole keeps, per direction (left, up, right, down: the summation order of compute_laplacian), either
-// the index of the neighbouring hole or the neighbour's fixed value; the iterations then touch shared memory
-// only. Each update gives k_hole_fill_persistent's value bit for bit (its division by the neighbour count is a
-// corrected reciprocal product). holes must be in ascending pixel order with the row starts behind them
-// (launch_hole_list).
-constexpr int kSmallHoles = 2048, kSmallThreads = 1024;
+// Hole filling in shared memory, without a grid barrier: one block (C = 1) for at most kSmallHoles holes, or one
+// cluster of C blocks for at most C * kSmallHoles, each block holding a contiguous share of the sorted hole list.
+// The visible pixels never change, so every hole keeps, per direction (left, up, right, down: the summation order
+// of compute_laplacian), either a reference to the neighbouring hole (block rank << 11 | index in that block's
+// share) or the neighbour's fixed value; the iterations then touch shared memory only, a cluster's blocks reading
+// each other's shares through distributed shared memory, with one cluster barrier per iteration. Each update
+// gives k_hole_fill_persistent's value bit for bit (its division by the neighbour count is a corrected
+// reciprocal product). holes must be in ascending pixel order with the row starts behind them (launch_hole_list).
+constexpr int kSmallHoles = 2048, kSmallThreads = 1024, kHoleCluster = 8;
+static_assert(kSmallHoles == 1 << 11 && kHoleCluster * kSmallHoles <= 32767, "hole references are 16-bit");
 constexpr size_t kSmallHoleSmem = (size_t)kSmallHoles * (6 * 4 + 12 * 4 + 4 * 2 + 4);
 
+template <int C>
 __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H, const int *__restrict__ holes,
                                                                    const int *__restrict__ count, float *A,
                                                                    int max_iter, double *state) {
     const int nh = *count;
-    if (nh > kSmallHoles) return;  // the grid-wide kernel takes it
+    // the sizes this form takes (every block of a cluster returns together, before any cluster barrier)
+    if (nh > C * kSmallHoles || (C > 1 && nh <= kSmallHoles)) return;
     extern __shared__ __align__(16) float hsm[];
     float *cur = hsm, *nxt = hsm + 3 * kSmallHoles;            // [3][kSmallHoles] each
     float *fixedv = hsm + 6 * kSmallHoles;                      // [4 dirs][3][kSmallHoles]
     float *wts = hsm + 18 * kSmallHoles;                        // [kSmallHoles]
     __shared__ float rws[kSmallHoles];                          // 1 / wts
-    short *nb = reinterpret_cast<short *>(hsm + 19 * kSmallHoles);  // [4][kSmallHoles]: hole index, -1 fixed, -2 none
+    short *nb = reinterpret_cast<short *>(hsm + 19 * kSmallHoles);  // [4][kSmallHoles]: reference, -1 fixed, -2 none
     __shared__ float wsum[2][kSmallThreads / 32];
     __shared__ int s_holes[kSmallHoles];
+    const int rank = C > 1 ? (int)cg::this_cluster().block_rank() : 0;
+    const int chunk = (nh + C - 1) / C, h0 = rank * chunk, nloc = max(0, min(nh - h0, chunk));
     const size_t N = (size_t)W * H;
-    for (int h = threadIdx.x; h < nh; h += kSmallThreads) s_holes[h] = __ldg(holes + h);
+    for (int h = threadIdx.x; h < nloc; h += kSmallThreads) s_holes[h] = __ldg(holes + h0 + h);
     __syncthreads();
     // row starts of the hole list (launch_hole_list keeps them in holes[N .. N + H)): a vertical neighbour is
     // searched in its row's few holes only, a horizontal one is the adjacent entry of the sorted list
     const int *row_start = holes + N;
-    for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
-        const int o = s_holes[h];
+    for (int h = threadIdx.x; h < nloc; h += kSmallThreads) {
+        const int g = h0 + h, o = s_holes[h];
         const int ox = o % W, oy = o / W;
         const bool has[4] = {ox > 0, oy > 0, ox < W - 1, oy < H - 1};
         const int q[4] = {o - 1, o - W, o + 1, o + W};
-        int lo[4] = {h - 1, 0, h + 1, 0}, hi[4] = {h - 1, -1, min(h + 1, nh - 1), -1};
+        int lo[4] = {g - 1, 0, g + 1, 0}, hi[4] = {g - 1, -1, min(g + 1, nh - 1), -1};
         if (has[1]) {
             lo[1] = __ldg(row_start + oy - 1);
             hi[1] = __ldg(row_start + oy) - 1;
@@ -1295,9 +1305,10 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
                 idx = -1;
                 int l = max(lo[d], 0), r = hi[d];
                 while (l <= r) {
-                    const int mid = (l + r) >> 1, v = s_holes[mid];
+                    const int mid = (l + r) >> 1, v = __ldg(holes + mid);
                     if (v == q[d]) {
-                        idx = (short)mid;
+                        const int rr = mid / chunk;
+                        idx = (short)((rr << 11) | (mid - rr * chunk));
                         break;
                     }
                     if (v < q[d]) l = mid + 1;
@@ -1316,11 +1327,13 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
                 for (int c = 0; c < 3; ++c) fixedv[(d * 3 + c) * kSmallHoles + h] = A[c * N + q[d]];
         for (int c = 0; c < 3; ++c) cur[c * kSmallHoles + h] = A[c * N + o];
     }
-    __syncthreads();
-    // only the warps that hold holes iterate (at least one, so that an empty hole set reports its one iteration
-    // as the reference does): the others leave, and the iterations synchronise on named barrier 1 with the
-    // iterating threads' count
-    const int active = max(32, min(kSmallThreads, (nh + 31) & ~31));
+    // a cluster: every block's share is in place before any block reads another's
+    if constexpr (C > 1) cg::this_cluster().sync();
+    else __syncthreads();
+    // one block: only the warps that hold holes iterate (at least one, so that an empty hole set reports its one
+    // iteration as the reference does); the others leave, and the iterations synchronise on named barrier 1 with
+    // the iterating threads' count. A cluster: every thread takes part in the cluster barriers.
+    const int active = C > 1 ? kSmallThreads : max(32, min(kSmallThreads, (nloc + 31) & ~31));
     if ((int)threadIdx.x >= active) return;
     float energy = 0.0f, previous = 0.0f;
     int k;
@@ -1329,7 +1342,7 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
         // the energy in FP32 (a handful of terms per thread, fixed shuffle trees): the FP64 pipe of this part is
         // narrow, and the stop test compares single-precision energies
         float acc = 0.f;
-        for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
+        for (int h = threadIdx.x; h < nloc; h += kSmallThreads) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
                 float v = 0.f;
@@ -1337,7 +1350,15 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
                 for (int d = 0; d < 4; ++d) {
                     const short idx = nb[d * kSmallHoles + h];
                     if (idx == -2) continue;
-                    v += (idx >= 0) ? cur[c * kSmallHoles + idx] : fixedv[(d * 3 + c) * kSmallHoles + h];
+                    if (idx == -1) {
+                        v += fixedv[(d * 3 + c) * kSmallHoles + h];
+                    } else {
+                        const int rr = idx >> 11, l = idx & (kSmallHoles - 1);
+                        const float *src = cur + c * kSmallHoles + l;
+                        if constexpr (C > 1)
+                            if (rr != rank) src = cg::this_cluster().map_shared_rank(src, rr);
+                        v += *src;
+                    }
                 }
                 // v / wt as the reciprocal product with one residual correction (Markstein): with rw the
                 // rounded reciprocal and q within an ulp of the quotient, q + rw (v - wt q) is the correctly
@@ -1357,13 +1378,26 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
         // one barrier per iteration: the warp sums alternate between two slots, and every warp sums the 32 of
-        // this iteration with the same fixed tree (down-shuffles, then lane 0's value), so all agree
+        // this iteration (of each block in rank order) with the same fixed tree, so all agree
         const int lane = threadIdx.x & 31;
         if (lane == 0) wsum[k & 1][threadIdx.x >> 5] = acc;
-        asm volatile("bar.sync 1, %0;" ::"r"(active) : "memory");
-        float tot = (lane < active / 32) ? wsum[k & 1][lane] : 0.f;
+        float tot;
+        if constexpr (C > 1) {
+            cg::this_cluster().sync();
+            tot = 0.f;
+            for (int rr = 0; rr < C; ++rr) {
+                const float *ws = cg::this_cluster().map_shared_rank(&wsum[k & 1][0], rr);
+                float t = ws[lane];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
+                for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+                tot += __shfl_sync(0xffffffffu, t, 0);
+            }
+        } else {
+            asm volatile("bar.sync 1, %0;" ::"r"(active) : "memory");
+            tot = (lane < active / 32) ? wsum[k & 1][lane] : 0.f;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) tot += __shfl_down_sync(0xffffffffu, tot, o);
+        }
         energy = __shfl_sync(0xffffffffu, tot, 0);
         float *t = cur;
         cur = nxt;
@@ -1373,12 +1407,14 @@ __global__ void __launch_bounds__(kSmallThreads) k_hole_fill_small(int W, int H,
             break;
         }
     }
-    for (int h = threadIdx.x; h < nh; h += kSmallThreads) {
+    for (int h = threadIdx.x; h < nloc; h += kSmallThreads) {
         const int o = s_holes[h];
 #pragma unroll
         for (int c = 0; c < 3; ++c) A[c * N + o] = cur[c * kSmallHoles + h];
     }
-    if (threadIdx.x == 0) state[0] = (double)k;
+    if (rank == 0 && threadIdx.x == 0) state[0] = (double)k;
+    // no block leaves while another may still read its shared memory
+    if constexpr (C > 1) cg::this_cluster().sync();
 }
 
 // Hole filling with the whole iteration loop in one launch (hole_filling, sources/gradientIBR.cu:87-152).
@@ -1394,11 +1430,11 @@ constexpr int kHoleFillPerBlock = 4 * kPersistThreads;
 __global__ void __launch_bounds__(kPersistThreads) k_hole_fill_persistent(int W, int H, const int *__restrict__ holes,
                                                                           const int *__restrict__ count, float *A,
                                                                           float *B, double *part, GridBarrier gb,
-                                                                          int max_iter, double *state) {
+                                                                          int max_iter, double *state, int handled) {
     __shared__ double sh[8];
     const size_t N = (size_t)W * H;
     const int nh = *count;
-    if (nh <= kSmallHoles) return;  // k_hole_fill_small has done it
+    if (nh <= handled) return;  // k_hole_fill_small (one block or one cluster) has done it
     const int active = min((int)gridDim.x, max(1, (nh + kHoleFillPerBlock - 1) / kHoleFillPerBlock));
     if ((int)blockIdx.x >= active) return;
     const int tid = blockIdx.x * blockDim.x + threadIdx.x, nthr = active * blockDim.x;
@@ -1744,22 +1780,78 @@ bool encode_tensor_map_3d(CUtensorMap *map, const float *base, int cols, int row
 cudaError_t launch_hole_fill_persistent(int W, int H, const int *holes, const int *count, float *A, float *B,
                                         double *part, GridBarrier gb, int max_iter, double *state, cudaStream_t st,
                                         LaunchCounter &lc) {
+    // The hole count is on the device: the three forms are queued, and each returns at once unless the count is
+    // in its range (one block up to kSmallHoles, one cluster of kHoleCluster blocks up to kHoleCluster times that
+    // where the device can place such a cluster, the grid-wide kernel above).
+    int handled = kSmallHoles;
     {
-        // few holes: one block in shared memory; the grid-wide kernel below then returns at once (and vice versa)
         ProfScope _ps(lc, "hole_fill_small", st);
-        cudaError_t e = cudaFuncSetAttribute(k_hole_fill_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kSmallHoleSmem);
-        if (e != cudaSuccess) return e;
-        k_hole_fill_small<<<1, kSmallThreads, kSmallHoleSmem, st>>>(W, H, holes, count, A, max_iter, state);
+        int dev = 0;
+        cudaGetDevice(&dev);
+        // per device: the shared-memory attributes, and whether a cluster of kHoleCluster such blocks fits
+        static std::mutex mu;
+        static int cluster_ok[64] = {};  // 0 unknown, 1 yes, -1 no
+        const int slot = (dev >= 0 && dev < 64) ? dev : 0;
+        int use_cluster = 0;
+        {
+            std::lock_guard<std::mutex> lock(mu);
+            if (cluster_ok[slot] == 0) {
+                cudaError_t e = cudaFuncSetAttribute(k_hole_fill_small<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                     (int)kSmallHoleSmem);
+                if (e != cudaSuccess) return e;
+                int ok = -1;
+                if (cudaFuncSetAttribute(k_hole_fill_small<kHoleCluster>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kSmallHoleSmem) == cudaSuccess) {
+                    cudaLaunchConfig_t q = {};
+                    cudaLaunchAttribute at[1];
+                    at[0].id = cudaLaunchAttributeClusterDimension;
+                    at[0].val.clusterDim.x = kHoleCluster;
+                    at[0].val.clusterDim.y = 1;
+                    at[0].val.clusterDim.z = 1;
+                    q.gridDim = dim3(kHoleCluster);
+                    q.blockDim = dim3(kSmallThreads);
+                    q.dynamicSmemBytes = kSmallHoleSmem;
+                    q.attrs = at;
+                    q.numAttrs = 1;
+                    int nclusters = 0;
+                    if (cudaOccupancyMaxActiveClusters(&nclusters, (const void *)k_hole_fill_small<kHoleCluster>, &q) ==
+                            cudaSuccess &&
+                        nclusters >= 1)
+                        ok = 1;
+                }
+                cudaGetLastError();  // a refused query leaves no error behind
+                cluster_ok[slot] = ok;
+            }
+            use_cluster = cluster_ok[slot] > 0;
+        }
+        k_hole_fill_small<1><<<1, kSmallThreads, kSmallHoleSmem, st>>>(W, H, holes, count, A, max_iter, state);
         lc.add(1);
-        e = cudaGetLastError();
+        cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
+        if (use_cluster) {
+            cudaLaunchConfig_t q = {};
+            cudaLaunchAttribute at[1];
+            at[0].id = cudaLaunchAttributeClusterDimension;
+            at[0].val.clusterDim.x = kHoleCluster;
+            at[0].val.clusterDim.y = 1;
+            at[0].val.clusterDim.z = 1;
+            q.gridDim = dim3(kHoleCluster);
+            q.blockDim = dim3(kSmallThreads);
+            q.dynamicSmemBytes = kSmallHoleSmem;
+            q.stream = st;
+            q.attrs = at;
+            q.numAttrs = 1;
+            e = cudaLaunchKernelEx(&q, k_hole_fill_small<kHoleCluster>, W, H, holes, count, A, max_iter, state);
+            if (e != cudaSuccess) return e;
+            lc.add(1);
+            handled = kHoleCluster * kSmallHoles;
+        }
     }
     ProfScope _ps(lc, "hole_fill", st);
     const size_t N = (size_t)W * H;
     const int blocks =
         coop_blocks((const void *)k_hole_fill_persistent, (int)((N + kPersistThreads - 1) / kPersistThreads));
-    void *args[] = {&W, &H, (void *)&holes, (void *)&count, &A, &B, &part, &gb, &max_iter, &state};
+    void *args[] = {&W, &H, (void *)&holes, (void *)&count, &A, &B, &part, &gb, &max_iter, &state, &handled};
     lc.add(1);
     return cudaLaunchCooperativeKernel((const void *)k_hole_fill_persistent, dim3(blocks), dim3(kPersistThreads), args,
                                        0, st);

@@ -172,23 +172,35 @@ def test_gradient_visibility(ctx, preset, w):
     assert np.array_equal(ctx.stage_gradient_visibility(cfg, tau), pyoracle.stage_gradient_visibility(cfg, tau, prec=1))
 
 
-# 868 holes take the single-block shared-memory kernel, 6000 the grid-wide persistent one
-@pytest.mark.parametrize("big", [False, True])
-def test_hole_fill(ctx, big):
+# 868 holes take the single-block shared-memory kernel; 6000 (one region) and about 9000 (scattered, so that many
+# neighbours sit in another block's share) the cluster of shared-memory blocks; 38000 the grid-wide persistent one
+@pytest.mark.parametrize("case", ["block", "cluster", "cluster_scattered", "grid"])
+def test_hole_fill(ctx, case):
     rng = np.random.default_rng(7)
-    H, W = (96, 128) if big else (64, 72)
+    H, W = {"block": (64, 72), "cluster": (96, 128), "cluster_scattered": (150, 150), "grid": (256, 256)}[case]
     U = rng.uniform(0.1, 0.9, (3, H, W)).astype(np.float32)
     vis = np.ones((H, W), np.uint8)
-    if big:
-        vis[20:80, 10:110] = 0
-    else:
+    if case == "block":
         vis[10:30, 5:40] = 0
         vis[50:64, 60:72] = 0
+    elif case == "cluster":
+        vis[20:80, 10:110] = 0
+    elif case == "cluster_scattered":
+        vis[rng.uniform(size=(H, W)) < 0.4] = 0
+    else:
+        vis[20:220, 10:200] = 0
     U[:, vis == 0] = 0.0
     out, it = ctx.stage_hole_fill(U, vis, 500)
     ref, rit = pyoracle.stage_hole_fill(U, vis, 500, prec=1)
-    assert it == rit
-    assert np.max(np.abs(out - ref)) < 1e-5
+    if case == "grid":
+        # the reference sums the stop test's energy sequentially in float over every pixel; the grid-wide kernel
+        # sums it in FP64. With 38000 terms the two roundings can put the stop a few iterations apart, near
+        # convergence, where an iteration changes the image little
+        assert abs(it - rit) <= 3, (it, rit)
+        assert np.max(np.abs(out - ref)) < 1e-3, np.max(np.abs(out - ref))
+    else:
+        assert it == rit
+        assert np.max(np.abs(out - ref)) < 1e-5
 
 
 @pytest.mark.parametrize("preset,w", [(1, 64), (2, 32)])
