@@ -9,6 +9,7 @@
 //   dtau/dz: tauPartial.frag:23-48 (sigma_z = 10 in channel 0).
 // Per input view the host folds the cameras into M = K_u R_u R_k^T K_k^-1 and b = K_u (t_u - R_u R_k^T t_k),
 // so the target homogeneous point of input pixel (x, y) at depth z is x_h = M (z (x, y, 1)) + b.
+#include <type_traits>
 #include "device_common.cuh"
 #include "kernels.h"
 
@@ -167,7 +168,7 @@ __device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigne
 //   - the depth is the triangle's 1/z plane (tri_cover's barycentric interpolation, which is affine over the
 //     triangle) evaluated at the centre the same way; it differs from tri_cover's quotient by float rounding
 //     only.
-// The 3 x 3 window is unrolled. Returns false when the quad needs raster_quad.
+// The window is unrolled at 2 x 2 or 3 x 3. Returns false when the quad needs raster_quad.
 __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc, int W, int H,
                                                   unsigned long long *zkey) {
     const float areaA = edgef(v[0][0], v[0][1], v[1][0], v[1][1], v[2][0], v[2][1]);
@@ -225,33 +226,39 @@ __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc,
     const unsigned int zlow = ~__float_as_uint(zc);
     // value of an affine function at row base r (its value at (0, j)) stepped i columns
     auto at = [](const Edge &e, float r, int i) { return i == 0 ? r : fmaf(e.gi, (float)i, r); };
-    // one row of the window at a time: the three cells' keys, then their depth-buffer loads together (the
-    // depth test of depth_test, its loads not serialised behind each other's branches)
+    // one row of the window at a time: the cells' keys, then their depth-buffer loads together (the depth test of
+    // depth_test, its loads not serialised behind each other's branches). The window is unrolled at its size: 2 x 2
+    // (the common box of a quad at twice the input resolution) or 3 x 3; each cell's values are the same either way
+    auto window = [&](auto nx_c) {
+        constexpr int NX = decltype(nx_c)::value;
 #pragma unroll
-    for (int j = 0; j < 3; ++j) {
-        if (j > ymax - ymin) break;
-        unsigned long long *row = zkey + (size_t)(ymin + j) * W + xmin;
-        auto base = [j](const Edge &e) { return j == 0 ? e.c0 : fmaf(e.gj, (float)j, e.c0); };
-        const float r12 = base(e12), ra1 = base(a1), ra2 = base(a2), rb0 = base(b0), rb1 = base(b1);
-        const float rA = base(pA), rB = base(pB);
-        unsigned long long key[3], cur[3];
-        bool hit[3];
+        for (int j = 0; j < NX; ++j) {
+            if (j > ymax - ymin) break;
+            unsigned long long *row = zkey + (size_t)(ymin + j) * W + xmin;
+            auto base = [j](const Edge &e) { return j == 0 ? e.c0 : fmaf(e.gj, (float)j, e.c0); };
+            const float r12 = base(e12), ra1 = base(a1), ra2 = base(a2), rb0 = base(b0), rb1 = base(b1);
+            const float rA = base(pA), rB = base(pB);
+            unsigned long long key[NX], cur[NX];
+            bool hit[NX];
 #pragma unroll
-        for (int i = 0; i < 3; ++i) {
-            const float w12 = at(e12, r12, i);
-            const bool inA = w12 >= e12.thr;
-            const float wa1 = at(a1, ra1, i), wa2 = at(a2, ra2, i), wb0 = at(b0, rb0, i), wb1 = at(b1, rb1, i);
-            const bool cov = inA ? (wa1 >= a1.thr && wa2 >= a2.thr) : (wb0 >= b0.thr && wb1 >= b1.thr);
-            const float iz = inA ? at(pA, rA, i) : at(pB, rB, i);
-            hit[i] = i <= xmax - xmin && cov && iz > 0.f;
-            key[i] = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
+            for (int i = 0; i < NX; ++i) {
+                const float w12 = at(e12, r12, i);
+                const bool inA = w12 >= e12.thr;
+                const float wa1 = at(a1, ra1, i), wa2 = at(a2, ra2, i), wb0 = at(b0, rb0, i), wb1 = at(b1, rb1, i);
+                const bool cov = inA ? (wa1 >= a1.thr && wa2 >= a2.thr) : (wb0 >= b0.thr && wb1 >= b1.thr);
+                const float iz = inA ? at(pA, rA, i) : at(pB, rB, i);
+                hit[i] = i <= xmax - xmin && cov && iz > 0.f;
+                key[i] = ((unsigned long long)__float_as_uint(iz) << 32) | zlow;
+            }
+#pragma unroll
+            for (int i = 0; i < NX; ++i) cur[i] = hit[i] ? __ldcg(row + i) : ~0ull;
+#pragma unroll
+            for (int i = 0; i < NX; ++i)
+                if (hit[i] && cur[i] < key[i]) atomicMax(row + i, key[i]);
         }
-#pragma unroll
-        for (int i = 0; i < 3; ++i) cur[i] = hit[i] ? __ldcg(row + i) : ~0ull;
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-            if (hit[i] && cur[i] < key[i]) atomicMax(row + i, key[i]);
-    }
+    };
+    if (xmax - xmin <= 1 && ymax - ymin <= 1) window(std::integral_constant<int, 2>{});
+    else window(std::integral_constant<int, 3>{});
     return true;
 }
 
