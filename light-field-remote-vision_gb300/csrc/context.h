@@ -34,7 +34,7 @@ struct Workspace {
     // inverse footprint map
     DevBuf b_count, b_start, b_entries, b_aux, b_mask;
     // target
-    DevBuf U, Ua, Ub, Uprev, P, Pa, F, G, g, g0, tmp, cov, norm, vis, Xq, gx, gy, mask, zkey, zbuf;
+    DevBuf U, Ua, Ub, Uprev, P, Pa, F, G, g, g0, tmp, cov, norm, vis, Xq, gx, gy, mask, zkey, zbuf, zdefer;
     // gradient data term (dt_beta)
     DevBuf lapU, resg, ugrad;
     // target depth keys of the warps-from-depth path

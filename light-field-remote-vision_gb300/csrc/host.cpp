@@ -1126,6 +1126,7 @@ static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfr
     for (int v = 0; v < V; ++v) fold_camera(cams[v], *target, wc.M[v], wc.b[v]);
     ws.zkey.ensure(sizeof(unsigned long long) * N);
     ws.zbuf.ensure(sizeof(float) * N);
+    ws.zdefer.ensure(sizeof(unsigned int) * zsplat_defer_words(V, w, h));
     launch_zbuffer_clear(W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
     // count_for (the solve's geometry, whose inverse map is built next from tau2): k_tau counts its buckets. The
     // counts are cleared here, ahead of the splat, so that k_tau directly follows the z-buffer kernels
@@ -1155,11 +1156,13 @@ static void warp(lfrv_ctx *c, int V, int w, int h, const float *depth, const lfr
                 std::memcpy(part.b[v - v0], wc.b[v], sizeof(wc.b[v]));
             }
             launch_zbuffer_splat(v1 - v0, w, h, depth + (size_t)v0 * 3 * w * h, part, W, H,
-                                 ws.zkey.as<unsigned long long>(), c->stream, c->launches);
+                                 ws.zkey.as<unsigned long long>(), ws.zdefer.as<unsigned int>(), c->stream,
+                                 c->launches);
             v0 = v1;
         }
     } else {
-        launch_zbuffer_splat(V, w, h, depth, wc, W, H, ws.zkey.as<unsigned long long>(), c->stream, c->launches);
+        launch_zbuffer_splat(V, w, h, depth, wc, W, H, ws.zkey.as<unsigned long long>(), ws.zdefer.as<unsigned int>(),
+                             c->stream, c->launches);
     }
     // the resolved depth map only when the caller wants it; otherwise k_tau samples the keys themselves
     if (zbuf_out)

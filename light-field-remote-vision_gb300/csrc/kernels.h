@@ -62,8 +62,10 @@ void launch_warp_from_depth(int V, int w, int h, int dsf, const float *depth, in
 void launch_radial_to_ortho(int V, int w, int h, const WarpCams &kinv, float *depth, cudaStream_t st,
                             LaunchCounter &lc);
 void launch_zbuffer_clear(int W, int H, unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc);
+// Words of the z-buffer splat's queue of large quads for V views of w x h (launch_zbuffer_splat's defer_q).
+size_t zsplat_defer_words(int V, int w, int h);
 void launch_zbuffer_splat(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H,
-                          unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc);
+                          unsigned long long *zkey, unsigned int *defer_q, cudaStream_t st, LaunchCounter &lc);
 void launch_zbuffer_resolve(int W, int H, const unsigned long long *zkey, float *zbuf, cudaStream_t st,
                             LaunchCounter &lc);
 // tau3/dpart3: reference format (V x 3 x n); tau2/dp2: solver format (V x 2 x n), dp2 premultiplied by sigma_z.

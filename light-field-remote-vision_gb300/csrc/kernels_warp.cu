@@ -9,6 +9,7 @@
 //   dtau/dz: tauPartial.frag:23-48 (sigma_z = 10 in channel 0).
 // Per input view the host folds the cameras into M = K_u R_u R_k^T K_k^-1 and b = K_u (t_u - R_u R_k^T t_k),
 // so the target homogeneous point of input pixel (x, y) at depth z is x_h = M (z (x, y, 1)) + b.
+#include <algorithm>
 #include <type_traits>
 #include "device_common.cuh"
 #include "kernels.h"
@@ -107,8 +108,11 @@ __device__ __forceinline__ bool tri_cover(const TriSetup &t, float e0, float e1,
 
 // The quad (strip BL v0, TL v1, BR v2, TR v3) as triangles A = (v0, v1, v2) and B = (v1, v2, v3), which share
 // the edge v1v2 (A's edge 0, B's edge 2). One pass over the union of their boxes evaluates that edge once per
-// pixel; each triangle's coverage and depth are those of rasterising it alone.
-__device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigned long long *zkey) {
+// pixel; each triangle's coverage and depth are those of rasterising it alone. The box's pixels are taken
+// first, first + stride, ... in row-major order (a warp shares one quad with first = lane, stride = 32; the
+// depth test's result does not depend on the order).
+__device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigned long long *zkey, int first = 0,
+                            int stride = 1) {
     const TriSetup A = tri_setup(v[0], v[1], v[2], W, H), B = tri_setup(v[1], v[2], v[3], W, H);
     if (!A.live && !B.live) return;
     const int xmin = A.live ? (B.live ? min(A.xmin, B.xmin) : A.xmin) : B.xmin;
@@ -116,14 +120,15 @@ __device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigne
     const int ymin = A.live ? (B.live ? min(A.ymin, B.ymin) : A.ymin) : B.ymin;
     const int ymax = A.live ? (B.live ? max(A.ymax, B.ymax) : A.ymax) : B.ymax;
     const unsigned int zlow = ~__float_as_uint(zc);
+    const int bw = xmax - xmin + 1, npx = bw * (ymax - ymin + 1);
     if (A.live && B.live && A.sgn != B.sgn) {
         // Opposite windings (a strip quad that does not fold): the shared edge splits the quad, and a pixel
         // centre on the edge belongs to the triangle whose edge is top-left (the two flags are complementary),
         // so only the triangle on the pixel's side is tested. With o = v0 (A) or v3 (B), its other edges are
         // v2 -> o and o -> v1, and its depth (e12 z_o + e2o z_1 + eo1 z_2) / (e12 + e2o + eo1) equals
         // tri_cover's (the winding sign cancels in the quotient).
-        for (int y = ymin; y <= ymax; ++y)
-            for (int x = xmin; x <= xmax; ++x) {
+        for (int p = first; p < npx; p += stride) {
+                const int y = ymin + p / bw, x = xmin + p % bw;
                 const float px = x + 0.5f, py = y + 0.5f;
                 const float e12 = edgef(v[1][0], v[1][1], v[2][0], v[2][1], px, py);
                 const float a12 = A.sgn * e12;
@@ -141,8 +146,8 @@ __device__ void raster_quad(const float (*v)[3], float zc, int W, int H, unsigne
             }
         return;
     }
-    for (int y = ymin; y <= ymax; ++y)
-        for (int x = xmin; x <= xmax; ++x) {
+    for (int p = first; p < npx; p += stride) {
+            const int y = ymin + p / bw, x = xmin + p % bw;
             const float px = x + 0.5f, py = y + 0.5f;
             const float e12 = edgef(v[1][0], v[1][1], v[2][0], v[2][1], px, py);
             float iz;
@@ -262,10 +267,12 @@ __device__ __forceinline__ bool raster_quad_small(const float (*v)[3], float zc,
     return true;
 }
 
-// One input pixel m of view cam c: its tilted quad into the depth buffer.
-__device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int m, int w, int n, float rw, float z, float zx,
-                                             float zy, int W, int H, unsigned long long *zkey) {
-    if (z >= 1000.0f * 0.5f) return;  // INVALID_DEPTH / 2 (depthSplatting.geom:21)
+// The tilted quad of input pixel m of view cam c in target pixel space: its corners (x, y, 1/w) in strip order
+// BL, TL, BR, TR and its centre depth zc. False when the pixel is not splatted (invalid depth, or a corner behind
+// the near plane).
+__device__ __forceinline__ bool zsplat_vertices(const ViewCam &c, int m, int w, int n, float rw, float z, float zx,
+                                                float zy, float (*vert)[3], float &zc) {
+    if (z >= 1000.0f * 0.5f) return false;  // INVALID_DEPTH / 2 (depthSplatting.geom:21)
     int px, py;
     pixel_of(m, w, n, rw, px, py);
     const float cx = px + 0.5f, cy = py + 0.5f;
@@ -274,9 +281,8 @@ __device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int m, int w, int
     // dy M_1) + b, M_0 and M_1 the first two columns of M
     float q[3];
     mv3(c.M, cx, cy, 1.f, q);
-    const float zc = fmaf(z, q[2], c.b[2]);
+    zc = fmaf(z, q[2], c.b[2]);
     const float off[4][2] = {{-0.5f, -0.5f}, {-0.5f, 0.5f}, {0.5f, -0.5f}, {0.5f, 0.5f}};  // BL TL BR TR
-    float vert[4][3];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
         const float dx = off[k][0], dy = off[k][1];
@@ -284,13 +290,34 @@ __device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int m, int w, int
         float xh[3];
 #pragma unroll
         for (int r = 0; r < 3; ++r) xh[r] = fmaf(zk, fmaf(dy, c.M[3 * r + 1], fmaf(dx, c.M[3 * r], q[r])), c.b[r]);
-        if (!(xh[2] > 1e-2f)) return;  // behind the near plane (zNear = 1e-2, sources/pinholeCamera.cpp:133)
+        if (!(xh[2] > 1e-2f)) return false;  // behind the near plane (zNear = 1e-2, sources/pinholeCamera.cpp:133)
         const float iw = __fdividef(1.0f, xh[2]);  // approximate reciprocal: vertex positions within 2 ulp
         vert[k][0] = xh[0] * iw;
         vert[k][1] = xh[1] * iw;
         vert[k][2] = iw;
     }
-    if (!raster_quad_small(vert, zc, W, H, zkey)) raster_quad(vert, zc, W, H, zkey);
+    return true;
+}
+
+// Queue of the quads that need the general rasteriser (a box beyond 3 x 3 pixel centres, or a folded strip):
+// word 0 counts them, entries (view << 24 | pixel) follow from word kZdeferHead. Those quads are few but their
+// boxes are large, so one lane rasterising one of them would hold its whole warp; k_zsplat_defer gives each a
+// warp. When the queue is full the quad is rasterised where it is.
+constexpr int kZdeferHead = 32;
+struct ZDefer {
+    unsigned int *q;
+    unsigned int cap;
+};
+
+// One input pixel m of view v (camera c): its tilted quad into the depth buffer.
+__device__ __forceinline__ void zsplat_pixel(const ViewCam &c, int v, int m, int w, int n, float rw, float z, float zx,
+                                             float zy, int W, int H, unsigned long long *zkey, ZDefer defer) {
+    float vert[4][3], zc;
+    if (!zsplat_vertices(c, m, w, n, rw, z, zx, zy, vert, zc)) return;
+    if (raster_quad_small(vert, zc, W, H, zkey)) return;
+    const unsigned int slot = defer.q ? atomicAdd(defer.q, 1u) : defer.cap;
+    if (slot < defer.cap) defer.q[kZdeferHead + slot] = ((unsigned int)v << 24) | (unsigned int)m;
+    else raster_quad(vert, zc, W, H, zkey);
 }
 
 // Two input pixels per thread (m and m + blockDim.x): the second pixel's depth is loaded before the first is
@@ -299,7 +326,7 @@ constexpr int kZsplatPerThread = 2;
 
 __global__ void __launch_bounds__(256, 4) k_zsplat(int V, int w, int h, const float *__restrict__ depth,
                                                 const WarpCams cams, int W, int H,
-                                                unsigned long long *__restrict__ zkey) {
+                                                unsigned long long *__restrict__ zkey, ZDefer defer) {
     pdl_trigger();  // k_tau, launched next, waits for this grid's completion
     const int m0 = blockIdx.x * blockDim.x * kZsplatPerThread + threadIdx.x, m1 = m0 + blockDim.x;
     const int v = blockIdx.y;
@@ -311,8 +338,32 @@ __global__ void __launch_bounds__(256, 4) k_zsplat(int V, int w, int h, const fl
     if (m1 < n) z1 = dz[m1], zx1 = dz[n + m1], zy1 = dz[2 * n + m1];
     const ViewCam c = view_cam(cams, v);
     const float rw = __frcp_rn((float)w);
-    zsplat_pixel(c, m0, w, n, rw, z0, zx0, zy0, W, H, zkey);
-    if (m1 < n) zsplat_pixel(c, m1, w, n, rw, z1, zx1, zy1, W, H, zkey);
+    zsplat_pixel(c, v, m0, w, n, rw, z0, zx0, zy0, W, H, zkey, defer);
+    if (m1 < n) zsplat_pixel(c, v, m1, w, n, rw, z1, zx1, zy1, W, H, zkey, defer);
+}
+
+// The queued quads of k_zsplat, one warp each: the corners again (the same arithmetic), then the lanes share
+// the general rasteriser's box.
+__global__ void __launch_bounds__(256) k_zsplat_defer(int w, int h, const float *__restrict__ depth,
+                                                     const WarpCams cams, int W, int H,
+                                                     unsigned long long *__restrict__ zkey, ZDefer defer) {
+    pdl_wait();
+    pdl_trigger();
+    const unsigned int cnt = min(__ldcg(defer.q), defer.cap);
+    const int lane = threadIdx.x & 31;
+    const unsigned int nw = (gridDim.x * blockDim.x) >> 5;
+    const int n = w * h;
+    const float rw = __frcp_rn((float)w);
+    for (unsigned int it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < cnt; it += nw) {
+        const unsigned int e = __ldcg(defer.q + kZdeferHead + it);
+        const int v = (int)(e >> 24), m = (int)(e & 0xFFFFFFu);
+        const float *dz = depth + (size_t)v * 3 * n;
+        float vert[4][3], zc;
+        if (!zsplat_vertices(view_cam(cams, v), m, w, n, rw, __ldg(dz + m), __ldg(dz + n + m), __ldg(dz + 2 * n + m),
+                             vert, zc))
+            continue;
+        raster_quad(vert, zc, W, H, zkey, lane, 32);
+    }
 }
 
 // The target depth a z-buffer key holds (its centre depth; 0 where nothing was splatted).
@@ -482,13 +533,28 @@ void launch_zbuffer_clear(int W, int H, unsigned long long *zkey, cudaStream_t s
     cudaMemsetAsync(zkey, 0, sizeof(unsigned long long) * (size_t)W * H, st);  // key 0: nothing splatted
 }
 
+size_t zsplat_defer_words(int V, int w, int h) {
+    const size_t quads = (size_t)V * w * h;
+    return kZdeferHead + std::max<size_t>(65536, quads / 64);
+}
+
 void launch_zbuffer_splat(int V, int w, int h, const float *depth, const WarpCams &cams, int W, int H,
-                          unsigned long long *zkey, cudaStream_t st, LaunchCounter &lc) {
+                          unsigned long long *zkey, unsigned int *defer_q, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "zbuffer_splat", st);
     const int n = w * h;
     const int per_block = 256 * kZsplatPerThread;
-    k_zsplat<<<dim3((n + per_block - 1) / per_block, V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zkey);
+    ZDefer defer{defer_q, defer_q ? (unsigned int)(zsplat_defer_words(V, w, h) - kZdeferHead) : 0u};
+    if (defer_q) cudaMemsetAsync(defer_q, 0, sizeof(unsigned int), st);
+    k_zsplat<<<dim3((n + per_block - 1) / per_block, V), 256, 0, st>>>(V, w, h, depth, cams, W, H, zkey, defer);
     lc.add(1);
+    if (defer_q) {
+        // one warp per queued quad, as many warps as two blocks per SM hold (the count is read on the device)
+        int dev = 0, sms = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        launch_pdl(k_zsplat_defer, dim3(2 * std::max(sms, 1)), dim3(256), 0, st, w, h, depth, cams, W, H, zkey, defer);
+        lc.add(1);
+    }
 }
 
 // ------------------------------------------------------------------ warps from depth maps without GL
