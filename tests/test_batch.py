@@ -119,3 +119,28 @@ def test_host_buffer_batch_equals_device_batch():
         np.testing.assert_array_equal(o, d.cpu().numpy())
         assert a.outer_iterations == b.outer_iterations
     assert not np.array_equal(outs[0], outs[1])
+
+
+def test_batches_of_both_lane_counts_in_one_context():
+    """A batch with a target of 2^21 pixels or more prepares its jobs on two lanes, a batch of small targets on four:
+    alternating them in one context gives each job what it gives alone, with the same statistics."""
+    import torch
+
+    big = scene(1, 1456)
+    small = [scene(2, 32), scene(1, 48)]
+    with lfrv.Context(0) as ctx:
+        for specs in ([big, small[0]], small, [big]):
+            jobs = [_job(torch, sc, gradient_config(sc), 1) for sc in specs]
+            torch.cuda.synchronize()
+            stats = ctx.render_views_dev([dict(cfg=j["cfg"], algorithm=1, d_views=j["views"].data_ptr(),
+                                               d_depth=j["depth"].data_ptr(), cams=j["cams"], target=j["target"],
+                                               d_out=j["out"].data_ptr()) for j in jobs])
+            torch.cuda.synchronize()
+            for j, st in zip(jobs, stats):
+                single = torch.zeros_like(j["out"])
+                st1 = ctx.render_view_dev(j["cfg"], 1, j["views"].data_ptr(), j["depth"].data_ptr(), j["cams"],
+                                          j["target"], single.data_ptr())
+                torch.cuda.synchronize()
+                assert st.outer_iterations == st1.outer_iterations
+                assert st.hole_fill_iterations == st1.hole_fill_iterations
+                assert np.max(np.abs(j["out"].cpu().numpy() - single.cpu().numpy())) < 1e-5
