@@ -964,17 +964,20 @@ __device__ __forceinline__ void rof_project(float p[6], float r) {
 // All niter inner ROF iterations in one cooperative launch, temporally blocked. One iteration is the dual step
 // p += sigma grad_fwd(U) (vtv_rof.cu:118-147), the reprojection of the 6 duals onto the ball of radius g
 // (vtv_rof.cu:280-320) and the primal prox U = (tau F + lambda (U + tau div_bwd p)) / (tau + lambda)
-// (cuda_kernels.cu:504-532). Each super-step runs up to kRofK iterations: a block stages a
-// (kRofTX + 2 kRofK) x (kRofTY + 2 kRofK) region of U, P, F, g in shared memory, iterates there (duals in
-// place, then the primal in place), and writes back its kRofTX x kRofTY tile, whose values depend only on
-// the region (the halo absorbs one pixel of staleness per iteration from each side). Super-steps read one
-// global (U, P) pair and write the other, with a bounded grid barrier between them.
-// K (iterations per super-step) and the block size are template parameters; the host picks an instantiation
-// per image size with a timing autotuner (rof_autotune).
+// (cuda_kernels.cu:504-532). Each super-step runs up to kRofK iterations on a (kRofTX + 2 kRofK) x
+// (kRofTY + 2 kRofK) region around a kRofTX x kRofTY tile and writes back the tile, whose values depend only on the
+// region (the halo absorbs one pixel of staleness per iteration from each side). Super-steps read one global
+// (U, P) pair and write the other, with a bounded grid barrier between them.
+// Every thread owns the same PPT region pixels in every iteration (their coordinates and border flags are worked
+// out once per tile): their U, P, F and g stay in registers, and shared memory carries only what the neighbours
+// read, U (right and lower neighbours, in the dual step) and the x and y duals (left and upper neighbours, in the
+// prox). The block sizes divide the region into equal shares, so no warp waits at the block barriers for a
+// second pass of the others. K (iterations per super-step) and the block size are template parameters; the
+// host picks an instantiation per image size with a timing autotuner (rof_autotune).
 constexpr int kRofTX = 32, kRofTY = 16;
 template <int K>
 constexpr size_t rof_smem() {
-    return (size_t)13 * (kRofTX + 2 * K) * (kRofTY + 2 * K) * sizeof(float);  // U 3, P 6, F 3, g 1 planes
+    return (size_t)9 * (kRofTX + 2 * K) * (kRofTY + 2 * K) * sizeof(float);  // U 3, x duals 3, y duals 3
 }
 
 template <int kRofK, int kRofThreads>
@@ -982,12 +985,17 @@ __global__ void __launch_bounds__(kRofThreads) k_rof_persistent(int W, int H, in
                                                                 float lam, float *U0, float *P0, float *U1,
                                                                 float *P1, const float *__restrict__ F,
                                                                 const float *__restrict__ g, GridBarrier gb) {
-    constexpr int kRofRX = kRofTX + 2 * kRofK, kRofRY = kRofTY + 2 * kRofK, kRofRN = kRofRX * kRofRY;
+    constexpr int RX = kRofTX + 2 * kRofK, RY = kRofTY + 2 * kRofK, RN = RX * RY;
+    constexpr int PPT = (RN + kRofThreads - 1) / kRofThreads;  // region pixels per thread
     extern __shared__ float sm[];
-    float *sU = sm, *sP = sm + 3 * kRofRN, *sF = sm + 9 * kRofRN, *sG = sm + 12 * kRofRN;
+    float *sU = sm, *sPx = sm + 3 * RN, *sPy = sm + 6 * RN;
     const int tiles_x = (W + kRofTX - 1) / kRofTX, ntiles = tiles_x * ((H + kRofTY - 1) / kRofTY);
     const size_t N = (size_t)W * H;
     const float denom = tau + lam;
+    // flags of an owned pixel: inside the image, its forward differences exist (x, y), its left / upper
+    // neighbour's dual enters the divergence (inside the image and the region), and it is a tile pixel
+    constexpr unsigned kIn = 1, kFx = 2, kFy = 4, kBx = 8, kBy = 16, kTile = 32, kRx = 64, kRy = 128;
+    constexpr int kDistShift = 8;
     unsigned int gen = 0;
     int step = 0;
     for (int done = 0; done < niter; done += kRofK, ++step) {
@@ -996,65 +1004,105 @@ __global__ void __launch_bounds__(kRofThreads) k_rof_persistent(int W, int H, in
         float *Uo = (step & 1) ? U0 : U1, *Po = (step & 1) ? P0 : P1;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
             const int rx0 = (t % tiles_x) * kRofTX - kRofK, ry0 = (t / tiles_x) * kRofTY - kRofK;
-            for (int i = threadIdx.x; i < kRofRN; i += kRofThreads) {
-                const int gx = rx0 + i % kRofRX, gy = ry0 + i / kRofRX;
-                const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
+            float u[PPT][3], p[PPT][6], f[PPT][3], gg[PPT];
+            unsigned int fl[PPT];
+            size_t go[PPT];
+#pragma unroll
+            for (int k = 0; k < PPT; ++k) {
+                const int i = threadIdx.x + k * kRofThreads;
+                const int lx = i % RX, ly = i / RX, gx = rx0 + lx, gy = ry0 + ly;
+                const bool in = i < RN && gx >= 0 && gx < W && gy >= 0 && gy < H;
+                unsigned int f0 = 0;
+                if (in) {
+                    f0 |= kIn;
+                    if (gx < W - 1) f0 |= kFx;
+                    if (gy < H - 1) f0 |= kFy;
+                    if (gx > 0) f0 |= kBx;
+                    if (gy > 0) f0 |= kBy;
+                    if (lx + 1 < RX) f0 |= kRx;
+                    if (ly + 1 < RY) f0 |= kRy;
+                    if (lx >= kRofK && lx < kRofK + kRofTX && ly >= kRofK && ly < kRofK + kRofTY) f0 |= kTile;
+                    // distance from the tile (Chebyshev, in pixels)
+                    const int dx = max(max(kRofK - lx, lx - (kRofK + kRofTX - 1)), 0);
+                    const int dy = max(max(kRofK - ly, ly - (kRofK + kRofTY - 1)), 0);
+                    f0 |= (unsigned int)max(dx, dy) << kDistShift;
+                }
+                fl[k] = f0;
                 const size_t o = in ? (size_t)gy * W + gx : 0;
+                go[k] = o;
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
-                    sU[c * kRofRN + i] = in ? __ldcg(Ui + c * N + o) : 0.f;
-                    sF[c * kRofRN + i] = in ? __ldg(F + c * N + o) : 0.f;
+                    u[k][c] = in ? __ldcg(Ui + c * N + o) : 0.f;
+                    f[k][c] = in ? __ldg(F + c * N + o) : 0.f;
                 }
 #pragma unroll
-                for (int c = 0; c < 6; ++c) sP[c * kRofRN + i] = in ? __ldcg(Pi + c * N + o) : 0.f;
-                sG[i] = in ? __ldg(g + o) : 0.f;
+                for (int c = 0; c < 6; ++c) p[k][c] = in ? __ldcg(Pi + c * N + o) : 0.f;
+                gg[k] = in ? __ldg(g + o) : 0.f;
+                if (i < RN) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        sU[c * RN + i] = u[k][c];
+                        sPx[c * RN + i] = p[k][2 * c];
+                        sPy[c * RN + i] = p[k][2 * c + 1];
+                    }
+                }
             }
             __syncthreads();
             for (int it = 0; it < iters; ++it) {
-                // dual step + reprojection, in place: reads U (unchanged here) and the pixel's own P
-                for (int i = threadIdx.x; i < kRofRN; i += kRofThreads) {
-                    const int lx = i % kRofRX, ly = i / kRofRX, gx = rx0 + lx, gy = ry0 + ly;
-                    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
-                    float p[6];
+                // Only the pixels the tile still depends on are updated: after iteration it the tile needs U within
+                // distance iters - it - 1 of it (the prox), and that prox reads the duals one pixel further out
+                // (the dual step, whose right and lower neighbours' U were updated in the iteration before).
+                // dual step + reprojection: the pixel's own U and p, its right and lower neighbours' U
+                const unsigned int dual_reach = (unsigned int)(iters - it) << kDistShift;
+                const unsigned int prox_reach = (unsigned int)(iters - it - 1) << kDistShift;
+#pragma unroll
+                for (int k = 0; k < PPT; ++k) {
+                    if (!(fl[k] & kIn) || (fl[k] & ~0xFFu) > dual_reach) continue;
+                    const int i = threadIdx.x + k * kRofThreads;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const float *u = sU + c * kRofRN;
-                        const float uc = u[i];
-                        const float ur = (lx + 1 < kRofRX) ? u[i + 1] : 0.f, ud = (ly + 1 < kRofRY) ? u[i + kRofRX] : 0.f;
-                        const float gxv = (gx < W - 1) ? ur - uc : 0.f;
-                        const float gyv = (gy < H - 1) ? ud - uc : 0.f;
-                        p[2 * c] = sP[(2 * c) * kRofRN + i] + sigma * gxv;
-                        p[2 * c + 1] = sP[(2 * c + 1) * kRofRN + i] + sigma * gyv;
+                        const float *su = sU + c * RN;
+                        const float uc = u[k][c];
+                        const float ur = (fl[k] & kRx) ? su[i + 1] : 0.f, ud = (fl[k] & kRy) ? su[i + RX] : 0.f;
+                        const float gxv = (fl[k] & kFx) ? ur - uc : 0.f;
+                        const float gyv = (fl[k] & kFy) ? ud - uc : 0.f;
+                        p[k][2 * c] = p[k][2 * c] + sigma * gxv;
+                        p[k][2 * c + 1] = p[k][2 * c + 1] + sigma * gyv;
                     }
-                    rof_project(p, sG[i]);
+                    rof_project(p[k], gg[k]);
 #pragma unroll
-                    for (int k = 0; k < 6; ++k) sP[k * kRofRN + i] = p[k];
+                    for (int c = 0; c < 3; ++c) {
+                        sPx[c * RN + i] = p[k][2 * c];
+                        sPy[c * RN + i] = p[k][2 * c + 1];
+                    }
                 }
                 __syncthreads();
-                // primal prox, in place: reads the new duals of the pixel and its left / upper neighbour
-                for (int i = threadIdx.x; i < kRofRN; i += kRofThreads) {
-                    const int lx = i % kRofRX, ly = i / kRofRX, gx = rx0 + lx, gy = ry0 + ly;
-                    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+                // primal prox: the pixel's new duals and its left / upper neighbours'
+#pragma unroll
+                for (int k = 0; k < PPT; ++k) {
+                    if (!(fl[k] & kIn) || (fl[k] & ~0xFFu) > prox_reach) continue;
+                    const int i = threadIdx.x + k * kRofThreads;
+                    const int lx = i % RX, ly = i / RX;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        float st = sP[(2 * c) * kRofRN + i] + sP[(2 * c + 1) * kRofRN + i];
-                        if (gx > 0) st -= (lx > 0) ? sP[(2 * c) * kRofRN + i - 1] : 0.f;
-                        if (gy > 0) st -= (ly > 0) ? sP[(2 * c + 1) * kRofRN + i - kRofRX] : 0.f;
-                        const float unew = sU[c * kRofRN + i] + tau * st;
-                        sU[c * kRofRN + i] = (tau * sF[c * kRofRN + i] + lam * unew) / denom;
+                        float st = p[k][2 * c] + p[k][2 * c + 1];
+                        if (fl[k] & kBx) st -= (lx > 0) ? sPx[c * RN + i - 1] : 0.f;
+                        if (fl[k] & kBy) st -= (ly > 0) ? sPy[c * RN + i - RX] : 0.f;
+                        const float unew = u[k][c] + tau * st;
+                        u[k][c] = (tau * f[k][c] + lam * unew) / denom;
+                        sU[c * RN + i] = u[k][c];
                     }
                 }
                 __syncthreads();
             }
-            for (int i = threadIdx.x; i < kRofTX * kRofTY; i += kRofThreads) {
-                const int lx = kRofK + i % kRofTX, ly = kRofK + i / kRofTX, gx = rx0 + lx, gy = ry0 + ly;
-                if (gx >= W || gy >= H) continue;
-                const size_t o = (size_t)gy * W + gx;
-                const int r = ly * kRofRX + lx;
 #pragma unroll
-                for (int c = 0; c < 3; ++c) Uo[c * N + o] = sU[c * kRofRN + r];
+            for (int k = 0; k < PPT; ++k) {
+                if ((fl[k] & (kIn | kTile)) != (kIn | kTile)) continue;
+                const size_t o = go[k];
 #pragma unroll
-                for (int c = 0; c < 6; ++c) Po[c * N + o] = sP[c * kRofRN + r];
+                for (int c = 0; c < 3; ++c) Uo[c * N + o] = u[k][c];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) Po[c * N + o] = p[k][c];
             }
             __syncthreads();  // the next tile overwrites the staged region
         }
@@ -1571,14 +1619,16 @@ struct RofVariant {
     size_t smem;
 };
 static const RofVariant kRofVariants[] = {
-    {2, 512, (const void *)k_rof_persistent<2, 512>, rof_smem<2>()},
-    {2, 1024, (const void *)k_rof_persistent<2, 1024>, rof_smem<2>()},
-    {4, 512, (const void *)k_rof_persistent<4, 512>, rof_smem<4>()},
-    {4, 1024, (const void *)k_rof_persistent<4, 1024>, rof_smem<4>()},
-    {8, 1024, (const void *)k_rof_persistent<8, 1024>, rof_smem<8>()},
+    // the region of K = 2, 4, 6, 8, 12 holds 720, 960, 1232, 1536, 2240 pixels: 2, 2, 2, 2 or 3, 4 per thread
+    {2, 384, (const void *)k_rof_persistent<2, 384>, rof_smem<2>()},
+    {4, 480, (const void *)k_rof_persistent<4, 480>, rof_smem<4>()},
+    {6, 640, (const void *)k_rof_persistent<6, 640>, rof_smem<6>()},
+    {8, 768, (const void *)k_rof_persistent<8, 768>, rof_smem<8>()},
+    {8, 512, (const void *)k_rof_persistent<8, 512>, rof_smem<8>()},
+    {12, 576, (const void *)k_rof_persistent<12, 576>, rof_smem<12>()},
 };
 int rof_variant_count() { return (int)(sizeof(kRofVariants) / sizeof(kRofVariants[0])); }
-int rof_default_variant() { return 3; }
+int rof_default_variant() { return 3; }  // K = 8, 768 threads
 
 // Number of super-steps of variant v for niter iterations: the result is in (U1, P1) when it is odd.
 int rof_persistent_steps(int niter, int v) { return (niter + kRofVariants[v].K - 1) / kRofVariants[v].K; }
