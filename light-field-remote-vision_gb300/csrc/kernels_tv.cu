@@ -129,102 +129,145 @@ __global__ void k_tv_clamp(size_t n, const float *__restrict__ in, float *__rest
 }
 
 // ------------------------------------------------------------------ FGP on the weighted ROF dual
-// One cooperative launch runs every inner iteration. Temporally blocked: a block stages its tile and a halo of
-// kFgpK pixels (q, p, F, lam, 1/L, g) in shared memory and runs kFgpK iterations there before it writes the tile
-// back and the grid synchronises (each iteration's dependence reaches one pixel in each direction, diagonals
-// included, so the tile stays exact). Per iteration, on the staged region:
+// One cooperative launch runs every inner iteration. Temporally blocked: a block takes a tile and a halo of K
+// pixels and runs K iterations on that region before it writes the tile back and the grid synchronises (each
+// iteration's dependence reaches one pixel in each direction, diagonals included, so the tile stays exact; the
+// updated part of the region shrinks by a pixel per iteration to what the tile still depends on). Per iteration:
 //   u = clamp(F + lam div q, 0, 1);  p' = proj_{|.|_F <= g}(q + grad u / L);  q = p' + beta_j (p' - p);  p = p'
 // with beta_j = (s_j - 1) / s_{j+1}, s_0 = 1, s_{j+1} = (1 + sqrt(1 + 4 s_j^2)) / 2 (Beck and Teboulle's FGP).
-constexpr int kFgpTX = 32, kFgpTY = 16, kFgpK = 4, kFgpThreads = 512;
-constexpr int kFgpRX = kFgpTX + 2 * kFgpK, kFgpRY = kFgpTY + 2 * kFgpK, kFgpRN = kFgpRX * kFgpRY;
+// Every thread owns the same PPT region pixels throughout: their q, p, F, lam, 1/L and g stay in registers, and
+// shared memory carries what the neighbours read (u for the gradient, the x and y components of q for the
+// divergence). The block sizes split the region evenly.
 // The dual p and the momentum point q are stored in FP64 (12 planes); u, F, lam, 1/L and g are FP32. TD is the
-// dual's arithmetic (and shared-memory) type. In FP32 the dual's rounding (a few ulp of |p| <= g) leaves
-// lambda div p, and with it the certificate's box term, a noise floor near 4e-4 relative at 256^2; with TD = double
-// the certificate reaches 1e-4 (the oracle's FP32 mirror shows the same). FP64 is slow on this GPU's narrow FP64
-// pipe, so the host runs TD = float while the gap is far above its floor and TD = double to finish.
-template <typename TD>
-constexpr size_t fgp_smem() { return (size_t)12 * kFgpRN * sizeof(TD) + (size_t)9 * kFgpRN * sizeof(float); }
+// dual's arithmetic type. In FP32 the dual's rounding (a few ulp of |p| <= g) leaves lambda div p, and with it the
+// certificate's box term, a noise floor near 4e-4 relative at 256^2; with TD = double the certificate reaches 1e-4
+// (the oracle's FP32 mirror shows the same). FP64 is slow on this GPU's narrow FP64 pipe, so the host runs
+// TD = float while the gap is far above its floor and TD = double to finish.
+constexpr int kFgpTX = 32, kFgpTY = 16;
+template <int K>
+constexpr int fgp_rn() { return (kFgpTX + 2 * K) * (kFgpTY + 2 * K); }
+template <typename TD, int K>
+constexpr size_t fgp_smem() { return (size_t)6 * fgp_rn<K>() * sizeof(TD) + (size_t)3 * fgp_rn<K>() * sizeof(float); }
+// (TD, K, threads): FP32 K = 8 (1536 region pixels, 2 per thread), FP64 K = 4 (960 pixels, 2 per thread)
+constexpr int kFgpKf = 8, kFgpThreadsF = 768, kFgpKd = 4, kFgpThreadsD = 480;
 
-template <typename TD>
-__global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter, const float *__restrict__ F,
-                                                        const float *__restrict__ lam, const float *__restrict__ linv,
-                                                        const float *__restrict__ g, double *P0, double *P1,
-                                                        double *Q0, double *Q1, float *__restrict__ U,
-                                                        GridBarrier gb) {
+template <typename TD, int K, int THREADS>
+__global__ void __launch_bounds__(THREADS) k_tv_fgp(int W, int H, int niter, const float *__restrict__ F,
+                                                    const float *__restrict__ lam, const float *__restrict__ linv,
+                                                    const float *__restrict__ g, double *P0, double *P1, double *Q0,
+                                                    double *Q1, float *__restrict__ U, GridBarrier gb) {
+    constexpr int RX = kFgpTX + 2 * K, RY = kFgpTY + 2 * K, RN = RX * RY;
+    constexpr int PPT = (RN + THREADS - 1) / THREADS;
+    constexpr unsigned kIn = 1, kFx = 2, kFy = 4, kBx = 8, kBy = 16, kTile = 32, kRx = 64, kRy = 128;
+    constexpr int kDistShift = 8;
     extern __shared__ __align__(16) unsigned char fgp_sm[];
-    TD *sQ = reinterpret_cast<TD *>(fgp_sm), *sP = sQ + 6 * kFgpRN;
-    float *sU = reinterpret_cast<float *>(sP + 6 * kFgpRN), *sF = sU + 3 * kFgpRN;
-    float *sL = sF + 3 * kFgpRN, *sI = sL + kFgpRN, *sG = sI + kFgpRN;
+    TD *sQx = reinterpret_cast<TD *>(fgp_sm), *sQy = sQx + 3 * RN;
+    float *sU = reinterpret_cast<float *>(sQy + 3 * RN);
     const int tiles_x = (W + kFgpTX - 1) / kFgpTX, ntiles = tiles_x * ((H + kFgpTY - 1) / kFgpTY);
     const size_t N = (size_t)W * H;
     unsigned int gen = 0;
     double s_step = 1.0;  // s_j at the start of the super-step (every thread follows the same sequence)
     int step = 0;
-    for (int done = 0; done < niter; done += kFgpK, ++step) {
-        const int iters = min(kFgpK, niter - done);
+    for (int done = 0; done < niter; done += K, ++step) {
+        const int iters = min(K, niter - done);
         const double *Pi = (step & 1) ? P1 : P0;
         double *Po = (step & 1) ? P0 : P1;
         const double *Qi = step == 0 ? P0 : ((step & 1) ? Q1 : Q0);  // q starts at p
         double *Qo = (step & 1) ? Q0 : Q1;
         for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
-            const int rx0 = (t % tiles_x) * kFgpTX - kFgpK, ry0 = (t / tiles_x) * kFgpTY - kFgpK;
-            for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
-                const int gx = rx0 + i % kFgpRX, gy = ry0 + i / kFgpRX;
-                const bool in = gx >= 0 && gx < W && gy >= 0 && gy < H;
-                const size_t o = in ? (size_t)gy * W + gx : 0;
+            const int rx0 = (t % tiles_x) * kFgpTX - K, ry0 = (t / tiles_x) * kFgpTY - K;
+            TD q[PPT][6], p[PPT][6];
+            float f[PPT][3], lm[PPT], li[PPT], gg[PPT];
+            unsigned int fl[PPT];
+            size_t go[PPT];
 #pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    sQ[k * kFgpRN + i] = in ? (TD)__ldcg(Qi + k * N + o) : TD(0);
-                    sP[k * kFgpRN + i] = in ? (TD)__ldcg(Pi + k * N + o) : TD(0);
+            for (int k = 0; k < PPT; ++k) {
+                const int i = threadIdx.x + k * THREADS;
+                const int lx = i % RX, ly = i / RX, gx = rx0 + lx, gy = ry0 + ly;
+                const bool in = i < RN && gx >= 0 && gx < W && gy >= 0 && gy < H;
+                unsigned int f0 = 0;
+                if (in) {
+                    f0 |= kIn;
+                    if (gx < W - 1) f0 |= kFx;
+                    if (gy < H - 1) f0 |= kFy;
+                    if (gx > 0) f0 |= kBx;
+                    if (gy > 0) f0 |= kBy;
+                    if (lx + 1 < RX) f0 |= kRx;
+                    if (ly + 1 < RY) f0 |= kRy;
+                    if (lx >= K && lx < K + kFgpTX && ly >= K && ly < K + kFgpTY) f0 |= kTile;
+                    const int dx = max(max(K - lx, lx - (K + kFgpTX - 1)), 0);
+                    const int dy = max(max(K - ly, ly - (K + kFgpTY - 1)), 0);
+                    f0 |= (unsigned int)max(dx, dy) << kDistShift;
+                }
+                fl[k] = f0;
+                const size_t o = in ? (size_t)gy * W + gx : 0;
+                go[k] = o;
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    q[k][c] = in ? (TD)__ldcg(Qi + c * N + o) : TD(0);
+                    p[k][c] = in ? (TD)__ldcg(Pi + c * N + o) : TD(0);
                 }
 #pragma unroll
-                for (int c = 0; c < 3; ++c) sF[c * kFgpRN + i] = in ? __ldg(F + c * N + o) : 0.f;
-                sL[i] = in ? __ldg(lam + o) : 0.f;
-                sI[i] = in ? __ldg(linv + o) : 0.f;
-                sG[i] = in ? __ldg(g + o) : 0.f;
+                for (int c = 0; c < 3; ++c) f[k][c] = in ? __ldg(F + c * N + o) : 0.f;
+                lm[k] = in ? __ldg(lam + o) : 0.f;
+                li[k] = in ? __ldg(linv + o) : 0.f;
+                gg[k] = in ? __ldg(g + o) : 0.f;
+                if (i < RN) {
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        sQx[c * RN + i] = q[k][c];
+                        sQy[c * RN + i] = q[k][3 + c];
+                    }
+                }
             }
             __syncthreads();
             double s = s_step;
             for (int it = 0; it < iters; ++it) {
                 const double s1 = 0.5 * (1.0 + sqrt(1.0 + 4.0 * s * s));
                 const TD beta = (TD)((s - 1.0) / s1);
-                // u(q) on the region (values next to the region's edge are stale and stay outside the tile)
-                for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
-                    const int lx = i % kFgpRX, ly = i / kFgpRX, gx = rx0 + lx, gy = ry0 + ly;
-                    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+                // u(q) where the tile still depends on it (values next to the region's edge are stale and stay
+                // outside the tile)
+                const unsigned int u_reach = (unsigned int)(iters - it) << kDistShift;
+                const unsigned int p_reach = (unsigned int)(iters - it - 1) << kDistShift;
+#pragma unroll
+                for (int k = 0; k < PPT; ++k) {
+                    if (!(fl[k] & kIn) || (fl[k] & ~0xFFu) > u_reach) continue;
+                    const int i = threadIdx.x + k * THREADS;
+                    const int lx = i % RX, ly = i / RX;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const TD *qx = sQ + c * kFgpRN, *qy = sQ + (3 + c) * kFgpRN;
                         TD d = 0;
-                        if (gx < W - 1) d += qx[i];
-                        if (gx > 0) d -= lx > 0 ? qx[i - 1] : TD(0);
-                        if (gy < H - 1) d += qy[i];
-                        if (gy > 0) d -= ly > 0 ? qy[i - kFgpRX] : TD(0);
-                        sU[c * kFgpRN + i] = fminf(1.0f, fmaxf(0.0f, sF[c * kFgpRN + i] + sL[i] * (float)d));
+                        if (fl[k] & kFx) d += q[k][c];
+                        if (fl[k] & kBx) d -= lx > 0 ? sQx[c * RN + i - 1] : TD(0);
+                        if (fl[k] & kFy) d += q[k][3 + c];
+                        if (fl[k] & kBy) d -= ly > 0 ? sQy[c * RN + i - RX] : TD(0);
+                        sU[c * RN + i] = fminf(1.0f, fmaxf(0.0f, f[k][c] + lm[k] * (float)d));
                     }
                 }
                 __syncthreads();
-                // p' = proj(q + grad u / L), q = p' + beta (p' - p), in place (own pixel only)
-                for (int i = threadIdx.x; i < kFgpRN; i += kFgpThreads) {
-                    const int lx = i % kFgpRX, ly = i / kFgpRX, gx = rx0 + lx, gy = ry0 + ly;
-                    if (gx < 0 || gx >= W || gy < 0 || gy >= H) continue;
+                // p' = proj(q + grad u / L), q = p' + beta (p' - p) (own pixel)
+#pragma unroll
+                for (int k = 0; k < PPT; ++k) {
+                    if (!(fl[k] & kIn) || (fl[k] & ~0xFFu) > p_reach) continue;
+                    const int i = threadIdx.x + k * THREADS;
                     TD v[6];
                     TD n2 = 0;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        const float *uc = sU + c * kFgpRN;
-                        const float ur = (lx + 1 < kFgpRX) ? uc[i + 1] : 0.f;
-                        const float ud = (ly + 1 < kFgpRY) ? uc[i + kFgpRX] : 0.f;
-                        const float gxv = gx < W - 1 ? ur - uc[i] : 0.f;
-                        const float gyv = gy < H - 1 ? ud - uc[i] : 0.f;
-                        v[c] = sQ[c * kFgpRN + i] + (TD)(gxv * sI[i]);
-                        v[3 + c] = sQ[(3 + c) * kFgpRN + i] + (TD)(gyv * sI[i]);
+                        const float *uc = sU + c * RN;
+                        const float ui = uc[i];
+                        const float ur = (fl[k] & kRx) ? uc[i + 1] : 0.f;
+                        const float ud = (fl[k] & kRy) ? uc[i + RX] : 0.f;
+                        const float gxv = (fl[k] & kFx) ? ur - ui : 0.f;
+                        const float gyv = (fl[k] & kFy) ? ud - ui : 0.f;
+                        v[c] = q[k][c] + (TD)(gxv * li[k]);
+                        v[3 + c] = q[k][3 + c] + (TD)(gyv * li[k]);
                         n2 += v[c] * v[c] + v[3 + c] * v[3 + c];
                     }
                     // projection onto |p| <= g without an FP64 square root or division (both are long sequences on
-                    // this GPU's narrow FP64 pipe): r = 1 / sqrt(n2) from the FP32 estimate and one FP64 Newton step
-                    // (relative error ~1e-14), applied only where the ball constraint is active
-                    const TD gv = (TD)sG[i];
+                    // this GPU's narrow FP64 pipe): r = 1 / sqrt(n2) from the FP32 estimate and two FP64 Newton
+                    // steps (relative error ~1e-14), applied only where the ball constraint is active
+                    const TD gv = (TD)gg[k];
                     TD sc = 1;
                     if (n2 > gv * gv) {
                         TD r = (TD)rsqrtf((float)n2);
@@ -235,24 +278,28 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
                         sc = gv * r;
                     }
 #pragma unroll
-                    for (int k = 0; k < 6; ++k) {
-                        const TD pn = v[k] * sc;
-                        sQ[k * kFgpRN + i] = pn + beta * (pn - sP[k * kFgpRN + i]);
-                        sP[k * kFgpRN + i] = pn;
+                    for (int c = 0; c < 6; ++c) {
+                        const TD pn = v[c] * sc;
+                        q[k][c] = pn + beta * (pn - p[k][c]);
+                        p[k][c] = pn;
+                    }
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        sQx[c * RN + i] = q[k][c];
+                        sQy[c * RN + i] = q[k][3 + c];
                     }
                 }
                 __syncthreads();
                 s = s1;
             }
-            for (int i = threadIdx.x; i < kFgpTX * kFgpTY; i += kFgpThreads) {
-                const int lx = kFgpK + i % kFgpTX, ly = kFgpK + i / kFgpTX, gx = rx0 + lx, gy = ry0 + ly;
-                if (gx >= W || gy >= H) continue;
-                const size_t o = (size_t)gy * W + gx;
-                const int r = ly * kFgpRX + lx;
 #pragma unroll
-                for (int k = 0; k < 6; ++k) {
-                    Po[k * N + o] = (double)sP[k * kFgpRN + r];
-                    Qo[k * N + o] = (double)sQ[k * kFgpRN + r];
+            for (int k = 0; k < PPT; ++k) {
+                if ((fl[k] & (kIn | kTile)) != (kIn | kTile)) continue;
+                const size_t o = go[k];
+#pragma unroll
+                for (int c = 0; c < 6; ++c) {
+                    Po[c * N + o] = (double)p[k][c];
+                    Qo[c * N + o] = (double)q[k][c];
                 }
             }
             __syncthreads();  // the next tile overwrites the staged region
@@ -261,7 +308,7 @@ __global__ void __launch_bounds__(kFgpThreads) k_tv_fgp(int W, int H, int niter,
         if (!grid_sync(gb, gen)) return;
     }
     // the final dual sits in P0 after an even number of super-steps, else in P1; u = clamp(F + lam div p)
-    const int steps = (niter + kFgpK - 1) / kFgpK;
+    const int steps = (niter + K - 1) / K;
     const double *Pf = (steps & 1) ? P1 : P0;
     double *Pother = (steps & 1) ? P0 : P1;
     for (size_t o = (size_t)blockIdx.x * blockDim.x + threadIdx.x; o < N; o += (size_t)gridDim.x * blockDim.x) {
@@ -330,8 +377,10 @@ cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *
                           double *P0, double *P1, double *Q0, double *Q1, float *U, GridBarrier gb, cudaStream_t st,
                           LaunchCounter &lc, bool fp64) {
     ProfScope _ps(lc, fp64 ? "tv_fgp_fp64" : "tv_fgp", st);
-    const void *kern = fp64 ? (const void *)k_tv_fgp<double> : (const void *)k_tv_fgp<float>;
-    const size_t smem = fp64 ? fgp_smem<double>() : fgp_smem<float>();
+    const void *kern = fp64 ? (const void *)k_tv_fgp<double, kFgpKd, kFgpThreadsD>
+                            : (const void *)k_tv_fgp<float, kFgpKf, kFgpThreadsF>;
+    const size_t smem = fp64 ? fgp_smem<double, kFgpKd>() : fgp_smem<float, kFgpKf>();
+    const int threads = fp64 ? kFgpThreadsD : kFgpThreadsF;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -340,13 +389,14 @@ cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *
     if (dev >= 0 && dev < 64) {
         std::lock_guard<std::mutex> lock(mu);
         if (!attr_set[dev]) {
-            cudaFuncSetAttribute(k_tv_fgp<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)fgp_smem<float>());
-            cudaFuncSetAttribute(k_tv_fgp<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)fgp_smem<double>());
+            cudaFuncSetAttribute(k_tv_fgp<float, kFgpKf, kFgpThreadsF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fgp_smem<float, kFgpKf>());
+            cudaFuncSetAttribute(k_tv_fgp<double, kFgpKd, kFgpThreadsD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fgp_smem<double, kFgpKd>());
             attr_set[dev] = true;
         }
     }
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFgpThreads, smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const int ntiles = ((W + kFgpTX - 1) / kFgpTX) * ((H + kFgpTY - 1) / kFgpTY);
@@ -356,7 +406,7 @@ cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *
     const int blocks = std::max(1, (ntiles + per_block - 1) / per_block);
     void *args[] = {&W, &H, &niter, (void *)&F, (void *)&lam, (void *)&linv, (void *)&g, &P0, &P1, &Q0, &Q1, &U, &gb};
     lc.add(1);
-    return cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(kFgpThreads), args, smem, st);
+    return cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(threads), args, smem, st);
 }
 
 }  // namespace lfrv
