@@ -150,6 +150,7 @@ template <typename TD, int K>
 constexpr size_t fgp_smem() { return (size_t)6 * fgp_rn<K>() * sizeof(TD) + (size_t)3 * fgp_rn<K>() * sizeof(float); }
 // (TD, K, threads): FP32 K = 8 (1536 region pixels, 2 per thread), FP64 K = 4 (960 pixels, 2 per thread)
 constexpr int kFgpKf = 8, kFgpThreadsF = 768, kFgpKd = 4, kFgpThreadsD = 480;
+constexpr int kFgpBetaTable = 256;
 
 template <typename TD, int K, int THREADS>
 __global__ void __launch_bounds__(THREADS) k_tv_fgp(int W, int H, int niter, const float *__restrict__ F,
@@ -163,10 +164,25 @@ __global__ void __launch_bounds__(THREADS) k_tv_fgp(int W, int H, int niter, con
     extern __shared__ __align__(16) unsigned char fgp_sm[];
     TD *sQx = reinterpret_cast<TD *>(fgp_sm), *sQy = sQx + 3 * RN;
     float *sU = reinterpret_cast<float *>(sQy + 3 * RN);
+    // the momentum weights beta_j of the first kFgpBetaTable iterations, worked out once per block (the FP64
+    // square root and division are long sequences on this GPU's narrow FP64 pipe; later iterations, if any,
+    // continue the sequence inline)
+    __shared__ double s_beta[kFgpBetaTable];
+    __shared__ double s_tail;  // s_j after the table
+    if (threadIdx.x == 0) {
+        double sj = 1.0;
+        for (int j = 0; j < min(niter, kFgpBetaTable); ++j) {
+            const double s1 = 0.5 * (1.0 + sqrt(1.0 + 4.0 * sj * sj));
+            s_beta[j] = (sj - 1.0) / s1;
+            sj = s1;
+        }
+        s_tail = sj;
+    }
+    __syncthreads();
     const int tiles_x = (W + kFgpTX - 1) / kFgpTX, ntiles = tiles_x * ((H + kFgpTY - 1) / kFgpTY);
     const size_t N = (size_t)W * H;
     unsigned int gen = 0;
-    double s_step = 1.0;  // s_j at the start of the super-step (every thread follows the same sequence)
+    double s_step = s_tail;  // s_j of the first iteration past the table (every thread follows the same sequence)
     int step = 0;
     for (int done = 0; done < niter; done += K, ++step) {
         const int iters = min(K, niter - done);
@@ -223,8 +239,15 @@ __global__ void __launch_bounds__(THREADS) k_tv_fgp(int W, int H, int niter, con
             __syncthreads();
             double s = s_step;
             for (int it = 0; it < iters; ++it) {
-                const double s1 = 0.5 * (1.0 + sqrt(1.0 + 4.0 * s * s));
-                const TD beta = (TD)((s - 1.0) / s1);
+                const int j = done + it;
+                double s1 = s;
+                TD beta;
+                if (j < kFgpBetaTable) {
+                    beta = (TD)s_beta[j];
+                } else {
+                    s1 = 0.5 * (1.0 + sqrt(1.0 + 4.0 * s * s));
+                    beta = (TD)((s - 1.0) / s1);
+                }
                 // u(q) where the tile still depends on it (values next to the region's edge are stale and stay
                 // outside the tile)
                 const unsigned int u_reach = (unsigned int)(iters - it) << kDistShift;
@@ -304,7 +327,8 @@ __global__ void __launch_bounds__(THREADS) k_tv_fgp(int W, int H, int niter, con
             }
             __syncthreads();  // the next tile overwrites the staged region
         }
-        for (int it = 0; it < iters; ++it) s_step = 0.5 * (1.0 + sqrt(1.0 + 4.0 * s_step * s_step));
+        for (int it = 0; it < iters; ++it)
+            if (done + it >= kFgpBetaTable) s_step = 0.5 * (1.0 + sqrt(1.0 + 4.0 * s_step * s_step));
         if (!grid_sync(gb, gen)) return;
     }
     // the final dual sits in P0 after an even number of super-steps, else in P1; u = clamp(F + lam div p)
