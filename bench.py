@@ -120,12 +120,16 @@ def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: in
     return table.get(kernel)
 
 
-# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from one ncu --set full capture of the
-# C2 step (5x5 light field of 512^2 views -> the 1024^2 target).
+# DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu --set full captures (summaries in
+# profiles/): the C2 step (5x5 light field of 512^2 views -> the 1024^2 target), the C1 ROF launch (256^2), and
+# for the C5 target (80 views of 1024^2 -> 2048^2) the z-buffer splat's C2 capture scaled by its algorithmic
+# bytes (at C2 its traffic is 1.03 x its algorithmic bytes: depth maps read once, keys in L2).
 NCU_TRAFFIC_BYTES = {
-    ("zbuffer_splat", 1024 * 1024): 83.937536e6 + 2.530560e6,
-    ("gradient_setup", 1024 * 1024): 224.049664e6 + 18.143744e6,
-    ("cg_persistent", 1024 * 1024): 21.045248e6 + 0.008192e6,
+    ("zbuffer_splat", 1024 * 1024): 83.942912e6 + 2.418432e6 + 0.335616e6,
+    ("gradient_setup", 1024 * 1024): 223.959296e6 + 18.378240e6,
+    ("cg_persistent", 1024 * 1024): 21.045248e6 + 0.000512e6,
+    ("zbuffer_splat", 2048 * 2048): 1.03 * (12 * 80 * 1024 * 1024 + 8 * 2048 * 2048),
+    ("rof_persistent", 256 * 256): 3.427584e6 + 0.028928e6,
 }
 
 
