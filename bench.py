@@ -111,10 +111,10 @@ def algorithmic_bytes(kernel: str, V: int, n: int, N: int, ks: int, cg_iters: in
         "rof_persistent": 88 * N * rof_iters,
         "residual": 12 * N + 24 * V * n + 12 * V * n,
         # the FGP iterations of one FISTA step in one launch; per iteration the FP64 dual p and momentum q (48 B
-        # each), F (12), lam, 1/L, g (4 each) read and p, q written (96): 216 B per target pixel (both precisions
-        # of the dual's arithmetic keep FP64 storage)
+        # each), F (12), lam, 1/L, g (4 each) read and p, q written (96): 216 B per target pixel (FP32 and
+        # double-float arithmetic of the dual both keep FP64 storage)
         "tv_fgp": 200 * 216 * N,
-        "tv_fgp_fp64": 200 * 216 * N,
+        "tv_fgp_df": 200 * 216 * N,
         "dataterm_F": 12 * V * n + 8 * V * n + 4 * V * n + 12 * N + 12 * N,
     }
     return table.get(kernel)

@@ -460,7 +460,7 @@ struct TvSolve {
     float *u = nullptr, *up = nullptr, *gf = nullptr, *gfp = nullptr, *D = nullptr, *lam = nullptr, *linv = nullptr;
     double *P0 = nullptr, *P1 = nullptr, *Q0 = nullptr, *Q1 = nullptr;
     double t = 1.0, E_prev = 1e300, E = 0.0, gap = 1e300;
-    bool fp64 = false, done = false;
+    bool extended = false, done = false;
     int k = 0, npart = 0;
     lfrv_stats *st = nullptr;  // energy trace destination (optional)
     int trace_pos = 0;
@@ -495,7 +495,7 @@ struct TvSolve {
         npart = tv_gap_partials(G.W, G.H);
         t = 1.0;
         E_prev = 1e300;
-        fp64 = false;
+        extended = false;
         done = false;
         k = 0;
     }
@@ -536,11 +536,11 @@ struct TvSolve {
         std::swap(u, up);
         std::swap(gf, gfp);
         const GridBarrier gb = fresh_barrier(c);
-        // FP32 dual arithmetic while the gap is far above FP32's floor, FP64 once it nears it (the switch only
-        // changes rounding, not the iteration)
-        fp64 = fp64 || gap < kTvFp64Below;
+        // FP32 dual arithmetic while the gap is far above FP32's floor, double-float once it nears it (the switch
+        // only changes rounding, not the iteration)
+        extended = extended || gap < kTvExtendedBelow;
         LFRV_CUDA(launch_tv_fgp(G.W, G.H, kTvInnerIterations, b.F, lam, linv, b.g, P0, P1, Q0, Q1, u, gb, s,
-                                c->launches, fp64));
+                                c->launches, extended));
         ++k;
     }
     // the solution back into ws.U

@@ -200,13 +200,13 @@ void launch_tv_fstep(int W, int H, const float *u, const float *up, const float 
 void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, LaunchCounter &lc);
 // niter FGP iterations on the dual of the weighted ROF problem (one cooperative launch): P0 holds the starting
 // dual (6 FP64 planes: x parts of the 3 channels, then the y parts) and receives the final one; P1, Q0, Q1 are
-// scratch (6 FP64 planes each); U receives clamp(F + lam div p, 0, 1). fp64: the dual's arithmetic in FP64 (else
-// FP32, with the same FP64 storage).
+// scratch (6 FP64 planes each); U receives clamp(F + lam div p, 0, 1). extended: the dual's arithmetic in
+// double-float (about 44 bits; else FP32), with the same FP64 storage.
 cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *lam, const float *linv, const float *g,
                           double *P0, double *P1, double *Q0, double *Q1, float *U, GridBarrier gb, cudaStream_t st,
-                          LaunchCounter &lc, bool fp64);
-// The gap above which the FGP runs in FP32 (its certificate floor is near 4e-4): FP64 takes over below it.
-constexpr double kTvFp64Below = 2e-3;
+                          LaunchCounter &lc, bool extended);
+// The gap above which the FGP runs in FP32 (its certificate floor is near 4e-4): double-float takes over below it.
+constexpr double kTvExtendedBelow = 2e-3;
 
 // One target of a batched CG launch (k_cg_batch): its image, buffers and the contiguous range of blocks that
 // work on it. state: [0..2] delta, [3] E, [4] gap, [5] iterations (written by the problem's first block).

@@ -15,6 +15,7 @@
 #include "lfrv_internal.h"
 
 #include <mutex>
+#include <type_traits>
 
 namespace lfrv {
 
@@ -140,15 +141,80 @@ __global__ void k_tv_clamp(size_t n, const float *__restrict__ in, float *__rest
 // divergence). The block sizes split the region evenly.
 // The dual p and the momentum point q are stored in FP64 (12 planes); u, F, lam, 1/L and g are FP32. TD is the
 // dual's arithmetic type. In FP32 the dual's rounding (a few ulp of |p| <= g) leaves lambda div p, and with it the
-// certificate's box term, a noise floor near 4e-4 relative at 256^2; with TD = double the certificate reaches 1e-4
-// (the oracle's FP32 mirror shows the same). FP64 is slow on this GPU's narrow FP64 pipe, so the host runs
-// TD = float while the gap is far above its floor and TD = double to finish.
+// certificate's box term, a noise floor near 4e-4 relative at 256^2; with the double-float type below (about 44
+// bits) the certificate reaches 1e-4, as with FP64 (the oracle's FP32 mirror shows the floor, its FP64 dual does
+// not). FP64 arithmetic is slow on this GPU's narrow FP64 pipe and double-float costs several FP32 operations per
+// operation, so the host runs TD = float while the gap is far above its floor and TD = dfloat to finish.
+// Double-float arithmetic (an unevaluated sum hi + lo of two floats, about 44 significant bits): the dual's
+// arithmetic where FP32 would leave its noise floor, on the FP32 pipes. Sums use the error-free two-sum (Knuth)
+// and products the FMA-based two-product (Dekker's splitting replaced by fmaf), each renormalised with the
+// fast two-sum; the add is the accurate form (both parts' errors carried), since p' - p cancels.
+struct dfloat {
+    float hi, lo;
+    __device__ __forceinline__ dfloat() : hi(0.f), lo(0.f) {}
+    __device__ __forceinline__ dfloat(int v) : hi((float)v), lo(0.f) {}
+    __device__ __forceinline__ dfloat(float v) : hi(v), lo(0.f) {}
+    __device__ __forceinline__ dfloat(double v) {
+        hi = __double2float_rn(v);
+        lo = __double2float_rn(v - (double)hi);
+    }
+    __device__ __forceinline__ dfloat(float h, float l) : hi(h), lo(l) {}
+    __device__ __forceinline__ explicit operator float() const { return hi + lo; }
+    __device__ __forceinline__ explicit operator double() const { return (double)hi + (double)lo; }
+};
+__device__ __forceinline__ dfloat df_fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return dfloat(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ dfloat df_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    return dfloat(s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb)));
+}
+__device__ __forceinline__ dfloat operator+(dfloat a, dfloat b) {
+    dfloat s = df_two_sum(a.hi, b.hi);
+    const dfloat t = df_two_sum(a.lo, b.lo);
+    s.lo = __fadd_rn(s.lo, t.hi);
+    s = df_fast_two_sum(s.hi, s.lo);
+    s.lo = __fadd_rn(s.lo, t.lo);
+    return df_fast_two_sum(s.hi, s.lo);
+}
+__device__ __forceinline__ dfloat operator-(dfloat a) { return dfloat(-a.hi, -a.lo); }
+__device__ __forceinline__ dfloat operator-(dfloat a, dfloat b) { return a + (-b); }
+__device__ __forceinline__ dfloat operator*(dfloat a, dfloat b) {
+    const float p = __fmul_rn(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.hi, -p);
+    e = __fmaf_rn(a.hi, b.lo, e);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ dfloat &operator+=(dfloat &a, dfloat b) { return a = a + b; }
+__device__ __forceinline__ dfloat &operator-=(dfloat &a, dfloat b) { return a = a - b; }
+__device__ __forceinline__ bool operator>(dfloat a, dfloat b) { return a.hi > b.hi || (a.hi == b.hi && a.lo > b.lo); }
+// a + b for a float b (no cancellation concerns: one two-sum, the low part added, renormalised)
+__device__ __forceinline__ dfloat df_add_f(dfloat a, float b) {
+    const dfloat s = df_two_sum(a.hi, b);
+    return df_fast_two_sum(s.hi, __fadd_rn(s.lo, a.lo));
+}
+// a + b where the sum cannot cancel (both of one sign, or b much smaller): the low parts are added in float
+__device__ __forceinline__ dfloat df_add_sloppy(dfloat a, dfloat b) {
+    const dfloat s = df_two_sum(a.hi, b.hi);
+    return df_fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+// a0 - a1 + a2 - a3 rounded to float: the high parts' sums are exact (two-sum), their errors and the low parts
+// are added in float, so the result carries an error of about one float ulp of itself (not of the terms)
+__device__ __forceinline__ float df_div4(dfloat a0, dfloat a1, dfloat a2, dfloat a3) {
+    const dfloat h1 = df_two_sum(a0.hi, -a1.hi), h2 = df_two_sum(a2.hi, -a3.hi), h = df_two_sum(h1.hi, h2.hi);
+    const float lo = __fadd_rn(__fsub_rn(a0.lo, a1.lo), __fsub_rn(a2.lo, a3.lo));
+    return __fadd_rn(h.hi, __fadd_rn(__fadd_rn(__fadd_rn(h1.lo, h2.lo), h.lo), lo));
+}
+
 constexpr int kFgpTX = 32, kFgpTY = 16;
 template <int K>
 constexpr int fgp_rn() { return (kFgpTX + 2 * K) * (kFgpTY + 2 * K); }
 template <typename TD, int K>
 constexpr size_t fgp_smem() { return (size_t)6 * fgp_rn<K>() * sizeof(TD) + (size_t)3 * fgp_rn<K>() * sizeof(float); }
-// (TD, K, threads): FP32 K = 8 (1536 region pixels, 2 per thread), FP64 K = 4 (960 pixels, 2 per thread)
+// (TD, K, threads): FP32 K = 8 (1536 region pixels, 2 per thread), double-float K = 4 (960 pixels, 2 per thread)
 constexpr int kFgpKf = 8, kFgpThreadsF = 768, kFgpKd = 4, kFgpThreadsD = 480;
 constexpr int kFgpBetaTable = 256;
 
@@ -259,12 +325,22 @@ __global__ void __launch_bounds__(THREADS) k_tv_fgp(int W, int H, int niter, con
                     const int lx = i % RX, ly = i / RX;
 #pragma unroll
                     for (int c = 0; c < 3; ++c) {
-                        TD d = 0;
-                        if (fl[k] & kFx) d += q[k][c];
-                        if (fl[k] & kBx) d -= lx > 0 ? sQx[c * RN + i - 1] : TD(0);
-                        if (fl[k] & kFy) d += q[k][3 + c];
-                        if (fl[k] & kBy) d -= ly > 0 ? sQy[c * RN + i - RX] : TD(0);
-                        sU[c * RN + i] = fminf(1.0f, fmaxf(0.0f, f[k][c] + lm[k] * (float)d));
+                        float dv;
+                        if constexpr (std::is_same<TD, dfloat>::value) {
+                            const dfloat z;
+                            dv = df_div4((fl[k] & kFx) ? q[k][c] : z,
+                                         ((fl[k] & kBx) && lx > 0) ? sQx[c * RN + i - 1] : z,
+                                         (fl[k] & kFy) ? q[k][3 + c] : z,
+                                         ((fl[k] & kBy) && ly > 0) ? sQy[c * RN + i - RX] : z);
+                        } else {
+                            TD d = 0;
+                            if (fl[k] & kFx) d += q[k][c];
+                            if (fl[k] & kBx) d -= lx > 0 ? sQx[c * RN + i - 1] : TD(0);
+                            if (fl[k] & kFy) d += q[k][3 + c];
+                            if (fl[k] & kBy) d -= ly > 0 ? sQy[c * RN + i - RX] : TD(0);
+                            dv = (float)d;
+                        }
+                        sU[c * RN + i] = fminf(1.0f, fmaxf(0.0f, f[k][c] + lm[k] * dv));
                     }
                 }
                 __syncthreads();
@@ -283,13 +359,19 @@ __global__ void __launch_bounds__(THREADS) k_tv_fgp(int W, int H, int niter, con
                         const float ud = (fl[k] & kRy) ? uc[i + RX] : 0.f;
                         const float gxv = (fl[k] & kFx) ? ur - ui : 0.f;
                         const float gyv = (fl[k] & kFy) ? ud - ui : 0.f;
-                        v[c] = q[k][c] + (TD)(gxv * li[k]);
-                        v[3 + c] = q[k][3 + c] + (TD)(gyv * li[k]);
-                        n2 += v[c] * v[c] + v[3 + c] * v[3 + c];
+                        if constexpr (std::is_same<TD, dfloat>::value) {
+                            v[c] = df_add_f(q[k][c], gxv * li[k]);
+                            v[3 + c] = df_add_f(q[k][3 + c], gyv * li[k]);
+                            n2 = df_add_sloppy(df_add_sloppy(n2, v[c] * v[c]), v[3 + c] * v[3 + c]);
+                        } else {
+                            v[c] = q[k][c] + (TD)(gxv * li[k]);
+                            v[3 + c] = q[k][3 + c] + (TD)(gyv * li[k]);
+                            n2 += v[c] * v[c] + v[3 + c] * v[3 + c];
+                        }
                     }
-                    // projection onto |p| <= g without an FP64 square root or division (both are long sequences on
-                    // this GPU's narrow FP64 pipe): r = 1 / sqrt(n2) from the FP32 estimate and two FP64 Newton
-                    // steps (relative error ~1e-14), applied only where the ball constraint is active
+                    // projection onto |p| <= g without a square root or division in the extended type: r = 1 / sqrt(n2)
+                    // from the FP32 estimate and two Newton steps in TD (relative error ~1e-13 in double-float),
+                    // applied only where the ball constraint is active
                     const TD gv = (TD)gg[k];
                     TD sc = 1;
                     if (n2 > gv * gv) {
@@ -303,7 +385,8 @@ __global__ void __launch_bounds__(THREADS) k_tv_fgp(int W, int H, int niter, con
 #pragma unroll
                     for (int c = 0; c < 6; ++c) {
                         const TD pn = v[c] * sc;
-                        q[k][c] = pn + beta * (pn - p[k][c]);
+                        if constexpr (std::is_same<TD, dfloat>::value) q[k][c] = df_add_sloppy(pn, beta * (pn - p[k][c]));
+                        else q[k][c] = pn + beta * (pn - p[k][c]);
                         p[k][c] = pn;
                     }
 #pragma unroll
@@ -399,12 +482,12 @@ void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, Lau
 
 cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *lam, const float *linv, const float *g,
                           double *P0, double *P1, double *Q0, double *Q1, float *U, GridBarrier gb, cudaStream_t st,
-                          LaunchCounter &lc, bool fp64) {
-    ProfScope _ps(lc, fp64 ? "tv_fgp_fp64" : "tv_fgp", st);
-    const void *kern = fp64 ? (const void *)k_tv_fgp<double, kFgpKd, kFgpThreadsD>
+                          LaunchCounter &lc, bool extended) {
+    ProfScope _ps(lc, extended ? "tv_fgp_df" : "tv_fgp", st);
+    const void *kern = extended ? (const void *)k_tv_fgp<dfloat, kFgpKd, kFgpThreadsD>
                             : (const void *)k_tv_fgp<float, kFgpKf, kFgpThreadsF>;
-    const size_t smem = fp64 ? fgp_smem<double, kFgpKd>() : fgp_smem<float, kFgpKf>();
-    const int threads = fp64 ? kFgpThreadsD : kFgpThreadsF;
+    const size_t smem = extended ? fgp_smem<dfloat, kFgpKd>() : fgp_smem<float, kFgpKf>();
+    const int threads = extended ? kFgpThreadsD : kFgpThreadsF;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -415,8 +498,8 @@ cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *
         if (!attr_set[dev]) {
             cudaFuncSetAttribute(k_tv_fgp<float, kFgpKf, kFgpThreadsF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)fgp_smem<float, kFgpKf>());
-            cudaFuncSetAttribute(k_tv_fgp<double, kFgpKd, kFgpThreadsD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)fgp_smem<double, kFgpKd>());
+            cudaFuncSetAttribute(k_tv_fgp<dfloat, kFgpKd, kFgpThreadsD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)fgp_smem<dfloat, kFgpKd>());
             attr_set[dev] = true;
         }
     }

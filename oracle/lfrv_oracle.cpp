@@ -866,7 +866,8 @@ void color_fista_iteration(ColorState<T> &S) {
 constexpr int kTvInner = 200;
 // The dual field p and its momentum point are double in both builds: in float, their rounding (a few ulp of
 // |p| <= g) leaves lambda div p, and with it the certificate's box term, a noise floor near 4e-4 relative at 256^2.
-// The GPU keeps the same FP64 dual with FP32 iterates, so the FP32 mirror stays its like-for-like reference.
+// The GPU stores the dual in FP64 too (its arithmetic FP32 far from the floor, double-float near it) with FP32
+// iterates, so the FP32 mirror stays its like-for-like reference.
 using TvDual = double;
 constexpr double kTvDelta = 1.0;
 
