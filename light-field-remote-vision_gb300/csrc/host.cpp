@@ -1733,13 +1733,12 @@ static void warm_features(lfrv_ctx *ctx, const lfrv_config &cfg, const float *d_
     begin_timing(ctx);
     Workspace &ws = ctx->ws;
     ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
-    ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
-    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr,
-         nullptr);
+    // no dtau/dz: IBR_gradient's weights multiply it by the gradient of U = 0 (as in lfrv_render_view_dev)
+    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), nullptr, nullptr, nullptr, &G);
     ColorBuffers b = color_buffers(ctx, G);
     float *U = ws.U.as<float>();
     ctx->pending = Pending{};
-    gradient_prepare(ctx, cfg, G, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, U, b.gx, b.gy, d_input);
+    gradient_prepare(ctx, cfg, G, d_views, ws.tau.as<float>(), nullptr, nullptr, U, b.gx, b.gy, d_input);
     if (d_u0) LFRV_CUDA(cudaMemcpyAsync(d_u0, U, 3 * G.N * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
     if (d_solution) {
         cg_persistent_async(ctx, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, U);
@@ -1759,16 +1758,13 @@ static void render_view_warm(lfrv_ctx *ctx, lfrv_warmstart *net, const lfrv_conf
     begin_timing(ctx);
     Workspace &ws = ctx->ws;
     ws.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
-    ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
     ws.learn_in.ensure(G.N * kLearnChannels * 2);
     ws.seed.ensure(3 * G.N * sizeof(float));
-    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), ws.dp.as<float>(), nullptr,
-         nullptr);
+    warp(ctx, G.V, G.w, G.h, d_depth, cams, target, nullptr, nullptr, ws.tau.as<float>(), nullptr, nullptr, nullptr, &G);
     ColorBuffers b = color_buffers(ctx, G);
     float *U = ws.U.as<float>(), *X = ws.seed.as<float>();
     ctx->pending = Pending{};
-    gradient_prepare(ctx, cfg, G, d_views, ws.tau.as<float>(), ws.dp.as<float>(), nullptr, U, b.gx, b.gy,
-                     ws.learn_in.p);
+    gradient_prepare(ctx, cfg, G, d_views, ws.tau.as<float>(), nullptr, nullptr, U, b.gx, b.gy, ws.learn_in.p);
     warmstart_predict_async(net, G.H, G.W, ws.learn_in.p, U, X);
     cg_persistent_async(ctx, G.W, G.H, cfg.cg_max_iter, cfg.cg_gap_tol, b.gx, b.gy, X, U);
     LFRV_CUDA(cudaMemcpyAsync(d_out, X, 3 * G.N * sizeof(float), cudaMemcpyDeviceToDevice, ctx->stream));
@@ -1896,12 +1892,13 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         const Geometry &G = sl.G;
         Workspace &lw = l->ws;
         lw.tau.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
-        lw.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
-        warp(l, G.V, G.w, G.h, J.d_depth, J.cams, J.target, nullptr, nullptr, lw.tau.as<float>(), lw.dp.as<float>(),
-             nullptr);
+        // no dtau/dz: IBR_gradient's weights multiply it by the gradient of U = 0 (as in lfrv_render_view_dev)
+        // k_tau counts the inverse map's buckets as it writes tau (no separate count pass)
+        warp(l, G.V, G.w, G.h, J.d_depth, J.cams, J.target, nullptr, nullptr, lw.tau.as<float>(), nullptr, nullptr,
+             nullptr, &G);
         float *U = base + sl.off;
-        gradient_prepare(l, *J.cfg, G, J.d_views, lw.tau.as<float>(), lw.dp.as<float>(), nullptr, U, U + 3 * G.N,
-                         U + 4 * G.N, sl.seeded ? U + 17 * G.N + 16 : nullptr);
+        gradient_prepare(l, *J.cfg, G, J.d_views, lw.tau.as<float>(), nullptr, nullptr, U, U + 3 * G.N, U + 4 * G.N,
+                         sl.seeded ? U + 17 * G.N + 16 : nullptr);
         // keep this job's hole-fill iteration count (state slot 8) beside its CG state
         double *st = reinterpret_cast<double *>(U + 14 * G.N);
         LFRV_CUDA(cudaMemcpyAsync(st + 6, lw.state.as<double>() + 8, sizeof(double), cudaMemcpyDeviceToDevice,
