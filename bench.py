@@ -778,10 +778,19 @@ def roofline_of(prof: dict, V: int, n: int, N: int, ks: int, stats, rof_iters, t
         roof = {"bound": "hbm", "kernel": dom, "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                 "peak_source": peak_kind, "traffic": NCU_TRAFFIC_BYTES.get((dom, N)),
                 "avg_launch_us": avg_s * 1e6, "algorithmic_bytes_per_launch": abytes}
-        if dom == "cg_persistent" and roof["traffic"]:
+        if roof["traffic"]:
             roof["dram_frac"] = roof["traffic"] / avg_s / 1e9 / peak
-            roof["limiter"] = ("two grid barriers per iteration and the FP64 block sums before them; r and d stay in "
-                               "shared memory, so DRAM moves only the one-time read of g and u")
+        # what bounds the kernel instead of HBM, from its ncu capture
+        roof["limiter"] = {
+            "cg_persistent": "two grid barriers per iteration and the FP64 block sums before them; r and d stay in "
+                             "shared memory, so DRAM moves only the one-time read of g and u",
+            "zbuffer_splat": "instruction issue (75% issue active): per source pixel four projected corners, a "
+                             "two-triangle set-up and the coverage and depth of its pixel centres; DRAM traffic is "
+                             "the algorithmic bytes",
+            "gradient_setup": "latency of dependent gathers at 24% occupancy (63 register partials per lane)",
+            "rof_persistent": "block barriers between the dual and primal phases and the grid barrier per super-step; "
+                              "the working set is L2-resident",
+        }.get(dom)
     kernels_ms = {k: v[0] / targets for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
     return roof, kernels_ms
 
