@@ -218,7 +218,7 @@ __device__ __forceinline__ double block_sum(double v, double *smem /* >= NT/32 *
 // ------------------------------------------------------------------ bounded grid barrier
 // For kernels launched cooperatively (all blocks co-resident). GridBarrier (kernels.h) holds a monotonically
 // increasing arrival counter and an error flag, both zeroed before the launch. Every wait is bounded: after
-// kSpinLimit polls (about 2^22 * 64 ns, a fraction of a second) the block sets *err and returns false;
+// kSpinLimit polls (2^22 L2 round trips, a few seconds at most) the block sets *err and returns false;
 // callers then exit, and the host reports LFRV_E_TIMEOUT.
 constexpr long long kSpinLimit = 1ll << 22;
 
@@ -232,21 +232,24 @@ __device__ __forceinline__ bool grid_sync(const GridBarrier &gb, unsigned int &g
         // every block that acquires the count after it; acquire: the other blocks' writes are visible here
         const unsigned int target = generation * nblocks;
         asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(gb.count) : "memory");
+        // each poll is one L2 round trip; another block's error flag is read every 64th poll, so it does not
+        // double the time between polls
         long long spins = 0;
         while (true) {
             unsigned int seen;
             asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(gb.count) : "memory");
             if ((int)(seen - target) >= 0) break;
-            if (*((volatile int *)gb.err)) {
-                ok = false;
-                break;
+            if ((++spins & 63) == 0) {
+                if (*((volatile int *)gb.err)) {
+                    ok = false;
+                    break;
+                }
+                if (spins > kSpinLimit) {
+                    atomicExch(gb.err, 1);
+                    ok = false;
+                    break;
+                }
             }
-            if (++spins > kSpinLimit) {
-                atomicExch(gb.err, 1);
-                ok = false;
-                break;
-            }
-            __nanosleep(32);
         }
     }
     __shared__ int s_ok;

@@ -1131,28 +1131,38 @@ __global__ void k_moving(size_t N, const float *__restrict__ A, const float *__r
 // cocolib/cocolib/cuda/cuda_convolutions.cu:110-238; kernel from gsl_kernel_gauss_1xn(11, 2.0)).
 __constant__ float c_gauss[11];
 
-__global__ void k_blur_rows(int W, int H, const float *__restrict__ in, float *__restrict__ out) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W || y >= H) return;
+// Both passes stage their block's rows (columns) with the 5-pixel halo in shared memory, clamped to the image as
+// the taps are, and sum the 11 taps there in the order of the reference's loop.
+constexpr int kBlurBX = 32, kBlurBY = 8, kBlurR = 5;
+
+__global__ void __launch_bounds__(kBlurBX * kBlurBY) k_blur_rows(int W, int H, const float *__restrict__ in,
+                                                                 float *__restrict__ out) {
+    __shared__ float t[kBlurBY][kBlurBX + 2 * kBlurR];
+    const int x0 = blockIdx.x * kBlurBX, y = min((int)(blockIdx.y * kBlurBY + threadIdx.y), H - 1);
+    for (int i = threadIdx.x; i < kBlurBX + 2 * kBlurR; i += kBlurBX)
+        t[threadIdx.y][i] = __ldg(in + (size_t)y * W + min(max(x0 - kBlurR + i, 0), W - 1));
+    __syncthreads();
+    const int x = x0 + threadIdx.x, yo = blockIdx.y * kBlurBY + threadIdx.y;
+    if (x >= W || yo >= H) return;
     float s = 0.f;
 #pragma unroll
-    for (int k = -5; k <= 5; ++k) {
-        const int xx = min(max(x + k, 0), W - 1);
-        s += in[(size_t)y * W + xx] * c_gauss[5 - k];
-    }
-    out[(size_t)y * W + x] = s;
+    for (int k = -kBlurR; k <= kBlurR; ++k) s += t[threadIdx.y][threadIdx.x + kBlurR + k] * c_gauss[5 - k];
+    out[(size_t)yo * W + x] = s;
 }
 
-__global__ void k_blur_cols(int W, int H, const float *__restrict__ in, float *__restrict__ out) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
-    if (x >= W || y >= H) return;
+__global__ void __launch_bounds__(kBlurBX * kBlurBY) k_blur_cols(int W, int H, const float *__restrict__ in,
+                                                                 float *__restrict__ out) {
+    __shared__ float t[kBlurBY + 2 * kBlurR][kBlurBX];
+    const int x = min((int)(blockIdx.x * kBlurBX + threadIdx.x), W - 1), y0 = blockIdx.y * kBlurBY;
+    for (int i = threadIdx.y; i < kBlurBY + 2 * kBlurR; i += kBlurBY)
+        t[i][threadIdx.x] = __ldg(in + (size_t)min(max(y0 - kBlurR + i, 0), H - 1) * W + x);
+    __syncthreads();
+    const int xo = blockIdx.x * kBlurBX + threadIdx.x, y = y0 + threadIdx.y;
+    if (xo >= W || y >= H) return;
     float s = 0.f;
 #pragma unroll
-    for (int k = -5; k <= 5; ++k) {
-        const int yy = min(max(y + k, 0), H - 1);
-        s += in[(size_t)yy * W + x] * c_gauss[5 - k];
-    }
-    out[(size_t)y * W + x] = s;
+    for (int k = -kBlurR; k <= kBlurR; ++k) s += t[threadIdx.y + kBlurR + k][threadIdx.x] * c_gauss[5 - k];
+    out[(size_t)y * W + xo] = s;
 }
 
 // Deterministic final reduction of FP64 partials (single block).
@@ -1664,8 +1674,9 @@ void set_gaussian(const float k[11]) { cudaMemcpyToSymbol(c_gauss, k, sizeof(flo
 
 void launch_blur(int W, int H, const float *in, float *tmp, float *out, cudaStream_t st, LaunchCounter &lc) {
     ProfScope _ps(lc, "blur", st);
-    k_blur_rows<<<grid2(W, H, kTile), kTile, 0, st>>>(W, H, in, tmp);
-    k_blur_cols<<<grid2(W, H, kTile), kTile, 0, st>>>(W, H, tmp, out);
+    const dim3 b(kBlurBX, kBlurBY);
+    k_blur_rows<<<grid2(W, H, b), b, 0, st>>>(W, H, in, tmp);
+    k_blur_cols<<<grid2(W, H, b), b, 0, st>>>(W, H, tmp, out);
     lc.add(2);
 }
 
