@@ -464,6 +464,12 @@ int lfrv_scene_params_preset(int which, lfrv_scene_params *p);
  * gt 3*H*W floats. Any output pointer may be NULL. */
 int lfrv_synth_scene(const lfrv_scene_params *p, float *views, float *depth, lfrv_camera *cams,
                      float *gt);
+/* The same scene generated on the GPU into DEVICE buffers (context stream; returns when they are written), with
+ * host cameras. It runs the same tracing code in double precision; the device's exp, log and cos may differ from
+ * the host library's in the last bit, so views and depth maps equal lfrv_synth_scene's to the rounding of the final
+ * float in all but rare pixels. For generating many scenes (training sets) at GPU speed. */
+int lfrv_synth_scene_dev(lfrv_ctx *ctx, const lfrv_scene_params *p, float *d_views, float *d_depth,
+                         lfrv_camera *cams, float *d_gt);
 
 /* PSNR with peak 1.0 over all channels, excluding a border of `border` pixels
  * (gsl_image_psnr, cocolib/cocolib/common/gsl_image.cpp:991-1025 uses border 2). */

@@ -32,7 +32,7 @@ ORACLE_LIB = ROOT / "oracle" / "liblfrv_oracle.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_COMMON = ["-std=c++17", "-O3", "-lineinfo", f"-I{INCLUDE}", f"-I{CSRC}",
                "-Xcompiler", "-fPIC,-ffp-contract=off,-fopenmp"]
-LIB_SOURCES = ["errors.cpp", "io.cpp", "png.cpp", "synth.cpp", "host.cpp", "learn.cpp",
+LIB_SOURCES = ["errors.cpp", "io.cpp", "png.cpp", "synth.cu", "host.cpp", "learn.cpp",
                "kernels_solver.cu", "kernels_tv.cu", "kernels_warp.cu", "kernels_pushpull.cu", "kernels_cg.cu", "kernels_learn.cu"]
 
 
@@ -83,6 +83,8 @@ def build_library(force: bool = False, verbose: bool = False) -> Path:
             extra = ["-Xptxas", "-v"] if (verbose and s.suffix == ".cu") else []
             if zlib and s.name == "png.cpp":
                 extra.append("-DLFRV_HAVE_ZLIB")
+            if s.name == "synth.cu":
+                extra.append("--fmad=false")  # the scene generator's device code rounds as its host code
             jobs.append([nvcc, *ARCH, *NVCC_COMMON, *extra, "-c", str(s), "-o", str(o)])
     if jobs:
         with cf.ThreadPoolExecutor(max_workers=min(len(jobs), os.cpu_count() or 4)) as ex:

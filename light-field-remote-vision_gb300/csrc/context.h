@@ -57,6 +57,8 @@ struct Workspace {
     DevBuf hb_in, hb_out;
     // corrected IBR_color: iterates, data gradients and metric (15 N floats), the FP64 dual / momentum fields (24 N)
     DevBuf tv;
+    // the device scene generator's planes and bumps
+    DevBuf scene;
 };
 
 // Per-kernel CUDA-event timing: a fixed pool of event pairs recorded in-stream. When the pool is full the

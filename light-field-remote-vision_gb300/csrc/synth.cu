@@ -7,8 +7,12 @@
 // analytic dz/dx, dz/dy (the (z, dz/dx, dz/dy) texture that depthSplatting.vert and tauWarp.frag read),
 // inputs rendered at ss x resolution and box-decimated, and additive Gaussian sensor noise.
 //
-// Host-only, OpenMP over rows; the arithmetic is plain IEEE double with a portable polynomial sine so
-// that x86-64 and aarch64 hosts produce the same scenes (the library is built with -ffp-contract=off).
+// The host form runs OpenMP over rows; the device form (lfrv_synth_scene_dev) runs the same tracing code, one
+// thread per pixel. The arithmetic is plain IEEE double with a portable polynomial sine so that x86-64 and
+// aarch64 hosts produce the same scenes (host code built with -ffp-contract=off, device code with -fmad=false);
+// the device's double exp, log and cos may differ from the host library's in the last bit, so the two forms
+// agree to the rounding of the final float in all but rare pixels.
+#include "context.h"
 #include "lfrv.h"
 #include "lfrv_internal.h"
 
@@ -17,19 +21,21 @@
 #include <cstring>
 #include <vector>
 
+#define LFRV_HD __host__ __device__ __forceinline__
+
 namespace {
 
 // ------------------------------------------------------------------ Philox4x32-10 (Salmon et al. 2011)
 struct Philox {
-    static inline void round(uint32_t ctr[4], const uint32_t key[2]) {
+    static LFRV_HD void round(uint32_t ctr[4], const uint32_t key[2]) {
         const uint64_t p0 = (uint64_t)0xD2511F53u * ctr[0];
         const uint64_t p1 = (uint64_t)0xCD9E8D57u * ctr[2];
         const uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
         const uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
         uint32_t out[4] = {hi1 ^ ctr[1] ^ key[0], lo1, hi0 ^ ctr[3] ^ key[1], lo0};
-        std::memcpy(ctr, out, sizeof(out));
+        for (int i = 0; i < 4; ++i) ctr[i] = out[i];
     }
-    static void gen(uint64_t seed, uint64_t c0, uint64_t c1, uint32_t out[4]) {
+    static LFRV_HD void gen(uint64_t seed, uint64_t c0, uint64_t c1, uint32_t out[4]) {
         uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
         uint32_t ctr[4] = {(uint32_t)c0, (uint32_t)(c0 >> 32), (uint32_t)c1, (uint32_t)(c1 >> 32)};
         for (int r = 0; r < 10; ++r) {
@@ -37,11 +43,11 @@ struct Philox {
             key[0] += 0x9E3779B9u;
             key[1] += 0xBB67AE85u;
         }
-        std::memcpy(out, ctr, sizeof(ctr));
+        for (int i = 0; i < 4; ++i) out[i] = ctr[i];
     }
 };
 
-inline double u01(uint32_t a, uint32_t b) {  // 53-bit uniform in (0,1)
+LFRV_HD double u01(uint32_t a, uint32_t b) {  // 53-bit uniform in (0,1)
     const uint64_t v = ((uint64_t)a << 21) ^ (uint64_t)b;
     return ((double)(v & ((1ull << 53) - 1)) + 0.5) * (1.0 / 9007199254740992.0);
 }
@@ -59,10 +65,10 @@ struct Stream {
 };
 
 // Portable sine: reduction to [-pi/2, pi/2] and a degree-19 Taylor polynomial (error < 3e-14).
-inline double psin(double x) {
+LFRV_HD double psin(double x) {
     const double twopi = 6.283185307179586476925286766559;
     const double pi = 3.1415926535897932384626433832795;
-    x -= twopi * std::nearbyint(x / twopi);
+    x -= twopi * nearbyint(x / twopi);
     if (x > 0.5 * pi) x = pi - x;
     else if (x < -0.5 * pi) x = -pi - x;
     const double x2 = x * x;
@@ -97,6 +103,17 @@ struct Scene {
     std::vector<Plane> planes;  // ascending depth
     std::vector<Bump> bumps;
 };
+
+// What the tracer reads: the planes and bumps as arrays (host vectors, or a copy in device memory).
+struct SceneView {
+    const Plane *planes;
+    int nplanes;
+    const Bump *bumps;
+    int nbumps;
+};
+inline SceneView view_of(const Scene &s) {
+    return SceneView{s.planes.data(), (int)s.planes.size(), s.bumps.data(), (int)s.bumps.size()};
+}
 
 struct Hit {
     double z, zx, zy;  // depth and derivatives wrt the rendering camera's pixel coordinates
@@ -151,15 +168,16 @@ Scene make_scene(const lfrv_scene_params &p, double world_width_per_depth) {
 }
 
 // Height field of plane k: depth(X,Y) and its gradient.
-inline void height(const Scene &s, int k, double X, double Y, double &h, double &hX, double &hY) {
+LFRV_HD void height(const SceneView &s, int k, double X, double Y, double &h, double &hX, double &hY) {
     h = s.planes[k].depth;
     hX = hY = 0.0;
-    for (const Bump &b : s.bumps) {
+    for (int i = 0; i < s.nbumps; ++i) {
+        const Bump &b = s.bumps[i];
         if (b.plane != k) continue;
         const double dx = X - b.X, dy = Y - b.Y;
         const double r2 = (dx * dx + dy * dy) / (b.sig * b.sig);
         if (r2 > 64.0) continue;
-        const double e = b.amp * std::exp(-0.5 * r2);
+        const double e = b.amp * exp(-0.5 * r2);
         h += e;
         hX -= e * dx / (b.sig * b.sig);
         hY -= e * dy / (b.sig * b.sig);
@@ -168,10 +186,10 @@ inline void height(const Scene &s, int k, double X, double Y, double &h, double 
 
 // Nearest surface hit of the ray through pixel-space point (px,py) of a camera at centre (Cx,Cy,0)
 // with focal f and principal point (cx,cy), R = I.
-bool trace(const Scene &s, double Cx, double Cy, double f, double cx, double cy, double px, double py,
-           bool want_colour, Hit &hit) {
+LFRV_HD bool trace(const SceneView &s, double Cx, double Cy, double f, double cx, double cy, double px, double py,
+                   bool want_colour, Hit &hit) {
     const double u = (px - cx) / f, v = (py - cy) / f;
-    for (int k = 0; k < (int)s.planes.size(); ++k) {
+    for (int k = 0; k < s.nplanes; ++k) {
         const Plane &pl = s.planes[k];
         double Z = pl.depth, h, hX, hY;
         // Newton on g(Z) = Z - h(Cx + Z u, Cy + Z v)
@@ -179,10 +197,10 @@ bool trace(const Scene &s, double Cx, double Cy, double f, double cx, double cy,
             height(s, k, Cx + Z * u, Cy + Z * v, h, hX, hY);
             const double g = Z - h;
             double gp = 1.0 - (hX * u + hY * v);
-            if (std::fabs(gp) < 0.2) gp = gp < 0 ? -0.2 : 0.2;
+            if (fabs(gp) < 0.2) gp = gp < 0 ? -0.2 : 0.2;
             const double step = g / gp;
             Z -= step;
-            if (std::fabs(step) < 1e-13) break;
+            if (fabs(step) < 1e-13) break;
         }
         height(s, k, Cx + Z * u, Cy + Z * v, h, hX, hY);
         const double X = Cx + Z * u, Y = Cy + Z * v;
@@ -203,11 +221,83 @@ bool trace(const Scene &s, double Cx, double Cy, double f, double cx, double cy,
     return false;
 }
 
-inline double gauss(uint64_t seed, uint64_t view, uint64_t idx) {
+LFRV_HD double gauss(uint64_t seed, uint64_t view, uint64_t idx) {
     uint32_t o[4];
     Philox::gen(seed ^ 0xA5A5A5A5DEADBEEFull, view, idx, o);
     const double u1 = u01(o[0], o[1]), u2 = u01(o[2], o[3]);
-    return std::sqrt(-2.0 * std::log(u1)) * std::cos(6.283185307179586 * u2);
+    return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+// One input pixel of a view: the ss x ss samples' colours averaged, plus noise (as lfrv_synth_scene's loop).
+LFRV_HD void view_pixel(const SceneView &s, const lfrv_scene_params &p, int v, double Cx, double Cy, double fr,
+                        double cxr, double cyr, int x, int y, int w, size_t plane_in, float *out) {
+    const int ss = p.ss;
+    Hit hit;
+    double acc[3] = {0, 0, 0};
+    for (int sy = 0; sy < ss; ++sy)
+        for (int sx = 0; sx < ss; ++sx) {
+            const double px = x * ss + sx + 0.5, py = y * ss + sy + 0.5;
+            if (trace(s, Cx, Cy, fr, cxr, cyr, px, py, true, hit))
+                for (int ch = 0; ch < 3; ++ch) acc[ch] += hit.col[ch];
+        }
+    const size_t o = (size_t)y * w + x;
+    for (int ch = 0; ch < 3; ++ch) {
+        double val = acc[ch] / (ss * ss);
+        if (p.noise_sigma > 0) val += p.noise_sigma * gauss(p.seed, (uint64_t)v, (uint64_t)(ch * plane_in + o));
+        out[ch * plane_in + o] = (float)val;
+    }
+}
+
+// One input pixel's depth map entry (z, dz/dx, dz/dy), or INVALID_DEPTH where the ray hits nothing
+// (sources/openGL/frameBuffer.h:13).
+LFRV_HD void depth_pixel(const SceneView &s, double Cx, double Cy, double f, int x, int y, int w, int h,
+                         size_t plane_in, float *out) {
+    Hit hit;
+    const size_t o = (size_t)y * w + x;
+    if (trace(s, Cx, Cy, f, 0.5 * w, 0.5 * h, x + 0.5, y + 0.5, false, hit)) {
+        out[o] = (float)hit.z;
+        out[plane_in + o] = (float)hit.zx;
+        out[2 * plane_in + o] = (float)hit.zy;
+    } else {
+        out[o] = 1000.0f;
+        out[plane_in + o] = 0.0f;
+        out[2 * plane_in + o] = 0.0f;
+    }
+}
+
+LFRV_HD void gt_pixel(const SceneView &s, double f, int x, int y, int W, int H, float *gt) {
+    Hit hit;
+    const size_t o = (size_t)y * W + x, plane_out = (size_t)W * H;
+    const bool ok = trace(s, 0.0, 0.0, f, 0.5 * W, 0.5 * H, x + 0.5, y + 0.5, true, hit);
+    for (int ch = 0; ch < 3; ++ch) gt[ch * plane_out + o] = ok ? (float)hit.col[ch] : 0.0f;
+}
+
+// ------------------------------------------------------------------ device form
+// Camera centres of the input views (views in lfrv_synth_scene's order), passed by value.
+struct SynthCentres {
+    double C[2 * 255];
+};
+
+__global__ void k_synth_views(SceneView s, lfrv_scene_params p, SynthCentres cs, double fr, double cxr, double cyr,
+                              float *views) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y, v = blockIdx.z;
+    if (x >= p.w || y >= p.h) return;
+    const size_t plane_in = (size_t)p.w * p.h;
+    view_pixel(s, p, v, cs.C[2 * v], cs.C[2 * v + 1], fr, cxr, cyr, x, y, p.w, plane_in,
+               views + (size_t)v * 3 * plane_in);
+}
+
+__global__ void k_synth_depth(SceneView s, lfrv_scene_params p, SynthCentres cs, double f, float *depth) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y, v = blockIdx.z;
+    if (x >= p.w || y >= p.h) return;
+    const size_t plane_in = (size_t)p.w * p.h;
+    depth_pixel(s, cs.C[2 * v], cs.C[2 * v + 1], f, x, y, p.w, p.h, plane_in, depth + (size_t)v * 3 * plane_in);
+}
+
+__global__ void k_synth_gt(SceneView s, double f, int W, int H, float *gt) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= W || y >= H) return;
+    gt_pixel(s, f, x, y, W, H, gt);
 }
 
 void camera(lfrv_camera &c, double f, int W, int H, double Cx, double Cy) {
@@ -274,6 +364,7 @@ extern "C" int lfrv_synth_scene(const lfrv_scene_params *p, float *views, float 
     const double f_input = f_target / p->dsf;
     const double world_width_per_depth = (double)W / f_target;
     const Scene scene = make_scene(*p, world_width_per_depth);
+    const SceneView sv = view_of(scene);
     const size_t plane_in = (size_t)w * h;
 
     int v = 0;
@@ -287,61 +378,73 @@ extern "C" int lfrv_synth_scene(const lfrv_scene_params *p, float *views, float 
             const double fr = f_input * ss, cxr = 0.5 * w * ss, cyr = 0.5 * h * ss;
             float *out = views + (size_t)v * 3 * plane_in;
 #pragma omp parallel for schedule(dynamic, 4)
-            for (int y = 0; y < h; ++y) {
-                Hit hit;
-                for (int x = 0; x < w; ++x) {
-                    double acc[3] = {0, 0, 0};
-                    for (int sy = 0; sy < ss; ++sy)
-                        for (int sx = 0; sx < ss; ++sx) {
-                            const double px = x * ss + sx + 0.5, py = y * ss + sy + 0.5;
-                            if (trace(scene, Cx, Cy, fr, cxr, cyr, px, py, true, hit))
-                                for (int ch = 0; ch < 3; ++ch) acc[ch] += hit.col[ch];
-                        }
-                    const size_t o = (size_t)y * w + x;
-                    for (int ch = 0; ch < 3; ++ch) {
-                        double val = acc[ch] / (ss * ss);
-                        if (p->noise_sigma > 0)
-                            val += p->noise_sigma * gauss(p->seed, (uint64_t)v, (uint64_t)(ch * plane_in + o));
-                        out[ch * plane_in + o] = (float)val;
-                    }
-                }
-            }
+            for (int y = 0; y < h; ++y)
+                for (int x = 0; x < w; ++x) view_pixel(sv, *p, v, Cx, Cy, fr, cxr, cyr, x, y, w, plane_in, out);
         }
         if (depth) {
             float *out = depth + (size_t)v * 3 * plane_in;
 #pragma omp parallel for schedule(dynamic, 4)
-            for (int y = 0; y < h; ++y) {
-                Hit hit;
-                for (int x = 0; x < w; ++x) {
-                    const size_t o = (size_t)y * w + x;
-                    if (trace(scene, Cx, Cy, f_input, 0.5 * w, 0.5 * h, x + 0.5, y + 0.5, false, hit)) {
-                        out[o] = (float)hit.z;
-                        out[plane_in + o] = (float)hit.zx;
-                        out[2 * plane_in + o] = (float)hit.zy;
-                    } else {
-                        out[o] = 1000.0f;  // INVALID_DEPTH (sources/openGL/frameBuffer.h:13)
-                        out[plane_in + o] = 0.0f;
-                        out[2 * plane_in + o] = 0.0f;
-                    }
-                }
-            }
+            for (int y = 0; y < h; ++y)
+                for (int x = 0; x < w; ++x) depth_pixel(sv, Cx, Cy, f_input, x, y, w, h, plane_in, out);
         }
         ++v;
     }
     if (cams) camera(cams[v], f_target, W, H, 0.0, 0.0);
     if (gt) {
-        const size_t plane_out = (size_t)W * H;
 #pragma omp parallel for schedule(dynamic, 4)
-        for (int y = 0; y < H; ++y) {
-            Hit hit;
-            for (int x = 0; x < W; ++x) {
-                const size_t o = (size_t)y * W + x;
-                const bool ok = trace(scene, 0.0, 0.0, f_target, 0.5 * W, 0.5 * H, x + 0.5, y + 0.5, true, hit);
-                for (int ch = 0; ch < 3; ++ch) gt[ch * plane_out + o] = ok ? (float)hit.col[ch] : 0.0f;
-            }
-        }
+        for (int y = 0; y < H; ++y)
+            for (int x = 0; x < W; ++x) gt_pixel(sv, f_target, x, y, W, H, gt);
     }
     return LFRV_OK;
+}
+
+extern "C" int lfrv_synth_scene_dev(lfrv_ctx *ctx, const lfrv_scene_params *p, float *d_views, float *d_depth,
+                                    lfrv_camera *cams, float *d_gt) {
+    LFRV_API_BEGIN
+    if (!ctx) return lfrv::fail(LFRV_E_ARG, "null context");
+    LFRV_CUDA(cudaSetDevice(ctx->device));
+    if (!p || p->grid < 2 || p->w <= 0 || p->h <= 0 || p->ss < 1 || p->dsf < 1 || p->nplanes < 1 ||
+        p->nplanes > 16 || p->grid * p->grid - 1 > 255 || p->nbumps < 0)
+        lfrv::raise(LFRV_E_ARG, "bad scene parameters");
+    const int n = p->grid, w = p->w, h = p->h, W = w * p->dsf, H = h * p->dsf;
+    const int center = (n / 2) * n + (n / 2);
+    const double c = 0.5 * (n - 1);
+    const double f_target = p->focal_per_256 * (double)W / 256.0;
+    const double f_input = f_target / p->dsf;
+    const Scene scene = make_scene(*p, (double)W / f_target);
+    // the planes and bumps in device memory (the context's scene buffer)
+    const size_t pb = sizeof(Plane) * scene.planes.size(), bb = sizeof(Bump) * scene.bumps.size();
+    lfrv::Workspace &ws = ctx->ws;
+    ws.scene.ensure(pb + bb + 16);
+    char *dscene = ws.scene.as<char>();
+    LFRV_CUDA(cudaMemcpyAsync(dscene, scene.planes.data(), pb, cudaMemcpyHostToDevice, ctx->stream));
+    if (bb) LFRV_CUDA(cudaMemcpyAsync(dscene + pb, scene.bumps.data(), bb, cudaMemcpyHostToDevice, ctx->stream));
+    const SceneView sv{reinterpret_cast<const Plane *>(dscene), (int)scene.planes.size(),
+                       reinterpret_cast<const Bump *>(dscene + pb), (int)scene.bumps.size()};
+    SynthCentres cs;
+    std::memset(&cs, 0, sizeof(cs));
+    int v = 0;
+    for (int s = 0; s < n * n; ++s) {
+        if (s == center) continue;
+        const double Cx = p->baseline * (s % n - c), Cy = p->baseline * (s / n - c);
+        cs.C[2 * v] = Cx;
+        cs.C[2 * v + 1] = Cy;
+        if (cams) camera(cams[v], f_input, w, h, Cx, Cy);
+        ++v;
+    }
+    if (cams) camera(cams[v], f_target, W, H, 0.0, 0.0);
+    const dim3 b(16, 8);
+    const dim3 gi((w + 15) / 16, (h + 7) / 8, v);
+    if (d_views)
+        k_synth_views<<<gi, b, 0, ctx->stream>>>(sv, *p, cs, f_input * p->ss, 0.5 * w * p->ss, 0.5 * h * p->ss,
+                                                 d_views);
+    if (d_depth) k_synth_depth<<<gi, b, 0, ctx->stream>>>(sv, *p, cs, f_input, d_depth);
+    if (d_gt) k_synth_gt<<<dim3((W + 15) / 16, (H + 7) / 8), b, 0, ctx->stream>>>(sv, f_target, W, H, d_gt);
+    ctx->launches.add((d_views ? 1 : 0) + (d_depth ? 1 : 0) + (d_gt ? 1 : 0));
+    LFRV_CUDA(cudaGetLastError());
+    // the scene buffer is reused by the next call: the host's copies above must be done with their sources
+    LFRV_CUDA(cudaStreamSynchronize(ctx->stream));
+    LFRV_API_END
 }
 
 extern "C" double lfrv_psnr(int W, int H, const float *a, const float *b, int border) {

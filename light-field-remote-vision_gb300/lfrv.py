@@ -125,7 +125,7 @@ EXPORTED = [
     "lfrv_stage_initial_image", "lfrv_stage_push_pull", "lfrv_stage_gradient_visibility", "lfrv_stage_hole_fill",
     "lfrv_stage_u_gradient", "lfrv_stage_cg", "lfrv_stage_poisson_jacobi", "lfrv_cg_solve_static", "lfrv_pfm_read", "lfrv_pfm_write", "lfrv_png_read", "lfrv_png_write",
     "lfrv_scene_params_preset",
-    "lfrv_synth_scene", "lfrv_psnr",
+    "lfrv_synth_scene", "lfrv_synth_scene_dev", "lfrv_psnr",
 ]
 
 
@@ -409,6 +409,15 @@ class Context:
                                         cameras_array(cams), C.byref(target), C.c_void_p(d_out), C.byref(st)))
         return st
 
+    def synth_scene_dev(self, p: SceneParams, d_views: int = 0, d_depth: int = 0, d_gt: int = 0):
+        """The scene of `p` generated on the GPU into device buffers (views and depth V x 3 x h x w, gt 3 x H x W;
+        0 skips one); returns (input cameras, target camera)."""
+        V = p.grid * p.grid - 1
+        cams = (Camera * (V + 1))()
+        _check(LIB.lfrv_synth_scene_dev(self._h, C.byref(p), C.c_void_p(d_views or None), C.c_void_p(d_depth or None),
+                                        cams, C.c_void_p(d_gt or None)))
+        return [cams[i] for i in range(V)], cams[V]
+
     def render_video_dev(self, cfg: Config, algorithm: int, d_views: int, d_depth: int, cams, cam_a: int, cam_b: int,
                          target: Camera, first_frame: int, nframes: int, d_out: int) -> list:
         """IBR_video frames first_frame .. first_frame + nframes - 1 as one batch; d_out: nframes x 3 x H x W."""
@@ -671,6 +680,7 @@ def _declare() -> None:
     LIB.lfrv_stage_push_pull.argtypes = [vp, C.c_int, C.c_int, C.c_int, _U8, _F]
     LIB.lfrv_stage_hole_fill.argtypes = [vp, C.c_int, C.c_int, C.c_int, _U8, _F, _I]
     LIB.lfrv_synth_scene.argtypes = [C.POINTER(SceneParams), _F, _F, C.POINTER(Camera), _F]
+    LIB.lfrv_synth_scene_dev.argtypes = [vp, C.POINTER(SceneParams), vp, vp, C.POINTER(Camera), vp]
     LIB.lfrv_scene_params_preset.argtypes = [C.c_int, C.POINTER(SceneParams)]
     LIB.lfrv_config_get_string.argtypes = [C.c_char_p, C.c_char_p, C.c_size_t]
     LIB.lfrv_pfm_read.argtypes = [C.c_char_p, _I, _I, _I, _F, C.c_size_t]
