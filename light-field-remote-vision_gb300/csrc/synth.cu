@@ -9,9 +9,10 @@
 //
 // The host form runs OpenMP over rows; the device form (lfrv_synth_scene_dev) runs the same tracing code, one
 // thread per pixel. The arithmetic is plain IEEE double with a portable polynomial sine so that x86-64 and
-// aarch64 hosts produce the same scenes (host code built with -ffp-contract=off, device code with -fmad=false);
-// the device's double exp, log and cos may differ from the host library's in the last bit, so the two forms
-// agree to the rounding of the final float in all but rare pixels.
+// aarch64 hosts produce the same scenes (host code built with -ffp-contract=off, device code with -fmad=false).
+// The device form multiplies by reciprocals where the host form divides (sine reduction, bump falloff), and its
+// double exp, log and cos may differ from the host library's in the last bit, so the two forms agree to the
+// rounding of the final float in all but rare pixels.
 #include "context.h"
 #include "lfrv.h"
 #include "lfrv_internal.h"
@@ -68,7 +69,11 @@ struct Stream {
 LFRV_HD double psin(double x) {
     const double twopi = 6.283185307179586476925286766559;
     const double pi = 3.1415926535897932384626433832795;
+#ifdef __CUDA_ARCH__
+    x -= twopi * nearbyint(x * (1.0 / twopi));  // a multiple of 2 pi off only at a half-period, where it is harmless
+#else
     x -= twopi * nearbyint(x / twopi);
+#endif
     if (x > 0.5 * pi) x = pi - x;
     else if (x < -0.5 * pi) x = -pi - x;
     const double x2 = x * x;
@@ -97,6 +102,7 @@ struct Plane {
 struct Bump {
     int plane;
     double X, Y, amp, sig;
+    double inv_s2;  // 1 / sig^2 (the device form multiplies by it where the host form divides)
 };
 
 struct Scene {
@@ -162,6 +168,7 @@ Scene make_scene(const lfrv_scene_params &p, double world_width_per_depth) {
         b.amp = (rng.uniform() < 0.5 ? -1.0 : 1.0) * p.bump_amp;
         // sigma in target pixels -> world units at the plane's depth
         b.sig = p.bump_sigma_px * world_width_per_depth * pl.depth / (double)(p.w * p.dsf);
+        b.inv_s2 = 1.0 / (b.sig * b.sig);
         s.bumps.push_back(b);
     }
     return s;
@@ -175,12 +182,22 @@ LFRV_HD void height(const SceneView &s, int k, double X, double Y, double &h, do
         const Bump &b = s.bumps[i];
         if (b.plane != k) continue;
         const double dx = X - b.X, dy = Y - b.Y;
+#ifdef __CUDA_ARCH__
+        // FP64 division is a long sequence on this GPU's narrow FP64 pipe: multiply by the reciprocal
+        const double r2 = (dx * dx + dy * dy) * b.inv_s2;
+        if (r2 > 64.0) continue;
+        const double e = b.amp * exp(-0.5 * r2);
+        h += e;
+        hX -= e * dx * b.inv_s2;
+        hY -= e * dy * b.inv_s2;
+#else
         const double r2 = (dx * dx + dy * dy) / (b.sig * b.sig);
         if (r2 > 64.0) continue;
         const double e = b.amp * exp(-0.5 * r2);
         h += e;
         hX -= e * dx / (b.sig * b.sig);
         hY -= e * dy / (b.sig * b.sig);
+#endif
     }
 }
 
