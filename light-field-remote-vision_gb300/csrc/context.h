@@ -130,6 +130,7 @@ struct lfrv_ctx {
     cudaEvent_t side_fork = nullptr, side_join = nullptr;
     lfrv::Pending pending;
     std::map<long long, int> rof_tuned;  // autotuned persistent-ROF variant per image size (W << 32 | H)
+    std::map<long long, int> fgp_tuned;  // autotuned FGP variant per image size and arithmetic
     lfrv::KernelProfiler prof;
     bool profiling = false;
     int device = 0;

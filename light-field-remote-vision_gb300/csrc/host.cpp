@@ -390,6 +390,48 @@ static int rof_autotune(lfrv_ctx *c, int W, int H, float tau, float sigma, float
     return best;
 }
 
+// The FGP's counterpart of rof_autotune: every instantiation of the arithmetic in use, timed on scratch copies of
+// the dual (16 iterations) on first use per image size; the fastest is cached. All give the same iterates.
+static int fgp_autotune(lfrv_ctx *c, int W, int H, bool extended, const float *F, const float *lam, const float *linv,
+                        const float *g, const double *P) {
+    const long long key = ((long long)W << 33) | ((long long)H << 1) | (extended ? 1 : 0);
+    auto it = c->fgp_tuned.find(key);
+    if (it != c->fgp_tuned.end()) return it->second;
+    const size_t N = (size_t)W * H;
+    c->ws.tune.ensure(sizeof(double) * 24 * N + sizeof(float) * 3 * N);
+    double *P0 = c->ws.tune.as<double>(), *P1 = P0 + 6 * N, *Q0 = P1 + 6 * N, *Q1 = Q0 + 6 * N;
+    float *U = reinterpret_cast<float *>(Q1 + 6 * N);
+    cudaStream_t s = c->stream;
+    cudaEvent_t e0, e1;
+    LFRV_CUDA(cudaEventCreate(&e0));
+    LFRV_CUDA(cudaEventCreate(&e1));
+    int best = tv_fgp_default_variant(extended);
+    float best_ms = 1e30f;
+    LaunchCounter quiet;  // trial launches are not the caller's kernels
+    for (int v = 0; v < tv_fgp_variant_count(extended); ++v) {
+        LFRV_CUDA(cudaMemcpyAsync(P0, P, sizeof(double) * 6 * N, cudaMemcpyDeviceToDevice, s));
+        const GridBarrier gb = fresh_barrier(c);
+        LFRV_CUDA(cudaEventRecord(e0, s));
+        const cudaError_t e = launch_tv_fgp(W, H, 16, F, lam, linv, g, P0, P1, Q0, Q1, U, gb, s, quiet, extended, v);
+        LFRV_CUDA(cudaEventRecord(e1, s));
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            continue;  // a variant that cannot launch here (occupancy) is skipped
+        }
+        LFRV_CUDA(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        LFRV_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+        if (ms < best_ms) {
+            best_ms = ms;
+            best = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->fgp_tuned[key] = best;
+    return best;
+}
+
 // ------------------------------------------------------------------ gradient data term (dt_beta)
 // Buffers of the gradient data term (vtv_sr_dataterm_gradients, sources/optimization.cu:1969-2116) and of the
 // gradient term of the energy (:1610-1700); empty when dt_beta == 0.
@@ -535,12 +577,13 @@ struct TvSolve {
         check_launch("tv step");
         std::swap(u, up);
         std::swap(gf, gfp);
-        const GridBarrier gb = fresh_barrier(c);
         // FP32 dual arithmetic while the gap is far above FP32's floor, double-float once it nears it (the switch
         // only changes rounding, not the iteration)
         extended = extended || gap < kTvExtendedBelow;
+        const int variant = fgp_autotune(c, G.W, G.H, extended, b.F, lam, linv, b.g, P0);
+        const GridBarrier gb = fresh_barrier(c);  // after the autotuner's trial launches, which use the barrier too
         LFRV_CUDA(launch_tv_fgp(G.W, G.H, kTvInnerIterations, b.F, lam, linv, b.g, P0, P1, Q0, Q1, u, gb, s,
-                                c->launches, extended));
+                                c->launches, extended, variant));
         ++k;
     }
     // the solution back into ws.U

@@ -202,9 +202,13 @@ void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, Lau
 // dual (6 FP64 planes: x parts of the 3 channels, then the y parts) and receives the final one; P1, Q0, Q1 are
 // scratch (6 FP64 planes each); U receives clamp(F + lam div p, 0, 1). extended: the dual's arithmetic in
 // double-float (about 44 bits; else FP32), with the same FP64 storage.
+// variant: the instantiation (iterations per super-step, block size) the autotuner picked; all give the same
+// iterates (tv_fgp_variant_count per arithmetic; out of range: the default).
 cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *lam, const float *linv, const float *g,
                           double *P0, double *P1, double *Q0, double *Q1, float *U, GridBarrier gb, cudaStream_t st,
-                          LaunchCounter &lc, bool extended);
+                          LaunchCounter &lc, bool extended, int variant = -1);
+int tv_fgp_variant_count(bool extended);
+int tv_fgp_default_variant(bool extended);
 // The gap above which the FGP runs in FP32 (its certificate floor is near 4e-4): double-float takes over below it.
 constexpr double kTvExtendedBelow = 2e-3;
 

@@ -214,8 +214,6 @@ template <int K>
 constexpr int fgp_rn() { return (kFgpTX + 2 * K) * (kFgpTY + 2 * K); }
 template <typename TD, int K>
 constexpr size_t fgp_smem() { return (size_t)6 * fgp_rn<K>() * sizeof(TD) + (size_t)3 * fgp_rn<K>() * sizeof(float); }
-// (TD, K, threads): FP32 K = 8 (1536 region pixels, 2 per thread), double-float K = 4 (960 pixels, 2 per thread)
-constexpr int kFgpKf = 8, kFgpThreadsF = 768, kFgpKd = 4, kFgpThreadsD = 480;
 constexpr int kFgpBetaTable = 256;
 
 template <typename TD, int K, int THREADS>
@@ -480,14 +478,31 @@ void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, Lau
     lc.add(1);
 }
 
+// Instantiations the FGP autotuner chooses from, per arithmetic: (iterations per super-step K, threads); the
+// region of K = 2, 4, 6, 8 holds 720, 960, 1232, 1536 pixels, two per thread. All give the same iterates.
+struct FgpVariant {
+    int K, threads;
+    const void *kernel;
+    size_t smem;
+};
+static const FgpVariant kFgpFloat[] = {
+    {4, 480, (const void *)k_tv_fgp<float, 4, 480>, fgp_smem<float, 4>()},
+    {6, 640, (const void *)k_tv_fgp<float, 6, 640>, fgp_smem<float, 6>()},
+    {8, 768, (const void *)k_tv_fgp<float, 8, 768>, fgp_smem<float, 8>()},
+};
+static const FgpVariant kFgpDfloat[] = {
+    {2, 384, (const void *)k_tv_fgp<dfloat, 2, 384>, fgp_smem<dfloat, 2>()},
+    {4, 480, (const void *)k_tv_fgp<dfloat, 4, 480>, fgp_smem<dfloat, 4>()},
+};
+int tv_fgp_variant_count(bool extended) { return extended ? 2 : 3; }
+int tv_fgp_default_variant(bool extended) { return extended ? 1 : 2; }
+
 cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *lam, const float *linv, const float *g,
                           double *P0, double *P1, double *Q0, double *Q1, float *U, GridBarrier gb, cudaStream_t st,
-                          LaunchCounter &lc, bool extended) {
+                          LaunchCounter &lc, bool extended, int variant) {
     ProfScope _ps(lc, extended ? "tv_fgp_df" : "tv_fgp", st);
-    const void *kern = extended ? (const void *)k_tv_fgp<dfloat, kFgpKd, kFgpThreadsD>
-                            : (const void *)k_tv_fgp<float, kFgpKf, kFgpThreadsF>;
-    const size_t smem = extended ? fgp_smem<dfloat, kFgpKd>() : fgp_smem<float, kFgpKf>();
-    const int threads = extended ? kFgpThreadsD : kFgpThreadsF;
+    if (variant < 0 || variant >= tv_fgp_variant_count(extended)) variant = tv_fgp_default_variant(extended);
+    const FgpVariant &R = extended ? kFgpDfloat[variant] : kFgpFloat[variant];
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -496,14 +511,14 @@ cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *
     if (dev >= 0 && dev < 64) {
         std::lock_guard<std::mutex> lock(mu);
         if (!attr_set[dev]) {
-            cudaFuncSetAttribute(k_tv_fgp<float, kFgpKf, kFgpThreadsF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)fgp_smem<float, kFgpKf>());
-            cudaFuncSetAttribute(k_tv_fgp<dfloat, kFgpKd, kFgpThreadsD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)fgp_smem<dfloat, kFgpKd>());
+            for (const FgpVariant &v : kFgpFloat)
+                cudaFuncSetAttribute(v.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem);
+            for (const FgpVariant &v : kFgpDfloat)
+                cudaFuncSetAttribute(v.kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)v.smem);
             attr_set[dev] = true;
         }
     }
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, R.kernel, R.threads, R.smem);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) return cudaErrorInvalidConfiguration;
     const int ntiles = ((W + kFgpTX - 1) / kFgpTX) * ((H + kFgpTY - 1) / kFgpTY);
@@ -513,7 +528,7 @@ cudaError_t launch_tv_fgp(int W, int H, int niter, const float *F, const float *
     const int blocks = std::max(1, (ntiles + per_block - 1) / per_block);
     void *args[] = {&W, &H, &niter, (void *)&F, (void *)&lam, (void *)&linv, (void *)&g, &P0, &P1, &Q0, &Q1, &U, &gb};
     lc.add(1);
-    return cudaLaunchCooperativeKernel(kern, dim3(blocks), dim3(threads), args, smem, st);
+    return cudaLaunchCooperativeKernel(R.kernel, dim3(blocks), dim3(R.threads), args, R.smem, st);
 }
 
 }  // namespace lfrv
