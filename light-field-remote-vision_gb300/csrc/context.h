@@ -59,6 +59,8 @@ struct Workspace {
     DevBuf tv;
     // the device scene generator's planes and bumps
     DevBuf scene;
+    // the device-side loop state of a graph-driven corrected IBR_color solve
+    DevBuf tvloop;
 };
 
 // Per-kernel CUDA-event timing: a fixed pool of event pairs recorded in-stream. When the pool is full the

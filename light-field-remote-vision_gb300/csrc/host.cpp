@@ -590,6 +590,146 @@ struct TvSolve {
     void finish() {
         LFRV_CUDA(cudaMemcpyAsync(c->ws.U.p, u, sizeof(float) * 3 * G.N, cudaMemcpyDeviceToDevice, c->stream));
     }
+
+    // The whole loop (begun) as one CUDA graph with the stop test on the device: eval and k_tv_decide, then a
+    // conditional WHILE node whose body is the FISTA step (theta from the device state; u and grad f kept as the
+    // previous ones by copies, so the body's buffers never change), a conditional IF node choosing the FGP's
+    // arithmetic (double-float or FP32, each autotuned beforehand), eval and k_tv_decide again. No host round trip
+    // per step; the same arithmetic and decisions as eval / decide / step. False when the graph cannot be built
+    // here (the caller then runs the host loop); the solve's state is unchanged then.
+    bool run_graph() {
+        if (c->launches.prof) return false;  // per-kernel profiling brackets launches with events
+        cudaStream_t s = c->stream;
+        Workspace &ws = c->ws;
+        const size_t N = G.N, N3 = 3 * N;
+        // everything the captured launches use, allocated and tuned before the capture
+        const int vf = fgp_autotune(c, G.W, G.H, false, b.F, lam, linv, b.g, P0);
+        const int vd = fgp_autotune(c, G.W, G.H, true, b.F, lam, linv, b.g, P0);
+        partial_buf(c, std::max<size_t>((size_t)residual_partials(G), 3 * (size_t)npart));
+        ws.sums.ensure(sizeof(double) * 64);
+        ws.tvloop.ensure(sizeof(TvLoopState));
+        const int cap = (st && st->energy_trace) ? st->trace_capacity : 0;
+        if (cap > 0) ws.trace.ensure(sizeof(double) * cap);
+        TvLoopState *loop = ws.tvloop.as<TvLoopState>();
+        TvLoopState init{};
+        init.t = t;
+        init.E_prev = E_prev;
+        init.E = E;
+        init.gap = gap;
+        init.k = k;
+        init.extended = extended ? 1 : 0;
+        init.trace_pos = trace_pos;
+        LFRV_CUDA(cudaMemcpyAsync(loop, &init, sizeof(init), cudaMemcpyHostToDevice, s));
+        LFRV_CUDA(cudaStreamSynchronize(s));
+        double *dtrace = cap > 0 ? ws.trace.as<double>() : nullptr;
+        const long long n0 = c->launches.n;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        std::vector<cudaGraph_t> pieces;
+        bool ok = false;
+        long long n_pro = 0, n_body = 0;
+        do {
+            if (cudaGraphCreate(&g, 0) != cudaSuccess) break;
+            cudaGraphConditionalHandle h_loop, h_ext;
+            if (cudaGraphConditionalHandleCreate(&h_loop, g, 0, 0) != cudaSuccess ||
+                cudaGraphConditionalHandleCreate(&h_ext, g, 0, 0) != cudaSuccess)
+                break;
+            auto capture = [&](auto &&fn, long long &count) -> cudaGraph_t {
+                cudaGraph_t piece = nullptr;
+                const long long before = c->launches.n;
+                if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return nullptr;
+                fn();
+                if (cudaStreamEndCapture(s, &piece) != cudaSuccess) return nullptr;
+                count += c->launches.n - before;
+                pieces.push_back(piece);
+                return piece;
+            };
+            auto eval_decide = [&]() {
+                const float s2 = cfg.sigma_sensor * cfg.sigma_sensor;
+                residual(c, G, u, img, tau2, b.wgt, s2, b.res, 1, true);
+                launch_tv_gradf(G, B, tau2, b.res, as2(), gf, s, c->launches);
+                double *part = partial_buf(c, 3 * (size_t)npart);
+                launch_tv_gap(G.W, G.H, u, gf, P0, b.g, cfg.lambda, part, s, c->launches);
+                for (int q = 0; q < 3; ++q) reduce_to(c, npart, part + (size_t)q * npart, 4 + q);
+                launch_tv_decide(ws.sums.as<double>(), (double)cfg.dt_alpha, (double)cfg.lambda, cfg.cg_gap_tol,
+                                 cfg.niter, loop, dtrace, cap, h_loop, h_ext, s, c->launches);
+            };
+            auto fgp = [&](bool ext, int variant) {
+                const GridBarrier gb = fresh_barrier(c);
+                cudaError_t e = launch_tv_fgp(G.W, G.H, kTvInnerIterations, b.F, lam, linv, b.g, P0, P1, Q0, Q1, u, gb,
+                                              s, c->launches, ext, variant);
+                if (e != cudaSuccess) cudaGetLastError();
+            };
+            long long n_fgp = 0;
+            cudaGraph_t g_pro = capture(eval_decide, n_pro);
+            cudaGraph_t g_step = capture(
+                [&]() {
+                    launch_tv_fstep(G.W, G.H, u, up, gf, gfp, D, 0.f, b.F, s, c->launches, loop);
+                    cudaMemcpyAsync(up, u, sizeof(float) * N3, cudaMemcpyDeviceToDevice, s);
+                    cudaMemcpyAsync(gfp, gf, sizeof(float) * N3, cudaMemcpyDeviceToDevice, s);
+                },
+                n_body);
+            long long n_dummy = 0;
+            cudaGraph_t g_df = capture([&]() { fgp(true, vd); }, n_fgp);
+            cudaGraph_t g_f = capture([&]() { fgp(false, vf); }, n_dummy);
+            cudaGraph_t g_ev = capture(eval_decide, n_body);
+            if (!g_pro || !g_step || !g_df || !g_f || !g_ev) break;
+            n_body += n_fgp;
+            cudaGraphNode_t n_p, n_w;
+            if (cudaGraphAddChildGraphNode(&n_p, g, nullptr, 0, g_pro) != cudaSuccess) break;
+            cudaGraphNodeParams wp = {};
+            wp.type = cudaGraphNodeTypeConditional;
+            wp.conditional.handle = h_loop;
+            wp.conditional.type = cudaGraphCondTypeWhile;
+            wp.conditional.size = 1;
+            if (cudaGraphAddNode(&n_w, g, &n_p, nullptr, 1, &wp) != cudaSuccess) break;
+            cudaGraph_t body = wp.conditional.phGraph_out[0];
+            cudaGraphNode_t b_step, b_if, b_ev;
+            if (cudaGraphAddChildGraphNode(&b_step, body, nullptr, 0, g_step) != cudaSuccess) break;
+            cudaGraphNodeParams ip = {};
+            ip.type = cudaGraphNodeTypeConditional;
+            ip.conditional.handle = h_ext;
+            ip.conditional.type = cudaGraphCondTypeIf;
+            ip.conditional.size = 2;
+            if (cudaGraphAddNode(&b_if, body, &b_step, nullptr, 1, &ip) != cudaSuccess) break;
+            cudaGraphNode_t b_df, b_f;
+            if (cudaGraphAddChildGraphNode(&b_df, ip.conditional.phGraph_out[0], nullptr, 0, g_df) != cudaSuccess ||
+                cudaGraphAddChildGraphNode(&b_f, ip.conditional.phGraph_out[1], nullptr, 0, g_f) != cudaSuccess)
+                break;
+            if (cudaGraphAddChildGraphNode(&b_ev, body, &b_if, 1, g_ev) != cudaSuccess) break;
+            if (cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) break;
+            ok = true;
+        } while (false);
+        for (cudaGraph_t piece : pieces) cudaGraphDestroy(piece);
+        if (!ok) {
+            cudaGetLastError();
+            if (exec) cudaGraphExecDestroy(exec);
+            if (g) cudaGraphDestroy(g);
+            c->launches.n = n0;
+            return false;
+        }
+        LFRV_CUDA(cudaGraphLaunch(exec, s));
+        TvLoopState fin{};
+        LFRV_CUDA(cudaMemcpyAsync(&fin, loop, sizeof(fin), cudaMemcpyDeviceToHost, s));
+        LFRV_CUDA(cudaStreamSynchronize(s));
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(g);
+        // launches: the prologue once, the body once per step taken
+        c->launches.n = n0 + n_pro + (long long)(fin.k - k) * n_body;
+        if (fin.err) raise(LFRV_E_NONFINITE, "non-finite energy in the corrected IBR_color solve");
+        if (cap > 0 && fin.trace_pos > trace_pos)
+            LFRV_CUDA(cudaMemcpy(st->energy_trace + trace_pos, dtrace + trace_pos,
+                                 sizeof(double) * (fin.trace_pos - trace_pos), cudaMemcpyDeviceToHost));
+        t = fin.t;
+        E_prev = fin.E_prev;
+        E = fin.E;
+        gap = fin.gap;
+        k = fin.k;
+        extended = fin.extended != 0;
+        trace_pos = fin.trace_pos;
+        done = true;
+        return true;
+    }
 };
 
 // ------------------------------------------------------------------ IBR_color
@@ -721,11 +861,13 @@ static void color_solve(lfrv_ctx *c, const lfrv_config &cfg, const float *img, c
     auto tv_meta = [&](int meta) -> int {
         TvSolve ts = tv_solver();
         ts.begin(meta);
-        for (;;) {
-            ts.eval();
-            sync(c);
-            if (ts.decide()) break;
-            ts.step();
+        if (!ts.run_graph()) {
+            for (;;) {
+                ts.eval();
+                sync(c);
+                if (ts.decide()) break;
+                ts.step();
+            }
         }
         ts.finish();
         tv_E = ts.E;

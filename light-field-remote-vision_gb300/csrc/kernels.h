@@ -193,9 +193,24 @@ void launch_tv_gradf(const Geometry &G, const Buckets &B, const float *tau, cons
 int tv_gap_partials(int W, int H);
 void launch_tv_gap(int W, int H, const float *u, const float *gf, const double *P, const float *g, float lambda,
                    double *partial, cudaStream_t st, LaunchCounter &lc);
-// F = y - grad f(y) / D, y = u + theta (u - u_prev), grad f(y) = (1 + theta) gf - theta gf_prev (3 planes).
+// Scalars of a corrected IBR_color solve whose loop runs on the device (a conditional graph): FISTA's t, the
+// previous and current energy, the certified gap, steps taken, the stop and arithmetic flags, the non-finite flag,
+// the energy trace's next slot, and the momentum weight theta of the next step.
+struct TvLoopState {
+    double t, E_prev, E, gap;
+    int k, done, extended, err, trace_pos, pad;
+    float theta;
+};
+// F = y - grad f(y) / D, y = u + theta (u - u_prev), grad f(y) = (1 + theta) gf - theta gf_prev (3 planes); theta
+// from loop->theta when loop is given.
 void launch_tv_fstep(int W, int H, const float *u, const float *up, const float *gf, const float *gfp, const float *D,
-                     float theta, float *F, cudaStream_t st, LaunchCounter &lc);
+                     float theta, float *F, cudaStream_t st, LaunchCounter &lc, const TvLoopState *loop = nullptr);
+// One thread: the energy and certified gap from the sums (slots 1, 4, 5, 6), the stop test (k >= niter or gap <=
+// tol), and when going on the restart / momentum update, the switch to double-float below kTvExtendedBelow, and
+// k + 1; sets h_loop to "go on" and h_extended to the arithmetic of the next step.
+void launch_tv_decide(const double *sums, double dt_alpha, double lambda, double tol, int niter, TvLoopState *loop,
+                      double *trace, int trace_cap, cudaGraphConditionalHandle h_loop,
+                      cudaGraphConditionalHandle h_extended, cudaStream_t st, LaunchCounter &lc);
 // out = clamp(in, 0, 1) over n floats.
 void launch_tv_clamp(size_t n, const float *in, float *out, cudaStream_t st, LaunchCounter &lc);
 // niter FGP iterations on the dual of the weighted ROF problem (one cooperative launch): P0 holds the starting

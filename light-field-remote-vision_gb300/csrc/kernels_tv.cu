@@ -116,9 +116,10 @@ __global__ void __launch_bounds__(kGapBX * kGapBY) k_tv_gap(int W, int H, const 
 
 __global__ void k_tv_fstep(size_t N, const float *__restrict__ u, const float *__restrict__ up,
                            const float *__restrict__ gf, const float *__restrict__ gfp, const float *__restrict__ D,
-                           float theta, float *__restrict__ F) {
+                           float theta_arg, const TvLoopState *__restrict__ loop, float *__restrict__ F) {
     const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 3 * N) return;
+    const float theta = loop ? loop->theta : theta_arg;
     const float y = u[i] + theta * (u[i] - up[i]);
     const float gy = (1.0f + theta) * gf[i] - theta * gfp[i];
     F[i] = y - gy / D[i % N];
@@ -465,10 +466,52 @@ void launch_tv_gap(int W, int H, const float *u, const float *gf, const double *
 }
 
 void launch_tv_fstep(int W, int H, const float *u, const float *up, const float *gf, const float *gfp, const float *D,
-                     float theta, float *F, cudaStream_t st, LaunchCounter &lc) {
+                     float theta, float *F, cudaStream_t st, LaunchCounter &lc, const TvLoopState *loop) {
     ProfScope _ps(lc, "tv_fstep", st);
     const size_t N = (size_t)W * H;
-    k_tv_fstep<<<(unsigned)((3 * N + 255) / 256), 256, 0, st>>>(N, u, up, gf, gfp, D, theta, F);
+    k_tv_fstep<<<(unsigned)((3 * N + 255) / 256), 256, 0, st>>>(N, u, up, gf, gfp, D, theta, loop, F);
+    lc.add(1);
+}
+
+// The stop test and momentum update of the corrected IBR_color solve on the device (TvSolve::decide and the scalar
+// part of TvSolve::step, the same double arithmetic), for a solve whose loop runs as a conditional graph: one
+// thread reads the certificate sums, records the energy, decides, and sets the loop's and the arithmetic's
+// conditions.
+__global__ void k_tv_decide(const double *__restrict__ sums, double dt_alpha, double lambda, double tol, int niter,
+                            double extended_below, TvLoopState *loop, double *trace, int trace_cap,
+                            cudaGraphConditionalHandle h_loop, cudaGraphConditionalHandle h_extended) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    const double f = 0.5 * dt_alpha * sums[1];
+    const double E = f + lambda * sums[4];
+    const double gap_abs = lambda * (sums[4] - sums[5]) + sums[6];
+    const double gap = E > 0 ? gap_abs / E : 1e300;
+    if (trace && loop->trace_pos < trace_cap) trace[loop->trace_pos++] = E;
+    bool done = loop->k >= niter || (tol > 0 && gap <= tol);
+    if (!isfinite(E) || !isfinite(gap)) {
+        loop->err = 1;
+        done = true;
+    }
+    loop->E = E;
+    loop->gap = gap;
+    if (!done) {
+        if (E > loop->E_prev) loop->t = 1.0;  // function-value restart of the momentum
+        loop->E_prev = E;
+        const double t = loop->t, t1 = 0.5 * (1.0 + sqrt(1.0 + 4.0 * t * t));
+        loop->theta = (float)((t - 1.0) / t1);
+        loop->t = t1;
+        loop->extended = loop->extended || gap < extended_below;
+        loop->k += 1;
+    }
+    loop->done = done ? 1 : 0;
+    cudaGraphSetConditional(h_loop, done ? 0u : 1u);
+    cudaGraphSetConditional(h_extended, loop->extended ? 1u : 0u);
+}
+
+void launch_tv_decide(const double *sums, double dt_alpha, double lambda, double tol, int niter, TvLoopState *loop,
+                      double *trace, int trace_cap, cudaGraphConditionalHandle h_loop,
+                      cudaGraphConditionalHandle h_extended, cudaStream_t st, LaunchCounter &lc) {
+    k_tv_decide<<<1, 32, 0, st>>>(sums, dt_alpha, lambda, tol, niter, kTvExtendedBelow, loop, trace, trace_cap, h_loop,
+                                  h_extended);
     lc.add(1);
 }
 
