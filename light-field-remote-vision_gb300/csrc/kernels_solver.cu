@@ -724,8 +724,14 @@ __global__ void k_initial_image(int W, int H, int n, int dsf, int BW, const unsi
 // kLearnViews views; [38..40] the CG's initial residual at u0 per channel, r0 = grad^T g + Delta u0 (FP32, the
 // operator's boundary rules, clamped to [-4, 4]); [41..47] zero. Per-view accumulators live in shared memory (one
 // column per thread), so the view index of an entry needs no register indexing.
+// Each entry's tap is computed alone, not through footprint_tap's KS^2 products: the footprint is an outer product,
+// so its norm is the product of the in-image row and column overlap sums, and the tap (j, i) is
+// dx_j * (dy_i / norm) with one reciprocal (within a few ulps of footprint_tap's quotient, as in the set-up's
+// anchor-row form). The gather is a chain of dependent loads (bucket bounds, entry, the view's data), so all KS x KS
+// buckets' bounds and first entries are loaded up front (a row's KS buckets are contiguous) and each bucket's loop
+// keeps the entry two ahead and the next entry's data in flight.
 template <int KS, typename TS>
-__global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int dsf, int BW,
+__global__ void __launch_bounds__(256, 4) k_learn_input(int W, int H, int n, int dsf, int BW,
                                                      const unsigned int *__restrict__ start,
                                                      const unsigned int *__restrict__ entries,
                                                      const float *__restrict__ tau, const TS *__restrict__ img,
@@ -734,27 +740,88 @@ __global__ void __launch_bounds__(256) k_learn_input(int W, int H, int n, int ds
                                                      const uint8_t *__restrict__ vis, __nv_bfloat16 *__restrict__ out) {
     __shared__ float acc[kLearnViews * 4][256];
     const int t = threadIdx.y * blockDim.x + threadIdx.x;
-    const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+    // a block covers 64 x 4 pixels; warp w takes the columns of parity w & 1 of row w >> 1, so that the lanes of a
+    // warp scan buckets of one anchor parity (with dsf 2 most entries sit on even anchors)
+    const int x = blockIdx.x * 64 + 2 * threadIdx.x + (threadIdx.y & 1), y = blockIdx.y * 4 + (threadIdx.y >> 1);
 #pragma unroll
     for (int i = 0; i < kLearnViews * 4; ++i) acc[i][t] = 0.f;
     if (x >= W || y >= H) return;
+    // row i's anchors x - KS + 1 .. x are buckets r .. r + KS - 1 of that row: column j's bucket is r + KS - 1 - j
+    unsigned int bs[KS][KS + 1];
 #pragma unroll
     for (int i = 0; i < KS; ++i) {
+        const size_t r = (size_t)(y - i + KS - 1) * BW + x;
+#pragma unroll
+        for (int q = 0; q <= KS; ++q) bs[i][q] = __ldg(start + r + q);
+    }
+    constexpr unsigned int kNone = 0xFFFFFFFFu;  // view 255: past the first views
+    auto ok = [](unsigned int ent) { return (int)(ent >> 24) < kLearnViews; };
+    // every bucket's first entry, loaded together
+    unsigned int first[KS][KS];
+#pragma unroll
+    for (int i = 0; i < KS; ++i)
+#pragma unroll
+        for (int j = 0; j < KS; ++j)
+            first[i][j] = bs[i][KS - 1 - j] < bs[i][KS - j] ? __ldg(entries + bs[i][KS - 1 - j]) : kNone;
+    struct Src {
+        float px, py, w, c0, c1, c2;
+    };
+    auto fetch = [&](unsigned int ent) {
+        const size_t v = ent >> 24, m = ent & 0xFFFFFFu;
+        Src d;
+        d.px = __ldg(tau + v * 2 * n + m) - 0.5f;
+        d.py = __ldg(tau + v * 2 * n + n + m) - 0.5f;
+        d.w = ldv(wgt + v * n + m);
+        d.c0 = ldv(img + (v * 3 + 0) * n + m);
+        d.c1 = ldv(img + (v * 3 + 1) * n + m);
+        d.c2 = ldv(img + (v * 3 + 2) * n + m);
+        return d;
+    };
+#pragma unroll
+    for (int i = 0; i < KS; ++i) {
+        const int ay = y - i;
+        bool iny[KS];
+#pragma unroll
+        for (int q = 0; q < KS; ++q) iny[q] = (0 <= ay + q && ay + q <= H - 1);
 #pragma unroll
         for (int j = 0; j < KS; ++j) {
-            const int ax = x - j, ay = y - i;
-            const size_t b = (size_t)(ay + KS - 1) * BW + (ax + KS - 1);
-            const unsigned int s0 = __ldg(start + b), e0 = __ldg(start + b + 1);
-            for (unsigned int k = s0; k < e0; ++k) {
-                const unsigned int ent = __ldg(entries + k);
-                const int v = (int)(ent >> 24), m = (int)(ent & 0xFFFFFFu);
-                if (v >= kLearnViews) break;  // a bucket's entries ascend by view: the rest are later views
-                const float tx = __ldg(tau + (size_t)v * 2 * n + m), ty = __ldg(tau + (size_t)v * 2 * n + n + m);
-                float raw;
-                const float A = footprint_tap<KS>(tx, ty, dsf, W, H, ax, ay, j, i, raw) * ldv(wgt + (size_t)v * n + m);
-                acc[v * 4 + 3][t] += A;
+            const int ax = x - j;
+            bool inx[KS];
 #pragma unroll
-                for (int c = 0; c < 3; ++c) acc[v * 4 + c][t] += A * ldv(img + ((size_t)v * 3 + c) * n + m);
+            for (int q = 0; q < KS; ++q) inx[q] = (0 <= ax + q && ax + q <= W - 1);
+            // software pipeline: the entry two ahead and the view data of the next entry are in flight while the
+            // current entry is added
+            const unsigned int s0 = bs[i][KS - 1 - j], e0 = bs[i][KS - j];
+            unsigned int cur = first[i][j];
+            if (!ok(cur)) continue;
+            unsigned int nxt = s0 + 1 < e0 ? __ldg(entries + s0 + 1) : kNone;
+            Src d = fetch(cur);
+            for (unsigned int k = s0;; ++k) {
+                const unsigned int n2 = (ok(nxt) && k + 2 < e0) ? __ldg(entries + k + 2) : kNone;
+                Src dn = {};
+                if (ok(nxt)) dn = fetch(nxt);
+                const int v = (int)(cur >> 24);
+                float sx = 0.f, sy = 0.f, dxj = 0.f, dyi = 0.f;
+#pragma unroll
+                for (int q = 0; q < KS; ++q) {
+                    const float dx = inx[q] ? fp_overlap(q, KS, ax + q, d.px, dsf) : 0.f;
+                    const float dy = iny[q] ? fp_overlap(q, KS, ay + q, d.py, dsf) : 0.f;
+                    sx = __fadd_rn(sx, dx);
+                    sy = __fadd_rn(sy, dy);
+                    if (q == j) dxj = dx;
+                    if (q == i) dyi = dy;
+                }
+                const float norm = __fmul_rn(sx, sy);
+                const float inv = (norm != 0.0f) ? __frcp_rn(norm) : 1.0f;
+                const float A = __fmul_rn(dxj, __fmul_rn(dyi, inv)) * d.w;
+                acc[v * 4 + 3][t] += A;
+                acc[v * 4 + 0][t] += A * d.c0;
+                acc[v * 4 + 1][t] += A * d.c1;
+                acc[v * 4 + 2][t] += A * d.c2;
+                if (!ok(nxt)) break;  // entries ascend by view: the rest of the bucket are later views
+                cur = nxt;
+                nxt = n2;
+                d = dn;
             }
         }
     }
@@ -1311,7 +1378,7 @@ template <typename TS>
 static void learn_input_typed(const Geometry &G, const Buckets &B, const float *tau, const TS *img, const TS *wgt,
                               const float *U, const float *gx, const float *gy, const uint8_t *vis,
                               __nv_bfloat16 *out, cudaStream_t st) {
-    const dim3 g = grid2(G.W, G.H, kTile);
+    const dim3 g((G.W + 63) / 64, (G.H + 3) / 4);  // 64 x 4 pixels per block of kTile (32 x 8) threads
     switch (G.dsf + 1) {
         case 2: k_learn_input<2, TS><<<g, kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau, img, wgt, U, gx, gy, vis, out); break;
         case 3: k_learn_input<3, TS><<<g, kTile, 0, st>>>(G.W, G.H, G.n, G.dsf, B.BW, B.start, B.entries, tau, img, wgt, U, gx, gy, vis, out); break;
