@@ -848,15 +848,22 @@ __global__ void __launch_bounds__(256, 4) k_learn_input(int W, int H, int n, int
         f[c] = uc;
         f[38 + c] = fminf(fmaxf(-(lx + ly), -4.f), 4.f);
     }
+    // quotients as products with one reciprocal each (within an ulp or two of the division; stored as BF16); a
+    // divisor below 1e-30, whose reciprocal could overflow, divides
+    auto quot = [](float num, float den, float rden) {
+        return den >= 1e-30f ? num * rden : (den > 0.f ? num / den : 0.f);
+    };
     float total = 0.f;
 #pragma unroll
     for (int v = 0; v < kLearnViews; ++v) total += acc[v * 4 + 3][t];
+    const float rtotal = total >= 1e-30f ? __frcp_rn(total) : 0.f;
 #pragma unroll
     for (int v = 0; v < kLearnViews; ++v) {
         const float a = acc[v * 4 + 3][t];
+        const float ra = a >= 1e-30f ? __frcp_rn(a) : 0.f;
 #pragma unroll
-        for (int c = 0; c < 3; ++c) f[6 + 3 * v + c] = a > 0.f ? acc[v * 4 + c][t] / a : 0.f;
-        f[6 + 3 * kLearnViews + v] = total > 0.f ? a / total : 0.f;
+        for (int c = 0; c < 3; ++c) f[6 + 3 * v + c] = quot(acc[v * 4 + c][t], a, ra);
+        f[6 + 3 * kLearnViews + v] = quot(a, total, rtotal);
     }
     uint4 *dst = reinterpret_cast<uint4 *>(out + o * kLearnChannels);
 #pragma unroll
