@@ -127,6 +127,7 @@ struct lfrv_ctx {
     // host-buffer calls upload on a second stream so the copies overlap the warp stage (created on first use)
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t up_start = nullptr, up_depth[4] = {}, up_views = nullptr;
+    cudaEvent_t out_ready = nullptr;  // a batched host-buffer call's job output is final (its download may start)
     // work that depends only on a call's inputs runs on a side stream, joined by event (created on first use)
     cudaStream_t side_stream = nullptr;
     cudaEvent_t side_fork = nullptr, side_join = nullptr;

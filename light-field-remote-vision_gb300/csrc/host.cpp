@@ -1415,6 +1415,8 @@ static void end_timing(lfrv_ctx *c, lfrv_stats *st, long long launches0) {
 
 using namespace lfrv;
 
+static cudaStream_t copy_stream(lfrv_ctx *c);
+
 // (every call starts without counted buckets: a count the warp stage took belongs to the call that took it)
 #define CTX_CHECK(ctx)                                                   \
     if (!(ctx)) return lfrv::fail(LFRV_E_ARG, "null context");           \
@@ -1480,6 +1482,7 @@ extern "C" int lfrv_ctx_destroy(lfrv_ctx *ctx) {
         cudaStreamDestroy(ctx->copy_stream);
         cudaEventDestroy(ctx->up_start);
         cudaEventDestroy(ctx->up_views);
+        cudaEventDestroy(ctx->out_ready);
         for (auto e : ctx->up_depth) cudaEventDestroy(e);
     }
     ctx->prof.destroy();
@@ -1983,7 +1986,12 @@ extern "C" int lfrv_render_view_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, con
 // IBR_gradient jobs with the corrected CG share one k_cg_batch launch (per launch at most as many jobs as resident
 // blocks); every other job runs on its own. Per gradient job the batch pool holds U, gx, gy, r, dA, dB (14 N
 // floats) and 8 doubles of state.
-static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv_warmstart *net = nullptr) {
+// Host-buffer calls pass host_out (per job: a pinned host destination, or nullptr) and sent (per job, zeroed): an
+// IBR_gradient job's output is then copied to host_out as soon as its CG is done, on the copy stream, while the next
+// jobs run, and sent[job] is set. views_ready (or nullptr): an event the jobs wait for before they read their colour
+// views (the warp stage reads only the depth maps, so it may start while the views are still being uploaded).
+static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv_warmstart *net = nullptr,
+                         float *const *host_out = nullptr, char *sent = nullptr, cudaEvent_t views_ready = nullptr) {
     if (count <= 0 || !jobs) raise(LFRV_E_ARG, "empty batch");
     cudaStream_t s = c->stream;
     Workspace &ws = c->ws;
@@ -2066,6 +2074,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         l->ws.dp.ensure(sizeof(float) * 2 * (size_t)G.V * G.n);
         warp(l, G.V, G.w, G.h, J.d_depth, J.cams, J.target, nullptr, nullptr, l->ws.tau.as<float>(),
              l->ws.dp.as<float>(), nullptr);
+        if (views_ready) LFRV_CUDA(cudaStreamWaitEvent(l->stream, views_ready, 0));
         color_solve(l, *J.cfg, J.d_views, l->ws.tau.as<float>(), l->ws.dp.as<float>(), nullptr, J.d_out, J.stats,
                     &tv[q]);
         l->pending.trace_host = nullptr;  // the solve writes its trace from the host
@@ -2082,6 +2091,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         warp(l, G.V, G.w, G.h, J.d_depth, J.cams, J.target, nullptr, nullptr, lw.tau.as<float>(), nullptr, nullptr,
              nullptr, &G);
         float *U = base + sl.off;
+        if (views_ready) LFRV_CUDA(cudaStreamWaitEvent(l->stream, views_ready, 0));
         gradient_prepare(l, *J.cfg, G, J.d_views, lw.tau.as<float>(), nullptr, nullptr, U, U + 3 * G.N, U + 4 * G.N,
                          sl.seeded ? U + 17 * G.N + 16 : nullptr);
         // keep this job's hole-fill iteration count (state slot 8) beside its CG state
@@ -2093,6 +2103,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         LFRV_CUDA(cudaEventRecord(c->lane_done[k], c->lanes[k]->stream));
         LFRV_CUDA(cudaStreamWaitEvent(s, c->lane_done[k], 0));
     }
+    if (views_ready) LFRV_CUDA(cudaStreamWaitEvent(s, views_ready, 0));
     // the other jobs, one after another on the context stream
     for (int j = 0; j < count; ++j) {
         const lfrv_view_job &J = jobs[j];
@@ -2137,6 +2148,16 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
     // it gains nothing from sharing a launch, so it runs the single-target persistent CG (shared-memory resident
     // or TMA form) on its pool buffers, one after another on the context stream. The others share k_cg_batch.
     const int resident = cg_batch_resident_blocks();
+    // a job's final output (the CG's iterate) to its host destination, after what the context stream has queued
+    auto send = [&](const Slot &sl) {
+        if (!host_out || !host_out[sl.job] || !sent) return;
+        cudaStream_t cs = copy_stream(c);
+        LFRV_CUDA(cudaEventRecord(c->out_ready, s));
+        LFRV_CUDA(cudaStreamWaitEvent(cs, c->out_ready, 0));
+        LFRV_CUDA(cudaMemcpyAsync(host_out[sl.job], base + sl.off + (sl.seeded ? 14 * sl.G.N + 16 : 0),
+                                  sizeof(float) * 3 * sl.G.N, cudaMemcpyDeviceToHost, cs));
+        sent[sl.job] = 1;
+    };
     std::vector<size_t> grouped;
     for (size_t q = 0; q < batched.size(); ++q) {
         const Slot &sl = batched[q];
@@ -2159,6 +2180,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
                                        sl.seeded ? U : nullptr, traced ? ws.trace.as<double>() + trace_off[q] : nullptr,
                                        traced ? jst->trace_capacity : 0));
         check_launch("batched job CG");
+        send(sl);
     }
     // the CG of the other gradient jobs, in launches of at most `resident` jobs
     for (size_t first = 0; first < grouped.size(); first += (size_t)resident) {
@@ -2227,6 +2249,7 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         const GridBarrier gb = fresh_barrier(c);
         LFRV_CUDA(launch_cg_batch(d_probs, d_block_prob, (int)cnt, used, part, part + 4 * (size_t)used, d_done, gb, s,
                                   c->launches));
+        for (size_t q = 0; q < cnt; ++q) send(batched[grouped[first + q]]);
         // the next launch rewrites the descriptors in batch_meta (the host vectors were staged by the copies)
         if (first + cnt < grouped.size()) LFRV_CUDA(cudaStreamSynchronize(s));
     }
@@ -2270,8 +2293,9 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         }
     }
     for (const Slot &sl : batched)
-        LFRV_CUDA(cudaMemcpyAsync(jobs[sl.job].d_out, base + sl.off + (sl.seeded ? 14 * sl.G.N + 16 : 0),
-                                  sizeof(float) * 3 * sl.G.N, cudaMemcpyDeviceToDevice, s));
+        if (!(sent && sent[sl.job]))
+            LFRV_CUDA(cudaMemcpyAsync(jobs[sl.job].d_out, base + sl.off + (sl.seeded ? 14 * sl.G.N + 16 : 0),
+                                      sizeof(float) * 3 * sl.G.N, cudaMemcpyDeviceToDevice, s));
     sync(c);
     for (lfrv_ctx *l : c->lanes) {
         c->launches.add((int)l->launches.n);
@@ -2317,19 +2341,26 @@ extern "C" int lfrv_render_views_warm_dev(lfrv_ctx *ctx, lfrv_warmstart *net, co
 
 // Host-buffer batched targets: the jobs' views, depth maps and outputs are host pointers. Each distinct input
 // buffer (same pointer and size, as when many targets share one light field) is uploaded once into one device
-// pool; the batch runs as lfrv_render_views_dev would; the outputs are copied back before the call returns.
+// pool: the depth maps on the context stream (the warp stage reads them first), the colour views on the copy stream
+// while the warp stage runs. The batch runs as lfrv_render_views_dev would. An IBR_gradient job whose output is
+// pinned host memory is downloaded on the copy stream as soon as its CG is done, while the next jobs run; the other
+// outputs are copied back at the end. The call returns once every output is in host memory.
 static void render_views_host(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv_warmstart *net) {
     if (count <= 0 || !jobs) raise(LFRV_E_ARG, "empty batch");
     struct Input {
         const void *host;
         size_t bytes, off;
+        bool depth;  // some job's depth maps: needed by the warp stage
     };
     std::vector<Input> inputs;
-    auto place = [&](const void *p, size_t bytes) -> size_t {
-        for (const Input &in : inputs)
-            if (in.host == p && in.bytes == bytes) return in.off;
+    auto place = [&](const void *p, size_t bytes, bool depth) -> size_t {
+        for (Input &in : inputs)
+            if (in.host == p && in.bytes == bytes) {
+                in.depth = in.depth || depth;
+                return in.off;
+            }
         const size_t off = inputs.empty() ? 0 : (inputs.back().off + inputs.back().bytes + 255) / 256 * 256;
-        inputs.push_back({p, bytes, off});
+        inputs.push_back({p, bytes, off, depth});
         return off;
     };
     std::vector<size_t> off_views(count), off_depth(count), off_out(count);
@@ -2339,8 +2370,8 @@ static void render_views_host(lfrv_ctx *c, const lfrv_view_job *jobs, int count,
         if (!J.cfg || !J.d_views || !J.d_depth || !J.d_out) raise(LFRV_E_ARG, "job %d: null argument", j);
         const Geometry G = geometry(*J.cfg);
         const size_t vb = (size_t)G.V * 3 * G.n * (J.cfg->bf16_storage ? 2 : 4);
-        off_views[j] = place(J.d_views, vb);
-        off_depth[j] = place(J.d_depth, (size_t)G.V * 3 * G.n * sizeof(float));
+        off_views[j] = place(J.d_views, vb, false);
+        off_depth[j] = place(J.d_depth, (size_t)G.V * 3 * G.n * sizeof(float), true);
         off_out[j] = out_bytes;
         out_bytes += (3 * G.N * sizeof(float) + 255) / 256 * 256;
     }
@@ -2348,21 +2379,43 @@ static void render_views_host(lfrv_ctx *c, const lfrv_view_job *jobs, int count,
     c->ws.hb_in.ensure(in_bytes);
     c->ws.hb_out.ensure(out_bytes);
     char *din = c->ws.hb_in.as<char>(), *dout = c->ws.hb_out.as<char>();
+    cudaStream_t cs = copy_stream(c);
+    // the copy stream starts after what the context stream has queued (an earlier call may still read the pool)
+    LFRV_CUDA(cudaEventRecord(c->up_start, c->stream));
+    LFRV_CUDA(cudaStreamWaitEvent(cs, c->up_start, 0));
     for (const Input &in : inputs)
-        LFRV_CUDA(cudaMemcpyAsync(din + in.off, in.host, in.bytes, cudaMemcpyHostToDevice, c->stream));
+        LFRV_CUDA(cudaMemcpyAsync(din + in.off, in.host, in.bytes, cudaMemcpyHostToDevice, in.depth ? c->stream : cs));
+    LFRV_CUDA(cudaEventRecord(c->up_views, cs));
+    // pinned destinations take the early download; a pageable one would make each copy wait on the host
+    std::vector<float *> host_out(count, nullptr);
+    for (int j = 0; j < count; ++j) {
+        cudaPointerAttributes a{};
+        if (cudaPointerGetAttributes(&a, jobs[j].d_out) == cudaSuccess && a.type == cudaMemoryTypeHost)
+            host_out[j] = jobs[j].d_out;
+        else
+            cudaGetLastError();
+    }
+    std::vector<char> sent(count, 0);
     std::vector<lfrv_view_job> dj(jobs, jobs + count);
     for (int j = 0; j < count; ++j) {
         dj[j].d_views = reinterpret_cast<const float *>(din + off_views[j]);
         dj[j].d_depth = reinterpret_cast<const float *>(din + off_depth[j]);
         dj[j].d_out = reinterpret_cast<float *>(dout + off_out[j]);
     }
-    render_views(c, dj.data(), count, net);
+    try {
+        render_views(c, dj.data(), count, net, host_out.data(), sent.data(), c->up_views);
+    } catch (...) {
+        cudaStreamSynchronize(cs);  // no copy into the caller's buffers outlives the call
+        throw;
+    }
     for (int j = 0; j < count; ++j) {
+        if (sent[j]) continue;
         const Geometry G = geometry(*jobs[j].cfg);
         LFRV_CUDA(cudaMemcpyAsync(jobs[j].d_out, dout + off_out[j], 3 * G.N * sizeof(float), cudaMemcpyDeviceToHost,
                                   c->stream));
     }
     sync(c);
+    LFRV_CUDA(cudaStreamSynchronize(cs));
 }
 
 extern "C" int lfrv_render_views(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count) {
@@ -2438,6 +2491,7 @@ static cudaStream_t copy_stream(lfrv_ctx *c) {
         LFRV_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
         LFRV_CUDA(cudaEventCreateWithFlags(&c->up_start, cudaEventDisableTiming));
         LFRV_CUDA(cudaEventCreateWithFlags(&c->up_views, cudaEventDisableTiming));
+        LFRV_CUDA(cudaEventCreateWithFlags(&c->out_ready, cudaEventDisableTiming));
         for (auto &e : c->up_depth) LFRV_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     return c->copy_stream;

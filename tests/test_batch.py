@@ -121,6 +121,43 @@ def test_host_buffer_batch_equals_device_batch():
     assert not np.array_equal(outs[0], outs[1])
 
 
+def test_host_buffer_batch_pinned_outputs():
+    """Pinned host outputs take the early download (each IBR_gradient job's output leaves for the host as soon as its
+    CG is done, while the next jobs run) and the colour views upload while the warp stage runs: the outputs equal
+    lfrv_render_views_dev's bit for bit, with a 1024^2 job on the single-target CG, a job with a pageable output and
+    a corrected IBR_color job (downloaded at the end) in the same call."""
+    import torch
+
+    specs = [(2, 32, 1, {}), (2, 512, 1, {}), (1, 48, 1, {}), (1, 48, 0, dict(faithful=0, niter=60, cg_gap_tol=1e-4))]
+    jobs = []
+    for preset, w, alg, kw in specs:
+        sc = scene(preset, w)
+        cfg = gradient_config(sc, **kw) if alg == 1 else color_config(sc, **kw)
+        H, W = cfg.h * cfg.dsf, cfg.w * cfg.dsf
+        jobs.append(dict(sc=sc, cfg=cfg, alg=alg, views=np.ascontiguousarray(sc.views),
+                         depth=np.ascontiguousarray(sc.depth), dout=torch.zeros((3, H, W), device="cuda"),
+                         dv=torch.from_numpy(sc.views).cuda(), dd=torch.from_numpy(sc.depth).cuda()))
+    pinned = [True, True, False, True]
+    for j, pin in zip(jobs, pinned):
+        H, W = j["cfg"].h * j["cfg"].dsf, j["cfg"].w * j["cfg"].dsf
+        j["hout"] = (torch.zeros((3, H, W)).pin_memory() if pin else torch.zeros((3, H, W)))
+    with lfrv.Context(0) as ctx:
+        for _ in range(2):  # the second call reuses the pool and the copy stream
+            for j in jobs:
+                j["hout"].fill_(-1.0)
+            st_h = ctx.render_views([dict(cfg=j["cfg"], algorithm=j["alg"], d_views=j["views"].ctypes.data,
+                                          d_depth=j["depth"].ctypes.data, cams=j["sc"].cams, target=j["sc"].target,
+                                          d_out=j["hout"].data_ptr()) for j in jobs])
+        torch.cuda.synchronize()
+        st_d = ctx.render_views_dev([dict(cfg=j["cfg"], algorithm=j["alg"], d_views=j["dv"].data_ptr(),
+                                          d_depth=j["dd"].data_ptr(), cams=j["sc"].cams, target=j["sc"].target,
+                                          d_out=j["dout"].data_ptr()) for j in jobs])
+        torch.cuda.synchronize()
+    for j, a, b in zip(jobs, st_h, st_d):
+        np.testing.assert_array_equal(j["hout"].numpy(), j["dout"].cpu().numpy())
+        assert a.outer_iterations == b.outer_iterations
+
+
 def test_batches_of_both_lane_counts_in_one_context():
     """A batch with a target of 2^21 pixels or more prepares its jobs on two lanes, a batch of small targets on four:
     alternating them in one context gives each job what it gives alone, with the same statistics."""
