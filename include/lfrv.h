@@ -247,7 +247,9 @@ typedef struct lfrv_view_job {
 int lfrv_render_views_dev(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count);
 /* The same batch from HOST buffers: each job's d_views, d_depth and d_out are host pointers (views BF16 when the
  * job's cfg->bf16_storage is 1). Input buffers shared by several jobs (same pointer and size, e.g. one light field
- * seen from many targets) are uploaded once; every output is copied back before the call returns. */
+ * seen from many targets) are uploaded once, the colour views while the warp stage runs. An IBR_gradient job's
+ * output in pinned (page-locked) host memory is copied back as soon as its CG ends, while later jobs run; every
+ * output is in host memory when the call returns. */
 int lfrv_render_views(lfrv_ctx *ctx, const lfrv_view_job *jobs, int count);
 
 /* ---------------------------------------------------------------- IBR_video
