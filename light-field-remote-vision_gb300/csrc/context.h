@@ -55,6 +55,8 @@ struct Workspace {
     DevBuf in_views, in_tau, in_dpart, in_init, out_img;
     // host-buffer batched calls: one device copy per distinct light field (views, depth) and the outputs
     DevBuf hb_in, hb_out;
+    // batched calls: the view gradients of each distinct light field, shared by the jobs that render from it
+    DevBuf vg_pool;
     // corrected IBR_color: iterates, data gradients and metric (15 N floats), the FP64 dual / momentum fields (24 N)
     DevBuf tv;
     // the device scene generator's planes and bumps
@@ -141,6 +143,7 @@ struct lfrv_ctx {
     lfrv::LaunchCounter launches;
     lfrv::Workspace ws;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    cudaEvent_t vg_ready = nullptr;  // a batched call's shared view gradients are written
     lfrv::RenderGraph graph;  // replay of a repeated lfrv_render_view_dev call
     // the warp stage counted the inverse map's buckets for this geometry (W, H, dsf, V, n): the next bucket build
     // of the same geometry skips its count pass

@@ -1443,6 +1443,7 @@ extern "C" int lfrv_ctx_create(lfrv_ctx **out, int device) {
     c->device = device;
     LFRV_CUDA(cudaEventCreate(&c->ev0));
     LFRV_CUDA(cudaEventCreate(&c->ev1));
+    LFRV_CUDA(cudaEventCreateWithFlags(&c->vg_ready, cudaEventDisableTiming));
     gaussian_kernel_init();
     {
         const cudaError_t e = cudaGetLastError();
@@ -1463,6 +1464,7 @@ extern "C" int lfrv_ctx_destroy(lfrv_ctx *ctx) {
     else cudaDeviceSynchronize();
     if (ctx->ev0) cudaEventDestroy(ctx->ev0);
     if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+    if (ctx->vg_ready) cudaEventDestroy(ctx->vg_ready);
     for (std::vector<lfrv_ctx *> *group : {&ctx->lanes, &ctx->tv_jobs})
         for (lfrv_ctx *l : *group) {
             cudaStreamSynchronize(l->stream);
@@ -2079,6 +2081,49 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
                     &tv[q]);
         l->pending.trace_host = nullptr;  // the solve writes its trace from the host
     }
+    // the view gradients (luminance Sobel of every view) depend only on the views: computed once per distinct light
+    // field of the batched jobs, on the context stream while the lanes run the warp stage, and joined by event
+    // before each job's set-up (targets that share a light field share them)
+    struct VgField {
+        const void *views;
+        int V, w, h;
+        bool bf;
+        size_t off;
+    };
+    std::vector<VgField> fields;
+    std::vector<size_t> vg_off(batched.size(), 0);
+    size_t vg_bytes = 0;
+    for (size_t q = 0; q < batched.size(); ++q) {
+        const Slot &sl = batched[q];
+        const lfrv_view_job &J = jobs[sl.job];
+        const bool bf = J.cfg->bf16_storage != 0;
+        size_t f = 0;
+        while (f < fields.size() && !(fields[f].views == (const void *)J.d_views && fields[f].V == sl.G.V &&
+                                      fields[f].w == sl.G.w && fields[f].h == sl.G.h && fields[f].bf == bf))
+            ++f;
+        if (f == fields.size()) {
+            fields.push_back({J.d_views, sl.G.V, sl.G.w, sl.G.h, bf, vg_bytes});
+            vg_bytes += (2 * (size_t)sl.G.V * sl.G.n * (bf ? 2 : 4) + 255) / 256 * 256;
+        }
+        vg_off[q] = fields[f].off;
+    }
+    if (!fields.empty()) {
+        ws.vg_pool.ensure(vg_bytes);
+        if (views_ready) LFRV_CUDA(cudaStreamWaitEvent(s, views_ready, 0));
+        for (const VgField &f : fields) {
+            const size_t n = (size_t)f.w * f.h;
+            if (f.bf) {
+                uint16_t *vg = reinterpret_cast<uint16_t *>(ws.vg_pool.as<char>() + f.off);
+                launch_view_sobel_bf16(f.w, f.h, f.V, f.views, 3 * n, n, vg, vg + n, 2 * n, s, c->launches);
+            } else {
+                float *vg = reinterpret_cast<float *>(ws.vg_pool.as<char>() + f.off);
+                launch_sobel(f.w, f.h, f.V, static_cast<const float *>(f.views), 3 * n, n, vg, vg + n, 2 * n,
+                             nullptr, nullptr, s, c->launches);
+            }
+            check_launch("view sobel (batch)");
+        }
+        LFRV_CUDA(cudaEventRecord(c->vg_ready, s));
+    }
     for (size_t q = 0; q < batched.size(); ++q) {
         const Slot &sl = batched[q];
         const lfrv_view_job &J = jobs[sl.job];
@@ -2091,9 +2136,10 @@ static void render_views(lfrv_ctx *c, const lfrv_view_job *jobs, int count, lfrv
         warp(l, G.V, G.w, G.h, J.d_depth, J.cams, J.target, nullptr, nullptr, lw.tau.as<float>(), nullptr, nullptr,
              nullptr, &G);
         float *U = base + sl.off;
-        if (views_ready) LFRV_CUDA(cudaStreamWaitEvent(l->stream, views_ready, 0));
+        // the shared view gradients are written (and so the views are uploaded, which the context stream waited for)
+        LFRV_CUDA(cudaStreamWaitEvent(l->stream, c->vg_ready, 0));
         gradient_prepare(l, *J.cfg, G, J.d_views, lw.tau.as<float>(), nullptr, nullptr, U, U + 3 * G.N, U + 4 * G.N,
-                         sl.seeded ? U + 17 * G.N + 16 : nullptr);
+                         sl.seeded ? U + 17 * G.N + 16 : nullptr, nullptr, ws.vg_pool.as<char>() + vg_off[q]);
         // keep this job's hole-fill iteration count (state slot 8) beside its CG state
         double *st = reinterpret_cast<double *>(U + 14 * G.N);
         LFRV_CUDA(cudaMemcpyAsync(st + 6, lw.state.as<double>() + 8, sizeof(double), cudaMemcpyDeviceToDevice,
