@@ -1,4 +1,4 @@
-"""Benchmark: converged views/sec of the depth-to-view pipeline on one GB300 -- BASELINE's metric, "views/sec to
+"""Benchmark: converged views/sec of the depth-to-view pipeline on one GB300 -- the headline metric, "views/sec to
 energy gap <= 1e-4: learned + batched vs plain solver, same GB300".
 
 Workload (default "c5", the full pipeline the metric is quoted on): one synthetic 9x9 light field of 1024x1024
@@ -20,7 +20,8 @@ products until the certified relative energy gap is <= 1e-4. One step = the 32 t
   vs_fp64 : the centre target against the FP64 CPU oracle run on the GPU's warps
 
 Other workloads (--workload): c1 (3x3 256^2, IBR_color 300 x 300 iterations), c2 (5x5 512^2 -> 1024^2, one target),
-c3 (batched targets of uneven size), c4 (learned warm start trained in the run, 512^2), net (the network alone).
+c3 (batched targets of uneven size), c4 (learned warm start trained in the run, 512^2), tv (the corrected
+IBR_color to a certified gap of 1e-4 on the 3x3 256^2 scene), net (the network alone).
 
 `--impl reference` times the CPU restatement alone as the reference arm (the reference's own path needs Qt, glm,
 OpenGL and its CUDA runtime and cannot run here).
