@@ -136,6 +136,25 @@ NCU_TRAFFIC_BYTES = {
 }
 
 
+def barrier() -> None:
+    """All ranks meet here before a timed region; nothing to do in a single process."""
+    import torch
+
+    if torch.distributed.is_available() and torch.distributed.is_initialized():
+        torch.distributed.barrier()
+
+
+def max_over_ranks(x: float, device: str = "cuda") -> float:
+    """The largest x over the ranks (the slowest replica's time); x itself in a single process."""
+    import torch
+
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def sample_clocks(path: str):
     return subprocess.Popen(
         ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -642,6 +661,7 @@ def run_full(args, rank: int, world: int) -> None:
         for _ in range(args.warmup):
             st = fn()
         torch.cuda.synchronize()
+        barrier()
         headline = name == "learned_batched"
         if headline:
             clk_path = tempfile.mktemp(prefix="lfrv_clocks_")
@@ -653,7 +673,7 @@ def run_full(args, rank: int, world: int) -> None:
             st = fn()
         e1.record(stream)
         torch.cuda.synchronize()
-        sec = e0.elapsed_time(e1) / 1e3
+        sec = max_over_ranks(e0.elapsed_time(e1) / 1e3)  # the slowest replica's time
         if headline:
             launches = ctx.launch_count() - l0
             clk.terminate()
@@ -662,10 +682,6 @@ def run_full(args, rank: int, world: int) -> None:
         results[name] = dict(views_per_s=len(targets) * args.steps / sec,
                              cg_iterations=int(sum(s.outer_iterations for s in st)),
                              max_gap=float(max(s.gap for s in st)))
-    if world > 1:
-        t = torch.tensor([len(targets) * args.steps / results["learned_batched"]["views_per_s"]], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        results["learned_batched"]["views_per_s"] = len(targets) * args.steps / float(t.item())
     # every arm against the plain FP32 solver's outputs (same targets)
     ref = [o.cpu().numpy() for o in outs["plain_single"]]
     for name in ("plain_batched", "bf16_batched", "learned_batched"):
@@ -693,10 +709,12 @@ def run_full(args, rank: int, world: int) -> None:
     for _ in range(max(1, args.warmup // 2)):
         ctx.render_views(hjobs, net)
     torch.cuda.synchronize()
+    barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         ctx.render_views(hjobs, net)
-    e2e_sec = time.perf_counter() - t0  # the call returns after its outputs are in host memory
+    # the call returns after its outputs are in host memory; the slowest replica's time
+    e2e_sec = max_over_ranks(time.perf_counter() - t0)
     e2e = {"value": world * len(targets) * args.steps / e2e_sec, "unit": "views/s",
            "h2d_bytes_per_step": int(hv.numel() * 2 + hd.numel() * 4),
            "d2h_bytes_per_step": int(len(targets) * 3 * H * W * 4)}
@@ -817,8 +835,7 @@ def run_ours(args, rank: int, world: int) -> None:
     torch.cuda.synchronize()
     # the working set (24 views x 6 planes x 1 MB + the 1024^2 target state) exceeds nothing in L2 between
     # steps: each step rewrites > 300 MB of buffers, so consecutive steps start from a cold L2
-    if world > 1:
-        torch.distributed.barrier()
+    barrier()
     clk_path = tempfile.mktemp(prefix="lfrv_clocks_")
     clk = sample_clocks(clk_path)
     l0 = ctx.launch_count()
@@ -833,11 +850,7 @@ def run_ours(args, rank: int, world: int) -> None:
     clk.terminate()
     clk.wait()
     clocks = summarize_clocks(clk_path)
-    sec = ms / 1e3
-    if world > 1:
-        t = torch.tensor([sec], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        sec = float(t.item())
+    sec = max_over_ranks(ms / 1e3)  # the slowest replica's time
     value = world * args.steps / sec
 
     # per-kernel device time over a second pass of the same steps (events on the launch stream)
@@ -855,6 +868,7 @@ def run_ours(args, rank: int, world: int) -> None:
     for _ in range(2):
         ctx.render_view(cfg, wl["algorithm"], hv.data_ptr(), hd.data_ptr(), sc.cams, sc.target, ho.data_ptr())
     torch.cuda.synchronize()
+    barrier()
     t0 = time.perf_counter()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     f0.record(stream)
@@ -864,7 +878,7 @@ def run_ours(args, rank: int, world: int) -> None:
     torch.cuda.synchronize()
     e2e_sec = max(f0.elapsed_time(f1) / 1e3, 1e-9)
     wall = time.perf_counter() - t0
-    e2e_value = world * args.steps / max(e2e_sec, wall)
+    e2e_value = world * args.steps / max_over_ranks(max(e2e_sec, wall))  # the slowest replica's time
 
     cpu, vs64 = None, None
     if rank == 0 and world == 1 and not args.no_cpu:
